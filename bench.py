@@ -1,0 +1,435 @@
+"""Benchmark: SX tape sweeps over many instances on one GB300.
+
+Workload (default): the cart-pole 20-step RK4 rollout F(x0[4], U[20]) -> (xN[4], cost),
+N = 262144 instances, FP64. One step = the forward-mode Jacobian of all outputs w.r.t. the
+24 inputs (values + 24 unit directions) plus the adjoint of the cost (values + 1 adjoint
+direction), over all N instances. `value` is instances per second for that step with inputs
+resident in HBM; `e2e` is the same step through the C ABI's host-buffer Map entry points
+(casadi_gb300_map_jacobian + casadi_gb300_map_reverse) with pinned host buffers, host<->device
+copies inside the timed region.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl native|reference]
+                       [--workload rollout20|cartpole|dag]
+For N > 1 (torchrun) every rank runs an independent replica on its own instances (the path
+has no exchange step); rank 0 prints the max-over-ranks time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SX tape evals/s & adjoint evals/s per GB300 vs plain kernel; % FP64/HBM roof"
+UNIT = "evals/s"
+L2_FLUSH_BYTES = 256 << 20
+
+
+# ---- workloads -------------------------------------------------------------------------------
+def make_workload(name):
+    from casadi_gb300 import workloads as W
+    if name == "rollout20":
+        F = W.cartpole_rollout(20)
+        n = 262144
+        args = W.cartpole_inputs(n, steps=20, seed=0)
+        desc = "cart-pole 20-step RK4 rollout F(x0[4],U[20])->(xN[4],cost), N=262144: " \
+               "forward Jacobian (24 unit directions) + adjoint of cost"
+        return F, n, args, [np.zeros((1, 4, n)), np.ones((1, 1, n))], desc
+    if name == "cartpole":
+        F = W.cartpole_step()
+        n = 65536
+        args = W.cartpole_inputs(n, steps=1, seed=0)
+        return F, n, args, [np.ones((1, 4, n))], "cart-pole RK4 step, N=65536"
+    if name == "dag":
+        F = W.random_dag()
+        n = 16384
+        args = W.dag_inputs(n)
+        return F, n, args, [np.ones((1, 16, n))], "random DAG 64in/10000 nodes/16out, N=16384"
+    raise SystemExit("unknown workload " + name)
+
+
+# ---- algorithmic work per instance (FP64 arithmetic the numeric formulas require) -----------
+def algorithmic_flops(tape, weights):
+    """FP64 operations per instance for each kernel family, from the tape's op histogram.
+
+    Value of an op: 1 for +,-,*, comparisons and selects; the measured FP64-pipe weight of
+    DIV, SQRT and each libm call (op_weights.json). Tangent per direction: 3 for a binary op
+    with recorded partials (d0*a + d1*b), 1 for ADD/SUB/TWICE and unary ops. Adjoint per
+    direction: 4 for a binary op (two products, two sums), 2 for ADD/SUB and unary ops."""
+    from casadi_gb300 import calculus as C
+    val = rec = tan = adj = 0.0
+    free = {C.OP_CONST, C.OP_INPUT, C.OP_OUTPUT}
+    for op, cnt in zip(*np.unique(tape.op, return_counts=True)):
+        op = int(op)
+        if op in free:
+            continue
+        name = C.OP_NAMES[op]
+        w = float(weights.get(name, 1.0))
+        val += cnt * w
+        rec += cnt * (w + float(weights.get(name + "_partial", 0.0)))
+        if op in (C.OP_ADD, C.OP_SUB):
+            tan += cnt * 1
+            adj += cnt * 2
+        elif op in (C.OP_NEG, C.OP_ASSIGN):
+            adj += cnt * 1
+        elif op in C.BINARY_OPS:
+            tan += cnt * 3
+            adj += cnt * 4
+        else:
+            tan += cnt * 1
+            adj += cnt * 2
+    return dict(eval=val, record=rec, tangent_per_dir=tan, adjoint_per_dir=adj)
+
+
+def load_weights():
+    p = os.path.join(ROOT, "casadi_gb300", "op_weights.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)["weights"]
+    return {}
+
+
+# ---- clocks ------------------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.QUERY,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---- FP64 peak, measured live ------------------------------------------------------------------
+def fp64_peak_tflops(torch):
+    """cuBLAS FP64 GEMM throughput (4096^3, best of 5) — the measured FP64 ceiling, in the
+    spirit of the driver's cuBLAS bf16 figure."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = max(best, 2 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    del a, b
+    return best
+
+
+# ---- CPU baseline (oracle port, all host threads, bounded sample) -------------------------------
+def cpu_step(tape, args, aseeds, n, threads, workload):
+    import oracle as O
+    nz = sum(tape.nnz_in)
+    if workload == "rollout20":
+        eye = np.eye(nz)
+        offs = np.cumsum([0] + tape.nnz_in)
+        fseeds = [np.ascontiguousarray(np.broadcast_to(eye[:, offs[j]:offs[j + 1], None],
+                                                       (nz, tape.nnz_in[j], n)))
+                  for j in range(len(tape.nnz_in))]
+        t0 = time.perf_counter()
+        O.forward(tape, args, fseeds, n, threads)
+        O.reverse(tape, args, aseeds, n, threads)
+        return time.perf_counter() - t0
+    t0 = time.perf_counter()
+    if workload == "dag":
+        O.reverse(tape, args, aseeds, n, threads)
+    else:
+        O.eval(tape, args, n, threads)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(F, args, aseeds, workload, budget_s=12.0):
+    threads = os.cpu_count() or 1
+    tape = F.tape
+    m = 256
+    sub = lambda arrs, k: [np.ascontiguousarray(a[..., :k]) for a in arrs]  # noqa: E731
+    t = cpu_step(tape, sub(args, m), sub(aseeds, m), m, threads, workload)
+    m2 = int(min(args[0].shape[-1], max(m, m * budget_s / max(t, 1e-6) / 2)))
+    t2 = cpu_step(tape, sub(args, m2), sub(aseeds, m2), m2, threads, workload)
+    return {"value": m2 / t2, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d of the instances, same step (oracle C restatement, OpenMP, %d threads)"
+                      % (m2, threads)}
+
+
+# ---- native arm ----------------------------------------------------------------------------------
+def run_native(a):
+    import torch
+    from casadi_gb300 import runtime as R
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    F, n, args_h, aseeds_h, desc = make_workload(a.workload)
+    ct = R.CudaTape(F)
+    dargs = [torch.from_numpy(x).cuda() for x in args_h]
+    daseeds = [torch.from_numpy(x).cuda() for x in aseeds_h]
+    nz = sum(F.tape.nnz_in)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    res = [torch.empty((k, n), dtype=torch.float64, device="cuda") for k in F.tape.nnz_out]
+    jac = [torch.empty((nz, k, n), dtype=torch.float64, device="cuda") for k in F.tape.nnz_out] \
+        if a.workload == "rollout20" else None
+    asens = [torch.empty((1, k, n), dtype=torch.float64, device="cuda") for k in F.tape.nnz_in]
+    ct.scratch(n)
+
+    def step():
+        if a.workload == "rollout20":
+            ct.jacobian(dargs, res=res, jac=jac, stream=stream)
+            ct.reverse(dargs, daseeds, res=res, asens=asens, stream=stream)
+        elif a.workload == "dag":
+            ct.reverse(dargs, daseeds, res=res, asens=asens, stream=stream)
+        else:
+            ct.eval(dargs, res=res, stream=stream)
+
+    for _ in range(a.warmup):
+        step()
+    ct.sync()
+    R.profile(True)
+    R.profile_collect()
+    times = []
+    with ClockSampler(local) as clk:
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        for _ in range(a.steps):
+            flush.fill_(1.0)  # evict L2 between timed steps (outside the events)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            times.append((e0, e1))
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+    ms = [e0.elapsed_time(e1) for e0, e1 in times]
+    prof = R.profile_collect()
+    R.profile(False)
+    ct.sync()
+    ms_step = sum(ms) / len(ms)
+    if dist:
+        t = torch.tensor([ms_step], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = world * n / (ms_step * 1e-3)
+
+    # component rates (outside the timed region): eval-only and adjoint-only
+    comps = {}
+
+    def rate(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        return n / (e0.elapsed_time(e1) / reps * 1e-3)
+
+    comps["eval_evals_per_s"] = rate(lambda: ct.eval(dargs, res=res, stream=stream))
+    comps["adjoint_evals_per_s"] = rate(
+        lambda: ct.reverse(dargs, daseeds, res=res, asens=asens, stream=stream))
+    if a.workload == "rollout20":
+        comps["jacobian24_evals_per_s"] = rate(
+            lambda: ct.jacobian(dargs, res=res, jac=jac, stream=stream))
+    ct.sync()
+
+    # roofline of the dominant kernel family (device time from the per-launch events)
+    weights = load_weights()
+    work = algorithmic_flops(F.tape, weights)
+    fam_ms = {k: v for k, v in prof.items() if v[1] > 0}
+    dom = max(fam_ms, key=lambda k: fam_ms[k][0])
+    dom_ms, dom_launches = fam_ms[dom]
+    per_inst = {"eval": work["eval"], "record": work["record"],
+                "tangent": work["tangent_per_dir"] * (nz if a.workload == "rollout20" else 1),
+                "adjoint": work["adjoint_per_dir"]}.get(dom, 0.0)
+    launches_per_step = dom_launches / a.steps
+    flops_per_launch = per_inst * n / launches_per_step
+    achieved = flops_per_launch / (dom_ms / dom_launches * 1e-3) / 1e12
+    peak = fp64_peak_tflops(torch)
+    gpu_launches = sum(v[1] for v in prof.values())
+    io_bytes = 8 * n * (sum(F.tape.nnz_in) + sum(F.tape.nnz_out))
+
+    # end-to-end through the host-buffer Map entry points (pinned host memory)
+    e2e = None
+    if rank == 0 or world > 1:
+        cm = R.CudaMap(ct, n)
+
+        def pinned(shape):
+            return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+
+        hargs = [pinned((n, x.shape[0])) for x in args_h]
+        for h, x in zip(hargs, args_h):
+            h[:] = x.T
+        hres = [pinned((n, k)) for k in F.tape.nnz_out]
+        hseed = [pinned((n, 1, k)) for k in F.tape.nnz_out]
+        for h, x in zip(hseed, aseeds_h):
+            h[:] = np.transpose(x, (2, 0, 1))
+        hasens = [pinned((n, 1, k)) for k in F.tape.nnz_in]
+        hjac = [pinned((n, nz, k)) for k in F.tape.nnz_out] if a.workload == "rollout20" else None
+
+        def e2e_step():
+            if a.workload == "rollout20":
+                cm.jacobian(*hargs, res=hres, jac=hjac)
+                cm.reverse(hargs, hseed, res=hres, asens=hasens)
+            elif a.workload == "dag":
+                cm.reverse(hargs, hseed, res=hres, asens=hasens)
+            else:
+                cm(*hargs, res=hres)
+
+        for _ in range(max(1, a.warmup)):
+            e2e_step()
+        t0 = time.perf_counter()
+        for _ in range(a.steps):
+            e2e_step()
+        t_e2e = (time.perf_counter() - t0) / a.steps
+        in_b = 8 * n * sum(F.tape.nnz_in)
+        out_b = 8 * n * sum(F.tape.nnz_out)
+        if a.workload == "rollout20":
+            h2d = 2 * in_b + 8 * n * sum(F.tape.nnz_out)
+            d2h = 2 * out_b + 8 * n * nz * sum(F.tape.nnz_out) + in_b
+        elif a.workload == "dag":
+            h2d = in_b + 8 * n * sum(F.tape.nnz_out)
+            d2h = out_b + in_b
+        else:
+            h2d, d2h = in_b, out_b
+        e2e = {"value": world * n / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "ms_per_step": t_e2e * 1e3}
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": desc, "instances_per_gpu": n, "tape_instructions": F.tape.n_instr,
+                   "sz_w": F.tape.sz_w, "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "flushed between timed steps (256 MiB write)"},
+        "components": comps,
+        "e2e": e2e,
+        "gpu_launches": gpu_launches,
+        "kernel_ms": {k: round(v[0], 4) for k, v in prof.items() if v[1]},
+        "roofline": {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": peak,
+                     "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
+                     "traffic": None, "peak_source": "cuBLAS FP64 GEMM measured in this run",
+                     "io_bytes_per_step": io_bytes,
+                     "hbm_gbs_io": io_bytes / (ms_step * 1e-3) / 1e9},
+        "clocks": clk.summary(),
+    }
+    if not a.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(F, args_h, aseeds_h, a.workload)
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+# ---- reference arm (the oracle port of CasADi's VM on the host cores) ----------------------------
+def run_reference(a):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    F, n, args_h, aseeds_h, desc = make_workload(a.workload)
+    threads = os.cpu_count() or 1
+    # bounded sample per step so that warmup + steps finish within a few minutes
+    m = 256
+    sub = lambda arrs, k: [np.ascontiguousarray(x[..., :k]) for x in arrs]  # noqa: E731
+    t = cpu_step(F.tape, sub(args_h, m), sub(aseeds_h, m), m, threads, a.workload)
+    per_step = 150.0 / max(1, a.steps + a.warmup)
+    m = int(min(n, max(m, m * per_step / max(t, 1e-6) / 2)))
+    sa, ss = sub(args_h, m), sub(aseeds_h, m)
+    for _ in range(a.warmup):
+        cpu_step(F.tape, sa, ss, m, threads, a.workload)
+    ts = [cpu_step(F.tape, sa, ss, m, threads, a.workload) for _ in range(a.steps)]
+    sec = sum(ts) / len(ts)
+    v = m / sec
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 1,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": sec * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": desc, "instances_per_step": m},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "%d instances per step of the same workload" % m},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="native", choices=["native", "reference"])
+    p.add_argument("--workload", default="rollout20", choices=["rollout20", "cartpole", "dag"])
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    a = p.parse_args()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_native(a)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,818 @@
+// C ABI of the GB300 SX-tape evaluator (declared in include/casadi_gb300.h).
+//
+// Host side: tape registry (int ids, as casadi/core/casadi_c.cpp:73-110 keeps Functions),
+// host validation of every tape index before anything reaches the GPU, instruction encoding,
+// launch-shape selection from the shared-memory footprint, and the wave loop that bounds
+// the AD scratch. No exception crosses the ABI: every entry point returns a status and
+// records a message for casadi_gb300_last_error().
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/casadi_gb300.h"
+#include "sweeps.cuh"
+
+using namespace cgb;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(CASADI_GB300_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+// CasADi operation ids (casadi/core/calculus.hpp:60-218) of the scalar ops numbered above
+// OP_CALL, and their device opcodes.
+constexpr int kOpConst = 44, kOpInput = 45, kOpOutput = 46, kOpParameter = 47, kOpCall = 48;
+
+int device_opcode(int op) {
+  if (op >= 0 && op <= 43) return op;  // ASSIGN .. ATAN2 keep their ids
+  switch (op) {
+    case kOpConst: return D_CONST;
+    case kOpInput: return D_INPUT;
+    case kOpOutput: return D_OUTPUT;
+    case 86: return D_ERFINV;
+    case 87: return D_PRINTME;
+    case 88: return D_LIFT;
+    case 93: return D_LOG1P;
+    case 94: return D_EXPM1;
+    case 95: return D_HYPOT;
+    case 97: return D_REMAINDER;
+    default: return -1;
+  }
+}
+
+struct Tape {
+  int device = 0;
+  int n_instr = 0, n_in = 0, n_out = 0, sz_w = 0, n_partials = 0, n_chunks = 0;
+  std::vector<int> nnz_in, nnz_out;
+  std::vector<int2> absent_in;
+  u64* d_code = nullptr;
+  double* d_consts = nullptr;
+  int2* d_absent = nullptr;
+  int* d_err = nullptr;
+  // launch shapes
+  int primal_block = 128, primal_grid_cap = 1;
+  int dir_warps = 4, dir_grid_cap = 1;
+
+  ~Tape() {
+    int cur = 0;
+    cudaGetDevice(&cur);
+    if (cur != device) cudaSetDevice(device);
+    cudaFree(d_code);
+    cudaFree(d_consts);
+    cudaFree(d_absent);
+    cudaFree(d_err);
+    if (cur != device) cudaSetDevice(cur);
+  }
+
+  TapeView view() const {
+    TapeView v;
+    v.code = d_code;
+    v.consts = d_consts;
+    v.absent_in = d_absent;
+    v.n_chunks = n_chunks;
+    v.n_absent_in = static_cast<int>(absent_in.size());
+    v.sz_w = sz_w;
+    v.n_partials = n_partials;
+    v.err = d_err;
+    return v;
+  }
+};
+
+struct Mem {
+  cudaStream_t stream = nullptr;
+  std::vector<void*> bufs;   // device staging buffers, grown on demand
+  std::vector<size_t> caps;
+  ~Mem() {
+    for (void* p : bufs) cudaFree(p);
+    if (stream) cudaStreamDestroy(stream);
+  }
+  // device buffer k of at least `bytes`
+  void* buf(size_t k, size_t bytes, cudaError_t* e) {
+    if (bufs.size() <= k) {
+      bufs.resize(k + 1, nullptr);
+      caps.resize(k + 1, 0);
+    }
+    if (caps[k] < bytes) {
+      cudaFree(bufs[k]);
+      bufs[k] = nullptr;
+      caps[k] = 0;
+      *e = cudaMalloc(&bufs[k], bytes);
+      if (*e != cudaSuccess) return nullptr;
+      caps[k] = bytes;
+    }
+    return bufs[k];
+  }
+};
+
+std::mutex g_mtx;
+std::vector<std::unique_ptr<Tape>> g_tapes;
+std::vector<std::unique_ptr<Mem>> g_mems;
+
+// ---- optional per-launch timing (CUDA events on the launch stream) -------------------------
+enum Family { F_EVAL = 0, F_RECORD, F_TANGENT, F_ADJOINT, F_SP_FORWARD, F_SP_REVERSE, F_COUNT };
+struct ProfEntry {
+  int family;
+  cudaEvent_t start, stop;
+};
+bool g_prof = false;
+std::vector<ProfEntry> g_prof_live;
+std::vector<cudaEvent_t> g_prof_pool;
+std::mutex g_prof_mtx;
+
+cudaEvent_t prof_event() {
+  if (!g_prof_pool.empty()) {
+    cudaEvent_t e = g_prof_pool.back();
+    g_prof_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// Launch `fn` (returning cudaError_t) on stream s, bracketed by events when profiling is on.
+template <class Fn>
+cudaError_t timed(int family, cudaStream_t s, Fn&& fn) {
+  if (!g_prof) return fn();
+  std::lock_guard<std::mutex> lk(g_prof_mtx);
+  ProfEntry p{family, prof_event(), prof_event()};
+  cudaEventRecord(p.start, s);
+  cudaError_t e = fn();
+  cudaEventRecord(p.stop, s);
+  g_prof_live.push_back(p);
+  return e;
+}
+
+Tape* get_tape(int id) {
+  std::lock_guard<std::mutex> lk(g_mtx);
+  if (id < 0 || id >= static_cast<int>(g_tapes.size()) || !g_tapes[id]) return nullptr;
+  return g_tapes[id].get();
+}
+
+int sm_count() {
+  int dev = 0, n = 0;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+    n = 1;
+  return n;
+}
+
+// Pick the CTA shapes that keep the most threads resident given the shared-memory footprint.
+void choose_shapes(Tape& t) {
+  const int max_smem = max_smem_optin();
+  const int sms = sm_count();
+  int best_threads = -1;
+  for (int bs : {256, 128, 64, 32}) {
+    const size_t sm = smem_primal(t.sz_w, bs);
+    if (sm > static_cast<size_t>(max_smem)) continue;
+    const int occ = occupancy_primal(bs, sm);
+    if (occ * bs > best_threads) {
+      best_threads = occ * bs;
+      t.primal_block = bs;
+      t.primal_grid_cap = occ * sms;
+    }
+  }
+  best_threads = -1;
+  for (int dw : {4, 2, 1}) {
+    const size_t sm = smem_dir(t.sz_w, dw);
+    if (sm > static_cast<size_t>(max_smem)) continue;
+    const int occ = occupancy_dir(sm);
+    // occupancy_dir measures the 4-warp variant; scale for narrower CTAs by shared memory
+    const int occ_dw = dw == 4 ? occ : std::max(occ, static_cast<int>(
+        std::min<size_t>(32, (228u * 1024u) / (sm + 1024u))));
+    if (occ_dw * dw * 32 > best_threads) {
+      best_threads = occ_dw * dw * 32;
+      t.dir_warps = dw;
+      t.dir_grid_cap = occ_dw * sms;
+    }
+  }
+}
+
+bool fits_smem(int sz_w) {
+  return smem_primal(sz_w, 32) <= static_cast<size_t>(max_smem_optin());
+}
+
+int check_device(const Tape& t) {
+  int cur = -1;
+  cudaError_t e = cudaGetDevice(&cur);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (cur != t.device)
+    return fail(CASADI_GB300_ERR_ARG, "tape lives on device %d, current device is %d", t.device,
+                cur);
+  return 0;
+}
+
+void fill_io(IoDesc* dst, int count, void* const* ptrs, const std::vector<int>& nnz,
+             long long ld, bool dir_major) {
+  for (int j = 0; j < count; ++j) {
+    dst[j].ptr = ptrs ? ptrs[j] : nullptr;
+    dst[j].nz_stride = ld;
+    dst[j].inst_stride = 1;
+    dst[j].dir_stride = dir_major ? static_cast<long long>(nnz[j]) * ld : 0;
+  }
+}
+
+SweepArgs base_args(const Tape& t, long long n, long long i_begin) {
+  SweepArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.t = t.view();
+  a.n = n;
+  a.i_begin = i_begin;
+  a.n_in = t.n_in;
+  a.n_out = t.n_out;
+  return a;
+}
+
+int grid_for(long long tiles, int cap) {
+  long long g = std::min<long long>(tiles, cap);
+  return static_cast<int>(std::max<long long>(g, 1));
+}
+
+// Instances per AD wave that fit in `bytes` of scratch (multiple of 32).
+long long wave_capacity(const Tape& t, long long n, size_t bytes) {
+  if (t.n_partials == 0) return n;
+  long long per = 8ll * t.n_partials;
+  long long w = static_cast<long long>(bytes / per);
+  w = (w / 32) * 32;
+  return std::min<long long>(w, ((n + 31) / 32) * 32);
+}
+
+int run_record_waves(Tape& t, long long n, long long ld, int ndir, bool adjoint,
+                     void* const* arg, void* const* res, void* const* seed, void* const* sens,
+                     void* scratch, size_t scratch_bytes, cudaStream_t s,
+                     bool identity = false) {
+  if (n == 0) return 0;
+  const long long cap = wave_capacity(t, n, scratch_bytes);
+  if (t.n_partials > 0 && (scratch == nullptr || cap < 32))
+    return fail(CASADI_GB300_ERR_SCRATCH,
+                "scratch of %zu bytes is below the minimum of %lld bytes for this tape",
+                scratch_bytes, 32ll * 8ll * t.n_partials);
+  for (long long i0 = 0; i0 < n; i0 += cap) {
+    const long long m = std::min(cap, n - i0);
+    SweepArgs a = base_args(t, m, i0);
+    a.partials = static_cast<double*>(scratch);
+    a.pt_stride = cap;
+    a.ndir = ndir;
+    a.identity_seed = identity ? 1 : 0;
+    for (int j = 0, off = 0; j < t.n_in; off += t.nnz_in[j], ++j) a.in_off[j] = off;
+    fill_io(a.in, t.n_in, arg, t.nnz_in, ld, false);
+    fill_io(a.out, t.n_out, res, t.nnz_out, ld, false);
+    a.block = t.primal_block;
+    cudaError_t e = timed(F_RECORD, s, [&] {
+      return launch_record(a, grid_for((m + a.block - 1) / a.block, t.primal_grid_cap), s);
+    });
+    if (e != cudaSuccess) return cuda_fail(e, "record sweep launch");
+    if (ndir > 0) {
+      if (adjoint) {
+        fill_io(a.seed, t.n_out, seed, t.nnz_out, ld, true);
+        fill_io(a.sens, t.n_in, sens, t.nnz_in, ld, true);
+      } else {
+        fill_io(a.seed, t.n_in, seed, t.nnz_in, ld, true);
+        fill_io(a.sens, t.n_out, sens, t.nnz_out, ld, true);
+      }
+      a.block = 32 * t.dir_warps;
+      const int gy = (ndir + t.dir_warps - 1) / t.dir_warps;
+      const int gx = grid_for((m + 31) / 32, std::max(1, t.dir_grid_cap / gy));
+      e = timed(adjoint ? F_ADJOINT : F_TANGENT, s, [&] {
+        return adjoint ? launch_adjoint(a, gx, gy, s) : launch_tangent(a, gx, gy, s);
+      });
+      if (e != cudaSuccess) return cuda_fail(e, "derivative sweep launch");
+    }
+  }
+  return 0;
+}
+
+// Pointer arrays of any element type, seen as untyped pointers (the kernels know the type).
+template <class T>
+void* const* vptrs(T* const* p) {
+  return (void* const*)(p);
+}
+
+int check_n(long long n, long long ld) {
+  if (n < 0) return fail(CASADI_GB300_ERR_ARG, "negative instance count");
+  if (ld < n) return fail(CASADI_GB300_ERR_ARG, "leading dimension %lld < n %lld", ld, n);
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* casadi_gb300_last_error(void) { return g_err.c_str(); }
+
+const char* casadi_gb300_version(void) { return "0.1.0"; }
+
+int casadi_gb300_tape_create(const casadi_gb300_atomic* alg, int n_instr, int n_in,
+                             const int* nnz_in, int n_out, const int* nnz_out, int sz_w) {
+  if (n_instr < 0 || (n_instr > 0 && !alg)) return fail(CASADI_GB300_ERR_ARG, "no instructions");
+  if (n_in < 0 || n_out < 0 || sz_w < 0) return fail(CASADI_GB300_ERR_ARG, "negative size");
+  if ((n_in > 0 && !nnz_in) || (n_out > 0 && !nnz_out))
+    return fail(CASADI_GB300_ERR_ARG, "missing nnz arrays");
+  if (n_in > kMaxIo || n_out > kMaxIo)
+    return fail(CASADI_GB300_ERR_UNSUPPORTED, "more than %d inputs or outputs", kMaxIo);
+  if (static_cast<unsigned>(sz_w) > kFieldMax)
+    return fail(CASADI_GB300_ERR_UNSUPPORTED, "work vector of %d slots exceeds %u", sz_w,
+                kFieldMax);
+  if (!fits_smem(sz_w))
+    return fail(CASADI_GB300_ERR_UNSUPPORTED,
+                "work vector of %d slots does not fit shared memory (global work vectors are "
+                "not available in this build)", sz_w);
+  auto t = std::make_unique<Tape>();
+  t->n_instr = n_instr;
+  t->n_in = n_in;
+  t->n_out = n_out;
+  t->sz_w = sz_w;
+  t->nnz_in.assign(nnz_in, nnz_in + n_in);
+  t->nnz_out.assign(nnz_out, nnz_out + n_out);
+  for (int v : t->nnz_in)
+    if (v < 0 || static_cast<unsigned>(v) > kFieldMax) return fail(CASADI_GB300_ERR_ARG, "bad nnz_in");
+  for (int v : t->nnz_out)
+    if (v < 0 || static_cast<unsigned>(v) > kFieldMax) return fail(CASADI_GB300_ERR_ARG, "bad nnz_out");
+
+  // validate and encode (every index is checked here; kernels trust the stream)
+  std::vector<u64> code;
+  std::vector<double> consts;
+  std::vector<std::vector<char>> seen_in(n_in);
+  std::vector<std::vector<char>> seen_out(n_out);
+  for (int j = 0; j < n_in; ++j) seen_in[j].assign(t->nnz_in[j], 0);
+  for (int j = 0; j < n_out; ++j) seen_out[j].assign(t->nnz_out[j], 0);
+  code.reserve(n_instr);
+  long long n_partials = 0;
+  auto slot_ok = [&](int s) { return s >= 0 && s < sz_w; };
+  for (int k = 0; k < n_instr; ++k) {
+    const casadi_gb300_atomic& e = alg[k];
+    const int op = e.op;
+    if (op == kOpParameter)
+      return fail(CASADI_GB300_ERR_UNSUPPORTED, "instruction %d: free parameter (OP_PARAMETER)", k);
+    if (op == kOpCall)
+      return fail(CASADI_GB300_ERR_UNSUPPORTED, "instruction %d: OP_CALL is not supported", k);
+    const int dop = device_opcode(op);
+    if (dop < 0) return fail(CASADI_GB300_ERR_UNSUPPORTED, "instruction %d: unknown op %d", k, op);
+    if (dop == D_CONST) {
+      if (!slot_ok(e.i0)) return fail(CASADI_GB300_ERR_ARG, "instruction %d: slot out of range", k);
+      if (consts.size() >= kFieldMax) return fail(CASADI_GB300_ERR_UNSUPPORTED, "too many constants");
+      code.push_back(enc(D_CONST, e.i0, static_cast<unsigned>(consts.size()), 0));
+      consts.push_back(e.a.d);
+    } else if (dop == D_INPUT) {
+      const int j = e.a.i[0], nz = e.a.i[1];
+      if (!slot_ok(e.i0) || j < 0 || j >= n_in || nz < 0 || nz >= t->nnz_in[j])
+        return fail(CASADI_GB300_ERR_ARG, "instruction %d: input reference out of range", k);
+      seen_in[j][nz] = 1;
+      code.push_back(enc(D_INPUT, e.i0, j, nz));
+    } else if (dop == D_OUTPUT) {
+      const int j = e.i0, s = e.a.i[0], nz = e.a.i[1];
+      if (j < 0 || j >= n_out || !slot_ok(s) || nz < 0 || nz >= t->nnz_out[j])
+        return fail(CASADI_GB300_ERR_ARG, "instruction %d: output reference out of range", k);
+      if (seen_out[j][nz])
+        return fail(CASADI_GB300_ERR_ARG, "instruction %d: output nonzero written twice", k);
+      seen_out[j][nz] = 1;
+      code.push_back(enc(D_OUTPUT, j, s, nz));
+    } else {
+      const int b = e.a.i[0], c = e.a.i[1];
+      if (!slot_ok(e.i0) || !slot_ok(b) || !slot_ok(c))
+        return fail(CASADI_GB300_ERR_ARG, "instruction %d: slot out of range", k);
+      code.push_back(enc(dop, e.i0, b, c));
+      n_partials += __builtin_popcount(partial_mask(dop));
+    }
+  }
+  for (int j = 0; j < n_out; ++j)
+    for (int nz = 0; nz < t->nnz_out[j]; ++nz)
+      if (!seen_out[j][nz])
+        return fail(CASADI_GB300_ERR_ARG, "output %d nonzero %d is never written", j, nz);
+  for (int j = 0; j < n_in; ++j)
+    for (int nz = 0; nz < t->nnz_in[j]; ++nz)
+      if (!seen_in[j][nz]) t->absent_in.push_back(make_int2(j, nz));
+  if (n_partials > (1ll << 31))
+    return fail(CASADI_GB300_ERR_UNSUPPORTED, "tape records too many partials");
+  t->n_partials = static_cast<int>(n_partials);
+  t->n_chunks = std::max(1, (n_instr + kChunk - 1) / kChunk);
+  code.resize(static_cast<size_t>(t->n_chunks) * kChunk, enc(D_NOP, 0, 0, 0));
+  if (consts.empty()) consts.push_back(0.0);
+
+  cudaError_t e = cudaGetDevice(&t->device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if ((e = cudaMalloc(&t->d_code, code.size() * sizeof(u64))) != cudaSuccess)
+    return cuda_fail(e, "cudaMalloc(code)");
+  if ((e = cudaMalloc(&t->d_consts, consts.size() * sizeof(double))) != cudaSuccess)
+    return cuda_fail(e, "cudaMalloc(consts)");
+  if ((e = cudaMalloc(&t->d_absent, std::max<size_t>(1, t->absent_in.size()) * sizeof(int2))) !=
+      cudaSuccess)
+    return cuda_fail(e, "cudaMalloc(absent)");
+  if ((e = cudaMalloc(&t->d_err, sizeof(int))) != cudaSuccess) return cuda_fail(e, "cudaMalloc(err)");
+  if ((e = cudaMemcpy(t->d_code, code.data(), code.size() * sizeof(u64), cudaMemcpyHostToDevice)) !=
+      cudaSuccess)
+    return cuda_fail(e, "upload code");
+  if ((e = cudaMemcpy(t->d_consts, consts.data(), consts.size() * sizeof(double),
+                      cudaMemcpyHostToDevice)) != cudaSuccess)
+    return cuda_fail(e, "upload constants");
+  if (!t->absent_in.empty() &&
+      (e = cudaMemcpy(t->d_absent, t->absent_in.data(), t->absent_in.size() * sizeof(int2),
+                      cudaMemcpyHostToDevice)) != cudaSuccess)
+    return cuda_fail(e, "upload absent inputs");
+  if ((e = cudaMemset(t->d_err, 0, sizeof(int))) != cudaSuccess) return cuda_fail(e, "clear err");
+  choose_shapes(*t);
+
+  std::lock_guard<std::mutex> lk(g_mtx);
+  g_tapes.push_back(std::move(t));
+  return static_cast<int>(g_tapes.size()) - 1;
+}
+
+int casadi_gb300_tape_free(int id) {
+  std::lock_guard<std::mutex> lk(g_mtx);
+  if (id < 0 || id >= static_cast<int>(g_tapes.size()) || !g_tapes[id])
+    return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  g_tapes[id].reset();
+  return 0;
+}
+
+int casadi_gb300_tape_info(int id, int* n_instr, int* n_in, int* n_out, int* sz_w,
+                           int* n_partials) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  if (n_instr) *n_instr = t->n_instr;
+  if (n_in) *n_in = t->n_in;
+  if (n_out) *n_out = t->n_out;
+  if (sz_w) *sz_w = t->sz_w;
+  if (n_partials) *n_partials = t->n_partials;
+  return 0;
+}
+
+int casadi_gb300_scratch_size(int id, int64_t n, size_t* bytes) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  if (!bytes || n < 0) return fail(CASADI_GB300_ERR_ARG, "bad arguments");
+  *bytes = static_cast<size_t>(8) * t->n_partials * static_cast<size_t>(((n + 31) / 32) * 32);
+  return 0;
+}
+
+int casadi_gb300_scratch_min(int id, size_t* bytes) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  if (!bytes) return fail(CASADI_GB300_ERR_ARG, "bad arguments");
+  *bytes = static_cast<size_t>(8) * 32 * t->n_partials;
+  return 0;
+}
+
+int casadi_gb300_eval(int id, int64_t n, int64_t ld, const double* const* arg,
+                      double* const* res, void* stream) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  if (int rc = check_device(*t)) return rc;
+  if (int rc = check_n(n, ld)) return rc;
+  if (n == 0) return 0;
+  SweepArgs a = base_args(*t, n, 0);
+  fill_io(a.in, t->n_in, vptrs(arg), t->nnz_in, ld, false);
+  fill_io(a.out, t->n_out, vptrs(res), t->nnz_out, ld, false);
+  a.block = t->primal_block;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = timed(F_EVAL, s, [&] {
+    return launch_eval(a, grid_for((n + a.block - 1) / a.block, t->primal_grid_cap), s);
+  });
+  if (e != cudaSuccess) return cuda_fail(e, "eval launch");
+  return 0;
+}
+
+int casadi_gb300_forward(int id, int64_t n, int64_t ld, int nfwd, const double* const* arg,
+                         double* const* res, const double* const* fseed, double* const* fsens,
+                         void* scratch, size_t scratch_bytes, void* stream) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  if (int rc = check_device(*t)) return rc;
+  if (int rc = check_n(n, ld)) return rc;
+  if (nfwd < 0 || nfwd > 65535) return fail(CASADI_GB300_ERR_ARG, "bad direction count %d", nfwd);
+  return run_record_waves(*t, n, ld, nfwd, false, vptrs(arg),
+                          vptrs(res),
+                          vptrs(fseed),
+                          vptrs(fsens), scratch, scratch_bytes,
+                          static_cast<cudaStream_t>(stream));
+}
+
+int casadi_gb300_reverse(int id, int64_t n, int64_t ld, int nadj, const double* const* arg,
+                         double* const* res, const double* const* aseed, double* const* asens,
+                         void* scratch, size_t scratch_bytes, void* stream) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  if (int rc = check_device(*t)) return rc;
+  if (int rc = check_n(n, ld)) return rc;
+  if (nadj < 0 || nadj > 65535) return fail(CASADI_GB300_ERR_ARG, "bad direction count %d", nadj);
+  return run_record_waves(*t, n, ld, nadj, true, vptrs(arg),
+                          vptrs(res),
+                          vptrs(aseed),
+                          vptrs(asens), scratch, scratch_bytes,
+                          static_cast<cudaStream_t>(stream));
+}
+
+int casadi_gb300_jacobian(int id, int64_t n, int64_t ld, const double* const* arg,
+                          double* const* res, double* const* jac, void* scratch,
+                          size_t scratch_bytes, void* stream) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  if (int rc = check_device(*t)) return rc;
+  if (int rc = check_n(n, ld)) return rc;
+  int nz = 0;
+  for (int v : t->nnz_in) nz += v;
+  if (nz == 0) return fail(CASADI_GB300_ERR_ARG, "tape has no input nonzeros");
+  return run_record_waves(*t, n, ld, nz, false, vptrs(arg), vptrs(res), nullptr, vptrs(jac),
+                          scratch, scratch_bytes, static_cast<cudaStream_t>(stream), true);
+}
+
+int casadi_gb300_profile(int enable) {
+  std::lock_guard<std::mutex> lk(g_prof_mtx);
+  g_prof = enable != 0;
+  return 0;
+}
+
+int casadi_gb300_profile_collect(double* ms, int* launches, int count) {
+  if (!ms || !launches || count <= 0) return fail(CASADI_GB300_ERR_ARG, "bad arguments");
+  std::lock_guard<std::mutex> lk(g_prof_mtx);
+  for (int k = 0; k < count; ++k) {
+    ms[k] = 0;
+    launches[k] = 0;
+  }
+  int rc = 0;
+  for (ProfEntry& p : g_prof_live) {
+    cudaError_t e = cudaEventSynchronize(p.stop);
+    float t = 0;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, p.start, p.stop);
+    if (e != cudaSuccess) rc = cuda_fail(e, "profile events");
+    if (p.family < count) {
+      ms[p.family] += t;
+      launches[p.family] += 1;
+    }
+    g_prof_pool.push_back(p.start);
+    g_prof_pool.push_back(p.stop);
+  }
+  g_prof_live.clear();
+  return rc;
+}
+
+int casadi_gb300_sp_forward(int id, int64_t n, int64_t ld, const uint64_t* const* arg,
+                            uint64_t* const* res, void* stream) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  if (int rc = check_device(*t)) return rc;
+  if (int rc = check_n(n, ld)) return rc;
+  if (n == 0) return 0;
+  SweepArgs a = base_args(*t, n, 0);
+  fill_io(a.in, t->n_in, vptrs(arg), t->nnz_in, ld, false);
+  fill_io(a.out, t->n_out, vptrs(res), t->nnz_out, ld, false);
+  a.block = t->primal_block;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = timed(F_SP_FORWARD, s, [&] {
+    return launch_sp_forward(a, grid_for((n + a.block - 1) / a.block, t->primal_grid_cap), s);
+  });
+  if (e != cudaSuccess) return cuda_fail(e, "sp_forward launch");
+  return 0;
+}
+
+int casadi_gb300_sp_reverse(int id, int64_t n, int64_t ld, uint64_t* const* arg,
+                            uint64_t* const* res, void* stream) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  if (int rc = check_device(*t)) return rc;
+  if (int rc = check_n(n, ld)) return rc;
+  if (n == 0) return 0;
+  SweepArgs a = base_args(*t, n, 0);
+  fill_io(a.in, t->n_in, vptrs(arg), t->nnz_in, ld, false);
+  fill_io(a.out, t->n_out, vptrs(res), t->nnz_out, ld, false);
+  a.block = t->primal_block;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = timed(F_SP_REVERSE, s, [&] {
+    return launch_sp_reverse(a, grid_for((n + a.block - 1) / a.block, t->primal_grid_cap), s);
+  });
+  if (e != cudaSuccess) return cuda_fail(e, "sp_reverse launch");
+  return 0;
+}
+
+int casadi_gb300_sync(int id, void* stream) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+  int flags = 0;
+  if ((e = cudaMemcpy(&flags, t->d_err, sizeof(int), cudaMemcpyDeviceToHost)) != cudaSuccess)
+    return cuda_fail(e, "read error word");
+  if (flags) {
+    cudaMemset(t->d_err, 0, sizeof(int));
+    return fail(CASADI_GB300_ERR_DEVICE, "device sweep reported error flags 0x%x%s", flags,
+                (flags & kErrWaitTimeout) ? " (instruction staging wait timed out)" : "");
+  }
+  return 0;
+}
+
+int casadi_gb300_checkout(void) {
+  auto m = std::make_unique<Mem>();
+  cudaError_t e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamCreate");
+  std::lock_guard<std::mutex> lk(g_mtx);
+  for (size_t k = 0; k < g_mems.size(); ++k) {
+    if (!g_mems[k]) {
+      g_mems[k] = std::move(m);
+      return static_cast<int>(k);
+    }
+  }
+  g_mems.push_back(std::move(m));
+  return static_cast<int>(g_mems.size()) - 1;
+}
+
+int casadi_gb300_release(int mem) {
+  std::lock_guard<std::mutex> lk(g_mtx);
+  if (mem < 0 || mem >= static_cast<int>(g_mems.size()) || !g_mems[mem])
+    return fail(CASADI_GB300_ERR_ID, "no memory object %d", mem);
+  g_mems[mem].reset();
+  return 0;
+}
+
+static Mem* get_mem(int mem) {
+  std::lock_guard<std::mutex> lk(g_mtx);
+  if (mem < 0 || mem >= static_cast<int>(g_mems.size()) || !g_mems[mem]) return nullptr;
+  return g_mems[mem].get();
+}
+
+// Instance-major device blocks for the host-buffer Map path: block j holds
+// n * per_inst[j] doubles; descriptor strides address (dir, nz, inst).
+static int stage_blocks(Mem& m, size_t first_buf, int count, const std::vector<int>& nnz,
+                        int ndir, long long n, const double* const* host, bool upload,
+                        IoDesc* desc, cudaStream_t s) {
+  for (int j = 0; j < count; ++j) {
+    desc[j].ptr = nullptr;
+    if (!host || !host[j] || nnz[j] == 0) continue;
+    const size_t bytes = sizeof(double) * static_cast<size_t>(n) * nnz[j] * std::max(1, ndir);
+    cudaError_t e = cudaSuccess;
+    void* d = m.buf(first_buf + j, bytes, &e);
+    if (!d) return cuda_fail(e, "cudaMalloc(staging)");
+    if (upload && (e = cudaMemcpyAsync(d, host[j], bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+      return cuda_fail(e, "cudaMemcpyAsync(H2D)");
+    desc[j].ptr = d;
+    desc[j].nz_stride = 1;
+    desc[j].dir_stride = nnz[j];
+    desc[j].inst_stride = static_cast<long long>(nnz[j]) * std::max(1, ndir);
+  }
+  return 0;
+}
+
+static int fetch_blocks(const IoDesc* desc, int count, const std::vector<int>& nnz, int ndir,
+                        long long n, double* const* host, cudaStream_t s) {
+  for (int j = 0; j < count; ++j) {
+    if (!host || !host[j] || !desc[j].ptr) continue;
+    const size_t bytes = sizeof(double) * static_cast<size_t>(n) * nnz[j] * std::max(1, ndir);
+    cudaError_t e = cudaMemcpyAsync(host[j], desc[j].ptr, bytes, cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(D2H)");
+  }
+  return 0;
+}
+
+int casadi_gb300_map_eval(int id, int mem, int64_t n, const double* const* arg,
+                          double* const* res) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  Mem* m = get_mem(mem);
+  if (!m) return fail(CASADI_GB300_ERR_ID, "no memory object %d", mem);
+  if (int rc = check_device(*t)) return rc;
+  if (n < 0) return fail(CASADI_GB300_ERR_ARG, "negative instance count");
+  if (n == 0) return 0;
+  cudaStream_t s = m->stream;
+  SweepArgs a = base_args(*t, n, 0);
+  if (int rc = stage_blocks(*m, 0, t->n_in, t->nnz_in, 1, n, arg, true, a.in, s)) return rc;
+  if (int rc = stage_blocks(*m, kMaxIo, t->n_out, t->nnz_out, 1, n,
+                            reinterpret_cast<const double* const*>(res), false, a.out, s))
+    return rc;
+  a.block = t->primal_block;
+  cudaError_t e = timed(F_EVAL, s, [&] {
+    return launch_eval(a, grid_for((n + a.block - 1) / a.block, t->primal_grid_cap), s);
+  });
+  if (e != cudaSuccess) return cuda_fail(e, "eval launch");
+  if (int rc = fetch_blocks(a.out, t->n_out, t->nnz_out, 1, n, res, s)) return rc;
+  return casadi_gb300_sync(id, s);
+}
+
+int casadi_gb300_map_jacobian(int id, int mem, int64_t n, const double* const* arg,
+                              double* const* res, double* const* jac) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  Mem* m = get_mem(mem);
+  if (!m) return fail(CASADI_GB300_ERR_ID, "no memory object %d", mem);
+  if (int rc = check_device(*t)) return rc;
+  if (n < 0) return fail(CASADI_GB300_ERR_ARG, "negative instance count");
+  if (n == 0) return 0;
+  int nz = 0;
+  for (int v : t->nnz_in) nz += v;
+  if (nz == 0) return fail(CASADI_GB300_ERR_ARG, "tape has no input nonzeros");
+  cudaStream_t s = m->stream;
+  IoDesc in[kMaxIo], out[kMaxIo], sens[kMaxIo];
+  if (int rc = stage_blocks(*m, 0, t->n_in, t->nnz_in, 1, n, arg, true, in, s)) return rc;
+  if (int rc = stage_blocks(*m, kMaxIo, t->n_out, t->nnz_out, 1, n,
+                            reinterpret_cast<const double* const*>(res), false, out, s))
+    return rc;
+  if (int rc = stage_blocks(*m, 3 * kMaxIo, t->n_out, t->nnz_out, nz, n,
+                            reinterpret_cast<const double* const*>(jac), false, sens, s))
+    return rc;
+  size_t need = 8ull * t->n_partials * static_cast<size_t>(((n + 31) / 32) * 32);
+  const size_t kMaxScratch = 8ull << 30;
+  need = std::min(need, std::max<size_t>(kMaxScratch, 8ull * 32 * t->n_partials));
+  cudaError_t e = cudaSuccess;
+  void* scratch = t->n_partials ? m->buf(4 * kMaxIo, need, &e) : nullptr;
+  if (t->n_partials && !scratch) return cuda_fail(e, "cudaMalloc(scratch)");
+  const long long cap = wave_capacity(*t, n, need);
+  for (long long i0 = 0; i0 < n; i0 += cap) {
+    const long long mcount = std::min(cap, n - i0);
+    SweepArgs a = base_args(*t, mcount, i0);
+    std::memcpy(a.in, in, sizeof(in));
+    std::memcpy(a.out, out, sizeof(out));
+    std::memcpy(a.sens, sens, sizeof(sens));
+    for (int j = 0, off = 0; j < t->n_in; off += t->nnz_in[j], ++j) a.in_off[j] = off;
+    a.identity_seed = 1;
+    a.partials = static_cast<double*>(scratch);
+    a.pt_stride = cap;
+    a.ndir = nz;
+    a.block = t->primal_block;
+    e = timed(F_RECORD, s, [&] {
+      return launch_record(a, grid_for((mcount + a.block - 1) / a.block, t->primal_grid_cap), s);
+    });
+    if (e != cudaSuccess) return cuda_fail(e, "record sweep launch");
+    a.block = 32 * t->dir_warps;
+    const int gy = (nz + t->dir_warps - 1) / t->dir_warps;
+    const int gx = grid_for((mcount + 31) / 32, std::max(1, t->dir_grid_cap / gy));
+    e = timed(F_TANGENT, s, [&] { return launch_tangent(a, gx, gy, s); });
+    if (e != cudaSuccess) return cuda_fail(e, "tangent launch");
+  }
+  if (int rc = fetch_blocks(out, t->n_out, t->nnz_out, 1, n, res, s)) return rc;
+  if (int rc = fetch_blocks(sens, t->n_out, t->nnz_out, nz, n, jac, s)) return rc;
+  return casadi_gb300_sync(id, s);
+}
+
+int casadi_gb300_map_reverse(int id, int mem, int64_t n, int nadj, const double* const* arg,
+                             double* const* res, const double* const* aseed,
+                             double* const* asens) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  Mem* m = get_mem(mem);
+  if (!m) return fail(CASADI_GB300_ERR_ID, "no memory object %d", mem);
+  if (int rc = check_device(*t)) return rc;
+  if (n < 0 || nadj < 1 || nadj > 65535) return fail(CASADI_GB300_ERR_ARG, "bad arguments");
+  if (n == 0) return 0;
+  cudaStream_t s = m->stream;
+  IoDesc in[kMaxIo], out[kMaxIo], seed[kMaxIo], sens[kMaxIo];
+  if (int rc = stage_blocks(*m, 0, t->n_in, t->nnz_in, 1, n, arg, true, in, s)) return rc;
+  if (int rc = stage_blocks(*m, kMaxIo, t->n_out, t->nnz_out, 1, n,
+                            reinterpret_cast<const double* const*>(res), false, out, s))
+    return rc;
+  if (int rc = stage_blocks(*m, 2 * kMaxIo, t->n_out, t->nnz_out, nadj, n, aseed, true, seed, s))
+    return rc;
+  if (int rc = stage_blocks(*m, 3 * kMaxIo, t->n_in, t->nnz_in, nadj, n,
+                            reinterpret_cast<const double* const*>(asens), false, sens, s))
+    return rc;
+  size_t need = 8ull * t->n_partials * static_cast<size_t>(((n + 31) / 32) * 32);
+  const size_t kMaxScratch = 8ull << 30;  // waves keep the partials scratch below 8 GiB
+  need = std::min(need, std::max<size_t>(kMaxScratch, 8ull * 32 * t->n_partials));
+  cudaError_t e = cudaSuccess;
+  void* scratch = t->n_partials ? m->buf(4 * kMaxIo, need, &e) : nullptr;
+  if (t->n_partials && !scratch) return cuda_fail(e, "cudaMalloc(scratch)");
+  const long long cap = wave_capacity(*t, n, need);
+  for (long long i0 = 0; i0 < n; i0 += cap) {
+    const long long mcount = std::min(cap, n - i0);
+    SweepArgs a = base_args(*t, mcount, i0);
+    std::memcpy(a.in, in, sizeof(in));
+    std::memcpy(a.out, out, sizeof(out));
+    std::memcpy(a.seed, seed, sizeof(seed));
+    std::memcpy(a.sens, sens, sizeof(sens));
+    a.partials = static_cast<double*>(scratch);
+    a.pt_stride = cap;
+    a.ndir = nadj;
+    a.block = t->primal_block;
+    e = timed(F_RECORD, s, [&] {
+      return launch_record(a, grid_for((mcount + a.block - 1) / a.block, t->primal_grid_cap), s);
+    });
+    if (e != cudaSuccess) return cuda_fail(e, "record sweep launch");
+    a.block = 32 * t->dir_warps;
+    const int gy = (nadj + t->dir_warps - 1) / t->dir_warps;
+    const int gx = grid_for((mcount + 31) / 32, std::max(1, t->dir_grid_cap / gy));
+    e = timed(F_ADJOINT, s, [&] { return launch_adjoint(a, gx, gy, s); });
+    if (e != cudaSuccess) return cuda_fail(e, "adjoint launch");
+  }
+  if (int rc = fetch_blocks(out, t->n_out, t->nnz_out, 1, n, res, s)) return rc;
+  if (int rc = fetch_blocks(sens, t->n_in, t->nnz_in, nadj, n, asens, s)) return rc;
+  return casadi_gb300_sync(id, s);
+}
+
+}  // extern "C"

@@ -1,0 +1,73 @@
+// Launch interface between the C-ABI layer (abi.cu) and the tape-sweep kernels (sweeps.cu).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "device_ops.cuh"
+
+namespace cgb {
+
+constexpr int kChunk = 256;      // instructions per staged chunk (2 KiB)
+constexpr int kMaxIo = 64;       // inputs/outputs per tape handled by one launch
+constexpr int kDirWarps = 4;     // directions per CTA in the derivative sweeps (one per warp)
+
+// One input/output block: element (direction d, nonzero k, instance i) lives at
+// ptr[d*dir_stride + k*nz_stride + i*inst_stride].
+struct IoDesc {
+  void* ptr;
+  long long nz_stride;
+  long long inst_stride;
+  long long dir_stride;
+};
+
+// What every sweep needs to know about the tape.
+struct TapeView {
+  const u64* code;          // kChunk-padded instruction stream (NOP padding)
+  const double* consts;     // constant pool
+  const int2* absent_in;    // (input, nonzero) pairs the tape never reads
+  int n_chunks;
+  int n_absent_in;
+  int sz_w;
+  int n_partials;           // partials recorded per instance
+  int* err;                 // device error word
+};
+
+struct SweepArgs {
+  TapeView t;
+  long long n;              // instances in this launch
+  long long i_begin;        // offset of the first instance inside the IoDesc blocks
+  int n_in, n_out;
+  int ndir;                 // directions (forward/adjoint sweeps)
+  int dir0;                 // first direction of this launch (identity seeds)
+  int identity_seed;        // forward: seed of direction d is the d-th unit vector
+  int block;                // threads per CTA
+  double* partials;         // scratch: partials[p*pt_stride + i_local]
+  long long pt_stride;
+  IoDesc in[kMaxIo];        // values in (eval / AD / sparsity)
+  IoDesc out[kMaxIo];       // values out
+  IoDesc seed[kMaxIo];      // forward: input seeds / adjoint: output seeds
+  IoDesc sens[kMaxIo];      // forward: output sensitivities / adjoint: input sensitivities
+  int in_off[kMaxIo];       // flat offset of each input's first nonzero (identity seeds)
+};
+
+// Error bits written to TapeView::err.
+constexpr int kErrWaitTimeout = 1;   // a bounded wait on a staged chunk ran out
+constexpr int kErrBadOpcode = 2;     // an instruction with an unknown opcode was met
+
+// Shared memory a launch needs (bytes).
+size_t smem_primal(int sz_w, int block);
+size_t smem_dir(int sz_w, int dir_warps);
+int max_smem_optin();
+
+cudaError_t launch_eval(const SweepArgs& a, int grid, cudaStream_t s);
+cudaError_t launch_record(const SweepArgs& a, int grid, cudaStream_t s);
+cudaError_t launch_tangent(const SweepArgs& a, int grid_x, int grid_y, cudaStream_t s);
+cudaError_t launch_adjoint(const SweepArgs& a, int grid_x, int grid_y, cudaStream_t s);
+cudaError_t launch_sp_forward(const SweepArgs& a, int grid, cudaStream_t s);
+cudaError_t launch_sp_reverse(const SweepArgs& a, int grid, cudaStream_t s);
+
+// Resident CTAs per SM for a given kernel family and shared-memory footprint.
+int occupancy_primal(int block, size_t smem);
+int occupancy_dir(size_t smem);
+
+}  // namespace cgb

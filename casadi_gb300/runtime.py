@@ -1,0 +1,327 @@
+"""Python host side of the GB300 evaluator: ctypes bindings over the C ABI in
+``include/casadi_gb300.h`` and a tape object that runs the sweeps on device tensors.
+
+The CUDA library is the only compute path. If it is missing or cannot be loaded this module
+raises; there is no CPU fallback.
+
+Device arrays use the instance-minor layout of the C ABI: one tensor per input/output of shape
+``(nnz, n)`` (float64, contiguous, on the tape's CUDA device); seeds and sensitivities have
+shape ``(ndir, nnz, n)``.
+"""
+import ctypes as ct
+import os
+import re
+
+import numpy as np
+
+from . import sx as _sx
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libcasadi_gb300.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "casadi_gb300.h")
+
+_lib = None
+
+
+class CasadiGpuError(RuntimeError):
+    """A C-ABI call returned a nonzero status."""
+
+    def __init__(self, status, message):
+        super().__init__("casadi_gb300 status %d: %s" % (status, message))
+        self.status = status
+
+
+class Atomic(ct.Structure):
+    """casadi_gb300_atomic: the 16-byte ScalarAtomic layout."""
+    _fields_ = [("op", ct.c_int), ("i0", ct.c_int), ("u", ct.c_uint64)]
+
+
+def declared_symbols():
+    """Entry points declared in include/casadi_gb300.h."""
+    with open(HEADER) as f:
+        text = f.read()
+    return sorted(set(re.findall(r"CASADI_GB300_API\s+[\w\s\*]+?\b(casadi_gb300_\w+)\s*\(", text)))
+
+
+def load(path=None):
+    """Load libcasadi_gb300.so (building it first if it is absent and nvcc exists)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        from . import build as _build
+        _build.build()
+    lib = ct.CDLL(path)
+    vp, i64, cint, sz = ct.c_void_p, ct.c_int64, ct.c_int, ct.c_size_t
+    sig = {
+        "casadi_gb300_last_error": (ct.c_char_p, []),
+        "casadi_gb300_version": (ct.c_char_p, []),
+        "casadi_gb300_tape_create": (cint, [vp, cint, cint, vp, cint, vp, cint]),
+        "casadi_gb300_tape_free": (cint, [cint]),
+        "casadi_gb300_tape_info": (cint, [cint, vp, vp, vp, vp, vp]),
+        "casadi_gb300_scratch_size": (cint, [cint, i64, vp]),
+        "casadi_gb300_scratch_min": (cint, [cint, vp]),
+        "casadi_gb300_eval": (cint, [cint, i64, i64, vp, vp, vp]),
+        "casadi_gb300_forward": (cint, [cint, i64, i64, cint, vp, vp, vp, vp, vp, sz, vp]),
+        "casadi_gb300_reverse": (cint, [cint, i64, i64, cint, vp, vp, vp, vp, vp, sz, vp]),
+        "casadi_gb300_sp_forward": (cint, [cint, i64, i64, vp, vp, vp]),
+        "casadi_gb300_sp_reverse": (cint, [cint, i64, i64, vp, vp, vp]),
+        "casadi_gb300_sync": (cint, [cint, vp]),
+        "casadi_gb300_checkout": (cint, []),
+        "casadi_gb300_release": (cint, [cint]),
+        "casadi_gb300_map_eval": (cint, [cint, cint, i64, vp, vp]),
+        "casadi_gb300_map_reverse": (cint, [cint, cint, i64, cint, vp, vp, vp, vp]),
+        "casadi_gb300_jacobian": (cint, [cint, i64, i64, vp, vp, vp, vp, sz, vp]),
+        "casadi_gb300_map_jacobian": (cint, [cint, cint, i64, vp, vp, vp]),
+        "casadi_gb300_profile": (cint, [cint]),
+        "casadi_gb300_profile_collect": (cint, [vp, vp, cint]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(status):
+    if status < 0:
+        msg = load().casadi_gb300_last_error().decode(errors="replace")
+        raise CasadiGpuError(status, msg)
+    return status
+
+
+def _ptr_array(tensors):
+    arr = (ct.c_void_p * max(1, len(tensors)))()
+    for k, t in enumerate(tensors):
+        arr[k] = None if t is None else t.data_ptr()
+    return arr
+
+
+def _stream_handle(stream):
+    if stream is None:
+        import torch
+        return ct.c_void_p(torch.cuda.current_stream().cuda_stream)
+    return ct.c_void_p(getattr(stream, "cuda_stream", stream))
+
+
+class CudaTape:
+    """A tape registered with the GPU library (one CUDA device)."""
+
+    def __init__(self, tape):
+        if isinstance(tape, _sx.Function):
+            tape = tape.tape
+        self.tape = tape
+        lib = load()
+        atoms = tape.atomic_array()
+        self._nnz_in = np.ascontiguousarray(tape.nnz_in, dtype=np.int32)
+        self._nnz_out = np.ascontiguousarray(tape.nnz_out, dtype=np.int32)
+        self.id = check(lib.casadi_gb300_tape_create(
+            atoms.ctypes.data, tape.n_instr, len(tape.nnz_in), self._nnz_in.ctypes.data,
+            len(tape.nnz_out), self._nnz_out.ctypes.data, tape.sz_w))
+        vals = [ct.c_int() for _ in range(5)]
+        check(lib.casadi_gb300_tape_info(self.id, *[ct.byref(v) for v in vals]))
+        self.n_instr, self.n_in, self.n_out, self.sz_w, self.n_partials = [v.value for v in vals]
+        self._scratch = None
+
+    def __del__(self):
+        try:
+            if getattr(self, "id", None) is not None and _lib is not None:
+                _lib.casadi_gb300_tape_free(self.id)
+        except Exception:
+            pass
+
+    @property
+    def nnz_in(self):
+        return list(self.tape.nnz_in)
+
+    @property
+    def nnz_out(self):
+        return list(self.tape.nnz_out)
+
+    # -- scratch for the AD sweeps (device memory owned by this object) --------------------------
+    def scratch_bytes(self, n):
+        b = ct.c_size_t()
+        check(load().casadi_gb300_scratch_size(self.id, n, ct.byref(b)))
+        return b.value
+
+    def scratch(self, n, max_bytes=None):
+        import torch
+        need = self.scratch_bytes(n)
+        if max_bytes is not None:
+            mn = ct.c_size_t()
+            check(load().casadi_gb300_scratch_min(self.id, ct.byref(mn)))
+            need = max(mn.value, min(need, max_bytes))
+        if self._scratch is None or self._scratch.numel() < need:
+            self._scratch = torch.empty(max(need, 8), dtype=torch.uint8, device="cuda")
+        return self._scratch
+
+    # -- sweeps on device tensors ----------------------------------------------------------------
+    def _outs(self, nnz, n, ndir=None, dtype=None):
+        import torch
+        dtype = dtype or torch.float64
+        shape = (lambda k: (k, n)) if ndir is None else (lambda k: (ndir, k, n))
+        return [torch.empty(shape(k), dtype=dtype, device="cuda") for k in nnz]
+
+    @staticmethod
+    def _n(args):
+        for a in args:
+            if a is not None:
+                return a.shape[-1]
+        raise ValueError("cannot infer the instance count from all-null inputs")
+
+    def eval(self, args, n=None, res=None, stream=None):
+        n = self._n(args) if n is None else n
+        res = self._outs(self.nnz_out, n) if res is None else res
+        check(load().casadi_gb300_eval(self.id, n, n, _ptr_array(args), _ptr_array(res),
+                                       _stream_handle(stream)))
+        return res
+
+    def forward(self, args, fseeds, n=None, res=None, fsens=None, stream=None,
+                scratch_limit=None):
+        n = self._n(args) if n is None else n
+        nfwd = next(s.shape[0] for s in fseeds if s is not None)
+        res = self._outs(self.nnz_out, n) if res is None else res
+        fsens = self._outs(self.nnz_out, n, nfwd) if fsens is None else fsens
+        sc = self.scratch(n, scratch_limit)
+        check(load().casadi_gb300_forward(
+            self.id, n, n, nfwd, _ptr_array(args), _ptr_array(res), _ptr_array(fseeds),
+            _ptr_array(fsens), ct.c_void_p(sc.data_ptr()), sc.numel(), _stream_handle(stream)))
+        return res, fsens
+
+    def reverse(self, args, aseeds, n=None, res=None, asens=None, stream=None,
+                scratch_limit=None):
+        n = self._n(args) if n is None else n
+        nadj = next(s.shape[0] for s in aseeds if s is not None)
+        res = self._outs(self.nnz_out, n) if res is None else res
+        asens = self._outs(self.nnz_in, n, nadj) if asens is None else asens
+        sc = self.scratch(n, scratch_limit)
+        check(load().casadi_gb300_reverse(
+            self.id, n, n, nadj, _ptr_array(args), _ptr_array(res), _ptr_array(aseeds),
+            _ptr_array(asens), ct.c_void_p(sc.data_ptr()), sc.numel(), _stream_handle(stream)))
+        return res, asens
+
+    def jacobian(self, args, n=None, res=None, jac=None, stream=None, scratch_limit=None):
+        """Values and the Jacobian of every output w.r.t. every input nonzero:
+        jac[j] has shape (nnz_in_total, nnz_out[j], n); jac[j][d, k, i] = d out_j[k] / d in[d]."""
+        n = self._n(args) if n is None else n
+        nz = sum(self.nnz_in)
+        res = self._outs(self.nnz_out, n) if res is None else res
+        jac = self._outs(self.nnz_out, n, nz) if jac is None else jac
+        sc = self.scratch(n, scratch_limit)
+        check(load().casadi_gb300_jacobian(
+            self.id, n, n, _ptr_array(args), _ptr_array(res), _ptr_array(jac),
+            ct.c_void_p(sc.data_ptr()), sc.numel(), _stream_handle(stream)))
+        return res, jac
+
+    def sp_forward(self, args, n=None, stream=None):
+        """args: int64 tensors holding bvec_t bit patterns, shape (nnz, n)."""
+        import torch
+        n = self._n(args) if n is None else n
+        res = self._outs(self.nnz_out, n, dtype=torch.int64)
+        check(load().casadi_gb300_sp_forward(self.id, n, n, _ptr_array(args), _ptr_array(res),
+                                             _stream_handle(stream)))
+        return res
+
+    def sp_reverse(self, args, res, n=None, stream=None):
+        """In place: args |= propagated bits, res cleared (SXFunction::sp_reverse)."""
+        n = self._n(args + res) if n is None else n
+        check(load().casadi_gb300_sp_reverse(self.id, n, n, _ptr_array(args), _ptr_array(res),
+                                             _stream_handle(stream)))
+        return args, res
+
+    def sync(self, stream=None):
+        check(load().casadi_gb300_sync(self.id, _stream_handle(stream)))
+
+
+class MapMemory:
+    """A checked-out memory object (stream + staging buffers) for the host-buffer path."""
+
+    def __init__(self):
+        self.id = check(load().casadi_gb300_checkout())
+
+    def __del__(self):
+        try:
+            if _lib is not None:
+                _lib.casadi_gb300_release(self.id)
+        except Exception:
+            pass
+
+
+def _host_ptrs(arrays):
+    arr = (ct.c_void_p * max(1, len(arrays)))()
+    for k, a in enumerate(arrays):
+        arr[k] = None if a is None else a.ctypes.data
+    return arr
+
+
+class CudaMap:
+    """``f.map(n, "cuda")``: evaluate an SX function over n instances with host buffers in
+    CasADi's Map layout (instance-major: input j of instance i at ``arg[j][i, :]``), like
+    ``Map::eval`` (casadi/core/map.cpp:141-157, :327-386)."""
+
+    parallelization = "cuda"
+    class_name = "CudaMap"
+
+    def __init__(self, f, n):
+        self.f = f
+        self.n = int(n)
+        self.tape = f if isinstance(f, CudaTape) else CudaTape(f)
+        self.mem = MapMemory()
+        self.name = "cudamap%d_%s" % (self.n, getattr(f, "name", "f"))
+
+    def _host_out(self, nnz, ndir=1):
+        return [np.empty((self.n, ndir * k) if ndir > 1 else (self.n, k)) for k in nnz]
+
+    def __call__(self, *args, res=None):
+        """args: arrays of shape (n, nnz_in[j]) (C-contiguous float64) or None."""
+        args = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in args]
+        res = self._host_out(self.tape.nnz_out) if res is None else res
+        check(load().casadi_gb300_map_eval(self.tape.id, self.mem.id, self.n, _host_ptrs(args),
+                                           _host_ptrs(res)))
+        return res
+
+    def jacobian(self, *args, res=None, jac=None):
+        """Jacobian with instance-major host buffers: jac[j] has shape
+        (n, nnz_in_total, nnz_out[j])."""
+        args = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in args]
+        nz = sum(self.tape.nnz_in)
+        res = self._host_out(self.tape.nnz_out) if res is None else res
+        jac = [np.empty((self.n, nz, k)) for k in self.tape.nnz_out] if jac is None else jac
+        check(load().casadi_gb300_map_jacobian(self.tape.id, self.mem.id, self.n,
+                                               _host_ptrs(args), _host_ptrs(res), _host_ptrs(jac)))
+        return res, jac
+
+    def reverse(self, args, aseeds, res=None, asens=None):
+        """Adjoint sweep with instance-major host buffers: aseeds[j] has shape
+        (n, nadj, nnz_out[j]); returns (res, asens) with asens[j] of shape (n, nadj, nnz_in[j])."""
+        args = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in args]
+        aseeds = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in aseeds]
+        nadj = next(a.shape[1] for a in aseeds if a is not None)
+        res = self._host_out(self.tape.nnz_out) if res is None else res
+        asens = [np.empty((self.n, nadj, k)) for k in self.tape.nnz_in] if asens is None else asens
+        check(load().casadi_gb300_map_reverse(self.tape.id, self.mem.id, self.n, nadj,
+                                              _host_ptrs(args), _host_ptrs(res),
+                                              _host_ptrs(aseeds), _host_ptrs(asens)))
+        return res, asens
+
+
+FAMILIES = ("eval", "record", "tangent", "adjoint", "sp_forward", "sp_reverse")
+
+
+def profile(enable=True):
+    """Turn per-launch CUDA-event timing of the sweep kernels on or off."""
+    check(load().casadi_gb300_profile(1 if enable else 0))
+
+
+def profile_collect():
+    """{family: (device ms summed, launches)} since the last collect."""
+    ms = (ct.c_double * len(FAMILIES))()
+    nl = (ct.c_int * len(FAMILIES))()
+    check(load().casadi_gb300_profile_collect(ms, nl, len(FAMILIES)))
+    return {f: (ms[k], nl[k]) for k, f in enumerate(FAMILIES)}
+
+
+def version():
+    return load().casadi_gb300_version().decode()

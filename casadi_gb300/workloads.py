@@ -1,0 +1,173 @@
+"""Synthetic SX workloads: the tapes and seeded inputs the tests and the benchmark run.
+
+* cart-pole RK4 step ``f(x[4], u) -> x_next[4]`` (mc=1.0, mp=0.1, l=0.5, g=9.81, dt=0.02);
+* a ``steps``-step cart-pole rollout ``F(x0[4], U[steps]) -> (xN[4], cost)`` with
+  cost = sum_k ||x_k||^2 + 0.01 u_k^2;
+* a seeded random DAG (64 inputs, 10 000 nodes, 16 outputs; op mix add .25, sub .15,
+  mul .25, div .05, sin .06, cos .06, exp(clip(x,-5,5)) .06, log(|x|+1) .04,
+  sqrt(x^2+1) .04, tanh .04; operands drawn from the previous 256 nodes);
+* a quadcopter multiple-shooting NLP (12 states, 4 inputs, RK4, 100 intervals, dt=0.05).
+
+Inputs are drawn from seeded generators with the distributions stated for each workload.
+"""
+import math
+import numpy as np
+
+from . import sx as S
+
+CARTPOLE = dict(mc=1.0, mp=0.1, l=0.5, g=9.81, dt=0.02)
+X_LO = np.array([-2.0, -3.0, -math.pi, -5.0])
+X_HI = np.array([2.0, 3.0, math.pi, 5.0])
+U_LO, U_HI = -10.0, 10.0
+
+
+def cartpole_ode(x, u, p=CARTPOLE):
+    """Cart-pole dynamics; x = (position, velocity, angle, angular velocity)."""
+    mc, mp, l, g = p["mc"], p["mp"], p["l"], p["g"]
+    th, om = x[2], x[3]
+    s = S.sin(th)
+    c = S.cos(th)
+    den = mc + mp * s * s
+    acc = (u + mp * s * (l * om * om + g * c)) / den
+    alpha = (-u * c - mp * l * om * om * c * s - (mc + mp) * g * s) / (l * den)
+    return [x[1], acc, om, alpha]
+
+
+def rk4_step(x, u, dt=CARTPOLE["dt"], ode=cartpole_ode):
+    k1 = ode(x, u)
+    k2 = ode([xi + dt / 2 * ki for xi, ki in zip(x, k1)], u)
+    k3 = ode([xi + dt / 2 * ki for xi, ki in zip(x, k2)], u)
+    k4 = ode([xi + dt * ki for xi, ki in zip(x, k3)], u)
+    return [xi + dt / 6 * (a + 2 * b + 2 * c + d)
+            for xi, a, b, c, d in zip(x, k1, k2, k3, k4)]
+
+
+def cartpole_step():
+    """``f(x[4], u[1]) -> x_next[4]``: one RK4 step."""
+    x = S.sym("x", 4)
+    u = S.sym("u")
+    return S.Function("f", [x, [u]], [rk4_step(x, u)])
+
+
+def cartpole_rollout(steps=20):
+    """``F(x0[4], U[steps]) -> (xN[4], cost)`` with cost = sum ||x_k||^2 + 0.01 u_k^2
+    over k = 0..steps-1 (x_k the state before control u_k)."""
+    x0 = S.sym("x0", 4)
+    U = S.sym("U", steps)
+    x = list(x0)
+    cost = S.const(0.0)
+    for k in range(steps):
+        cost = cost + (x[0] * x[0] + x[1] * x[1] + x[2] * x[2] + x[3] * x[3]) \
+            + 0.01 * U[k] * U[k]
+        x = rk4_step(x, U[k])
+    return S.Function("F", [x0, U], [x, [cost]])
+
+
+def cartpole_inputs(n, steps=1, seed=0):
+    """x ~ U([-2,2]x[-3,3]x[-pi,pi]x[-5,5]), u ~ U(-10,10); instance-minor (nnz, n)."""
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(X_LO[:, None], X_HI[:, None], size=(4, n))
+    u = rng.uniform(U_LO, U_HI, size=(steps, n))
+    return [x, u]
+
+
+# ---- random DAG ------------------------------------------------------------------------------
+DAG_OPS = ["add", "sub", "mul", "div", "sin", "cos", "exp", "log", "sqrt", "tanh"]
+DAG_P = [0.25, 0.15, 0.25, 0.05, 0.06, 0.06, 0.06, 0.04, 0.04, 0.04]
+
+
+def random_dag(n_in=64, n_nodes=10000, n_out=16, seed=0, window=256):
+    """A seeded random expression DAG. Node k (k >= n_in) applies an op drawn from the
+    mix above to operands drawn uniformly from the previous ``window`` nodes; the
+    outputs are the last ``n_out`` nodes. Unary ops are guarded: exp(clip(x,-5,5)),
+    log(|x|+1), sqrt(x^2+1)."""
+    rng = np.random.default_rng(seed)
+    xs = S.sym("x", n_in)
+    nodes = list(xs)
+    cum = np.cumsum(DAG_P)
+    for k in range(n_in, n_nodes):
+        r = rng.random()
+        op = DAG_OPS[int(np.searchsorted(cum, r * cum[-1], side="right"))]
+        lo = max(0, k - window)
+        a = nodes[int(rng.integers(lo, k))]
+        b = nodes[int(rng.integers(lo, k))]
+        if op == "add":
+            e = a + b
+        elif op == "sub":
+            e = a - b
+        elif op == "mul":
+            e = a * b
+        elif op == "div":
+            e = a / (S.sq(b) + 1.0)
+        elif op == "sin":
+            e = S.sin(a)
+        elif op == "cos":
+            e = S.cos(a)
+        elif op == "exp":
+            e = S.exp(S.fmin(S.fmax(a, -5.0), 5.0))
+        elif op == "log":
+            e = S.log(S.fabs(a) + 1.0)
+        elif op == "sqrt":
+            e = S.sqrt(S.sq(a) + 1.0)
+        else:
+            e = S.tanh(a)
+        nodes.append(e)
+    outs = nodes[-n_out:]
+    return S.Function("G", [xs], [outs])
+
+
+def dag_inputs(n, n_in=64, seed=0):
+    rng = np.random.default_rng(seed)
+    return [rng.standard_normal((n_in, n))]
+
+
+# ---- quadcopter multiple shooting -----------------------------------------------------------
+QUAD = dict(m=1.0, Ixx=0.01, Iyy=0.01, Izz=0.02, g=9.81, dt=0.05)
+
+
+def quad_ode(x, u, p=QUAD):
+    """Quadcopter with thrust/torque inputs u = (T, tau_x, tau_y, tau_z);
+    x = (px, py, pz, vx, vy, vz, phi, theta, psi, p, q, r)."""
+    m, Ixx, Iyy, Izz, g = p["m"], p["Ixx"], p["Iyy"], p["Izz"], p["g"]
+    phi, th, psi = x[6], x[7], x[8]
+    pr, qr, rr = x[9], x[10], x[11]
+    T = u[0]
+    cphi, sphi = S.cos(phi), S.sin(phi)
+    cth, sth = S.cos(th), S.sin(th)
+    cpsi, spsi = S.cos(psi), S.sin(psi)
+    ax = T / m * (cphi * sth * cpsi + sphi * spsi)
+    ay = T / m * (cphi * sth * spsi - sphi * cpsi)
+    az = T / m * (cphi * cth) - g
+    tth = sth / cth
+    dphi = pr + (qr * sphi + rr * cphi) * tth
+    dth = qr * cphi - rr * sphi
+    dpsi = (qr * sphi + rr * cphi) / cth
+    dp = (u[1] + (Iyy - Izz) * qr * rr) / Ixx
+    dq = (u[2] + (Izz - Ixx) * pr * rr) / Iyy
+    dr = (u[3] + (Ixx - Iyy) * pr * qr) / Izz
+    return [x[3], x[4], x[5], ax, ay, az, dphi, dth, dpsi, dp, dq, dr]
+
+
+def quad_ms_lagrangian(intervals=100):
+    """Multiple-shooting NLP pieces: decision vector w = (x_0, u_0, ..., x_{K-1}, u_{K-1},
+    x_K) with 12 + 4 variables per interval, constraints g_k = F(x_k, u_k) - x_{k+1}
+    (and x_0 - x0bar), objective sum ||x_k||^2 + 0.1 ||u_k||^2.
+    Returns Function ``L(w, lam, x0bar) -> (g, lagrangian)``."""
+    nx, nu = 12, 4
+    K = intervals
+    w = S.sym("w", K * (nx + nu) + nx)
+    lam = S.sym("lam", (K + 1) * nx)
+    x0bar = S.sym("x0", nx)
+    xs = [w[k * (nx + nu): k * (nx + nu) + nx] for k in range(K + 1)]
+    us = [w[k * (nx + nu) + nx: k * (nx + nu) + nx + nu] for k in range(K)]
+    g = [xs[0][i] - x0bar[i] for i in range(nx)]
+    obj = S.const(0.0)
+    for k in range(K):
+        xn = rk4_step(xs[k], us[k], dt=QUAD["dt"], ode=lambda x, u: quad_ode(x, u))
+        g += [xn[i] - xs[k + 1][i] for i in range(nx)]
+        obj = obj + sum((xi * xi for xi in xs[k]), S.const(0.0)) + \
+            0.1 * sum((ui * ui for ui in us[k]), S.const(0.0))
+    lag = obj
+    for i, gi in enumerate(g):
+        lag = lag + lam[i] * gi
+    return S.Function("L", [w, lam, x0bar], [g, [lag]])

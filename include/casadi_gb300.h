@@ -1,0 +1,183 @@
+/*
+ * casadi_gb300.h — C ABI of the GB300 (sm_103a) evaluator for CasADi SX tapes.
+ *
+ * The library evaluates an SXFunction algorithm tape (CasADi's ScalarAtomic list,
+ * casadi/core/sx_function.hpp:37-44) over many instances at once, on one GPU:
+ *   eval         forward value sweep      (replaces SXFunction::eval,
+ *                                          casadi/core/sx_function.cpp:72-127)
+ *   forward      forward-mode AD sweep    (numeric analogue of SXFunction::ad_forward,
+ *                                          casadi/core/sx_function.cpp:1194-1366)
+ *   reverse      adjoint sweep            (numeric analogue of SXFunction::ad_reverse,
+ *                                          casadi/core/sx_function.cpp:1368-1569)
+ *   sp_forward   bvec_t sparsity, forward (SXFunction::sp_forward, sx_function.cpp:1657-1682)
+ *   sp_reverse   bvec_t sparsity, reverse (SXFunction::sp_reverse, sx_function.cpp:1742-1782)
+ *   map_eval     Map::eval with host buffers in the Map's instance-major layout
+ *                (casadi/core/map.cpp:141-157, :327-386)
+ *
+ * Conventions follow CasADi's C API (casadi/casadi_c.h:76-127, casadi/core/casadi_c.cpp:298-332):
+ * tapes are addressed by an int id from a process-wide registry, every entry point returns an
+ * int status (0 = success, negative = failure), nothing throws, and the text of the last error
+ * of the calling thread is available from casadi_gb300_last_error(). Registry creation and
+ * destruction are not thread-safe with respect to each other (as noted in casadi_c.h:55-68);
+ * evaluation calls on distinct streams are.
+ *
+ * Device data layout ("instance-minor"): for input j with nnz_in[j] nonzeros, nonzero k of
+ * instance i is at arg[j][k*ld + i], ld >= n. Outputs likewise. Direction d of a seed or
+ * sensitivity block is at ptr[(d*nnz + k)*ld + i]. A null pointer for an input reads zeros and
+ * a null pointer for an output skips it, exactly as SXFunction::eval treats null arg/res.
+ * All device pointers must be 8-byte aligned device memory of the current CUDA device.
+ *
+ * Streams are passed as void* (a cudaStream_t, 0 for the legacy default stream). Device-side
+ * sweeps are asynchronous; casadi_gb300_sync() waits and reports device-side error flags.
+ */
+#ifndef CASADI_GB300_H
+#define CASADI_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define CASADI_GB300_API __attribute__((visibility("default")))
+#else
+#define CASADI_GB300_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* One tape instruction, with the same 16-byte layout as CasADi's ScalarAtomic
+ * (casadi/core/sx_function.hpp:37-44): op, i0, then either the constant d (OP_CONST)
+ * or the two ints i1, i2. A CasADi build can pass algorithm_.data() unchanged. */
+typedef struct {
+  int op;
+  int i0;
+  union {
+    double d;
+    int i[2];
+  } a;
+} casadi_gb300_atomic;
+
+/* Status codes (the negative values of casadi_c.cpp:320-332 plus device-specific ones). */
+#define CASADI_GB300_OK 0
+#define CASADI_GB300_ERR_ID (-1)       /* no tape with this id */
+#define CASADI_GB300_ERR_ARG (-2)      /* invalid argument or tape */
+#define CASADI_GB300_ERR_CUDA (-3)     /* a CUDA runtime call failed */
+#define CASADI_GB300_ERR_DEVICE (-4)   /* a sweep reported a device-side error flag */
+#define CASADI_GB300_ERR_SCRATCH (-5)  /* the scratch buffer is too small */
+#define CASADI_GB300_ERR_UNSUPPORTED (-6)
+
+/* Message of the last failed call on this thread ("" if none). */
+CASADI_GB300_API const char* casadi_gb300_last_error(void);
+
+/* Library version as "major.minor.patch". */
+CASADI_GB300_API const char* casadi_gb300_version(void);
+
+/* Register a tape. The tape is validated on the host: every slot index < sz_w, every
+ * INPUT/OUTPUT reference inside nnz_in/nnz_out, every op a supported scalar op (OP_CALL and
+ * free OP_PARAMETER are rejected with CASADI_GB300_ERR_UNSUPPORTED), then uploaded to the
+ * current device. Returns the tape id (>= 0) or a negative status.
+ * Replaces: SXFunction::init's product algorithm_/worksize_ (sx_function.cpp:476-841) as
+ * consumed by the caller; the tape is taken, not rebuilt. */
+CASADI_GB300_API int casadi_gb300_tape_create(const casadi_gb300_atomic* alg, int n_instr, int n_in,
+                             const int* nnz_in, int n_out, const int* nnz_out, int sz_w);
+
+/* Release a tape and its device memory. Cf. casadi_c_decref_id (casadi_c.h:113). */
+CASADI_GB300_API int casadi_gb300_tape_free(int id);
+
+/* Shape queries. Cf. casadi_c_n_in_id/casadi_c_n_out_id/casadi_c_work_id (casadi_c.h:115-124):
+ * sz_w is the tape's work-vector length; n_partials the partial derivatives one instance
+ * records for the AD sweeps. */
+CASADI_GB300_API int casadi_gb300_tape_info(int id, int* n_instr, int* n_in, int* n_out, int* sz_w,
+                           int* n_partials);
+
+/* Scratch bytes the AD sweeps need to process n instances in one wave. A smaller scratch
+ * buffer is accepted down to casadi_gb300_scratch_min(); the sweep then runs in waves. */
+CASADI_GB300_API int casadi_gb300_scratch_size(int id, int64_t n, size_t* bytes);
+CASADI_GB300_API int casadi_gb300_scratch_min(int id, size_t* bytes);
+
+/* Forward value sweep over n instances (device pointers, instance-minor, leading dim ld).
+ * Replaces SXFunction::eval (sx_function.cpp:72-127) called once per instance by
+ * Map/OmpMap::eval (map.cpp:141-157, :340-386). */
+CASADI_GB300_API int casadi_gb300_eval(int id, int64_t n, int64_t ld, const double* const* arg,
+                      double* const* res, void* stream);
+
+/* Forward-mode AD: values plus nfwd directional derivatives.
+ * fseed[j]: nfwd x nnz_in[j] x ld, fsens[j]: nfwd x nnz_out[j] x ld (direction-major).
+ * res may be all-null. scratch: device buffer of scratch_bytes (casadi_gb300_scratch_size).
+ * Replaces evaluating Function::forward(nfwd) (function_internal.cpp:2220-2283, built by
+ * SXFunction::ad_forward, sx_function.cpp:1194-1366) under a Map. */
+CASADI_GB300_API int casadi_gb300_forward(int id, int64_t n, int64_t ld, int nfwd, const double* const* arg,
+                         double* const* res, const double* const* fseed, double* const* fsens,
+                         void* scratch, size_t scratch_bytes, void* stream);
+
+/* Reverse-mode AD: values plus nadj adjoint sensitivities.
+ * aseed[j]: nadj x nnz_out[j] x ld (output seeds), asens[j]: nadj x nnz_in[j] x ld
+ * (overwritten, not accumulated). Replaces evaluating Function::reverse(nadj)
+ * (function_internal.cpp:2285-2340, built by SXFunction::ad_reverse, sx_function.cpp:1368-1569)
+ * under a Map. */
+CASADI_GB300_API int casadi_gb300_reverse(int id, int64_t n, int64_t ld, int nadj, const double* const* arg,
+                         double* const* res, const double* const* aseed, double* const* asens,
+                         void* scratch, size_t scratch_bytes, void* stream);
+
+/* Jacobian of every output with respect to every input nonzero, by forward mode with unit
+ * seeds generated on the device (no seed memory). Direction d is the d-th input nonzero in
+ * input order; jac[j] is nnz_in_total x nnz_out[j] x ld (direction-major), i.e. column d of
+ * the Jacobian block of output j. Replaces evaluating Function::jacobian()
+ * (casadi/core/function.cpp:1068-1074, function_internal.cpp:2403-2442, built by
+ * XFunction::jac, casadi/core/x_function.hpp:441-840) under a Map. */
+CASADI_GB300_API int casadi_gb300_jacobian(int id, int64_t n, int64_t ld, const double* const* arg,
+                          double* const* res, double* const* jac, void* scratch,
+                          size_t scratch_bytes, void* stream);
+
+/* Sparsity propagation with bvec_t = uint64_t (casadi/core/casadi_common.hpp:126-130).
+ * sp_forward: res[j] = dependency bits of the outputs given arg bits
+ * (SXFunction::sp_forward, sx_function.cpp:1657-1682).
+ * sp_reverse: arg[j] |= bits propagated back from res[j]; res[j] is cleared
+ * (SXFunction::sp_reverse, sx_function.cpp:1742-1782). */
+CASADI_GB300_API int casadi_gb300_sp_forward(int id, int64_t n, int64_t ld, const uint64_t* const* arg,
+                            uint64_t* const* res, void* stream);
+CASADI_GB300_API int casadi_gb300_sp_reverse(int id, int64_t n, int64_t ld, uint64_t* const* arg,
+                            uint64_t* const* res, void* stream);
+
+/* Wait for all work on `stream` and report device-side error flags raised by sweeps of this
+ * tape (bounded waits that ran out, malformed instructions). Clears the flags. */
+CASADI_GB300_API int casadi_gb300_sync(int id, void* stream);
+
+/* Memory objects for the host-buffer path (cf. casadi_c_checkout_id/release_id,
+ * casadi_c.h:114-115): each owns a CUDA stream and device staging buffers that grow on
+ * demand and are reused across calls. */
+CASADI_GB300_API int casadi_gb300_checkout(void);
+CASADI_GB300_API int casadi_gb300_release(int mem);
+
+/* Map::eval with HOST buffers in the Map's instance-major layout: input j of instance i at
+ * arg[j] + i*nnz_in[j] (map.cpp:150-153). Copies in, runs the sweep, copies out, and waits.
+ * Pinned host memory gives the fastest copies. Replaces OmpMap::eval (map.cpp:340-386). */
+CASADI_GB300_API int casadi_gb300_map_eval(int id, int mem, int64_t n, const double* const* arg,
+                          double* const* res);
+
+/* Map over the Jacobian with host buffers: jac[j] is instance-major
+ * (jac[j] + (i*nnz_in_total + d)*nnz_out[j] holds column d of instance i). */
+CASADI_GB300_API int casadi_gb300_map_jacobian(int id, int mem, int64_t n, const double* const* arg,
+                              double* const* res, double* const* jac);
+
+/* Map over the reverse sweep with host buffers: aseed[j] is instance-major
+ * (aseed[j] + (i*nadj + d)*nnz_out[j] holds direction d of instance i), asens likewise. */
+CASADI_GB300_API int casadi_gb300_map_reverse(int id, int mem, int64_t n, int nadj, const double* const* arg,
+                             double* const* res, const double* const* aseed,
+                             double* const* asens);
+
+/* Per-launch timing. While enabled, every sweep kernel launch is bracketed by CUDA events
+ * recorded on its own stream. casadi_gb300_profile_collect waits for the recorded launches
+ * and returns, per kernel family, the summed device milliseconds and the launch count, then
+ * forgets them. Families: 0 eval, 1 record (values + partials), 2 tangent, 3 adjoint,
+ * 4 sp_forward, 5 sp_reverse. This has no counterpart in the reference (CasADi's FStats
+ * timers, casadi/core/timing.hpp:60-80, time host calls). */
+CASADI_GB300_API int casadi_gb300_profile(int enable);
+CASADI_GB300_API int casadi_gb300_profile_collect(double* ms, int* launches, int count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CASADI_GB300_H */

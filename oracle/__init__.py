@@ -1,0 +1,227 @@
+"""ORACLE — test infrastructure only.
+
+ctypes access to the plain-C restatement (``sxvm.c`` -> ``_build/liboracle.so``) and, where
+the reference tree was available at build time, to the reference-op-semantics harness
+(``ref_calculus.cpp`` -> ``_ref/libref_calculus.so``). Only tests, the smoke check and the
+CPU-baseline leg of the benchmark use this package; the product never does.
+
+Array layout: instance-minor, ``(nnz, n)`` per input/output; forward/adjoint seeds
+``(ndir, nnz, n)``.
+"""
+import ctypes as ct
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libref_calculus.so")
+REFERENCE_TREE = "/root/reference"
+
+_lib = None
+_ref = None
+
+
+def build(ref=None):
+    """Compile the oracle; also the reference harness when the reference tree exists."""
+    subprocess.check_call(["make", "-s", "-C", HERE, "all"])
+    if ref is None:
+        ref = os.path.isdir(os.path.join(REFERENCE_TREE, "casadi", "core"))
+    if ref:
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref", "REF=" + REFERENCE_TREE])
+
+
+class _Tape(ct.Structure):
+    _fields_ = [("n_instr", ct.c_int), ("op", ct.c_void_p), ("i0", ct.c_void_p),
+                ("i1", ct.c_void_p), ("i2", ct.c_void_p), ("d", ct.c_void_p),
+                ("n_in", ct.c_int), ("nnz_in", ct.c_void_p), ("n_out", ct.c_int),
+                ("nnz_out", ct.c_void_p), ("sz_w", ct.c_int)]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build(ref=False)
+        _lib = ct.CDLL(LIB_PATH)
+        _lib.sxo_fun.restype = ct.c_double
+        _lib.sxo_fun.argtypes = [ct.c_int, ct.c_double, ct.c_double]
+        _lib.sxo_der.argtypes = [ct.c_int, ct.c_double, ct.c_double, ct.c_double, ct.c_void_p]
+        for name in ("sxo_eval", "sxo_forward", "sxo_reverse", "sxo_sp_forward",
+                     "sxo_sp_reverse"):
+            getattr(_lib, name).restype = ct.c_int
+    return _lib
+
+
+def ref_available():
+    return os.path.exists(REF_PATH)
+
+
+def ref():
+    global _ref
+    if _ref is None:
+        _ref = ct.CDLL(REF_PATH)
+        _ref.ref_fun.restype = ct.c_double
+        _ref.ref_fun.argtypes = [ct.c_int, ct.c_double, ct.c_double]
+        _ref.ref_der.argtypes = [ct.c_int, ct.c_double, ct.c_double, ct.c_double, ct.c_void_p]
+        _ref.ref_op_id.argtypes = [ct.c_char_p]
+        _ref.ref_op_id.restype = ct.c_int
+        _ref.ref_ndeps.restype = ct.c_int
+    return _ref
+
+
+class TapeArrays:
+    """Keeps contiguous int32/float64 copies of a tape alive for the C calls."""
+
+    def __init__(self, tape):
+        self.tape = tape
+        self.op = np.ascontiguousarray(tape.op, dtype=np.int32)
+        self.i0 = np.ascontiguousarray(tape.i0, dtype=np.int32)
+        self.i1 = np.ascontiguousarray(tape.i1, dtype=np.int32)
+        self.i2 = np.ascontiguousarray(tape.i2, dtype=np.int32)
+        self.d = np.ascontiguousarray(tape.d, dtype=np.float64)
+        self.nnz_in = np.ascontiguousarray(tape.nnz_in, dtype=np.int32)
+        self.nnz_out = np.ascontiguousarray(tape.nnz_out, dtype=np.int32)
+        self.struct = _Tape(tape.n_instr, self.op.ctypes.data, self.i0.ctypes.data,
+                            self.i1.ctypes.data, self.i2.ctypes.data, self.d.ctypes.data,
+                            len(tape.nnz_in), self.nnz_in.ctypes.data, len(tape.nnz_out),
+                            self.nnz_out.ctypes.data, tape.sz_w)
+
+
+def _ptrs(arrays):
+    return (ct.c_void_p * max(1, len(arrays)))(
+        *[(a.ctypes.data if a is not None else None) for a in arrays])
+
+
+def _outs(nnz, n, ndir=None, dtype=np.float64):
+    if ndir is None:
+        return [np.zeros((k, n), dtype=dtype) for k in nnz]
+    return [np.zeros((ndir, k, n), dtype=dtype) for k in nnz]
+
+
+def _prep(args, dtype=np.float64):
+    return [None if a is None else np.ascontiguousarray(a, dtype=dtype) for a in args]
+
+
+def eval(tape, args, n, nthreads=1):
+    t = TapeArrays(tape)
+    args = _prep(args)
+    res = _outs(tape.nnz_out, n)
+    rc = lib().sxo_eval(ct.byref(t.struct), ct.c_long(n), _ptrs(args), _ptrs(res),
+                        ct.c_int(nthreads))
+    assert rc == 0
+    return res
+
+
+def forward(tape, args, fseeds, n, nthreads=1):
+    """Values and nfwd forward sensitivities; fseeds[j] has shape (nfwd, nnz_in[j], n)."""
+    t = TapeArrays(tape)
+    args = _prep(args)
+    fseeds = _prep(fseeds)
+    nfwd = next(s.shape[0] for s in fseeds if s is not None)
+    res = _outs(tape.nnz_out, n)
+    fsens = _outs(tape.nnz_out, n, nfwd)
+    rc = lib().sxo_forward(ct.byref(t.struct), ct.c_long(n), ct.c_int(nfwd), _ptrs(args),
+                           _ptrs(res), _ptrs(fseeds), _ptrs(fsens), ct.c_int(nthreads))
+    assert rc == 0
+    return res, fsens
+
+
+def reverse(tape, args, aseeds, n, nthreads=1):
+    """Values and nadj adjoint sensitivities; aseeds[j] has shape (nadj, nnz_out[j], n)."""
+    t = TapeArrays(tape)
+    args = _prep(args)
+    aseeds = _prep(aseeds)
+    nadj = next(s.shape[0] for s in aseeds if s is not None)
+    res = _outs(tape.nnz_out, n)
+    asens = _outs(tape.nnz_in, n, nadj)
+    rc = lib().sxo_reverse(ct.byref(t.struct), ct.c_long(n), ct.c_int(nadj), _ptrs(args),
+                           _ptrs(res), _ptrs(aseeds), _ptrs(asens), ct.c_int(nthreads))
+    assert rc == 0
+    return res, asens
+
+
+def sp_forward(tape, args, n, nthreads=1):
+    t = TapeArrays(tape)
+    args = _prep(args, np.uint64)
+    res = _outs(tape.nnz_out, n, dtype=np.uint64)
+    rc = lib().sxo_sp_forward(ct.byref(t.struct), ct.c_long(n), _ptrs(args), _ptrs(res),
+                              ct.c_int(nthreads))
+    assert rc == 0
+    return res
+
+
+def sp_reverse(tape, args, res, n, nthreads=1):
+    """In place, like SXFunction::sp_reverse: args |= sensitivities, res seeds cleared."""
+    t = TapeArrays(tape)
+    rc = lib().sxo_sp_reverse(ct.byref(t.struct), ct.c_long(n), _ptrs(args), _ptrs(res),
+                              ct.c_int(nthreads))
+    assert rc == 0
+    return args, res
+
+
+def fun(op, x, y):
+    return lib().sxo_fun(op, x, y)
+
+
+def der(op, x, y, f):
+    d = np.zeros(2)
+    lib().sxo_der(op, x, y, f, d.ctypes.data)
+    return d
+
+
+# ---- reference harness (only where it was built) --------------------------------------------
+def ref_fun(op, x, y):
+    return ref().ref_fun(op, x, y)
+
+
+def ref_der(op, x, y, f):
+    d = np.zeros(2)
+    ref().ref_der(op, x, y, f, d.ctypes.data)
+    return d
+
+
+def ref_eval(tape, args, n):
+    t = TapeArrays(tape)
+    args = _prep(args)
+    res = _outs(tape.nnz_out, n)
+    rc = ref().ref_eval(ct.c_int(tape.n_instr), t.op.ctypes.data_as(ct.c_void_p),
+                        t.i0.ctypes.data_as(ct.c_void_p), t.i1.ctypes.data_as(ct.c_void_p),
+                        t.i2.ctypes.data_as(ct.c_void_p), t.d.ctypes.data_as(ct.c_void_p),
+                        ct.c_int(tape.sz_w), ct.c_long(n), _ptrs(args), _ptrs(res))
+    assert rc == 0
+    return res
+
+
+def ref_forward(tape, args, fseeds, n):
+    t = TapeArrays(tape)
+    args = _prep(args)
+    fseeds = _prep(fseeds)
+    nfwd = next(s.shape[0] for s in fseeds if s is not None)
+    fsens = _outs(tape.nnz_out, n, nfwd)
+    rc = ref().ref_forward(ct.c_int(tape.n_instr), t.op.ctypes.data_as(ct.c_void_p),
+                           t.i0.ctypes.data_as(ct.c_void_p), t.i1.ctypes.data_as(ct.c_void_p),
+                           t.i2.ctypes.data_as(ct.c_void_p), t.d.ctypes.data_as(ct.c_void_p),
+                           ct.c_int(tape.sz_w), t.nnz_in.ctypes.data_as(ct.c_void_p),
+                           t.nnz_out.ctypes.data_as(ct.c_void_p), ct.c_long(n),
+                           ct.c_int(nfwd), _ptrs(args), _ptrs(fseeds), _ptrs(fsens))
+    assert rc == 0
+    return fsens
+
+
+def ref_reverse(tape, args, aseeds, n):
+    t = TapeArrays(tape)
+    args = _prep(args)
+    aseeds = _prep(aseeds)
+    nadj = next(s.shape[0] for s in aseeds if s is not None)
+    asens = _outs(tape.nnz_in, n, nadj)
+    rc = ref().ref_reverse(ct.c_int(tape.n_instr), t.op.ctypes.data_as(ct.c_void_p),
+                           t.i0.ctypes.data_as(ct.c_void_p), t.i1.ctypes.data_as(ct.c_void_p),
+                           t.i2.ctypes.data_as(ct.c_void_p), t.d.ctypes.data_as(ct.c_void_p),
+                           ct.c_int(tape.sz_w), ct.c_int(len(tape.nnz_in)),
+                           t.nnz_in.ctypes.data_as(ct.c_void_p),
+                           t.nnz_out.ctypes.data_as(ct.c_void_p), ct.c_long(n),
+                           ct.c_int(nadj), _ptrs(args), _ptrs(aseeds), _ptrs(asens))
+    assert rc == 0
+    return asens

@@ -1,0 +1,174 @@
+// ORACLE PIN — test infrastructure only, built into oracle/_ref/ from the reference's own
+// sources where they lie (the reference tree is needed at build time; it is not copied).
+//
+// The reference's scalar-op semantics are header-only templates in casadi/core/calculus.hpp.
+// This harness compiles that header as is and exposes, over a C ABI:
+//   ref_fun / ref_der   casadi_math<double>::fun / der (calculus.hpp:1299-1439)
+//   ref_ndeps           casadi_math<double>::ndeps (calculus.hpp:1632-1647)
+//   ref_op_id           the numeric value of enum Operation members (calculus.hpp:60-218)
+//   ref_eval            SXFunction::eval's instruction loop (casadi/core/sx_function.cpp:110-124)
+//                       driving the reference's own CASADI_MATH_FUN_BUILTIN dispatch macro
+//   ref_forward / ref_reverse
+//                       the numeric forward/adjoint sweeps that mirror the structure of
+//                       SXFunction::ad_forward/ad_reverse (sx_function.cpp:1248-1364,
+//                       :1418-1560) with partials from CASADI_MATH_DER_BUILTIN
+// The rest of libcasadi needs CMake-generated headers and is not built.
+#include <iomanip>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#include "casadi/core/exception.hpp"
+#include "casadi/core/calculus.hpp"
+
+namespace casadi {
+// calculus.hpp's printme() writes to uout(); libcasadi defines it in casadi_logger.cpp.
+std::ostream& uout() { return std::cout; }
+}  // namespace casadi
+
+using namespace casadi;
+
+extern "C" {
+
+double ref_fun(int op, double x, double y) {
+  double f;
+  casadi_math<double>::fun(static_cast<unsigned char>(op), x, y, f);
+  return f;
+}
+
+void ref_der(int op, double x, double y, double f, double* d) {
+  casadi_math<double>::der(static_cast<unsigned char>(op), x, y, f, d);
+}
+
+int ref_ndeps(int op) { return static_cast<int>(casadi_math<double>::ndeps(op)); }
+
+int ref_op_id(const char* name) {
+#define ID(X) if (!std::strcmp(name, #X)) return X;
+  ID(OP_ASSIGN) ID(OP_ADD) ID(OP_SUB) ID(OP_MUL) ID(OP_DIV) ID(OP_NEG) ID(OP_EXP) ID(OP_LOG)
+  ID(OP_POW) ID(OP_CONSTPOW) ID(OP_SQRT) ID(OP_SQ) ID(OP_TWICE) ID(OP_SIN) ID(OP_COS)
+  ID(OP_TAN) ID(OP_ASIN) ID(OP_ACOS) ID(OP_ATAN) ID(OP_LT) ID(OP_LE) ID(OP_EQ) ID(OP_NE)
+  ID(OP_NOT) ID(OP_AND) ID(OP_OR) ID(OP_FLOOR) ID(OP_CEIL) ID(OP_FMOD) ID(OP_FABS)
+  ID(OP_SIGN) ID(OP_COPYSIGN) ID(OP_IF_ELSE_ZERO) ID(OP_ERF) ID(OP_FMIN) ID(OP_FMAX)
+  ID(OP_INV) ID(OP_SINH) ID(OP_COSH) ID(OP_TANH) ID(OP_ASINH) ID(OP_ACOSH) ID(OP_ATANH)
+  ID(OP_ATAN2) ID(OP_CONST) ID(OP_INPUT) ID(OP_OUTPUT) ID(OP_PARAMETER) ID(OP_CALL)
+  ID(OP_ERFINV) ID(OP_PRINTME) ID(OP_LIFT) ID(OP_LOG1P) ID(OP_EXPM1) ID(OP_HYPOT)
+  ID(OP_REMAINDER)
+#undef ID
+  return -1;
+}
+
+// Instance-minor layout: arg[j][k*n + i]; see oracle/sxvm.c.
+int ref_eval(int n_instr, const int* op, const int* i0, const int* i1, const int* i2,
+             const double* d, int sz_w, long n, const double* const* arg,
+             double* const* res) {
+  std::vector<double> w(sz_w > 0 ? sz_w : 1);
+  for (long i = 0; i < n; ++i) {
+    for (int k = 0; k < n_instr; ++k) {
+      switch (op[k]) {
+        CASADI_MATH_FUN_BUILTIN(w[i1[k]], w[i2[k]], w[i0[k]])
+        case OP_CONST: w[i0[k]] = d[k]; break;
+        case OP_INPUT: w[i0[k]] = arg[i1[k]] == nullptr ? 0 : arg[i1[k]][i2[k] * n + i]; break;
+        case OP_OUTPUT: if (res[i0[k]] != nullptr) res[i0[k]][i2[k] * n + i] = w[i1[k]]; break;
+        default: return 1;
+      }
+    }
+  }
+  return 0;
+}
+
+static void partials(int n_instr, const int* op, const int* i0, const int* i1, const int* i2,
+                     const double* d, long n, long i, const double* const* arg,
+                     std::vector<double>& w, std::vector<double>& dp) {
+  for (int k = 0; k < n_instr; ++k) {
+    switch (op[k]) {
+      case OP_CONST: w[i0[k]] = d[k]; break;
+      case OP_INPUT: w[i0[k]] = arg[i1[k]] == nullptr ? 0 : arg[i1[k]][i2[k] * n + i]; break;
+      case OP_OUTPUT: break;
+      default: {
+        double x = w[i1[k]], y = w[i2[k]], f;
+        casadi_math<double>::fun(static_cast<unsigned char>(op[k]), x, y, f);
+        casadi_math<double>::der(static_cast<unsigned char>(op[k]), x, y, f, &dp[2 * k]);
+        w[i0[k]] = f;
+      }
+    }
+  }
+}
+
+int ref_forward(int n_instr, const int* op, const int* i0, const int* i1, const int* i2,
+                const double* d, int sz_w, const int* nnz_in, const int* nnz_out, long n,
+                int nfwd, const double* const* arg, const double* const* fseed,
+                double* const* fsens) {
+  std::vector<double> w(sz_w > 0 ? sz_w : 1), wd(sz_w > 0 ? sz_w : 1), dp(2 * n_instr + 2);
+  for (long i = 0; i < n; ++i) {
+    partials(n_instr, op, i0, i1, i2, d, n, i, arg, w, dp);
+    for (int dir = 0; dir < nfwd; ++dir) {
+      for (int k = 0; k < n_instr; ++k) {
+        const double* p = &dp[2 * k];
+        switch (op[k]) {
+          case OP_INPUT:
+            wd[i0[k]] = fseed[i1[k]] ? fseed[i1[k]][(dir * nnz_in[i1[k]] + i2[k]) * n + i] : 0;
+            break;
+          case OP_OUTPUT:
+            if (fsens[i0[k]]) fsens[i0[k]][(dir * nnz_out[i0[k]] + i2[k]) * n + i] = wd[i1[k]];
+            break;
+          case OP_CONST: case OP_PARAMETER: wd[i0[k]] = 0; break;
+          case OP_IF_ELSE_ZERO: wd[i0[k]] = if_else_zero(p[1], wd[i2[k]]); break;
+          CASADI_MATH_BINARY_BUILTIN
+            wd[i0[k]] = p[0] * wd[i1[k]] + p[1] * wd[i2[k]];
+            break;
+          default:
+            wd[i0[k]] = p[0] * wd[i1[k]];
+        }
+      }
+    }
+  }
+  return 0;
+}
+
+int ref_reverse(int n_instr, const int* op, const int* i0, const int* i1, const int* i2,
+                const double* d, int sz_w, int n_in, const int* nnz_in, const int* nnz_out,
+                long n, int nadj, const double* const* arg, const double* const* aseed,
+                double* const* asens) {
+  std::vector<double> w(sz_w > 0 ? sz_w : 1), wb(sz_w > 0 ? sz_w : 1), dp(2 * n_instr + 2);
+  for (long i = 0; i < n; ++i) {
+    partials(n_instr, op, i0, i1, i2, d, n, i, arg, w, dp);
+    for (int dir = 0; dir < nadj; ++dir) {
+      std::fill(wb.begin(), wb.end(), 0.0);
+      for (int j = 0; j < n_in; ++j) {
+        if (!asens[j]) continue;
+        for (int k = 0; k < nnz_in[j]; ++k) asens[j][(dir * nnz_in[j] + k) * n + i] = 0;
+      }
+      for (int k = n_instr - 1; k >= 0; --k) {
+        const double* p = &dp[2 * k];
+        double seed;
+        switch (op[k]) {
+          case OP_INPUT:
+            if (asens[i1[k]]) asens[i1[k]][(dir * nnz_in[i1[k]] + i2[k]) * n + i] = wb[i0[k]];
+            wb[i0[k]] = 0;
+            break;
+          case OP_OUTPUT:
+            if (aseed[i0[k]]) wb[i1[k]] += aseed[i0[k]][(dir * nnz_out[i0[k]] + i2[k]) * n + i];
+            break;
+          case OP_CONST: case OP_PARAMETER: wb[i0[k]] = 0; break;
+          case OP_IF_ELSE_ZERO:
+            seed = wb[i0[k]];
+            wb[i0[k]] = 0;
+            wb[i2[k]] += if_else_zero(p[1], seed);
+            break;
+          CASADI_MATH_BINARY_BUILTIN
+            seed = wb[i0[k]];
+            wb[i0[k]] = 0;
+            wb[i1[k]] += p[0] * seed;
+            wb[i2[k]] += p[1] * seed;
+            break;
+          default:
+            seed = wb[i0[k]];
+            wb[i0[k]] = 0;
+            wb[i1[k]] += p[0] * seed;
+        }
+      }
+    }
+  }
+  return 0;
+}
+
+}  // extern "C"

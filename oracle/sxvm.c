@@ -1,0 +1,427 @@
+/*
+ * ORACLE — test infrastructure only. Nothing in the product links or calls this file;
+ * only tests/, the smoke check and the CPU-baseline leg of bench.py load it, as the
+ * checker of the CUDA sweeps and as the timed CPU port.
+ *
+ * A plain-C restatement of CasADi's SX virtual machine over many instances:
+ *   sxo_fun / sxo_der   casadi_math<double>::fun / der   (casadi/core/calculus.hpp:598-1018,
+ *                        dispatch macros :1302-1355 and :1388-1439, sign :270,
+ *                        if_else_zero :295, erfinv :297-328)
+ *   sxo_eval            SXFunction::eval                 (casadi/core/sx_function.cpp:110-124)
+ *   sxo_forward         numeric analogue of SXFunction::ad_forward (sx_function.cpp:1248-1364)
+ *   sxo_reverse         numeric analogue of SXFunction::ad_reverse (sx_function.cpp:1418-1560)
+ *   sxo_sp_forward      SXFunction::sp_forward           (sx_function.cpp:1657-1682)
+ *   sxo_sp_reverse      SXFunction::sp_reverse           (sx_function.cpp:1742-1782)
+ *
+ * Data layout (the layout the CUDA sweeps use): instance-minor. Input j of instance i,
+ * nonzero k lives at arg[j][k*n + i]; outputs likewise. A null arg[j] reads zeros, a null
+ * res[j] is skipped, as in SXFunction::eval.
+ *
+ * Forward seeds: fseed[j][(d*nnz_in[j] + k)*n + i] for direction d; sensitivities likewise.
+ * Adjoint seeds aseed[j] (outputs) and sensitivities asens[j] (inputs) use the same
+ * direction-major layout.
+ *
+ * Built with -ffp-contract=off: every operation rounds to double as the reference does.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "sxvm.h"
+
+static double sxo_sign(double x) { return x < 0 ? -1 : x > 0 ? 1 : x; }
+
+/* std::fmin/fmax as the reference build resolves them on x86-64: a NaN operand yields the
+ * other operand and a tie (+0 vs -0 included) yields the first operand. C leaves the sign
+ * of a zero tie unspecified; this fixes it so results compare bit for bit. */
+static double sxo_fmin(double x, double y) {
+  if (isnan(x)) return y;
+  if (isnan(y)) return x;
+  return y < x ? y : x;
+}
+static double sxo_fmax(double x, double y) {
+  if (isnan(x)) return y;
+  if (isnan(y)) return x;
+  return y > x ? y : x;
+}
+
+/* calculus.hpp:297-328, used because the C library provides no erfinv */
+static double sxo_erfinv(double x) {
+  if (x >= 1) {
+    return x == 1 ? INFINITY : NAN;
+  } else if (x <= -1) {
+    return x == -1 ? -INFINITY : NAN;
+  } else if (x < -0.7) {
+    double z = sqrt(-log((1.0 + x) / 2.0));
+    return -(((1.641345311 * z + 3.429567803) * z - 1.624906493) * z - 1.970840454) /
+           ((1.637067800 * z + 3.543889200) * z + 1.0);
+  } else {
+    double y;
+    if (x < 0.7) {
+      double z = x * x;
+      y = x * (((-0.140543331 * z + 0.914624893) * z - 1.645349621) * z + 0.886226899) /
+          ((((-0.329097515 * z + 0.012229801) * z + 1.442710462) * z - 2.118377725) * z + 1.0);
+    } else {
+      double z = sqrt(-log((1.0 - x) / 2.0));
+      y = (((1.641345311 * z + 3.429567803) * z - 1.624906493) * z - 1.970840454) /
+          ((1.637067800 * z + 3.543889200) * z + 1.0);
+    }
+    y = y - (erf(y) - x) / (2.0 / sqrt(M_PI) * exp(-y * y));
+    y = y - (erf(y) - x) / (2.0 / sqrt(M_PI) * exp(-y * y));
+    return y;
+  }
+}
+
+double sxo_fun(int op, double x, double y) {
+  switch (op) {
+    case SXO_ASSIGN: return x;
+    case SXO_ADD: return x + y;
+    case SXO_SUB: return x - y;
+    case SXO_MUL: return x * y;
+    case SXO_DIV: return x / y;
+    case SXO_NEG: return -x;
+    case SXO_EXP: return exp(x);
+    case SXO_LOG: return log(x);
+    case SXO_POW: return pow(x, y);
+    case SXO_CONSTPOW: return pow(x, y);
+    case SXO_SQRT: return sqrt(x);
+    case SXO_SQ: return x * x;
+    case SXO_TWICE: return 2. * x;
+    case SXO_SIN: return sin(x);
+    case SXO_COS: return cos(x);
+    case SXO_TAN: return tan(x);
+    case SXO_ASIN: return asin(x);
+    case SXO_ACOS: return acos(x);
+    case SXO_ATAN: return atan(x);
+    case SXO_LT: return x < y;
+    case SXO_LE: return x <= y;
+    case SXO_EQ: return x == y;
+    case SXO_NE: return x != y;
+    case SXO_NOT: return !x;
+    case SXO_AND: return x && y;
+    case SXO_OR: return x || y;
+    case SXO_FLOOR: return floor(x);
+    case SXO_CEIL: return ceil(x);
+    case SXO_FMOD: return fmod(x, y);
+    case SXO_REMAINDER: return remainder(x, y);
+    case SXO_FABS: return fabs(x);
+    case SXO_SIGN: return sxo_sign(x);
+    case SXO_COPYSIGN: return copysign(x, y);
+    case SXO_IF_ELSE_ZERO: return x == 0 ? 0 : y;
+    case SXO_ERF: return erf(x);
+    case SXO_FMIN: return sxo_fmin(x, y);
+    case SXO_FMAX: return sxo_fmax(x, y);
+    case SXO_INV: return 1. / x;
+    case SXO_SINH: return sinh(x);
+    case SXO_COSH: return cosh(x);
+    case SXO_TANH: return tanh(x);
+    case SXO_ASINH: return asinh(x);
+    case SXO_ACOSH: return acosh(x);
+    case SXO_ATANH: return atanh(x);
+    case SXO_ATAN2: return atan2(x, y);
+    case SXO_ERFINV: return sxo_erfinv(x);
+    case SXO_PRINTME: return x; /* the reference also prints; the oracle does not */
+    case SXO_LIFT: return x;
+    case SXO_LOG1P: return log1p(x);
+    case SXO_EXPM1: return expm1(x);
+    case SXO_HYPOT: return hypot(x, y);
+    default: return NAN;
+  }
+}
+
+/* BinaryOperation<OP>::der (calculus.hpp:598-1018); unary ops set d[1] = 0 (:384-387) */
+void sxo_der(int op, double x, double y, double f, double* d) {
+  d[1] = 0;
+  switch (op) {
+    case SXO_ASSIGN: d[0] = 1; break;
+    case SXO_ADD: d[0] = d[1] = 1; break;
+    case SXO_SUB: d[0] = 1; d[1] = -1; break;
+    case SXO_MUL: d[0] = y; d[1] = x; break;
+    case SXO_DIV: d[0] = 1 / y; d[1] = -f / y; break;
+    case SXO_NEG: d[0] = -1; break;
+    case SXO_EXP: d[0] = f; break;
+    case SXO_LOG: d[0] = 1 / x; break;
+    case SXO_POW: d[0] = y * pow(x, y - 1); d[1] = log(x) * f; break;
+    case SXO_CONSTPOW: d[0] = y * pow(x, y - 1); d[1] = 0; break;
+    case SXO_SQRT: d[0] = 1 / (f + f); break;
+    case SXO_SQ: d[0] = x + x; break;
+    case SXO_TWICE: d[0] = 2; break;
+    case SXO_SIN: d[0] = cos(x); break;
+    case SXO_COS: d[0] = -sin(x); break;
+    case SXO_TAN: { double c = cos(x); d[0] = 1 / (c * c); } break;
+    case SXO_ASIN: d[0] = 1 / sqrt(1 - x * x); break;
+    case SXO_ACOS: d[0] = -1 / sqrt(1 - x * x); break;
+    case SXO_ATAN: d[0] = 1 / (1 + x * x); break;
+    case SXO_LT: case SXO_LE: case SXO_EQ: case SXO_NE: case SXO_AND: case SXO_OR:
+      d[0] = d[1] = 0; break;
+    case SXO_NOT: case SXO_FLOOR: case SXO_CEIL: case SXO_SIGN: d[0] = 0; break;
+    case SXO_FMOD: case SXO_REMAINDER: d[0] = 1; d[1] = (f - x) / y; break;
+    case SXO_FABS: d[0] = sxo_sign(x); break;
+    case SXO_COPYSIGN: d[0] = copysign(1.0, y); d[1] = 0; break;
+    case SXO_IF_ELSE_ZERO: d[0] = 0; d[1] = x; break;
+    case SXO_ERF: d[0] = (2 / sqrt(M_PI)) * exp(-x * x); break;
+    case SXO_FMIN: {
+      double a = x <= y, b = y <= x, c = a + b;
+      d[0] = a / c; d[1] = b / c;
+    } break;
+    case SXO_FMAX: {
+      double a = y <= x, b = x <= y, c = a + b;
+      d[0] = a / c; d[1] = b / c;
+    } break;
+    case SXO_INV: d[0] = -f * f; break;
+    case SXO_SINH: d[0] = cosh(x); break;
+    case SXO_COSH: d[0] = sinh(x); break;
+    case SXO_TANH: d[0] = 1 - f * f; break;
+    case SXO_ASINH: d[0] = 1 / sqrt(1 + x * x); break;
+    case SXO_ACOSH: d[0] = 1 / sqrt(x - 1) / sqrt(x + 1); break;
+    case SXO_ATANH: d[0] = 1 / (1 - x * x); break;
+    case SXO_ATAN2: { double t = x * x + y * y; d[0] = y / t; d[1] = -x / t; } break;
+    case SXO_ERFINV: d[0] = (sqrt(M_PI) / 2) * exp(f * f); break;
+    case SXO_PRINTME: case SXO_LIFT: d[0] = 1; d[1] = 0; break;
+    case SXO_LOG1P: d[0] = 1 / (1 + x); break;
+    case SXO_EXPM1: d[0] = exp(x); break;
+    case SXO_HYPOT: d[0] = x / f; d[1] = y / f; break;
+    default: d[0] = d[1] = NAN;
+  }
+}
+
+int sxo_ndeps(int op) {
+  switch (op) {
+    case SXO_CONST: case SXO_PARAMETER: case SXO_INPUT: return 0;
+    case SXO_ADD: case SXO_SUB: case SXO_MUL: case SXO_DIV: case SXO_POW: case SXO_CONSTPOW:
+    case SXO_LT: case SXO_LE: case SXO_EQ: case SXO_NE: case SXO_AND: case SXO_OR:
+    case SXO_COPYSIGN: case SXO_FMOD: case SXO_REMAINDER: case SXO_FMIN: case SXO_FMAX:
+    case SXO_ATAN2: case SXO_PRINTME: case SXO_LIFT: case SXO_HYPOT: case SXO_IF_ELSE_ZERO:
+      return 2;
+    default: return 1;
+  }
+}
+
+/* ---------------------------------------------------------------------------------------- */
+/* one instance                                                                              */
+/* ---------------------------------------------------------------------------------------- */
+
+static void eval_one(const sxo_tape* t, long n, long i, const double* const* arg,
+                     double* const* res, double* w) {
+  for (int k = 0; k < t->n_instr; ++k) {
+    int op = t->op[k], i0 = t->i0[k], i1 = t->i1[k], i2 = t->i2[k];
+    switch (op) {
+      case SXO_CONST: w[i0] = t->d[k]; break;
+      case SXO_INPUT: w[i0] = arg[i1] ? arg[i1][(long)i2 * n + i] : 0; break;
+      case SXO_OUTPUT: if (res[i0]) res[i0][(long)i2 * n + i] = w[i1]; break;
+      default: w[i0] = sxo_fun(op, w[i1], w[i2]);
+    }
+  }
+}
+
+/* values plus the partials of every arithmetic instruction, in tape order */
+static void eval_partials(const sxo_tape* t, long n, long i, const double* const* arg,
+                          double* const* res, double* w, double* dp) {
+  for (int k = 0; k < t->n_instr; ++k) {
+    int op = t->op[k], i0 = t->i0[k], i1 = t->i1[k], i2 = t->i2[k];
+    switch (op) {
+      case SXO_CONST: w[i0] = t->d[k]; break;
+      case SXO_INPUT: w[i0] = arg[i1] ? arg[i1][(long)i2 * n + i] : 0; break;
+      case SXO_OUTPUT: if (res && res[i0]) res[i0][(long)i2 * n + i] = w[i1]; break;
+      default: {
+        double x = w[i1], y = w[i2];
+        double f = sxo_fun(op, x, y);
+        sxo_der(op, x, y, f, dp + 2 * (long)k);
+        w[i0] = f;
+      }
+    }
+  }
+}
+
+int sxo_eval(const sxo_tape* t, long n, const double* const* arg, double* const* res,
+             int nthreads) {
+  int err = 0;
+#pragma omp parallel num_threads(nthreads > 0 ? nthreads : 1)
+  {
+    double* w = (double*)malloc(sizeof(double) * (t->sz_w > 0 ? t->sz_w : 1));
+    if (!w) {
+#pragma omp atomic write
+      err = 1;
+    } else {
+#pragma omp for schedule(static)
+      for (long i = 0; i < n; ++i) eval_one(t, n, i, arg, res, w);
+    }
+    free(w);
+  }
+  return err;
+}
+
+int sxo_forward(const sxo_tape* t, long n, int nfwd, const double* const* arg,
+                double* const* res, const double* const* fseed, double* const* fsens,
+                int nthreads) {
+  int err = 0;
+#pragma omp parallel num_threads(nthreads > 0 ? nthreads : 1)
+  {
+    double* w = (double*)malloc(sizeof(double) * (t->sz_w > 0 ? t->sz_w : 1));
+    double* wd = (double*)malloc(sizeof(double) * (t->sz_w > 0 ? t->sz_w : 1));
+    double* dp = (double*)malloc(sizeof(double) * 2 * (t->n_instr > 0 ? t->n_instr : 1));
+    if (!w || !wd || !dp) {
+#pragma omp atomic write
+      err = 1;
+    } else {
+#pragma omp for schedule(static)
+      for (long i = 0; i < n; ++i) {
+        eval_partials(t, n, i, arg, res, w, dp);
+        for (int dir = 0; dir < nfwd; ++dir) {
+          for (int k = 0; k < t->n_instr; ++k) {
+            int op = t->op[k], i0 = t->i0[k], i1 = t->i1[k], i2 = t->i2[k];
+            const double* d = dp + 2 * (long)k;
+            switch (op) {
+              case SXO_INPUT: {
+                const double* s = fseed[i1];
+                wd[i0] = s ? s[((long)dir * t->nnz_in[i1] + i2) * n + i] : 0;
+              } break;
+              case SXO_OUTPUT: {
+                double* s = fsens[i0];
+                if (s) s[((long)dir * t->nnz_out[i0] + i2) * n + i] = wd[i1];
+              } break;
+              case SXO_CONST: case SXO_PARAMETER: wd[i0] = 0; break;
+              case SXO_IF_ELSE_ZERO: wd[i0] = d[1] == 0 ? 0 : wd[i2]; break;
+              default:
+                if (sxo_ndeps(op) == 2) wd[i0] = d[0] * wd[i1] + d[1] * wd[i2];
+                else wd[i0] = d[0] * wd[i1];
+            }
+          }
+        }
+      }
+    }
+    free(w); free(wd); free(dp);
+  }
+  return err;
+}
+
+int sxo_reverse(const sxo_tape* t, long n, int nadj, const double* const* arg,
+                double* const* res, const double* const* aseed, double* const* asens,
+                int nthreads) {
+  int err = 0;
+#pragma omp parallel num_threads(nthreads > 0 ? nthreads : 1)
+  {
+    double* w = (double*)malloc(sizeof(double) * (t->sz_w > 0 ? t->sz_w : 1));
+    double* wb = (double*)malloc(sizeof(double) * (t->sz_w > 0 ? t->sz_w : 1));
+    double* dp = (double*)malloc(sizeof(double) * 2 * (t->n_instr > 0 ? t->n_instr : 1));
+    if (!w || !wb || !dp) {
+#pragma omp atomic write
+      err = 1;
+    } else {
+#pragma omp for schedule(static)
+      for (long i = 0; i < n; ++i) {
+        eval_partials(t, n, i, arg, res, w, dp);
+        for (int dir = 0; dir < nadj; ++dir) {
+          for (int s = 0; s < t->sz_w; ++s) wb[s] = 0;
+          /* asens starts at zero for every input nonzero (sx_function.cpp:1413-1422) */
+          for (int j = 0; j < t->n_in; ++j) {
+            if (!asens[j]) continue;
+            for (int k = 0; k < t->nnz_in[j]; ++k)
+              asens[j][((long)dir * t->nnz_in[j] + k) * n + i] = 0;
+          }
+          for (int k = t->n_instr - 1; k >= 0; --k) {
+            int op = t->op[k], i0 = t->i0[k], i1 = t->i1[k], i2 = t->i2[k];
+            const double* d = dp + 2 * (long)k;
+            double seed;
+            switch (op) {
+              case SXO_INPUT: {
+                double* s = asens[i1];
+                if (s) s[((long)dir * t->nnz_in[i1] + i2) * n + i] = wb[i0];
+                wb[i0] = 0;
+              } break;
+              case SXO_OUTPUT: {
+                const double* s = aseed[i0];
+                if (s) wb[i1] += s[((long)dir * t->nnz_out[i0] + i2) * n + i];
+              } break;
+              case SXO_CONST: case SXO_PARAMETER: wb[i0] = 0; break;
+              case SXO_IF_ELSE_ZERO:
+                seed = wb[i0]; wb[i0] = 0;
+                wb[i2] += d[1] == 0 ? 0 : seed;
+                break;
+              default:
+                seed = wb[i0]; wb[i0] = 0;
+                if (sxo_ndeps(op) == 2) {
+                  wb[i1] += d[0] * seed;
+                  wb[i2] += d[1] * seed;
+                } else {
+                  wb[i1] += d[0] * seed;
+                }
+            }
+          }
+        }
+      }
+    }
+    free(w); free(wb); free(dp);
+  }
+  return err;
+}
+
+int sxo_sp_forward(const sxo_tape* t, long n, const uint64_t* const* arg,
+                   uint64_t* const* res, int nthreads) {
+  int err = 0;
+#pragma omp parallel num_threads(nthreads > 0 ? nthreads : 1)
+  {
+    uint64_t* w = (uint64_t*)malloc(sizeof(uint64_t) * (t->sz_w > 0 ? t->sz_w : 1));
+    if (!w) {
+#pragma omp atomic write
+      err = 1;
+    } else {
+#pragma omp for schedule(static)
+      for (long i = 0; i < n; ++i) {
+        for (int k = 0; k < t->n_instr; ++k) {
+          int op = t->op[k], i0 = t->i0[k], i1 = t->i1[k], i2 = t->i2[k];
+          switch (op) {
+            case SXO_CONST: case SXO_PARAMETER: w[i0] = 0; break;
+            case SXO_INPUT: w[i0] = arg[i1] ? arg[i1][(long)i2 * n + i] : 0; break;
+            case SXO_OUTPUT: if (res[i0]) res[i0][(long)i2 * n + i] = w[i1]; break;
+            default: w[i0] = w[i1] | w[i2];
+          }
+        }
+      }
+    }
+    free(w);
+  }
+  return err;
+}
+
+int sxo_sp_reverse(const sxo_tape* t, long n, uint64_t* const* arg, uint64_t* const* res,
+                   int nthreads) {
+  int err = 0;
+#pragma omp parallel num_threads(nthreads > 0 ? nthreads : 1)
+  {
+    uint64_t* w = (uint64_t*)malloc(sizeof(uint64_t) * (t->sz_w > 0 ? t->sz_w : 1));
+    if (!w) {
+#pragma omp atomic write
+      err = 1;
+    } else {
+#pragma omp for schedule(static)
+      for (long i = 0; i < n; ++i) {
+        for (int s = 0; s < t->sz_w; ++s) w[s] = 0;
+        for (int k = t->n_instr - 1; k >= 0; --k) {
+          int op = t->op[k], i0 = t->i0[k], i1 = t->i1[k], i2 = t->i2[k];
+          uint64_t seed;
+          switch (op) {
+            case SXO_CONST: case SXO_PARAMETER: w[i0] = 0; break;
+            case SXO_INPUT:
+              if (arg[i1]) arg[i1][(long)i2 * n + i] |= w[i0];
+              w[i0] = 0;
+              break;
+            case SXO_OUTPUT:
+              if (res[i0]) {
+                w[i1] |= res[i0][(long)i2 * n + i];
+                res[i0][(long)i2 * n + i] = 0;
+              }
+              break;
+            default:
+              seed = w[i0]; w[i0] = 0;
+              w[i1] |= seed;
+              w[i2] |= seed;
+          }
+        }
+      }
+    }
+    free(w);
+  }
+  return err;
+}

@@ -1,0 +1,321 @@
+"""GPU parity of the tape sweeps, through the C ABI, against the golden fixtures (reference op
+semantics) and the oracle on the same seeded inputs.
+
+Bars: bit-exact for sparsity and for tapes of +,-,*,/,sqrt; relative error <= 1e-13 where
+libm transcendentals are involved (helpers.RTOL)."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from casadi_gb300 import calculus as C
+from casadi_gb300 import sx as S
+from casadi_gb300 import workloads as W
+from casadi_gb300.runtime import CudaMap, CudaTape, CasadiGpuError
+
+from helpers import (EXACT_OPS, assert_bitexact, assert_close, golden_list, golden_tape,
+                     load_npz)
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+NTHREADS = os.cpu_count() or 1
+
+
+def dev(arrs, dtype=None):
+    out = []
+    for a in arrs:
+        if a is None:
+            out.append(None)
+        else:
+            t = torch.from_numpy(np.ascontiguousarray(a))
+            out.append(t.cuda() if dtype is None else t.to(dtype).cuda())
+    return out
+
+
+def host(ts):
+    torch.cuda.synchronize()
+    return [t.cpu().numpy() for t in ts]
+
+
+def u64_to_i64(a):
+    return np.ascontiguousarray(a, np.uint64).view(np.int64)
+
+
+# ---- golden fixtures (reference op semantics) ------------------------------------------------
+@pytest.mark.parametrize("name", ["cartpole", "rollout", "dag"])
+def test_golden_eval_forward_reverse(gpu_lib, name):
+    z = load_npz("tapes.npz")
+    t = golden_tape(z, name)
+    ct = CudaTape(t)
+    args = golden_list(z, name, "arg", len(t.nnz_in))
+    res = host(ct.eval(dev(args)))
+    ct.sync()
+    for j, r in enumerate(golden_list(z, name, "res", len(t.nnz_out))):
+        assert_close(res[j], r, "%s eval res%d" % (name, j))
+    fseeds = golden_list(z, name, "fseed", len(t.nnz_in))
+    res2, fsens = ct.forward(dev(args), dev(fseeds))
+    res2, fsens = host(res2), host(fsens)
+    for j, r in enumerate(golden_list(z, name, "fsens", len(t.nnz_out))):
+        assert_close(fsens[j], r, "%s fsens%d" % (name, j))
+    aseeds = golden_list(z, name, "aseed", len(t.nnz_out))
+    res3, asens = ct.reverse(dev(args), dev(aseeds))
+    res3, asens = host(res3), host(asens)
+    for j, r in enumerate(golden_list(z, name, "asens", len(t.nnz_in))):
+        assert_close(asens[j], r, "%s asens%d" % (name, j))
+    # the value outputs of all three sweeps are the same numbers
+    for a, b, c in zip(res, res2, res3):
+        assert_bitexact(a, b, "eval vs forward values")
+        assert_bitexact(a, c, "eval vs reverse values")
+    ct.sync()
+
+
+# ---- every op, value and both partials, over the golden grid ---------------------------------
+def _single_op_tape(op):
+    binary = op in C.BINARY_OPS
+    ops = [C.OP_INPUT, C.OP_INPUT, op, C.OP_OUTPUT]
+    i0 = [0, 1, 2, 0]
+    i1 = [0, 1, 0, 2]
+    i2 = [0, 0, 1 if binary else 0, 0]
+    return S.Tape(ops, i0, i1, i2, [0.0] * 4, [1, 1], [1], 3)
+
+
+def test_ops_grid_values_and_partials(gpu_lib):
+    z = load_npz("ops.npz")
+    for op in sorted(set(z["op"].tolist())):
+        m = z["op"] == op
+        x, y = z["x"][m][None, :], z["y"][m][None, :]
+        ct = CudaTape(_single_op_tape(op))
+        f = host(ct.eval(dev([x, y])))[0][0]
+        name = C.OP_NAMES[op]
+        if op in EXACT_OPS:
+            assert_bitexact(f, z["f"][m], name + " value")
+        else:
+            assert_close(f, z["f"][m], name + " value", floor=1e-300)
+        # adjoint seed 1 on the output gives d0 on x and d1 on y (0 + d*1)
+        n = x.shape[1]
+        _, asens = ct.reverse(dev([x, y]), dev([np.ones((1, 1, n))]))
+        ax, ay = host(asens)
+        d1 = z["d1"][m]
+        if op == C.OP_IF_ELSE_ZERO:
+            # the adjoint rule is if_else_zero(d1, seed), not d1*seed (sx_function.cpp:1470-1474)
+            d1 = np.where(d1 == 0, 0.0, 1.0)
+        for got, ref, what in ((ax[0, 0], z["d0"][m], "d0"), (ay[0, 0], d1, "d1")):
+            ref = ref + 0.0  # 0 + d: the sweep accumulates into a zero adjoint
+            if op in EXACT_OPS:
+                assert_bitexact(got, ref, "%s %s" % (name, what))
+            else:
+                assert_close(got, ref, "%s %s" % (name, what), floor=1e-300)
+        ct.sync()
+
+
+# ---- bit-exact on +,-,*,/,sqrt tapes -----------------------------------------------------------
+def _arith_dag(n_in=24, n_nodes=3000, n_out=8, seed=11):
+    rng = np.random.default_rng(seed)
+    xs = S.sym("x", n_in)
+    nodes = list(xs)
+    for k in range(n_in, n_nodes):
+        a = nodes[int(rng.integers(max(0, k - 128), k))]
+        b = nodes[int(rng.integers(max(0, k - 128), k))]
+        r = rng.random()
+        if r < 0.3:
+            e = a + b
+        elif r < 0.5:
+            e = a - b
+        elif r < 0.8:
+            e = a * b * 0.5
+        elif r < 0.9:
+            e = a / (b * b + 1.0)
+        else:
+            e = S.sqrt(a * a + 1.0)
+        nodes.append(e)
+    return S.Function("A", [xs], [nodes[-n_out:]])
+
+
+def test_arithmetic_tape_bitexact(gpu_lib):
+    f = _arith_dag()
+    t = f.tape
+    assert set(C.OP_NAMES[o] for o in np.unique(t.op)) <= {
+        "ADD", "SUB", "MUL", "DIV", "SQRT", "SQ", "TWICE", "CONST", "INPUT", "OUTPUT", "NEG"}
+    n = 3001
+    rng = np.random.default_rng(0)
+    args = [rng.uniform(-1, 1, (24, n))]
+    ct = CudaTape(t)
+    got = host(ct.eval(dev(args)))
+    want = O.eval(t, args, n, NTHREADS)
+    assert_bitexact(got[0], want[0], "eval")
+    fseeds = [rng.standard_normal((3, 24, n))]
+    _, fs = ct.forward(dev(args), dev(fseeds))
+    _, wfs = O.forward(t, args, fseeds, n, NTHREADS)
+    assert_bitexact(host(fs)[0], wfs[0], "forward")
+    aseeds = [rng.standard_normal((2, 8, n))]
+    _, asn = ct.reverse(dev(args), dev(aseeds))
+    _, was = O.reverse(t, args, aseeds, n, NTHREADS)
+    assert_bitexact(host(asn)[0], was[0], "reverse")
+    ct.sync()
+
+
+# ---- the benchmark workloads against the oracle --------------------------------------------
+def test_cartpole_full_size(gpu_lib):
+    f = W.cartpole_step()
+    n = 65536
+    args = W.cartpole_inputs(n, steps=1, seed=0)
+    ct = CudaTape(f)
+    got = host(ct.eval(dev(args)))
+    want = O.eval(f.tape, args, n, NTHREADS)
+    assert_close(got[0], want[0], "cartpole eval N=65536")
+    ct.sync()
+
+
+def test_rollout_jacobian_and_adjoint(gpu_lib):
+    F = W.cartpole_rollout(20)
+    n = 8192
+    args = W.cartpole_inputs(n, steps=20, seed=3)
+    ct = CudaTape(F)
+    # forward Jacobian of xN: 24 identity seed directions over (x0, U)
+    eye = np.eye(24)
+    fseeds = [np.repeat(eye[:, :4, None], n, axis=2), np.repeat(eye[:, 4:, None], n, axis=2)]
+    res, fsens = ct.forward(dev(args), dev(fseeds))
+    res, fsens = host(res), host(fsens)
+    wres, wfsens = O.forward(F.tape, args, fseeds, n, NTHREADS)
+    assert_close(res[0], wres[0], "xN")
+    assert_close(fsens[0], wfsens[0], "d xN / d (x0,U)")
+    # adjoint of cost
+    aseeds = [np.zeros((1, 4, n)), np.ones((1, 1, n))]
+    _, asens = ct.reverse(dev(args), dev(aseeds))
+    asens = host(asens)
+    _, wasens = O.reverse(F.tape, args, aseeds, n, NTHREADS)
+    assert_close(asens[0], wasens[0], "d cost / d x0")
+    assert_close(asens[1], wasens[1], "d cost / d U")
+    # the adjoint agrees with the forward Jacobian of the cost output row
+    jac_cost = np.concatenate([fsens[1][:, 0, :]], axis=0)  # (24, n)
+    adj = np.concatenate([asens[0][0], asens[1][0]], axis=0)  # (24, n)
+    assert_close(adj, jac_cost, "adjoint vs forward", rtol=1e-12)
+    # and central finite differences (h = 1e-6) on a few instances
+    h = 1e-6
+    m = 16
+    sub = [a[:, :m].copy() for a in args]
+    fd = np.zeros((24, m))
+    for k in range(24):
+        p = [a.copy() for a in sub]
+        q = [a.copy() for a in sub]
+        blk, row = (0, k) if k < 4 else (1, k - 4)
+        p[blk][row] += h
+        q[blk][row] -= h
+        fd[k] = (O.eval(F.tape, p, m)[1][0] - O.eval(F.tape, q, m)[1][0]) / (2 * h)
+    assert np.max(np.abs(fd - adj[:, :m]) / np.maximum(np.abs(adj[:, :m]), 1.0)) < 1e-5
+    ct.sync()
+
+
+def test_dag_full_size_eval_and_adjoint(gpu_lib):
+    G = W.random_dag()
+    n = 2048
+    args = W.dag_inputs(n)
+    ct = CudaTape(G)
+    got = host(ct.eval(dev(args)))
+    want = O.eval(G.tape, args, n, NTHREADS)
+    assert_close(got[0], want[0], "dag eval")
+    aseeds = [np.ones((1, 16, n))]
+    _, asens = ct.reverse(dev(args), dev(aseeds))
+    _, wasens = O.reverse(G.tape, args, aseeds, n, NTHREADS)
+    assert_close(host(asens)[0], wasens[0], "dag adjoint of sum of outputs")
+    ct.sync()
+
+
+# ---- sparsity (bit-exact) -----------------------------------------------------------------------
+def test_sparsity_sweeps_bitexact(gpu_lib):
+    G = W.random_dag()
+    t = G.tape
+    n = 777
+    rng = np.random.default_rng(5)
+    bits = rng.integers(0, 2**63, size=(64, n), dtype=np.int64).view(np.uint64)
+    bits &= rng.integers(0, 2**63, size=(64, n), dtype=np.int64).view(np.uint64)
+    ct = CudaTape(t)
+    got = host(ct.sp_forward(dev([u64_to_i64(bits)])))[0].view(np.uint64)
+    want = O.sp_forward(t, [bits], n)[0]
+    assert np.array_equal(got, want)
+    arg0 = rng.integers(0, 2**63, size=(64, n), dtype=np.int64).view(np.uint64) & np.uint64(0xff)
+    seeds = rng.integers(0, 2**63, size=(16, n), dtype=np.int64).view(np.uint64)
+    a_dev, r_dev = dev([u64_to_i64(arg0)]), dev([u64_to_i64(seeds)])
+    ct.sp_reverse(a_dev, r_dev)
+    ga, gr = host(a_dev)[0].view(np.uint64), host(r_dev)[0].view(np.uint64)
+    wa, wr = [arg0.copy()], [seeds.copy()]
+    O.sp_reverse(t, wa, wr, n)
+    assert np.array_equal(ga, wa[0]) and np.array_equal(gr, wr[0])
+    assert (gr == 0).all()
+    ct.sync()
+
+
+# ---- edge cases ----------------------------------------------------------------------------------
+def test_edge_sizes_null_io_and_waves(gpu_lib):
+    F = W.cartpole_rollout(4)
+    t = F.tape
+    ct = CudaTape(F)
+    for n in (1, 2, 31, 33, 1000):
+        args = W.cartpole_inputs(n, steps=4, seed=n)
+        got = host(ct.eval(dev(args)))
+        want = O.eval(t, args, n)
+        for g, w in zip(got, want):
+            assert_close(g, w, "n=%d" % n)
+    # n = 0 is a no-op
+    e = torch.empty((4, 0), dtype=torch.float64, device="cuda")
+    ct.eval([e, torch.empty((4, 0), dtype=torch.float64, device="cuda")], n=0)
+    # null input reads zeros, null output is skipped
+    n = 50
+    args = W.cartpole_inputs(n, steps=4, seed=1)
+    res = ct.eval(dev([args[0], None]), n=n, res=[torch.zeros((4, n), dtype=torch.float64,
+                                                             device="cuda"), None])
+    want = O.eval(t, [args[0], None], n)
+    assert_close(host([res[0]])[0], want[0], "null input")
+    # adjoint in several waves (scratch limited to ~3 warps of instances) == one wave
+    n = 1000
+    args = W.cartpole_inputs(n, steps=4, seed=2)
+    aseeds = [np.random.default_rng(0).standard_normal((3, 4, n)), np.ones((3, 1, n))]
+    _, one = ct.reverse(dev(args), dev(aseeds))
+    one = host(one)
+    ct2 = CudaTape(F)
+    _, many = ct2.reverse(dev(args), dev(aseeds), scratch_limit=8 * ct2.n_partials * 96)
+    many = host(many)
+    for a, b in zip(one, many):
+        assert_bitexact(a, b, "waves")
+    # forward with a direction count that is not a multiple of the CTA direction width
+    fseeds = [np.random.default_rng(1).standard_normal((5, 4, n)),
+              np.random.default_rng(2).standard_normal((5, 4, n))]
+    _, fs = ct.forward(dev(args), dev(fseeds))
+    _, wfs = O.forward(t, args, fseeds, n)
+    for g, w in zip(host(fs), wfs):
+        assert_close(g, w, "nfwd=5")
+    ct.sync()
+    ct2.sync()
+
+
+def test_scratch_too_small_is_an_error(gpu_lib):
+    F = W.cartpole_rollout(2)
+    ct = CudaTape(F)
+    args = dev(W.cartpole_inputs(64, steps=2))
+    sc = torch.empty(16, dtype=torch.uint8, device="cuda")
+    import ctypes as ct_
+    from casadi_gb300 import runtime as R
+    aseeds = dev([np.ones((1, 4, 64)), np.ones((1, 1, 64))])
+    asens = [torch.empty((1, k, 64), dtype=torch.float64, device="cuda") for k in (4, 2)]
+    st = R.load().casadi_gb300_reverse(ct.id, 64, 64, 1, R._ptr_array(args), R._ptr_array(
+        [torch.empty((k, 64), dtype=torch.float64, device="cuda") for k in (4, 1)]),
+        R._ptr_array(aseeds), R._ptr_array(asens), ct_.c_void_p(sc.data_ptr()), 16, None)
+    assert st == -5
+    assert "scratch" in R.load().casadi_gb300_last_error().decode()
+
+
+# ---- host-buffer Map path --------------------------------------------------------------------------
+def test_map_eval_and_reverse_host_buffers(gpu_lib):
+    f = W.cartpole_step()
+    n = 4099
+    x, u = W.cartpole_inputs(n, steps=1, seed=9)
+    F = CudaMap(f, n)
+    out = F(x.T.copy(), u.T.copy())[0]          # instance-major (n, 4)
+    want = O.eval(f.tape, [x, u], n)[0]          # instance-minor (4, n)
+    assert_close(out.T, want, "map eval")
+    aseed = np.random.default_rng(3).standard_normal((n, 2, 4))
+    res, asens = F.reverse([x.T.copy(), u.T.copy()], [aseed])
+    _, wasens = O.reverse(f.tape, [x, u], [np.transpose(aseed, (1, 2, 0))], n)
+    assert_close(np.transpose(asens[0], (1, 2, 0)), wasens[0], "map reverse x")
+    assert_close(np.transpose(asens[1], (1, 2, 0)), wasens[1], "map reverse u")

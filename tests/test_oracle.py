@@ -1,0 +1,120 @@
+"""The oracle (plain-C restatement of the SX VM) checked against the golden fixtures that the
+reference's own op semantics produced, and, where the reference harness is built, directly
+against it. These pin the oracle before it is trusted as the GPU parity checker."""
+import math
+
+import numpy as np
+import pytest
+
+import oracle as O
+from casadi_gb300 import calculus as C
+
+from helpers import (EXACT_OPS, RTOL, assert_bitexact, assert_close, golden_list, golden_tape,
+                     load_npz, same_bits)
+
+
+def test_enum_ids_match_reference():
+    z = load_npz("enum.npz")
+    by_name = {v: k for k, v in C.OP_NAMES.items()}
+    for name, rid in zip(z["names"], z["ids"]):
+        assert by_name[str(name)] == int(rid), name
+
+
+def _grid_eval(fun, der):
+    z = load_npz("ops.npz")
+    f = np.array([fun(int(o), x, y) for o, x, y in zip(z["op"], z["x"], z["y"])])
+    d = np.array([der(int(o), x, y, fr) for o, x, y, fr in zip(z["op"], z["x"], z["y"], z["f"])])
+    return z, f, d
+
+
+def test_oracle_ops_vs_golden():
+    z, f, d = _grid_eval(O.fun, O.der)
+    exact = np.isin(z["op"], list(EXACT_OPS))
+    assert_bitexact(f[exact], z["f"][exact], "exact-op values")
+    assert_bitexact(d[exact, 0], z["d0"][exact], "exact-op d0")
+    assert_bitexact(d[exact, 1], z["d1"][exact], "exact-op d1")
+    # transcendentals: the oracle calls the host libm; allow a few ulp between libm builds
+    for op in sorted(set(z["op"].tolist()) - EXACT_OPS):
+        m = z["op"] == op
+        for got, ref, what in ((f[m], z["f"][m], "f"), (d[m, 0], z["d0"][m], "d0"),
+                               (d[m, 1], z["d1"][m], "d1")):
+            assert_close(got, ref, "%s %s" % (C.OP_NAMES[op], what), rtol=4e-16 * 8,
+                         floor=1e-300)
+
+
+def test_python_folding_vs_golden():
+    z = load_npz("ops.npz")
+    f = np.array([C.fun(int(o), x, y) for o, x, y in zip(z["op"], z["x"], z["y"])])
+    exact = np.isin(z["op"], list(EXACT_OPS))
+    assert_bitexact(f[exact], z["f"][exact], "folding exact ops")
+    for op in sorted(set(z["op"].tolist()) - EXACT_OPS):
+        m = z["op"] == op
+        assert_close(f[m], z["f"][m], C.OP_NAMES[op], rtol=4e-16 * 8, floor=1e-300)
+
+
+@pytest.mark.parametrize("name", ["cartpole", "rollout", "dag"])
+def test_oracle_tapes_vs_golden(name):
+    z = load_npz("tapes.npz")
+    t = golden_tape(z, name)
+    args = golden_list(z, name, "arg", len(t.nnz_in))
+    n = args[0].shape[-1]
+    res = O.eval(t, args, n)
+    for j, r in enumerate(golden_list(z, name, "res", len(t.nnz_out))):
+        assert_close(res[j], r, "%s res%d" % (name, j))
+    fseeds = golden_list(z, name, "fseed", len(t.nnz_in))
+    _, fsens = O.forward(t, args, fseeds, n)
+    for j, r in enumerate(golden_list(z, name, "fsens", len(t.nnz_out))):
+        assert_close(fsens[j], r, "%s fsens%d" % (name, j))
+    aseeds = golden_list(z, name, "aseed", len(t.nnz_out))
+    _, asens = O.reverse(t, args, aseeds, n)
+    for j, r in enumerate(golden_list(z, name, "asens", len(t.nnz_in))):
+        assert_close(asens[j], r, "%s asens%d" % (name, j))
+
+
+def test_oracle_threads_agree():
+    z = load_npz("tapes.npz")
+    t = golden_tape(z, "rollout")
+    args = golden_list(z, "rollout", "arg", 2)
+    a = O.eval(t, args, args[0].shape[-1], nthreads=1)
+    b = O.eval(t, args, args[0].shape[-1], nthreads=4)
+    for x, y in zip(a, b):
+        assert same_bits(x, y).all()
+
+
+def test_oracle_sparsity_matches_structure():
+    """sp_forward with one bit per input gives exactly the dependency pattern, and
+    sp_reverse with one bit per output gives its transpose (SXFunction::sp_forward/
+    sp_reverse semantics)."""
+    from casadi_gb300 import workloads as W
+    f = W.random_dag(n_in=16, n_nodes=600, n_out=8, seed=5)
+    t = f.tape
+    n = 3
+    bits = np.zeros((16, n), np.uint64)
+    for k in range(16):
+        bits[k, :] = np.uint64(1) << np.uint64(k)
+    fwd = O.sp_forward(t, [bits], n)[0]
+    seeds = np.zeros((8, n), np.uint64)
+    for k in range(8):
+        seeds[k, :] = np.uint64(1) << np.uint64(k)
+    sens = np.zeros((16, n), np.uint64)
+    O.sp_reverse(t, [sens], [seeds], n)
+    assert (seeds == 0).all()  # seeds are consumed
+    for o in range(8):
+        for i in range(16):
+            dep_f = bool(int(fwd[o, 0]) >> i & 1)
+            dep_r = bool(int(sens[i, 0]) >> o & 1)
+            assert dep_f == dep_r
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="reference harness not built on this host")
+def test_oracle_matches_reference_harness_exactly():
+    """On the host where the reference harness is built, the oracle's libm is the reference's
+    libm: every op value and partial must agree bit for bit."""
+    z, f, d = _grid_eval(O.fun, O.der)
+    _, rf, rd = _grid_eval(O.ref_fun, O.ref_der)
+    assert_bitexact(f, rf, "values")
+    assert_bitexact(d, rd, "partials")
+
+
+def test_rtol_is_the_documented_tolerance():
+    assert RTOL == 1e-13 and math.isfinite(RTOL)
