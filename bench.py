@@ -33,25 +33,26 @@ L2_FLUSH_BYTES = 256 << 20
 
 
 # ---- workloads -------------------------------------------------------------------------------
-def make_workload(name):
+def make_workload(name, instances=None):
     from casadi_gb300 import workloads as W
     if name == "rollout20":
         F = W.cartpole_rollout(20)
-        n = 262144
+        n = instances or 262144
         args = W.cartpole_inputs(n, steps=20, seed=0)
-        desc = "cart-pole 20-step RK4 rollout F(x0[4],U[20])->(xN[4],cost), N=262144: " \
-               "forward Jacobian (24 unit directions) + adjoint of cost"
+        desc = "cart-pole 20-step RK4 rollout F(x0[4],U[20])->(xN[4],cost), N=%d: " \
+               "forward Jacobian (24 unit directions) + adjoint of cost" % n
         return F, n, args, [np.zeros((1, 4, n)), np.ones((1, 1, n))], desc
     if name == "cartpole":
         F = W.cartpole_step()
-        n = 65536
+        n = instances or 65536
         args = W.cartpole_inputs(n, steps=1, seed=0)
-        return F, n, args, [np.ones((1, 4, n))], "cart-pole RK4 step, N=65536"
+        return F, n, args, [np.ones((1, 4, n))], "cart-pole RK4 step, N=%d" % n
     if name == "dag":
         F = W.random_dag()
-        n = 16384
+        n = instances or 16384
         args = W.dag_inputs(n)
-        return F, n, args, [np.ones((1, 16, n))], "random DAG 64in/10000 nodes/16out, N=16384"
+        return F, n, args, [np.ones((1, 16, n))], \
+            "random DAG 64in/10000 nodes/16out, N=%d" % n
     raise SystemExit("unknown workload " + name)
 
 
@@ -220,7 +221,7 @@ def run_native(a):
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
-    F, n, args_h, aseeds_h, desc = make_workload(a.workload)
+    F, n, args_h, aseeds_h, desc = make_workload(a.workload, a.instances)
     ct = R.CudaTape(F)
     dargs = [torch.from_numpy(x).cuda() for x in args_h]
     daseeds = [torch.from_numpy(x).cuda() for x in aseeds_h]
@@ -392,7 +393,7 @@ def run_reference(a):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    F, n, args_h, aseeds_h, desc = make_workload(a.workload)
+    F, n, args_h, aseeds_h, desc = make_workload(a.workload, a.instances)
     threads = os.cpu_count() or 1
     # bounded sample per step so that warmup + steps finish within a few minutes
     m = 256
@@ -424,6 +425,8 @@ def main():
     p.add_argument("--impl", default="native", choices=["native", "reference"])
     p.add_argument("--workload", default="rollout20", choices=["rollout20", "cartpole", "dag"])
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    p.add_argument("--instances", type=int, default=None,
+                   help="override the workload's instance count (profiling captures)")
     a = p.parse_args()
     if a.impl == "reference":
         run_reference(a)

@@ -65,19 +65,23 @@ struct Tape {
   int n_instr = 0, n_in = 0, n_out = 0, sz_w = 0, n_partials = 0, n_chunks = 0;
   std::vector<int> nnz_in, nnz_out;
   std::vector<int2> absent_in;
+  std::vector<int> pofs;    // partials recorded before instruction k*kPofsGran
   u64* d_code = nullptr;
+  int* d_pofs = nullptr;
   double* d_consts = nullptr;
   int2* d_absent = nullptr;
   int* d_err = nullptr;
   // launch shapes
   int primal_block = 128, primal_grid_cap = 1;
-  int dir_warps = 4, dir_grid_cap = 1;
+  std::mutex shape_mtx;
+  std::vector<std::pair<int, int>> dir_shape_cache;  // (ndir, packed shape)
 
   ~Tape() {
     int cur = 0;
     cudaGetDevice(&cur);
     if (cur != device) cudaSetDevice(device);
     cudaFree(d_code);
+    cudaFree(d_pofs);
     cudaFree(d_consts);
     cudaFree(d_absent);
     cudaFree(d_err);
@@ -87,6 +91,7 @@ struct Tape {
   TapeView view() const {
     TapeView v;
     v.code = d_code;
+    v.pofs = d_pofs;
     v.consts = d_consts;
     v.absent_in = d_absent;
     v.n_chunks = n_chunks;
@@ -192,20 +197,53 @@ void choose_shapes(Tape& t) {
       t.primal_grid_cap = occ * sms;
     }
   }
-  best_threads = -1;
-  for (int dw : {4, 2, 1}) {
-    const size_t sm = smem_dir(t.sz_w, dw);
-    if (sm > static_cast<size_t>(max_smem)) continue;
-    const int occ = occupancy_dir(sm);
-    // occupancy_dir measures the 4-warp variant; scale for narrower CTAs by shared memory
-    const int occ_dw = dw == 4 ? occ : std::max(occ, static_cast<int>(
-        std::min<size_t>(32, (228u * 1024u) / (sm + 1024u))));
-    if (occ_dw * dw * 32 > best_threads) {
-      best_threads = occ_dw * dw * 32;
-      t.dir_warps = dw;
-      t.dir_grid_cap = occ_dw * sms;
+}
+
+// Shape of a derivative-sweep launch: DW warps (one direction each) per CTA on one 32-instance
+// tile, `ch` instructions per staged chunk. Prefers the configuration with the most resident
+// warps per SM (enough to keep every sub-partition's FP64 unit busy), then the fewest idle
+// direction slots, then the longest chunk.
+struct DirShape {
+  int dw = 1, ch = 16, blocks_per_sm = 1;
+};
+
+DirShape dir_shape(Tape& t, int ndir) {
+  {
+    std::lock_guard<std::mutex> lk(t.shape_mtx);
+    for (auto& e : t.dir_shape_cache)
+      if (e.first == ndir) {
+        DirShape d;
+        d.dw = e.second & 0xff;
+        d.ch = (e.second >> 8) & 0xfff;
+        d.blocks_per_sm = e.second >> 20;
+        return d;
+      }
+  }
+  const int max_smem = max_smem_optin();
+  DirShape best;
+  double best_score = -1;
+  for (int ch : {64, 32, 16}) {
+    for (int dw : {8, 6, 4, 2, 1}) {
+      if (dw > 1 && dw >= 2 * ndir) continue;
+      const size_t sm = smem_dir(t.sz_w, dw, ch);
+      if (sm > static_cast<size_t>(max_smem)) continue;
+      const int occ = occupancy_dir(dw, sm);
+      if (occ <= 0) continue;
+      const int groups = (ndir + dw - 1) / dw;
+      const double used = static_cast<double>(ndir) / (groups * dw);
+      const double warps = std::min(occ * dw, 8);
+      const double score = warps * used * (1.0 + 0.01 * ch);
+      if (score > best_score) {
+        best_score = score;
+        best.dw = dw;
+        best.ch = ch;
+        best.blocks_per_sm = occ;
+      }
     }
   }
+  std::lock_guard<std::mutex> lk(t.shape_mtx);
+  t.dir_shape_cache.emplace_back(ndir, best.dw | (best.ch << 8) | (best.blocks_per_sm << 20));
+  return best;
 }
 
 bool fits_smem(int sz_w) {
@@ -257,44 +295,47 @@ long long wave_capacity(const Tape& t, long long n, size_t bytes) {
   return std::min<long long>(w, ((n + 31) / 32) * 32);
 }
 
-int run_record_waves(Tape& t, long long n, long long ld, int ndir, bool adjoint,
-                     void* const* arg, void* const* res, void* const* seed, void* const* sens,
-                     void* scratch, size_t scratch_bytes, cudaStream_t s,
-                     bool identity = false) {
+// Values + partials (record sweep) followed by the derivative sweep, in waves of as many
+// instances as the scratch holds. `in/out/seed/sens` address the whole instance range.
+int run_ad(Tape& t, long long n, const IoDesc* in, const IoDesc* out, const IoDesc* seed,
+           const IoDesc* sens, int ndir, bool adjoint, bool identity, void* scratch,
+           size_t scratch_bytes, cudaStream_t s) {
   if (n == 0) return 0;
   const long long cap = wave_capacity(t, n, scratch_bytes);
   if (t.n_partials > 0 && (scratch == nullptr || cap < 32))
     return fail(CASADI_GB300_ERR_SCRATCH,
                 "scratch of %zu bytes is below the minimum of %lld bytes for this tape",
                 scratch_bytes, 32ll * 8ll * t.n_partials);
+  const DirShape ds = dir_shape(t, std::max(ndir, 1));
+  const int groups = (ndir + ds.dw - 1) / ds.dw;
+  const int sms = sm_count();
   for (long long i0 = 0; i0 < n; i0 += cap) {
     const long long m = std::min(cap, n - i0);
     SweepArgs a = base_args(t, m, i0);
     a.partials = static_cast<double*>(scratch);
-    a.pt_stride = cap;
+    a.pofs = t.d_pofs;
+    a.n_code = t.n_chunks * kChunk;
     a.ndir = ndir;
     a.identity_seed = identity ? 1 : 0;
     for (int j = 0, off = 0; j < t.n_in; off += t.nnz_in[j], ++j) a.in_off[j] = off;
-    fill_io(a.in, t.n_in, arg, t.nnz_in, ld, false);
-    fill_io(a.out, t.n_out, res, t.nnz_out, ld, false);
+    std::memcpy(a.in, in, sizeof(IoDesc) * t.n_in);
+    std::memcpy(a.out, out, sizeof(IoDesc) * t.n_out);
     a.block = t.primal_block;
     cudaError_t e = timed(F_RECORD, s, [&] {
       return launch_record(a, grid_for((m + a.block - 1) / a.block, t.primal_grid_cap), s);
     });
     if (e != cudaSuccess) return cuda_fail(e, "record sweep launch");
     if (ndir > 0) {
-      if (adjoint) {
-        fill_io(a.seed, t.n_out, seed, t.nnz_out, ld, true);
-        fill_io(a.sens, t.n_in, sens, t.nnz_in, ld, true);
-      } else {
-        fill_io(a.seed, t.n_in, seed, t.nnz_in, ld, true);
-        fill_io(a.sens, t.n_out, sens, t.nnz_out, ld, true);
-      }
-      a.block = 32 * t.dir_warps;
-      const int gy = (ndir + t.dir_warps - 1) / t.dir_warps;
-      const int gx = grid_for((m + 31) / 32, std::max(1, t.dir_grid_cap / gy));
+      std::memcpy(a.seed, seed, sizeof(IoDesc) * (adjoint ? t.n_out : t.n_in));
+      std::memcpy(a.sens, sens, sizeof(IoDesc) * (adjoint ? t.n_in : t.n_out));
+      a.block = 32 * ds.dw;
+      a.chunk = ds.ch;
+      const long long tiles = (m + 31) / 32;
+      const long long per_group = std::max<long long>(
+          1, std::min<long long>(tiles, static_cast<long long>(sms) * ds.blocks_per_sm / groups));
+      const int grid = static_cast<int>(per_group * groups);
       e = timed(adjoint ? F_ADJOINT : F_TANGENT, s, [&] {
-        return adjoint ? launch_adjoint(a, gx, gy, s) : launch_tangent(a, gx, gy, s);
+        return adjoint ? launch_adjoint(a, grid, s) : launch_tangent(a, grid, s);
       });
       if (e != cudaSuccess) return cuda_fail(e, "derivative sweep launch");
     }
@@ -407,6 +448,14 @@ int casadi_gb300_tape_create(const casadi_gb300_atomic* alg, int n_instr, int n_
   t->n_partials = static_cast<int>(n_partials);
   t->n_chunks = std::max(1, (n_instr + kChunk - 1) / kChunk);
   code.resize(static_cast<size_t>(t->n_chunks) * kChunk, enc(D_NOP, 0, 0, 0));
+  t->pofs.assign(code.size() / kPofsGran + 1, 0);
+  for (size_t k = 0, acc = 0; k < code.size(); ++k) {
+    if (k % kPofsGran == 0) t->pofs[k / kPofsGran] = static_cast<int>(acc);
+    const unsigned op = dec_op(code[k]);
+    if (op != D_CONST && op != D_INPUT && op != D_OUTPUT && op != D_NOP)
+      acc += __builtin_popcount(partial_mask(op));
+    if (k + 1 == code.size()) t->pofs[code.size() / kPofsGran] = static_cast<int>(acc);
+  }
   if (consts.empty()) consts.push_back(0.0);
 
   cudaError_t e = cudaGetDevice(&t->device);
@@ -419,6 +468,11 @@ int casadi_gb300_tape_create(const casadi_gb300_atomic* alg, int n_instr, int n_
       cudaSuccess)
     return cuda_fail(e, "cudaMalloc(absent)");
   if ((e = cudaMalloc(&t->d_err, sizeof(int))) != cudaSuccess) return cuda_fail(e, "cudaMalloc(err)");
+  if ((e = cudaMalloc(&t->d_pofs, t->pofs.size() * sizeof(int))) != cudaSuccess)
+    return cuda_fail(e, "cudaMalloc(pofs)");
+  if ((e = cudaMemcpy(t->d_pofs, t->pofs.data(), t->pofs.size() * sizeof(int),
+                      cudaMemcpyHostToDevice)) != cudaSuccess)
+    return cuda_fail(e, "upload partial offsets");
   if ((e = cudaMemcpy(t->d_code, code.data(), code.size() * sizeof(u64), cudaMemcpyHostToDevice)) !=
       cudaSuccess)
     return cuda_fail(e, "upload code");
@@ -500,11 +554,13 @@ int casadi_gb300_forward(int id, int64_t n, int64_t ld, int nfwd, const double* 
   if (int rc = check_device(*t)) return rc;
   if (int rc = check_n(n, ld)) return rc;
   if (nfwd < 0 || nfwd > 65535) return fail(CASADI_GB300_ERR_ARG, "bad direction count %d", nfwd);
-  return run_record_waves(*t, n, ld, nfwd, false, vptrs(arg),
-                          vptrs(res),
-                          vptrs(fseed),
-                          vptrs(fsens), scratch, scratch_bytes,
-                          static_cast<cudaStream_t>(stream));
+  IoDesc in[kMaxIo], out[kMaxIo], seed[kMaxIo], sens[kMaxIo];
+  fill_io(in, t->n_in, vptrs(arg), t->nnz_in, ld, false);
+  fill_io(out, t->n_out, vptrs(res), t->nnz_out, ld, false);
+  fill_io(seed, t->n_in, vptrs(fseed), t->nnz_in, ld, true);
+  fill_io(sens, t->n_out, vptrs(fsens), t->nnz_out, ld, true);
+  return run_ad(*t, n, in, out, seed, sens, nfwd, false, false, scratch, scratch_bytes,
+                static_cast<cudaStream_t>(stream));
 }
 
 int casadi_gb300_reverse(int id, int64_t n, int64_t ld, int nadj, const double* const* arg,
@@ -515,11 +571,13 @@ int casadi_gb300_reverse(int id, int64_t n, int64_t ld, int nadj, const double* 
   if (int rc = check_device(*t)) return rc;
   if (int rc = check_n(n, ld)) return rc;
   if (nadj < 0 || nadj > 65535) return fail(CASADI_GB300_ERR_ARG, "bad direction count %d", nadj);
-  return run_record_waves(*t, n, ld, nadj, true, vptrs(arg),
-                          vptrs(res),
-                          vptrs(aseed),
-                          vptrs(asens), scratch, scratch_bytes,
-                          static_cast<cudaStream_t>(stream));
+  IoDesc in[kMaxIo], out[kMaxIo], seed[kMaxIo], sens[kMaxIo];
+  fill_io(in, t->n_in, vptrs(arg), t->nnz_in, ld, false);
+  fill_io(out, t->n_out, vptrs(res), t->nnz_out, ld, false);
+  fill_io(seed, t->n_out, vptrs(aseed), t->nnz_out, ld, true);
+  fill_io(sens, t->n_in, vptrs(asens), t->nnz_in, ld, true);
+  return run_ad(*t, n, in, out, seed, sens, nadj, true, false, scratch, scratch_bytes,
+                static_cast<cudaStream_t>(stream));
 }
 
 int casadi_gb300_jacobian(int id, int64_t n, int64_t ld, const double* const* arg,
@@ -532,8 +590,13 @@ int casadi_gb300_jacobian(int id, int64_t n, int64_t ld, const double* const* ar
   int nz = 0;
   for (int v : t->nnz_in) nz += v;
   if (nz == 0) return fail(CASADI_GB300_ERR_ARG, "tape has no input nonzeros");
-  return run_record_waves(*t, n, ld, nz, false, vptrs(arg), vptrs(res), nullptr, vptrs(jac),
-                          scratch, scratch_bytes, static_cast<cudaStream_t>(stream), true);
+  IoDesc in[kMaxIo], out[kMaxIo], seed[kMaxIo], sens[kMaxIo];
+  fill_io(in, t->n_in, vptrs(arg), t->nnz_in, ld, false);
+  fill_io(out, t->n_out, vptrs(res), t->nnz_out, ld, false);
+  fill_io(seed, t->n_in, nullptr, t->nnz_in, ld, true);
+  fill_io(sens, t->n_out, vptrs(jac), t->nnz_out, ld, true);
+  return run_ad(*t, n, in, out, seed, sens, nz, false, true, scratch, scratch_bytes,
+                static_cast<cudaStream_t>(stream));
 }
 
 int casadi_gb300_profile(int enable) {
@@ -682,6 +745,21 @@ static int fetch_blocks(const IoDesc* desc, int count, const std::vector<int>& n
   return 0;
 }
 
+// Partials scratch of a memory object for the host-buffer AD paths; waves keep it <= 8 GiB.
+static int map_scratch(const Tape& t, Mem& m, long long n, void** scratch, size_t* bytes) {
+  *scratch = nullptr;
+  *bytes = 0;
+  if (t.n_partials == 0) return 0;
+  size_t need = 8ull * t.n_partials * static_cast<size_t>(((n + 31) / 32) * 32);
+  const size_t kMaxScratch = 8ull << 30;
+  need = std::min(need, std::max<size_t>(kMaxScratch, 8ull * 32 * t.n_partials));
+  cudaError_t e = cudaSuccess;
+  *scratch = m.buf(4 * kMaxIo, need, &e);
+  if (!*scratch) return cuda_fail(e, "cudaMalloc(scratch)");
+  *bytes = need;
+  return 0;
+}
+
 int casadi_gb300_map_eval(int id, int mem, int64_t n, const double* const* arg,
                           double* const* res) {
   Tape* t = get_tape(id);
@@ -727,35 +805,12 @@ int casadi_gb300_map_jacobian(int id, int mem, int64_t n, const double* const* a
   if (int rc = stage_blocks(*m, 3 * kMaxIo, t->n_out, t->nnz_out, nz, n,
                             reinterpret_cast<const double* const*>(jac), false, sens, s))
     return rc;
-  size_t need = 8ull * t->n_partials * static_cast<size_t>(((n + 31) / 32) * 32);
-  const size_t kMaxScratch = 8ull << 30;
-  need = std::min(need, std::max<size_t>(kMaxScratch, 8ull * 32 * t->n_partials));
-  cudaError_t e = cudaSuccess;
-  void* scratch = t->n_partials ? m->buf(4 * kMaxIo, need, &e) : nullptr;
-  if (t->n_partials && !scratch) return cuda_fail(e, "cudaMalloc(scratch)");
-  const long long cap = wave_capacity(*t, n, need);
-  for (long long i0 = 0; i0 < n; i0 += cap) {
-    const long long mcount = std::min(cap, n - i0);
-    SweepArgs a = base_args(*t, mcount, i0);
-    std::memcpy(a.in, in, sizeof(in));
-    std::memcpy(a.out, out, sizeof(out));
-    std::memcpy(a.sens, sens, sizeof(sens));
-    for (int j = 0, off = 0; j < t->n_in; off += t->nnz_in[j], ++j) a.in_off[j] = off;
-    a.identity_seed = 1;
-    a.partials = static_cast<double*>(scratch);
-    a.pt_stride = cap;
-    a.ndir = nz;
-    a.block = t->primal_block;
-    e = timed(F_RECORD, s, [&] {
-      return launch_record(a, grid_for((mcount + a.block - 1) / a.block, t->primal_grid_cap), s);
-    });
-    if (e != cudaSuccess) return cuda_fail(e, "record sweep launch");
-    a.block = 32 * t->dir_warps;
-    const int gy = (nz + t->dir_warps - 1) / t->dir_warps;
-    const int gx = grid_for((mcount + 31) / 32, std::max(1, t->dir_grid_cap / gy));
-    e = timed(F_TANGENT, s, [&] { return launch_tangent(a, gx, gy, s); });
-    if (e != cudaSuccess) return cuda_fail(e, "tangent launch");
-  }
+  void* scratch = nullptr;
+  size_t bytes = 0;
+  if (int rc = map_scratch(*t, *m, n, &scratch, &bytes)) return rc;
+  IoDesc seed[kMaxIo];
+  std::memset(seed, 0, sizeof(seed));
+  if (int rc = run_ad(*t, n, in, out, seed, sens, nz, false, true, scratch, bytes, s)) return rc;
   if (int rc = fetch_blocks(out, t->n_out, t->nnz_out, 1, n, res, s)) return rc;
   if (int rc = fetch_blocks(sens, t->n_out, t->nnz_out, nz, n, jac, s)) return rc;
   return casadi_gb300_sync(id, s);
@@ -782,34 +837,10 @@ int casadi_gb300_map_reverse(int id, int mem, int64_t n, int nadj, const double*
   if (int rc = stage_blocks(*m, 3 * kMaxIo, t->n_in, t->nnz_in, nadj, n,
                             reinterpret_cast<const double* const*>(asens), false, sens, s))
     return rc;
-  size_t need = 8ull * t->n_partials * static_cast<size_t>(((n + 31) / 32) * 32);
-  const size_t kMaxScratch = 8ull << 30;  // waves keep the partials scratch below 8 GiB
-  need = std::min(need, std::max<size_t>(kMaxScratch, 8ull * 32 * t->n_partials));
-  cudaError_t e = cudaSuccess;
-  void* scratch = t->n_partials ? m->buf(4 * kMaxIo, need, &e) : nullptr;
-  if (t->n_partials && !scratch) return cuda_fail(e, "cudaMalloc(scratch)");
-  const long long cap = wave_capacity(*t, n, need);
-  for (long long i0 = 0; i0 < n; i0 += cap) {
-    const long long mcount = std::min(cap, n - i0);
-    SweepArgs a = base_args(*t, mcount, i0);
-    std::memcpy(a.in, in, sizeof(in));
-    std::memcpy(a.out, out, sizeof(out));
-    std::memcpy(a.seed, seed, sizeof(seed));
-    std::memcpy(a.sens, sens, sizeof(sens));
-    a.partials = static_cast<double*>(scratch);
-    a.pt_stride = cap;
-    a.ndir = nadj;
-    a.block = t->primal_block;
-    e = timed(F_RECORD, s, [&] {
-      return launch_record(a, grid_for((mcount + a.block - 1) / a.block, t->primal_grid_cap), s);
-    });
-    if (e != cudaSuccess) return cuda_fail(e, "record sweep launch");
-    a.block = 32 * t->dir_warps;
-    const int gy = (nadj + t->dir_warps - 1) / t->dir_warps;
-    const int gx = grid_for((mcount + 31) / 32, std::max(1, t->dir_grid_cap / gy));
-    e = timed(F_ADJOINT, s, [&] { return launch_adjoint(a, gx, gy, s); });
-    if (e != cudaSuccess) return cuda_fail(e, "adjoint launch");
-  }
+  void* scratch = nullptr;
+  size_t bytes = 0;
+  if (int rc = map_scratch(*t, *m, n, &scratch, &bytes)) return rc;
+  if (int rc = run_ad(*t, n, in, out, seed, sens, nadj, true, false, scratch, bytes, s)) return rc;
   if (int rc = fetch_blocks(out, t->n_out, t->nnz_out, 1, n, res, s)) return rc;
   if (int rc = fetch_blocks(sens, t->n_in, t->nnz_in, nadj, n, asens, s)) return rc;
   return casadi_gb300_sync(id, s);

@@ -185,11 +185,11 @@ __global__ void __launch_bounds__(BS) k_primal(const __grid_constant__ SweepArgs
             double d0 = 0.0, d1 = 0.0;
             const double f = dev_fun_der(op, x, y, d0, d1);
             if (m & 1u) {
-              if (active) a.partials[pidx * a.pt_stride + il] = d0;
+              if (active) a.partials[((il >> 5) * a.t.n_partials + pidx) * 32 + (il & 31)] = d0;
               ++pidx;
             }
             if (m & 2u) {
-              if (active) a.partials[pidx * a.pt_stride + il] = d1;
+              if (active) a.partials[((il >> 5) * a.t.n_partials + pidx) * 32 + (il & 31)] = d1;
               ++pidx;
             }
             w[A * BS + tid] = f;
@@ -204,111 +204,200 @@ __global__ void __launch_bounds__(BS) k_primal(const __grid_constant__ SweepArgs
 }
 
 // ---------------------------------------------------------------------------------------------
-// Forward-mode directions from recorded partials. CTA = 32 instances x DW directions
-// (warp = direction), so each recorded partial is fetched by DW warps of one CTA.
+// Derivative sweeps from recorded partials.
+//
+// The record sweep stores partials tile-major: for the 32-instance tile T of a wave,
+// partial p of lane l is at partials[(T*P + p)*32 + l]. The partials an instruction chunk
+// consumes for one tile are therefore one contiguous block, staged into shared memory by a
+// single TMA bulk copy on the same mbarrier as the chunk's instructions. A CTA works on one
+// tile with DW warps, one direction per warp; consecutive CTAs take the direction groups of
+// the same tile, so a tile's partial block is read from HBM once and from L2 for the others.
+// ---------------------------------------------------------------------------------------------
+struct DirSmem {
+  u64* ring;      // 2 x chunk instructions
+  double* pbuf;   // 2 x (2*chunk partials x 32 lanes)
+  u64* bars;      // 2 mbarriers
+  double* wd;     // sz_w x (32*DW) tangents/adjoints
+  unsigned char* act;  // DW x act_stride: structural activity of each slot, per warp
+};
+
+// Bytes per warp of the activity table (slots rounded up to 16).
+__host__ __device__ __forceinline__ int act_stride(int sz_w) { return ((sz_w > 0 ? sz_w : 1) + 15) & ~15; }
+
+__device__ __forceinline__ DirSmem dir_smem(unsigned char* smem, int ch, int sz_w, int bs) {
+  DirSmem s;
+  s.ring = reinterpret_cast<u64*>(smem);
+  s.pbuf = reinterpret_cast<double*>(smem + 2 * ch * sizeof(u64));
+  s.bars = reinterpret_cast<u64*>(s.pbuf + 2 * (2 * ch * 32));
+  s.wd = reinterpret_cast<double*>(s.bars + 2);
+  s.act = reinterpret_cast<unsigned char*>(s.wd + static_cast<size_t>(sz_w > 0 ? sz_w : 1) * bs);
+  return s;
+}
+
+__device__ __forceinline__ int chunk_p0(const SweepArgs& a, int c) {
+  return __ldg(a.pofs + c * (a.chunk / kPofsGran));
+}
+
+// Stage instruction chunk c and its partial block for wave-local tile `tl` into slot seq&1.
+__device__ __forceinline__ void stage_dir(const SweepArgs& a, const DirSmem& s, unsigned seq,
+                                          int c, long long tl) {
+  const int ch = a.chunk;
+  const int p0 = chunk_p0(a, c), p1 = chunk_p0(a, c + 1);
+  const unsigned ibytes = ch * sizeof(u64);
+  const unsigned pbytes = static_cast<unsigned>(p1 - p0) * 32u * sizeof(double);
+  const unsigned slot = seq & 1u;
+  u64* bar = s.bars + slot;
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(ibytes + pbytes)
+               : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_u32(s.ring + slot * ch)),
+      "l"(a.t.code + static_cast<size_t>(c) * ch), "r"(ibytes), "r"(smem_u32(bar))
+      : "memory");
+  if (pbytes) {
+    const double* src = a.partials + (tl * a.t.n_partials + p0) * 32;
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+            "r"(smem_u32(s.pbuf + slot * (2 * ch * 32))),
+        "l"(src), "r"(pbytes), "r"(smem_u32(bar))
+        : "memory");
+  }
+}
+
 // w'[i0] = d0*w'[i1] + d1*w'[i2] (binary), d0*w'[i1] (unary),
 // if_else_zero(d1, w'[i2]) (IF_ELSE_ZERO): sx_function.cpp:1280-1363.
-// ---------------------------------------------------------------------------------------------
 template <int DW>
 __global__ void __launch_bounds__(32 * DW) k_tangent(const __grid_constant__ SweepArgs a) {
   constexpr int BS = 32 * DW;
   extern __shared__ __align__(128) unsigned char smem[];
-  u64* ring = reinterpret_cast<u64*>(smem);
-  u64* bars = ring + 2 * kChunk;
-  double* wd = reinterpret_cast<double*>(smem + kHeaderBytes);
+  const DirSmem s = dir_smem(smem, a.chunk, a.t.sz_w, BS);
+  double* wd = s.wd;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid == 0) stage_init(bars);
+  unsigned char* act = s.act + warp * act_stride(a.t.sz_w);
+  if (tid == 0) stage_init(s.bars);
   __syncthreads();
-  const long long dir = static_cast<long long>(blockIdx.y) * DW + warp;
+  const int ngroups = (a.ndir + DW - 1) / DW;
+  const int group = blockIdx.x % ngroups;
+  const long long dir = static_cast<long long>(group) * DW + warp;
   const bool dir_ok = dir < a.ndir;
-  unsigned seq = 0;
+  const int ch = a.chunk, nch = a.n_code / ch;
   const long long ntiles = (a.n + 31) / 32;
-  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+  const long long tstride = gridDim.x / ngroups;
+  unsigned seq = 0;
+  for (long long tile = blockIdx.x / ngroups; tile < ntiles; tile += tstride) {
     const long long il = tile * 32 + lane;
     const bool inst_ok = il < a.n;
     const bool active = inst_ok && dir_ok;
     const long long ig = a.i_begin + il;
-    long long pidx = 0;
-    const bool ok = sweep_forward(a.t, ring, bars, seq, [&](u64 ins) {
-      const unsigned op = dec_op(ins), A = dec_a(ins), B = dec_b(ins), C = dec_c(ins);
-      // operand slots are read only by the ops whose b/c fields are slots
-      double* wa = wd + A * BS + tid;
-      switch (op) {
-        case D_NOP:
-          break;
-        case D_CONST:
-          *wa = 0.0;
-          break;
-        case D_INPUT: {
-          double v = 0.0;
-          if (a.identity_seed) {
-            v = (a.in_off[B] + static_cast<int>(C) == a.dir0 + dir) ? 1.0 : 0.0;
-          } else {
-            const IoDesc& d = a.seed[B];
+    if (tid == 0) stage_dir(a, s, seq, 0, tile);
+#pragma unroll 1
+    for (int c = 0; c < nch; ++c) {
+      const bool more = c + 1 < nch;
+      if (tid == 0 && more) stage_dir(a, s, seq + 1, c + 1, tile);
+      const bool ok = stage_wait(s.bars, seq);
+      if (!__syncthreads_and(ok)) {
+        stage_abort(a.t, s.bars, seq, more);
+        return;
+      }
+      const u64* code = s.ring + (seq & 1u) * ch;
+      const double* pb = s.pbuf + (seq & 1u) * (2 * ch * 32) + lane;
+      int pl = 0;
+#pragma unroll 1
+      for (int k = 0; k < ch; ++k) {
+        const u64 ins = code[k];
+        const unsigned op = dec_op(ins), A = dec_a(ins), B = dec_b(ins), C = dec_c(ins);
+        double* wa = wd + A * BS + tid;
+        switch (op) {
+          case D_NOP:
+            break;
+          case D_CONST:
+            act[A] = 0;
+            break;
+          case D_INPUT: {
+            bool on;
+            double v = 0.0;
+            if (a.identity_seed) {
+              on = a.in_off[B] + static_cast<int>(C) == a.dir0 + dir;
+              v = 1.0;
+            } else {
+              const IoDesc& d = a.seed[B];
+              on = d.ptr != nullptr;
+              if (active && on)
+                v = __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir, C, ig));
+            }
+            if (on) *wa = v;
+            act[A] = on;
+          } break;
+          case D_OUTPUT: {
+            const IoDesc& d = a.sens[A];
             if (active && d.ptr)
-              v = __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir, C, ig));
-          }
-          *wa = v;
-        } break;
-        case D_OUTPUT: {
-          const IoDesc& d = a.sens[A];
-          if (active && d.ptr) static_cast<double*>(d.ptr)[io_off(d, dir, C, ig)] = wd[B * BS + tid];
-        } break;
-        case D_ADD: *wa = __dadd_rn(wd[B * BS + tid], wd[C * BS + tid]); break;
-        case D_SUB: *wa = __dsub_rn(wd[B * BS + tid], wd[C * BS + tid]); break;
-        case D_NEG: *wa = d_neg(wd[B * BS + tid]); break;
-        case D_TWICE: { const double xb = wd[B * BS + tid]; *wa = __dadd_rn(xb, xb); } break;
-        case D_ASSIGN: *wa = wd[B * BS + tid]; break;
-        default: {
-          const double xb = wd[B * BS + tid];
-          const unsigned m = partial_mask(op);
-          double d0 = const_d0(op), d1 = const_d1(op);
-          if (m & 1u) {
-            if (inst_ok) d0 = __ldg(a.partials + pidx * a.pt_stride + il);
-            ++pidx;
-          }
-          if (m & 2u) {
-            if (inst_ok) d1 = __ldg(a.partials + pidx * a.pt_stride + il);
-            ++pidx;
-          }
-          if (op == D_IF_ELSE_ZERO) {
-            *wa = d1 == 0.0 ? 0.0 : wd[C * BS + tid];
-          } else if (is_binary(op)) {
-            *wa = __dadd_rn(__dmul_rn(d0, xb), __dmul_rn(d1, wd[C * BS + tid]));
-          } else {
-            *wa = __dmul_rn(d0, xb);
+              static_cast<double*>(d.ptr)[io_off(d, dir, C, ig)] = act[B] ? wd[B * BS + tid] : 0.0;
+          } break;
+          default: {
+            const unsigned m = partial_mask(op);
+            double d0 = const_d0(op), d1 = const_d1(op);
+            if (m & 1u) d0 = pb[32 * pl++];
+            if (m & 2u) d1 = pb[32 * pl++];
+            // operand contributes when its tangent is structurally nonzero and its partial is
+            // not the constant zero (the reference's 0*x -> 0 and x+0 -> x simplifications)
+            const bool cb = act[B] && ((m & 1u) || const_d0(op) != 0.0);
+            const bool cc = is_binary(op) && act[C] && ((m & 2u) || const_d1(op) != 0.0);
+            if (cb || cc) {
+              const double xb = cb ? wd[B * BS + tid] : 0.0;
+              const double xc = cc ? wd[C * BS + tid] : 0.0;
+              double r;
+              switch (op) {
+                case D_ADD: r = cb && cc ? __dadd_rn(xb, xc) : (cb ? xb : xc); break;
+                case D_SUB: r = cb && cc ? __dsub_rn(xb, xc) : (cb ? xb : d_neg(xc)); break;
+                case D_NEG: r = d_neg(xb); break;
+                case D_TWICE: r = __dadd_rn(xb, xb); break;
+                case D_ASSIGN: r = xb; break;
+                case D_IF_ELSE_ZERO: r = d1 == 0.0 ? 0.0 : xc; break;
+                default:
+                  r = cb && cc ? __dadd_rn(__dmul_rn(d0, xb), __dmul_rn(d1, xc))
+                               : (cb ? __dmul_rn(d0, xb) : __dmul_rn(d1, xc));
+              }
+              *wa = r;
+            }
+            act[A] = cb || cc;
           }
         }
       }
-    });
-    if (!ok) return;
+      __syncthreads();
+      ++seq;
+    }
   }
 }
 
-// ---------------------------------------------------------------------------------------------
-// Adjoint directions from recorded partials, last instruction first.
 // seed = w'[i0]; w'[i0] = 0; w'[i1] += d0*seed; w'[i2] += d1*seed (sx_function.cpp:1454-1560).
-// ---------------------------------------------------------------------------------------------
 template <int DW>
 __global__ void __launch_bounds__(32 * DW) k_adjoint(const __grid_constant__ SweepArgs a) {
   constexpr int BS = 32 * DW;
   extern __shared__ __align__(128) unsigned char smem[];
-  u64* ring = reinterpret_cast<u64*>(smem);
-  u64* bars = ring + 2 * kChunk;
-  double* wb = reinterpret_cast<double*>(smem + kHeaderBytes);
+  const DirSmem s = dir_smem(smem, a.chunk, a.t.sz_w, BS);
+  double* wb = s.wd;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid == 0) stage_init(bars);
+  unsigned char* act = s.act + warp * act_stride(a.t.sz_w);
+  if (tid == 0) stage_init(s.bars);
   __syncthreads();
-  const long long dir = static_cast<long long>(blockIdx.y) * DW + warp;
+  const int ngroups = (a.ndir + DW - 1) / DW;
+  const int group = blockIdx.x % ngroups;
+  const long long dir = static_cast<long long>(group) * DW + warp;
   const bool dir_ok = dir < a.ndir;
-  unsigned seq = 0;
+  const int ch = a.chunk, nch = a.n_code / ch;
   const long long ntiles = (a.n + 31) / 32;
-  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+  const long long tstride = gridDim.x / ngroups;
+  unsigned seq = 0;
+  for (long long tile = blockIdx.x / ngroups; tile < ntiles; tile += tstride) {
     const long long il = tile * 32 + lane;
     const bool inst_ok = il < a.n;
     const bool active = inst_ok && dir_ok;
     const long long ig = a.i_begin + il;
-    for (int s = 0; s < a.t.sz_w; ++s) wb[s * BS + tid] = 0.0;
+    if (tid == 0) stage_dir(a, s, seq, nch - 1, tile);
+    for (int q = 0; q < a.t.sz_w; ++q) wb[q * BS + tid] = 0.0;
+    for (int q = lane; q < a.t.sz_w; q += 32) act[q] = 0;
+    __syncwarp();
     if (active) {
       // input nonzeros the tape never reads have a zero sensitivity
       for (int k = 0; k < a.t.n_absent_in; ++k) {
@@ -317,66 +406,86 @@ __global__ void __launch_bounds__(32 * DW) k_adjoint(const __grid_constant__ Swe
         if (d.ptr) static_cast<double*>(d.ptr)[io_off(d, dir, jk.y, ig)] = 0.0;
       }
     }
-    long long pidx = a.t.n_partials;
-    const bool ok = sweep_reverse(a.t, ring, bars, seq, [&](u64 ins) {
-      const unsigned op = dec_op(ins), A = dec_a(ins), B = dec_b(ins), C = dec_c(ins);
-      switch (op) {
-        case D_NOP:
-          break;
-        case D_CONST:
-          wb[A * BS + tid] = 0.0;
-          break;
-        case D_INPUT: {
-          const IoDesc& d = a.sens[B];
-          if (active && d.ptr) static_cast<double*>(d.ptr)[io_off(d, dir, C, ig)] = wb[A * BS + tid];
-          wb[A * BS + tid] = 0.0;
-        } break;
-        case D_OUTPUT: {
-          const IoDesc& d = a.seed[A];
-          if (active && d.ptr) {
-            const double s = __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir, C, ig));
-            wb[B * BS + tid] = __dadd_rn(wb[B * BS + tid], s);
-          }
-        } break;
-        default: {
-          const double seed = wb[A * BS + tid];
-          wb[A * BS + tid] = 0.0;
-          double* w1 = wb + B * BS + tid;
-          double* w2 = wb + C * BS + tid;
-          switch (op) {
-            case D_ADD: *w1 = __dadd_rn(*w1, seed); *w2 = __dadd_rn(*w2, seed); break;
-            case D_SUB: *w1 = __dadd_rn(*w1, seed); *w2 = __dadd_rn(*w2, d_neg(seed)); break;
-            case D_NEG: *w1 = __dadd_rn(*w1, d_neg(seed)); break;
-            case D_TWICE: *w1 = __dadd_rn(*w1, __dadd_rn(seed, seed)); break;
-            case D_ASSIGN: *w1 = __dadd_rn(*w1, seed); break;
-            default: {
-              const unsigned m = partial_mask(op);
-              double d0 = const_d0(op), d1 = const_d1(op);
-              if (m & 2u) {
-                --pidx;
-                if (inst_ok) d1 = __ldg(a.partials + pidx * a.pt_stride + il);
+#pragma unroll 1
+    for (int c = nch - 1; c >= 0; --c) {
+      const bool more = c > 0;
+      if (tid == 0 && more) stage_dir(a, s, seq + 1, c - 1, tile);
+      const bool ok = stage_wait(s.bars, seq);
+      if (!__syncthreads_and(ok)) {
+        stage_abort(a.t, s.bars, seq, more);
+        return;
+      }
+      const u64* code = s.ring + (seq & 1u) * ch;
+      const double* pb = s.pbuf + (seq & 1u) * (2 * ch * 32) + lane;
+      int pl = chunk_p0(a, c + 1) - chunk_p0(a, c);
+#pragma unroll 1
+      for (int k = ch - 1; k >= 0; --k) {
+        const u64 ins = code[k];
+        const unsigned op = dec_op(ins), A = dec_a(ins), B = dec_b(ins), C = dec_c(ins);
+        switch (op) {
+          case D_NOP:
+            break;
+          case D_CONST:
+            wb[A * BS + tid] = 0.0;
+            act[A] = 0;
+            break;
+          case D_INPUT: {
+            const IoDesc& d = a.sens[B];
+            if (active && d.ptr)
+              static_cast<double*>(d.ptr)[io_off(d, dir, C, ig)] = act[A] ? wb[A * BS + tid] : 0.0;
+            wb[A * BS + tid] = 0.0;
+            act[A] = 0;
+          } break;
+          case D_OUTPUT: {
+            const IoDesc& d = a.seed[A];
+            if (d.ptr) {
+              const double sd =
+                  active ? __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir, C, ig)) : 0.0;
+              wb[B * BS + tid] = act[B] ? __dadd_rn(wb[B * BS + tid], sd) : sd;
+              act[B] = 1;
+            }
+          } break;
+          default: {
+            const unsigned m = partial_mask(op);
+            double d0 = const_d0(op), d1 = const_d1(op);
+            if (m & 2u) d1 = pb[32 * --pl];
+            if (m & 1u) d0 = pb[32 * --pl];
+            if (!act[A]) break;  // structurally zero adjoint: nothing to propagate
+            const double seed = wb[A * BS + tid];
+            wb[A * BS + tid] = 0.0;
+            act[A] = 0;
+            if ((m & 1u) || const_d0(op) != 0.0) {
+              double c;
+              switch (op) {
+                case D_ADD: case D_SUB: case D_ASSIGN: c = seed; break;
+                case D_NEG: c = d_neg(seed); break;
+                case D_TWICE: c = __dadd_rn(seed, seed); break;
+                default: c = __dmul_rn(d0, seed);
               }
-              if (m & 1u) {
-                --pidx;
-                if (inst_ok) d0 = __ldg(a.partials + pidx * a.pt_stride + il);
+              double* w1 = wb + B * BS + tid;
+              *w1 = act[B] ? __dadd_rn(*w1, c) : c;
+              act[B] = 1;
+            }
+            if (is_binary(op) && ((m & 2u) || const_d1(op) != 0.0)) {
+              double c;
+              switch (op) {
+                case D_ADD: c = seed; break;
+                case D_SUB: c = d_neg(seed); break;
+                case D_IF_ELSE_ZERO: c = d1 == 0.0 ? 0.0 : seed; break;
+                default: c = __dmul_rn(d1, seed);
               }
-              if (op == D_IF_ELSE_ZERO) {
-                *w2 = __dadd_rn(*w2, d1 == 0.0 ? 0.0 : seed);
-              } else if (is_binary(op)) {
-                *w1 = __dadd_rn(*w1, __dmul_rn(d0, seed));
-                *w2 = __dadd_rn(*w2, __dmul_rn(d1, seed));
-              } else {
-                *w1 = __dadd_rn(*w1, __dmul_rn(d0, seed));
-              }
+              double* w2 = wb + C * BS + tid;
+              *w2 = act[C] ? __dadd_rn(*w2, c) : c;
+              act[C] = 1;
             }
           }
         }
       }
-    });
-    if (!ok) return;
+      __syncthreads();
+      ++seq;
+    }
   }
 }
-
 // ---------------------------------------------------------------------------------------------
 // bvec_t sparsity sweeps (uint64 bit sets, 64 directions at once).
 // ---------------------------------------------------------------------------------------------
@@ -476,8 +585,10 @@ __global__ void __launch_bounds__(BS) k_sp_reverse(const __grid_constant__ Sweep
 size_t smem_primal(int sz_w, int block) {
   return kHeaderBytes + static_cast<size_t>(sz_w > 0 ? sz_w : 1) * block * 8;
 }
-size_t smem_dir(int sz_w, int dir_warps) {
-  return kHeaderBytes + static_cast<size_t>(sz_w > 0 ? sz_w : 1) * 32 * dir_warps * 8;
+size_t smem_dir(int sz_w, int dir_warps, int chunk) {
+  return static_cast<size_t>(2 * chunk) * sizeof(u64) + static_cast<size_t>(4 * chunk * 32) * 8 +
+         2 * sizeof(u64) + static_cast<size_t>(sz_w > 0 ? sz_w : 1) * 32 * dir_warps * 8 +
+         static_cast<size_t>(act_stride(sz_w)) * dir_warps;
 }
 
 int max_smem_optin() {
@@ -530,28 +641,24 @@ cudaError_t launch_sp_reverse(const SweepArgs& a, int grid, cudaStream_t s) {
   CGB_DISPATCH_BS(k_sp_reverse)
 }
 
-cudaError_t launch_tangent(const SweepArgs& a, int grid_x, int grid_y, cudaStream_t s) {
-  const int dw = a.block / 32;
-  const size_t smem = smem_dir(a.t.sz_w, dw);
-  const dim3 grid(grid_x, grid_y);
-  switch (dw) {
-    case 1: return launch_k(k_tangent<1>, grid, 32, smem, a, s);
-    case 2: return launch_k(k_tangent<2>, grid, 64, smem, a, s);
-    case 4: return launch_k(k_tangent<4>, grid, 128, smem, a, s);
-    default: return cudaErrorInvalidValue;
+#define CGB_DISPATCH_DW(KT)                                                           \
+  switch (a.block / 32) {                                                             \
+    case 1: return launch_k(KT<1>, dim3(grid), 32, smem, a, s);                       \
+    case 2: return launch_k(KT<2>, dim3(grid), 64, smem, a, s);                       \
+    case 4: return launch_k(KT<4>, dim3(grid), 128, smem, a, s);                      \
+    case 6: return launch_k(KT<6>, dim3(grid), 192, smem, a, s);                      \
+    case 8: return launch_k(KT<8>, dim3(grid), 256, smem, a, s);                      \
+    default: return cudaErrorInvalidValue;                                            \
   }
+
+cudaError_t launch_tangent(const SweepArgs& a, int grid, cudaStream_t s) {
+  const size_t smem = smem_dir(a.t.sz_w, a.block / 32, a.chunk);
+  CGB_DISPATCH_DW(k_tangent)
 }
 
-cudaError_t launch_adjoint(const SweepArgs& a, int grid_x, int grid_y, cudaStream_t s) {
-  const int dw = a.block / 32;
-  const size_t smem = smem_dir(a.t.sz_w, dw);
-  const dim3 grid(grid_x, grid_y);
-  switch (dw) {
-    case 1: return launch_k(k_adjoint<1>, grid, 32, smem, a, s);
-    case 2: return launch_k(k_adjoint<2>, grid, 64, smem, a, s);
-    case 4: return launch_k(k_adjoint<4>, grid, 128, smem, a, s);
-    default: return cudaErrorInvalidValue;
-  }
+cudaError_t launch_adjoint(const SweepArgs& a, int grid, cudaStream_t s) {
+  const size_t smem = smem_dir(a.t.sz_w, a.block / 32, a.chunk);
+  CGB_DISPATCH_DW(k_adjoint)
 }
 
 int occupancy_primal(int block, size_t smem) {
@@ -578,11 +685,26 @@ int occupancy_primal(int block, size_t smem) {
   return (e == cudaSuccess && n > 0) ? n : 1;
 }
 
-int occupancy_dir(size_t smem) {
+template <class K>
+static int occ_of(K kernel, int block, size_t smem) {
   int n = 0;
-  cudaFuncSetAttribute(k_adjoint<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_adjoint<4>, 128, smem);
-  return (e == cudaSuccess && n > 0) ? n : 1;
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
+    return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, block, smem) != cudaSuccess)
+    return 0;
+  return n;
+}
+
+int occupancy_dir(int dir_warps, size_t smem) {
+  switch (dir_warps) {
+    case 1: return occ_of(k_tangent<1>, 32, smem);
+    case 2: return occ_of(k_tangent<2>, 64, smem);
+    case 4: return occ_of(k_tangent<4>, 128, smem);
+    case 6: return occ_of(k_tangent<6>, 192, smem);
+    case 8: return occ_of(k_tangent<8>, 256, smem);
+    default: return 0;
+  }
 }
 
 }  // namespace cgb

@@ -7,7 +7,8 @@
 
 namespace cgb {
 
-constexpr int kChunk = 256;      // instructions per staged chunk (2 KiB)
+constexpr int kChunk = 256;      // instructions per staged chunk (2 KiB), value sweeps
+constexpr int kPofsGran = 16;    // granularity of the per-chunk partial offsets
 constexpr int kMaxIo = 64;       // inputs/outputs per tape handled by one launch
 constexpr int kDirWarps = 4;     // directions per CTA in the derivative sweeps (one per warp)
 
@@ -23,6 +24,7 @@ struct IoDesc {
 // What every sweep needs to know about the tape.
 struct TapeView {
   const u64* code;          // kChunk-padded instruction stream (NOP padding)
+  const int* pofs;          // pofs[k]: partials recorded before instruction k*kPofsGran
   const double* consts;     // constant pool
   const int2* absent_in;    // (input, nonzero) pairs the tape never reads
   int n_chunks;
@@ -41,8 +43,10 @@ struct SweepArgs {
   int dir0;                 // first direction of this launch (identity seeds)
   int identity_seed;        // forward: seed of direction d is the d-th unit vector
   int block;                // threads per CTA
-  double* partials;         // scratch: partials[p*pt_stride + i_local]
-  long long pt_stride;
+  double* partials;         // scratch, tile-major: partials[(tile*P + p)*32 + lane]
+  const int* pofs;          // = t.pofs
+  int chunk;                // instructions per staged chunk in the derivative sweeps
+  int n_code;               // padded instruction count (multiple of kChunk)
   IoDesc in[kMaxIo];        // values in (eval / AD / sparsity)
   IoDesc out[kMaxIo];       // values out
   IoDesc seed[kMaxIo];      // forward: input seeds / adjoint: output seeds
@@ -56,18 +60,20 @@ constexpr int kErrBadOpcode = 2;     // an instruction with an unknown opcode wa
 
 // Shared memory a launch needs (bytes).
 size_t smem_primal(int sz_w, int block);
-size_t smem_dir(int sz_w, int dir_warps);
+size_t smem_dir(int sz_w, int dir_warps, int chunk);
 int max_smem_optin();
 
 cudaError_t launch_eval(const SweepArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_record(const SweepArgs& a, int grid, cudaStream_t s);
-cudaError_t launch_tangent(const SweepArgs& a, int grid_x, int grid_y, cudaStream_t s);
-cudaError_t launch_adjoint(const SweepArgs& a, int grid_x, int grid_y, cudaStream_t s);
+// Derivative sweeps: 1-D grid whose size is a multiple of the direction-group count
+// ceil(ndir / (block/32)); CTA b works on direction group b % groups.
+cudaError_t launch_tangent(const SweepArgs& a, int grid, cudaStream_t s);
+cudaError_t launch_adjoint(const SweepArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_sp_forward(const SweepArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_sp_reverse(const SweepArgs& a, int grid, cudaStream_t s);
 
 // Resident CTAs per SM for a given kernel family and shared-memory footprint.
 int occupancy_primal(int block, size_t smem);
-int occupancy_dir(size_t smem);
+int occupancy_dir(int dir_warps, size_t smem);
 
 }  // namespace cgb

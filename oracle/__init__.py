@@ -48,8 +48,8 @@ def lib():
         _lib.sxo_fun.restype = ct.c_double
         _lib.sxo_fun.argtypes = [ct.c_int, ct.c_double, ct.c_double]
         _lib.sxo_der.argtypes = [ct.c_int, ct.c_double, ct.c_double, ct.c_double, ct.c_void_p]
-        for name in ("sxo_eval", "sxo_forward", "sxo_reverse", "sxo_sp_forward",
-                     "sxo_sp_reverse"):
+        for name in ("sxo_eval", "sxo_forward", "sxo_jacobian", "sxo_reverse",
+                     "sxo_sp_forward", "sxo_sp_reverse"):
             getattr(_lib, name).restype = ct.c_int
     return _lib
 
@@ -128,6 +128,20 @@ def forward(tape, args, fseeds, n, nthreads=1):
     return res, fsens
 
 
+def jacobian(tape, args, n, nthreads=1):
+    """Values and the Jacobian by unit forward seeds: jac[j] has shape (nnz_in_total,
+    nnz_out[j], n)."""
+    t = TapeArrays(tape)
+    args = _prep(args)
+    nz = sum(tape.nnz_in)
+    res = _outs(tape.nnz_out, n)
+    jac = _outs(tape.nnz_out, n, nz)
+    rc = lib().sxo_jacobian(ct.byref(t.struct), ct.c_long(n), _ptrs(args), _ptrs(res),
+                            _ptrs(jac), ct.c_int(nthreads))
+    assert rc == 0
+    return res, jac
+
+
 def reverse(tape, args, aseeds, n, nthreads=1):
     """Values and nadj adjoint sensitivities; aseeds[j] has shape (nadj, nnz_out[j], n)."""
     t = TapeArrays(tape)
@@ -203,11 +217,28 @@ def ref_forward(tape, args, fseeds, n):
     rc = ref().ref_forward(ct.c_int(tape.n_instr), t.op.ctypes.data_as(ct.c_void_p),
                            t.i0.ctypes.data_as(ct.c_void_p), t.i1.ctypes.data_as(ct.c_void_p),
                            t.i2.ctypes.data_as(ct.c_void_p), t.d.ctypes.data_as(ct.c_void_p),
-                           ct.c_int(tape.sz_w), t.nnz_in.ctypes.data_as(ct.c_void_p),
+                           ct.c_int(tape.sz_w), ct.c_int(len(tape.nnz_in)),
+                           t.nnz_in.ctypes.data_as(ct.c_void_p),
                            t.nnz_out.ctypes.data_as(ct.c_void_p), ct.c_long(n),
                            ct.c_int(nfwd), _ptrs(args), _ptrs(fseeds), _ptrs(fsens))
     assert rc == 0
     return fsens
+
+
+def ref_jacobian(tape, args, n):
+    t = TapeArrays(tape)
+    args = _prep(args)
+    nz = sum(tape.nnz_in)
+    jac = _outs(tape.nnz_out, n, nz)
+    rc = ref().ref_jacobian(ct.c_int(tape.n_instr), t.op.ctypes.data_as(ct.c_void_p),
+                            t.i0.ctypes.data_as(ct.c_void_p), t.i1.ctypes.data_as(ct.c_void_p),
+                            t.i2.ctypes.data_as(ct.c_void_p), t.d.ctypes.data_as(ct.c_void_p),
+                            ct.c_int(tape.sz_w), ct.c_int(len(tape.nnz_in)),
+                            t.nnz_in.ctypes.data_as(ct.c_void_p),
+                            t.nnz_out.ctypes.data_as(ct.c_void_p), ct.c_long(n), _ptrs(args),
+                            _ptrs(jac))
+    assert rc == 0
+    return jac
 
 
 def ref_reverse(tape, args, aseeds, n):

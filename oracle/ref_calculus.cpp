@@ -8,10 +8,11 @@
 //   ref_op_id           the numeric value of enum Operation members (calculus.hpp:60-218)
 //   ref_eval            SXFunction::eval's instruction loop (casadi/core/sx_function.cpp:110-124)
 //                       driving the reference's own CASADI_MATH_FUN_BUILTIN dispatch macro
-//   ref_forward / ref_reverse
+//   ref_forward / ref_jacobian / ref_reverse
 //                       the numeric forward/adjoint sweeps that mirror the structure of
 //                       SXFunction::ad_forward/ad_reverse (sx_function.cpp:1248-1364,
-//                       :1418-1560) with partials from CASADI_MATH_DER_BUILTIN
+//                       :1418-1560) with partials from CASADI_MATH_DER_BUILTIN and the
+//                       structural-zero rules of the reference's derivative expressions
 // The rest of libcasadi needs CMake-generated headers and is not built.
 #include <iomanip>
 #include <cstdint>
@@ -93,11 +94,32 @@ static void partials(int n_instr, const int* op, const int* i0, const int* i1, c
   }
 }
 
-int ref_forward(int n_instr, const int* op, const int* i0, const int* i1, const int* i2,
-                const double* d, int sz_w, const int* nnz_in, const int* nnz_out, long n,
-                int nfwd, const double* const* arg, const double* const* fseed,
-                double* const* fsens) {
+// Structural activity: an operand contributes when its derivative is not structurally zero
+// and its partial is not the constant zero -- the simplifications 0*x -> 0, x+0 -> x,
+// 0-x -> -x that the reference applies while building derivative expressions
+// (calculus.hpp:1872-1990). The partials come from CASADI_MATH_DER_BUILTIN; an operand's
+// partial is a constant zero exactly when the reference's der() writes a literal 0 for it.
+static bool const_zero_partial(int op, int which) {
+  // evaluate der() at points on both sides of x == y; a literal zero is zero at all of them
+  const double pts[3][2] = {{0.3, 0.7}, {2.3, 0.7}, {-1.9, 2.3}};
+  for (const auto& q : pts) {
+    double f, d[2];
+    casadi_math<double>::fun(static_cast<unsigned char>(op), q[0], q[1], f);
+    casadi_math<double>::der(static_cast<unsigned char>(op), q[0], q[1], f, d);
+    if (!(d[which] == 0)) return false;
+  }
+  return true;
+}
+
+static int forward_impl(int n_instr, const int* op, const int* i0, const int* i1,
+                        const int* i2, const double* d, int sz_w, int n_in, const int* nnz_in,
+                        const int* nnz_out, long n, int nfwd, bool unit,
+                        const double* const* arg, const double* const* fseed,
+                        double* const* fsens) {
   std::vector<double> w(sz_w > 0 ? sz_w : 1), wd(sz_w > 0 ? sz_w : 1), dp(2 * n_instr + 2);
+  std::vector<char> act(sz_w > 0 ? sz_w : 1);
+  std::vector<int> off(n_in + 1, 0);
+  for (int j = 0; j < n_in; ++j) off[j + 1] = off[j] + nnz_in[j];
   for (long i = 0; i < n; ++i) {
     partials(n_instr, op, i0, i1, i2, d, n, i, arg, w, dp);
     for (int dir = 0; dir < nfwd; ++dir) {
@@ -105,18 +127,33 @@ int ref_forward(int n_instr, const int* op, const int* i0, const int* i1, const 
         const double* p = &dp[2 * k];
         switch (op[k]) {
           case OP_INPUT:
-            wd[i0[k]] = fseed[i1[k]] ? fseed[i1[k]][(dir * nnz_in[i1[k]] + i2[k]) * n + i] : 0;
+            if (unit) {
+              act[i0[k]] = off[i1[k]] + i2[k] == dir;
+              if (act[i0[k]]) wd[i0[k]] = 1.0;
+            } else {
+              act[i0[k]] = fseed[i1[k]] != nullptr;
+              if (fseed[i1[k]]) wd[i0[k]] = fseed[i1[k]][(dir * nnz_in[i1[k]] + i2[k]) * n + i];
+            }
             break;
           case OP_OUTPUT:
-            if (fsens[i0[k]]) fsens[i0[k]][(dir * nnz_out[i0[k]] + i2[k]) * n + i] = wd[i1[k]];
+            if (fsens[i0[k]])
+              fsens[i0[k]][(dir * nnz_out[i0[k]] + i2[k]) * n + i] = act[i1[k]] ? wd[i1[k]] : 0;
             break;
-          case OP_CONST: case OP_PARAMETER: wd[i0[k]] = 0; break;
-          case OP_IF_ELSE_ZERO: wd[i0[k]] = if_else_zero(p[1], wd[i2[k]]); break;
-          CASADI_MATH_BINARY_BUILTIN
-            wd[i0[k]] = p[0] * wd[i1[k]] + p[1] * wd[i2[k]];
-            break;
-          default:
-            wd[i0[k]] = p[0] * wd[i1[k]];
+          case OP_CONST: case OP_PARAMETER: act[i0[k]] = 0; break;
+          default: {
+            bool bin = casadi_math<double>::ndeps(op[k]) == 2;
+            bool cb = act[i1[k]] && !const_zero_partial(op[k], 0);
+            bool cc = bin && act[i2[k]] && !const_zero_partial(op[k], 1);
+            if (cb || cc) {
+              double xb = cb ? wd[i1[k]] : 0, xc = cc ? wd[i2[k]] : 0, r;
+              if (op[k] == OP_IF_ELSE_ZERO) r = if_else_zero(p[1], xc);
+              else if (cb && cc) r = p[0] * xb + p[1] * xc;
+              else if (cb) r = p[0] * xb;
+              else r = p[1] * xc;
+              wd[i0[k]] = r;
+            }
+            act[i0[k]] = cb || cc;
+          }
         }
       }
     }
@@ -124,46 +161,71 @@ int ref_forward(int n_instr, const int* op, const int* i0, const int* i1, const 
   return 0;
 }
 
+int ref_forward(int n_instr, const int* op, const int* i0, const int* i1, const int* i2,
+                const double* d, int sz_w, int n_in, const int* nnz_in, const int* nnz_out,
+                long n, int nfwd, const double* const* arg, const double* const* fseed,
+                double* const* fsens) {
+  return forward_impl(n_instr, op, i0, i1, i2, d, sz_w, n_in, nnz_in, nnz_out, n, nfwd, false,
+                      arg, fseed, fsens);
+}
+
+int ref_jacobian(int n_instr, const int* op, const int* i0, const int* i1, const int* i2,
+                 const double* d, int sz_w, int n_in, const int* nnz_in, const int* nnz_out,
+                 long n, const double* const* arg, double* const* jac) {
+  int nz = 0;
+  for (int j = 0; j < n_in; ++j) nz += nnz_in[j];
+  return forward_impl(n_instr, op, i0, i1, i2, d, sz_w, n_in, nnz_in, nnz_out, n, nz, true, arg,
+                      nullptr, jac);
+}
+
 int ref_reverse(int n_instr, const int* op, const int* i0, const int* i1, const int* i2,
                 const double* d, int sz_w, int n_in, const int* nnz_in, const int* nnz_out,
                 long n, int nadj, const double* const* arg, const double* const* aseed,
                 double* const* asens) {
   std::vector<double> w(sz_w > 0 ? sz_w : 1), wb(sz_w > 0 ? sz_w : 1), dp(2 * n_instr + 2);
+  std::vector<char> act(sz_w > 0 ? sz_w : 1);
   for (long i = 0; i < n; ++i) {
     partials(n_instr, op, i0, i1, i2, d, n, i, arg, w, dp);
     for (int dir = 0; dir < nadj; ++dir) {
       std::fill(wb.begin(), wb.end(), 0.0);
+      std::fill(act.begin(), act.end(), 0);
       for (int j = 0; j < n_in; ++j) {
         if (!asens[j]) continue;
         for (int k = 0; k < nnz_in[j]; ++k) asens[j][(dir * nnz_in[j] + k) * n + i] = 0;
       }
       for (int k = n_instr - 1; k >= 0; --k) {
         const double* p = &dp[2 * k];
-        double seed;
         switch (op[k]) {
           case OP_INPUT:
-            if (asens[i1[k]]) asens[i1[k]][(dir * nnz_in[i1[k]] + i2[k]) * n + i] = wb[i0[k]];
+            if (asens[i1[k]])
+              asens[i1[k]][(dir * nnz_in[i1[k]] + i2[k]) * n + i] = act[i0[k]] ? wb[i0[k]] : 0;
             wb[i0[k]] = 0;
+            act[i0[k]] = 0;
             break;
           case OP_OUTPUT:
-            if (aseed[i0[k]]) wb[i1[k]] += aseed[i0[k]][(dir * nnz_out[i0[k]] + i2[k]) * n + i];
+            if (aseed[i0[k]]) {
+              double v = aseed[i0[k]][(dir * nnz_out[i0[k]] + i2[k]) * n + i];
+              wb[i1[k]] = act[i1[k]] ? wb[i1[k]] + v : v;
+              act[i1[k]] = 1;
+            }
             break;
-          case OP_CONST: case OP_PARAMETER: wb[i0[k]] = 0; break;
-          case OP_IF_ELSE_ZERO:
-            seed = wb[i0[k]];
+          case OP_CONST: case OP_PARAMETER: wb[i0[k]] = 0; act[i0[k]] = 0; break;
+          default: {
+            if (!act[i0[k]]) break;
+            double seed = wb[i0[k]], c;
             wb[i0[k]] = 0;
-            wb[i2[k]] += if_else_zero(p[1], seed);
-            break;
-          CASADI_MATH_BINARY_BUILTIN
-            seed = wb[i0[k]];
-            wb[i0[k]] = 0;
-            wb[i1[k]] += p[0] * seed;
-            wb[i2[k]] += p[1] * seed;
-            break;
-          default:
-            seed = wb[i0[k]];
-            wb[i0[k]] = 0;
-            wb[i1[k]] += p[0] * seed;
+            act[i0[k]] = 0;
+            if (!const_zero_partial(op[k], 0)) {
+              c = p[0] * seed;
+              wb[i1[k]] = act[i1[k]] ? wb[i1[k]] + c : c;
+              act[i1[k]] = 1;
+            }
+            if (casadi_math<double>::ndeps(op[k]) == 2 && !const_zero_partial(op[k], 1)) {
+              c = op[k] == OP_IF_ELSE_ZERO ? if_else_zero(p[1], seed) : p[1] * seed;
+              wb[i2[k]] = act[i2[k]] ? wb[i2[k]] + c : c;
+              act[i2[k]] = 1;
+            }
+          }
         }
       }
     }

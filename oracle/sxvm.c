@@ -9,6 +9,8 @@
  *                        if_else_zero :295, erfinv :297-328)
  *   sxo_eval            SXFunction::eval                 (casadi/core/sx_function.cpp:110-124)
  *   sxo_forward         numeric analogue of SXFunction::ad_forward (sx_function.cpp:1248-1364)
+ *   sxo_jacobian        forward mode with unit seeds, the numeric analogue of the Jacobian
+ *                       that XFunction::jac builds (casadi/core/x_function.hpp:441-840)
  *   sxo_reverse         numeric analogue of SXFunction::ad_reverse (sx_function.cpp:1418-1560)
  *   sxo_sp_forward      SXFunction::sp_forward           (sx_function.cpp:1657-1682)
  *   sxo_sp_reverse      SXFunction::sp_reverse           (sx_function.cpp:1742-1782)
@@ -252,48 +254,114 @@ int sxo_eval(const sxo_tape* t, long n, const double* const* arg, double* const*
   return err;
 }
 
-int sxo_forward(const sxo_tape* t, long n, int nfwd, const double* const* arg,
-                double* const* res, const double* const* fseed, double* const* fsens,
-                int nthreads) {
+/* Structural activity (both AD sweeps): a slot is active when its derivative is not
+ * structurally zero. The reference builds derivatives symbolically, where constants and
+ * unseeded inputs are the zero expression and 0*x -> 0, x+0 -> x, 0-x -> -x simplify away
+ * (casadi/core/calculus.hpp:1872-1990); the numeric sweeps below apply the same rules, so an
+ * operand contributes only when it is active and its partial is not the constant zero. */
+static int nonzero_d0(int op) {
+  switch (op) {
+    case SXO_LT: case SXO_LE: case SXO_EQ: case SXO_NE: case SXO_AND: case SXO_OR:
+    case SXO_NOT: case SXO_FLOOR: case SXO_CEIL: case SXO_SIGN: case SXO_IF_ELSE_ZERO:
+      return 0;
+    default: return 1;
+  }
+}
+static int nonzero_d1(int op) {
+  switch (op) {
+    case SXO_ADD: case SXO_SUB: case SXO_MUL: case SXO_DIV: case SXO_POW: case SXO_FMOD:
+    case SXO_REMAINDER: case SXO_FMIN: case SXO_FMAX: case SXO_ATAN2: case SXO_HYPOT:
+    case SXO_IF_ELSE_ZERO:
+      return 1;
+    default: return 0;
+  }
+}
+
+/* one forward direction over one instance; seed(j, k) gives the seed (NAN-free) of input
+ * nonzero k of input j, active(j, k) whether it is seeded */
+static void tangent_one(const sxo_tape* t, const double* dp, double* wd, char* act,
+                        const int* in_off, int unit_dir, long n, long i, int dir,
+                        const double* const* fseed, double* const* fsens) {
+  for (int k = 0; k < t->n_instr; ++k) {
+    int op = t->op[k], i0 = t->i0[k], i1 = t->i1[k], i2 = t->i2[k];
+    const double* d = dp + 2 * (long)k;
+    switch (op) {
+      case SXO_INPUT:
+        if (unit_dir >= 0) {
+          act[i0] = in_off[i1] + i2 == unit_dir;
+          if (act[i0]) wd[i0] = 1.0;
+        } else {
+          const double* s = fseed[i1];
+          act[i0] = s != 0;
+          if (s) wd[i0] = s[((long)dir * t->nnz_in[i1] + i2) * n + i];
+        }
+        break;
+      case SXO_OUTPUT: {
+        double* s = fsens[i0];
+        if (s) s[((long)dir * t->nnz_out[i0] + i2) * n + i] = act[i1] ? wd[i1] : 0;
+      } break;
+      case SXO_CONST: case SXO_PARAMETER: act[i0] = 0; break;
+      default: {
+        int bin = sxo_ndeps(op) == 2;
+        int cb = act[i1] && nonzero_d0(op);
+        int cc = bin && act[i2] && nonzero_d1(op);
+        if (cb || cc) {
+          double xb = cb ? wd[i1] : 0, xc = cc ? wd[i2] : 0, r;
+          if (op == SXO_IF_ELSE_ZERO) r = d[1] == 0 ? 0 : xc;
+          else if (cb && cc) r = d[0] * xb + d[1] * xc;
+          else if (cb) r = d[0] * xb;
+          else r = d[1] * xc;
+          wd[i0] = r;
+        }
+        act[i0] = cb || cc;
+      }
+    }
+  }
+}
+
+static int forward_impl(const sxo_tape* t, long n, int nfwd, int unit, const double* const* arg,
+                        double* const* res, const double* const* fseed, double* const* fsens,
+                        int nthreads) {
   int err = 0;
+  int in_off[256];
+  if (t->n_in > 256) return 1;
+  for (int j = 0, o = 0; j < t->n_in; o += t->nnz_in[j], ++j) in_off[j] = o;
 #pragma omp parallel num_threads(nthreads > 0 ? nthreads : 1)
   {
-    double* w = (double*)malloc(sizeof(double) * (t->sz_w > 0 ? t->sz_w : 1));
-    double* wd = (double*)malloc(sizeof(double) * (t->sz_w > 0 ? t->sz_w : 1));
+    int sz = t->sz_w > 0 ? t->sz_w : 1;
+    double* w = (double*)malloc(sizeof(double) * sz);
+    double* wd = (double*)malloc(sizeof(double) * sz);
+    char* act = (char*)malloc(sz);
     double* dp = (double*)malloc(sizeof(double) * 2 * (t->n_instr > 0 ? t->n_instr : 1));
-    if (!w || !wd || !dp) {
+    if (!w || !wd || !act || !dp) {
 #pragma omp atomic write
       err = 1;
     } else {
 #pragma omp for schedule(static)
       for (long i = 0; i < n; ++i) {
         eval_partials(t, n, i, arg, res, w, dp);
-        for (int dir = 0; dir < nfwd; ++dir) {
-          for (int k = 0; k < t->n_instr; ++k) {
-            int op = t->op[k], i0 = t->i0[k], i1 = t->i1[k], i2 = t->i2[k];
-            const double* d = dp + 2 * (long)k;
-            switch (op) {
-              case SXO_INPUT: {
-                const double* s = fseed[i1];
-                wd[i0] = s ? s[((long)dir * t->nnz_in[i1] + i2) * n + i] : 0;
-              } break;
-              case SXO_OUTPUT: {
-                double* s = fsens[i0];
-                if (s) s[((long)dir * t->nnz_out[i0] + i2) * n + i] = wd[i1];
-              } break;
-              case SXO_CONST: case SXO_PARAMETER: wd[i0] = 0; break;
-              case SXO_IF_ELSE_ZERO: wd[i0] = d[1] == 0 ? 0 : wd[i2]; break;
-              default:
-                if (sxo_ndeps(op) == 2) wd[i0] = d[0] * wd[i1] + d[1] * wd[i2];
-                else wd[i0] = d[0] * wd[i1];
-            }
-          }
-        }
+        for (int dir = 0; dir < nfwd; ++dir)
+          tangent_one(t, dp, wd, act, in_off, unit ? dir : -1, n, i, dir, fseed, fsens);
       }
     }
-    free(w); free(wd); free(dp);
+    free(w); free(wd); free(act); free(dp);
   }
   return err;
+}
+
+int sxo_forward(const sxo_tape* t, long n, int nfwd, const double* const* arg,
+                double* const* res, const double* const* fseed, double* const* fsens,
+                int nthreads) {
+  return forward_impl(t, n, nfwd, 0, arg, res, fseed, fsens, nthreads);
+}
+
+/* Jacobian by forward mode with unit seeds: direction d is input nonzero d (input order);
+ * jac[j][(d*nnz_out[j] + k)*n + i]. */
+int sxo_jacobian(const sxo_tape* t, long n, const double* const* arg, double* const* res,
+                 double* const* jac, int nthreads) {
+  int nz = 0;
+  for (int j = 0; j < t->n_in; ++j) nz += t->nnz_in[j];
+  return forward_impl(t, n, nz, 1, arg, res, 0, jac, nthreads);
 }
 
 int sxo_reverse(const sxo_tape* t, long n, int nadj, const double* const* arg,
@@ -302,10 +370,12 @@ int sxo_reverse(const sxo_tape* t, long n, int nadj, const double* const* arg,
   int err = 0;
 #pragma omp parallel num_threads(nthreads > 0 ? nthreads : 1)
   {
-    double* w = (double*)malloc(sizeof(double) * (t->sz_w > 0 ? t->sz_w : 1));
-    double* wb = (double*)malloc(sizeof(double) * (t->sz_w > 0 ? t->sz_w : 1));
+    int sz = t->sz_w > 0 ? t->sz_w : 1;
+    double* w = (double*)malloc(sizeof(double) * sz);
+    double* wb = (double*)malloc(sizeof(double) * sz);
+    char* act = (char*)malloc(sz);
     double* dp = (double*)malloc(sizeof(double) * 2 * (t->n_instr > 0 ? t->n_instr : 1));
-    if (!w || !wb || !dp) {
+    if (!w || !wb || !act || !dp) {
 #pragma omp atomic write
       err = 1;
     } else {
@@ -313,7 +383,7 @@ int sxo_reverse(const sxo_tape* t, long n, int nadj, const double* const* arg,
       for (long i = 0; i < n; ++i) {
         eval_partials(t, n, i, arg, res, w, dp);
         for (int dir = 0; dir < nadj; ++dir) {
-          for (int s = 0; s < t->sz_w; ++s) wb[s] = 0;
+          for (int s = 0; s < t->sz_w; ++s) { wb[s] = 0; act[s] = 0; }
           /* asens starts at zero for every input nonzero (sx_function.cpp:1413-1422) */
           for (int j = 0; j < t->n_in; ++j) {
             if (!asens[j]) continue;
@@ -323,36 +393,42 @@ int sxo_reverse(const sxo_tape* t, long n, int nadj, const double* const* arg,
           for (int k = t->n_instr - 1; k >= 0; --k) {
             int op = t->op[k], i0 = t->i0[k], i1 = t->i1[k], i2 = t->i2[k];
             const double* d = dp + 2 * (long)k;
-            double seed;
             switch (op) {
               case SXO_INPUT: {
                 double* s = asens[i1];
-                if (s) s[((long)dir * t->nnz_in[i1] + i2) * n + i] = wb[i0];
-                wb[i0] = 0;
+                if (s) s[((long)dir * t->nnz_in[i1] + i2) * n + i] = act[i0] ? wb[i0] : 0;
+                wb[i0] = 0; act[i0] = 0;
               } break;
               case SXO_OUTPUT: {
                 const double* s = aseed[i0];
-                if (s) wb[i1] += s[((long)dir * t->nnz_out[i0] + i2) * n + i];
-              } break;
-              case SXO_CONST: case SXO_PARAMETER: wb[i0] = 0; break;
-              case SXO_IF_ELSE_ZERO:
-                seed = wb[i0]; wb[i0] = 0;
-                wb[i2] += d[1] == 0 ? 0 : seed;
-                break;
-              default:
-                seed = wb[i0]; wb[i0] = 0;
-                if (sxo_ndeps(op) == 2) {
-                  wb[i1] += d[0] * seed;
-                  wb[i2] += d[1] * seed;
-                } else {
-                  wb[i1] += d[0] * seed;
+                if (s) {
+                  double v = s[((long)dir * t->nnz_out[i0] + i2) * n + i];
+                  wb[i1] = act[i1] ? wb[i1] + v : v;
+                  act[i1] = 1;
                 }
+              } break;
+              case SXO_CONST: case SXO_PARAMETER: wb[i0] = 0; act[i0] = 0; break;
+              default: {
+                if (!act[i0]) break;
+                double seed = wb[i0], c;
+                wb[i0] = 0; act[i0] = 0;
+                if (nonzero_d0(op)) {
+                  c = d[0] * seed;
+                  wb[i1] = act[i1] ? wb[i1] + c : c;
+                  act[i1] = 1;
+                }
+                if (sxo_ndeps(op) == 2 && nonzero_d1(op)) {
+                  c = op == SXO_IF_ELSE_ZERO ? (d[1] == 0 ? 0 : seed) : d[1] * seed;
+                  wb[i2] = act[i2] ? wb[i2] + c : c;
+                  act[i2] = 1;
+                }
+              }
             }
           }
         }
       }
     }
-    free(w); free(wb); free(dp);
+    free(w); free(wb); free(act); free(dp);
   }
   return err;
 }

@@ -39,6 +39,8 @@ int sxo_eval(const sxo_tape* t, long n, const double* const* arg, double* const*
 int sxo_forward(const sxo_tape* t, long n, int nfwd, const double* const* arg,
                 double* const* res, const double* const* fseed, double* const* fsens,
                 int nthreads);
+int sxo_jacobian(const sxo_tape* t, long n, const double* const* arg, double* const* res,
+                 double* const* jac, int nthreads);
 int sxo_reverse(const sxo_tape* t, long n, int nadj, const double* const* arg,
                 double* const* res, const double* const* aseed, double* const* asens,
                 int nthreads);

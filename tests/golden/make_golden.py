@@ -13,8 +13,9 @@ Fixtures:
   tapes.npz      the cart-pole step, the 20-step rollout and a small random DAG as tapes, with
                  seeded inputs, forward seeds and adjoint seeds, and the reference harness's
                  outputs: values (SXFunction::eval's loop over CASADI_MATH_FUN_BUILTIN),
-                 forward sensitivities and adjoint sensitivities (numeric sweeps with partials
-                 from CASADI_MATH_DER_BUILTIN).
+                 forward sensitivities, adjoint sensitivities and the unit-seed Jacobian
+                 (numeric sweeps with partials from CASADI_MATH_DER_BUILTIN and the
+                 structural-zero rules of the reference's derivative expressions).
 """
 import math
 import os
@@ -67,6 +68,7 @@ def tape_case(name, fun, args, nfwd_seed_dirs=None, nadj=1, seed=7):
     fsens = O.ref_forward(t, args, fseeds, n)
     aseeds = [rng.standard_normal((nadj, k, n)) for k in t.nnz_out]
     asens = O.ref_reverse(t, args, aseeds, n)
+    jac = O.ref_jacobian(t, args, n)
     out = {name + "/op": t.op, name + "/i0": t.i0, name + "/i1": t.i1, name + "/i2": t.i2,
            name + "/d": t.d, name + "/nnz_in": np.array(t.nnz_in), name + "/nnz_out":
            np.array(t.nnz_out), name + "/sz_w": np.array(t.sz_w)}
@@ -82,6 +84,8 @@ def tape_case(name, fun, args, nfwd_seed_dirs=None, nadj=1, seed=7):
         out["%s/aseed%d" % (name, j)] = s
     for j, s in enumerate(asens):
         out["%s/asens%d" % (name, j)] = s
+    for j, s in enumerate(jac):
+        out["%s/jac%d" % (name, j)] = s
     return out
 
 

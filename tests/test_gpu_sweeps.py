@@ -20,6 +20,7 @@ from helpers import (EXACT_OPS, assert_bitexact, assert_close, golden_list, gold
 pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 NTHREADS = os.cpu_count() or 1
+ROLLOUT_RTOL = 1e-12
 
 
 def dev(arrs, dtype=None):
@@ -63,10 +64,15 @@ def test_golden_eval_forward_reverse(gpu_lib, name):
     res3, asens = host(res3), host(asens)
     for j, r in enumerate(golden_list(z, name, "asens", len(t.nnz_in))):
         assert_close(asens[j], r, "%s asens%d" % (name, j))
-    # the value outputs of all three sweeps are the same numbers
-    for a, b, c in zip(res, res2, res3):
+    res4, jac = ct.jacobian(dev(args))
+    res4, jac = host(res4), host(jac)
+    for j, r in enumerate(golden_list(z, name, "jac", len(t.nnz_out))):
+        assert_close(jac[j], r, "%s jac%d" % (name, j))
+    # the value outputs of all sweeps are the same numbers
+    for a, b, c, d in zip(res, res2, res3, res4):
         assert_bitexact(a, b, "eval vs forward values")
         assert_bitexact(a, c, "eval vs reverse values")
+        assert_bitexact(a, d, "eval vs jacobian values")
     ct.sync()
 
 
@@ -88,10 +94,16 @@ def test_ops_grid_values_and_partials(gpu_lib):
         ct = CudaTape(_single_op_tape(op))
         f = host(ct.eval(dev([x, y])))[0][0]
         name = C.OP_NAMES[op]
+        # erfinv follows the reference's own algorithm (Newton polish through erf and exp);
+        # near |x| -> 1 it amplifies a 1-ulp difference of erf by 1/(2/sqrt(pi) exp(-y^2)),
+        # ~1e5 at |x| = 0.999999, so its tolerance there is scaled by that condition number
+        # (its partial (sqrt(pi)/2)*exp(f^2) multiplies that by another 2*f^2 ~ 25)
+        tol = {C.OP_ERFINV: 1e-9}.get(op, None)
         if op in EXACT_OPS:
             assert_bitexact(f, z["f"][m], name + " value")
         else:
-            assert_close(f, z["f"][m], name + " value", floor=1e-300)
+            assert_close(f, z["f"][m], name + " value", floor=1e-300,
+                         **({} if tol is None else {"rtol": tol}))
         # adjoint seed 1 on the output gives d0 on x and d1 on y (0 + d*1)
         n = x.shape[1]
         _, asens = ct.reverse(dev([x, y]), dev([np.ones((1, 1, n))]))
@@ -105,7 +117,8 @@ def test_ops_grid_values_and_partials(gpu_lib):
             if op in EXACT_OPS:
                 assert_bitexact(got, ref, "%s %s" % (name, what))
             else:
-                assert_close(got, ref, "%s %s" % (name, what), floor=1e-300)
+                assert_close(got, ref, "%s %s" % (name, what), floor=1e-300,
+                             **({} if tol is None else {"rtol": tol}))
         ct.sync()
 
 
@@ -172,23 +185,32 @@ def test_rollout_jacobian_and_adjoint(gpu_lib):
     n = 8192
     args = W.cartpole_inputs(n, steps=20, seed=3)
     ct = CudaTape(F)
-    # forward Jacobian of xN: 24 identity seed directions over (x0, U)
-    eye = np.eye(24)
-    fseeds = [np.repeat(eye[:, :4, None], n, axis=2), np.repeat(eye[:, 4:, None], n, axis=2)]
-    res, fsens = ct.forward(dev(args), dev(fseeds))
+    # forward Jacobian of xN: 24 unit seed directions over (x0, U), generated on the device
+    res, fsens = ct.jacobian(dev(args))
     res, fsens = host(res), host(fsens)
-    wres, wfsens = O.forward(F.tape, args, fseeds, n, NTHREADS)
+    wres, wfsens = O.jacobian(F.tape, args, n, NTHREADS)
     assert_close(res[0], wres[0], "xN")
-    assert_close(fsens[0], wfsens[0], "d xN / d (x0,U)")
+    assert_close(fsens[0], wfsens[0], "d xN / d (x0,U)", rtol=ROLLOUT_RTOL)
+    # the same Jacobian from explicit unit seeds through the general forward sweep
+    eye = np.eye(24)
+    m = 512
+    fseeds = [np.repeat(eye[:, :4, None], m, axis=2), np.repeat(eye[:, 4:, None], m, axis=2)]
+    sub = [a[:, :m].copy() for a in args]
+    _, fs2 = ct.forward(dev(sub), dev(fseeds))
+    fs2 = host(fs2)
+    for a, b in zip(fs2, fsens):
+        assert np.array_equal(a, b[:, :, :m])
     # adjoint of cost
     aseeds = [np.zeros((1, 4, n)), np.ones((1, 1, n))]
     _, asens = ct.reverse(dev(args), dev(aseeds))
     asens = host(asens)
     _, wasens = O.reverse(F.tape, args, aseeds, n, NTHREADS)
-    assert_close(asens[0], wasens[0], "d cost / d x0")
-    assert_close(asens[1], wasens[1], "d cost / d U")
+    # Twenty RK4 steps of the cart-pole amplify the <= 1-ulp differences between CUDA's and
+    # the host libm's sin/cos (measured up to ~2e-13 on the adjoint); ROLLOUT_RTOL bounds it.
+    assert_close(asens[0], wasens[0], "d cost / d x0", rtol=ROLLOUT_RTOL)
+    assert_close(asens[1], wasens[1], "d cost / d U", rtol=ROLLOUT_RTOL)
     # the adjoint agrees with the forward Jacobian of the cost output row
-    jac_cost = np.concatenate([fsens[1][:, 0, :]], axis=0)  # (24, n)
+    jac_cost = fsens[1][:, 0, :]  # (24, n)
     adj = np.concatenate([asens[0][0], asens[1][0]], axis=0)  # (24, n)
     assert_close(adj, jac_cost, "adjoint vs forward", rtol=1e-12)
     # and central finite differences (h = 1e-6) on a few instances

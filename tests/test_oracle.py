@@ -69,6 +69,24 @@ def test_oracle_tapes_vs_golden(name):
     _, asens = O.reverse(t, args, aseeds, n)
     for j, r in enumerate(golden_list(z, name, "asens", len(t.nnz_in))):
         assert_close(asens[j], r, "%s asens%d" % (name, j))
+    _, jac = O.jacobian(t, args, n)
+    for j, r in enumerate(golden_list(z, name, "jac", len(t.nnz_out))):
+        assert_close(jac[j], r, "%s jac%d" % (name, j))
+
+
+def test_jacobian_equals_forward_with_unit_seeds():
+    z = load_npz("tapes.npz")
+    t = golden_tape(z, "rollout")
+    args = golden_list(z, "rollout", "arg", 2)
+    n = args[0].shape[-1]
+    nz = sum(t.nnz_in)
+    eye = np.eye(nz)
+    fseeds = [np.repeat(eye[:, :4, None], n, axis=2), np.repeat(eye[:, 4:, None], n, axis=2)]
+    _, fs = O.forward(t, args, fseeds, n)
+    _, jac = O.jacobian(t, args, n)
+    for a, b in zip(fs, jac):
+        # unit seeds only add exact zeros: same numbers up to the sign of zero
+        assert np.array_equal(a, b)
 
 
 def test_oracle_threads_agree():
