@@ -60,6 +60,39 @@ int device_opcode(int op) {
   }
 }
 
+// Activity plan of the tangent sweep for one seed pattern and launch shape.
+struct TanPlan {
+  int ndir = 0, dw = 0, ch = 0;
+  bool identity = false;
+  std::vector<char> seeded;  // per input: seed pointer given (general seeds)
+  int groups = 0;
+  unsigned short* d_bits = nullptr;
+  int* d_list = nullptr;
+  int* d_off = nullptr;
+  ~TanPlan() {
+    cudaFree(d_bits);
+    cudaFree(d_list);
+    cudaFree(d_off);
+  }
+};
+
+// Activity plan of the adjoint sweep for one pattern of seeded outputs and chunk size.
+struct AdjPlan {
+  int ch = 0;
+  std::vector<char> seeded;  // per output: seed pointer given
+  unsigned char* d_bits = nullptr;
+  int* d_list = nullptr;
+  int* d_off = nullptr;
+  int2* d_zero = nullptr;
+  int n_zero = 0;
+  ~AdjPlan() {
+    cudaFree(d_bits);
+    cudaFree(d_list);
+    cudaFree(d_off);
+    cudaFree(d_zero);
+  }
+};
+
 struct Tape {
   int device = 0;
   int n_instr = 0, n_in = 0, n_out = 0, sz_w = 0, n_partials = 0, n_chunks = 0;
@@ -75,11 +108,16 @@ struct Tape {
   int primal_block = 128, primal_grid_cap = 1;
   std::mutex shape_mtx;
   std::vector<std::pair<int, int>> dir_shape_cache;  // (ndir, packed shape)
+  std::vector<u64> h_code;                            // padded instruction stream
+  std::vector<std::unique_ptr<TanPlan>> tan_plans;
+  std::vector<std::unique_ptr<AdjPlan>> adj_plans;
 
   ~Tape() {
     int cur = 0;
     cudaGetDevice(&cur);
     if (cur != device) cudaSetDevice(device);
+    tan_plans.clear();
+    adj_plans.clear();
     cudaFree(d_code);
     cudaFree(d_pofs);
     cudaFree(d_consts);
@@ -295,6 +333,160 @@ long long wave_capacity(const Tape& t, long long n, size_t bytes) {
   return std::min<long long>(w, ((n + 31) / 32) * 32);
 }
 
+template <class T>
+cudaError_t upload(T** dst, const std::vector<T>& v) {
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(dst), std::max<size_t>(1, v.size()) * sizeof(T));
+  if (e != cudaSuccess) return e;
+  if (v.empty()) return cudaSuccess;
+  return cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+// Structural activity of the tangent sweep, per direction: an input slot is active when it is
+// seeded (unit seeds: when it is the direction's own input nonzero), an arithmetic result
+// when an operand that carries a derivative is active (the reference's 0*x -> 0, x+0 -> x).
+const TanPlan* tan_plan(Tape& t, int ndir, int dw, int ch, bool identity,
+                        const std::vector<char>& seeded, int* err) {
+  std::lock_guard<std::mutex> lk(t.shape_mtx);
+  for (auto& p : t.tan_plans)
+    if (p->ndir == ndir && p->dw == dw && p->ch == ch && p->identity == identity &&
+        (identity || p->seeded == seeded))
+      return p.get();
+  auto p = std::make_unique<TanPlan>();
+  p->ndir = ndir;
+  p->dw = dw;
+  p->ch = ch;
+  p->identity = identity;
+  p->seeded = seeded;
+  p->groups = (ndir + dw - 1) / dw;
+  const size_t nc = t.h_code.size();
+  std::vector<int> off(t.n_in + 1, 0);
+  for (int j = 0; j < t.n_in; ++j) off[j + 1] = off[j] + t.nnz_in[j];
+  std::vector<unsigned short> bits(static_cast<size_t>(p->groups) * nc, 0);
+  std::vector<char> act(std::max(1, t.sz_w));
+  const int ncomp = identity ? ndir : 1;  // general seeds: every direction has the same pattern
+  for (int d = 0; d < ncomp; ++d) {
+    std::fill(act.begin(), act.end(), 0);
+    for (size_t k = 0; k < nc; ++k) {
+      const u64 w = t.h_code[k];
+      const unsigned op = dec_op(w), A = dec_a(w), B = dec_b(w), C = dec_c(w);
+      unsigned b = 0;
+      if (op == D_NOP) continue;
+      if (op == D_CONST) {
+        act[A] = 0;
+        continue;
+      }
+      if (op == D_INPUT) {
+        const bool on = identity ? (off[B] + static_cast<int>(C) == d) : seeded[B] != 0;
+        act[A] = on;
+        b = on ? 1u : 0u;
+      } else if (op == D_OUTPUT) {
+        b = act[B] ? 1u : 0u;
+      } else {
+        const bool cb = act[B] && carries_d0(op);
+        const bool cc = act[C] && carries_d1(op);
+        act[A] = cb || cc;
+        b = (cb ? 1u : 0u) | (cc ? 2u : 0u);
+      }
+      if (!b) continue;
+      if (identity) {
+        bits[static_cast<size_t>(d / dw) * nc + k] |= static_cast<unsigned short>(b << (2 * (d % dw)));
+      } else {
+        for (int dd = 0; dd < ndir; ++dd)
+          bits[static_cast<size_t>(dd / dw) * nc + k] |=
+              static_cast<unsigned short>(b << (2 * (dd % dw)));
+      }
+    }
+  }
+  std::vector<int> list, offs(1, 0);
+  for (int g = 0; g < p->groups; ++g) {
+    for (size_t c = 0; c < nc / ch; ++c) {
+      bool need = false;
+      for (int k = 0; k < ch && !need; ++k) {
+        const size_t kk = c * ch + k;
+        need = bits[g * nc + kk] != 0 || dec_op(t.h_code[kk]) == D_OUTPUT;
+      }
+      if (need) list.push_back(static_cast<int>(c));
+    }
+    offs.push_back(static_cast<int>(list.size()));
+  }
+  cudaError_t e;
+  if ((e = upload(&p->d_bits, bits)) != cudaSuccess || (e = upload(&p->d_list, list)) != cudaSuccess ||
+      (e = upload(&p->d_off, offs)) != cudaSuccess) {
+    *err = cuda_fail(e, "upload tangent plan");
+    return nullptr;
+  }
+  t.tan_plans.push_back(std::move(p));
+  return t.tan_plans.back().get();
+}
+
+// Structural activity of the adjoint sweep (direction-independent), last instruction first.
+// Flags: 1 adjoint of the result is nonzero, 2/4 operand b/c receives a contribution,
+// 8/16 that contribution is the first to b/c, 32 a seeded output.
+const AdjPlan* adj_plan(Tape& t, int ch, const std::vector<char>& seeded, int* err) {
+  std::lock_guard<std::mutex> lk(t.shape_mtx);
+  for (auto& p : t.adj_plans)
+    if (p->ch == ch && p->seeded == seeded) return p.get();
+  auto p = std::make_unique<AdjPlan>();
+  p->ch = ch;
+  p->seeded = seeded;
+  const size_t nc = t.h_code.size();
+  std::vector<unsigned char> bits(nc, 0);
+  std::vector<char> act(std::max(1, t.sz_w), 0);
+  std::vector<int2> zero(t.absent_in);
+  for (size_t kk = nc; kk-- > 0;) {
+    const u64 w = t.h_code[kk];
+    const unsigned op = dec_op(w), A = dec_a(w), B = dec_b(w), C = dec_c(w);
+    unsigned f = 0;
+    if (op == D_NOP) continue;
+    if (op == D_OUTPUT) {
+      if (seeded[A]) {
+        f = 32u | (act[B] ? 0u : 8u);
+        act[B] = 1;
+      }
+    } else if (op == D_INPUT) {
+      if (act[A]) {
+        f = 1;
+        act[A] = 0;
+      } else {
+        zero.push_back(make_int2(static_cast<int>(B), static_cast<int>(C)));
+      }
+    } else if (op == D_CONST) {
+      if (act[A]) {
+        f = 1;
+        act[A] = 0;
+      }
+    } else if (act[A]) {
+      f = 1;
+      act[A] = 0;
+      if (carries_d0(op)) {
+        f |= 2u | (act[B] ? 0u : 8u);
+        act[B] = 1;
+      }
+      if (carries_d1(op)) {
+        f |= 4u | (act[C] ? 0u : 16u);
+        act[C] = 1;
+      }
+    }
+    bits[kk] = static_cast<unsigned char>(f);
+  }
+  std::vector<int> list, offs(1, 0);
+  for (size_t c = 0; c < nc / ch; ++c) {
+    bool need = false;
+    for (int k = 0; k < ch && !need; ++k) need = bits[c * ch + k] != 0;
+    if (need) list.push_back(static_cast<int>(c));
+  }
+  offs.push_back(static_cast<int>(list.size()));
+  p->n_zero = static_cast<int>(zero.size());
+  cudaError_t e;
+  if ((e = upload(&p->d_bits, bits)) != cudaSuccess || (e = upload(&p->d_list, list)) != cudaSuccess ||
+      (e = upload(&p->d_off, offs)) != cudaSuccess || (e = upload(&p->d_zero, zero)) != cudaSuccess) {
+    *err = cuda_fail(e, "upload adjoint plan");
+    return nullptr;
+  }
+  t.adj_plans.push_back(std::move(p));
+  return t.adj_plans.back().get();
+}
+
 // Values + partials (record sweep) followed by the derivative sweep, in waves of as many
 // instances as the scratch holds. `in/out/seed/sens` address the whole instance range.
 int run_ad(Tape& t, long long n, const IoDesc* in, const IoDesc* out, const IoDesc* seed,
@@ -309,6 +501,21 @@ int run_ad(Tape& t, long long n, const IoDesc* in, const IoDesc* out, const IoDe
   const DirShape ds = dir_shape(t, std::max(ndir, 1));
   const int groups = (ndir + ds.dw - 1) / ds.dw;
   const int sms = sm_count();
+  const TanPlan* tp = nullptr;
+  const AdjPlan* ap = nullptr;
+  if (ndir > 0) {
+    int err = 0;
+    if (adjoint) {
+      std::vector<char> seeded(t.n_out);
+      for (int j = 0; j < t.n_out; ++j) seeded[j] = seed[j].ptr != nullptr;
+      ap = adj_plan(t, ds.ch, seeded, &err);
+    } else {
+      std::vector<char> seeded(t.n_in);
+      for (int j = 0; j < t.n_in; ++j) seeded[j] = seed[j].ptr != nullptr;
+      tp = tan_plan(t, ndir, ds.dw, ds.ch, identity, seeded, &err);
+    }
+    if (!tp && !ap) return err ? err : fail(CASADI_GB300_ERR_CUDA, "activity plan");
+  }
   for (long long i0 = 0; i0 < n; i0 += cap) {
     const long long m = std::min(cap, n - i0);
     SweepArgs a = base_args(t, m, i0);
@@ -330,6 +537,17 @@ int run_ad(Tape& t, long long n, const IoDesc* in, const IoDesc* out, const IoDe
       std::memcpy(a.sens, sens, sizeof(IoDesc) * (adjoint ? t.n_in : t.n_out));
       a.block = 32 * ds.dw;
       a.chunk = ds.ch;
+      if (tp) {
+        a.tan_bits = tp->d_bits;
+        a.chunk_list = tp->d_list;
+        a.chunk_list_off = tp->d_off;
+      } else {
+        a.adj_bits = ap->d_bits;
+        a.chunk_list = ap->d_list;
+        a.chunk_list_off = ap->d_off;
+        a.zero_in = ap->d_zero;
+        a.n_zero = ap->n_zero;
+      }
       const long long tiles = (m + 31) / 32;
       const long long per_group = std::max<long long>(
           1, std::min<long long>(tiles, static_cast<long long>(sms) * ds.blocks_per_sm / groups));
@@ -448,6 +666,7 @@ int casadi_gb300_tape_create(const casadi_gb300_atomic* alg, int n_instr, int n_
   t->n_partials = static_cast<int>(n_partials);
   t->n_chunks = std::max(1, (n_instr + kChunk - 1) / kChunk);
   code.resize(static_cast<size_t>(t->n_chunks) * kChunk, enc(D_NOP, 0, 0, 0));
+  t->h_code = code;
   t->pofs.assign(code.size() / kPofsGran + 1, 0);
   for (size_t k = 0, acc = 0; k < code.size(); ++k) {
     if (k % kPofsGran == 0) t->pofs[k / kPofsGran] = static_cast<int>(acc);

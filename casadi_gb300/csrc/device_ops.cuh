@@ -29,22 +29,22 @@ enum DevOp : unsigned {
   D_NOP = 63
 };
 
-// 64-bit instruction word: op in bits 0-5, then three 19-bit fields a (bits 6-24),
-// b (25-43), c (44-62).
+// 64-bit instruction word: op in bits 0-5, three 18-bit fields a (bits 6-23), b (24-41),
+// c (42-59), then the op's recorded-partial mask (bits 60-61, see partial_mask) and a
+// binary-op flag (bit 62), so the AD sweeps read both without a lookup.
 //   arithmetic: a = result slot, b, c = operand slots (c == b for unary ops)
 //   CONST:      a = slot, b = index into the constant pool
 //   INPUT:      a = slot, b = input index, c = nonzero
 //   OUTPUT:     a = output index, b = slot, c = nonzero
-constexpr unsigned kFieldBits = 19;
+constexpr unsigned kFieldBits = 18;
 constexpr unsigned kFieldMax = (1u << kFieldBits) - 1;
 
-__host__ __device__ __forceinline__ u64 enc(unsigned op, unsigned a, unsigned b, unsigned c) {
-  return (u64)op | ((u64)a << 6) | ((u64)b << 25) | ((u64)c << 44);
-}
 __host__ __device__ __forceinline__ unsigned dec_op(u64 w) { return (unsigned)(w & 63u); }
 __host__ __device__ __forceinline__ unsigned dec_a(u64 w) { return (unsigned)(w >> 6) & kFieldMax; }
-__host__ __device__ __forceinline__ unsigned dec_b(u64 w) { return (unsigned)(w >> 25) & kFieldMax; }
-__host__ __device__ __forceinline__ unsigned dec_c(u64 w) { return (unsigned)(w >> 44) & kFieldMax; }
+__host__ __device__ __forceinline__ unsigned dec_b(u64 w) { return (unsigned)(w >> 24) & kFieldMax; }
+__host__ __device__ __forceinline__ unsigned dec_c(u64 w) { return (unsigned)(w >> 42) & kFieldMax; }
+__host__ __device__ __forceinline__ unsigned dec_pmask(u64 w) { return (unsigned)(w >> 60) & 3u; }
+__host__ __device__ __forceinline__ bool dec_binary(u64 w) { return (w >> 62) & 1u; }
 
 // Partials an instruction records for the AD sweeps: bit 0 = d0, bit 1 = d1.
 // Ops whose partials are constants (ADD, SUB, NEG, TWICE, ASSIGN, comparisons, ...) record
@@ -95,6 +95,19 @@ __host__ __device__ __forceinline__ double const_d1(unsigned op) {
     case D_SUB: return -1.0;
     default: return 0.0;
   }
+}
+
+__host__ __device__ __forceinline__ u64 enc(unsigned op, unsigned a, unsigned b, unsigned c) {
+  return (u64)op | ((u64)a << 6) | ((u64)b << 24) | ((u64)c << 42) |
+         ((u64)partial_mask(op) << 60) | ((u64)(is_binary(op) ? 1u : 0u) << 62);
+}
+
+// Whether an operand's partial is not the constant zero (it can carry a derivative).
+__host__ __device__ __forceinline__ bool carries_d0(unsigned op) {
+  return (partial_mask(op) & 1u) || const_d0(op) != 0.0;
+}
+__host__ __device__ __forceinline__ bool carries_d1(unsigned op) {
+  return is_binary(op) && ((partial_mask(op) & 2u) || const_d1(op) != 0.0);
 }
 
 #ifdef __CUDACC__

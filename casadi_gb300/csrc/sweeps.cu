@@ -208,29 +208,40 @@ __global__ void __launch_bounds__(BS) k_primal(const __grid_constant__ SweepArgs
 //
 // The record sweep stores partials tile-major: for the 32-instance tile T of a wave,
 // partial p of lane l is at partials[(T*P + p)*32 + l]. The partials an instruction chunk
-// consumes for one tile are therefore one contiguous block, staged into shared memory by a
-// single TMA bulk copy on the same mbarrier as the chunk's instructions. A CTA works on one
-// tile with DW warps, one direction per warp; consecutive CTAs take the direction groups of
-// the same tile, so a tile's partial block is read from HBM once and from L2 for the others.
+// consumes for one tile are therefore one contiguous block. Each chunk is staged with three
+// TMA bulk copies on one mbarrier: its instruction words, its partial block, and its
+// activity plan. A CTA works on one tile with DW warps, one direction per warp; consecutive
+// CTAs take the direction groups of the same tile, so a tile's partial block is read from
+// HBM once and from L2 for the other groups.
+//
+// Activity plan: which derivatives are structurally zero does not depend on the instance,
+// only on the tape and the seed pattern, so the host precomputes it. For the tangent sweep
+// each instruction carries two bits per direction of the group (operand b carries a
+// derivative, operand c carries one); chunks in which no direction of the group does any
+// work are left out of the group's chunk list and never fetched. For the adjoint sweep each
+// instruction carries five bits shared by all directions (its adjoint is nonzero, operand b
+// / c receives a contribution, that contribution is the first one to b / c).
 // ---------------------------------------------------------------------------------------------
 struct DirSmem {
-  u64* ring;      // 2 x chunk instructions
+  u64* ring;      // 2 x chunk instruction words
   double* pbuf;   // 2 x (2*chunk partials x 32 lanes)
+  unsigned char* abuf;  // 2 x chunk activity entries (2 bytes each for the tangent sweep)
   u64* bars;      // 2 mbarriers
   double* wd;     // sz_w x (32*DW) tangents/adjoints
-  unsigned char* act;  // DW x act_stride: structural activity of each slot, per warp
 };
 
-// Bytes per warp of the activity table (slots rounded up to 16).
-__host__ __device__ __forceinline__ int act_stride(int sz_w) { return ((sz_w > 0 ? sz_w : 1) + 15) & ~15; }
+__host__ __device__ __forceinline__ size_t dir_header_bytes(int ch) {
+  return static_cast<size_t>(2 * ch) * sizeof(u64) + static_cast<size_t>(4 * ch * 32) * 8 +
+         static_cast<size_t>(2 * ch) * 2 + 2 * sizeof(u64);
+}
 
-__device__ __forceinline__ DirSmem dir_smem(unsigned char* smem, int ch, int sz_w, int bs) {
+__device__ __forceinline__ DirSmem dir_smem(unsigned char* smem, int ch) {
   DirSmem s;
   s.ring = reinterpret_cast<u64*>(smem);
   s.pbuf = reinterpret_cast<double*>(smem + 2 * ch * sizeof(u64));
-  s.bars = reinterpret_cast<u64*>(s.pbuf + 2 * (2 * ch * 32));
+  s.abuf = reinterpret_cast<unsigned char*>(s.pbuf + 2 * (2 * ch * 32));
+  s.bars = reinterpret_cast<u64*>(s.abuf + 2 * ch * 2);
   s.wd = reinterpret_cast<double*>(s.bars + 2);
-  s.act = reinterpret_cast<unsigned char*>(s.wd + static_cast<size_t>(sz_w > 0 ? sz_w : 1) * bs);
   return s;
 }
 
@@ -238,63 +249,70 @@ __device__ __forceinline__ int chunk_p0(const SweepArgs& a, int c) {
   return __ldg(a.pofs + c * (a.chunk / kPofsGran));
 }
 
-// Stage instruction chunk c and its partial block for wave-local tile `tl` into slot seq&1.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, u64* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Stage chunk c (instructions, partial block of wave-local tile tl, activity entries of
+// `abytes_per` bytes from plan `plan`) into slot seq&1.
 __device__ __forceinline__ void stage_dir(const SweepArgs& a, const DirSmem& s, unsigned seq,
-                                          int c, long long tl) {
+                                          int c, long long tl, const unsigned char* plan,
+                                          unsigned abytes_per) {
   const int ch = a.chunk;
   const int p0 = chunk_p0(a, c), p1 = chunk_p0(a, c + 1);
   const unsigned ibytes = ch * sizeof(u64);
   const unsigned pbytes = static_cast<unsigned>(p1 - p0) * 32u * sizeof(double);
+  const unsigned abytes = ch * abytes_per;
   const unsigned slot = seq & 1u;
   u64* bar = s.bars + slot;
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-               "r"(ibytes + pbytes)
+               "r"(ibytes + pbytes + abytes)
                : "memory");
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
-          "r"(smem_u32(s.ring + slot * ch)),
-      "l"(a.t.code + static_cast<size_t>(c) * ch), "r"(ibytes), "r"(smem_u32(bar))
-      : "memory");
-  if (pbytes) {
-    const double* src = a.partials + (tl * a.t.n_partials + p0) * 32;
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
-            "r"(smem_u32(s.pbuf + slot * (2 * ch * 32))),
-        "l"(src), "r"(pbytes), "r"(smem_u32(bar))
-        : "memory");
-  }
+  bulk_g2s(s.ring + slot * ch, a.t.code + static_cast<size_t>(c) * ch, ibytes, bar);
+  bulk_g2s(s.abuf + slot * ch * 2, plan + static_cast<size_t>(c) * ch * abytes_per, abytes, bar);
+  if (pbytes)
+    bulk_g2s(s.pbuf + slot * (2 * ch * 32), a.partials + (tl * a.t.n_partials + p0) * 32, pbytes,
+             bar);
 }
 
-// w'[i0] = d0*w'[i1] + d1*w'[i2] (binary), d0*w'[i1] (unary),
-// if_else_zero(d1, w'[i2]) (IF_ELSE_ZERO): sx_function.cpp:1280-1363.
+// w'[i0] = d0*w'[i1] + d1*w'[i2] over the operands that carry a derivative
+// (sx_function.cpp:1280-1363 with the reference's structural simplifications).
 template <int DW>
 __global__ void __launch_bounds__(32 * DW) k_tangent(const __grid_constant__ SweepArgs a) {
   constexpr int BS = 32 * DW;
   extern __shared__ __align__(128) unsigned char smem[];
-  const DirSmem s = dir_smem(smem, a.chunk, a.t.sz_w, BS);
+  const DirSmem s = dir_smem(smem, a.chunk);
   double* wd = s.wd;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  unsigned char* act = s.act + warp * act_stride(a.t.sz_w);
   if (tid == 0) stage_init(s.bars);
   __syncthreads();
   const int ngroups = (a.ndir + DW - 1) / DW;
   const int group = blockIdx.x % ngroups;
   const long long dir = static_cast<long long>(group) * DW + warp;
   const bool dir_ok = dir < a.ndir;
-  const int ch = a.chunk, nch = a.n_code / ch;
+  const int ch = a.chunk;
+  const int* clist = a.chunk_list + __ldg(a.chunk_list_off + group);
+  const int nlist = __ldg(a.chunk_list_off + group + 1) - __ldg(a.chunk_list_off + group);
+  const unsigned char* plan =
+      reinterpret_cast<const unsigned char*>(a.tan_bits + static_cast<size_t>(group) * a.n_code);
+  const unsigned shift = 2u * warp;
   const long long ntiles = (a.n + 31) / 32;
   const long long tstride = gridDim.x / ngroups;
   unsigned seq = 0;
+  if (nlist == 0) return;
   for (long long tile = blockIdx.x / ngroups; tile < ntiles; tile += tstride) {
     const long long il = tile * 32 + lane;
-    const bool inst_ok = il < a.n;
-    const bool active = inst_ok && dir_ok;
+    const bool active = il < a.n && dir_ok;
     const long long ig = a.i_begin + il;
-    if (tid == 0) stage_dir(a, s, seq, 0, tile);
+    if (tid == 0) stage_dir(a, s, seq, __ldg(clist), tile, plan, 2);
 #pragma unroll 1
-    for (int c = 0; c < nch; ++c) {
-      const bool more = c + 1 < nch;
-      if (tid == 0 && more) stage_dir(a, s, seq + 1, c + 1, tile);
+    for (int idx = 0; idx < nlist; ++idx) {
+      const bool more = idx + 1 < nlist;
+      if (tid == 0 && more) stage_dir(a, s, seq + 1, __ldg(clist + idx + 1), tile, plan, 2);
       const bool ok = stage_wait(s.bars, seq);
       if (!__syncthreads_and(ok)) {
         stage_abort(a.t, s.bars, seq, more);
@@ -302,66 +320,158 @@ __global__ void __launch_bounds__(32 * DW) k_tangent(const __grid_constant__ Swe
       }
       const u64* code = s.ring + (seq & 1u) * ch;
       const double* pb = s.pbuf + (seq & 1u) * (2 * ch * 32) + lane;
+      const unsigned short* bits =
+          reinterpret_cast<const unsigned short*>(s.abuf + (seq & 1u) * ch * 2);
       int pl = 0;
 #pragma unroll 1
       for (int k = 0; k < ch; ++k) {
         const u64 ins = code[k];
         const unsigned op = dec_op(ins), A = dec_a(ins), B = dec_b(ins), C = dec_c(ins);
-        double* wa = wd + A * BS + tid;
-        switch (op) {
-          case D_NOP:
-            break;
-          case D_CONST:
-            act[A] = 0;
-            break;
-          case D_INPUT: {
-            bool on;
-            double v = 0.0;
-            if (a.identity_seed) {
-              on = a.in_off[B] + static_cast<int>(C) == a.dir0 + dir;
-              v = 1.0;
-            } else {
-              const IoDesc& d = a.seed[B];
-              on = d.ptr != nullptr;
-              if (active && on)
-                v = __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir, C, ig));
-            }
-            if (on) *wa = v;
-            act[A] = on;
-          } break;
-          case D_OUTPUT: {
-            const IoDesc& d = a.sens[A];
-            if (active && d.ptr)
-              static_cast<double*>(d.ptr)[io_off(d, dir, C, ig)] = act[B] ? wd[B * BS + tid] : 0.0;
-          } break;
-          default: {
-            const unsigned m = partial_mask(op);
-            double d0 = const_d0(op), d1 = const_d1(op);
-            if (m & 1u) d0 = pb[32 * pl++];
-            if (m & 2u) d1 = pb[32 * pl++];
-            // operand contributes when its tangent is structurally nonzero and its partial is
-            // not the constant zero (the reference's 0*x -> 0 and x+0 -> x simplifications)
-            const bool cb = act[B] && ((m & 1u) || const_d0(op) != 0.0);
-            const bool cc = is_binary(op) && act[C] && ((m & 2u) || const_d1(op) != 0.0);
-            if (cb || cc) {
-              const double xb = cb ? wd[B * BS + tid] : 0.0;
-              const double xc = cc ? wd[C * BS + tid] : 0.0;
-              double r;
-              switch (op) {
-                case D_ADD: r = cb && cc ? __dadd_rn(xb, xc) : (cb ? xb : xc); break;
-                case D_SUB: r = cb && cc ? __dsub_rn(xb, xc) : (cb ? xb : d_neg(xc)); break;
-                case D_NEG: r = d_neg(xb); break;
-                case D_TWICE: r = __dadd_rn(xb, xb); break;
-                case D_ASSIGN: r = xb; break;
-                case D_IF_ELSE_ZERO: r = d1 == 0.0 ? 0.0 : xc; break;
-                default:
-                  r = cb && cc ? __dadd_rn(__dmul_rn(d0, xb), __dmul_rn(d1, xc))
-                               : (cb ? __dmul_rn(d0, xb) : __dmul_rn(d1, xc));
-              }
-              *wa = r;
-            }
-            act[A] = cb || cc;
+        const unsigned m = dec_pmask(ins);
+        const unsigned ab = (bits[k] >> shift) & 3u;
+        double d0 = 1.0, d1 = 0.0;
+        if (m & 1u) d0 = pb[32 * pl++];
+        if (m & 2u) d1 = pb[32 * pl++];
+        if (op == D_OUTPUT) {
+          const IoDesc& d = a.sens[A];
+          if (active && d.ptr)
+            static_cast<double*>(d.ptr)[io_off(d, dir, C, ig)] = (ab & 1u) ? wd[B * BS + tid] : 0.0;
+          continue;
+        }
+        if (!ab) continue;  // structurally zero for this direction
+        double r;
+        if (op == D_INPUT) {
+          r = 1.0;
+          if (!a.identity_seed) {
+            const IoDesc& d = a.seed[B];
+            r = active ? __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir, C, ig)) : 0.0;
           }
+        } else {
+          const bool cb = ab & 1u, cc = ab & 2u;
+          const double xb = cb ? wd[B * BS + tid] : 0.0;
+          const double xc = cc ? wd[C * BS + tid] : 0.0;
+          switch (op) {
+            case D_ADD: r = cb && cc ? __dadd_rn(xb, xc) : (cb ? xb : xc); break;
+            case D_SUB: r = cb && cc ? __dsub_rn(xb, xc) : (cb ? xb : d_neg(xc)); break;
+            case D_NEG: r = d_neg(xb); break;
+            case D_TWICE: r = __dadd_rn(xb, xb); break;
+            case D_ASSIGN: r = xb; break;
+            case D_IF_ELSE_ZERO: r = d1 == 0.0 ? 0.0 : xc; break;
+            default:
+              r = cb && cc ? __dadd_rn(__dmul_rn(d0, xb), __dmul_rn(d1, xc))
+                           : (cb ? __dmul_rn(d0, xb) : __dmul_rn(d1, xc));
+          }
+        }
+        wd[A * BS + tid] = r;
+      }
+      __syncthreads();
+      ++seq;
+    }
+  }
+}
+
+// seed = w'[i0]; w'[i0] = 0; w'[i1] += d0*seed; w'[i2] += d1*seed (sx_function.cpp:1454-1560),
+// with structurally zero adjoints skipped and first contributions assigned (0 + x -> x).
+template <int DW>
+__global__ void __launch_bounds__(32 * DW) k_adjoint(const __grid_constant__ SweepArgs a) {
+  constexpr int BS = 32 * DW;
+  extern __shared__ __align__(128) unsigned char smem[];
+  const DirSmem s = dir_smem(smem, a.chunk);
+  double* wb = s.wd;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) stage_init(s.bars);
+  __syncthreads();
+  const int ngroups = (a.ndir + DW - 1) / DW;
+  const int group = blockIdx.x % ngroups;
+  const long long dir = static_cast<long long>(group) * DW + warp;
+  const bool dir_ok = dir < a.ndir;
+  const int ch = a.chunk;
+  const int nlist = __ldg(a.chunk_list_off + 1);
+  const long long ntiles = (a.n + 31) / 32;
+  const long long tstride = gridDim.x / ngroups;
+  unsigned seq = 0;
+  for (int q = 0; q < a.t.sz_w; ++q) wb[q * BS + tid] = 0.0;
+  for (long long tile = blockIdx.x / ngroups; tile < ntiles; tile += tstride) {
+    const long long il = tile * 32 + lane;
+    const bool active = il < a.n && dir_ok;
+    const long long ig = a.i_begin + il;
+    if (active) {
+      // input nonzeros whose adjoint is structurally zero (or never read) get a zero
+      for (int k = 0; k < a.n_zero; ++k) {
+        const int2 jk = __ldg(a.zero_in + k);
+        const IoDesc& d = a.sens[jk.x];
+        if (d.ptr) static_cast<double*>(d.ptr)[io_off(d, dir, jk.y, ig)] = 0.0;
+      }
+    }
+    if (nlist == 0) continue;
+    if (tid == 0) stage_dir(a, s, seq, __ldg(a.chunk_list + nlist - 1), tile, a.adj_bits, 1);
+#pragma unroll 1
+    for (int idx = nlist - 1; idx >= 0; --idx) {
+      const bool more = idx > 0;
+      if (tid == 0 && more)
+        stage_dir(a, s, seq + 1, __ldg(a.chunk_list + idx - 1), tile, a.adj_bits, 1);
+      const bool ok = stage_wait(s.bars, seq);
+      if (!__syncthreads_and(ok)) {
+        stage_abort(a.t, s.bars, seq, more);
+        return;
+      }
+      const int c = __ldg(a.chunk_list + idx);
+      const u64* code = s.ring + (seq & 1u) * ch;
+      const double* pb = s.pbuf + (seq & 1u) * (2 * ch * 32) + lane;
+      const unsigned char* bits = s.abuf + (seq & 1u) * ch * 2;
+      int pl = chunk_p0(a, c + 1) - chunk_p0(a, c);
+#pragma unroll 1
+      for (int k = ch - 1; k >= 0; --k) {
+        const u64 ins = code[k];
+        const unsigned op = dec_op(ins), A = dec_a(ins), B = dec_b(ins), C = dec_c(ins);
+        const unsigned m = dec_pmask(ins);
+        const unsigned f = bits[k];
+        double d0 = 1.0, d1 = 0.0;
+        if (m & 2u) d1 = pb[32 * --pl];
+        if (m & 1u) d0 = pb[32 * --pl];
+        if (op == D_OUTPUT) {
+          const IoDesc& d = a.seed[A];
+          if (d.ptr) {
+            const double sd =
+                active ? __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir, C, ig)) : 0.0;
+            wb[B * BS + tid] = (f & 8u) ? sd : __dadd_rn(wb[B * BS + tid], sd);
+          }
+          continue;
+        }
+        if (!(f & 1u)) continue;  // structurally zero adjoint
+        if (op == D_INPUT) {
+          const IoDesc& d = a.sens[B];
+          if (active && d.ptr) static_cast<double*>(d.ptr)[io_off(d, dir, C, ig)] = wb[A * BS + tid];
+          wb[A * BS + tid] = 0.0;
+          continue;
+        }
+        if (op == D_CONST) {
+          wb[A * BS + tid] = 0.0;
+          continue;
+        }
+        const double seed = wb[A * BS + tid];
+        wb[A * BS + tid] = 0.0;
+        if (f & 2u) {
+          double c0;
+          switch (op) {
+            case D_ADD: case D_SUB: case D_ASSIGN: c0 = seed; break;
+            case D_NEG: c0 = d_neg(seed); break;
+            case D_TWICE: c0 = __dadd_rn(seed, seed); break;
+            default: c0 = __dmul_rn(d0, seed);
+          }
+          double* w1 = wb + B * BS + tid;
+          *w1 = (f & 8u) ? c0 : __dadd_rn(*w1, c0);
+        }
+        if (f & 4u) {
+          double c1;
+          switch (op) {
+            case D_ADD: c1 = seed; break;
+            case D_SUB: c1 = d_neg(seed); break;
+            case D_IF_ELSE_ZERO: c1 = d1 == 0.0 ? 0.0 : seed; break;
+            default: c1 = __dmul_rn(d1, seed);
+          }
+          double* w2 = wb + C * BS + tid;
+          *w2 = (f & 16u) ? c1 : __dadd_rn(*w2, c1);
         }
       }
       __syncthreads();
@@ -370,122 +480,6 @@ __global__ void __launch_bounds__(32 * DW) k_tangent(const __grid_constant__ Swe
   }
 }
 
-// seed = w'[i0]; w'[i0] = 0; w'[i1] += d0*seed; w'[i2] += d1*seed (sx_function.cpp:1454-1560).
-template <int DW>
-__global__ void __launch_bounds__(32 * DW) k_adjoint(const __grid_constant__ SweepArgs a) {
-  constexpr int BS = 32 * DW;
-  extern __shared__ __align__(128) unsigned char smem[];
-  const DirSmem s = dir_smem(smem, a.chunk, a.t.sz_w, BS);
-  double* wb = s.wd;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  unsigned char* act = s.act + warp * act_stride(a.t.sz_w);
-  if (tid == 0) stage_init(s.bars);
-  __syncthreads();
-  const int ngroups = (a.ndir + DW - 1) / DW;
-  const int group = blockIdx.x % ngroups;
-  const long long dir = static_cast<long long>(group) * DW + warp;
-  const bool dir_ok = dir < a.ndir;
-  const int ch = a.chunk, nch = a.n_code / ch;
-  const long long ntiles = (a.n + 31) / 32;
-  const long long tstride = gridDim.x / ngroups;
-  unsigned seq = 0;
-  for (long long tile = blockIdx.x / ngroups; tile < ntiles; tile += tstride) {
-    const long long il = tile * 32 + lane;
-    const bool inst_ok = il < a.n;
-    const bool active = inst_ok && dir_ok;
-    const long long ig = a.i_begin + il;
-    if (tid == 0) stage_dir(a, s, seq, nch - 1, tile);
-    for (int q = 0; q < a.t.sz_w; ++q) wb[q * BS + tid] = 0.0;
-    for (int q = lane; q < a.t.sz_w; q += 32) act[q] = 0;
-    __syncwarp();
-    if (active) {
-      // input nonzeros the tape never reads have a zero sensitivity
-      for (int k = 0; k < a.t.n_absent_in; ++k) {
-        const int2 jk = a.t.absent_in[k];
-        const IoDesc& d = a.sens[jk.x];
-        if (d.ptr) static_cast<double*>(d.ptr)[io_off(d, dir, jk.y, ig)] = 0.0;
-      }
-    }
-#pragma unroll 1
-    for (int c = nch - 1; c >= 0; --c) {
-      const bool more = c > 0;
-      if (tid == 0 && more) stage_dir(a, s, seq + 1, c - 1, tile);
-      const bool ok = stage_wait(s.bars, seq);
-      if (!__syncthreads_and(ok)) {
-        stage_abort(a.t, s.bars, seq, more);
-        return;
-      }
-      const u64* code = s.ring + (seq & 1u) * ch;
-      const double* pb = s.pbuf + (seq & 1u) * (2 * ch * 32) + lane;
-      int pl = chunk_p0(a, c + 1) - chunk_p0(a, c);
-#pragma unroll 1
-      for (int k = ch - 1; k >= 0; --k) {
-        const u64 ins = code[k];
-        const unsigned op = dec_op(ins), A = dec_a(ins), B = dec_b(ins), C = dec_c(ins);
-        switch (op) {
-          case D_NOP:
-            break;
-          case D_CONST:
-            wb[A * BS + tid] = 0.0;
-            act[A] = 0;
-            break;
-          case D_INPUT: {
-            const IoDesc& d = a.sens[B];
-            if (active && d.ptr)
-              static_cast<double*>(d.ptr)[io_off(d, dir, C, ig)] = act[A] ? wb[A * BS + tid] : 0.0;
-            wb[A * BS + tid] = 0.0;
-            act[A] = 0;
-          } break;
-          case D_OUTPUT: {
-            const IoDesc& d = a.seed[A];
-            if (d.ptr) {
-              const double sd =
-                  active ? __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir, C, ig)) : 0.0;
-              wb[B * BS + tid] = act[B] ? __dadd_rn(wb[B * BS + tid], sd) : sd;
-              act[B] = 1;
-            }
-          } break;
-          default: {
-            const unsigned m = partial_mask(op);
-            double d0 = const_d0(op), d1 = const_d1(op);
-            if (m & 2u) d1 = pb[32 * --pl];
-            if (m & 1u) d0 = pb[32 * --pl];
-            if (!act[A]) break;  // structurally zero adjoint: nothing to propagate
-            const double seed = wb[A * BS + tid];
-            wb[A * BS + tid] = 0.0;
-            act[A] = 0;
-            if ((m & 1u) || const_d0(op) != 0.0) {
-              double c;
-              switch (op) {
-                case D_ADD: case D_SUB: case D_ASSIGN: c = seed; break;
-                case D_NEG: c = d_neg(seed); break;
-                case D_TWICE: c = __dadd_rn(seed, seed); break;
-                default: c = __dmul_rn(d0, seed);
-              }
-              double* w1 = wb + B * BS + tid;
-              *w1 = act[B] ? __dadd_rn(*w1, c) : c;
-              act[B] = 1;
-            }
-            if (is_binary(op) && ((m & 2u) || const_d1(op) != 0.0)) {
-              double c;
-              switch (op) {
-                case D_ADD: c = seed; break;
-                case D_SUB: c = d_neg(seed); break;
-                case D_IF_ELSE_ZERO: c = d1 == 0.0 ? 0.0 : seed; break;
-                default: c = __dmul_rn(d1, seed);
-              }
-              double* w2 = wb + C * BS + tid;
-              *w2 = act[C] ? __dadd_rn(*w2, c) : c;
-              act[C] = 1;
-            }
-          }
-        }
-      }
-      __syncthreads();
-      ++seq;
-    }
-  }
-}
 // ---------------------------------------------------------------------------------------------
 // bvec_t sparsity sweeps (uint64 bit sets, 64 directions at once).
 // ---------------------------------------------------------------------------------------------
@@ -586,9 +580,7 @@ size_t smem_primal(int sz_w, int block) {
   return kHeaderBytes + static_cast<size_t>(sz_w > 0 ? sz_w : 1) * block * 8;
 }
 size_t smem_dir(int sz_w, int dir_warps, int chunk) {
-  return static_cast<size_t>(2 * chunk) * sizeof(u64) + static_cast<size_t>(4 * chunk * 32) * 8 +
-         2 * sizeof(u64) + static_cast<size_t>(sz_w > 0 ? sz_w : 1) * 32 * dir_warps * 8 +
-         static_cast<size_t>(act_stride(sz_w)) * dir_warps;
+  return dir_header_bytes(chunk) + static_cast<size_t>(sz_w > 0 ? sz_w : 1) * 32 * dir_warps * 8;
 }
 
 int max_smem_optin() {

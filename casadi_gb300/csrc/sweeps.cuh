@@ -52,6 +52,13 @@ struct SweepArgs {
   IoDesc seed[kMaxIo];      // forward: input seeds / adjoint: output seeds
   IoDesc sens[kMaxIo];      // forward: output sensitivities / adjoint: input sensitivities
   int in_off[kMaxIo];       // flat offset of each input's first nonzero (identity seeds)
+  // activity plans (host-computed; see the derivative sweeps)
+  const unsigned short* tan_bits;   // [group][n_code]: 2 bits per direction of the group
+  const unsigned char* adj_bits;    // [n_code]: adjoint activity flags
+  const int* chunk_list;            // chunk indices to process, per group (tangent) or one list
+  const int* chunk_list_off;        // offsets into chunk_list, groups + 1 entries
+  const int2* zero_in;              // adjoint: (input, nonzero) pairs with a zero sensitivity
+  int n_zero;
 };
 
 // Error bits written to TapeView::err.
