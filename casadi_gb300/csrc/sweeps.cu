@@ -372,7 +372,9 @@ __global__ void __launch_bounds__(32 * DW) k_tangent(const __grid_constant__ Swe
 
 // seed = w'[i0]; w'[i0] = 0; w'[i1] += d0*seed; w'[i2] += d1*seed (sx_function.cpp:1454-1560),
 // with structurally zero adjoints skipped and first contributions assigned (0 + x -> x).
-template <int DW>
+// kDense: the variant without an activity plan (every chunk, every instruction active,
+// contributions always added to a zeroed adjoint); it needs no plan memory.
+template <int DW, bool kDense = false>
 __global__ void __launch_bounds__(32 * DW) k_adjoint(const __grid_constant__ SweepArgs a) {
   constexpr int BS = 32 * DW;
   extern __shared__ __align__(128) unsigned char smem[];
@@ -386,7 +388,7 @@ __global__ void __launch_bounds__(32 * DW) k_adjoint(const __grid_constant__ Swe
   const long long dir = static_cast<long long>(group) * DW + warp;
   const bool dir_ok = dir < a.ndir;
   const int ch = a.chunk;
-  const int nlist = __ldg(a.chunk_list_off + 1);
+  const int nlist = kDense ? a.n_code / ch : __ldg(a.chunk_list_off + 1);
   const long long ntiles = (a.n + 31) / 32;
   const long long tstride = gridDim.x / ngroups;
   unsigned seq = 0;
@@ -397,25 +399,30 @@ __global__ void __launch_bounds__(32 * DW) k_adjoint(const __grid_constant__ Swe
     const long long ig = a.i_begin + il;
     if (active) {
       // input nonzeros whose adjoint is structurally zero (or never read) get a zero
-      for (int k = 0; k < a.n_zero; ++k) {
-        const int2 jk = __ldg(a.zero_in + k);
+      const int nz = kDense ? a.t.n_absent_in : a.n_zero;
+      const int2* zl = kDense ? a.t.absent_in : a.zero_in;
+      for (int k = 0; k < nz; ++k) {
+        const int2 jk = __ldg(zl + k);
         const IoDesc& d = a.sens[jk.x];
         if (d.ptr) static_cast<double*>(d.ptr)[io_off(d, dir, jk.y, ig)] = 0.0;
       }
     }
     if (nlist == 0) continue;
-    if (tid == 0) stage_dir(a, s, seq, __ldg(a.chunk_list + nlist - 1), tile, a.adj_bits, 1);
+    // the dense variant stages instruction bytes in place of plan bytes (never read)
+    const unsigned char* plan = kDense ? reinterpret_cast<const unsigned char*>(a.t.code) : a.adj_bits;
+    if (tid == 0)
+      stage_dir(a, s, seq, kDense ? nlist - 1 : __ldg(a.chunk_list + nlist - 1), tile, plan, 1);
 #pragma unroll 1
     for (int idx = nlist - 1; idx >= 0; --idx) {
       const bool more = idx > 0;
       if (tid == 0 && more)
-        stage_dir(a, s, seq + 1, __ldg(a.chunk_list + idx - 1), tile, a.adj_bits, 1);
+        stage_dir(a, s, seq + 1, kDense ? idx - 1 : __ldg(a.chunk_list + idx - 1), tile, plan, 1);
       const bool ok = stage_wait(s.bars, seq);
       if (!__syncthreads_and(ok)) {
         stage_abort(a.t, s.bars, seq, more);
         return;
       }
-      const int c = __ldg(a.chunk_list + idx);
+      const int c = kDense ? idx : __ldg(a.chunk_list + idx);
       const u64* code = s.ring + (seq & 1u) * ch;
       const double* pb = s.pbuf + (seq & 1u) * (2 * ch * 32) + lane;
       const unsigned char* bits = s.abuf + (seq & 1u) * ch * 2;
@@ -425,7 +432,15 @@ __global__ void __launch_bounds__(32 * DW) k_adjoint(const __grid_constant__ Swe
         const u64 ins = code[k];
         const unsigned op = dec_op(ins), A = dec_a(ins), B = dec_b(ins), C = dec_c(ins);
         const unsigned m = dec_pmask(ins);
-        const unsigned f = bits[k];
+        unsigned f;
+        if (kDense) {
+          f = op == D_OUTPUT ? 32u
+                             : (op == D_NOP ? 0u
+                                            : 1u | (carries_d0(op) ? 2u : 0u) |
+                                                  (carries_d1(op) ? 4u : 0u));
+        } else {
+          f = bits[k];
+        }
         double d0 = 1.0, d1 = 0.0;
         if (m & 2u) d1 = pb[32 * --pl];
         if (m & 1u) d0 = pb[32 * --pl];
@@ -651,6 +666,18 @@ cudaError_t launch_tangent(const SweepArgs& a, int grid, cudaStream_t s) {
 cudaError_t launch_adjoint(const SweepArgs& a, int grid, cudaStream_t s) {
   const size_t smem = smem_dir(a.t.sz_w, a.block / 32, a.chunk);
   CGB_DISPATCH_DW(k_adjoint)
+}
+
+cudaError_t launch_adjoint_dense(const SweepArgs& a, int grid, cudaStream_t s) {
+  const size_t smem = smem_dir(a.t.sz_w, a.block / 32, a.chunk);
+  switch (a.block / 32) {
+    case 1: return launch_k(k_adjoint<1, true>, dim3(grid), 32, smem, a, s);
+    case 2: return launch_k(k_adjoint<2, true>, dim3(grid), 64, smem, a, s);
+    case 4: return launch_k(k_adjoint<4, true>, dim3(grid), 128, smem, a, s);
+    case 6: return launch_k(k_adjoint<6, true>, dim3(grid), 192, smem, a, s);
+    case 8: return launch_k(k_adjoint<8, true>, dim3(grid), 256, smem, a, s);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 int occupancy_primal(int block, size_t smem) {

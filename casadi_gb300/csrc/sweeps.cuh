@@ -76,6 +76,8 @@ cudaError_t launch_record(const SweepArgs& a, int grid, cudaStream_t s);
 // ceil(ndir / (block/32)); CTA b works on direction group b % groups.
 cudaError_t launch_tangent(const SweepArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_adjoint(const SweepArgs& a, int grid, cudaStream_t s);
+// The adjoint sweep without an activity plan (see k_adjoint<DW, true>).
+cudaError_t launch_adjoint_dense(const SweepArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_sp_forward(const SweepArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_sp_reverse(const SweepArgs& a, int grid, cudaStream_t s);
 

@@ -74,6 +74,7 @@ def load(path=None):
         "casadi_gb300_map_reverse": (cint, [cint, cint, i64, cint, vp, vp, vp, vp]),
         "casadi_gb300_jacobian": (cint, [cint, i64, i64, vp, vp, vp, vp, sz, vp]),
         "casadi_gb300_map_jacobian": (cint, [cint, cint, i64, vp, vp, vp]),
+        "casadi_gb300_reverse_noalloc": (cint, [cint, i64, i64, cint, vp, vp, vp, vp, vp]),
         "casadi_gb300_profile": (cint, [cint]),
         "casadi_gb300_profile_collect": (cint, [vp, vp, cint]),
     }
