@@ -56,37 +56,107 @@ def make_workload(name, instances=None):
     raise SystemExit("unknown workload " + name)
 
 
-# ---- algorithmic work per instance (FP64 arithmetic the numeric formulas require) -----------
-def algorithmic_flops(tape, weights):
-    """FP64 operations per instance for each kernel family, from the tape's op histogram.
-
-    Value of an op: 1 for +,-,*, comparisons and selects; the measured FP64-pipe weight of
-    DIV, SQRT and each libm call (op_weights.json). Tangent per direction: 3 for a binary op
-    with recorded partials (d0*a + d1*b), 1 for ADD/SUB/TWICE and unary ops. Adjoint per
-    direction: 4 for a binary op (two products, two sums), 2 for ADD/SUB and unary ops."""
+# ---- algorithmic work per instance --------------------------------------------------------------
+# Counted in FP64-pipe instructions (DADD, DMUL and DFMA each count one; a libm call counts its
+# measured DFMA-instruction equivalents from op_weights.json): that is what bounds these sweeps
+# on GB300. The ceiling in the same unit is the DFMA instruction rate, i.e. the cuBLAS DGEMM
+# FLOP/s measured in the run divided by two.
+def _carries(op):
     from casadi_gb300 import calculus as C
-    val = rec = tan = adj = 0.0
-    free = {C.OP_CONST, C.OP_INPUT, C.OP_OUTPUT}
+    zero_d0 = {C.OP_LT, C.OP_LE, C.OP_EQ, C.OP_NE, C.OP_NOT, C.OP_AND, C.OP_OR, C.OP_FLOOR,
+               C.OP_CEIL, C.OP_SIGN, C.OP_IF_ELSE_ZERO}
+    d1 = {C.OP_ADD, C.OP_SUB, C.OP_MUL, C.OP_DIV, C.OP_POW, C.OP_FMOD, C.OP_REMAINDER,
+          C.OP_FMIN, C.OP_FMAX, C.OP_ATAN2, C.OP_HYPOT, C.OP_IF_ELSE_ZERO}
+    return op not in zero_d0, op in d1
+
+
+def structural_tangent_ops(tape, unit_dirs=True, ndir=None):
+    """FP64 instructions of the forward sweep with unit seeds, summed over all directions,
+    following the structural rules the sweeps apply (same cases as the tangent kernel)."""
+    from casadi_gb300 import calculus as C
+    nz = sum(tape.nnz_in)
+    offs = np.cumsum([0] + list(tape.nnz_in))
+    ops, i0, i1, i2 = (tape.op.tolist(), tape.i0.tolist(), tape.i1.tolist(), tape.i2.tolist())
+    carry = {op: _carries(op) for op in set(ops)}
+    total = 0
+    for d in range(nz if unit_dirs else 1):
+        act = [False] * max(1, tape.sz_w)
+        for k, op in enumerate(ops):
+            if op == C.OP_INPUT:
+                act[i0[k]] = (offs[i1[k]] + i2[k] == d) if unit_dirs else True
+                continue
+            if op == C.OP_CONST:
+                act[i0[k]] = False
+                continue
+            if op == C.OP_OUTPUT:
+                continue
+            c0, c1 = carry[op]
+            cb = act[i1[k]] and c0
+            cc = op in C.BINARY_OPS and act[i2[k]] and c1
+            act[i0[k]] = cb or cc
+            if not (cb or cc):
+                continue
+            if op in (C.OP_ADD, C.OP_SUB):
+                total += 1 if (cb and cc) else 0
+            elif op == C.OP_TWICE:
+                total += 1
+            elif op in (C.OP_NEG, C.OP_ASSIGN, C.OP_IF_ELSE_ZERO):
+                pass
+            else:
+                total += 3 if (cb and cc) else 1
+    return total * (1 if unit_dirs else (ndir or 1))
+
+
+def structural_adjoint_ops(tape, seeded_out):
+    """FP64 instructions of one adjoint direction (same cases as the adjoint kernel)."""
+    from casadi_gb300 import calculus as C
+    ops, i0, i1, i2 = (tape.op.tolist(), tape.i0.tolist(), tape.i1.tolist(), tape.i2.tolist())
+    act = [False] * max(1, tape.sz_w)
+    total = 0
+    for k in range(len(ops) - 1, -1, -1):
+        op = ops[k]
+        if op == C.OP_OUTPUT:
+            if seeded_out[i0[k]]:
+                total += 1 if act[i1[k]] else 0
+                act[i1[k]] = True
+            continue
+        if op in (C.OP_INPUT, C.OP_CONST):
+            act[i0[k]] = False
+            continue
+        if not act[i0[k]]:
+            continue
+        act[i0[k]] = False
+        c0, c1 = _carries(op)
+        for slot, carries, which in ((i1[k], c0, 0), (i2[k], c1 and op in C.BINARY_OPS, 1)):
+            if not carries:
+                continue
+            first = not act[slot]
+            if op in (C.OP_ADD, C.OP_SUB, C.OP_ASSIGN, C.OP_NEG, C.OP_IF_ELSE_ZERO):
+                total += 0 if first else 1
+            elif op == C.OP_TWICE:
+                total += 1 if first else 2
+            else:
+                total += 1 if first else 2
+            act[slot] = True
+    return total
+
+
+def algorithmic_flops(tape, weights, seeded_out=None, unit_dirs=True):
+    """FP64-pipe instructions per instance for each kernel family (see above)."""
+    from casadi_gb300 import calculus as C
+    val = rec = 0.0
     for op, cnt in zip(*np.unique(tape.op, return_counts=True)):
         op = int(op)
-        if op in free:
+        if op in (C.OP_CONST, C.OP_INPUT, C.OP_OUTPUT):
             continue
         name = C.OP_NAMES[op]
         w = float(weights.get(name, 1.0))
         val += cnt * w
         rec += cnt * (w + float(weights.get(name + "_partial", 0.0)))
-        if op in (C.OP_ADD, C.OP_SUB):
-            tan += cnt * 1
-            adj += cnt * 2
-        elif op in (C.OP_NEG, C.OP_ASSIGN):
-            adj += cnt * 1
-        elif op in C.BINARY_OPS:
-            tan += cnt * 3
-            adj += cnt * 4
-        else:
-            tan += cnt * 1
-            adj += cnt * 2
-    return dict(eval=val, record=rec, tangent_per_dir=tan, adjoint_per_dir=adj)
+    seeded_out = seeded_out or [True] * len(tape.nnz_out)
+    return dict(eval=val, record=rec,
+                tangent_all_dirs=float(structural_tangent_ops(tape, unit_dirs)),
+                adjoint_per_dir=float(structural_adjoint_ops(tape, seeded_out)))
 
 
 def load_weights():
@@ -304,12 +374,11 @@ def run_native(a):
     dom = max(fam_ms, key=lambda k: fam_ms[k][0])
     dom_ms, dom_launches = fam_ms[dom]
     per_inst = {"eval": work["eval"], "record": work["record"],
-                "tangent": work["tangent_per_dir"] * (nz if a.workload == "rollout20" else 1),
-                "adjoint": work["adjoint_per_dir"]}.get(dom, 0.0)
+                "tangent": work["tangent_all_dirs"], "adjoint": work["adjoint_per_dir"]}.get(dom, 0.0)
     launches_per_step = dom_launches / a.steps
     flops_per_launch = per_inst * n / launches_per_step
     achieved = flops_per_launch / (dom_ms / dom_launches * 1e-3) / 1e12
-    peak = fp64_peak_tflops(torch)
+    peak = fp64_peak_tflops(torch) / 2.0  # DFMA instructions/s: the FP64-pipe instruction rate
     gpu_launches = sum(v[1] for v in prof.values())
     io_bytes = 8 * n * (sum(F.tape.nnz_in) + sum(F.tape.nnz_out))
 
@@ -376,7 +445,11 @@ def run_native(a):
         "kernel_ms": {k: round(v[0], 4) for k, v in prof.items() if v[1]},
         "roofline": {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
-                     "traffic": None, "peak_source": "cuBLAS FP64 GEMM measured in this run",
+                     "traffic": None,
+                     "flop": "one FP64-pipe instruction (DADD, DMUL, DFMA); libm calls weighted by "
+                             "casadi_gb300/op_weights.json; derivative sweeps count structural work",
+                     "peak_source": "cuBLAS FP64 GEMM FLOP/s measured in this run / 2 "
+                                    "(DFMA instructions per second)",
                      "io_bytes_per_step": io_bytes,
                      "hbm_gbs_io": io_bytes / (ms_step * 1e-3) / 1e9},
         "clocks": clk.summary(),

@@ -66,13 +66,11 @@ struct TanPlan {
   bool identity = false;
   std::vector<char> seeded;  // per input: seed pointer given (general seeds)
   int groups = 0;
-  unsigned short* d_bits = nullptr;
-  int* d_list = nullptr;
-  int* d_off = nullptr;
+  uint4* d_stream = nullptr;  // entry streams of all directions
+  int2* d_chunks = nullptr;   // per direction: (first entry, entry count)
   ~TanPlan() {
-    cudaFree(d_bits);
-    cudaFree(d_list);
-    cudaFree(d_off);
+    cudaFree(d_stream);
+    cudaFree(d_chunks);
   }
 };
 
@@ -80,15 +78,14 @@ struct TanPlan {
 struct AdjPlan {
   int ch = 0;
   std::vector<char> seeded;  // per output: seed pointer given
-  unsigned char* d_bits = nullptr;
-  int* d_list = nullptr;
-  int* d_off = nullptr;
+  int dw = 0;
+  uint4* d_stream = nullptr;  // entry stream
+  int2* d_chunks = nullptr;   // (first entry, entry count)
   int2* d_zero = nullptr;
   int n_zero = 0;
   ~AdjPlan() {
-    cudaFree(d_bits);
-    cudaFree(d_list);
-    cudaFree(d_off);
+    cudaFree(d_stream);
+    cudaFree(d_chunks);
     cudaFree(d_zero);
   }
 };
@@ -263,7 +260,7 @@ DirShape dir_shape(Tape& t, int ndir) {
   for (int ch : {64, 32, 16}) {
     for (int dw : {8, 6, 4, 2, 1}) {
       if (dw > 1 && dw >= 2 * ndir) continue;
-      const size_t sm = smem_dir(t.sz_w, dw, ch);
+      const size_t sm = smem_lean(t.sz_w, dw, ch);
       if (sm > static_cast<size_t>(max_smem)) continue;
       const int occ = occupancy_dir(dw, sm);
       if (occ <= 0) continue;
@@ -341,9 +338,63 @@ cudaError_t upload(T** dst, const std::vector<T>& v) {
   return cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
 }
 
+unsigned lean_kind(unsigned op) {
+  switch (op) {
+    case D_ADD: return LK_ADD;
+    case D_SUB: return LK_SUB;
+    case D_NEG: return LK_NEG;
+    case D_TWICE: return LK_TWICE;
+    case D_ASSIGN: return LK_ASSIGN;
+    case D_IF_ELSE_ZERO: return LK_IFZ;
+    case D_INPUT: return LK_INPUT;
+    case D_OUTPUT: return LK_OUTPUT;
+    case D_CONST: return LK_CONST;
+    case D_NOP: return LK_NOP;
+    default: return LK_GEN;
+  }
+}
+
+// Entry of instruction word w (flags: see the derivative sweeps); slot fields become byte
+// offsets into the warp's work vector w[slot][lane] (slot * 256).
+uint4 dir_entry(u64 w, unsigned flags, int pk) {
+  const unsigned op = dec_op(w), A = dec_a(w), B = dec_b(w), C = dec_c(w);
+  uint4 e;
+  if (op == D_INPUT) {
+    e = make_uint4(A * 256u, B, C, 0);
+  } else if (op == D_OUTPUT) {
+    e = make_uint4(A, B * 256u, C, 0);
+  } else {
+    e = make_uint4(A * 256u, B * 256u, C * 256u, 0);
+  }
+  e.w = (flags & 31u) | (lean_kind(op) << 5) | (dec_pmask(w) << 9) |
+        (static_cast<unsigned>(pk) << 11);
+  return e;
+}
+
+// Appends one stream, padded with NOP entries to whole groups; returns (first, count).
+int2 push_stream(std::vector<uint4>& all, const std::vector<uint4>& ents) {
+  const int first = static_cast<int>(all.size());
+  all.insert(all.end(), ents.begin(), ents.end());
+  while ((all.size() - first) % kEntGroup) all.push_back(make_uint4(0, 0, 0, 0));
+  return make_int2(first, static_cast<int>(all.size()) - first);
+}
+
+std::vector<int> partial_starts(const Tape& t) {
+  std::vector<int> pk(t.h_code.size());
+  int acc = 0;
+  for (size_t k = 0; k < t.h_code.size(); ++k) {
+    pk[k] = acc;
+    const unsigned op = dec_op(t.h_code[k]);
+    if (op != D_CONST && op != D_INPUT && op != D_OUTPUT && op != D_NOP)
+      acc += __builtin_popcount(partial_mask(op));
+  }
+  return pk;
+}
+
 // Structural activity of the tangent sweep, per direction: an input slot is active when it is
 // seeded (unit seeds: when it is the direction's own input nonzero), an arithmetic result
 // when an operand that carries a derivative is active (the reference's 0*x -> 0, x+0 -> x).
+// Each direction group gets a compacted entry stream of the instructions with work for it.
 const TanPlan* tan_plan(Tape& t, int ndir, int dw, int ch, bool identity,
                         const std::vector<char>& seeded, int* err) {
   std::lock_guard<std::mutex> lk(t.shape_mtx);
@@ -388,30 +439,32 @@ const TanPlan* tan_plan(Tape& t, int ndir, int dw, int ch, bool identity,
         b = (cb ? 1u : 0u) | (cc ? 2u : 0u);
       }
       if (!b) continue;
-      if (identity) {
-        bits[static_cast<size_t>(d / dw) * nc + k] |= static_cast<unsigned short>(b << (2 * (d % dw)));
-      } else {
-        for (int dd = 0; dd < ndir; ++dd)
-          bits[static_cast<size_t>(dd / dw) * nc + k] |=
-              static_cast<unsigned short>(b << (2 * (dd % dw)));
-      }
+      for (int dd = identity ? d : 0; dd < (identity ? d + 1 : ndir); ++dd)
+        bits[static_cast<size_t>(dd / dw) * nc + k] |=
+            static_cast<unsigned short>(b << (2 * (dd % dw)));
     }
   }
-  std::vector<int> list, offs(1, 0);
-  for (int g = 0; g < p->groups; ++g) {
-    for (size_t c = 0; c < nc / ch; ++c) {
-      bool need = false;
-      for (int k = 0; k < ch && !need; ++k) {
-        const size_t kk = c * ch + k;
-        need = bits[g * nc + kk] != 0 || dec_op(t.h_code[kk]) == D_OUTPUT;
-      }
-      if (need) list.push_back(static_cast<int>(c));
+  const std::vector<int> pk = partial_starts(t);
+  std::vector<uint4> all;
+  std::vector<int2> se(ndir);
+  for (int d = 0; d < ndir; ++d) {
+    if (!identity && d > 0) {
+      se[d] = se[0];  // general seeds: one stream serves every direction
+      continue;
     }
-    offs.push_back(static_cast<int>(list.size()));
+    std::vector<uint4> ents;
+    const size_t g = static_cast<size_t>(d / dw), sh = 2 * (d % dw);
+    for (size_t k = 0; k < nc; ++k) {
+      const unsigned op = dec_op(t.h_code[k]);
+      const unsigned b = (bits[g * nc + k] >> sh) & 3u;
+      if (!b && op != D_OUTPUT) continue;
+      ents.push_back(dir_entry(t.h_code[k], b, pk[k]));
+    }
+    se[d] = push_stream(all, ents);
   }
   cudaError_t e;
-  if ((e = upload(&p->d_bits, bits)) != cudaSuccess || (e = upload(&p->d_list, list)) != cudaSuccess ||
-      (e = upload(&p->d_off, offs)) != cudaSuccess) {
+  if ((e = upload(&p->d_stream, all)) != cudaSuccess ||
+      (e = upload(&p->d_chunks, se)) != cudaSuccess) {
     *err = cuda_fail(e, "upload tangent plan");
     return nullptr;
   }
@@ -421,13 +474,15 @@ const TanPlan* tan_plan(Tape& t, int ndir, int dw, int ch, bool identity,
 
 // Structural activity of the adjoint sweep (direction-independent), last instruction first.
 // Flags: 1 adjoint of the result is nonzero, 2/4 operand b/c receives a contribution,
-// 8/16 that contribution is the first to b/c, 32 a seeded output.
-const AdjPlan* adj_plan(Tape& t, int ch, const std::vector<char>& seeded, int* err) {
+// 8/16 that contribution is the first to b/c, 32 a seeded output. Entries without work are
+// left out of the stream; inputs whose adjoint is structurally zero go to the zero list.
+const AdjPlan* adj_plan(Tape& t, int dw, int ch, const std::vector<char>& seeded, int* err) {
   std::lock_guard<std::mutex> lk(t.shape_mtx);
   for (auto& p : t.adj_plans)
-    if (p->ch == ch && p->seeded == seeded) return p.get();
+    if (p->ch == ch && p->dw == dw && p->seeded == seeded) return p.get();
   auto p = std::make_unique<AdjPlan>();
   p->ch = ch;
+  p->dw = dw;
   p->seeded = seeded;
   const size_t nc = t.h_code.size();
   std::vector<unsigned char> bits(nc, 0);
@@ -469,17 +524,17 @@ const AdjPlan* adj_plan(Tape& t, int ch, const std::vector<char>& seeded, int* e
     }
     bits[kk] = static_cast<unsigned char>(f);
   }
-  std::vector<int> list, offs(1, 0);
-  for (size_t c = 0; c < nc / ch; ++c) {
-    bool need = false;
-    for (int k = 0; k < ch && !need; ++k) need = bits[c * ch + k] != 0;
-    if (need) list.push_back(static_cast<int>(c));
+  const std::vector<int> pk = partial_starts(t);
+  std::vector<uint4> ents, all;
+  for (size_t k = 0; k < nc; ++k) {
+    if (!bits[k]) continue;
+    ents.push_back(dir_entry(t.h_code[k], bits[k] & 31u, pk[k]));
   }
-  offs.push_back(static_cast<int>(list.size()));
+  std::vector<int2> se = {push_stream(all, ents)};
   p->n_zero = static_cast<int>(zero.size());
   cudaError_t e;
-  if ((e = upload(&p->d_bits, bits)) != cudaSuccess || (e = upload(&p->d_list, list)) != cudaSuccess ||
-      (e = upload(&p->d_off, offs)) != cudaSuccess || (e = upload(&p->d_zero, zero)) != cudaSuccess) {
+  if ((e = upload(&p->d_stream, all)) != cudaSuccess ||
+      (e = upload(&p->d_chunks, se)) != cudaSuccess || (e = upload(&p->d_zero, zero)) != cudaSuccess) {
     *err = cuda_fail(e, "upload adjoint plan");
     return nullptr;
   }
@@ -498,8 +553,18 @@ int run_ad(Tape& t, long long n, const IoDesc* in, const IoDesc* out, const IoDe
     return fail(CASADI_GB300_ERR_SCRATCH,
                 "scratch of %zu bytes is below the minimum of %lld bytes for this tape",
                 scratch_bytes, 32ll * 8ll * t.n_partials);
-  const DirShape ds = dir_shape(t, std::max(ndir, 1));
-  const int groups = (ndir + ds.dw - 1) / ds.dw;
+  // derivative sweeps: one-warp CTAs, as many per SM as the work vector allows
+  DirShape ds;
+  ds.dw = 1;
+  ds.ch = 0;
+  const size_t dsmem = smem_lean(t.sz_w, 1, 0);
+  if (ndir > 0 && dsmem > static_cast<size_t>(max_smem_optin()))
+    return fail(CASADI_GB300_ERR_UNSUPPORTED,
+                "work vector of %d slots does not fit the derivative sweeps' shared memory", t.sz_w);
+  if (ndir > 0 && static_cast<unsigned>(t.n_partials) >= kMaxPartials)
+    return fail(CASADI_GB300_ERR_UNSUPPORTED, "tape records %d partials per instance (max %u)",
+                t.n_partials, kMaxPartials - 1);
+  ds.blocks_per_sm = ndir > 0 ? std::max(1, occupancy_dir(1, dsmem)) : 1;
   const int sms = sm_count();
   const TanPlan* tp = nullptr;
   const AdjPlan* ap = nullptr;
@@ -508,7 +573,7 @@ int run_ad(Tape& t, long long n, const IoDesc* in, const IoDesc* out, const IoDe
     if (adjoint) {
       std::vector<char> seeded(t.n_out);
       for (int j = 0; j < t.n_out; ++j) seeded[j] = seed[j].ptr != nullptr;
-      ap = adj_plan(t, ds.ch, seeded, &err);
+      ap = adj_plan(t, ds.dw, ds.ch, seeded, &err);
     } else {
       std::vector<char> seeded(t.n_in);
       for (int j = 0; j < t.n_in; ++j) seeded[j] = seed[j].ptr != nullptr;
@@ -538,20 +603,17 @@ int run_ad(Tape& t, long long n, const IoDesc* in, const IoDesc* out, const IoDe
       a.block = 32 * ds.dw;
       a.chunk = ds.ch;
       if (tp) {
-        a.tan_bits = tp->d_bits;
-        a.chunk_list = tp->d_list;
-        a.chunk_list_off = tp->d_off;
+        a.dstream = tp->d_stream;
+        a.dchunks = tp->d_chunks;
       } else {
-        a.adj_bits = ap->d_bits;
-        a.chunk_list = ap->d_list;
-        a.chunk_list_off = ap->d_off;
+        a.dstream = ap->d_stream;
+        a.dchunks = ap->d_chunks;
         a.zero_in = ap->d_zero;
         a.n_zero = ap->n_zero;
       }
-      const long long tiles = (m + 31) / 32;
-      const long long per_group = std::max<long long>(
-          1, std::min<long long>(tiles, static_cast<long long>(sms) * ds.blocks_per_sm / groups));
-      const int grid = static_cast<int>(per_group * groups);
+      const long long work = (m + 31) / 32 * ndir;
+      const int grid = static_cast<int>(
+          std::max<long long>(1, std::min<long long>(work, static_cast<long long>(sms) * ds.blocks_per_sm)));
       e = timed(adjoint ? F_ADJOINT : F_TANGENT, s, [&] {
         return adjoint ? launch_adjoint(a, grid, s) : launch_tangent(a, grid, s);
       });
@@ -1119,7 +1181,7 @@ DirShape noalloc_shape(const Tape& t, int ndir) {
       if (dw > 1 && dw >= 2 * ndir) continue;
       const size_t sm = smem_dir(t.sz_w, dw, ch);
       if (sm > static_cast<size_t>(max_smem)) continue;
-      const int occ = occupancy_dir(dw, sm);
+      const int occ = occupancy_dense(dw, sm);
       if (occ <= 0) continue;
       const int groups = (ndir + dw - 1) / dw;
       const double used = static_cast<double>(ndir) / (groups * dw);

@@ -119,6 +119,10 @@ __device__ __forceinline__ double d_neg(double x) {
 __device__ __forceinline__ double d_fabs(double x) {
   return __longlong_as_double(__double_as_longlong(x) & (long long)~kSignBit);
 }
+// x == 0.0 (either sign) on the bit pattern, without an FP64 comparison
+__device__ __forceinline__ bool d_iszero(double x) {
+  return (__double_as_longlong(x) & (long long)~kSignBit) == 0;
+}
 __device__ __forceinline__ bool d_isnan(double x) {
   return (__double_as_longlong(x) & (long long)~kSignBit) > 0x7ff0000000000000ll;
 }

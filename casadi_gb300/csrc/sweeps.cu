@@ -279,103 +279,12 @@ __device__ __forceinline__ void stage_dir(const SweepArgs& a, const DirSmem& s, 
              bar);
 }
 
-// w'[i0] = d0*w'[i1] + d1*w'[i2] over the operands that carry a derivative
-// (sx_function.cpp:1280-1363 with the reference's structural simplifications).
-template <int DW>
-__global__ void __launch_bounds__(32 * DW) k_tangent(const __grid_constant__ SweepArgs a) {
-  constexpr int BS = 32 * DW;
-  extern __shared__ __align__(128) unsigned char smem[];
-  const DirSmem s = dir_smem(smem, a.chunk);
-  double* wd = s.wd;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid == 0) stage_init(s.bars);
-  __syncthreads();
-  const int ngroups = (a.ndir + DW - 1) / DW;
-  const int group = blockIdx.x % ngroups;
-  const long long dir = static_cast<long long>(group) * DW + warp;
-  const bool dir_ok = dir < a.ndir;
-  const int ch = a.chunk;
-  const int* clist = a.chunk_list + __ldg(a.chunk_list_off + group);
-  const int nlist = __ldg(a.chunk_list_off + group + 1) - __ldg(a.chunk_list_off + group);
-  const unsigned char* plan =
-      reinterpret_cast<const unsigned char*>(a.tan_bits + static_cast<size_t>(group) * a.n_code);
-  const unsigned shift = 2u * warp;
-  const long long ntiles = (a.n + 31) / 32;
-  const long long tstride = gridDim.x / ngroups;
-  unsigned seq = 0;
-  if (nlist == 0) return;
-  for (long long tile = blockIdx.x / ngroups; tile < ntiles; tile += tstride) {
-    const long long il = tile * 32 + lane;
-    const bool active = il < a.n && dir_ok;
-    const long long ig = a.i_begin + il;
-    if (tid == 0) stage_dir(a, s, seq, __ldg(clist), tile, plan, 2);
-#pragma unroll 1
-    for (int idx = 0; idx < nlist; ++idx) {
-      const bool more = idx + 1 < nlist;
-      if (tid == 0 && more) stage_dir(a, s, seq + 1, __ldg(clist + idx + 1), tile, plan, 2);
-      const bool ok = stage_wait(s.bars, seq);
-      if (!__syncthreads_and(ok)) {
-        stage_abort(a.t, s.bars, seq, more);
-        return;
-      }
-      const u64* code = s.ring + (seq & 1u) * ch;
-      const double* pb = s.pbuf + (seq & 1u) * (2 * ch * 32) + lane;
-      const unsigned short* bits =
-          reinterpret_cast<const unsigned short*>(s.abuf + (seq & 1u) * ch * 2);
-      int pl = 0;
-#pragma unroll 1
-      for (int k = 0; k < ch; ++k) {
-        const u64 ins = code[k];
-        const unsigned op = dec_op(ins), A = dec_a(ins), B = dec_b(ins), C = dec_c(ins);
-        const unsigned m = dec_pmask(ins);
-        const unsigned ab = (bits[k] >> shift) & 3u;
-        double d0 = 1.0, d1 = 0.0;
-        if (m & 1u) d0 = pb[32 * pl++];
-        if (m & 2u) d1 = pb[32 * pl++];
-        if (op == D_OUTPUT) {
-          const IoDesc& d = a.sens[A];
-          if (active && d.ptr)
-            static_cast<double*>(d.ptr)[io_off(d, dir, C, ig)] = (ab & 1u) ? wd[B * BS + tid] : 0.0;
-          continue;
-        }
-        if (!ab) continue;  // structurally zero for this direction
-        double r;
-        if (op == D_INPUT) {
-          r = 1.0;
-          if (!a.identity_seed) {
-            const IoDesc& d = a.seed[B];
-            r = active ? __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir, C, ig)) : 0.0;
-          }
-        } else {
-          const bool cb = ab & 1u, cc = ab & 2u;
-          const double xb = cb ? wd[B * BS + tid] : 0.0;
-          const double xc = cc ? wd[C * BS + tid] : 0.0;
-          switch (op) {
-            case D_ADD: r = cb && cc ? __dadd_rn(xb, xc) : (cb ? xb : xc); break;
-            case D_SUB: r = cb && cc ? __dsub_rn(xb, xc) : (cb ? xb : d_neg(xc)); break;
-            case D_NEG: r = d_neg(xb); break;
-            case D_TWICE: r = __dadd_rn(xb, xb); break;
-            case D_ASSIGN: r = xb; break;
-            case D_IF_ELSE_ZERO: r = d1 == 0.0 ? 0.0 : xc; break;
-            default:
-              r = cb && cc ? __dadd_rn(__dmul_rn(d0, xb), __dmul_rn(d1, xc))
-                           : (cb ? __dmul_rn(d0, xb) : __dmul_rn(d1, xc));
-          }
-        }
-        wd[A * BS + tid] = r;
-      }
-      __syncthreads();
-      ++seq;
-    }
-  }
-}
-
-// seed = w'[i0]; w'[i0] = 0; w'[i1] += d0*seed; w'[i2] += d1*seed (sx_function.cpp:1454-1560),
-// with structurally zero adjoints skipped and first contributions assigned (0 + x -> x).
-// kDense: the variant without an activity plan (every chunk, every instruction active,
-// contributions always added to a zeroed adjoint); it needs no plan memory.
-template <int DW, bool kDense = false>
-__global__ void __launch_bounds__(32 * DW) k_adjoint(const __grid_constant__ SweepArgs a) {
+// Adjoint sweep over the 8-byte instruction stream (seed = w'[i0]; w'[i0] = 0;
+// w'[i1] += d0*seed; w'[i2] += d1*seed, sx_function.cpp:1454-1560). With kDense it needs no
+// activity plan (every chunk, every instruction active, contributions always added to a
+// zeroed adjoint) and so no plan memory; the allocation-free entry point uses that variant.
+template <int DW, bool kDense>
+__global__ void __launch_bounds__(32 * DW) k_adjoint_tape(const __grid_constant__ SweepArgs a) {
   constexpr int BS = 32 * DW;
   extern __shared__ __align__(128) unsigned char smem[];
   const DirSmem s = dir_smem(smem, a.chunk);
@@ -496,6 +405,280 @@ __global__ void __launch_bounds__(32 * DW) k_adjoint(const __grid_constant__ Swe
 }
 
 // ---------------------------------------------------------------------------------------------
+// Derivative sweeps, warp-independent.
+//
+// Each warp owns one (32-instance tile, direction) work item at a time and walks its own
+// host-compiled entry stream: for the tangent sweep the stream of its direction (only the
+// instructions whose derivative is structurally nonzero for that direction, plus outputs),
+// for the adjoint sweep the one stream of instructions with a nonzero adjoint. Warps never
+// wait for each other, so a sparse direction finishes early instead of waiting for a dense
+// one. Entries and recorded partials are loaded straight from global memory (L2-resident,
+// one coalesced 256-byte request per partial) and software-pipelined through registers:
+// entries two groups of kGroup ahead, partials one group ahead. Shared memory holds only
+// the work vector, w[slot][lane], so as many warps fit as the work vector allows.
+//
+// Entry: {a, b, c, meta}; a/b/c are slot byte offsets (slot*256) or I/O indices; meta bits
+// 0-4 flags (tangent: 1/2 operand b/c carries a derivative; adjoint: 2/4 operand b/c
+// receives a contribution, 8/16 it is the first one), 5-8 kind, 9-10 recorded-partial mask,
+// 11-31 index of the instruction's first recorded partial.
+// ---------------------------------------------------------------------------------------------
+constexpr int kGroup = 8;
+
+__device__ __forceinline__ double& wreg(unsigned char* base, unsigned off) {
+  return *reinterpret_cast<double*>(base + off);
+}
+
+// meta layout shared by both streams
+__host__ __device__ __forceinline__ unsigned ent_flags(unsigned m) { return m & 31u; }
+__host__ __device__ __forceinline__ unsigned ent_kind(unsigned m) { return (m >> 5) & 15u; }
+__host__ __device__ __forceinline__ unsigned ent_pmask(unsigned m) { return (m >> 9) & 3u; }
+__host__ __device__ __forceinline__ unsigned ent_pk(unsigned m) { return m >> 11; }
+
+// Load the partials of one group of entries (d0 at pk, d1 at pk+1 or pk).
+__device__ __forceinline__ void load_partials(const uint4 (&E)[kGroup], const double* pt,
+                                              double (&P0)[kGroup], double (&P1)[kGroup]) {
+#pragma unroll
+  for (int i = 0; i < kGroup; ++i) {
+    const unsigned m = ent_pmask(E[i].w);
+    const size_t pk = ent_pk(E[i].w);
+    P0[i] = (m & 1u) ? __ldg(pt + pk * 32) : 1.0;
+    P1[i] = (m & 2u) ? __ldg(pt + (pk + ((m & 1u) ? 1 : 0)) * 32) : 0.0;
+  }
+}
+
+__device__ __forceinline__ void load_group(const uint4* st, int g, int ngr, uint4 (&E)[kGroup]) {
+#pragma unroll
+  for (int i = 0; i < kGroup; ++i)
+    E[i] = g < ngr ? __ldg(st + g * kGroup + i) : make_uint4(0, 0, 0, 0);
+}
+
+template <int DW>
+__global__ void __launch_bounds__(32 * DW) k_tangent(const __grid_constant__ SweepArgs a) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned char* wb = smem + static_cast<size_t>(warp) * a.t.sz_w * 256 + lane * 8;
+  const long long ntiles = (a.n + 31) / 32;
+  const long long nwork = ntiles * a.ndir;
+  const long long wstride = static_cast<long long>(gridDim.x) * DW;
+  for (long long work = static_cast<long long>(blockIdx.x) * DW + warp; work < nwork;
+       work += wstride) {
+    const long long tile = work / a.ndir;
+    const int dir = static_cast<int>(work % a.ndir);
+    const long long il = tile * 32 + lane;
+    const bool active = il < a.n;
+    const long long ig = a.i_begin + il;
+    const int2 se = __ldg(a.dchunks + dir);  // (first entry, entry count) of this direction
+    const uint4* st = a.dstream + se.x;
+    const int ngr = se.y / kGroup;
+    const double* pt = a.partials + static_cast<size_t>(tile) * a.t.n_partials * 32 + lane;
+    uint4 E0[kGroup], E1[kGroup];
+    double P0[kGroup], Q0[kGroup];
+    load_group(st, 0, ngr, E0);
+    load_group(st, 1, ngr, E1);
+    load_partials(E0, pt, P0, Q0);
+#pragma unroll 1
+    for (int g = 0; g < ngr; ++g) {
+      uint4 E2[kGroup];
+      double P1[kGroup], Q1[kGroup];
+      load_group(st, g + 2, ngr, E2);
+      load_partials(E1, pt, P1, Q1);
+#pragma unroll
+      for (int i = 0; i < kGroup; ++i) {
+        const uint4 cur = E0[i];
+        const unsigned meta = cur.w;
+        // one jump-table dispatch on (kind, active operands): every case holds only the FP64
+        // operations it needs, so nothing is computed speculatively (an FP64 instruction holds
+        // a sub-partition's FP64 unit for ~64 cycles on GB300)
+        const unsigned key = (ent_kind(meta) << 2) | (ent_flags(meta) & 3u);
+        double r;
+        switch (key) {
+          case (LK_OUTPUT << 2) | 0u:
+          case (LK_OUTPUT << 2) | 1u: {
+            const IoDesc& d = a.sens[cur.x];
+            if (active && d.ptr)
+              static_cast<double*>(d.ptr)[io_off(d, dir, cur.z, ig)] =
+                  (meta & 1u) ? wreg(wb, cur.y) : 0.0;
+            continue;
+          }
+          case (LK_INPUT << 2) | 1u:
+            if (a.identity_seed) {
+              r = 1.0;
+            } else {
+              const IoDesc& d = a.seed[cur.y];
+              r = active ? __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir, cur.z, ig)) : 0.0;
+            }
+            break;
+          case (LK_GEN << 2) | 1u: r = __dmul_rn(P0[i], wreg(wb, cur.y)); break;
+          case (LK_GEN << 2) | 2u: r = __dmul_rn(Q0[i], wreg(wb, cur.z)); break;
+          case (LK_GEN << 2) | 3u:
+            r = __dadd_rn(__dmul_rn(P0[i], wreg(wb, cur.y)), __dmul_rn(Q0[i], wreg(wb, cur.z)));
+            break;
+          case (LK_ADD << 2) | 1u: r = wreg(wb, cur.y); break;
+          case (LK_ADD << 2) | 2u: r = wreg(wb, cur.z); break;
+          case (LK_ADD << 2) | 3u: r = __dadd_rn(wreg(wb, cur.y), wreg(wb, cur.z)); break;
+          case (LK_SUB << 2) | 1u: r = wreg(wb, cur.y); break;
+          case (LK_SUB << 2) | 2u: r = d_neg(wreg(wb, cur.z)); break;
+          case (LK_SUB << 2) | 3u: r = __dsub_rn(wreg(wb, cur.y), wreg(wb, cur.z)); break;
+          case (LK_NEG << 2) | 1u: r = d_neg(wreg(wb, cur.y)); break;
+          case (LK_TWICE << 2) | 1u: {
+            const double xb = wreg(wb, cur.y);
+            r = __dadd_rn(xb, xb);
+          } break;
+          case (LK_ASSIGN << 2) | 1u: r = wreg(wb, cur.y); break;
+          case (LK_IFZ << 2) | 2u: r = d_iszero(Q0[i]) ? 0.0 : wreg(wb, cur.z); break;
+          default:
+            continue;  // NOP padding
+        }
+        wreg(wb, cur.x) = r;
+      }
+#pragma unroll
+      for (int i = 0; i < kGroup; ++i) {
+        E0[i] = E1[i];
+        E1[i] = E2[i];
+        P0[i] = P1[i];
+        Q0[i] = Q1[i];
+      }
+    }
+  }
+}
+
+// Flags (bits 0-4): 2/4 operand b/c receives a contribution, 8/16 it is the first one
+// (1 marks an entry with work; outputs carry 8 when their seed is the slot's first).
+template <int DW>
+__global__ void __launch_bounds__(32 * DW) k_adjoint(const __grid_constant__ SweepArgs a) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned char* wb = smem + static_cast<size_t>(warp) * a.t.sz_w * 256 + lane * 8;
+  const long long ntiles = (a.n + 31) / 32;
+  const long long nwork = ntiles * a.ndir;
+  const long long wstride = static_cast<long long>(gridDim.x) * DW;
+  const int2 se = __ldg(a.dchunks);
+  const int ngr = se.y / kGroup;
+  const uint4* st = a.dstream + se.x;
+  for (int q = 0; q < a.t.sz_w; ++q) wreg(wb, q * 256) = 0.0;
+  for (long long work = static_cast<long long>(blockIdx.x) * DW + warp; work < nwork;
+       work += wstride) {
+    const long long tile = work / a.ndir;
+    const int dir = static_cast<int>(work % a.ndir);
+    const long long il = tile * 32 + lane;
+    const bool active = il < a.n;
+    const long long ig = a.i_begin + il;
+    if (active) {
+      // input nonzeros whose adjoint is structurally zero (or never read) get a zero
+      for (int k = 0; k < a.n_zero; ++k) {
+        const int2 jk = __ldg(a.zero_in + k);
+        const IoDesc& d = a.sens[jk.x];
+        if (d.ptr) static_cast<double*>(d.ptr)[io_off(d, dir, jk.y, ig)] = 0.0;
+      }
+    }
+    const double* pt = a.partials + static_cast<size_t>(tile) * a.t.n_partials * 32 + lane;
+    uint4 E0[kGroup], E1[kGroup];
+    double P0[kGroup], Q0[kGroup];
+    load_group(st, ngr - 1, ngr, E0);
+    load_group(st, ngr - 2 >= 0 ? ngr - 2 : ngr, ngr, E1);
+    load_partials(E0, pt, P0, Q0);
+#pragma unroll 1
+    for (int g = ngr - 1; g >= 0; --g) {
+      uint4 E2[kGroup];
+      double P1[kGroup], Q1[kGroup];
+      load_group(st, g - 2 >= 0 ? g - 2 : ngr, ngr, E2);
+      load_partials(E1, pt, P1, Q1);
+#pragma unroll
+      for (int i = kGroup - 1; i >= 0; --i) {
+        const uint4 cur = E0[i];
+        const unsigned meta = cur.w;
+        const unsigned f = ent_flags(meta);
+        const unsigned kind = ent_kind(meta);
+        // first contributions are assigned (0 + x -> x); dispatch on (kind, flags) so only the
+        // FP64 operations a case needs are issued
+        switch (kind) {
+          case LK_OUTPUT: {
+            const IoDesc& d = a.seed[cur.x];
+            const double sd =
+                active ? __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir, cur.z, ig)) : 0.0;
+            double& w = wreg(wb, cur.y);
+            if (f & 8u) w = sd; else w = __dadd_rn(w, sd);
+          } break;
+          case LK_INPUT: {
+            const IoDesc& d = a.sens[cur.y];
+            if (active && d.ptr)
+              static_cast<double*>(d.ptr)[io_off(d, dir, cur.z, ig)] = wreg(wb, cur.x);
+            wreg(wb, cur.x) = 0.0;
+          } break;
+          case LK_CONST:
+            wreg(wb, cur.x) = 0.0;
+            break;
+          case LK_NOP:
+            break;
+          default: {
+            const double seed = wreg(wb, cur.x);
+            wreg(wb, cur.x) = 0.0;
+            // contribution to operand b
+            switch ((kind << 2) | ((f >> 1) & 1u) | ((f >> 2) & 2u)) {  // (kind, b?, first?)
+              case (LK_GEN << 2) | 1u: {
+                double& w1 = wreg(wb, cur.y);
+                w1 = __dadd_rn(w1, __dmul_rn(P0[i], seed));
+              } break;
+              case (LK_GEN << 2) | 3u: wreg(wb, cur.y) = __dmul_rn(P0[i], seed); break;
+              case (LK_ADD << 2) | 1u: case (LK_SUB << 2) | 1u: case (LK_ASSIGN << 2) | 1u: {
+                double& w1 = wreg(wb, cur.y);
+                w1 = __dadd_rn(w1, seed);
+              } break;
+              case (LK_ADD << 2) | 3u: case (LK_SUB << 2) | 3u: case (LK_ASSIGN << 2) | 3u:
+                wreg(wb, cur.y) = seed;
+                break;
+              case (LK_NEG << 2) | 1u: {
+                double& w1 = wreg(wb, cur.y);
+                w1 = __dsub_rn(w1, seed);
+              } break;
+              case (LK_NEG << 2) | 3u: wreg(wb, cur.y) = d_neg(seed); break;
+              case (LK_TWICE << 2) | 1u: {
+                double& w1 = wreg(wb, cur.y);
+                w1 = __dadd_rn(w1, __dadd_rn(seed, seed));
+              } break;
+              case (LK_TWICE << 2) | 3u: wreg(wb, cur.y) = __dadd_rn(seed, seed); break;
+              default: break;  // operand b receives nothing
+            }
+            // contribution to operand c
+            switch ((kind << 2) | ((f >> 2) & 1u) | ((f >> 3) & 2u)) {  // (kind, c?, first?)
+              case (LK_GEN << 2) | 1u: {
+                double& w2 = wreg(wb, cur.z);
+                w2 = __dadd_rn(w2, __dmul_rn(Q0[i], seed));
+              } break;
+              case (LK_GEN << 2) | 3u: wreg(wb, cur.z) = __dmul_rn(Q0[i], seed); break;
+              case (LK_ADD << 2) | 1u: {
+                double& w2 = wreg(wb, cur.z);
+                w2 = __dadd_rn(w2, seed);
+              } break;
+              case (LK_ADD << 2) | 3u: wreg(wb, cur.z) = seed; break;
+              case (LK_SUB << 2) | 1u: {
+                double& w2 = wreg(wb, cur.z);
+                w2 = __dsub_rn(w2, seed);
+              } break;
+              case (LK_SUB << 2) | 3u: wreg(wb, cur.z) = d_neg(seed); break;
+              case (LK_IFZ << 2) | 1u: {
+                double& w2 = wreg(wb, cur.z);
+                if (!d_iszero(Q0[i])) w2 = __dadd_rn(w2, seed);
+                else w2 = __dadd_rn(w2, 0.0);
+              } break;
+              case (LK_IFZ << 2) | 3u: wreg(wb, cur.z) = d_iszero(Q0[i]) ? 0.0 : seed; break;
+              default: break;  // operand c receives nothing
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < kGroup; ++i) {
+        E0[i] = E1[i];
+        E1[i] = E2[i];
+        P0[i] = P1[i];
+        Q0[i] = Q1[i];
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
 // bvec_t sparsity sweeps (uint64 bit sets, 64 directions at once).
 // ---------------------------------------------------------------------------------------------
 template <int BS>
@@ -594,6 +777,11 @@ __global__ void __launch_bounds__(BS) k_sp_reverse(const __grid_constant__ Sweep
 size_t smem_primal(int sz_w, int block) {
   return kHeaderBytes + static_cast<size_t>(sz_w > 0 ? sz_w : 1) * block * 8;
 }
+size_t smem_lean(int sz_w, int dir_warps, int chunk) {
+  (void)chunk;
+  return static_cast<size_t>(sz_w > 0 ? sz_w : 1) * 32 * dir_warps * 8;
+}
+
 size_t smem_dir(int sz_w, int dir_warps, int chunk) {
   return dir_header_bytes(chunk) + static_cast<size_t>(sz_w > 0 ? sz_w : 1) * 32 * dir_warps * 8;
 }
@@ -659,23 +847,23 @@ cudaError_t launch_sp_reverse(const SweepArgs& a, int grid, cudaStream_t s) {
   }
 
 cudaError_t launch_tangent(const SweepArgs& a, int grid, cudaStream_t s) {
-  const size_t smem = smem_dir(a.t.sz_w, a.block / 32, a.chunk);
+  const size_t smem = smem_lean(a.t.sz_w, a.block / 32, a.chunk);
   CGB_DISPATCH_DW(k_tangent)
 }
 
 cudaError_t launch_adjoint(const SweepArgs& a, int grid, cudaStream_t s) {
-  const size_t smem = smem_dir(a.t.sz_w, a.block / 32, a.chunk);
+  const size_t smem = smem_lean(a.t.sz_w, a.block / 32, a.chunk);
   CGB_DISPATCH_DW(k_adjoint)
 }
 
 cudaError_t launch_adjoint_dense(const SweepArgs& a, int grid, cudaStream_t s) {
   const size_t smem = smem_dir(a.t.sz_w, a.block / 32, a.chunk);
   switch (a.block / 32) {
-    case 1: return launch_k(k_adjoint<1, true>, dim3(grid), 32, smem, a, s);
-    case 2: return launch_k(k_adjoint<2, true>, dim3(grid), 64, smem, a, s);
-    case 4: return launch_k(k_adjoint<4, true>, dim3(grid), 128, smem, a, s);
-    case 6: return launch_k(k_adjoint<6, true>, dim3(grid), 192, smem, a, s);
-    case 8: return launch_k(k_adjoint<8, true>, dim3(grid), 256, smem, a, s);
+    case 1: return launch_k(k_adjoint_tape<1, true>, dim3(grid), 32, smem, a, s);
+    case 2: return launch_k(k_adjoint_tape<2, true>, dim3(grid), 64, smem, a, s);
+    case 4: return launch_k(k_adjoint_tape<4, true>, dim3(grid), 128, smem, a, s);
+    case 6: return launch_k(k_adjoint_tape<6, true>, dim3(grid), 192, smem, a, s);
+    case 8: return launch_k(k_adjoint_tape<8, true>, dim3(grid), 256, smem, a, s);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -713,6 +901,17 @@ static int occ_of(K kernel, int block, size_t smem) {
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, block, smem) != cudaSuccess)
     return 0;
   return n;
+}
+
+int occupancy_dense(int dir_warps, size_t smem) {
+  switch (dir_warps) {
+    case 1: return occ_of(k_adjoint_tape<1, true>, 32, smem);
+    case 2: return occ_of(k_adjoint_tape<2, true>, 64, smem);
+    case 4: return occ_of(k_adjoint_tape<4, true>, 128, smem);
+    case 6: return occ_of(k_adjoint_tape<6, true>, 192, smem);
+    case 8: return occ_of(k_adjoint_tape<8, true>, 256, smem);
+    default: return 0;
+  }
 }
 
 int occupancy_dir(int dir_warps, size_t smem) {

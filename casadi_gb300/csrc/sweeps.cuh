@@ -9,6 +9,15 @@ namespace cgb {
 
 constexpr int kChunk = 256;      // instructions per staged chunk (2 KiB), value sweeps
 constexpr int kPofsGran = 16;    // granularity of the per-chunk partial offsets
+constexpr int kLeanPB = 63;      // partials per staged chunk block (plan-free adjoint)
+constexpr int kEntGroup = 8;     // entries per software-pipelined group (derivative sweeps)
+constexpr unsigned kMaxPartials = 1u << 21;  // recorded partials per instance the entries address
+
+// Entry kinds of the lean derivative streams (bits 16-19 of an entry's meta word).
+enum LeanKind : unsigned {
+  LK_NOP = 0, LK_GEN, LK_ADD, LK_SUB, LK_NEG, LK_TWICE, LK_ASSIGN, LK_IFZ, LK_INPUT, LK_OUTPUT,
+  LK_CONST
+};
 constexpr int kMaxIo = 64;       // inputs/outputs per tape handled by one launch
 constexpr int kDirWarps = 4;     // directions per CTA in the derivative sweeps (one per warp)
 
@@ -59,6 +68,10 @@ struct SweepArgs {
   const int* chunk_list_off;        // offsets into chunk_list, groups + 1 entries
   const int2* zero_in;              // adjoint: (input, nonzero) pairs with a zero sensitivity
   int n_zero;
+  // derivative entry streams (host-compiled; see the derivative sweeps)
+  const uint4* dstream;             // entries of all streams
+  const int2* dchunks;              // per direction (tangent) or one (adjoint): first entry, count
+  const int* dchunk_off;            // unused by the warp-independent sweeps
 };
 
 // Error bits written to TapeView::err.
@@ -67,7 +80,8 @@ constexpr int kErrBadOpcode = 2;     // an instruction with an unknown opcode wa
 
 // Shared memory a launch needs (bytes).
 size_t smem_primal(int sz_w, int block);
-size_t smem_dir(int sz_w, int dir_warps, int chunk);
+size_t smem_dir(int sz_w, int dir_warps, int chunk);   // plan-free adjoint (8-byte stream)
+size_t smem_lean(int sz_w, int dir_warps, int chunk);  // lean tangent / adjoint
 int max_smem_optin();
 
 cudaError_t launch_eval(const SweepArgs& a, int grid, cudaStream_t s);
@@ -83,6 +97,7 @@ cudaError_t launch_sp_reverse(const SweepArgs& a, int grid, cudaStream_t s);
 
 // Resident CTAs per SM for a given kernel family and shared-memory footprint.
 int occupancy_primal(int block, size_t smem);
-int occupancy_dir(int dir_warps, size_t smem);
+int occupancy_dir(int dir_warps, size_t smem);     // lean derivative sweeps
+int occupancy_dense(int dir_warps, size_t smem);   // plan-free adjoint
 
 }  // namespace cgb
