@@ -278,6 +278,62 @@ def cpu_baseline(F, args, aseeds, workload, budget_s=12.0):
 
 
 # ---- native arm ----------------------------------------------------------------------------------
+def mixed_component(torch, R, stream, reps=3):
+    """Eight random DAG tapes (200..20000 nodes) over log-normal instance counts, about 1M
+    instances in all, each evaluated with one adjoint direction: one launch per tape (record +
+    adjoint, one tape after the other on one stream) against the persistent batch (one launch
+    for all tapes, replayed from a CUDA graph)."""
+    from casadi_gb300 import workloads as W
+    items = W.mixed_batch(n_tapes=8, total=1 << 20, seed=0)
+    rng = np.random.default_rng(0)
+    b = R.Batch()
+    plain = []
+    total = 0
+    for f, n, sd in items:
+        t = R.CudaTape(f)
+        args = [torch.from_numpy(x).cuda() for x in W.dag_inputs(n, n_in=16, seed=sd)]
+        seeds = [torch.from_numpy(rng.standard_normal((1, k, n))).cuda() for k in f.tape.nnz_out]
+        res, asens = b.add(t, args, seeds)
+        plain.append((t, args, seeds, [torch.empty_like(r) for r in res],
+                      [torch.empty_like(x) for x in asens]))
+        total += n
+    limit = max(b.scratch_bytes(), 1 << 30)
+    shared = torch.empty(limit, dtype=torch.uint8, device="cuda")
+    for p in plain:
+        p[0]._scratch = shared
+
+    def run_plain():
+        for t, args, seeds, res, asens in plain:
+            t.reverse(args, seeds, res=res, asens=asens, stream=stream, scratch_limit=limit)
+
+    def run_batch():
+        b.run(graph=True, stream=stream)
+
+    def timeit(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    ms_plain = timeit(run_plain)
+    ms_batch = timeit(run_batch)
+    same = all(bool(torch.equal(x.view(torch.int64), y.view(torch.int64))) for (_, _, _, r0, s0), (_, _, r1, _, s1) in
+               zip(plain, b._keep) for x, y in zip(r0 + s0, r1 + s1))
+    for p in plain:
+        p[0].sync()
+        p[0]._scratch = None
+    return {"instances": total, "tapes": [[f.tape.n_instr, n] for f, n, _ in items],
+            "plain_ms": ms_plain, "persistent_ms": ms_batch,
+            "plain_evals_per_s": total / (ms_plain * 1e-3),
+            "persistent_evals_per_s": total / (ms_batch * 1e-3),
+            "speedup": ms_plain / ms_batch, "bitwise_equal": same}
+
+
 def run_native(a):
     import torch
     from casadi_gb300 import runtime as R
@@ -366,6 +422,9 @@ def run_native(a):
         comps["jacobian24_evals_per_s"] = rate(
             lambda: ct.jacobian(dargs, res=res, jac=jac, stream=stream))
     ct.sync()
+
+    if not a.no_mixed:
+        comps["mixed_batch"] = mixed_component(torch, R, stream)
 
     # roofline of the dominant kernel family (device time from the per-launch events)
     weights = load_weights()
@@ -500,6 +559,8 @@ def main():
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     p.add_argument("--instances", type=int, default=None,
                    help="override the workload's instance count (profiling captures)")
+    p.add_argument("--no-mixed", action="store_true",
+                   help="skip the mixed multi-tape component (profiling captures)")
     a = p.parse_args()
     if a.impl == "reference":
         run_reference(a)

@@ -169,7 +169,8 @@ std::vector<std::unique_ptr<Tape>> g_tapes;
 std::vector<std::unique_ptr<Mem>> g_mems;
 
 // ---- optional per-launch timing (CUDA events on the launch stream) -------------------------
-enum Family { F_EVAL = 0, F_RECORD, F_TANGENT, F_ADJOINT, F_SP_FORWARD, F_SP_REVERSE, F_COUNT };
+enum Family { F_EVAL = 0, F_RECORD, F_TANGENT, F_ADJOINT, F_SP_FORWARD, F_SP_REVERSE, F_BATCH,
+              F_COUNT };
 struct ProfEntry {
   int family;
   cudaEvent_t start, stop;
@@ -1243,6 +1244,261 @@ int casadi_gb300_reverse_noalloc(int id, int64_t n, int64_t ld, int nadj,
       1, std::min<long long>(tiles, static_cast<long long>(sm_count()) * ds.blocks_per_sm / groups));
   e = launch_adjoint_dense(a, static_cast<int>(per_group * groups), s);
   if (e != cudaSuccess) return cuda_fail(e, "adjoint launch");
+  return 0;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Persistent multi-tape batches.
+// ---------------------------------------------------------------------------------------------
+namespace {
+
+struct BatchHost {
+  struct Item {
+    int tape;
+    long long n;
+    int ndir;
+    std::vector<IoDesc> io;  // 4*kMaxIo
+  };
+  std::vector<Item> items;
+  bool dirty = true;
+  // device side, rebuilt when dirty
+  BatchItem* d_items = nullptr;
+  IoDesc* d_io = nullptr;
+  int2* d_units = nullptr;
+  unsigned* d_counter = nullptr;
+  int n_units = 0;
+  int szw = 1, pmax = 0, grid = 1;
+  size_t smem = 0;
+  int device = 0;
+  cudaStream_t stream = nullptr;  // owned: graph capture needs a non-legacy stream
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  void* exec_scratch = nullptr;
+  ~BatchHost() {
+    if (exec) cudaGraphExecDestroy(exec);
+    cudaFree(d_items);
+    cudaFree(d_io);
+    cudaFree(d_units);
+    cudaFree(d_counter);
+    if (ev_in) cudaEventDestroy(ev_in);
+    if (ev_out) cudaEventDestroy(ev_out);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+std::vector<std::unique_ptr<BatchHost>> g_batches;
+
+BatchHost* get_batch(int id) {
+  std::lock_guard<std::mutex> lk(g_mtx);
+  if (id < 0 || id >= static_cast<int>(g_batches.size()) || !g_batches[id]) return nullptr;
+  return g_batches[id].get();
+}
+
+// Build items, the longest-first unit list and the launch shape.
+int batch_prepare(BatchHost& b) {
+  if (!b.dirty) return 0;
+  if (b.exec) {
+    cudaGraphExecDestroy(b.exec);
+    b.exec = nullptr;
+  }
+  cudaFree(b.d_items);
+  cudaFree(b.d_io);
+  cudaFree(b.d_units);
+  b.d_items = nullptr;
+  b.d_io = nullptr;
+  b.d_units = nullptr;
+  std::vector<BatchItem> items;
+  std::vector<IoDesc> io;
+  std::vector<std::pair<double, int2>> units;
+  b.szw = 1;
+  b.pmax = 0;
+  for (size_t k = 0; k < b.items.size(); ++k) {
+    const auto& it = b.items[k];
+    Tape* t = get_tape(it.tape);
+    if (!t) return fail(CASADI_GB300_ERR_ID, "batch item %zu: tape %d is gone", k, it.tape);
+    BatchItem bi;
+    std::memset(&bi, 0, sizeof(bi));
+    bi.t = t->view();
+    bi.n_code = t->n_chunks * kChunk;
+    bi.ndir = it.ndir;
+    bi.n = it.n;
+    if (it.ndir > 0) {
+      if (static_cast<unsigned>(t->n_partials) >= kMaxPartials)
+        return fail(CASADI_GB300_ERR_UNSUPPORTED, "batch item %zu records too many partials", k);
+      std::vector<char> seeded(t->n_out);
+      for (int j = 0; j < t->n_out; ++j) seeded[j] = it.io[2 * kMaxIo + j].ptr != nullptr;
+      int err = 0;
+      const AdjPlan* ap = adj_plan(*t, 1, 0, seeded, &err);
+      if (!ap) return err;
+      int2 se;
+      cudaError_t e = cudaMemcpy(&se, ap->d_chunks, sizeof(int2), cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) return cuda_fail(e, "read adjoint plan");
+      bi.adj_stream = ap->d_stream + se.x;
+      bi.adj_ngr = se.y / kEntGroup;
+      bi.zero_in = ap->d_zero;
+      bi.n_zero = ap->n_zero;
+      b.pmax = std::max(b.pmax, t->n_partials);
+    }
+    b.szw = std::max(b.szw, t->sz_w);
+    // cost of one tile: instructions x (1 value sweep + directions)
+    const double cost = static_cast<double>(t->n_instr) * (1 + it.ndir);
+    for (long long tile = 0; tile < (it.n + 31) / 32; ++tile)
+      units.push_back({cost, make_int2(static_cast<int>(k), static_cast<int>(tile))});
+    items.push_back(bi);
+    io.insert(io.end(), it.io.begin(), it.io.end());
+  }
+  std::stable_sort(units.begin(), units.end(),
+                   [](const std::pair<double, int2>& x, const std::pair<double, int2>& y) {
+                     return x.first > y.first;
+                   });
+  std::vector<int2> ulist(units.size());
+  for (size_t k = 0; k < units.size(); ++k) ulist[k] = units[k].second;
+  cudaError_t e;
+  if ((e = upload(&b.d_io, io)) != cudaSuccess) return cuda_fail(e, "upload batch I/O");
+  for (size_t k = 0; k < items.size(); ++k) items[k].io = b.d_io + k * 4 * kMaxIo;
+  if ((e = upload(&b.d_items, items)) != cudaSuccess || (e = upload(&b.d_units, ulist)) != cudaSuccess)
+    return cuda_fail(e, "upload batch");
+  if (!b.d_counter && (e = cudaMalloc(&b.d_counter, sizeof(unsigned))) != cudaSuccess)
+    return cuda_fail(e, "cudaMalloc(counter)");
+  b.n_units = static_cast<int>(ulist.size());
+  b.smem = static_cast<size_t>(b.szw) * 256;
+  if (b.smem > static_cast<size_t>(max_smem_optin()))
+    return fail(CASADI_GB300_ERR_UNSUPPORTED, "batch work vector of %d slots does not fit", b.szw);
+  const int occ = std::max(1, occupancy_batch(b.smem));
+  b.grid = std::max(1, std::min(sm_count() * occ, std::max(1, b.n_units)));
+  b.dirty = false;
+  return 0;
+}
+
+int batch_enqueue(BatchHost& b, void* scratch, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(b.d_counter, 0, sizeof(unsigned), s);
+  if (e != cudaSuccess) return cuda_fail(e, "reset batch counter");
+  BatchArgs a;
+  a.items = b.d_items;
+  a.units = b.d_units;
+  a.n_units = b.n_units;
+  a.counter = b.d_counter;
+  a.scratch = static_cast<double*>(scratch);
+  a.scratch_stride = static_cast<long long>(b.pmax) * 32;
+  e = launch_batch(a, b.grid, b.smem, s);
+  if (e != cudaSuccess) return cuda_fail(e, "batch launch");
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int casadi_gb300_batch_create(void) {
+  auto b = std::make_unique<BatchHost>();
+  cudaError_t e = cudaGetDevice(&b->device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if ((e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&b->ev_in, cudaEventDisableTiming)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&b->ev_out, cudaEventDisableTiming)) != cudaSuccess)
+    return cuda_fail(e, "batch stream");
+  std::lock_guard<std::mutex> lk(g_mtx);
+  g_batches.push_back(std::move(b));
+  return static_cast<int>(g_batches.size()) - 1;
+}
+
+int casadi_gb300_batch_free(int batch) {
+  std::lock_guard<std::mutex> lk(g_mtx);
+  if (batch < 0 || batch >= static_cast<int>(g_batches.size()) || !g_batches[batch])
+    return fail(CASADI_GB300_ERR_ID, "no batch %d", batch);
+  g_batches[batch].reset();
+  return 0;
+}
+
+int casadi_gb300_batch_add(int batch, int id, int64_t n, int64_t ld, int nadj,
+                           const double* const* arg, double* const* res,
+                           const double* const* aseed, double* const* asens) {
+  BatchHost* b = get_batch(batch);
+  if (!b) return fail(CASADI_GB300_ERR_ID, "no batch %d", batch);
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  if (int rc = check_device(*t)) return rc;
+  if (int rc = check_n(n, ld)) return rc;
+  if (nadj < 0 || nadj > 65535) return fail(CASADI_GB300_ERR_ARG, "bad direction count %d", nadj);
+  if (n > (1ll << 36)) return fail(CASADI_GB300_ERR_ARG, "too many instances");
+  BatchHost::Item it;
+  it.tape = id;
+  it.n = n;
+  it.ndir = nadj;
+  it.io.assign(4 * kMaxIo, IoDesc{nullptr, 0, 0, 0});
+  fill_io(it.io.data(), t->n_in, vptrs(arg), t->nnz_in, ld, false);
+  fill_io(it.io.data() + kMaxIo, t->n_out, vptrs(res), t->nnz_out, ld, false);
+  if (nadj > 0) {
+    fill_io(it.io.data() + 2 * kMaxIo, t->n_out, vptrs(aseed), t->nnz_out, ld, true);
+    fill_io(it.io.data() + 3 * kMaxIo, t->n_in, vptrs(asens), t->nnz_in, ld, true);
+  }
+  b->items.push_back(std::move(it));
+  b->dirty = true;
+  return static_cast<int>(b->items.size()) - 1;
+}
+
+int casadi_gb300_batch_scratch_size(int batch, size_t* bytes) {
+  BatchHost* b = get_batch(batch);
+  if (!b) return fail(CASADI_GB300_ERR_ID, "no batch %d", batch);
+  if (!bytes) return fail(CASADI_GB300_ERR_ARG, "bad arguments");
+  if (int rc = batch_prepare(*b)) return rc;
+  *bytes = static_cast<size_t>(b->grid) * b->pmax * 32 * 8;
+  return 0;
+}
+
+int casadi_gb300_batch_run(int batch, void* scratch, size_t scratch_bytes, int use_graph,
+                           void* stream) {
+  BatchHost* b = get_batch(batch);
+  if (!b) return fail(CASADI_GB300_ERR_ID, "no batch %d", batch);
+  int cur = -1;
+  cudaGetDevice(&cur);
+  if (cur != b->device) return fail(CASADI_GB300_ERR_ARG, "batch lives on device %d", b->device);
+  if (int rc = batch_prepare(*b)) return rc;
+  const size_t need = static_cast<size_t>(b->grid) * b->pmax * 32 * 8;
+  if (need > 0 && (!scratch || scratch_bytes < need))
+    return fail(CASADI_GB300_ERR_SCRATCH, "batch needs %zu bytes of scratch, got %zu", need,
+                scratch_bytes);
+  cudaStream_t caller = static_cast<cudaStream_t>(stream);
+  // order after the caller's stream, run on the owned stream, order the caller after it
+  cudaError_t e = cudaEventRecord(b->ev_in, caller);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->ev_in, 0);
+  if (e != cudaSuccess) return cuda_fail(e, "batch ordering");
+  if (use_graph) {
+    if (b->exec && b->exec_scratch != scratch) {
+      cudaGraphExecDestroy(b->exec);
+      b->exec = nullptr;
+    }
+    if (!b->exec) {
+      cudaGraph_t g = nullptr;
+      e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+      if (e != cudaSuccess) return cuda_fail(e, "begin capture");
+      int rc = batch_enqueue(*b, scratch, b->stream);
+      e = cudaStreamEndCapture(b->stream, &g);
+      if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+      }
+      if (e != cudaSuccess) return cuda_fail(e, "end capture");
+      e = cudaGraphInstantiate(&b->exec, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return cuda_fail(e, "instantiate batch graph");
+      b->exec_scratch = scratch;
+    }
+    e = timed(F_BATCH, b->stream, [&] { return cudaGraphLaunch(b->exec, b->stream); });
+    if (e != cudaSuccess) return cuda_fail(e, "graph launch");
+  } else {
+    int rc = 0;
+    e = timed(F_BATCH, b->stream, [&] {
+      rc = batch_enqueue(*b, scratch, b->stream);
+      return cudaSuccess;
+    });
+    if (rc) return rc;
+  }
+  e = cudaEventRecord(b->ev_out, b->stream);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(caller, b->ev_out, 0);
+  if (e != cudaSuccess) return cuda_fail(e, "batch ordering");
   return 0;
 }
 

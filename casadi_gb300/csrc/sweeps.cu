@@ -434,15 +434,23 @@ __host__ __device__ __forceinline__ unsigned ent_kind(unsigned m) { return (m >>
 __host__ __device__ __forceinline__ unsigned ent_pmask(unsigned m) { return (m >> 9) & 3u; }
 __host__ __device__ __forceinline__ unsigned ent_pk(unsigned m) { return m >> 11; }
 
-// Load the partials of one group of entries (d0 at pk, d1 at pk+1 or pk).
+// Load the partials of one group of entries (d0 at pk, d1 at pk+1 or pk). kNC: read-only
+// path (partials written by an earlier launch); otherwise L2 loads that see the same
+// kernel's stores.
+template <bool kNC>
+__device__ __forceinline__ double ld_partial(const double* p) {
+  return kNC ? __ldg(p) : __ldcg(p);
+}
+
+template <bool kNC = true>
 __device__ __forceinline__ void load_partials(const uint4 (&E)[kGroup], const double* pt,
                                               double (&P0)[kGroup], double (&P1)[kGroup]) {
 #pragma unroll
   for (int i = 0; i < kGroup; ++i) {
     const unsigned m = ent_pmask(E[i].w);
     const size_t pk = ent_pk(E[i].w);
-    P0[i] = (m & 1u) ? __ldg(pt + pk * 32) : 1.0;
-    P1[i] = (m & 2u) ? __ldg(pt + (pk + ((m & 1u) ? 1 : 0)) * 32) : 0.0;
+    P0[i] = (m & 1u) ? ld_partial<kNC>(pt + pk * 32) : 1.0;
+    P1[i] = (m & 2u) ? ld_partial<kNC>(pt + (pk + ((m & 1u) ? 1 : 0)) * 32) : 0.0;
   }
 }
 
@@ -542,6 +550,118 @@ __global__ void __launch_bounds__(32 * DW) k_tangent(const __grid_constant__ Swe
   }
 }
 
+// One adjoint sweep of one 32-instance tile by one warp: entry stream st (ngr groups),
+// recorded partials at pt (lane-offset, tile-local), work vector at wb (lane-offset).
+template <bool kNC = true>
+__device__ __forceinline__ void adjoint_walk(const uint4* st, int ngr, const double* pt,
+                                             unsigned char* wb, const IoDesc* seed,
+                                             const IoDesc* sens, bool active, long long dir,
+                                             long long ig) {
+  uint4 E0[kGroup], E1[kGroup];
+  double P0[kGroup], Q0[kGroup];
+  load_group(st, ngr - 1, ngr, E0);
+  load_group(st, ngr - 2 >= 0 ? ngr - 2 : ngr, ngr, E1);
+  load_partials<kNC>(E0, pt, P0, Q0);
+#pragma unroll 1
+  for (int g = ngr - 1; g >= 0; --g) {
+    uint4 E2[kGroup];
+    double P1[kGroup], Q1[kGroup];
+    load_group(st, g - 2 >= 0 ? g - 2 : ngr, ngr, E2);
+    load_partials<kNC>(E1, pt, P1, Q1);
+#pragma unroll
+    for (int i = kGroup - 1; i >= 0; --i) {
+      const uint4 cur = E0[i];
+      const unsigned meta = cur.w;
+      const unsigned f = ent_flags(meta);
+      const unsigned kind = ent_kind(meta);
+      // first contributions are assigned (0 + x -> x); dispatch on (kind, flags) so only the
+      // FP64 operations a case needs are issued
+      switch (kind) {
+        case LK_OUTPUT: {
+          const IoDesc& d = seed[cur.x];
+          const double sd =
+              active ? __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir, cur.z, ig)) : 0.0;
+          double& w = wreg(wb, cur.y);
+          if (f & 8u) w = sd; else w = __dadd_rn(w, sd);
+        } break;
+        case LK_INPUT: {
+          const IoDesc& d = sens[cur.y];
+          if (active && d.ptr)
+            static_cast<double*>(d.ptr)[io_off(d, dir, cur.z, ig)] = wreg(wb, cur.x);
+          wreg(wb, cur.x) = 0.0;
+        } break;
+        case LK_CONST:
+          wreg(wb, cur.x) = 0.0;
+          break;
+        case LK_NOP:
+          break;
+        default: {
+          const double seed = wreg(wb, cur.x);
+          wreg(wb, cur.x) = 0.0;
+          // contribution to operand b
+          switch ((kind << 2) | ((f >> 1) & 1u) | ((f >> 2) & 2u)) {  // (kind, b?, first?)
+            case (LK_GEN << 2) | 1u: {
+              double& w1 = wreg(wb, cur.y);
+              w1 = __dadd_rn(w1, __dmul_rn(P0[i], seed));
+            } break;
+            case (LK_GEN << 2) | 3u: wreg(wb, cur.y) = __dmul_rn(P0[i], seed); break;
+            case (LK_ADD << 2) | 1u: case (LK_SUB << 2) | 1u: case (LK_ASSIGN << 2) | 1u: {
+              double& w1 = wreg(wb, cur.y);
+              w1 = __dadd_rn(w1, seed);
+            } break;
+            case (LK_ADD << 2) | 3u: case (LK_SUB << 2) | 3u: case (LK_ASSIGN << 2) | 3u:
+              wreg(wb, cur.y) = seed;
+              break;
+            case (LK_NEG << 2) | 1u: {
+              double& w1 = wreg(wb, cur.y);
+              w1 = __dsub_rn(w1, seed);
+            } break;
+            case (LK_NEG << 2) | 3u: wreg(wb, cur.y) = d_neg(seed); break;
+            case (LK_TWICE << 2) | 1u: {
+              double& w1 = wreg(wb, cur.y);
+              w1 = __dadd_rn(w1, __dadd_rn(seed, seed));
+            } break;
+            case (LK_TWICE << 2) | 3u: wreg(wb, cur.y) = __dadd_rn(seed, seed); break;
+            default: break;  // operand b receives nothing
+          }
+          // contribution to operand c
+          switch ((kind << 2) | ((f >> 2) & 1u) | ((f >> 3) & 2u)) {  // (kind, c?, first?)
+            case (LK_GEN << 2) | 1u: {
+              double& w2 = wreg(wb, cur.z);
+              w2 = __dadd_rn(w2, __dmul_rn(Q0[i], seed));
+            } break;
+            case (LK_GEN << 2) | 3u: wreg(wb, cur.z) = __dmul_rn(Q0[i], seed); break;
+            case (LK_ADD << 2) | 1u: {
+              double& w2 = wreg(wb, cur.z);
+              w2 = __dadd_rn(w2, seed);
+            } break;
+            case (LK_ADD << 2) | 3u: wreg(wb, cur.z) = seed; break;
+            case (LK_SUB << 2) | 1u: {
+              double& w2 = wreg(wb, cur.z);
+              w2 = __dsub_rn(w2, seed);
+            } break;
+            case (LK_SUB << 2) | 3u: wreg(wb, cur.z) = d_neg(seed); break;
+            case (LK_IFZ << 2) | 1u: {
+              double& w2 = wreg(wb, cur.z);
+              if (!d_iszero(Q0[i])) w2 = __dadd_rn(w2, seed);
+              else w2 = __dadd_rn(w2, 0.0);
+            } break;
+            case (LK_IFZ << 2) | 3u: wreg(wb, cur.z) = d_iszero(Q0[i]) ? 0.0 : seed; break;
+            default: break;  // operand c receives nothing
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < kGroup; ++i) {
+      E0[i] = E1[i];
+      E1[i] = E2[i];
+      P0[i] = P1[i];
+      Q0[i] = Q1[i];
+    }
+  }
+}
+
 // Flags (bits 0-4): 2/4 operand b/c receives a contribution, 8/16 it is the first one
 // (1 marks an entry with work; outputs carry 8 when their seed is the slot's first).
 template <int DW>
@@ -572,108 +692,99 @@ __global__ void __launch_bounds__(32 * DW) k_adjoint(const __grid_constant__ Swe
       }
     }
     const double* pt = a.partials + static_cast<size_t>(tile) * a.t.n_partials * 32 + lane;
-    uint4 E0[kGroup], E1[kGroup];
-    double P0[kGroup], Q0[kGroup];
-    load_group(st, ngr - 1, ngr, E0);
-    load_group(st, ngr - 2 >= 0 ? ngr - 2 : ngr, ngr, E1);
-    load_partials(E0, pt, P0, Q0);
+    adjoint_walk(st, ngr, pt, wb, a.seed, a.sens, active, dir, ig);
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Persistent multi-tape batch: one launch drains a host-built list of work units
+// (item, 32-instance tile), longest first, through an atomic counter. An item is one tape over
+// its own instance range, either a value sweep or a value+adjoint sweep. Each one-warp CTA
+// grabs a unit, runs the warp-level value (or record) walk for its tile and, for adjoint items,
+// the adjoint walk of every direction, then grabs the next unit. Tapes of any length and
+// instance count share the GPU in one launch instead of one underfilled launch per tape.
+// ---------------------------------------------------------------------------------------------
+// Warp-level value sweep of one tile; instruction words are read straight from the tape
+// (uniform across the warp, cached) with the next word prefetched. RECORD writes partials to
+// pt (lane-offset, tile-local [partial][lane]).
+template <bool RECORD>
+__device__ __forceinline__ void primal_walk(const TapeView& t, int n_code, double* pt,
+                                            unsigned char* wb, const IoDesc* in,
+                                            const IoDesc* out, bool active, long long ig) {
+  const u64* code = t.code;
+  int pidx = 0;
+  u64 nxt = __ldg(code);
 #pragma unroll 1
-    for (int g = ngr - 1; g >= 0; --g) {
-      uint4 E2[kGroup];
-      double P1[kGroup], Q1[kGroup];
-      load_group(st, g - 2 >= 0 ? g - 2 : ngr, ngr, E2);
-      load_partials(E1, pt, P1, Q1);
-#pragma unroll
-      for (int i = kGroup - 1; i >= 0; --i) {
-        const uint4 cur = E0[i];
-        const unsigned meta = cur.w;
-        const unsigned f = ent_flags(meta);
-        const unsigned kind = ent_kind(meta);
-        // first contributions are assigned (0 + x -> x); dispatch on (kind, flags) so only the
-        // FP64 operations a case needs are issued
-        switch (kind) {
-          case LK_OUTPUT: {
-            const IoDesc& d = a.seed[cur.x];
-            const double sd =
-                active ? __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir, cur.z, ig)) : 0.0;
-            double& w = wreg(wb, cur.y);
-            if (f & 8u) w = sd; else w = __dadd_rn(w, sd);
-          } break;
-          case LK_INPUT: {
-            const IoDesc& d = a.sens[cur.y];
-            if (active && d.ptr)
-              static_cast<double*>(d.ptr)[io_off(d, dir, cur.z, ig)] = wreg(wb, cur.x);
-            wreg(wb, cur.x) = 0.0;
-          } break;
-          case LK_CONST:
-            wreg(wb, cur.x) = 0.0;
-            break;
-          case LK_NOP:
-            break;
-          default: {
-            const double seed = wreg(wb, cur.x);
-            wreg(wb, cur.x) = 0.0;
-            // contribution to operand b
-            switch ((kind << 2) | ((f >> 1) & 1u) | ((f >> 2) & 2u)) {  // (kind, b?, first?)
-              case (LK_GEN << 2) | 1u: {
-                double& w1 = wreg(wb, cur.y);
-                w1 = __dadd_rn(w1, __dmul_rn(P0[i], seed));
-              } break;
-              case (LK_GEN << 2) | 3u: wreg(wb, cur.y) = __dmul_rn(P0[i], seed); break;
-              case (LK_ADD << 2) | 1u: case (LK_SUB << 2) | 1u: case (LK_ASSIGN << 2) | 1u: {
-                double& w1 = wreg(wb, cur.y);
-                w1 = __dadd_rn(w1, seed);
-              } break;
-              case (LK_ADD << 2) | 3u: case (LK_SUB << 2) | 3u: case (LK_ASSIGN << 2) | 3u:
-                wreg(wb, cur.y) = seed;
-                break;
-              case (LK_NEG << 2) | 1u: {
-                double& w1 = wreg(wb, cur.y);
-                w1 = __dsub_rn(w1, seed);
-              } break;
-              case (LK_NEG << 2) | 3u: wreg(wb, cur.y) = d_neg(seed); break;
-              case (LK_TWICE << 2) | 1u: {
-                double& w1 = wreg(wb, cur.y);
-                w1 = __dadd_rn(w1, __dadd_rn(seed, seed));
-              } break;
-              case (LK_TWICE << 2) | 3u: wreg(wb, cur.y) = __dadd_rn(seed, seed); break;
-              default: break;  // operand b receives nothing
-            }
-            // contribution to operand c
-            switch ((kind << 2) | ((f >> 2) & 1u) | ((f >> 3) & 2u)) {  // (kind, c?, first?)
-              case (LK_GEN << 2) | 1u: {
-                double& w2 = wreg(wb, cur.z);
-                w2 = __dadd_rn(w2, __dmul_rn(Q0[i], seed));
-              } break;
-              case (LK_GEN << 2) | 3u: wreg(wb, cur.z) = __dmul_rn(Q0[i], seed); break;
-              case (LK_ADD << 2) | 1u: {
-                double& w2 = wreg(wb, cur.z);
-                w2 = __dadd_rn(w2, seed);
-              } break;
-              case (LK_ADD << 2) | 3u: wreg(wb, cur.z) = seed; break;
-              case (LK_SUB << 2) | 1u: {
-                double& w2 = wreg(wb, cur.z);
-                w2 = __dsub_rn(w2, seed);
-              } break;
-              case (LK_SUB << 2) | 3u: wreg(wb, cur.z) = d_neg(seed); break;
-              case (LK_IFZ << 2) | 1u: {
-                double& w2 = wreg(wb, cur.z);
-                if (!d_iszero(Q0[i])) w2 = __dadd_rn(w2, seed);
-                else w2 = __dadd_rn(w2, 0.0);
-              } break;
-              case (LK_IFZ << 2) | 3u: wreg(wb, cur.z) = d_iszero(Q0[i]) ? 0.0 : seed; break;
-              default: break;  // operand c receives nothing
-            }
-          }
+  for (int k = 0; k < n_code; ++k) {
+    const u64 ins = nxt;
+    if (k + 1 < n_code) nxt = __ldg(code + k + 1);
+    const unsigned op = dec_op(ins), A = dec_a(ins), B = dec_b(ins), C = dec_c(ins);
+    switch (op) {
+      case D_NOP:
+        break;
+      case D_CONST:
+        wreg(wb, A * 256u) = __ldg(t.consts + B);
+        break;
+      case D_INPUT: {
+        const IoDesc& d = in[B];
+        double v = 0.0;
+        if (active && d.ptr) v = __ldg(static_cast<const double*>(d.ptr) + io_off(d, 0, C, ig));
+        wreg(wb, A * 256u) = v;
+      } break;
+      case D_OUTPUT: {
+        const IoDesc& d = out[A];
+        if (active && d.ptr) static_cast<double*>(d.ptr)[io_off(d, 0, C, ig)] = wreg(wb, B * 256u);
+      } break;
+      default: {
+        const double x = wreg(wb, B * 256u), y = wreg(wb, C * 256u);
+        if (RECORD) {
+          const unsigned m = dec_pmask(ins);
+          double d0 = 0.0, d1 = 0.0;
+          const double f = dev_fun_der(op, x, y, d0, d1);
+          if (m & 1u) pt[32 * pidx++] = d0;
+          if (m & 2u) pt[32 * pidx++] = d1;
+          wreg(wb, A * 256u) = f;
+        } else {
+          wreg(wb, A * 256u) = dev_fun(op, x, y);
         }
       }
-#pragma unroll
-      for (int i = 0; i < kGroup; ++i) {
-        E0[i] = E1[i];
-        E1[i] = E2[i];
-        P0[i] = P1[i];
-        Q0[i] = Q1[i];
+    }
+  }
+}
+
+__global__ void __launch_bounds__(32) k_batch(const __grid_constant__ BatchArgs b) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int lane = threadIdx.x;
+  unsigned char* wb = smem + lane * 8;
+  double* pt = b.scratch + static_cast<size_t>(blockIdx.x) * b.scratch_stride + lane;
+  for (;;) {
+    unsigned u = 0;
+    if (lane == 0) u = atomicAdd(b.counter, 1u);
+    u = __shfl_sync(0xffffffffu, u, 0);
+    if (u >= static_cast<unsigned>(b.n_units)) break;
+    const int2 unit = __ldg(b.units + u);
+    const BatchItem& it = b.items[unit.x];
+    const long long il = static_cast<long long>(unit.y) * 32 + lane;
+    const bool active = il < it.n;
+    const IoDesc* io = it.io;
+    if (it.ndir == 0) {
+      primal_walk<false>(it.t, it.n_code, pt, wb, io, io + kMaxIo, active, il);
+      continue;
+    }
+    primal_walk<true>(it.t, it.n_code, pt, wb, io, io + kMaxIo, active, il);
+    // the warp's own partial stores must be visible to its loads below
+    __syncwarp();
+    for (int dir = 0; dir < it.ndir; ++dir) {
+      for (int q = 0; q < it.t.sz_w; ++q) wreg(wb, q * 256u) = 0.0;
+      if (active) {
+        for (int k = 0; k < it.n_zero; ++k) {
+          const int2 jk = __ldg(it.zero_in + k);
+          const IoDesc& d = io[3 * kMaxIo + jk.x];
+          if (d.ptr) static_cast<double*>(d.ptr)[io_off(d, dir, jk.y, il)] = 0.0;
+        }
       }
+      adjoint_walk<false>(it.adj_stream, it.adj_ngr, pt, wb, io + 2 * kMaxIo, io + 3 * kMaxIo,
+                          active, dir, il);
     }
   }
 }
@@ -868,6 +979,17 @@ cudaError_t launch_adjoint_dense(const SweepArgs& a, int grid, cudaStream_t s) {
   }
 }
 
+cudaError_t launch_batch(const BatchArgs& b, int grid, size_t smem, cudaStream_t s) {
+  // the attribute is raised once to the device maximum, so a captured graph never depends on
+  // a later call lowering it
+  static const cudaError_t set = cudaFuncSetAttribute(
+      k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_optin());
+  if (set != cudaSuccess) return set;
+  if (smem > static_cast<size_t>(max_smem_optin())) return cudaErrorInvalidValue;
+  k_batch<<<grid, 32, smem, s>>>(b);
+  return cudaGetLastError();
+}
+
 int occupancy_primal(int block, size_t smem) {
   int n = 0;
   cudaError_t e = cudaErrorInvalidValue;
@@ -899,6 +1021,16 @@ static int occ_of(K kernel, int block, size_t smem) {
       cudaSuccess)
     return 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, block, smem) != cudaSuccess)
+    return 0;
+  return n;
+}
+
+int occupancy_batch(size_t smem) {
+  if (cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           max_smem_optin()) != cudaSuccess)
+    return 0;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch, 32, smem) != cudaSuccess)
     return 0;
   return n;
 }

@@ -74,6 +74,31 @@ struct SweepArgs {
   const int* dchunk_off;            // unused by the warp-independent sweeps
 };
 
+// One item of a persistent batch: a tape over its own instance range.
+struct BatchItem {
+  TapeView t;
+  int n_code;
+  int ndir;                 // 0: value sweep only; >0: value + adjoint directions
+  long long n;              // instances
+  const IoDesc* io;         // 4*kMaxIo descriptors: inputs, outputs, adjoint seeds, sensitivities
+  const uint4* adj_stream;  // adjoint entry stream (ndir > 0)
+  int adj_ngr;              // its groups of kEntGroup entries
+  const int2* zero_in;      // inputs with a structurally zero adjoint
+  int n_zero;
+};
+
+struct BatchArgs {
+  const BatchItem* items;
+  const int2* units;        // (item, tile), longest first
+  int n_units;
+  unsigned* counter;        // next unit (zeroed before each launch)
+  double* scratch;          // partials, scratch_stride doubles per CTA
+  long long scratch_stride;
+};
+
+cudaError_t launch_batch(const BatchArgs& b, int grid, size_t smem, cudaStream_t s);
+int occupancy_batch(size_t smem);
+
 // Error bits written to TapeView::err.
 constexpr int kErrWaitTimeout = 1;   // a bounded wait on a staged chunk ran out
 constexpr int kErrBadOpcode = 2;     // an instruction with an unknown opcode was met

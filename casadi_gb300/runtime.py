@@ -77,6 +77,11 @@ def load(path=None):
         "casadi_gb300_reverse_noalloc": (cint, [cint, i64, i64, cint, vp, vp, vp, vp, vp]),
         "casadi_gb300_profile": (cint, [cint]),
         "casadi_gb300_profile_collect": (cint, [vp, vp, cint]),
+        "casadi_gb300_batch_create": (cint, []),
+        "casadi_gb300_batch_free": (cint, [cint]),
+        "casadi_gb300_batch_add": (cint, [cint, cint, i64, i64, cint, vp, vp, vp, vp]),
+        "casadi_gb300_batch_scratch_size": (cint, [cint, vp]),
+        "casadi_gb300_batch_run": (cint, [cint, vp, sz, cint, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -308,7 +313,59 @@ class CudaMap:
         return res, asens
 
 
-FAMILIES = ("eval", "record", "tangent", "adjoint", "sp_forward", "sp_reverse")
+class Batch:
+    """Several tapes over their own instance ranges, evaluated in ONE persistent launch.
+
+    ``add(tape, args, aseeds=None)`` queues a value sweep (no seeds) or a value + adjoint
+    sweep of ``tape`` (a :class:`CudaTape`) on device tensors; it returns ``(res, asens)``
+    tensors that ``run()`` fills. ``run(graph=True)`` replays a captured CUDA graph after the
+    first call. The tensors passed to or returned by ``add`` are held by the batch so the
+    pointers the launch uses stay valid."""
+
+    def __init__(self):
+        self.id = check(load().casadi_gb300_batch_create())
+        self._keep = []
+        self._scratch = None
+
+    def __del__(self):
+        try:
+            if getattr(self, "id", None) is not None and _lib is not None:
+                _lib.casadi_gb300_batch_free(self.id)
+        except Exception:
+            pass
+
+    def add(self, tape, args, aseeds=None, n=None, res=None, asens=None):
+        n = CudaTape._n(args) if n is None else n
+        nadj = 0
+        if aseeds is not None:
+            nadj = next(s.shape[0] for s in aseeds if s is not None)
+        res = tape._outs(tape.nnz_out, n) if res is None else res
+        if nadj:
+            asens = tape._outs(tape.nnz_in, n, nadj) if asens is None else asens
+        else:
+            aseeds, asens = [], []
+        check(load().casadi_gb300_batch_add(self.id, tape.id, n, n, nadj, _ptr_array(args),
+                                            _ptr_array(res), _ptr_array(aseeds),
+                                            _ptr_array(asens)))
+        self._keep.append((tape, list(args), res, list(aseeds), asens))
+        return res, asens
+
+    def scratch_bytes(self):
+        b = ct.c_size_t()
+        check(load().casadi_gb300_batch_scratch_size(self.id, ct.byref(b)))
+        return b.value
+
+    def run(self, graph=False, stream=None):
+        import torch
+        need = self.scratch_bytes()
+        if self._scratch is None or self._scratch.numel() < need:
+            self._scratch = torch.empty(max(need, 8), dtype=torch.uint8, device="cuda")
+        check(load().casadi_gb300_batch_run(self.id, ct.c_void_p(self._scratch.data_ptr()),
+                                            self._scratch.numel(), 1 if graph else 0,
+                                            _stream_handle(stream)))
+
+
+FAMILIES = ("eval", "record", "tangent", "adjoint", "sp_forward", "sp_reverse", "batch")
 
 
 def profile(enable=True):

@@ -76,11 +76,13 @@ DAG_OPS = ["add", "sub", "mul", "div", "sin", "cos", "exp", "log", "sqrt", "tanh
 DAG_P = [0.25, 0.15, 0.25, 0.05, 0.06, 0.06, 0.06, 0.04, 0.04, 0.04]
 
 
-def random_dag(n_in=64, n_nodes=10000, n_out=16, seed=0, window=256):
+def random_dag(n_in=64, n_nodes=10000, n_out=16, seed=0, window=256, bounded=False):
     """A seeded random expression DAG. Node k (k >= n_in) applies an op drawn from the
     mix above to operands drawn uniformly from the previous ``window`` nodes; the
     outputs are the last ``n_out`` nodes. Unary ops are guarded: exp(clip(x,-5,5)),
-    log(|x|+1), sqrt(x^2+1)."""
+    log(|x|+1), sqrt(x^2+1). With ``bounded`` the sums are averaged (0.5*(a+b)), products
+    take one tanh-squashed factor (a*tanh(b)) and exp is clipped to [-1, 1], which keeps
+    every node of a deep, narrow DAG finite and of order one."""
     rng = np.random.default_rng(seed)
     xs = S.sym("x", n_in)
     nodes = list(xs)
@@ -92,11 +94,11 @@ def random_dag(n_in=64, n_nodes=10000, n_out=16, seed=0, window=256):
         a = nodes[int(rng.integers(lo, k))]
         b = nodes[int(rng.integers(lo, k))]
         if op == "add":
-            e = a + b
+            e = 0.5 * (a + b) if bounded else a + b
         elif op == "sub":
-            e = a - b
+            e = 0.5 * (a - b) if bounded else a - b
         elif op == "mul":
-            e = a * b
+            e = a * S.tanh(b) if bounded else a * b
         elif op == "div":
             e = a / (S.sq(b) + 1.0)
         elif op == "sin":
@@ -104,7 +106,8 @@ def random_dag(n_in=64, n_nodes=10000, n_out=16, seed=0, window=256):
         elif op == "cos":
             e = S.cos(a)
         elif op == "exp":
-            e = S.exp(S.fmin(S.fmax(a, -5.0), 5.0))
+            c = 1.0 if bounded else 5.0
+            e = S.exp(S.fmin(S.fmax(a, -c), c))
         elif op == "log":
             e = S.log(S.fabs(a) + 1.0)
         elif op == "sqrt":
@@ -119,6 +122,24 @@ def random_dag(n_in=64, n_nodes=10000, n_out=16, seed=0, window=256):
 def dag_inputs(n, n_in=64, seed=0):
     rng = np.random.default_rng(seed)
     return [rng.standard_normal((n_in, n))]
+
+
+def mixed_batch(n_tapes=8, total=1 << 20, seed=0, n_in=16, n_out=4, window=64):
+    """A mixed multi-tape workload: ``n_tapes`` random DAGs whose node counts are spread
+    log-uniformly over 200..20000 and whose instance counts are drawn log-normal (median
+    4096, sigma 1.5) and rescaled to about ``total`` instances in all. Returns a list of
+    ``(Function, n_instances, seed)``."""
+    rng = np.random.default_rng(seed)
+    nodes = np.exp(np.linspace(np.log(200), np.log(20000), n_tapes)).astype(int)
+    counts = rng.lognormal(mean=np.log(4096), sigma=1.5, size=n_tapes)
+    counts = np.maximum(32, np.round(counts * total / counts.sum())).astype(int)
+    perm = rng.permutation(n_tapes)
+    out = []
+    for k in range(n_tapes):
+        f = random_dag(n_in=n_in, n_nodes=int(nodes[k]), n_out=n_out, seed=seed * 100 + k,
+                       window=window, bounded=True)
+        out.append((f, int(counts[perm[k]]), seed * 100 + k))
+    return out
 
 
 # ---- quadcopter multiple shooting -----------------------------------------------------------

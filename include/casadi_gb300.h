@@ -167,6 +167,25 @@ CASADI_GB300_API int casadi_gb300_map_reverse(int id, int mem, int64_t n, int na
                              double* const* res, const double* const* aseed,
                              double* const* asens);
 
+/* Persistent multi-tape batches. A batch is a list of items, each one tape over its own
+ * instance range (device pointers, instance-minor layout as above): nadj == 0 runs the value
+ * sweep, nadj > 0 the value sweep plus nadj adjoint directions (aseed/asens as in
+ * casadi_gb300_reverse). casadi_gb300_batch_run evaluates every item in ONE persistent launch
+ * whose warps drain a longest-first list of (item, 32-instance tile) units, so tapes of
+ * uneven length and instance count keep the GPU full. With use_graph the launch is captured
+ * once into a CUDA graph (on a stream the batch owns, ordered after and before the caller's
+ * stream) and replayed; adding items or changing the scratch buffer re-captures it.
+ * casadi_gb300_batch_add returns the item index. No counterpart in the reference: a CasADi
+ * Map evaluates one Function per call (casadi/core/map.cpp:141-157). */
+CASADI_GB300_API int casadi_gb300_batch_create(void);
+CASADI_GB300_API int casadi_gb300_batch_free(int batch);
+CASADI_GB300_API int casadi_gb300_batch_add(int batch, int id, int64_t n, int64_t ld, int nadj,
+                           const double* const* arg, double* const* res,
+                           const double* const* aseed, double* const* asens);
+CASADI_GB300_API int casadi_gb300_batch_scratch_size(int batch, size_t* bytes);
+CASADI_GB300_API int casadi_gb300_batch_run(int batch, void* scratch, size_t scratch_bytes,
+                           int use_graph, void* stream);
+
 /* Allocation-free adjoint sweep: the same values and adjoint sensitivities as
  * casadi_gb300_reverse (arguments and layouts alike, no scratch argument), for callers that
  * cannot allocate device memory when they need derivatives -- solvers inside a CUDA graph
@@ -188,7 +207,7 @@ CASADI_GB300_API int casadi_gb300_reverse_noalloc(int id, int64_t n, int64_t ld,
  * recorded on its own stream. casadi_gb300_profile_collect waits for the recorded launches
  * and returns, per kernel family, the summed device milliseconds and the launch count, then
  * forgets them. Families: 0 eval, 1 record (values + partials), 2 tangent, 3 adjoint,
- * 4 sp_forward, 5 sp_reverse. This has no counterpart in the reference (CasADi's FStats
+ * 4 sp_forward, 5 sp_reverse, 6 batch. This has no counterpart in the reference (CasADi's FStats
  * timers, casadi/core/timing.hpp:60-80, time host calls). */
 CASADI_GB300_API int casadi_gb300_profile(int enable);
 CASADI_GB300_API int casadi_gb300_profile_collect(double* ms, int* launches, int count);

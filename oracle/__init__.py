@@ -104,9 +104,20 @@ def _prep(args, dtype=np.float64):
     return [None if a is None else np.ascontiguousarray(a, dtype=dtype) for a in args]
 
 
+def _check(arrays, nnz, n, what, ndir=None):
+    """The C sweeps trust the buffer sizes: refuse any array of the wrong shape."""
+    if len(arrays) != len(nnz):
+        raise ValueError("%s: %d arrays for %d slots" % (what, len(arrays), len(nnz)))
+    for a, k in zip(arrays, nnz):
+        want = (k, n) if ndir is None else (ndir, k, n)
+        if a is not None and a.shape != want:
+            raise ValueError("%s: shape %s, expected %s" % (what, a.shape, want))
+
+
 def eval(tape, args, n, nthreads=1):
     t = TapeArrays(tape)
     args = _prep(args)
+    _check(args, tape.nnz_in, n, "arguments")
     res = _outs(tape.nnz_out, n)
     rc = lib().sxo_eval(ct.byref(t.struct), ct.c_long(n), _ptrs(args), _ptrs(res),
                         ct.c_int(nthreads))
@@ -120,6 +131,8 @@ def forward(tape, args, fseeds, n, nthreads=1):
     args = _prep(args)
     fseeds = _prep(fseeds)
     nfwd = next(s.shape[0] for s in fseeds if s is not None)
+    _check(args, tape.nnz_in, n, "arguments")
+    _check(fseeds, tape.nnz_in, n, "forward seeds", nfwd)
     res = _outs(tape.nnz_out, n)
     fsens = _outs(tape.nnz_out, n, nfwd)
     rc = lib().sxo_forward(ct.byref(t.struct), ct.c_long(n), ct.c_int(nfwd), _ptrs(args),
@@ -133,6 +146,7 @@ def jacobian(tape, args, n, nthreads=1):
     nnz_out[j], n)."""
     t = TapeArrays(tape)
     args = _prep(args)
+    _check(args, tape.nnz_in, n, "arguments")
     nz = sum(tape.nnz_in)
     res = _outs(tape.nnz_out, n)
     jac = _outs(tape.nnz_out, n, nz)
@@ -148,6 +162,8 @@ def reverse(tape, args, aseeds, n, nthreads=1):
     args = _prep(args)
     aseeds = _prep(aseeds)
     nadj = next(s.shape[0] for s in aseeds if s is not None)
+    _check(args, tape.nnz_in, n, "arguments")
+    _check(aseeds, tape.nnz_out, n, "adjoint seeds", nadj)
     res = _outs(tape.nnz_out, n)
     asens = _outs(tape.nnz_in, n, nadj)
     rc = lib().sxo_reverse(ct.byref(t.struct), ct.c_long(n), ct.c_int(nadj), _ptrs(args),
@@ -213,6 +229,8 @@ def ref_forward(tape, args, fseeds, n):
     args = _prep(args)
     fseeds = _prep(fseeds)
     nfwd = next(s.shape[0] for s in fseeds if s is not None)
+    _check(args, tape.nnz_in, n, "arguments")
+    _check(fseeds, tape.nnz_in, n, "forward seeds", nfwd)
     fsens = _outs(tape.nnz_out, n, nfwd)
     rc = ref().ref_forward(ct.c_int(tape.n_instr), t.op.ctypes.data_as(ct.c_void_p),
                            t.i0.ctypes.data_as(ct.c_void_p), t.i1.ctypes.data_as(ct.c_void_p),
@@ -246,6 +264,8 @@ def ref_reverse(tape, args, aseeds, n):
     args = _prep(args)
     aseeds = _prep(aseeds)
     nadj = next(s.shape[0] for s in aseeds if s is not None)
+    _check(args, tape.nnz_in, n, "arguments")
+    _check(aseeds, tape.nnz_out, n, "adjoint seeds", nadj)
     asens = _outs(tape.nnz_in, n, nadj)
     rc = ref().ref_reverse(ct.c_int(tape.n_instr), t.op.ctypes.data_as(ct.c_void_p),
                            t.i0.ctypes.data_as(ct.c_void_p), t.i1.ctypes.data_as(ct.c_void_p),
