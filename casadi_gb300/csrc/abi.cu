@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "../../include/casadi_gb300.h"
+#include "schedule.cuh"
 #include "sweeps.cuh"
 
 using namespace cgb;
@@ -60,6 +61,23 @@ int device_opcode(int op) {
   }
 }
 
+int reference_opcode(unsigned dop) {
+  if (dop <= 43) return static_cast<int>(dop);
+  switch (dop) {
+    case D_CONST: return kOpConst;
+    case D_INPUT: return kOpInput;
+    case D_OUTPUT: return kOpOutput;
+    case D_ERFINV: return 86;
+    case D_PRINTME: return 87;
+    case D_LIFT: return 88;
+    case D_LOG1P: return 93;
+    case D_EXPM1: return 94;
+    case D_HYPOT: return 95;
+    case D_REMAINDER: return 97;
+    default: return -1;
+  }
+}
+
 // Activity plan of the tangent sweep for one seed pattern and launch shape.
 struct TanPlan {
   int ndir = 0, dw = 0, ch = 0;
@@ -93,6 +111,7 @@ struct AdjPlan {
 struct Tape {
   int device = 0;
   int n_instr = 0, n_in = 0, n_out = 0, sz_w = 0, n_partials = 0, n_chunks = 0;
+  int ref_sz_w = 0;  // the work-vector length the tape came with (sz_w: after scheduling)
   std::vector<int> nnz_in, nnz_out;
   std::vector<int2> absent_in;
   std::vector<int> pofs;    // partials recorded before instruction k*kPofsGran
@@ -104,7 +123,7 @@ struct Tape {
   // launch shapes
   int primal_block = 128, primal_grid_cap = 1;
   std::mutex shape_mtx;
-  std::vector<std::pair<int, int>> dir_shape_cache;  // (ndir, packed shape)
+  int tuned[3] = {-1, -1, -1};  // derivative-sweep variant per kind (seeded/identity tangent, adjoint)
   std::vector<u64> h_code;                            // padded instruction stream
   std::vector<std::unique_ptr<TanPlan>> tan_plans;
   std::vector<std::unique_ptr<AdjPlan>> adj_plans;
@@ -243,44 +262,13 @@ struct DirShape {
   int dw = 1, ch = 16, blocks_per_sm = 1;
 };
 
-DirShape dir_shape(Tape& t, int ndir) {
-  {
-    std::lock_guard<std::mutex> lk(t.shape_mtx);
-    for (auto& e : t.dir_shape_cache)
-      if (e.first == ndir) {
-        DirShape d;
-        d.dw = e.second & 0xff;
-        d.ch = (e.second >> 8) & 0xfff;
-        d.blocks_per_sm = e.second >> 20;
-        return d;
-      }
-  }
-  const int max_smem = max_smem_optin();
-  DirShape best;
-  double best_score = -1;
-  for (int ch : {64, 32, 16}) {
-    for (int dw : {8, 6, 4, 2, 1}) {
-      if (dw > 1 && dw >= 2 * ndir) continue;
-      const size_t sm = smem_lean(t.sz_w, dw, ch);
-      if (sm > static_cast<size_t>(max_smem)) continue;
-      const int occ = occupancy_dir(dw, sm);
-      if (occ <= 0) continue;
-      const int groups = (ndir + dw - 1) / dw;
-      const double used = static_cast<double>(ndir) / (groups * dw);
-      const double warps = std::min(occ * dw, 8);
-      const double score = warps * used * (1.0 + 0.01 * ch);
-      if (score > best_score) {
-        best_score = score;
-        best.dw = dw;
-        best.ch = ch;
-        best.blocks_per_sm = occ;
-      }
-    }
-  }
-  std::lock_guard<std::mutex> lk(t.shape_mtx);
-  t.dir_shape_cache.emplace_back(ndir, best.dw | (best.ch << 8) | (best.blocks_per_sm << 20));
-  return best;
-}
+// Autotuning of the derivative sweeps: the first large enough call of each kind on a tape
+// runs every variant once on its first wave (same arithmetic, same results), times them with
+// CUDA events and keeps the fastest for the tape. It synchronizes the stream once; it is
+// skipped while the stream is being captured into a graph, and can be switched off.
+bool g_autotune = true;
+constexpr int kDefaultVariant = DV_G4_R128;  // fastest on the rollout tapes measured
+
 
 bool fits_smem(int sz_w) {
   return smem_primal(sz_w, 32) <= static_cast<size_t>(max_smem_optin());
@@ -543,6 +531,22 @@ const AdjPlan* adj_plan(Tape& t, int dw, int ch, const std::vector<char>& seeded
   return t.adj_plans.back().get();
 }
 
+// Runs `fn` (launches on stream s) once between two events and waits for it.
+template <class F>
+int time_once(cudaStream_t s, F fn, float* ms) {
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  if (e == cudaSuccess) e = cudaEventRecord(e0, s);
+  if (e == cudaSuccess) e = fn();
+  if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+  if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  if (e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  return e == cudaSuccess ? 0 : cuda_fail(e, "autotune timing");
+}
+
 // Values + partials (record sweep) followed by the derivative sweep, in waves of as many
 // instances as the scratch holds. `in/out/seed/sens` address the whole instance range.
 int run_ad(Tape& t, long long n, const IoDesc* in, const IoDesc* out, const IoDesc* seed,
@@ -565,7 +569,7 @@ int run_ad(Tape& t, long long n, const IoDesc* in, const IoDesc* out, const IoDe
   if (ndir > 0 && static_cast<unsigned>(t.n_partials) >= kMaxPartials)
     return fail(CASADI_GB300_ERR_UNSUPPORTED, "tape records %d partials per instance (max %u)",
                 t.n_partials, kMaxPartials - 1);
-  ds.blocks_per_sm = ndir > 0 ? std::max(1, occupancy_dir(1, dsmem)) : 1;
+  const int kind = adjoint ? 2 : (identity ? 1 : 0);
   const int sms = sm_count();
   const TanPlan* tp = nullptr;
   const AdjPlan* ap = nullptr;
@@ -613,11 +617,35 @@ int run_ad(Tape& t, long long n, const IoDesc* in, const IoDesc* out, const IoDe
         a.n_zero = ap->n_zero;
       }
       const long long work = (m + 31) / 32 * ndir;
-      const int grid = static_cast<int>(
-          std::max<long long>(1, std::min<long long>(work, static_cast<long long>(sms) * ds.blocks_per_sm)));
-      e = timed(adjoint ? F_ADJOINT : F_TANGENT, s, [&] {
-        return adjoint ? launch_adjoint(a, grid, s) : launch_tangent(a, grid, s);
-      });
+      auto grid_of = [&](int v) {
+        const int occ = std::max(1, occupancy_dir(v, adjoint, dsmem));
+        return static_cast<int>(std::max<long long>(
+            1, std::min<long long>(work, static_cast<long long>(sms) * occ)));
+      };
+      auto launch = [&](int v) {
+        return adjoint ? launch_adjoint(a, grid_of(v), v, s) : launch_tangent(a, grid_of(v), v, s);
+      };
+      int variant = t.tuned[kind];
+      if (variant < 0) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(s, &cs);
+        // tune on waves that fill the GPU at least twice at 8 warps per SM, outside capture
+        if (g_autotune && cs == cudaStreamCaptureStatusNone && work >= 2ll * sms * 8) {
+          float best = 0;
+          for (int v = 0; v < DV_COUNT; ++v) {
+            float ms = 0;
+            if (int rc = time_once(s, [&] { return launch(v); }, &ms)) return rc;
+            if (variant < 0 || ms < best) {
+              best = ms;
+              variant = v;
+            }
+          }
+          t.tuned[kind] = variant;
+          continue;  // the last variant's run already produced this wave's results
+        }
+        variant = kDefaultVariant;
+      }
+      e = timed(adjoint ? F_ADJOINT : F_TANGENT, s, [&] { return launch(variant); });
       if (e != cudaSuccess) return cuda_fail(e, "derivative sweep launch");
     }
   }
@@ -636,16 +664,17 @@ int check_n(long long n, long long ld) {
   return 0;
 }
 
-}  // namespace
+// Validation and encoding of a reference-format tape (host only: no device calls, so the
+// checks and the scheduler also run on machines without a GPU).
+struct Encoded {
+  std::vector<u64> code;  // reference order and slots
+  std::vector<double> consts;
+  std::vector<int2> absent_in;
+  long long n_partials = 0;
+};
 
-extern "C" {
-
-const char* casadi_gb300_last_error(void) { return g_err.c_str(); }
-
-const char* casadi_gb300_version(void) { return "0.1.0"; }
-
-int casadi_gb300_tape_create(const casadi_gb300_atomic* alg, int n_instr, int n_in,
-                             const int* nnz_in, int n_out, const int* nnz_out, int sz_w) {
+int encode_tape(const casadi_gb300_atomic* alg, int n_instr, int n_in, const int* nnz_in,
+                int n_out, const int* nnz_out, int sz_w, Encoded& enc_out) {
   if (n_instr < 0 || (n_instr > 0 && !alg)) return fail(CASADI_GB300_ERR_ARG, "no instructions");
   if (n_in < 0 || n_out < 0 || sz_w < 0) return fail(CASADI_GB300_ERR_ARG, "negative size");
   if ((n_in > 0 && !nnz_in) || (n_out > 0 && !nnz_out))
@@ -655,29 +684,19 @@ int casadi_gb300_tape_create(const casadi_gb300_atomic* alg, int n_instr, int n_
   if (static_cast<unsigned>(sz_w) > kFieldMax)
     return fail(CASADI_GB300_ERR_UNSUPPORTED, "work vector of %d slots exceeds %u", sz_w,
                 kFieldMax);
-  if (!fits_smem(sz_w))
-    return fail(CASADI_GB300_ERR_UNSUPPORTED,
-                "work vector of %d slots does not fit shared memory (global work vectors are "
-                "not available in this build)", sz_w);
-  auto t = std::make_unique<Tape>();
-  t->n_instr = n_instr;
-  t->n_in = n_in;
-  t->n_out = n_out;
-  t->sz_w = sz_w;
-  t->nnz_in.assign(nnz_in, nnz_in + n_in);
-  t->nnz_out.assign(nnz_out, nnz_out + n_out);
-  for (int v : t->nnz_in)
-    if (v < 0 || static_cast<unsigned>(v) > kFieldMax) return fail(CASADI_GB300_ERR_ARG, "bad nnz_in");
-  for (int v : t->nnz_out)
-    if (v < 0 || static_cast<unsigned>(v) > kFieldMax) return fail(CASADI_GB300_ERR_ARG, "bad nnz_out");
-
-  // validate and encode (every index is checked here; kernels trust the stream)
-  std::vector<u64> code;
-  std::vector<double> consts;
+  for (int j = 0; j < n_in; ++j)
+    if (nnz_in[j] < 0 || static_cast<unsigned>(nnz_in[j]) > kFieldMax)
+      return fail(CASADI_GB300_ERR_ARG, "bad nnz_in");
+  for (int j = 0; j < n_out; ++j)
+    if (nnz_out[j] < 0 || static_cast<unsigned>(nnz_out[j]) > kFieldMax)
+      return fail(CASADI_GB300_ERR_ARG, "bad nnz_out");
+  // every index is checked here; kernels trust the stream
+  std::vector<u64>& code = enc_out.code;
+  std::vector<double>& consts = enc_out.consts;
   std::vector<std::vector<char>> seen_in(n_in);
   std::vector<std::vector<char>> seen_out(n_out);
-  for (int j = 0; j < n_in; ++j) seen_in[j].assign(t->nnz_in[j], 0);
-  for (int j = 0; j < n_out; ++j) seen_out[j].assign(t->nnz_out[j], 0);
+  for (int j = 0; j < n_in; ++j) seen_in[j].assign(nnz_in[j], 0);
+  for (int j = 0; j < n_out; ++j) seen_out[j].assign(nnz_out[j], 0);
   code.reserve(n_instr);
   long long n_partials = 0;
   auto slot_ok = [&](int s) { return s >= 0 && s < sz_w; };
@@ -697,20 +716,20 @@ int casadi_gb300_tape_create(const casadi_gb300_atomic* alg, int n_instr, int n_
       consts.push_back(e.a.d);
     } else if (dop == D_INPUT) {
       const int j = e.a.i[0], nz = e.a.i[1];
-      if (!slot_ok(e.i0) || j < 0 || j >= n_in || nz < 0 || nz >= t->nnz_in[j])
+      if (!slot_ok(e.i0) || j < 0 || j >= n_in || nz < 0 || nz >= nnz_in[j])
         return fail(CASADI_GB300_ERR_ARG, "instruction %d: input reference out of range", k);
       seen_in[j][nz] = 1;
       code.push_back(enc(D_INPUT, e.i0, j, nz));
     } else if (dop == D_OUTPUT) {
       const int j = e.i0, s = e.a.i[0], nz = e.a.i[1];
-      if (j < 0 || j >= n_out || !slot_ok(s) || nz < 0 || nz >= t->nnz_out[j])
+      if (j < 0 || j >= n_out || !slot_ok(s) || nz < 0 || nz >= nnz_out[j])
         return fail(CASADI_GB300_ERR_ARG, "instruction %d: output reference out of range", k);
       if (seen_out[j][nz])
         return fail(CASADI_GB300_ERR_ARG, "instruction %d: output nonzero written twice", k);
       seen_out[j][nz] = 1;
       code.push_back(enc(D_OUTPUT, j, s, nz));
     } else {
-      const int b = e.a.i[0], c = e.a.i[1];
+      const int b = e.a.i[0], c = is_binary(dop) ? e.a.i[1] : e.a.i[0];
       if (!slot_ok(e.i0) || !slot_ok(b) || !slot_ok(c))
         return fail(CASADI_GB300_ERR_ARG, "instruction %d: slot out of range", k);
       code.push_back(enc(dop, e.i0, b, c));
@@ -718,14 +737,60 @@ int casadi_gb300_tape_create(const casadi_gb300_atomic* alg, int n_instr, int n_
     }
   }
   for (int j = 0; j < n_out; ++j)
-    for (int nz = 0; nz < t->nnz_out[j]; ++nz)
+    for (int nz = 0; nz < nnz_out[j]; ++nz)
       if (!seen_out[j][nz])
         return fail(CASADI_GB300_ERR_ARG, "output %d nonzero %d is never written", j, nz);
   for (int j = 0; j < n_in; ++j)
-    for (int nz = 0; nz < t->nnz_in[j]; ++nz)
-      if (!seen_in[j][nz]) t->absent_in.push_back(make_int2(j, nz));
+    for (int nz = 0; nz < nnz_in[j]; ++nz)
+      if (!seen_in[j][nz]) enc_out.absent_in.push_back(make_int2(j, nz));
   if (n_partials > (1ll << 31))
     return fail(CASADI_GB300_ERR_UNSUPPORTED, "tape records too many partials");
+  enc_out.n_partials = n_partials;
+  return 0;
+}
+
+// Encoded tape in the scheduled order; returns the scheduled work-vector length or a status.
+int encode_and_schedule(const casadi_gb300_atomic* alg, int n_instr, int n_in,
+                        const int* nnz_in, int n_out, const int* nnz_out, int sz_w,
+                        Encoded& e) {
+  if (int rc = encode_tape(alg, n_instr, n_in, nnz_in, n_out, nnz_out, sz_w, e)) return rc;
+  std::vector<u64> sched;
+  std::string err;
+  const int w = schedule_code(e.code, sched, err);
+  if (w < 0) return fail(CASADI_GB300_ERR_ARG, "%s", err.c_str());
+  e.code.swap(sched);
+  return w;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* casadi_gb300_last_error(void) { return g_err.c_str(); }
+
+const char* casadi_gb300_version(void) { return "0.1.0"; }
+
+int casadi_gb300_tape_create(const casadi_gb300_atomic* alg, int n_instr, int n_in,
+                             const int* nnz_in, int n_out, const int* nnz_out, int sz_w) {
+  Encoded en;
+  const int wlen = encode_and_schedule(alg, n_instr, n_in, nnz_in, n_out, nnz_out, sz_w, en);
+  if (wlen < 0) return wlen;
+  if (!fits_smem(wlen))
+    return fail(CASADI_GB300_ERR_UNSUPPORTED,
+                "work vector of %d slots (after scheduling) does not fit shared memory (global "
+                "work vectors are not available in this build)", wlen);
+  auto t = std::make_unique<Tape>();
+  t->n_instr = n_instr;
+  t->n_in = n_in;
+  t->n_out = n_out;
+  t->sz_w = wlen;
+  t->ref_sz_w = sz_w;
+  t->nnz_in.assign(nnz_in, nnz_in + n_in);
+  t->nnz_out.assign(nnz_out, nnz_out + n_out);
+  t->absent_in = en.absent_in;
+  std::vector<u64>& code = en.code;
+  std::vector<double>& consts = en.consts;
+  const long long n_partials = en.n_partials;
   t->n_partials = static_cast<int>(n_partials);
   t->n_chunks = std::max(1, (n_instr + kChunk - 1) / kChunk);
   code.resize(static_cast<size_t>(t->n_chunks) * kChunk, enc(D_NOP, 0, 0, 0));
@@ -771,6 +836,36 @@ int casadi_gb300_tape_create(const casadi_gb300_atomic* alg, int n_instr, int n_
   std::lock_guard<std::mutex> lk(g_mtx);
   g_tapes.push_back(std::move(t));
   return static_cast<int>(g_tapes.size()) - 1;
+}
+
+int casadi_gb300_tape_schedule(const casadi_gb300_atomic* alg, int n_instr, int n_in,
+                               const int* nnz_in, int n_out, const int* nnz_out, int sz_w,
+                               casadi_gb300_atomic* out, int* sz_w_out) {
+  if (!out || !sz_w_out) return fail(CASADI_GB300_ERR_ARG, "bad arguments");
+  Encoded en;
+  const int wlen = encode_and_schedule(alg, n_instr, n_in, nnz_in, n_out, nnz_out, sz_w, en);
+  if (wlen < 0) return wlen;
+  for (int k = 0; k < n_instr; ++k) {
+    const u64 w = en.code[k];
+    const unsigned op = dec_op(w);
+    casadi_gb300_atomic& e = out[k];
+    std::memset(&e, 0, sizeof(e));
+    e.op = reference_opcode(op);
+    if (op == D_CONST) {
+      e.i0 = static_cast<int>(dec_a(w));
+      e.a.d = en.consts[dec_b(w)];
+    } else if (op == D_OUTPUT) {
+      e.i0 = static_cast<int>(dec_a(w));
+      e.a.i[0] = static_cast<int>(dec_b(w));
+      e.a.i[1] = static_cast<int>(dec_c(w));
+    } else {
+      e.i0 = static_cast<int>(dec_a(w));
+      e.a.i[0] = static_cast<int>(dec_b(w));
+      e.a.i[1] = static_cast<int>(dec_c(w));
+    }
+  }
+  *sz_w_out = wlen;
+  return 0;
 }
 
 int casadi_gb300_tape_free(int id) {
@@ -884,6 +979,29 @@ int casadi_gb300_jacobian(int id, int64_t n, int64_t ld, const double* const* ar
 int casadi_gb300_profile(int enable) {
   std::lock_guard<std::mutex> lk(g_prof_mtx);
   g_prof = enable != 0;
+  return 0;
+}
+
+int casadi_gb300_autotune(int enable) {
+  std::lock_guard<std::mutex> lk(g_mtx);
+  g_autotune = enable != 0;
+  return 0;
+}
+
+int casadi_gb300_tuned_variant(int id, int kind, int* variant) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  if (kind < 0 || kind > 2 || !variant) return fail(CASADI_GB300_ERR_ARG, "bad arguments");
+  *variant = t->tuned[kind];
+  return 0;
+}
+
+int casadi_gb300_set_variant(int id, int kind, int variant) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  if (kind < 0 || kind > 2 || variant < -1 || variant >= DV_COUNT)
+    return fail(CASADI_GB300_ERR_ARG, "bad arguments");
+  t->tuned[kind] = variant;
   return 0;
 }
 
@@ -1336,7 +1454,7 @@ int batch_prepare(BatchHost& b) {
       cudaError_t e = cudaMemcpy(&se, ap->d_chunks, sizeof(int2), cudaMemcpyDeviceToHost);
       if (e != cudaSuccess) return cuda_fail(e, "read adjoint plan");
       bi.adj_stream = ap->d_stream + se.x;
-      bi.adj_ngr = se.y / kEntGroup;
+      bi.adj_ngr = se.y / kBatchGroup;
       bi.zero_in = ap->d_zero;
       bi.n_zero = ap->n_zero;
       b.pmax = std::max(b.pmax, t->n_partials);

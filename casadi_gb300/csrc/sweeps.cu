@@ -414,7 +414,7 @@ __global__ void __launch_bounds__(32 * DW) k_adjoint_tape(const __grid_constant_
 // wait for each other, so a sparse direction finishes early instead of waiting for a dense
 // one. Entries and recorded partials are loaded straight from global memory (L2-resident,
 // one coalesced 256-byte request per partial) and software-pipelined through registers:
-// entries two groups of kGroup ahead, partials one group ahead. Shared memory holds only
+// entries two groups of G ahead, partials one group ahead. Shared memory holds only
 // the work vector, w[slot][lane], so as many warps fit as the work vector allows.
 //
 // Entry: {a, b, c, meta}; a/b/c are slot byte offsets (slot*256) or I/O indices; meta bits
@@ -422,7 +422,6 @@ __global__ void __launch_bounds__(32 * DW) k_adjoint_tape(const __grid_constant_
 // receives a contribution, 8/16 it is the first one), 5-8 kind, 9-10 recorded-partial mask,
 // 11-31 index of the instruction's first recorded partial.
 // ---------------------------------------------------------------------------------------------
-constexpr int kGroup = 8;
 
 __device__ __forceinline__ double& wreg(unsigned char* base, unsigned off) {
   return *reinterpret_cast<double*>(base + off);
@@ -442,11 +441,11 @@ __device__ __forceinline__ double ld_partial(const double* p) {
   return kNC ? __ldg(p) : __ldcg(p);
 }
 
-template <bool kNC = true>
-__device__ __forceinline__ void load_partials(const uint4 (&E)[kGroup], const double* pt,
-                                              double (&P0)[kGroup], double (&P1)[kGroup]) {
+template <bool kNC, int G>
+__device__ __forceinline__ void load_partials(const uint4 (&E)[G], const double* pt,
+                                              double (&P0)[G], double (&P1)[G]) {
 #pragma unroll
-  for (int i = 0; i < kGroup; ++i) {
+  for (int i = 0; i < G; ++i) {
     const unsigned m = ent_pmask(E[i].w);
     const size_t pk = ent_pk(E[i].w);
     P0[i] = (m & 1u) ? ld_partial<kNC>(pt + pk * 32) : 1.0;
@@ -454,22 +453,24 @@ __device__ __forceinline__ void load_partials(const uint4 (&E)[kGroup], const do
   }
 }
 
-__device__ __forceinline__ void load_group(const uint4* st, int g, int ngr, uint4 (&E)[kGroup]) {
+template <int G>
+__device__ __forceinline__ void load_group(const uint4* st, int g, int ngr, uint4 (&E)[G]) {
 #pragma unroll
-  for (int i = 0; i < kGroup; ++i)
-    E[i] = g < ngr ? __ldg(st + g * kGroup + i) : make_uint4(0, 0, 0, 0);
+  for (int i = 0; i < G; ++i)
+    E[i] = g < ngr ? __ldg(st + g * G + i) : make_uint4(0, 0, 0, 0);
 }
 
-template <int DW>
-__global__ void __launch_bounds__(32 * DW) k_tangent(const __grid_constant__ SweepArgs a) {
+// G: entries per software-pipeline group; MB: minimum resident CTAs per SM the register
+// allocation must allow (1: unconstrained). The variants trade prefetch depth for occupancy.
+template <int G, int MB>
+__global__ void __launch_bounds__(32, MB) k_tangent(const __grid_constant__ SweepArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  unsigned char* wb = smem + static_cast<size_t>(warp) * a.t.sz_w * 256 + lane * 8;
+  const int lane = threadIdx.x & 31;
+  unsigned char* wb = smem + lane * 8;
   const long long ntiles = (a.n + 31) / 32;
   const long long nwork = ntiles * a.ndir;
-  const long long wstride = static_cast<long long>(gridDim.x) * DW;
-  for (long long work = static_cast<long long>(blockIdx.x) * DW + warp; work < nwork;
-       work += wstride) {
+  const long long wstride = gridDim.x;
+  for (long long work = blockIdx.x; work < nwork; work += wstride) {
     const long long tile = work / a.ndir;
     const int dir = static_cast<int>(work % a.ndir);
     const long long il = tile * 32 + lane;
@@ -477,21 +478,21 @@ __global__ void __launch_bounds__(32 * DW) k_tangent(const __grid_constant__ Swe
     const long long ig = a.i_begin + il;
     const int2 se = __ldg(a.dchunks + dir);  // (first entry, entry count) of this direction
     const uint4* st = a.dstream + se.x;
-    const int ngr = se.y / kGroup;
+    const int ngr = se.y / G;
     const double* pt = a.partials + static_cast<size_t>(tile) * a.t.n_partials * 32 + lane;
-    uint4 E0[kGroup], E1[kGroup];
-    double P0[kGroup], Q0[kGroup];
-    load_group(st, 0, ngr, E0);
-    load_group(st, 1, ngr, E1);
-    load_partials(E0, pt, P0, Q0);
+    uint4 E0[G], E1[G];
+    double P0[G], Q0[G];
+    load_group<G>(st, 0, ngr, E0);
+    load_group<G>(st, 1, ngr, E1);
+    load_partials<true, G>(E0, pt, P0, Q0);
 #pragma unroll 1
     for (int g = 0; g < ngr; ++g) {
-      uint4 E2[kGroup];
-      double P1[kGroup], Q1[kGroup];
-      load_group(st, g + 2, ngr, E2);
-      load_partials(E1, pt, P1, Q1);
+      uint4 E2[G];
+      double P1[G], Q1[G];
+      load_group<G>(st, g + 2, ngr, E2);
+      load_partials<true, G>(E1, pt, P1, Q1);
 #pragma unroll
-      for (int i = 0; i < kGroup; ++i) {
+      for (int i = 0; i < G; ++i) {
         const uint4 cur = E0[i];
         const unsigned meta = cur.w;
         // one jump-table dispatch on (kind, active operands): every case holds only the FP64
@@ -540,7 +541,7 @@ __global__ void __launch_bounds__(32 * DW) k_tangent(const __grid_constant__ Swe
         wreg(wb, cur.x) = r;
       }
 #pragma unroll
-      for (int i = 0; i < kGroup; ++i) {
+      for (int i = 0; i < G; ++i) {
         E0[i] = E1[i];
         E1[i] = E2[i];
         P0[i] = P1[i];
@@ -552,24 +553,24 @@ __global__ void __launch_bounds__(32 * DW) k_tangent(const __grid_constant__ Swe
 
 // One adjoint sweep of one 32-instance tile by one warp: entry stream st (ngr groups),
 // recorded partials at pt (lane-offset, tile-local), work vector at wb (lane-offset).
-template <bool kNC = true>
+template <bool kNC, int G>
 __device__ __forceinline__ void adjoint_walk(const uint4* st, int ngr, const double* pt,
                                              unsigned char* wb, const IoDesc* seed,
                                              const IoDesc* sens, bool active, long long dir,
                                              long long ig) {
-  uint4 E0[kGroup], E1[kGroup];
-  double P0[kGroup], Q0[kGroup];
-  load_group(st, ngr - 1, ngr, E0);
-  load_group(st, ngr - 2 >= 0 ? ngr - 2 : ngr, ngr, E1);
-  load_partials<kNC>(E0, pt, P0, Q0);
+  uint4 E0[G], E1[G];
+  double P0[G], Q0[G];
+  load_group<G>(st, ngr - 1, ngr, E0);
+  load_group<G>(st, ngr - 2 >= 0 ? ngr - 2 : ngr, ngr, E1);
+  load_partials<kNC, G>(E0, pt, P0, Q0);
 #pragma unroll 1
   for (int g = ngr - 1; g >= 0; --g) {
-    uint4 E2[kGroup];
-    double P1[kGroup], Q1[kGroup];
-    load_group(st, g - 2 >= 0 ? g - 2 : ngr, ngr, E2);
-    load_partials<kNC>(E1, pt, P1, Q1);
+    uint4 E2[G];
+    double P1[G], Q1[G];
+    load_group<G>(st, g - 2 >= 0 ? g - 2 : ngr, ngr, E2);
+    load_partials<kNC, G>(E1, pt, P1, Q1);
 #pragma unroll
-    for (int i = kGroup - 1; i >= 0; --i) {
+    for (int i = G - 1; i >= 0; --i) {
       const uint4 cur = E0[i];
       const unsigned meta = cur.w;
       const unsigned f = ent_flags(meta);
@@ -653,7 +654,7 @@ __device__ __forceinline__ void adjoint_walk(const uint4* st, int ngr, const dou
       }
     }
 #pragma unroll
-    for (int i = 0; i < kGroup; ++i) {
+    for (int i = 0; i < G; ++i) {
       E0[i] = E1[i];
       E1[i] = E2[i];
       P0[i] = P1[i];
@@ -664,20 +665,19 @@ __device__ __forceinline__ void adjoint_walk(const uint4* st, int ngr, const dou
 
 // Flags (bits 0-4): 2/4 operand b/c receives a contribution, 8/16 it is the first one
 // (1 marks an entry with work; outputs carry 8 when their seed is the slot's first).
-template <int DW>
-__global__ void __launch_bounds__(32 * DW) k_adjoint(const __grid_constant__ SweepArgs a) {
+template <int G, int MB>
+__global__ void __launch_bounds__(32, MB) k_adjoint(const __grid_constant__ SweepArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  unsigned char* wb = smem + static_cast<size_t>(warp) * a.t.sz_w * 256 + lane * 8;
+  const int lane = threadIdx.x & 31;
+  unsigned char* wb = smem + lane * 8;
   const long long ntiles = (a.n + 31) / 32;
   const long long nwork = ntiles * a.ndir;
-  const long long wstride = static_cast<long long>(gridDim.x) * DW;
+  const long long wstride = gridDim.x;
   const int2 se = __ldg(a.dchunks);
-  const int ngr = se.y / kGroup;
+  const int ngr = se.y / G;
   const uint4* st = a.dstream + se.x;
   for (int q = 0; q < a.t.sz_w; ++q) wreg(wb, q * 256) = 0.0;
-  for (long long work = static_cast<long long>(blockIdx.x) * DW + warp; work < nwork;
-       work += wstride) {
+  for (long long work = blockIdx.x; work < nwork; work += wstride) {
     const long long tile = work / a.ndir;
     const int dir = static_cast<int>(work % a.ndir);
     const long long il = tile * 32 + lane;
@@ -692,7 +692,7 @@ __global__ void __launch_bounds__(32 * DW) k_adjoint(const __grid_constant__ Swe
       }
     }
     const double* pt = a.partials + static_cast<size_t>(tile) * a.t.n_partials * 32 + lane;
-    adjoint_walk(st, ngr, pt, wb, a.seed, a.sens, active, dir, ig);
+    adjoint_walk<true, G>(st, ngr, pt, wb, a.seed, a.sens, active, dir, ig);
   }
 }
 
@@ -752,7 +752,7 @@ __device__ __forceinline__ void primal_walk(const TapeView& t, int n_code, doubl
   }
 }
 
-__global__ void __launch_bounds__(32) k_batch(const __grid_constant__ BatchArgs b) {
+__global__ void __launch_bounds__(32, 16) k_batch(const __grid_constant__ BatchArgs b) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x;
   unsigned char* wb = smem + lane * 8;
@@ -783,7 +783,7 @@ __global__ void __launch_bounds__(32) k_batch(const __grid_constant__ BatchArgs 
           if (d.ptr) static_cast<double*>(d.ptr)[io_off(d, dir, jk.y, il)] = 0.0;
         }
       }
-      adjoint_walk<false>(it.adj_stream, it.adj_ngr, pt, wb, io + 2 * kMaxIo, io + 3 * kMaxIo,
+      adjoint_walk<false, kBatchGroup>(it.adj_stream, it.adj_ngr, pt, wb, io + 2 * kMaxIo, io + 3 * kMaxIo,
                           active, dir, il);
     }
   }
@@ -947,24 +947,25 @@ cudaError_t launch_sp_reverse(const SweepArgs& a, int grid, cudaStream_t s) {
   CGB_DISPATCH_BS(k_sp_reverse)
 }
 
-#define CGB_DISPATCH_DW(KT)                                                           \
-  switch (a.block / 32) {                                                             \
-    case 1: return launch_k(KT<1>, dim3(grid), 32, smem, a, s);                       \
-    case 2: return launch_k(KT<2>, dim3(grid), 64, smem, a, s);                       \
-    case 4: return launch_k(KT<4>, dim3(grid), 128, smem, a, s);                      \
-    case 6: return launch_k(KT<6>, dim3(grid), 192, smem, a, s);                      \
-    case 8: return launch_k(KT<8>, dim3(grid), 256, smem, a, s);                      \
-    default: return cudaErrorInvalidValue;                                            \
+// Derivative-sweep variants (G entries per group, MB minimum CTAs per SM), see DirVariant.
+#define CGB_DISPATCH_VARIANT(KT)                                            \
+  switch (variant) {                                                        \
+    case DV_G8: return launch_k(KT<8, 1>, dim3(grid), 32, smem, a, s);      \
+    case DV_G4: return launch_k(KT<4, 1>, dim3(grid), 32, smem, a, s);      \
+    case DV_G4_R128: return launch_k(KT<4, 16>, dim3(grid), 32, smem, a, s); \
+    case DV_G4_R80: return launch_k(KT<4, 24>, dim3(grid), 32, smem, a, s);  \
+    case DV_G8_R128: return launch_k(KT<8, 16>, dim3(grid), 32, smem, a, s); \
+    default: return cudaErrorInvalidValue;                                  \
   }
 
-cudaError_t launch_tangent(const SweepArgs& a, int grid, cudaStream_t s) {
-  const size_t smem = smem_lean(a.t.sz_w, a.block / 32, a.chunk);
-  CGB_DISPATCH_DW(k_tangent)
+cudaError_t launch_tangent(const SweepArgs& a, int grid, int variant, cudaStream_t s) {
+  const size_t smem = smem_lean(a.t.sz_w, 1, 0);
+  CGB_DISPATCH_VARIANT(k_tangent)
 }
 
-cudaError_t launch_adjoint(const SweepArgs& a, int grid, cudaStream_t s) {
-  const size_t smem = smem_lean(a.t.sz_w, a.block / 32, a.chunk);
-  CGB_DISPATCH_DW(k_adjoint)
+cudaError_t launch_adjoint(const SweepArgs& a, int grid, int variant, cudaStream_t s) {
+  const size_t smem = smem_lean(a.t.sz_w, 1, 0);
+  CGB_DISPATCH_VARIANT(k_adjoint)
 }
 
 cudaError_t launch_adjoint_dense(const SweepArgs& a, int grid, cudaStream_t s) {
@@ -1046,13 +1047,16 @@ int occupancy_dense(int dir_warps, size_t smem) {
   }
 }
 
-int occupancy_dir(int dir_warps, size_t smem) {
-  switch (dir_warps) {
-    case 1: return occ_of(k_tangent<1>, 32, smem);
-    case 2: return occ_of(k_tangent<2>, 64, smem);
-    case 4: return occ_of(k_tangent<4>, 128, smem);
-    case 6: return occ_of(k_tangent<6>, 192, smem);
-    case 8: return occ_of(k_tangent<8>, 256, smem);
+int occupancy_dir(int variant, bool adjoint, size_t smem) {
+  switch (variant) {
+#define CGB_OCC(V, G, MB) \
+  case V: return adjoint ? occ_of(k_adjoint<G, MB>, 32, smem) : occ_of(k_tangent<G, MB>, 32, smem);
+    CGB_OCC(DV_G8, 8, 1)
+    CGB_OCC(DV_G4, 4, 1)
+    CGB_OCC(DV_G4_R128, 4, 16)
+    CGB_OCC(DV_G4_R80, 4, 24)
+    CGB_OCC(DV_G8_R128, 8, 16)
+#undef CGB_OCC
     default: return 0;
   }
 }

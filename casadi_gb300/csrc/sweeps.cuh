@@ -10,7 +10,8 @@ namespace cgb {
 constexpr int kChunk = 256;      // instructions per staged chunk (2 KiB), value sweeps
 constexpr int kPofsGran = 16;    // granularity of the per-chunk partial offsets
 constexpr int kLeanPB = 63;      // partials per staged chunk block (plan-free adjoint)
-constexpr int kEntGroup = 8;     // entries per software-pipelined group (derivative sweeps)
+constexpr int kEntGroup = 8;     // entry streams are padded to a multiple of this
+constexpr int kBatchGroup = 4;   // entries per software-pipelined group in the batch kernel
 constexpr unsigned kMaxPartials = 1u << 21;  // recorded partials per instance the entries address
 
 // Entry kinds of the lean derivative streams (bits 16-19 of an entry's meta word).
@@ -82,7 +83,7 @@ struct BatchItem {
   long long n;              // instances
   const IoDesc* io;         // 4*kMaxIo descriptors: inputs, outputs, adjoint seeds, sensitivities
   const uint4* adj_stream;  // adjoint entry stream (ndir > 0)
-  int adj_ngr;              // its groups of kEntGroup entries
+  int adj_ngr;              // its groups of kBatchGroup entries
   const int2* zero_in;      // inputs with a structurally zero adjoint
   int n_zero;
 };
@@ -113,8 +114,12 @@ cudaError_t launch_eval(const SweepArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_record(const SweepArgs& a, int grid, cudaStream_t s);
 // Derivative sweeps: 1-D grid whose size is a multiple of the direction-group count
 // ceil(ndir / (block/32)); CTA b works on direction group b % groups.
-cudaError_t launch_tangent(const SweepArgs& a, int grid, cudaStream_t s);
-cudaError_t launch_adjoint(const SweepArgs& a, int grid, cudaStream_t s);
+// Variants of the warp-independent derivative sweeps: entries per software-pipeline group
+// (8 or 4) and a register cap that lets more one-warp CTAs reside per SM. All variants do the
+// same arithmetic in the same order; only speed differs, so the host may pick any.
+enum DirVariant : int { DV_G8 = 0, DV_G4, DV_G4_R128, DV_G4_R80, DV_G8_R128, DV_COUNT };
+cudaError_t launch_tangent(const SweepArgs& a, int grid, int variant, cudaStream_t s);
+cudaError_t launch_adjoint(const SweepArgs& a, int grid, int variant, cudaStream_t s);
 // The adjoint sweep without an activity plan (see k_adjoint<DW, true>).
 cudaError_t launch_adjoint_dense(const SweepArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_sp_forward(const SweepArgs& a, int grid, cudaStream_t s);
@@ -122,7 +127,7 @@ cudaError_t launch_sp_reverse(const SweepArgs& a, int grid, cudaStream_t s);
 
 // Resident CTAs per SM for a given kernel family and shared-memory footprint.
 int occupancy_primal(int block, size_t smem);
-int occupancy_dir(int dir_warps, size_t smem);     // lean derivative sweeps
+int occupancy_dir(int variant, bool adjoint, size_t smem);  // warp-independent sweeps
 int occupancy_dense(int dir_warps, size_t smem);   // plan-free adjoint
 
 }  // namespace cgb

@@ -59,6 +59,7 @@ def load(path=None):
         "casadi_gb300_version": (ct.c_char_p, []),
         "casadi_gb300_tape_create": (cint, [vp, cint, cint, vp, cint, vp, cint]),
         "casadi_gb300_tape_free": (cint, [cint]),
+        "casadi_gb300_tape_schedule": (cint, [vp, cint, cint, vp, cint, vp, cint, vp, vp]),
         "casadi_gb300_tape_info": (cint, [cint, vp, vp, vp, vp, vp]),
         "casadi_gb300_scratch_size": (cint, [cint, i64, vp]),
         "casadi_gb300_scratch_min": (cint, [cint, vp]),
@@ -77,6 +78,9 @@ def load(path=None):
         "casadi_gb300_reverse_noalloc": (cint, [cint, i64, i64, cint, vp, vp, vp, vp, vp]),
         "casadi_gb300_profile": (cint, [cint]),
         "casadi_gb300_profile_collect": (cint, [vp, vp, cint]),
+        "casadi_gb300_autotune": (cint, [cint]),
+        "casadi_gb300_tuned_variant": (cint, [cint, cint, vp]),
+        "casadi_gb300_set_variant": (cint, [cint, cint, cint]),
         "casadi_gb300_batch_create": (cint, []),
         "casadi_gb300_batch_free": (cint, [cint]),
         "casadi_gb300_batch_add": (cint, [cint, cint, i64, i64, cint, vp, vp, vp, vp]),
@@ -110,6 +114,25 @@ def _stream_handle(stream):
         import torch
         return ct.c_void_p(torch.cuda.current_stream().cuda_stream)
     return ct.c_void_p(getattr(stream, "cuda_stream", stream))
+
+
+def schedule(tape):
+    """The tape in the order and slots the GPU sweeps run it (host only, no device needed):
+    returns a new :class:`sx.Tape` with the same instructions reordered for fewer live values
+    and a shorter work vector."""
+    if isinstance(tape, _sx.Function):
+        tape = tape.tape
+    lib = load()
+    atoms = tape.atomic_array()
+    out = np.zeros_like(atoms)
+    nnz_in = np.ascontiguousarray(tape.nnz_in, dtype=np.int32)
+    nnz_out = np.ascontiguousarray(tape.nnz_out, dtype=np.int32)
+    szw = ct.c_int()
+    check(lib.casadi_gb300_tape_schedule(atoms.ctypes.data, tape.n_instr, len(tape.nnz_in),
+                                         nnz_in.ctypes.data, len(tape.nnz_out),
+                                         nnz_out.ctypes.data, tape.sz_w, out.ctypes.data,
+                                         ct.byref(szw)))
+    return _sx.Tape.from_atomic_array(out, tape.nnz_in, tape.nnz_out, szw.value)
 
 
 class CudaTape:
@@ -240,6 +263,16 @@ class CudaTape:
     def sync(self, stream=None):
         check(load().casadi_gb300_sync(self.id, _stream_handle(stream)))
 
+    def set_variant(self, kind, variant):
+        """Fix the derivative-sweep variant of one kind (-1: let the autotuner choose)."""
+        check(load().casadi_gb300_set_variant(self.id, kind, variant))
+
+    def tuned_variant(self, kind):
+        """Derivative-sweep variant the autotuner kept: kind 0 forward, 1 Jacobian, 2 adjoint."""
+        v = ct.c_int()
+        check(load().casadi_gb300_tuned_variant(self.id, kind, ct.byref(v)))
+        return v.value
+
 
 class MapMemory:
     """A checked-out memory object (stream + staging buffers) for the host-buffer path."""
@@ -365,6 +398,8 @@ class Batch:
                                             _stream_handle(stream)))
 
 
+N_VARIANTS = 5
+
 FAMILIES = ("eval", "record", "tangent", "adjoint", "sp_forward", "sp_reverse", "batch")
 
 
@@ -379,6 +414,11 @@ def profile_collect():
     nl = (ct.c_int * len(FAMILIES))()
     check(load().casadi_gb300_profile_collect(ms, nl, len(FAMILIES)))
     return {f: (ms[k], nl[k]) for k, f in enumerate(FAMILIES)}
+
+
+def autotune(enable=True):
+    """Turn the derivative-sweep autotuner on or off (process-wide)."""
+    check(load().casadi_gb300_autotune(1 if enable else 0))
 
 
 def version():

@@ -593,6 +593,17 @@ class Tape:
         a["u"] = np.where(self.op == C.OP_CONST, dbits, ints)
         return a
 
+    @staticmethod
+    def from_atomic_array(a, nnz_in, nnz_out, sz_w):
+        """Inverse of :meth:`atomic_array`."""
+        op = np.asarray(a["op"], np.int32)
+        u = np.asarray(a["u"], np.uint64)
+        is_c = op == C.OP_CONST
+        i1 = np.where(is_c, 0, (u & np.uint64(0xFFFFFFFF)).astype(np.uint32).view(np.int32))
+        i2 = np.where(is_c, 0, (u >> np.uint64(32)).astype(np.uint32).view(np.int32))
+        d = np.where(is_c, u.view(np.float64), 0.0)
+        return Tape(op, np.asarray(a["i0"], np.int32), i1, i2, d, nnz_in, nnz_out, sz_w)
+
     def histogram(self):
         ops, counts = np.unique(self.op, return_counts=True)
         return {C.OP_NAMES.get(int(o), str(int(o))): int(c) for o, c in zip(ops, counts)}

@@ -85,6 +85,20 @@ CASADI_GB300_API int casadi_gb300_tape_create(const casadi_gb300_atomic* alg, in
 /* Release a tape and its device memory. Cf. casadi_c_decref_id (casadi_c.h:113). */
 CASADI_GB300_API int casadi_gb300_tape_free(int id);
 
+/* The tape as the GPU sweeps run it: casadi_gb300_tape_create reorders the instructions so
+ * fewer values are live at once (the work vector of every 32-instance tile sits in shared
+ * memory, and its length decides how many tiles an SM runs at a time) and reassigns the slots.
+ * Each instruction keeps its operation and operand values, and the users of every value keep
+ * their relative order, so values, forward and adjoint sensitivities are bit-identical to the
+ * original order. This entry point returns the scheduled tape (n_instr atomics written to out,
+ * same layout as alg) and its work-vector length, without touching a device. It replaces the
+ * reference's depth-first order and last-in first-out slot assignment for the GPU
+ * (SXFunction::init, casadi/core/sx_function.cpp:530-540 and 690-753); the reference has no
+ * separate call for it. */
+CASADI_GB300_API int casadi_gb300_tape_schedule(const casadi_gb300_atomic* alg, int n_instr,
+                               int n_in, const int* nnz_in, int n_out, const int* nnz_out,
+                               int sz_w, casadi_gb300_atomic* out, int* sz_w_out);
+
 /* Shape queries. Cf. casadi_c_n_in_id/casadi_c_n_out_id/casadi_c_work_id (casadi_c.h:115-124):
  * sz_w is the tape's work-vector length; n_partials the partial derivatives one instance
  * records for the AD sweeps. */
@@ -166,6 +180,18 @@ CASADI_GB300_API int casadi_gb300_map_jacobian(int id, int mem, int64_t n, const
 CASADI_GB300_API int casadi_gb300_map_reverse(int id, int mem, int64_t n, int nadj, const double* const* arg,
                              double* const* res, const double* const* aseed,
                              double* const* asens);
+
+/* Autotuning of the derivative sweeps (on by default): the first call of each kind
+ * (0 seeded forward, 1 Jacobian, 2 adjoint) on a tape whose wave fills the GPU several times
+ * runs each kernel variant once on that wave, keeps the fastest for the tape and synchronizes
+ * the stream once; it is skipped while the stream is being captured into a CUDA graph.
+ * Variants differ only in speed: every variant does the same arithmetic in the same order.
+ * casadi_gb300_tuned_variant reports the kept variant (-1: not tuned yet). No counterpart in
+ * the reference, whose Map has one code path per parallelization (casadi/core/map.cpp:39-51). */
+CASADI_GB300_API int casadi_gb300_autotune(int enable);
+CASADI_GB300_API int casadi_gb300_tuned_variant(int id, int kind, int* variant);
+/* Fixes the variant of one kind on a tape (0..4), or clears it for retuning (-1). */
+CASADI_GB300_API int casadi_gb300_set_variant(int id, int kind, int variant);
 
 /* Persistent multi-tape batches. A batch is a list of items, each one tape over its own
  * instance range (device pointers, instance-minor layout as above): nadj == 0 runs the value

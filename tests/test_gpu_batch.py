@@ -13,6 +13,7 @@ from helpers import RTOL, assert_close, same_bits
 
 pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
+DAG_RTOL = 1e-12
 
 
 def _cuda(a):
@@ -80,17 +81,20 @@ def test_batch_matches_oracle(gpu_lib):
                            [_cuda(s) for s in seeds] if seeds else None)
         queued.append((f, n, args, seeds, res, asens, t))
     b.run()
-    for f, n, args, seeds, res, asens, t in queued:
+    for k, (f, n, args, seeds, res, asens, t) in enumerate(queued):
         t.sync()
+        # thousands of sin/cos/exp/tanh nodes carry the <= 1-ulp differences between CUDA's and
+        # the host libm into the adjoint (measured 2.6e-13 on the 3000-node DAG)
+        rtol = RTOL if f.tape.n_instr < 1000 else DAG_RTOL
         want = O.eval(f.tape, args, n)
         for j, (g, w) in enumerate(zip(res, want)):
-            assert_close(g.cpu().numpy(), w, "batch value %d" % j, rtol=RTOL)
+            assert_close(g.cpu().numpy(), w, "item %d value %d" % (k, j), rtol=rtol)
         if seeds:
             for d in range(seeds[0].shape[0]):
                 _, ws = O.reverse(f.tape, args, [s[d:d + 1] for s in seeds], n)
                 for j, w in enumerate(ws):
-                    assert_close(asens[j][d].cpu().numpy(), w[0], "batch adjoint %d/%d" % (d, j),
-                                 rtol=RTOL)
+                    assert_close(asens[j][d].cpu().numpy(), w[0],
+                                 "item %d adjoint %d/%d" % (k, d, j), rtol=rtol)
 
 
 def test_batch_graph_replay_sees_new_inputs(gpu_lib):

@@ -341,3 +341,48 @@ def test_map_eval_and_reverse_host_buffers(gpu_lib):
     _, wasens = O.reverse(f.tape, [x, u], [np.transpose(aseed, (1, 2, 0))], n)
     assert_close(np.transpose(asens[0], (1, 2, 0)), wasens[0], "map reverse x")
     assert_close(np.transpose(asens[1], (1, 2, 0)), wasens[1], "map reverse u")
+
+
+# ---- derivative-sweep variants and the autotuner ------------------------------------------------
+def test_every_variant_gives_the_same_bits(gpu_lib):
+    """The variants differ in prefetch depth and register cap only: forward, Jacobian and
+    adjoint results must be identical bit for bit across all of them."""
+    from casadi_gb300 import runtime as R
+    F = W.cartpole_rollout(6)
+    n = 2500
+    args = dev(W.cartpole_inputs(n, steps=6, seed=21))
+    rng = np.random.default_rng(21)
+    fseeds = dev([rng.standard_normal((3, k, n)) for k in F.tape.nnz_in])
+    aseeds = dev([rng.standard_normal((2, k, n)) for k in F.tape.nnz_out])
+    ct = CudaTape(F)
+    base = None
+    for v in range(R.N_VARIANTS):
+        for kind in range(3):
+            ct.set_variant(kind, v)
+        got = [host(ct.forward(args, fseeds)[1]), host(ct.jacobian(args)[1]),
+               host(ct.reverse(args, aseeds)[1])]
+        if base is None:
+            base = got
+            continue
+        for g, b in zip(got, base):
+            for x, y in zip(g, b):
+                assert_bitexact(x, y, "variant %d" % v)
+    ct.sync()
+
+
+def test_autotuner_keeps_a_variant_and_results(gpu_lib):
+    from casadi_gb300 import runtime as R
+    F = W.cartpole_rollout(4)
+    n = 400000  # a wave that fills the GPU several times over
+    args = dev(W.cartpole_inputs(n, steps=4, seed=22))
+    aseeds = dev([np.ones((1, 4, n)), np.ones((1, 1, n))])
+    ct = CudaTape(F)
+    ct.set_variant(2, 0)
+    _, want = ct.reverse(args, aseeds)
+    ct.set_variant(2, -1)
+    R.autotune(True)
+    _, got = ct.reverse(args, aseeds)
+    assert 0 <= ct.tuned_variant(2) < R.N_VARIANTS
+    for x, y in zip(host(got), host(want)):
+        assert_bitexact(x, y, "autotuned adjoint")
+    ct.sync()
