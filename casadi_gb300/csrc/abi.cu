@@ -617,15 +617,22 @@ int run_ad(Tape& t, long long n, const IoDesc* in, const IoDesc* out, const IoDe
         a.n_zero = ap->n_zero;
       }
       const long long work = (m + 31) / 32 * ndir;
+      // a variant whose work vector (IPT tiles per warp) does not fit is never launched
+      auto fits = [&](int v) {
+        return smem_lean(t.sz_w, variant_ipt(v), 0) <= static_cast<size_t>(max_smem_optin());
+      };
       auto grid_of = [&](int v) {
-        const int occ = std::max(1, occupancy_dir(v, adjoint, dsmem));
+        const int ipt = variant_ipt(v);
+        const long long vwork = ((m + 31) / 32 + ipt - 1) / ipt * ndir;
+        const int occ = std::max(1, occupancy_dir(v, adjoint, smem_lean(t.sz_w, ipt, 0)));
         return static_cast<int>(std::max<long long>(
-            1, std::min<long long>(work, static_cast<long long>(sms) * occ)));
+            1, std::min<long long>(vwork, static_cast<long long>(sms) * occ)));
       };
       auto launch = [&](int v) {
         return adjoint ? launch_adjoint(a, grid_of(v), v, s) : launch_tangent(a, grid_of(v), v, s);
       };
       int variant = t.tuned[kind];
+      if (variant >= 0 && !fits(variant)) variant = -1;
       if (variant < 0) {
         cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
         cudaStreamIsCapturing(s, &cs);
@@ -633,6 +640,7 @@ int run_ad(Tape& t, long long n, const IoDesc* in, const IoDesc* out, const IoDe
         if (g_autotune && cs == cudaStreamCaptureStatusNone && work >= 2ll * sms * 8) {
           float best = 0;
           for (int v = 0; v < DV_COUNT; ++v) {
+            if (!fits(v)) continue;
             float ms = 0;
             if (int rc = time_once(s, [&] { return launch(v); }, &ms)) return rc;
             if (variant < 0 || ms < best) {
@@ -641,7 +649,7 @@ int run_ad(Tape& t, long long n, const IoDesc* in, const IoDesc* out, const IoDe
             }
           }
           t.tuned[kind] = variant;
-          continue;  // the last variant's run already produced this wave's results
+          continue;  // every variant's run produced this wave's (identical) results
         }
         variant = kDefaultVariant;
       }

@@ -441,18 +441,6 @@ __device__ __forceinline__ double ld_partial(const double* p) {
   return kNC ? __ldg(p) : __ldcg(p);
 }
 
-template <bool kNC, int G>
-__device__ __forceinline__ void load_partials(const uint4 (&E)[G], const double* pt,
-                                              double (&P0)[G], double (&P1)[G]) {
-#pragma unroll
-  for (int i = 0; i < G; ++i) {
-    const unsigned m = ent_pmask(E[i].w);
-    const size_t pk = ent_pk(E[i].w);
-    P0[i] = (m & 1u) ? ld_partial<kNC>(pt + pk * 32) : 1.0;
-    P1[i] = (m & 2u) ? ld_partial<kNC>(pt + (pk + ((m & 1u) ? 1 : 0)) * 32) : 0.0;
-  }
-}
-
 template <int G>
 __device__ __forceinline__ void load_group(const uint4* st, int g, int ngr, uint4 (&E)[G]) {
 #pragma unroll
@@ -461,36 +449,69 @@ __device__ __forceinline__ void load_group(const uint4* st, int g, int ngr, uint
 }
 
 // G: entries per software-pipeline group; MB: minimum resident CTAs per SM the register
-// allocation must allow (1: unconstrained). The variants trade prefetch depth for occupancy.
-template <int G, int MB>
+// allocation must allow (1: unconstrained); IPT: 32-instance tiles per warp (each lane
+// carries IPT instances of the same direction, whose FP64 chains are independent). The work
+// vector is w[slot][j][lane]: byte offset slot*256*IPT + j*256 + lane*8.
+template <int IPT>
+__device__ __forceinline__ double& wj(unsigned char* wb, unsigned off, int j) {
+  return wreg(wb, off * IPT + j * 256);
+}
+
+// Partials of one group of entries for IPT tiles (tile j's block at pt + j*tstride; tiles
+// past the wave's end are not read).
+template <bool kNC, int G, int IPT>
+__device__ __forceinline__ void load_partials_n(const uint4 (&E)[G], const double* pt,
+                                                size_t tstride, const bool (&tok)[IPT],
+                                                double (&P0)[G][IPT], double (&P1)[G][IPT]) {
+#pragma unroll
+  for (int i = 0; i < G; ++i) {
+    const unsigned m = ent_pmask(E[i].w);
+    const size_t pk = ent_pk(E[i].w);
+    const size_t k1 = pk + ((m & 1u) ? 1 : 0);
+#pragma unroll
+    for (int j = 0; j < IPT; ++j) {
+      P0[i][j] = ((m & 1u) && tok[j]) ? ld_partial<kNC>(pt + j * tstride + pk * 32) : 1.0;
+      P1[i][j] = ((m & 2u) && tok[j]) ? ld_partial<kNC>(pt + j * tstride + k1 * 32) : 0.0;
+    }
+  }
+}
+
+template <int G, int MB, int IPT>
 __global__ void __launch_bounds__(32, MB) k_tangent(const __grid_constant__ SweepArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x & 31;
   unsigned char* wb = smem + lane * 8;
   const long long ntiles = (a.n + 31) / 32;
-  const long long nwork = ntiles * a.ndir;
-  const long long wstride = gridDim.x;
-  for (long long work = blockIdx.x; work < nwork; work += wstride) {
-    const long long tile = work / a.ndir;
+  const long long nwork = (ntiles + IPT - 1) / IPT * a.ndir;
+  const size_t tstride = static_cast<size_t>(a.t.n_partials) * 32;
+  for (long long work = blockIdx.x; work < nwork; work += gridDim.x) {
+    const long long tg = work / a.ndir;
     const int dir = static_cast<int>(work % a.ndir);
-    const long long il = tile * 32 + lane;
-    const bool active = il < a.n;
-    const long long ig = a.i_begin + il;
+    bool active[IPT], tok[IPT];
+    long long ig[IPT];
+#pragma unroll
+    for (int j = 0; j < IPT; ++j) {
+      const long long tile = tg * IPT + j;
+      const long long il = tile * 32 + lane;
+      tok[j] = tile < ntiles;
+      active[j] = il < a.n;
+      ig[j] = a.i_begin + il;
+    }
     const int2 se = __ldg(a.dchunks + dir);  // (first entry, entry count) of this direction
     const uint4* st = a.dstream + se.x;
     const int ngr = se.y / G;
-    const double* pt = a.partials + static_cast<size_t>(tile) * a.t.n_partials * 32 + lane;
+    const double* pt = a.partials + static_cast<size_t>(tg * IPT) * tstride + lane;
     uint4 E0[G], E1[G];
-    double P0[G], Q0[G];
+    double P0[G][IPT], Q0[G][IPT];
     load_group<G>(st, 0, ngr, E0);
     load_group<G>(st, 1, ngr, E1);
-    load_partials<true, G>(E0, pt, P0, Q0);
+    load_partials_n<true, G, IPT>(E0, pt, tstride, tok, P0, Q0);
 #pragma unroll 1
     for (int g = 0; g < ngr; ++g) {
       uint4 E2[G];
-      double P1[G], Q1[G];
+      double P1[G][IPT], Q1[G][IPT];
       load_group<G>(st, g + 2, ngr, E2);
-      load_partials<true, G>(E1, pt, P1, Q1);
+      load_partials_n<true, G, IPT>(E1, pt, tstride, tok, P1, Q1);
 #pragma unroll
       for (int i = 0; i < G; ++i) {
         const uint4 cur = E0[i];
@@ -499,76 +520,94 @@ __global__ void __launch_bounds__(32, MB) k_tangent(const __grid_constant__ Swee
         // operations it needs, so nothing is computed speculatively (an FP64 instruction holds
         // a sub-partition's FP64 unit for ~64 cycles on GB300)
         const unsigned key = (ent_kind(meta) << 2) | (ent_flags(meta) & 3u);
-        double r;
+        double r[IPT];
+#define CGB_J _Pragma("unroll") for (int j = 0; j < IPT; ++j)
         switch (key) {
           case (LK_OUTPUT << 2) | 0u:
           case (LK_OUTPUT << 2) | 1u: {
             const IoDesc& d = a.sens[cur.x];
-            if (active && d.ptr)
-              static_cast<double*>(d.ptr)[io_off(d, dir, cur.z, ig)] =
-                  (meta & 1u) ? wreg(wb, cur.y) : 0.0;
+            CGB_J {
+              if (active[j] && d.ptr)
+                static_cast<double*>(d.ptr)[io_off(d, dir, cur.z, ig[j])] =
+                    (meta & 1u) ? wj<IPT>(wb, cur.y, j) : 0.0;
+            }
             continue;
           }
           case (LK_INPUT << 2) | 1u:
             if (a.identity_seed) {
-              r = 1.0;
+              CGB_J r[j] = 1.0;
             } else {
               const IoDesc& d = a.seed[cur.y];
-              r = active ? __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir, cur.z, ig)) : 0.0;
+              CGB_J r[j] = active[j]
+                  ? __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir, cur.z, ig[j])) : 0.0;
             }
             break;
-          case (LK_GEN << 2) | 1u: r = __dmul_rn(P0[i], wreg(wb, cur.y)); break;
-          case (LK_GEN << 2) | 2u: r = __dmul_rn(Q0[i], wreg(wb, cur.z)); break;
+          case (LK_GEN << 2) | 1u: CGB_J r[j] = __dmul_rn(P0[i][j], wj<IPT>(wb, cur.y, j)); break;
+          case (LK_GEN << 2) | 2u: CGB_J r[j] = __dmul_rn(Q0[i][j], wj<IPT>(wb, cur.z, j)); break;
           case (LK_GEN << 2) | 3u:
-            r = __dadd_rn(__dmul_rn(P0[i], wreg(wb, cur.y)), __dmul_rn(Q0[i], wreg(wb, cur.z)));
+            CGB_J r[j] = __dadd_rn(__dmul_rn(P0[i][j], wj<IPT>(wb, cur.y, j)),
+                                   __dmul_rn(Q0[i][j], wj<IPT>(wb, cur.z, j)));
             break;
-          case (LK_ADD << 2) | 1u: r = wreg(wb, cur.y); break;
-          case (LK_ADD << 2) | 2u: r = wreg(wb, cur.z); break;
-          case (LK_ADD << 2) | 3u: r = __dadd_rn(wreg(wb, cur.y), wreg(wb, cur.z)); break;
-          case (LK_SUB << 2) | 1u: r = wreg(wb, cur.y); break;
-          case (LK_SUB << 2) | 2u: r = d_neg(wreg(wb, cur.z)); break;
-          case (LK_SUB << 2) | 3u: r = __dsub_rn(wreg(wb, cur.y), wreg(wb, cur.z)); break;
-          case (LK_NEG << 2) | 1u: r = d_neg(wreg(wb, cur.y)); break;
-          case (LK_TWICE << 2) | 1u: {
-            const double xb = wreg(wb, cur.y);
-            r = __dadd_rn(xb, xb);
-          } break;
-          case (LK_ASSIGN << 2) | 1u: r = wreg(wb, cur.y); break;
-          case (LK_IFZ << 2) | 2u: r = d_iszero(Q0[i]) ? 0.0 : wreg(wb, cur.z); break;
+          case (LK_ADD << 2) | 1u: CGB_J r[j] = wj<IPT>(wb, cur.y, j); break;
+          case (LK_ADD << 2) | 2u: CGB_J r[j] = wj<IPT>(wb, cur.z, j); break;
+          case (LK_ADD << 2) | 3u:
+            CGB_J r[j] = __dadd_rn(wj<IPT>(wb, cur.y, j), wj<IPT>(wb, cur.z, j));
+            break;
+          case (LK_SUB << 2) | 1u: CGB_J r[j] = wj<IPT>(wb, cur.y, j); break;
+          case (LK_SUB << 2) | 2u: CGB_J r[j] = d_neg(wj<IPT>(wb, cur.z, j)); break;
+          case (LK_SUB << 2) | 3u:
+            CGB_J r[j] = __dsub_rn(wj<IPT>(wb, cur.y, j), wj<IPT>(wb, cur.z, j));
+            break;
+          case (LK_NEG << 2) | 1u: CGB_J r[j] = d_neg(wj<IPT>(wb, cur.y, j)); break;
+          case (LK_TWICE << 2) | 1u:
+            CGB_J {
+              const double xb = wj<IPT>(wb, cur.y, j);
+              r[j] = __dadd_rn(xb, xb);
+            }
+            break;
+          case (LK_ASSIGN << 2) | 1u: CGB_J r[j] = wj<IPT>(wb, cur.y, j); break;
+          case (LK_IFZ << 2) | 2u:
+            CGB_J r[j] = d_iszero(Q0[i][j]) ? 0.0 : wj<IPT>(wb, cur.z, j);
+            break;
           default:
             continue;  // NOP padding
         }
-        wreg(wb, cur.x) = r;
+        CGB_J wj<IPT>(wb, cur.x, j) = r[j];
       }
 #pragma unroll
       for (int i = 0; i < G; ++i) {
         E0[i] = E1[i];
         E1[i] = E2[i];
-        P0[i] = P1[i];
-        Q0[i] = Q1[i];
+#pragma unroll
+        for (int j = 0; j < IPT; ++j) {
+          P0[i][j] = P1[i][j];
+          Q0[i][j] = Q1[i][j];
+        }
       }
     }
   }
 }
 
-// One adjoint sweep of one 32-instance tile by one warp: entry stream st (ngr groups),
-// recorded partials at pt (lane-offset, tile-local), work vector at wb (lane-offset).
-template <bool kNC, int G>
+// One adjoint sweep of IPT 32-instance tiles by one warp: entry stream st (ngr groups),
+// recorded partials at pt (lane-offset, first tile; tile j at pt + j*tstride), work vector at
+// wb (lane-offset, w[slot][j][lane]).
+template <bool kNC, int G, int IPT>
 __device__ __forceinline__ void adjoint_walk(const uint4* st, int ngr, const double* pt,
+                                             size_t tstride, const bool (&tok)[IPT],
                                              unsigned char* wb, const IoDesc* seed,
-                                             const IoDesc* sens, bool active, long long dir,
-                                             long long ig) {
+                                             const IoDesc* sens, const bool (&active)[IPT],
+                                             long long dir, const long long (&ig)[IPT]) {
   uint4 E0[G], E1[G];
-  double P0[G], Q0[G];
+  double P0[G][IPT], Q0[G][IPT];
   load_group<G>(st, ngr - 1, ngr, E0);
   load_group<G>(st, ngr - 2 >= 0 ? ngr - 2 : ngr, ngr, E1);
-  load_partials<kNC, G>(E0, pt, P0, Q0);
+  load_partials_n<kNC, G, IPT>(E0, pt, tstride, tok, P0, Q0);
 #pragma unroll 1
   for (int g = ngr - 1; g >= 0; --g) {
     uint4 E2[G];
-    double P1[G], Q1[G];
+    double P1[G][IPT], Q1[G][IPT];
     load_group<G>(st, g - 2 >= 0 ? g - 2 : ngr, ngr, E2);
-    load_partials<kNC, G>(E1, pt, P1, Q1);
+    load_partials_n<kNC, G, IPT>(E1, pt, tstride, tok, P1, Q1);
 #pragma unroll
     for (int i = G - 1; i >= 0; --i) {
       const uint4 cur = E0[i];
@@ -580,74 +619,99 @@ __device__ __forceinline__ void adjoint_walk(const uint4* st, int ngr, const dou
       switch (kind) {
         case LK_OUTPUT: {
           const IoDesc& d = seed[cur.x];
-          const double sd =
-              active ? __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir, cur.z, ig)) : 0.0;
-          double& w = wreg(wb, cur.y);
-          if (f & 8u) w = sd; else w = __dadd_rn(w, sd);
+          CGB_J {
+            const double sd = active[j]
+                ? __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir, cur.z, ig[j])) : 0.0;
+            double& w = wj<IPT>(wb, cur.y, j);
+            if (f & 8u) w = sd; else w = __dadd_rn(w, sd);
+          }
         } break;
         case LK_INPUT: {
           const IoDesc& d = sens[cur.y];
-          if (active && d.ptr)
-            static_cast<double*>(d.ptr)[io_off(d, dir, cur.z, ig)] = wreg(wb, cur.x);
-          wreg(wb, cur.x) = 0.0;
+          CGB_J {
+            if (active[j] && d.ptr)
+              static_cast<double*>(d.ptr)[io_off(d, dir, cur.z, ig[j])] = wj<IPT>(wb, cur.x, j);
+            wj<IPT>(wb, cur.x, j) = 0.0;
+          }
         } break;
         case LK_CONST:
-          wreg(wb, cur.x) = 0.0;
+          CGB_J wj<IPT>(wb, cur.x, j) = 0.0;
           break;
         case LK_NOP:
           break;
         default: {
-          const double seed = wreg(wb, cur.x);
-          wreg(wb, cur.x) = 0.0;
+          double sd[IPT];
+          CGB_J {
+            sd[j] = wj<IPT>(wb, cur.x, j);
+            wj<IPT>(wb, cur.x, j) = 0.0;
+          }
           // contribution to operand b
           switch ((kind << 2) | ((f >> 1) & 1u) | ((f >> 2) & 2u)) {  // (kind, b?, first?)
-            case (LK_GEN << 2) | 1u: {
-              double& w1 = wreg(wb, cur.y);
-              w1 = __dadd_rn(w1, __dmul_rn(P0[i], seed));
-            } break;
-            case (LK_GEN << 2) | 3u: wreg(wb, cur.y) = __dmul_rn(P0[i], seed); break;
-            case (LK_ADD << 2) | 1u: case (LK_SUB << 2) | 1u: case (LK_ASSIGN << 2) | 1u: {
-              double& w1 = wreg(wb, cur.y);
-              w1 = __dadd_rn(w1, seed);
-            } break;
-            case (LK_ADD << 2) | 3u: case (LK_SUB << 2) | 3u: case (LK_ASSIGN << 2) | 3u:
-              wreg(wb, cur.y) = seed;
+            case (LK_GEN << 2) | 1u:
+              CGB_J {
+                double& w1 = wj<IPT>(wb, cur.y, j);
+                w1 = __dadd_rn(w1, __dmul_rn(P0[i][j], sd[j]));
+              }
               break;
-            case (LK_NEG << 2) | 1u: {
-              double& w1 = wreg(wb, cur.y);
-              w1 = __dsub_rn(w1, seed);
-            } break;
-            case (LK_NEG << 2) | 3u: wreg(wb, cur.y) = d_neg(seed); break;
-            case (LK_TWICE << 2) | 1u: {
-              double& w1 = wreg(wb, cur.y);
-              w1 = __dadd_rn(w1, __dadd_rn(seed, seed));
-            } break;
-            case (LK_TWICE << 2) | 3u: wreg(wb, cur.y) = __dadd_rn(seed, seed); break;
+            case (LK_GEN << 2) | 3u: CGB_J wj<IPT>(wb, cur.y, j) = __dmul_rn(P0[i][j], sd[j]); break;
+            case (LK_ADD << 2) | 1u: case (LK_SUB << 2) | 1u: case (LK_ASSIGN << 2) | 1u:
+              CGB_J {
+                double& w1 = wj<IPT>(wb, cur.y, j);
+                w1 = __dadd_rn(w1, sd[j]);
+              }
+              break;
+            case (LK_ADD << 2) | 3u: case (LK_SUB << 2) | 3u: case (LK_ASSIGN << 2) | 3u:
+              CGB_J wj<IPT>(wb, cur.y, j) = sd[j];
+              break;
+            case (LK_NEG << 2) | 1u:
+              CGB_J {
+                double& w1 = wj<IPT>(wb, cur.y, j);
+                w1 = __dsub_rn(w1, sd[j]);
+              }
+              break;
+            case (LK_NEG << 2) | 3u: CGB_J wj<IPT>(wb, cur.y, j) = d_neg(sd[j]); break;
+            case (LK_TWICE << 2) | 1u:
+              CGB_J {
+                double& w1 = wj<IPT>(wb, cur.y, j);
+                w1 = __dadd_rn(w1, __dadd_rn(sd[j], sd[j]));
+              }
+              break;
+            case (LK_TWICE << 2) | 3u: CGB_J wj<IPT>(wb, cur.y, j) = __dadd_rn(sd[j], sd[j]); break;
             default: break;  // operand b receives nothing
           }
           // contribution to operand c
           switch ((kind << 2) | ((f >> 2) & 1u) | ((f >> 3) & 2u)) {  // (kind, c?, first?)
-            case (LK_GEN << 2) | 1u: {
-              double& w2 = wreg(wb, cur.z);
-              w2 = __dadd_rn(w2, __dmul_rn(Q0[i], seed));
-            } break;
-            case (LK_GEN << 2) | 3u: wreg(wb, cur.z) = __dmul_rn(Q0[i], seed); break;
-            case (LK_ADD << 2) | 1u: {
-              double& w2 = wreg(wb, cur.z);
-              w2 = __dadd_rn(w2, seed);
-            } break;
-            case (LK_ADD << 2) | 3u: wreg(wb, cur.z) = seed; break;
-            case (LK_SUB << 2) | 1u: {
-              double& w2 = wreg(wb, cur.z);
-              w2 = __dsub_rn(w2, seed);
-            } break;
-            case (LK_SUB << 2) | 3u: wreg(wb, cur.z) = d_neg(seed); break;
-            case (LK_IFZ << 2) | 1u: {
-              double& w2 = wreg(wb, cur.z);
-              if (!d_iszero(Q0[i])) w2 = __dadd_rn(w2, seed);
-              else w2 = __dadd_rn(w2, 0.0);
-            } break;
-            case (LK_IFZ << 2) | 3u: wreg(wb, cur.z) = d_iszero(Q0[i]) ? 0.0 : seed; break;
+            case (LK_GEN << 2) | 1u:
+              CGB_J {
+                double& w2 = wj<IPT>(wb, cur.z, j);
+                w2 = __dadd_rn(w2, __dmul_rn(Q0[i][j], sd[j]));
+              }
+              break;
+            case (LK_GEN << 2) | 3u: CGB_J wj<IPT>(wb, cur.z, j) = __dmul_rn(Q0[i][j], sd[j]); break;
+            case (LK_ADD << 2) | 1u:
+              CGB_J {
+                double& w2 = wj<IPT>(wb, cur.z, j);
+                w2 = __dadd_rn(w2, sd[j]);
+              }
+              break;
+            case (LK_ADD << 2) | 3u: CGB_J wj<IPT>(wb, cur.z, j) = sd[j]; break;
+            case (LK_SUB << 2) | 1u:
+              CGB_J {
+                double& w2 = wj<IPT>(wb, cur.z, j);
+                w2 = __dsub_rn(w2, sd[j]);
+              }
+              break;
+            case (LK_SUB << 2) | 3u: CGB_J wj<IPT>(wb, cur.z, j) = d_neg(sd[j]); break;
+            case (LK_IFZ << 2) | 1u:
+              CGB_J {
+                double& w2 = wj<IPT>(wb, cur.z, j);
+                if (!d_iszero(Q0[i][j])) w2 = __dadd_rn(w2, sd[j]);
+                else w2 = __dadd_rn(w2, 0.0);
+              }
+              break;
+            case (LK_IFZ << 2) | 3u:
+              CGB_J wj<IPT>(wb, cur.z, j) = d_iszero(Q0[i][j]) ? 0.0 : sd[j];
+              break;
             default: break;  // operand c receives nothing
           }
         }
@@ -657,44 +721,55 @@ __device__ __forceinline__ void adjoint_walk(const uint4* st, int ngr, const dou
     for (int i = 0; i < G; ++i) {
       E0[i] = E1[i];
       E1[i] = E2[i];
-      P0[i] = P1[i];
-      Q0[i] = Q1[i];
+#pragma unroll
+      for (int j = 0; j < IPT; ++j) {
+        P0[i][j] = P1[i][j];
+        Q0[i][j] = Q1[i][j];
+      }
     }
   }
 }
 
 // Flags (bits 0-4): 2/4 operand b/c receives a contribution, 8/16 it is the first one
 // (1 marks an entry with work; outputs carry 8 when their seed is the slot's first).
-template <int G, int MB>
+template <int G, int MB, int IPT>
 __global__ void __launch_bounds__(32, MB) k_adjoint(const __grid_constant__ SweepArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x & 31;
   unsigned char* wb = smem + lane * 8;
   const long long ntiles = (a.n + 31) / 32;
-  const long long nwork = ntiles * a.ndir;
-  const long long wstride = gridDim.x;
+  const long long nwork = (ntiles + IPT - 1) / IPT * a.ndir;
+  const size_t tstride = static_cast<size_t>(a.t.n_partials) * 32;
   const int2 se = __ldg(a.dchunks);
   const int ngr = se.y / G;
   const uint4* st = a.dstream + se.x;
-  for (int q = 0; q < a.t.sz_w; ++q) wreg(wb, q * 256) = 0.0;
-  for (long long work = blockIdx.x; work < nwork; work += wstride) {
-    const long long tile = work / a.ndir;
+  for (int q = 0; q < a.t.sz_w * IPT; ++q) wreg(wb, q * 256) = 0.0;
+  for (long long work = blockIdx.x; work < nwork; work += gridDim.x) {
+    const long long tg = work / a.ndir;
     const int dir = static_cast<int>(work % a.ndir);
-    const long long il = tile * 32 + lane;
-    const bool active = il < a.n;
-    const long long ig = a.i_begin + il;
-    if (active) {
-      // input nonzeros whose adjoint is structurally zero (or never read) get a zero
-      for (int k = 0; k < a.n_zero; ++k) {
-        const int2 jk = __ldg(a.zero_in + k);
-        const IoDesc& d = a.sens[jk.x];
-        if (d.ptr) static_cast<double*>(d.ptr)[io_off(d, dir, jk.y, ig)] = 0.0;
+    bool active[IPT], tok[IPT];
+    long long ig[IPT];
+#pragma unroll
+    for (int j = 0; j < IPT; ++j) {
+      const long long tile = tg * IPT + j;
+      const long long il = tile * 32 + lane;
+      tok[j] = tile < ntiles;
+      active[j] = il < a.n;
+      ig[j] = a.i_begin + il;
+      if (active[j]) {
+        // input nonzeros whose adjoint is structurally zero (or never read) get a zero
+        for (int k = 0; k < a.n_zero; ++k) {
+          const int2 jk = __ldg(a.zero_in + k);
+          const IoDesc& d = a.sens[jk.x];
+          if (d.ptr) static_cast<double*>(d.ptr)[io_off(d, dir, jk.y, ig[j])] = 0.0;
+        }
       }
     }
-    const double* pt = a.partials + static_cast<size_t>(tile) * a.t.n_partials * 32 + lane;
-    adjoint_walk<true, G>(st, ngr, pt, wb, a.seed, a.sens, active, dir, ig);
+    const double* pt = a.partials + static_cast<size_t>(tg * IPT) * tstride + lane;
+    adjoint_walk<true, G, IPT>(st, ngr, pt, tstride, tok, wb, a.seed, a.sens, active, dir, ig);
   }
 }
+#undef CGB_J
 
 // ---------------------------------------------------------------------------------------------
 // Persistent multi-tape batch: one launch drains a host-built list of work units
@@ -783,8 +858,10 @@ __global__ void __launch_bounds__(32, 16) k_batch(const __grid_constant__ BatchA
           if (d.ptr) static_cast<double*>(d.ptr)[io_off(d, dir, jk.y, il)] = 0.0;
         }
       }
-      adjoint_walk<false, kBatchGroup>(it.adj_stream, it.adj_ngr, pt, wb, io + 2 * kMaxIo, io + 3 * kMaxIo,
-                          active, dir, il);
+      const bool act1[1] = {active}, tok1[1] = {true};
+      const long long ig1[1] = {il};
+      adjoint_walk<false, kBatchGroup, 1>(it.adj_stream, it.adj_ngr, pt, 0, tok1, wb,
+                                          io + 2 * kMaxIo, io + 3 * kMaxIo, act1, dir, ig1);
     }
   }
 }
@@ -947,24 +1024,40 @@ cudaError_t launch_sp_reverse(const SweepArgs& a, int grid, cudaStream_t s) {
   CGB_DISPATCH_BS(k_sp_reverse)
 }
 
-// Derivative-sweep variants (G entries per group, MB minimum CTAs per SM), see DirVariant.
-#define CGB_DISPATCH_VARIANT(KT)                                            \
-  switch (variant) {                                                        \
-    case DV_G8: return launch_k(KT<8, 1>, dim3(grid), 32, smem, a, s);      \
-    case DV_G4: return launch_k(KT<4, 1>, dim3(grid), 32, smem, a, s);      \
-    case DV_G4_R128: return launch_k(KT<4, 16>, dim3(grid), 32, smem, a, s); \
-    case DV_G4_R80: return launch_k(KT<4, 24>, dim3(grid), 32, smem, a, s);  \
-    case DV_G8_R128: return launch_k(KT<8, 16>, dim3(grid), 32, smem, a, s); \
-    default: return cudaErrorInvalidValue;                                  \
+// Derivative-sweep variants (G entries per group, MB minimum CTAs per SM, IPT tiles per
+// warp), see DirVariant. CGB_VARIANTS(X) lists them as X(variant, G, MB, IPT).
+#define CGB_VARIANTS(X)        \
+  X(DV_G4_R128, 4, 16, 1)      \
+  X(DV_G4_R80, 4, 24, 1)       \
+  X(DV_G2_R80, 2, 24, 1)       \
+  X(DV_G2_R64, 2, 32, 1)       \
+  X(DV_G1_R64, 1, 32, 1)       \
+  X(DV_G2_I2_R128, 2, 16, 2)
+
+int variant_ipt(int variant) {
+  switch (variant) {
+#define CGB_IPT(V, G, MB, IPT) case V: return IPT;
+    CGB_VARIANTS(CGB_IPT)
+#undef CGB_IPT
+    default: return 1;
   }
+}
+
+#define CGB_DISPATCH_VARIANT(KT)                                                          \
+  switch (variant) {                                                                      \
+    CGB_VARIANTS(CGB_LAUNCH_##KT)                                                         \
+    default: return cudaErrorInvalidValue;                                                \
+  }
+#define CGB_LAUNCH_k_tangent(V, G, MB, IPT) \
+  case V: return launch_k(k_tangent<G, MB, IPT>, dim3(grid), 32, smem_lean(a.t.sz_w, IPT, 0), a, s);
+#define CGB_LAUNCH_k_adjoint(V, G, MB, IPT) \
+  case V: return launch_k(k_adjoint<G, MB, IPT>, dim3(grid), 32, smem_lean(a.t.sz_w, IPT, 0), a, s);
 
 cudaError_t launch_tangent(const SweepArgs& a, int grid, int variant, cudaStream_t s) {
-  const size_t smem = smem_lean(a.t.sz_w, 1, 0);
   CGB_DISPATCH_VARIANT(k_tangent)
 }
 
 cudaError_t launch_adjoint(const SweepArgs& a, int grid, int variant, cudaStream_t s) {
-  const size_t smem = smem_lean(a.t.sz_w, 1, 0);
   CGB_DISPATCH_VARIANT(k_adjoint)
 }
 
@@ -1049,13 +1142,11 @@ int occupancy_dense(int dir_warps, size_t smem) {
 
 int occupancy_dir(int variant, bool adjoint, size_t smem) {
   switch (variant) {
-#define CGB_OCC(V, G, MB) \
-  case V: return adjoint ? occ_of(k_adjoint<G, MB>, 32, smem) : occ_of(k_tangent<G, MB>, 32, smem);
-    CGB_OCC(DV_G8, 8, 1)
-    CGB_OCC(DV_G4, 4, 1)
-    CGB_OCC(DV_G4_R128, 4, 16)
-    CGB_OCC(DV_G4_R80, 4, 24)
-    CGB_OCC(DV_G8_R128, 8, 16)
+#define CGB_OCC(V, G, MB, IPT)                                              \
+  case V:                                                                   \
+    return adjoint ? occ_of(k_adjoint<G, MB, IPT>, 32, smem)                \
+                   : occ_of(k_tangent<G, MB, IPT>, 32, smem);
+    CGB_VARIANTS(CGB_OCC)
 #undef CGB_OCC
     default: return 0;
   }

@@ -114,10 +114,14 @@ cudaError_t launch_eval(const SweepArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_record(const SweepArgs& a, int grid, cudaStream_t s);
 // Derivative sweeps: 1-D grid whose size is a multiple of the direction-group count
 // ceil(ndir / (block/32)); CTA b works on direction group b % groups.
-// Variants of the warp-independent derivative sweeps: entries per software-pipeline group
-// (8 or 4) and a register cap that lets more one-warp CTAs reside per SM. All variants do the
-// same arithmetic in the same order; only speed differs, so the host may pick any.
-enum DirVariant : int { DV_G8 = 0, DV_G4, DV_G4_R128, DV_G4_R80, DV_G8_R128, DV_COUNT };
+// Variants of the warp-independent derivative sweeps: entries per software-pipeline group,
+// a register cap that lets more one-warp CTAs reside per SM, and 32-instance tiles per warp
+// (IPT). All variants do the same arithmetic in the same order; only speed differs, so the
+// host may pick any. The work vector of a variant takes smem_lean(sz_w, IPT, 0) bytes.
+enum DirVariant : int {
+  DV_G4_R128 = 0, DV_G4_R80, DV_G2_R80, DV_G2_R64, DV_G1_R64, DV_G2_I2_R128, DV_COUNT
+};
+int variant_ipt(int variant);
 cudaError_t launch_tangent(const SweepArgs& a, int grid, int variant, cudaStream_t s);
 cudaError_t launch_adjoint(const SweepArgs& a, int grid, int variant, cudaStream_t s);
 // The adjoint sweep without an activity plan (see k_adjoint<DW, true>).

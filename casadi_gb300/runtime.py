@@ -398,7 +398,7 @@ class Batch:
                                             _stream_handle(stream)))
 
 
-N_VARIANTS = 5
+N_VARIANTS = 6
 
 FAMILIES = ("eval", "record", "tangent", "adjoint", "sp_forward", "sp_reverse", "batch")
 

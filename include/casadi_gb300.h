@@ -190,7 +190,7 @@ CASADI_GB300_API int casadi_gb300_map_reverse(int id, int mem, int64_t n, int na
  * the reference, whose Map has one code path per parallelization (casadi/core/map.cpp:39-51). */
 CASADI_GB300_API int casadi_gb300_autotune(int enable);
 CASADI_GB300_API int casadi_gb300_tuned_variant(int id, int kind, int* variant);
-/* Fixes the variant of one kind on a tape (0..4), or clears it for retuning (-1). */
+/* Fixes the variant of one kind on a tape (0..5), or clears it for retuning (-1). */
 CASADI_GB300_API int casadi_gb300_set_variant(int id, int kind, int variant);
 
 /* Persistent multi-tape batches. A batch is a list of items, each one tape over its own
