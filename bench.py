@@ -279,28 +279,29 @@ def cpu_baseline(F, args, aseeds, workload, budget_s=12.0):
 
 # ---- native arm ----------------------------------------------------------------------------------
 def mixed_component(torch, R, stream, reps=3):
-    """Eight random DAG tapes (200..20000 nodes) over log-normal instance counts, about 1M
-    instances in all, each evaluated with one adjoint direction: one launch per tape (record +
-    adjoint, one tape after the other on one stream) against the persistent batch (one launch
-    for all tapes, replayed from a CUDA graph)."""
+    """Mixed-size batch: eight random-DAG tapes (200..20000 nodes, 64 inputs, 16 outputs)
+    and work items with log-normal instance counts (median 4096, sigma 1.5) up to 2^20
+    instances, each evaluated with the adjoint of the sum of its outputs: one launch pair per
+    item (record + adjoint, one item after the other on one stream) against the persistent
+    batch (all items in one launch, replayed from a CUDA graph)."""
     from casadi_gb300 import workloads as W
-    items = W.mixed_batch(n_tapes=8, total=1 << 20, seed=0)
-    rng = np.random.default_rng(0)
+    funs, items = W.mixed_batch(n_tapes=8, total=1 << 20, seed=0)
+    tapes = [R.CudaTape(f) for f in funs]
     b = R.Batch()
     plain = []
     total = 0
-    for f, n, sd in items:
-        t = R.CudaTape(f)
-        args = [torch.from_numpy(x).cuda() for x in W.dag_inputs(n, n_in=16, seed=sd)]
-        seeds = [torch.from_numpy(rng.standard_normal((1, k, n))).cuda() for k in f.tape.nnz_out]
+    for k, n, sd in items:
+        t = tapes[k]
+        args = [torch.from_numpy(x).cuda() for x in W.dag_inputs(n, n_in=64, seed=sd)]
+        seeds = [torch.ones((1, 16, n), dtype=torch.float64, device="cuda")]
         res, asens = b.add(t, args, seeds)
         plain.append((t, args, seeds, [torch.empty_like(r) for r in res],
                       [torch.empty_like(x) for x in asens]))
         total += n
     limit = max(b.scratch_bytes(), 1 << 30)
     shared = torch.empty(limit, dtype=torch.uint8, device="cuda")
-    for p in plain:
-        p[0]._scratch = shared
+    for t in tapes:
+        t._scratch = shared
 
     def run_plain():
         for t, args, seeds, res, asens in plain:
@@ -322,12 +323,16 @@ def mixed_component(torch, R, stream, reps=3):
 
     ms_plain = timeit(run_plain)
     ms_batch = timeit(run_batch)
-    same = all(bool(torch.equal(x.view(torch.int64), y.view(torch.int64))) for (_, _, _, r0, s0), (_, _, r1, _, s1) in
-               zip(plain, b._keep) for x, y in zip(r0 + s0, r1 + s1))
-    for p in plain:
-        p[0].sync()
-        p[0]._scratch = None
-    return {"instances": total, "tapes": [[f.tape.n_instr, n] for f, n, _ in items],
+    same = all(bool(torch.equal(x.view(torch.int64), y.view(torch.int64))) for
+               (_, _, _, r0, s0), (_, _, r1, _, s1) in zip(plain, b._keep)
+               for x, y in zip(r0 + s0, r1 + s1))
+    for t in tapes:
+        t.sync()
+        t._scratch = None
+    counts = [n for _, n, _ in items]
+    return {"instances": total, "items": len(items),
+            "tape_instructions": [f.tape.n_instr for f in funs],
+            "item_instances_median": int(np.median(counts)), "item_instances_max": max(counts),
             "plain_ms": ms_plain, "persistent_ms": ms_batch,
             "plain_evals_per_s": total / (ms_plain * 1e-3),
             "persistent_evals_per_s": total / (ms_batch * 1e-3),

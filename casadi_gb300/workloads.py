@@ -124,22 +124,24 @@ def dag_inputs(n, n_in=64, seed=0):
     return [rng.standard_normal((n_in, n))]
 
 
-def mixed_batch(n_tapes=8, total=1 << 20, seed=0, n_in=16, n_out=4, window=64):
-    """A mixed multi-tape workload: ``n_tapes`` random DAGs whose node counts are spread
-    log-uniformly over 200..20000 and whose instance counts are drawn log-normal (median
-    4096, sigma 1.5) and rescaled to about ``total`` instances in all. Returns a list of
-    ``(Function, n_instances, seed)``."""
+def mixed_batch(n_tapes=8, total=1 << 20, seed=0, median=4096, sigma=1.5, bounded=False):
+    """The mixed-size multi-tape workload: ``n_tapes`` random DAGs from the generator above
+    (64 inputs, 16 outputs, operands from the previous 256 nodes) whose node counts are
+    spread log-uniformly over 200..20000, and work items (tape, instance count) with counts
+    drawn log-normal (median ``median``, log-sigma ``sigma``) on tapes drawn uniformly, until
+    ``total`` instances. Returns ``(functions, items)`` with items ``[(tape index, n, seed)]``.
+    With ``bounded`` the DAGs use the bounded op variants (finite values at any depth)."""
     rng = np.random.default_rng(seed)
     nodes = np.exp(np.linspace(np.log(200), np.log(20000), n_tapes)).astype(int)
-    counts = rng.lognormal(mean=np.log(4096), sigma=1.5, size=n_tapes)
-    counts = np.maximum(32, np.round(counts * total / counts.sum())).astype(int)
-    perm = rng.permutation(n_tapes)
-    out = []
-    for k in range(n_tapes):
-        f = random_dag(n_in=n_in, n_nodes=int(nodes[k]), n_out=n_out, seed=seed * 100 + k,
-                       window=window, bounded=True)
-        out.append((f, int(counts[perm[k]]), seed * 100 + k))
-    return out
+    funs = [random_dag(n_in=64, n_nodes=int(nodes[k]), n_out=16, seed=seed * 100 + k,
+                       window=256, bounded=bounded) for k in range(n_tapes)]
+    items = []
+    left = total
+    while left > 0:
+        n = int(min(left, max(1, round(rng.lognormal(np.log(median), sigma)))))
+        items.append((int(rng.integers(n_tapes)), n, seed * 100000 + len(items)))
+        left -= n
+    return funs, items
 
 
 # ---- quadcopter multiple shooting -----------------------------------------------------------
