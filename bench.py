@@ -367,8 +367,8 @@ def run_native(a):
 
     def step():
         if a.workload == "rollout20":
-            ct.jacobian(dargs, res=res, jac=jac, stream=stream)
-            ct.reverse(dargs, daseeds, res=res, asens=asens, stream=stream)
+            # one record sweep feeds the Jacobian (24 unit directions) and the cost adjoint
+            ct.jacobian_reverse(dargs, daseeds, res=res, jac=jac, asens=asens, stream=stream)
         elif a.workload == "dag":
             ct.reverse(dargs, daseeds, res=res, asens=asens, stream=stream)
         else:
@@ -466,8 +466,7 @@ def run_native(a):
 
         def e2e_step():
             if a.workload == "rollout20":
-                cm.jacobian(*hargs, res=hres, jac=hjac)
-                cm.reverse(hargs, hseed, res=hres, asens=hasens)
+                cm.jacobian_reverse(hargs, hseed, res=hres, jac=hjac, asens=hasens)
             elif a.workload == "dag":
                 cm.reverse(hargs, hseed, res=hres, asens=hasens)
             else:
@@ -482,8 +481,8 @@ def run_native(a):
         in_b = 8 * n * sum(F.tape.nnz_in)
         out_b = 8 * n * sum(F.tape.nnz_out)
         if a.workload == "rollout20":
-            h2d = 2 * in_b + 8 * n * sum(F.tape.nnz_out)
-            d2h = 2 * out_b + 8 * n * nz * sum(F.tape.nnz_out) + in_b
+            h2d = in_b + 8 * n * sum(F.tape.nnz_out)
+            d2h = out_b + 8 * n * nz * sum(F.tape.nnz_out) + in_b
         elif a.workload == "dag":
             h2d = in_b + 8 * n * sum(F.tape.nnz_out)
             d2h = out_b + in_b

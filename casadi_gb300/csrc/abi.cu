@@ -267,7 +267,6 @@ struct DirShape {
 // CUDA events and keeps the fastest for the tape. It synchronizes the stream once; it is
 // skipped while the stream is being captured into a graph, and can be switched off.
 bool g_autotune = true;
-constexpr int kDefaultVariant = DV_G4_R128;  // fastest on the rollout tapes measured
 
 
 bool fits_smem(int sz_w) {
@@ -433,23 +432,37 @@ const TanPlan* tan_plan(Tape& t, int ndir, int dw, int ch, bool identity,
             static_cast<unsigned short>(b << (2 * (dd % dw)));
     }
   }
+  // one stream per group of dw directions (the union of their work); an entry whose flags
+  // differ between the group's directions becomes LK_MIXED with the real kind in x bits
+  // 19-22 and the flags of direction k in bits 24+2k (see the tangent kernel)
   const std::vector<int> pk = partial_starts(t);
   std::vector<uint4> all;
-  std::vector<int2> se(ndir);
-  for (int d = 0; d < ndir; ++d) {
-    if (!identity && d > 0) {
-      se[d] = se[0];  // general seeds: one stream serves every direction
+  std::vector<int2> se(p->groups);
+  for (int g = 0; g < p->groups; ++g) {
+    if (!identity && g > 0) {
+      se[g] = se[0];  // general seeds: one stream serves every group
       continue;
     }
+    const int kv = std::min(dw, ndir - g * dw);  // directions in this group
     std::vector<uint4> ents;
-    const size_t g = static_cast<size_t>(d / dw), sh = 2 * (d % dw);
     for (size_t k = 0; k < nc; ++k) {
-      const unsigned op = dec_op(t.h_code[k]);
-      const unsigned b = (bits[g * nc + k] >> sh) & 3u;
-      if (!b && op != D_OUTPUT) continue;
-      ents.push_back(dir_entry(t.h_code[k], b, pk[k]));
+      const u64 w = t.h_code[k];
+      const unsigned op = dec_op(w);
+      const unsigned gb = bits[static_cast<size_t>(g) * nc + k];
+      if (!gb && op != D_OUTPUT) continue;
+      const unsigned f0 = gb & 3u;
+      bool uniform = true;
+      for (int d = 1; d < kv; ++d) uniform = uniform && ((gb >> (2 * d)) & 3u) == f0;
+      if (uniform) {
+        ents.push_back(dir_entry(w, f0, pk[k]));
+      } else {
+        uint4 e = dir_entry(w, 0, pk[k]);
+        e.x |= (lean_kind(op) << 19) | ((gb & 0xffu) << 24);
+        e.w = (e.w & ~(15u << 5)) | (static_cast<unsigned>(LK_MIXED) << 5);
+        ents.push_back(e);
+      }
     }
-    se[d] = push_stream(all, ents);
+    se[g] = push_stream(all, ents);
   }
   cudaError_t e;
   if ((e = upload(&p->d_stream, all)) != cudaSuccess ||
@@ -549,51 +562,140 @@ int time_once(cudaStream_t s, F fn, float* ms) {
 
 // Values + partials (record sweep) followed by the derivative sweep, in waves of as many
 // instances as the scratch holds. `in/out/seed/sens` address the whole instance range.
-int run_ad(Tape& t, long long n, const IoDesc* in, const IoDesc* out, const IoDesc* seed,
-           const IoDesc* sens, int ndir, bool adjoint, bool identity, void* scratch,
-           size_t scratch_bytes, cudaStream_t s) {
+// One derivative sweep after the record sweep: ndir directions, forward (seeded or identity)
+// or adjoint, with its seed and sensitivity descriptors over the whole instance range.
+struct DerivReq {
+  int ndir = 0;
+  bool adjoint = false;
+  bool identity = false;
+  const IoDesc* seed = nullptr;
+  const IoDesc* sens = nullptr;
+};
+
+// Runs one derivative sweep of wave `a` (values and partials already recorded).
+int run_deriv(Tape& t, SweepArgs a, long long m, const DerivReq& rq, cudaStream_t s) {
+  const int ndir = rq.ndir;
+  const bool adjoint = rq.adjoint, identity = rq.identity;
+  const int kind = adjoint ? 2 : (identity ? 1 : 0);
+  const int sms = sm_count();
+  int err = 0;
+  const AdjPlan* ap = nullptr;
+  std::vector<char> seeded_in(t.n_in);
+  for (int j = 0; j < t.n_in; ++j) seeded_in[j] = rq.seed && rq.seed[j].ptr != nullptr;
+  if (adjoint) {
+    std::vector<char> seeded(t.n_out);
+    for (int j = 0; j < t.n_out; ++j) seeded[j] = rq.seed[j].ptr != nullptr;
+    ap = adj_plan(t, 1, 0, seeded, &err);
+    if (!ap) return err ? err : fail(CASADI_GB300_ERR_CUDA, "activity plan");
+  }
+  a.ndir = ndir;
+  a.identity_seed = identity ? 1 : 0;
+  std::memcpy(a.seed, rq.seed, sizeof(IoDesc) * (adjoint ? t.n_out : t.n_in));
+  std::memcpy(a.sens, rq.sens, sizeof(IoDesc) * (adjoint ? t.n_in : t.n_out));
+  a.block = 32;
+  a.chunk = 0;
+  if (ap) {
+    a.dstream = ap->d_stream;
+    a.dchunks = ap->d_chunks;
+    a.zero_in = ap->d_zero;
+    a.n_zero = ap->n_zero;
+  }
+  const long long tiles = (m + 31) / 32;
+  auto shape = [&](int v, int* ipt, int* kd) {
+    if (adjoint) {
+      *ipt = adj_variant_ipt(v);
+      *kd = 1;
+    } else {
+      tan_variant_shape(v, ipt, kd);
+    }
+  };
+  // a variant whose work vector (IPT tiles x K directions per warp) does not fit, or whose
+  // union-stream encoding does not (K > 1 needs slot offsets below 2^19), is never launched
+  auto fits = [&](int v) {
+    int ipt, kd;
+    shape(v, &ipt, &kd);
+    if (kd > 1 && static_cast<long long>(t.sz_w) * 256 >= (1ll << 19)) return false;
+    return smem_lean(t.sz_w, ipt * kd, 0) <= static_cast<size_t>(max_smem_optin());
+  };
+  auto grid_of = [&](int v) {
+    int ipt, kd;
+    shape(v, &ipt, &kd);
+    const long long vwork = (tiles + ipt - 1) / ipt * ((ndir + kd - 1) / kd);
+    const int occ = std::max(1, occupancy_dir(v, adjoint, smem_lean(t.sz_w, ipt * kd, 0)));
+    return static_cast<int>(std::max<long long>(
+        1, std::min<long long>(vwork, static_cast<long long>(sms) * occ)));
+  };
+  int plan_err = 0;
+  auto launch = [&](int v) {
+    if (adjoint) return launch_adjoint(a, grid_of(v), v, s);
+    int ipt = 1, kd = 1;
+    tan_variant_shape(v, &ipt, &kd);
+    const TanPlan* tp = tan_plan(t, ndir, kd, 0, identity, seeded_in, &plan_err);
+    if (!tp) return cudaErrorInvalidValue;
+    a.dstream = tp->d_stream;
+    a.dchunks = tp->d_chunks;
+    return launch_tangent(a, grid_of(v), v, s);
+  };
+  const long long work = tiles * ndir;
+  const int n_variants = adjoint ? AV_COUNT : TV_COUNT;
+  int variant = t.tuned[kind];
+  if (variant >= 0 && !fits(variant)) variant = -1;
+  if (variant < 0) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(s, &cs);
+    // tune on waves that fill the GPU at least twice at 8 warps per SM, outside capture
+    if (g_autotune && cs == cudaStreamCaptureStatusNone && work >= 2ll * sms * 8) {
+      float best = 0;
+      for (int v = 0; v < n_variants; ++v) {
+        if (!fits(v)) continue;
+        float ms = 0;
+        if (int rc = time_once(s, [&] { return launch(v); }, &ms)) return plan_err ? plan_err : rc;
+        if (variant < 0 || ms < best) {
+          best = ms;
+          variant = v;
+        }
+      }
+      t.tuned[kind] = variant;
+      return 0;  // every variant's run produced this wave's (identical) results
+    }
+    variant = 0;  // the first variant of each list: fastest on the tapes measured
+    while (variant < n_variants && !fits(variant)) ++variant;
+    if (variant == n_variants)
+      return fail(CASADI_GB300_ERR_UNSUPPORTED, "no derivative-sweep variant fits");
+  }
+  cudaError_t e = timed(adjoint ? F_ADJOINT : F_TANGENT, s, [&] { return launch(variant); });
+  if (plan_err) return plan_err;
+  if (e != cudaSuccess) return cuda_fail(e, "derivative sweep launch");
+  return 0;
+}
+
+// Values + partials (record sweep) followed by the derivative sweeps `reqs`, which all read
+// the same recorded partials, in waves of as many instances as the scratch holds.
+// `in/out` and the requests' descriptors address the whole instance range.
+int run_ad_multi(Tape& t, long long n, const IoDesc* in, const IoDesc* out,
+                 const DerivReq* reqs, int nreq, void* scratch, size_t scratch_bytes,
+                 cudaStream_t s) {
   if (n == 0) return 0;
   const long long cap = wave_capacity(t, n, scratch_bytes);
   if (t.n_partials > 0 && (scratch == nullptr || cap < 32))
     return fail(CASADI_GB300_ERR_SCRATCH,
                 "scratch of %zu bytes is below the minimum of %lld bytes for this tape",
                 scratch_bytes, 32ll * 8ll * t.n_partials);
+  bool any = false;
+  for (int r = 0; r < nreq; ++r) any = any || reqs[r].ndir > 0;
   // derivative sweeps: one-warp CTAs, as many per SM as the work vector allows
-  DirShape ds;
-  ds.dw = 1;
-  ds.ch = 0;
-  const size_t dsmem = smem_lean(t.sz_w, 1, 0);
-  if (ndir > 0 && dsmem > static_cast<size_t>(max_smem_optin()))
+  if (any && smem_lean(t.sz_w, 1, 0) > static_cast<size_t>(max_smem_optin()))
     return fail(CASADI_GB300_ERR_UNSUPPORTED,
                 "work vector of %d slots does not fit the derivative sweeps' shared memory", t.sz_w);
-  if (ndir > 0 && static_cast<unsigned>(t.n_partials) >= kMaxPartials)
+  if (any && static_cast<unsigned>(t.n_partials) >= kMaxPartials)
     return fail(CASADI_GB300_ERR_UNSUPPORTED, "tape records %d partials per instance (max %u)",
                 t.n_partials, kMaxPartials - 1);
-  const int kind = adjoint ? 2 : (identity ? 1 : 0);
-  const int sms = sm_count();
-  const TanPlan* tp = nullptr;
-  const AdjPlan* ap = nullptr;
-  if (ndir > 0) {
-    int err = 0;
-    if (adjoint) {
-      std::vector<char> seeded(t.n_out);
-      for (int j = 0; j < t.n_out; ++j) seeded[j] = seed[j].ptr != nullptr;
-      ap = adj_plan(t, ds.dw, ds.ch, seeded, &err);
-    } else {
-      std::vector<char> seeded(t.n_in);
-      for (int j = 0; j < t.n_in; ++j) seeded[j] = seed[j].ptr != nullptr;
-      tp = tan_plan(t, ndir, ds.dw, ds.ch, identity, seeded, &err);
-    }
-    if (!tp && !ap) return err ? err : fail(CASADI_GB300_ERR_CUDA, "activity plan");
-  }
   for (long long i0 = 0; i0 < n; i0 += cap) {
     const long long m = std::min(cap, n - i0);
     SweepArgs a = base_args(t, m, i0);
     a.partials = static_cast<double*>(scratch);
     a.pofs = t.d_pofs;
     a.n_code = t.n_chunks * kChunk;
-    a.ndir = ndir;
-    a.identity_seed = identity ? 1 : 0;
     for (int j = 0, off = 0; j < t.n_in; off += t.nnz_in[j], ++j) a.in_off[j] = off;
     std::memcpy(a.in, in, sizeof(IoDesc) * t.n_in);
     std::memcpy(a.out, out, sizeof(IoDesc) * t.n_out);
@@ -602,62 +704,23 @@ int run_ad(Tape& t, long long n, const IoDesc* in, const IoDesc* out, const IoDe
       return launch_record(a, grid_for((m + a.block - 1) / a.block, t.primal_grid_cap), s);
     });
     if (e != cudaSuccess) return cuda_fail(e, "record sweep launch");
-    if (ndir > 0) {
-      std::memcpy(a.seed, seed, sizeof(IoDesc) * (adjoint ? t.n_out : t.n_in));
-      std::memcpy(a.sens, sens, sizeof(IoDesc) * (adjoint ? t.n_in : t.n_out));
-      a.block = 32 * ds.dw;
-      a.chunk = ds.ch;
-      if (tp) {
-        a.dstream = tp->d_stream;
-        a.dchunks = tp->d_chunks;
-      } else {
-        a.dstream = ap->d_stream;
-        a.dchunks = ap->d_chunks;
-        a.zero_in = ap->d_zero;
-        a.n_zero = ap->n_zero;
-      }
-      const long long work = (m + 31) / 32 * ndir;
-      // a variant whose work vector (IPT tiles per warp) does not fit is never launched
-      auto fits = [&](int v) {
-        return smem_lean(t.sz_w, variant_ipt(v), 0) <= static_cast<size_t>(max_smem_optin());
-      };
-      auto grid_of = [&](int v) {
-        const int ipt = variant_ipt(v);
-        const long long vwork = ((m + 31) / 32 + ipt - 1) / ipt * ndir;
-        const int occ = std::max(1, occupancy_dir(v, adjoint, smem_lean(t.sz_w, ipt, 0)));
-        return static_cast<int>(std::max<long long>(
-            1, std::min<long long>(vwork, static_cast<long long>(sms) * occ)));
-      };
-      auto launch = [&](int v) {
-        return adjoint ? launch_adjoint(a, grid_of(v), v, s) : launch_tangent(a, grid_of(v), v, s);
-      };
-      int variant = t.tuned[kind];
-      if (variant >= 0 && !fits(variant)) variant = -1;
-      if (variant < 0) {
-        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-        cudaStreamIsCapturing(s, &cs);
-        // tune on waves that fill the GPU at least twice at 8 warps per SM, outside capture
-        if (g_autotune && cs == cudaStreamCaptureStatusNone && work >= 2ll * sms * 8) {
-          float best = 0;
-          for (int v = 0; v < DV_COUNT; ++v) {
-            if (!fits(v)) continue;
-            float ms = 0;
-            if (int rc = time_once(s, [&] { return launch(v); }, &ms)) return rc;
-            if (variant < 0 || ms < best) {
-              best = ms;
-              variant = v;
-            }
-          }
-          t.tuned[kind] = variant;
-          continue;  // every variant's run produced this wave's (identical) results
-        }
-        variant = kDefaultVariant;
-      }
-      e = timed(adjoint ? F_ADJOINT : F_TANGENT, s, [&] { return launch(variant); });
-      if (e != cudaSuccess) return cuda_fail(e, "derivative sweep launch");
-    }
+    for (int r = 0; r < nreq; ++r)
+      if (reqs[r].ndir > 0)
+        if (int rc = run_deriv(t, a, m, reqs[r], s)) return rc;
   }
   return 0;
+}
+
+int run_ad(Tape& t, long long n, const IoDesc* in, const IoDesc* out, const IoDesc* seed,
+           const IoDesc* sens, int ndir, bool adjoint, bool identity, void* scratch,
+           size_t scratch_bytes, cudaStream_t s) {
+  DerivReq rq;
+  rq.ndir = ndir;
+  rq.adjoint = adjoint;
+  rq.identity = identity;
+  rq.seed = seed;
+  rq.sens = sens;
+  return run_ad_multi(t, n, in, out, &rq, 1, scratch, scratch_bytes, s);
 }
 
 // Pointer arrays of any element type, seen as untyped pointers (the kernels know the type).
@@ -984,6 +1047,38 @@ int casadi_gb300_jacobian(int id, int64_t n, int64_t ld, const double* const* ar
                 static_cast<cudaStream_t>(stream));
 }
 
+int casadi_gb300_jacobian_reverse(int id, int64_t n, int64_t ld, const double* const* arg,
+                                  double* const* res, double* const* jac, int nadj,
+                                  const double* const* aseed, double* const* asens,
+                                  void* scratch, size_t scratch_bytes, void* stream) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  if (int rc = check_device(*t)) return rc;
+  if (int rc = check_n(n, ld)) return rc;
+  if (nadj < 0) return fail(CASADI_GB300_ERR_ARG, "negative direction count");
+  int nz = 0;
+  for (int v : t->nnz_in) nz += v;
+  if (nz == 0) return fail(CASADI_GB300_ERR_ARG, "tape has no input nonzeros");
+  IoDesc in[kMaxIo], out[kMaxIo], fseed[kMaxIo], fsens[kMaxIo], aseedd[kMaxIo], asensd[kMaxIo];
+  fill_io(in, t->n_in, vptrs(arg), t->nnz_in, ld, false);
+  fill_io(out, t->n_out, vptrs(res), t->nnz_out, ld, false);
+  fill_io(fseed, t->n_in, nullptr, t->nnz_in, ld, true);
+  fill_io(fsens, t->n_out, vptrs(jac), t->nnz_out, ld, true);
+  fill_io(aseedd, t->n_out, vptrs(aseed), t->nnz_out, ld, true);
+  fill_io(asensd, t->n_in, vptrs(asens), t->nnz_in, ld, true);
+  DerivReq rq[2];
+  rq[0].ndir = nz;
+  rq[0].identity = true;
+  rq[0].seed = fseed;
+  rq[0].sens = fsens;
+  rq[1].ndir = nadj;
+  rq[1].adjoint = true;
+  rq[1].seed = aseedd;
+  rq[1].sens = asensd;
+  return run_ad_multi(*t, n, in, out, rq, 2, scratch, scratch_bytes,
+                      static_cast<cudaStream_t>(stream));
+}
+
 int casadi_gb300_profile(int enable) {
   std::lock_guard<std::mutex> lk(g_prof_mtx);
   g_prof = enable != 0;
@@ -1007,7 +1102,7 @@ int casadi_gb300_tuned_variant(int id, int kind, int* variant) {
 int casadi_gb300_set_variant(int id, int kind, int variant) {
   Tape* t = get_tape(id);
   if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
-  if (kind < 0 || kind > 2 || variant < -1 || variant >= DV_COUNT)
+  if (kind < 0 || kind > 2 || variant < -1 || variant >= (kind == 2 ? AV_COUNT : TV_COUNT))
     return fail(CASADI_GB300_ERR_ARG, "bad arguments");
   t->tuned[kind] = variant;
   return 0;
@@ -1251,6 +1346,53 @@ int casadi_gb300_map_reverse(int id, int mem, int64_t n, int nadj, const double*
   if (int rc = run_ad(*t, n, in, out, seed, sens, nadj, true, false, scratch, bytes, s)) return rc;
   if (int rc = fetch_blocks(out, t->n_out, t->nnz_out, 1, n, res, s)) return rc;
   if (int rc = fetch_blocks(sens, t->n_in, t->nnz_in, nadj, n, asens, s)) return rc;
+  return casadi_gb300_sync(id, s);
+}
+
+int casadi_gb300_map_jacobian_reverse(int id, int mem, int64_t n, const double* const* arg,
+                                      double* const* res, double* const* jac, int nadj,
+                                      const double* const* aseed, double* const* asens) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  Mem* m = get_mem(mem);
+  if (!m) return fail(CASADI_GB300_ERR_ID, "no memory object %d", mem);
+  if (int rc = check_device(*t)) return rc;
+  if (n < 0 || nadj < 0 || nadj > 65535) return fail(CASADI_GB300_ERR_ARG, "bad arguments");
+  if (n == 0) return 0;
+  int nz = 0;
+  for (int v : t->nnz_in) nz += v;
+  if (nz == 0) return fail(CASADI_GB300_ERR_ARG, "tape has no input nonzeros");
+  cudaStream_t s = m->stream;
+  IoDesc in[kMaxIo], out[kMaxIo], fsens[kMaxIo], aseedd[kMaxIo], asensd[kMaxIo], fseed[kMaxIo];
+  std::memset(fseed, 0, sizeof(fseed));
+  if (int rc = stage_blocks(*m, 0, t->n_in, t->nnz_in, 1, n, arg, true, in, s)) return rc;
+  if (int rc = stage_blocks(*m, kMaxIo, t->n_out, t->nnz_out, 1, n,
+                            reinterpret_cast<const double* const*>(res), false, out, s))
+    return rc;
+  if (int rc = stage_blocks(*m, 2 * kMaxIo, t->n_out, t->nnz_out, nadj, n, aseed, true, aseedd, s))
+    return rc;
+  if (int rc = stage_blocks(*m, 3 * kMaxIo, t->n_out, t->nnz_out, nz, n,
+                            reinterpret_cast<const double* const*>(jac), false, fsens, s))
+    return rc;
+  if (int rc = stage_blocks(*m, 5 * kMaxIo, t->n_in, t->nnz_in, nadj, n,
+                            reinterpret_cast<const double* const*>(asens), false, asensd, s))
+    return rc;
+  void* scratch = nullptr;
+  size_t bytes = 0;
+  if (int rc = map_scratch(*t, *m, n, &scratch, &bytes)) return rc;
+  DerivReq rq[2];
+  rq[0].ndir = nz;
+  rq[0].identity = true;
+  rq[0].seed = fseed;
+  rq[0].sens = fsens;
+  rq[1].ndir = nadj;
+  rq[1].adjoint = true;
+  rq[1].seed = aseedd;
+  rq[1].sens = asensd;
+  if (int rc = run_ad_multi(*t, n, in, out, rq, 2, scratch, bytes, s)) return rc;
+  if (int rc = fetch_blocks(out, t->n_out, t->nnz_out, 1, n, res, s)) return rc;
+  if (int rc = fetch_blocks(fsens, t->n_out, t->nnz_out, nz, n, jac, s)) return rc;
+  if (int rc = fetch_blocks(asensd, t->n_in, t->nnz_in, nadj, n, asens, s)) return rc;
   return casadi_gb300_sync(id, s);
 }
 

@@ -458,35 +458,52 @@ __device__ __forceinline__ double& wj(unsigned char* wb, unsigned off, int j) {
 }
 
 // Partials of one group of entries for IPT tiles (tile j's block at pt + j*tstride; tiles
-// past the wave's end are not read).
-template <bool kNC, int G, int IPT>
+// past the wave's end are not read). Only the partials an entry uses are loaded: a tangent
+// entry uses d0 when operand b carries a derivative (flag 1) and d1 when c does (flag 2); an
+// adjoint entry uses d0 when b receives a contribution (flag 2) and d1 when c does (flag 4);
+// a mixed tangent entry (flags per direction) loads both.
+template <bool kNC, bool kAdj, int G, int IPT>
 __device__ __forceinline__ void load_partials_n(const uint4 (&E)[G], const double* pt,
                                                 size_t tstride, const bool (&tok)[IPT],
                                                 double (&P0)[G][IPT], double (&P1)[G][IPT]) {
 #pragma unroll
   for (int i = 0; i < G; ++i) {
-    const unsigned m = ent_pmask(E[i].w);
-    const size_t pk = ent_pk(E[i].w);
+    const unsigned meta = E[i].w;
+    const unsigned f = ent_flags(meta);
+    const unsigned use = kAdj ? (f >> 1) & 3u : (ent_kind(meta) == LK_MIXED ? 3u : f & 3u);
+    const unsigned m = ent_pmask(meta);
+    const size_t pk = ent_pk(meta);
     const size_t k1 = pk + ((m & 1u) ? 1 : 0);
 #pragma unroll
     for (int j = 0; j < IPT; ++j) {
-      P0[i][j] = ((m & 1u) && tok[j]) ? ld_partial<kNC>(pt + j * tstride + pk * 32) : 1.0;
-      P1[i][j] = ((m & 2u) && tok[j]) ? ld_partial<kNC>(pt + j * tstride + k1 * 32) : 0.0;
+      P0[i][j] = ((m & use & 1u) && tok[j]) ? ld_partial<kNC>(pt + j * tstride + pk * 32) : 1.0;
+      P1[i][j] = ((m & use & 2u) && tok[j]) ? ld_partial<kNC>(pt + j * tstride + k1 * 32) : 0.0;
     }
   }
 }
 
-template <int G, int MB, int IPT>
+// Tangent sweep. A warp takes one work item (IPT tiles, K directions): the work vector holds
+// IPT*K values per slot and lane, w[slot][j*K + k][lane]. With K > 1 the warp walks the
+// union stream of its K directions: recorded partials and entries are loaded once for all K,
+// and the K directions give independent FP64 chains. An entry whose flags are the same for
+// every direction of the group is dispatched once ("uniform"); otherwise its kind is
+// LK_MIXED and x carries the real kind (bits 19-22) and the flags of direction k (bits
+// 24+2k, 25+2k), handled one direction at a time.
+constexpr unsigned kTanXMask = (1u << 19) - 1;
+
+template <int G, int MB, int IPT, int K>
 __global__ void __launch_bounds__(32, MB) k_tangent(const __grid_constant__ SweepArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x & 31;
   unsigned char* wb = smem + lane * 8;
   const long long ntiles = (a.n + 31) / 32;
-  const long long nwork = (ntiles + IPT - 1) / IPT * a.ndir;
+  const int ngroups = (a.ndir + K - 1) / K;
+  const long long nwork = (ntiles + IPT - 1) / IPT * ngroups;
   const size_t tstride = static_cast<size_t>(a.t.n_partials) * 32;
   for (long long work = blockIdx.x; work < nwork; work += gridDim.x) {
-    const long long tg = work / a.ndir;
-    const int dir = static_cast<int>(work % a.ndir);
+    const long long tg = work / ngroups;
+    const int grp = static_cast<int>(work % ngroups);
+    const int dir0 = grp * K;
     bool active[IPT], tok[IPT];
     long long ig[IPT];
 #pragma unroll
@@ -497,7 +514,7 @@ __global__ void __launch_bounds__(32, MB) k_tangent(const __grid_constant__ Swee
       active[j] = il < a.n;
       ig[j] = a.i_begin + il;
     }
-    const int2 se = __ldg(a.dchunks + dir);  // (first entry, entry count) of this direction
+    const int2 se = __ldg(a.dchunks + grp);  // (first entry, entry count) of this group
     const uint4* st = a.dstream + se.x;
     const int ngr = se.y / G;
     const double* pt = a.partials + static_cast<size_t>(tg * IPT) * tstride + lane;
@@ -505,74 +522,134 @@ __global__ void __launch_bounds__(32, MB) k_tangent(const __grid_constant__ Swee
     double P0[G][IPT], Q0[G][IPT];
     load_group<G>(st, 0, ngr, E0);
     load_group<G>(st, 1, ngr, E1);
-    load_partials_n<true, G, IPT>(E0, pt, tstride, tok, P0, Q0);
+    load_partials_n<true, false, G, IPT>(E0, pt, tstride, tok, P0, Q0);
 #pragma unroll 1
     for (int g = 0; g < ngr; ++g) {
       uint4 E2[G];
       double P1[G][IPT], Q1[G][IPT];
       load_group<G>(st, g + 2, ngr, E2);
-      load_partials_n<true, G, IPT>(E1, pt, tstride, tok, P1, Q1);
+      load_partials_n<true, false, G, IPT>(E1, pt, tstride, tok, P1, Q1);
 #pragma unroll
       for (int i = 0; i < G; ++i) {
         const uint4 cur = E0[i];
         const unsigned meta = cur.w;
+        const unsigned xo = K > 1 ? (cur.x & kTanXMask) : cur.x;
+#define CGB_W(off, j, k) wj<IPT * K>(wb, (off), (j) * K + (k))
+#define CGB_JK _Pragma("unroll") for (int j = 0; j < IPT; ++j) _Pragma("unroll") for (int k = 0; k < K; ++k)
+// tangent of one arithmetic entry (kind and flags in `key`) for tile j, direction k
+#define CGB_TAN_CASES(R, j, k)                                                               \
+  case (LK_GEN << 2) | 1u: R = __dmul_rn(P0[i][j], CGB_W(cur.y, j, k)); break;               \
+  case (LK_GEN << 2) | 2u: R = __dmul_rn(Q0[i][j], CGB_W(cur.z, j, k)); break;               \
+  case (LK_GEN << 2) | 3u:                                                                   \
+    R = __dadd_rn(__dmul_rn(P0[i][j], CGB_W(cur.y, j, k)), __dmul_rn(Q0[i][j], CGB_W(cur.z, j, k))); \
+    break;                                                                                   \
+  case (LK_ADD << 2) | 1u: R = CGB_W(cur.y, j, k); break;                                    \
+  case (LK_ADD << 2) | 2u: R = CGB_W(cur.z, j, k); break;                                    \
+  case (LK_ADD << 2) | 3u: R = __dadd_rn(CGB_W(cur.y, j, k), CGB_W(cur.z, j, k)); break;     \
+  case (LK_SUB << 2) | 1u: R = CGB_W(cur.y, j, k); break;                                    \
+  case (LK_SUB << 2) | 2u: R = d_neg(CGB_W(cur.z, j, k)); break;                             \
+  case (LK_SUB << 2) | 3u: R = __dsub_rn(CGB_W(cur.y, j, k), CGB_W(cur.z, j, k)); break;     \
+  case (LK_NEG << 2) | 1u: R = d_neg(CGB_W(cur.y, j, k)); break;                             \
+  case (LK_TWICE << 2) | 1u: {                                                               \
+    const double xb = CGB_W(cur.y, j, k);                                                    \
+    R = __dadd_rn(xb, xb);                                                                   \
+  } break;                                                                                   \
+  case (LK_ASSIGN << 2) | 1u: R = CGB_W(cur.y, j, k); break;                                 \
+  case (LK_IFZ << 2) | 2u: R = d_iszero(Q0[i][j]) ? 0.0 : CGB_W(cur.z, j, k); break;
         // one jump-table dispatch on (kind, active operands): every case holds only the FP64
         // operations it needs, so nothing is computed speculatively (an FP64 instruction holds
         // a sub-partition's FP64 unit for ~64 cycles on GB300)
         const unsigned key = (ent_kind(meta) << 2) | (ent_flags(meta) & 3u);
-        double r[IPT];
-#define CGB_J _Pragma("unroll") for (int j = 0; j < IPT; ++j)
+        double r[IPT][K];
         switch (key) {
           case (LK_OUTPUT << 2) | 0u:
           case (LK_OUTPUT << 2) | 1u: {
-            const IoDesc& d = a.sens[cur.x];
-            CGB_J {
-              if (active[j] && d.ptr)
-                static_cast<double*>(d.ptr)[io_off(d, dir, cur.z, ig[j])] =
-                    (meta & 1u) ? wj<IPT>(wb, cur.y, j) : 0.0;
+            const IoDesc& d = a.sens[xo];
+            CGB_JK {
+              if (dir0 + k < a.ndir && active[j] && d.ptr)
+                static_cast<double*>(d.ptr)[io_off(d, dir0 + k, cur.z, ig[j])] =
+                    (meta & 1u) ? CGB_W(cur.y, j, k) : 0.0;
             }
             continue;
           }
           case (LK_INPUT << 2) | 1u:
             if (a.identity_seed) {
-              CGB_J r[j] = 1.0;
+              CGB_JK r[j][k] = 1.0;
             } else {
               const IoDesc& d = a.seed[cur.y];
-              CGB_J r[j] = active[j]
-                  ? __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir, cur.z, ig[j])) : 0.0;
+              CGB_JK r[j][k] = (active[j] && dir0 + k < a.ndir)
+                  ? __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir0 + k, cur.z, ig[j]))
+                  : 0.0;
             }
             break;
-          case (LK_GEN << 2) | 1u: CGB_J r[j] = __dmul_rn(P0[i][j], wj<IPT>(wb, cur.y, j)); break;
-          case (LK_GEN << 2) | 2u: CGB_J r[j] = __dmul_rn(Q0[i][j], wj<IPT>(wb, cur.z, j)); break;
-          case (LK_GEN << 2) | 3u:
-            CGB_J r[j] = __dadd_rn(__dmul_rn(P0[i][j], wj<IPT>(wb, cur.y, j)),
-                                   __dmul_rn(Q0[i][j], wj<IPT>(wb, cur.z, j)));
-            break;
-          case (LK_ADD << 2) | 1u: CGB_J r[j] = wj<IPT>(wb, cur.y, j); break;
-          case (LK_ADD << 2) | 2u: CGB_J r[j] = wj<IPT>(wb, cur.z, j); break;
-          case (LK_ADD << 2) | 3u:
-            CGB_J r[j] = __dadd_rn(wj<IPT>(wb, cur.y, j), wj<IPT>(wb, cur.z, j));
-            break;
-          case (LK_SUB << 2) | 1u: CGB_J r[j] = wj<IPT>(wb, cur.y, j); break;
-          case (LK_SUB << 2) | 2u: CGB_J r[j] = d_neg(wj<IPT>(wb, cur.z, j)); break;
-          case (LK_SUB << 2) | 3u:
-            CGB_J r[j] = __dsub_rn(wj<IPT>(wb, cur.y, j), wj<IPT>(wb, cur.z, j));
-            break;
-          case (LK_NEG << 2) | 1u: CGB_J r[j] = d_neg(wj<IPT>(wb, cur.y, j)); break;
-          case (LK_TWICE << 2) | 1u:
-            CGB_J {
-              const double xb = wj<IPT>(wb, cur.y, j);
-              r[j] = __dadd_rn(xb, xb);
+#define CGB_UNIFORM(KEY) \
+  case KEY: {            \
+    CGB_JK switch (KEY) { CGB_TAN_CASES(r[j][k], j, k) default: break; } \
+  } break;
+          CGB_UNIFORM((LK_GEN << 2) | 1u)
+          CGB_UNIFORM((LK_GEN << 2) | 2u)
+          CGB_UNIFORM((LK_GEN << 2) | 3u)
+          CGB_UNIFORM((LK_ADD << 2) | 1u)
+          CGB_UNIFORM((LK_ADD << 2) | 2u)
+          CGB_UNIFORM((LK_ADD << 2) | 3u)
+          CGB_UNIFORM((LK_SUB << 2) | 1u)
+          CGB_UNIFORM((LK_SUB << 2) | 2u)
+          CGB_UNIFORM((LK_SUB << 2) | 3u)
+          CGB_UNIFORM((LK_NEG << 2) | 1u)
+          CGB_UNIFORM((LK_TWICE << 2) | 1u)
+          CGB_UNIFORM((LK_ASSIGN << 2) | 1u)
+          CGB_UNIFORM((LK_IFZ << 2) | 2u)
+#undef CGB_UNIFORM
+          case (LK_MIXED << 2): {
+            if (K == 1) continue;
+            // directions of the group differ: one dispatch per direction
+            const unsigned rk = (cur.x >> 19) & 15u;
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+              const unsigned fk = (cur.x >> (24 + 2 * k)) & 3u;
+              if (rk == LK_OUTPUT) {
+                const IoDesc& d = a.sens[xo];
+#pragma unroll
+                for (int j = 0; j < IPT; ++j)
+                  if (dir0 + k < a.ndir && active[j] && d.ptr)
+                    static_cast<double*>(d.ptr)[io_off(d, dir0 + k, cur.z, ig[j])] =
+                        (fk & 1u) ? CGB_W(cur.y, j, k) : 0.0;
+                continue;
+              }
+              if (!fk) continue;
+              if (rk == LK_INPUT) {
+#pragma unroll
+                for (int j = 0; j < IPT; ++j) {
+                  double v = 1.0;
+                  if (!a.identity_seed) {
+                    const IoDesc& d = a.seed[cur.y];
+                    v = (active[j] && dir0 + k < a.ndir)
+                        ? __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir0 + k, cur.z, ig[j]))
+                        : 0.0;
+                  }
+                  CGB_W(xo, j, k) = v;
+                }
+                continue;
+              }
+#pragma unroll
+              for (int j = 0; j < IPT; ++j) {
+                double rr = 0.0;
+                switch ((rk << 2) | fk) {
+                  CGB_TAN_CASES(rr, j, k)
+                  default: break;
+                }
+                CGB_W(xo, j, k) = rr;
+              }
             }
-            break;
-          case (LK_ASSIGN << 2) | 1u: CGB_J r[j] = wj<IPT>(wb, cur.y, j); break;
-          case (LK_IFZ << 2) | 2u:
-            CGB_J r[j] = d_iszero(Q0[i][j]) ? 0.0 : wj<IPT>(wb, cur.z, j);
-            break;
+            continue;
+          }
           default:
             continue;  // NOP padding
         }
-        CGB_J wj<IPT>(wb, cur.x, j) = r[j];
+        CGB_JK CGB_W(xo, j, k) = r[j][k];
+#undef CGB_TAN_CASES
+#undef CGB_JK
+#undef CGB_W
       }
 #pragma unroll
       for (int i = 0; i < G; ++i) {
@@ -588,6 +665,8 @@ __global__ void __launch_bounds__(32, MB) k_tangent(const __grid_constant__ Swee
   }
 }
 
+#define CGB_J _Pragma("unroll") for (int j = 0; j < IPT; ++j)
+
 // One adjoint sweep of IPT 32-instance tiles by one warp: entry stream st (ngr groups),
 // recorded partials at pt (lane-offset, first tile; tile j at pt + j*tstride), work vector at
 // wb (lane-offset, w[slot][j][lane]).
@@ -601,13 +680,13 @@ __device__ __forceinline__ void adjoint_walk(const uint4* st, int ngr, const dou
   double P0[G][IPT], Q0[G][IPT];
   load_group<G>(st, ngr - 1, ngr, E0);
   load_group<G>(st, ngr - 2 >= 0 ? ngr - 2 : ngr, ngr, E1);
-  load_partials_n<kNC, G, IPT>(E0, pt, tstride, tok, P0, Q0);
+  load_partials_n<kNC, true, G, IPT>(E0, pt, tstride, tok, P0, Q0);
 #pragma unroll 1
   for (int g = ngr - 1; g >= 0; --g) {
     uint4 E2[G];
     double P1[G][IPT], Q1[G][IPT];
     load_group<G>(st, g - 2 >= 0 ? g - 2 : ngr, ngr, E2);
-    load_partials_n<kNC, G, IPT>(E1, pt, tstride, tok, P1, Q1);
+    load_partials_n<kNC, true, G, IPT>(E1, pt, tstride, tok, P1, Q1);
 #pragma unroll
     for (int i = G - 1; i >= 0; --i) {
       const uint4 cur = E0[i];
@@ -1024,41 +1103,64 @@ cudaError_t launch_sp_reverse(const SweepArgs& a, int grid, cudaStream_t s) {
   CGB_DISPATCH_BS(k_sp_reverse)
 }
 
-// Derivative-sweep variants (G entries per group, MB minimum CTAs per SM, IPT tiles per
-// warp), see DirVariant. CGB_VARIANTS(X) lists them as X(variant, G, MB, IPT).
-#define CGB_VARIANTS(X)        \
-  X(DV_G4_R128, 4, 16, 1)      \
-  X(DV_G4_R80, 4, 24, 1)       \
-  X(DV_G2_R80, 2, 24, 1)       \
-  X(DV_G2_R64, 2, 32, 1)       \
-  X(DV_G1_R64, 1, 32, 1)       \
-  X(DV_G2_I2_R128, 2, 16, 2)
+// Derivative-sweep variants: G entries per software-pipeline group, MB minimum CTAs per SM
+// (register cap), IPT tiles per warp and, for the tangent sweep, K directions per warp.
+// CGB_TAN_VARIANTS(X) lists X(variant, G, MB, IPT, K); CGB_ADJ_VARIANTS(X) X(variant, G, MB, IPT).
+#define CGB_TAN_VARIANTS(X)    \
+  X(TV_G2_R80, 2, 24, 1, 1)    \
+  X(TV_G2_R64, 2, 32, 1, 1)    \
+  X(TV_G1_R64, 1, 32, 1, 1)    \
+  X(TV_G2_K2, 2, 16, 1, 2)     \
+  X(TV_G2_K4, 2, 8, 1, 4)
+#define CGB_ADJ_VARIANTS(X)    \
+  X(AV_G2_R80, 2, 24, 1)       \
+  X(AV_G1_R64, 1, 32, 1)       \
+  X(AV_G2_R64, 2, 32, 1)       \
+  X(AV_G2_I2_R128, 2, 16, 2)   \
+  X(AV_G4_R128, 4, 16, 1)
 
-int variant_ipt(int variant) {
+void tan_variant_shape(int variant, int* ipt, int* k) {
+  *ipt = 1;
+  *k = 1;
+  switch (variant) {
+#define CGB_SHAPE(V, G, MB, IPT, K) \
+  case V: *ipt = IPT; *k = K; break;
+    CGB_TAN_VARIANTS(CGB_SHAPE)
+#undef CGB_SHAPE
+    default: break;
+  }
+}
+
+int adj_variant_ipt(int variant) {
   switch (variant) {
 #define CGB_IPT(V, G, MB, IPT) case V: return IPT;
-    CGB_VARIANTS(CGB_IPT)
+    CGB_ADJ_VARIANTS(CGB_IPT)
 #undef CGB_IPT
     default: return 1;
   }
 }
 
-#define CGB_DISPATCH_VARIANT(KT)                                                          \
-  switch (variant) {                                                                      \
-    CGB_VARIANTS(CGB_LAUNCH_##KT)                                                         \
-    default: return cudaErrorInvalidValue;                                                \
-  }
-#define CGB_LAUNCH_k_tangent(V, G, MB, IPT) \
-  case V: return launch_k(k_tangent<G, MB, IPT>, dim3(grid), 32, smem_lean(a.t.sz_w, IPT, 0), a, s);
-#define CGB_LAUNCH_k_adjoint(V, G, MB, IPT) \
-  case V: return launch_k(k_adjoint<G, MB, IPT>, dim3(grid), 32, smem_lean(a.t.sz_w, IPT, 0), a, s);
-
 cudaError_t launch_tangent(const SweepArgs& a, int grid, int variant, cudaStream_t s) {
-  CGB_DISPATCH_VARIANT(k_tangent)
+  switch (variant) {
+#define CGB_LAUNCH(V, G, MB, IPT, K)                                                          \
+  case V:                                                                                     \
+    return launch_k(k_tangent<G, MB, IPT, K>, dim3(grid), 32, smem_lean(a.t.sz_w, IPT * K, 0), \
+                    a, s);
+    CGB_TAN_VARIANTS(CGB_LAUNCH)
+#undef CGB_LAUNCH
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 cudaError_t launch_adjoint(const SweepArgs& a, int grid, int variant, cudaStream_t s) {
-  CGB_DISPATCH_VARIANT(k_adjoint)
+  switch (variant) {
+#define CGB_LAUNCH(V, G, MB, IPT)                                                              \
+  case V:                                                                                      \
+    return launch_k(k_adjoint<G, MB, IPT>, dim3(grid), 32, smem_lean(a.t.sz_w, IPT, 0), a, s);
+    CGB_ADJ_VARIANTS(CGB_LAUNCH)
+#undef CGB_LAUNCH
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 cudaError_t launch_adjoint_dense(const SweepArgs& a, int grid, cudaStream_t s) {
@@ -1141,12 +1243,19 @@ int occupancy_dense(int dir_warps, size_t smem) {
 }
 
 int occupancy_dir(int variant, bool adjoint, size_t smem) {
+  if (adjoint) {
+    switch (variant) {
+#define CGB_OCC(V, G, MB, IPT) \
+  case V: return occ_of(k_adjoint<G, MB, IPT>, 32, smem);
+      CGB_ADJ_VARIANTS(CGB_OCC)
+#undef CGB_OCC
+      default: return 0;
+    }
+  }
   switch (variant) {
-#define CGB_OCC(V, G, MB, IPT)                                              \
-  case V:                                                                   \
-    return adjoint ? occ_of(k_adjoint<G, MB, IPT>, 32, smem)                \
-                   : occ_of(k_tangent<G, MB, IPT>, 32, smem);
-    CGB_VARIANTS(CGB_OCC)
+#define CGB_OCC(V, G, MB, IPT, K) \
+  case V: return occ_of(k_tangent<G, MB, IPT, K>, 32, smem);
+    CGB_TAN_VARIANTS(CGB_OCC)
 #undef CGB_OCC
     default: return 0;
   }

@@ -17,7 +17,7 @@ constexpr unsigned kMaxPartials = 1u << 21;  // recorded partials per instance t
 // Entry kinds of the lean derivative streams (bits 16-19 of an entry's meta word).
 enum LeanKind : unsigned {
   LK_NOP = 0, LK_GEN, LK_ADD, LK_SUB, LK_NEG, LK_TWICE, LK_ASSIGN, LK_IFZ, LK_INPUT, LK_OUTPUT,
-  LK_CONST
+  LK_CONST, LK_MIXED
 };
 constexpr int kMaxIo = 64;       // inputs/outputs per tape handled by one launch
 constexpr int kDirWarps = 4;     // directions per CTA in the derivative sweeps (one per warp)
@@ -115,13 +115,14 @@ cudaError_t launch_record(const SweepArgs& a, int grid, cudaStream_t s);
 // Derivative sweeps: 1-D grid whose size is a multiple of the direction-group count
 // ceil(ndir / (block/32)); CTA b works on direction group b % groups.
 // Variants of the warp-independent derivative sweeps: entries per software-pipeline group,
-// a register cap that lets more one-warp CTAs reside per SM, and 32-instance tiles per warp
-// (IPT). All variants do the same arithmetic in the same order; only speed differs, so the
-// host may pick any. The work vector of a variant takes smem_lean(sz_w, IPT, 0) bytes.
-enum DirVariant : int {
-  DV_G4_R128 = 0, DV_G4_R80, DV_G2_R80, DV_G2_R64, DV_G1_R64, DV_G2_I2_R128, DV_COUNT
-};
-int variant_ipt(int variant);
+// a register cap that lets more one-warp CTAs reside per SM, 32-instance tiles per warp (IPT)
+// and, for the tangent sweep, directions per warp (K, walking the union stream of K
+// directions). All variants do the same arithmetic in the same order; only speed differs, so
+// the host may pick any. A variant's work vector takes smem_lean(sz_w, IPT*K, 0) bytes.
+enum TanVariant : int { TV_G2_R80 = 0, TV_G2_R64, TV_G1_R64, TV_G2_K2, TV_G2_K4, TV_COUNT };
+enum AdjVariant : int { AV_G2_R80 = 0, AV_G1_R64, AV_G2_R64, AV_G2_I2_R128, AV_G4_R128, AV_COUNT };
+void tan_variant_shape(int variant, int* ipt, int* k);
+int adj_variant_ipt(int variant);
 cudaError_t launch_tangent(const SweepArgs& a, int grid, int variant, cudaStream_t s);
 cudaError_t launch_adjoint(const SweepArgs& a, int grid, int variant, cudaStream_t s);
 // The adjoint sweep without an activity plan (see k_adjoint<DW, true>).

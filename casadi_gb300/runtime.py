@@ -75,6 +75,9 @@ def load(path=None):
         "casadi_gb300_map_reverse": (cint, [cint, cint, i64, cint, vp, vp, vp, vp]),
         "casadi_gb300_jacobian": (cint, [cint, i64, i64, vp, vp, vp, vp, sz, vp]),
         "casadi_gb300_map_jacobian": (cint, [cint, cint, i64, vp, vp, vp]),
+        "casadi_gb300_jacobian_reverse": (cint, [cint, i64, i64, vp, vp, vp, cint, vp, vp, vp, sz,
+                                                 vp]),
+        "casadi_gb300_map_jacobian_reverse": (cint, [cint, cint, i64, vp, vp, vp, cint, vp, vp]),
         "casadi_gb300_reverse_noalloc": (cint, [cint, i64, i64, cint, vp, vp, vp, vp, vp]),
         "casadi_gb300_profile": (cint, [cint]),
         "casadi_gb300_profile_collect": (cint, [vp, vp, cint]),
@@ -244,6 +247,23 @@ class CudaTape:
             ct.c_void_p(sc.data_ptr()), sc.numel(), _stream_handle(stream)))
         return res, jac
 
+    def jacobian_reverse(self, args, aseeds, n=None, res=None, jac=None, asens=None,
+                         stream=None, scratch_limit=None):
+        """Jacobian (as :meth:`jacobian`) and adjoint sensitivities (as :meth:`reverse`) from
+        one record sweep."""
+        n = self._n(args) if n is None else n
+        nz = sum(self.nnz_in)
+        nadj = next(s.shape[0] for s in aseeds if s is not None)
+        res = self._outs(self.nnz_out, n) if res is None else res
+        jac = self._outs(self.nnz_out, n, nz) if jac is None else jac
+        asens = self._outs(self.nnz_in, n, nadj) if asens is None else asens
+        sc = self.scratch(n, scratch_limit)
+        check(load().casadi_gb300_jacobian_reverse(
+            self.id, n, n, _ptr_array(args), _ptr_array(res), _ptr_array(jac), nadj,
+            _ptr_array(aseeds), _ptr_array(asens), ct.c_void_p(sc.data_ptr()), sc.numel(),
+            _stream_handle(stream)))
+        return res, jac, asens
+
     def sp_forward(self, args, n=None, stream=None):
         """args: int64 tensors holding bvec_t bit patterns, shape (nnz, n)."""
         import torch
@@ -332,6 +352,21 @@ class CudaMap:
                                                _host_ptrs(args), _host_ptrs(res), _host_ptrs(jac)))
         return res, jac
 
+    def jacobian_reverse(self, args, aseeds, res=None, jac=None, asens=None):
+        """Host-buffer Jacobian (as :meth:`jacobian`) and adjoint (as :meth:`reverse`) from
+        one record sweep."""
+        args = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in args]
+        aseeds = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in aseeds]
+        nadj = next(a.shape[1] for a in aseeds if a is not None)
+        nz = sum(self.tape.nnz_in)
+        res = self._host_out(self.tape.nnz_out) if res is None else res
+        jac = [np.empty((self.n, nz, k)) for k in self.tape.nnz_out] if jac is None else jac
+        asens = [np.empty((self.n, nadj, k)) for k in self.tape.nnz_in] if asens is None else asens
+        check(load().casadi_gb300_map_jacobian_reverse(
+            self.tape.id, self.mem.id, self.n, _host_ptrs(args), _host_ptrs(res),
+            _host_ptrs(jac), nadj, _host_ptrs(aseeds), _host_ptrs(asens)))
+        return res, jac, asens
+
     def reverse(self, args, aseeds, res=None, asens=None):
         """Adjoint sweep with instance-major host buffers: aseeds[j] has shape
         (n, nadj, nnz_out[j]); returns (res, asens) with asens[j] of shape (n, nadj, nnz_in[j])."""
@@ -398,7 +433,8 @@ class Batch:
                                             _stream_handle(stream)))
 
 
-N_VARIANTS = 6
+N_TAN_VARIANTS = 5  # tangent-sweep kernel variants (forward, Jacobian)
+N_ADJ_VARIANTS = 5  # adjoint-sweep kernel variants
 
 FAMILIES = ("eval", "record", "tangent", "adjoint", "sp_forward", "sp_reverse", "batch")
 

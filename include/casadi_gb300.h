@@ -144,6 +144,16 @@ CASADI_GB300_API int casadi_gb300_jacobian(int id, int64_t n, int64_t ld, const 
                           double* const* res, double* const* jac, void* scratch,
                           size_t scratch_bytes, void* stream);
 
+/* Jacobian and adjoint sensitivities in one call: one record sweep, then the identity-seeded
+ * forward sweep (jac as in casadi_gb300_jacobian) and nadj adjoint directions (aseed/asens as
+ * in casadi_gb300_reverse), both reading the same recorded partials. Results equal those of
+ * the two separate calls bit for bit. Replaces evaluating CasADi's jacobian() and reverse()
+ * Functions (casadi/core/function_internal.cpp:2285-2340) one after the other on a Map. */
+CASADI_GB300_API int casadi_gb300_jacobian_reverse(int id, int64_t n, int64_t ld,
+                           const double* const* arg, double* const* res, double* const* jac,
+                           int nadj, const double* const* aseed, double* const* asens,
+                           void* scratch, size_t scratch_bytes, void* stream);
+
 /* Sparsity propagation with bvec_t = uint64_t (casadi/core/casadi_common.hpp:126-130).
  * sp_forward: res[j] = dependency bits of the outputs given arg bits
  * (SXFunction::sp_forward, sx_function.cpp:1657-1682).
@@ -180,6 +190,11 @@ CASADI_GB300_API int casadi_gb300_map_jacobian(int id, int mem, int64_t n, const
 CASADI_GB300_API int casadi_gb300_map_reverse(int id, int mem, int64_t n, int nadj, const double* const* arg,
                              double* const* res, const double* const* aseed,
                              double* const* asens);
+/* Host-buffer form of casadi_gb300_jacobian_reverse: arg/res/aseed as in the two calls
+ * above, jac[j] as in casadi_gb300_map_jacobian, asens[j] as in casadi_gb300_map_reverse. */
+CASADI_GB300_API int casadi_gb300_map_jacobian_reverse(int id, int mem, int64_t n,
+                           const double* const* arg, double* const* res, double* const* jac,
+                           int nadj, const double* const* aseed, double* const* asens);
 
 /* Autotuning of the derivative sweeps (on by default): the first call of each kind
  * (0 seeded forward, 1 Jacobian, 2 adjoint) on a tape whose wave fills the GPU several times
@@ -190,7 +205,8 @@ CASADI_GB300_API int casadi_gb300_map_reverse(int id, int mem, int64_t n, int na
  * the reference, whose Map has one code path per parallelization (casadi/core/map.cpp:39-51). */
 CASADI_GB300_API int casadi_gb300_autotune(int enable);
 CASADI_GB300_API int casadi_gb300_tuned_variant(int id, int kind, int* variant);
-/* Fixes the variant of one kind on a tape (0..5), or clears it for retuning (-1). */
+/* Fixes the variant of one kind on a tape (kinds 0 and 1: 0..4; kind 2: 0..4), or clears it
+ * for retuning (-1). */
 CASADI_GB300_API int casadi_gb300_set_variant(int id, int kind, int variant);
 
 /* Persistent multi-tape batches. A batch is a list of items, each one tape over its own

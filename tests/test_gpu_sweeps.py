@@ -352,13 +352,14 @@ def test_every_variant_gives_the_same_bits(gpu_lib):
     n = 2500
     args = dev(W.cartpole_inputs(n, steps=6, seed=21))
     rng = np.random.default_rng(21)
-    fseeds = dev([rng.standard_normal((3, k, n)) for k in F.tape.nnz_in])
+    fseeds = dev([rng.standard_normal((5, k, n)) for k in F.tape.nnz_in])  # 5: ragged groups
     aseeds = dev([rng.standard_normal((2, k, n)) for k in F.tape.nnz_out])
     ct = CudaTape(F)
     base = None
-    for v in range(R.N_VARIANTS):
-        for kind in range(3):
-            ct.set_variant(kind, v)
+    for v in range(max(R.N_TAN_VARIANTS, R.N_ADJ_VARIANTS)):
+        ct.set_variant(0, min(v, R.N_TAN_VARIANTS - 1))
+        ct.set_variant(1, min(v, R.N_TAN_VARIANTS - 1))
+        ct.set_variant(2, min(v, R.N_ADJ_VARIANTS - 1))
         got = [host(ct.forward(args, fseeds)[1]), host(ct.jacobian(args)[1]),
                host(ct.reverse(args, aseeds)[1])]
         if base is None:
@@ -382,7 +383,35 @@ def test_autotuner_keeps_a_variant_and_results(gpu_lib):
     ct.set_variant(2, -1)
     R.autotune(True)
     _, got = ct.reverse(args, aseeds)
-    assert 0 <= ct.tuned_variant(2) < R.N_VARIANTS
+    assert 0 <= ct.tuned_variant(2) < R.N_ADJ_VARIANTS
     for x, y in zip(host(got), host(want)):
         assert_bitexact(x, y, "autotuned adjoint")
+    ct.sync()
+
+
+def test_jacobian_reverse_equals_the_two_calls(gpu_lib):
+    """One record sweep feeding both derivative sweeps gives the same bits as calling
+    jacobian and reverse one after the other, on device buffers and on host buffers."""
+    F = W.cartpole_rollout(5)
+    n = 3001
+    args_h = W.cartpole_inputs(n, steps=5, seed=31)
+    rng = np.random.default_rng(31)
+    aseeds_h = [rng.standard_normal((2, k, n)) for k in F.tape.nnz_out]
+    ct = CudaTape(F)
+    args, aseeds = dev(args_h), dev(aseeds_h)
+    r1, jac1 = ct.jacobian(args)
+    _, as1 = ct.reverse(args, aseeds)
+    r2, jac2, as2 = ct.jacobian_reverse(args, aseeds)
+    for a, b in zip(host(r1) + host(jac1) + host(as1), host(r2) + host(jac2) + host(as2)):
+        assert_bitexact(a, b, "fused jacobian+reverse")
+    m = CudaMap(F, n)
+    hargs = [a.T.copy() for a in args_h]
+    hseeds = [np.transpose(s, (2, 0, 1)).copy() for s in aseeds_h]
+    _, hj1 = m.jacobian(*hargs)
+    _, ha1 = m.reverse(hargs, hseeds)
+    _, hj2, ha2 = m.jacobian_reverse(hargs, hseeds)
+    for a, b in zip(hj1 + ha1, hj2 + ha2):
+        assert_bitexact(a, b, "host-buffer fused jacobian+reverse")
+    # host layout agrees with the device layout
+    assert_bitexact(np.transpose(hj2[0], (1, 2, 0)), host(jac2)[0], "layouts")
     ct.sync()
