@@ -444,6 +444,17 @@ def run_native(a):
     achieved = flops_per_launch / (dom_ms / dom_launches * 1e-3) / 1e12
     peak = fp64_peak_tflops(torch) / 2.0  # DFMA instructions/s: the FP64-pipe instruction rate
     gpu_launches = sum(v[1] for v in prof.values())
+    # DRAM bytes per launch of the dominant kernel from the committed ncu capture, scaled by
+    # the instances one launch processes (traffic grows in proportion: the partial reads do)
+    traffic = None
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles",
+                               "traffic.json")) as f:
+            tr = json.load(f).get(dom)
+        if tr and a.workload == "rollout20":
+            traffic = tr["dram_bytes_per_launch"] * (n / launches_per_step) / tr["instances"]
+    except (OSError, ValueError, KeyError):
+        traffic = None
     io_bytes = 8 * n * (sum(F.tape.nnz_in) + sum(F.tape.nnz_out))
 
     # end-to-end through the host-buffer Map entry points (pinned host memory)
@@ -508,7 +519,8 @@ def run_native(a):
         "kernel_ms": {k: round(v[0], 4) for k, v in prof.items() if v[1]},
         "roofline": {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
-                     "traffic": None,
+                     "traffic": traffic,
+                     "traffic_unit": "bytes per launch (ncu, scaled from the committed capture)",
                      "flop": "one FP64-pipe instruction (DADD, DMUL, DFMA); libm calls weighted by "
                              "casadi_gb300/op_weights.json; derivative sweeps count structural work",
                      "peak_source": "cuBLAS FP64 GEMM FLOP/s measured in this run / 2 "
