@@ -52,7 +52,8 @@ def make_workload(name, instances=None):
         n = instances or 16384
         args = W.dag_inputs(n)
         return F, n, args, [np.ones((1, 16, n))], \
-            "random DAG 64in/10000 nodes/16out, N=%d" % n
+            "random DAG 64in/10000 nodes/16out, N=%d: eval + adjoint of the sum of outputs + " \
+            "sp_forward + sp_reverse" % n
     raise SystemExit("unknown workload " + name)
 
 
@@ -259,6 +260,10 @@ def cpu_step(tape, args, aseeds, n, threads, workload):
     t0 = time.perf_counter()
     if workload == "dag":
         O.reverse(tape, args, aseeds, n, threads)
+        bits = [np.repeat((np.uint64(1) << np.arange(64, dtype=np.uint64))[:, None], n, axis=1)]
+        O.sp_forward(tape, bits, n, threads)
+        seeds = [np.repeat((np.uint64(1) << np.arange(16, dtype=np.uint64))[:, None], n, axis=1)]
+        O.sp_reverse(tape, [np.zeros((64, n), np.uint64)], seeds, n, threads)
     else:
         O.eval(tape, args, n, threads)
     return time.perf_counter() - t0
@@ -339,6 +344,40 @@ def mixed_component(torch, R, stream, reps=3):
             "speedup": ms_plain / ms_batch, "bitwise_equal": same}
 
 
+def rollout_autograd_component(torch, stream, n=1 << 20, reps=2):
+    """The cart-pole 100-step rollout over 2^20 instances differentiated through
+    torch.autograd: ten checkpointed 10-step segment tapes; forward stores only the segment
+    inputs, backward re-runs each segment's record sweep and its adjoint sweep. One step =
+    forward + backward of sum(cost) with respect to x0 and U[100]."""
+    from casadi_gb300 import workloads as W
+    from casadi_gb300.autograd import CheckpointedRollout
+    x0, U = W.cartpole_inputs(n, steps=100, seed=3)
+    tx = torch.from_numpy(x0).cuda().requires_grad_(True)
+    tu = torch.from_numpy(U * 0.1).cuda().requires_grad_(True)
+    roll = CheckpointedRollout(steps=100, every=10)
+
+    def fb():
+        tx.grad = None
+        tu.grad = None
+        _, cost = roll(tx, tu)
+        cost.sum().backward()
+
+    fb()
+    torch.cuda.synchronize()
+    torch.cuda.reset_peak_memory_stats()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(torch.cuda.current_stream())
+    for _ in range(reps):
+        fb()
+    e1.record(torch.cuda.current_stream())
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    finite = bool(torch.isfinite(tu.grad).all().item())
+    return {"instances": n, "steps": 100, "checkpoint_every": 10, "ms": ms,
+            "evals_per_s": n / (ms * 1e-3), "grad_finite": finite,
+            "peak_device_gb": torch.cuda.max_memory_allocated() / 1e9}
+
+
 def run_native(a):
     import torch
     from casadi_gb300 import runtime as R
@@ -365,12 +404,27 @@ def run_native(a):
     asens = [torch.empty((1, k, n), dtype=torch.float64, device="cuda") for k in F.tape.nnz_in]
     ct.scratch(n)
 
+    if a.workload == "dag":
+        # bvec_t patterns: input nonzero k carries bit k (64 inputs, one forward sweep);
+        # output nonzero k seeds bit k of the reverse sweep (16 outputs, one sweep)
+        sp_in = torch.tensor([1 << k if k < 63 else -(1 << 63) for k in range(64)],
+                             dtype=torch.int64, device="cuda")[:, None].expand(64, n).contiguous()
+        sp_seed0 = torch.tensor([1 << k for k in range(16)], dtype=torch.int64,
+                                device="cuda")[:, None].expand(16, n).contiguous()
+        sp_seed = torch.empty_like(sp_seed0)
+        sp_sens = torch.empty((64, n), dtype=torch.int64, device="cuda")
+
     def step():
         if a.workload == "rollout20":
             # one record sweep feeds the Jacobian (24 unit directions) and the cost adjoint
             ct.jacobian_reverse(dargs, daseeds, res=res, jac=jac, asens=asens, stream=stream)
         elif a.workload == "dag":
+            # eval + adjoint of the sum of outputs, then both sparsity sweeps
             ct.reverse(dargs, daseeds, res=res, asens=asens, stream=stream)
+            ct.sp_forward([sp_in], stream=stream)
+            sp_seed.copy_(sp_seed0)
+            sp_sens.zero_()
+            ct.sp_reverse([sp_sens], [sp_seed], stream=stream)
         else:
             ct.eval(dargs, res=res, stream=stream)
 
@@ -430,6 +484,7 @@ def run_native(a):
 
     if not a.no_mixed:
         comps["mixed_batch"] = mixed_component(torch, R, stream)
+        comps["rollout100_autograd"] = rollout_autograd_component(torch, stream)
 
     # roofline of the dominant kernel family (device time from the per-launch events)
     weights = load_weights()
