@@ -378,6 +378,41 @@ def rollout_autograd_component(torch, stream, n=1 << 20, reps=2):
             "peak_device_gb": torch.cuda.max_memory_allocated() / 1e9}
 
 
+def mpc_sparse_component(torch, stream, n=4096, intervals=100, reps=3):
+    """Scenario MPC: the quadcopter multiple-shooting NLP (100 intervals, 1612 decision
+    variables, 1212 constraints) over 4096 scenarios: the constraint Jacobian by uni-coloured
+    forward sweeps and the Lagrangian Hessian by star-coloured forward sweeps over the
+    symbolic gradient, nonzeros recovered on the device. One step = both, all scenarios."""
+    from casadi_gb300 import workloads as W
+    from casadi_gb300.sparse_ad import ColoredHessian, ColoredJacobian
+    t0 = time.perf_counter()
+    F = W.quad_ms_lagrangian(intervals)
+    J = ColoredJacobian(W.quad_ms_constraints(intervals), out=0, wrt=0)
+    H = ColoredHessian(F, out=1, wrt=0)
+    setup_s = time.perf_counter() - t0
+    args = [torch.from_numpy(x).cuda() for x in W.quad_ms_inputs(n, intervals, seed=5)]
+
+    def step():
+        J(args, stream=stream)
+        H(args, stream=stream)
+
+    step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        step()
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    return {"scenarios": n, "intervals": intervals, "decision_variables": F.tape.nnz_in[0],
+            "constraints": F.tape.nnz_out[0], "lagrangian_instructions": F.tape.n_instr,
+            "gradient_instructions": H.gradient_function.tape.n_instr,
+            "jacobian_nnz": J.pattern.nnz, "jacobian_colors": J.n_colors,
+            "hessian_nnz_lower": int(H.rows.size), "hessian_colors": H.n_colors,
+            "ms": ms, "scenarios_per_s": n / (ms * 1e-3), "host_setup_s": setup_s}
+
+
 def run_native(a):
     import torch
     from casadi_gb300 import runtime as R
@@ -485,6 +520,7 @@ def run_native(a):
     if not a.no_mixed:
         comps["mixed_batch"] = mixed_component(torch, R, stream)
         comps["rollout100_autograd"] = rollout_autograd_component(torch, stream)
+        comps["mpc_sparse_hessian"] = mpc_sparse_component(torch, stream)
 
     # roofline of the dominant kernel family (device time from the per-launch events)
     weights = load_weights()

@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "../../include/casadi_gb300.h"
+#include "coloring.cuh"
 #include "schedule.cuh"
 #include "sweeps.cuh"
 
@@ -82,6 +83,8 @@ int reference_opcode(unsigned dop) {
 struct TanPlan {
   int ndir = 0, dw = 0, ch = 0;
   bool identity = false;
+  std::vector<int> dirmap;   // identity mode: direction seeded by each flat input nonzero
+                             // (empty: nonzero k seeds direction k; -1: not seeded)
   std::vector<char> seeded;  // per input: seed pointer given (general seeds)
   int groups = 0;
   uint4* d_stream = nullptr;  // entry streams of all directions
@@ -384,17 +387,19 @@ std::vector<int> partial_starts(const Tape& t) {
 // when an operand that carries a derivative is active (the reference's 0*x -> 0, x+0 -> x).
 // Each direction group gets a compacted entry stream of the instructions with work for it.
 const TanPlan* tan_plan(Tape& t, int ndir, int dw, int ch, bool identity,
-                        const std::vector<char>& seeded, int* err) {
+                        const std::vector<char>& seeded, const std::vector<int>& dirmap,
+                        int* err) {
   std::lock_guard<std::mutex> lk(t.shape_mtx);
   for (auto& p : t.tan_plans)
     if (p->ndir == ndir && p->dw == dw && p->ch == ch && p->identity == identity &&
-        (identity || p->seeded == seeded))
+        (identity ? p->dirmap == dirmap : p->seeded == seeded))
       return p.get();
   auto p = std::make_unique<TanPlan>();
   p->ndir = ndir;
   p->dw = dw;
   p->ch = ch;
   p->identity = identity;
+  p->dirmap = dirmap;
   p->seeded = seeded;
   p->groups = (ndir + dw - 1) / dw;
   const size_t nc = t.h_code.size();
@@ -415,7 +420,9 @@ const TanPlan* tan_plan(Tape& t, int ndir, int dw, int ch, bool identity,
         continue;
       }
       if (op == D_INPUT) {
-        const bool on = identity ? (off[B] + static_cast<int>(C) == d) : seeded[B] != 0;
+        const int flat = off[B] + static_cast<int>(C);
+        const bool on = identity ? ((dirmap.empty() ? flat : dirmap[flat]) == d)
+                                 : seeded[B] != 0;
         act[A] = on;
         b = on ? 1u : 0u;
       } else if (op == D_OUTPUT) {
@@ -568,6 +575,7 @@ struct DerivReq {
   int ndir = 0;
   bool adjoint = false;
   bool identity = false;
+  const std::vector<int>* dirmap = nullptr;  // identity mode: direction of each input nonzero
   const IoDesc* seed = nullptr;
   const IoDesc* sens = nullptr;
 };
@@ -630,7 +638,9 @@ int run_deriv(Tape& t, SweepArgs a, long long m, const DerivReq& rq, cudaStream_
     if (adjoint) return launch_adjoint(a, grid_of(v), v, s);
     int ipt = 1, kd = 1;
     tan_variant_shape(v, &ipt, &kd);
-    const TanPlan* tp = tan_plan(t, ndir, kd, 0, identity, seeded_in, &plan_err);
+    static const std::vector<int> kNoMap;
+    const TanPlan* tp =
+        tan_plan(t, ndir, kd, 0, identity, seeded_in, rq.dirmap ? *rq.dirmap : kNoMap, &plan_err);
     if (!tp) return cudaErrorInvalidValue;
     a.dstream = tp->d_stream;
     a.dchunks = tp->d_chunks;
@@ -939,6 +949,37 @@ int casadi_gb300_tape_schedule(const casadi_gb300_atomic* alg, int n_instr, int 
   return 0;
 }
 
+static int check_ccs(int nrow, int ncol, const int* colind, const int* row) {
+  if (nrow < 0 || ncol < 0 || !colind) return fail(CASADI_GB300_ERR_ARG, "bad pattern size");
+  if (colind[0] != 0) return fail(CASADI_GB300_ERR_ARG, "colind[0] must be 0");
+  for (int j = 0; j < ncol; ++j)
+    if (colind[j] > colind[j + 1]) return fail(CASADI_GB300_ERR_ARG, "colind not increasing");
+  const int nnz = colind[ncol];
+  if (nnz > 0 && !row) return fail(CASADI_GB300_ERR_ARG, "missing row array");
+  for (int j = 0; j < ncol; ++j)
+    for (int k = colind[j]; k < colind[j + 1]; ++k) {
+      if (row[k] < 0 || row[k] >= nrow) return fail(CASADI_GB300_ERR_ARG, "row out of range");
+      if (k > colind[j] && row[k] <= row[k - 1])
+        return fail(CASADI_GB300_ERR_ARG, "rows not sorted within column %d", j);
+    }
+  return 0;
+}
+
+int casadi_gb300_uni_coloring(int nrow, int ncol, const int* colind, const int* row,
+                              int* color) {
+  if (int rc = check_ccs(nrow, ncol, colind, row)) return rc;
+  if (ncol > 0 && !color) return fail(CASADI_GB300_ERR_ARG, "missing color array");
+  return uni_coloring_ccs(nrow, ncol, colind, row, color);
+}
+
+int casadi_gb300_star_coloring(int n, const int* colind, const int* row, int ordering,
+                               int* color) {
+  if (int rc = check_ccs(n, n, colind, row)) return rc;
+  if (n > 0 && !color) return fail(CASADI_GB300_ERR_ARG, "missing color array");
+  if (ordering != 0 && ordering != 1) return fail(CASADI_GB300_ERR_ARG, "ordering must be 0 or 1");
+  return star_coloring_ccs(n, colind, row, ordering, color);
+}
+
 int casadi_gb300_tape_free(int id) {
   std::lock_guard<std::mutex> lk(g_mtx);
   if (id < 0 || id >= static_cast<int>(g_tapes.size()) || !g_tapes[id])
@@ -1045,6 +1086,48 @@ int casadi_gb300_jacobian(int id, int64_t n, int64_t ld, const double* const* ar
   fill_io(sens, t->n_out, vptrs(jac), t->nnz_out, ld, true);
   return run_ad(*t, n, in, out, seed, sens, nz, false, true, scratch, scratch_bytes,
                 static_cast<cudaStream_t>(stream));
+}
+
+int casadi_gb300_jacobian_colored(int id, int64_t n, int64_t ld, int n_colors,
+                                  const int* color, const double* const* arg,
+                                  double* const* res, double* const* comp, void* scratch,
+                                  size_t scratch_bytes, void* stream) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  if (int rc = check_device(*t)) return rc;
+  if (int rc = check_n(n, ld)) return rc;
+  int nz = 0;
+  for (int v : t->nnz_in) nz += v;
+  if (!color || n_colors < 1 || n_colors > nz)
+    return fail(CASADI_GB300_ERR_ARG, "bad colouring (%d colours for %d input nonzeros)",
+                n_colors, nz);
+  std::vector<int> dirmap(color, color + nz);
+  for (int v : dirmap)
+    if (v < -1 || v >= n_colors) return fail(CASADI_GB300_ERR_ARG, "colour %d out of range", v);
+  IoDesc in[kMaxIo], out[kMaxIo], seed[kMaxIo], sens[kMaxIo];
+  fill_io(in, t->n_in, vptrs(arg), t->nnz_in, ld, false);
+  fill_io(out, t->n_out, vptrs(res), t->nnz_out, ld, false);
+  fill_io(seed, t->n_in, nullptr, t->nnz_in, ld, true);
+  fill_io(sens, t->n_out, vptrs(comp), t->nnz_out, ld, true);
+  DerivReq rq;
+  rq.ndir = n_colors;
+  rq.identity = true;
+  rq.dirmap = &dirmap;
+  rq.seed = seed;
+  rq.sens = sens;
+  return run_ad_multi(*t, n, in, out, &rq, 1, scratch, scratch_bytes,
+                      static_cast<cudaStream_t>(stream));
+}
+
+int casadi_gb300_gather(int64_t n, int64_t ld, int count, const int64_t* src_row,
+                        const double* src, double* dst, void* stream) {
+  if (n < 0 || ld < n || count < 0 || (count > 0 && (!src_row || !src || !dst)))
+    return fail(CASADI_GB300_ERR_ARG, "bad arguments");
+  if (n == 0 || count == 0) return 0;
+  cudaError_t e = launch_gather(n, ld, count, reinterpret_cast<const long long*>(src_row), src,
+                                dst, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "gather launch");
+  return 0;
 }
 
 int casadi_gb300_jacobian_reverse(int id, int64_t n, int64_t ld, const double* const* arg,

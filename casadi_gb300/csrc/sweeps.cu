@@ -22,6 +22,8 @@
 // Waits on the staging barriers are bounded: after ~1 s without completion a kernel sets
 // kErrWaitTimeout in the tape's error word, waits (again bounded) for its own copies in
 // flight and returns. No kernel traps.
+#include <algorithm>
+
 #include "sweeps.cuh"
 
 namespace cgb {
@@ -1173,6 +1175,27 @@ cudaError_t launch_adjoint_dense(const SweepArgs& a, int grid, cudaStream_t s) {
     case 8: return launch_k(k_adjoint_tape<8, true>, dim3(grid), 256, smem, a, s);
     default: return cudaErrorInvalidValue;
   }
+}
+
+// Gather of rows: dst[e*ld + i] = src[src_row[e]*ld + i] (recovery of sparse Jacobian and
+// Hessian nonzeros from colour-compressed products; HBM-bound, coalesced over instances).
+__global__ void __launch_bounds__(256) k_gather(long long n, long long ld, int count,
+                                                const long long* __restrict__ src_row,
+                                                const double* __restrict__ src,
+                                                double* __restrict__ dst) {
+  const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int e = blockIdx.y; e < count; e += gridDim.y)
+    dst[static_cast<long long>(e) * ld + i] = __ldg(src + __ldg(src_row + e) * ld + i);
+}
+
+cudaError_t launch_gather(long long n, long long ld, int count, const long long* src_row,
+                          const double* src, double* dst, cudaStream_t s) {
+  const long long bx = (n + 255) / 256;
+  if (bx > 0x7fffffffll) return cudaErrorInvalidValue;
+  dim3 grid(static_cast<unsigned>(bx), static_cast<unsigned>(std::min(count, 65535)));
+  k_gather<<<grid, 256, 0, s>>>(n, ld, count, src_row, src, dst);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_batch(const BatchArgs& b, int grid, size_t smem, cudaStream_t s) {

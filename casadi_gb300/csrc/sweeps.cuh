@@ -97,6 +97,8 @@ struct BatchArgs {
   long long scratch_stride;
 };
 
+cudaError_t launch_gather(long long n, long long ld, int count, const long long* src_row,
+                          const double* src, double* dst, cudaStream_t s);
 cudaError_t launch_batch(const BatchArgs& b, int grid, size_t smem, cudaStream_t s);
 int occupancy_batch(size_t smem);
 

@@ -84,6 +84,11 @@ def load(path=None):
         "casadi_gb300_autotune": (cint, [cint]),
         "casadi_gb300_tuned_variant": (cint, [cint, cint, vp]),
         "casadi_gb300_set_variant": (cint, [cint, cint, cint]),
+        "casadi_gb300_uni_coloring": (cint, [cint, cint, vp, vp, vp]),
+        "casadi_gb300_jacobian_colored": (cint, [cint, i64, i64, cint, vp, vp, vp, vp, vp, sz,
+                                                 vp]),
+        "casadi_gb300_gather": (cint, [i64, i64, cint, vp, vp, vp, vp]),
+        "casadi_gb300_star_coloring": (cint, [cint, vp, vp, cint, vp]),
         "casadi_gb300_batch_create": (cint, []),
         "casadi_gb300_batch_free": (cint, [cint]),
         "casadi_gb300_batch_add": (cint, [cint, cint, i64, i64, cint, vp, vp, vp, vp]),

@@ -677,6 +677,31 @@ class Function:
         return float(self.tape.d[k])
 
 
+def _sorted_nodes(outputs):
+    """Depth-first topological order of the nodes that the outputs depend on, with a None
+    marker after each output nonzero (sort_depth_first, x_function.hpp:411-438)."""
+    temp = {}  # node -> SXNode::temp during the sort
+    nodes = []
+    for vec in outputs:
+        for e in vec:
+            s = [e]
+            while s:
+                t = s[-1]
+                tt = temp.get(t, 0)
+                if tt >= 0:
+                    temp[t] = tt + 1
+                    if tt < t.n_dep():
+                        s.append(t.dep(tt))
+                    else:
+                        nodes.append(t)
+                        temp[t] = -1
+                        s.pop()
+                else:
+                    s.pop()
+            nodes.append(None)
+    return nodes
+
+
 def _build_tape(inputs, outputs, live_variables=True):
     temp = {}  # node -> SXNode::temp during the sort
 
@@ -776,3 +801,152 @@ def _build_tape(inputs, outputs, live_variables=True):
     d = np.array([a[4] for a in alg], dtype=np.float64)
     return Tape(arr[:, 0], arr[:, 1], arr[:, 2], arr[:, 3], d,
                 [len(v) for v in inputs], [len(v) for v in outputs], worksize)
+
+
+# ---- symbolic reverse mode (SXFunction::ad_reverse, sx_function.cpp:1368-1569) ----------------
+def _der_sx(op, x, y, f):
+    """Symbolic partials (d0, d1) of op at operands x, y with result f, as
+    BinaryOperation<OP>::der / UnaryOperation<OP>::der write them (calculus.hpp:598-1018)."""
+    one, zero = const(1.0), const(0.0)
+    if op in (C.OP_ASSIGN, C.OP_PRINTME, C.OP_LIFT):
+        return one, zero
+    if op == C.OP_ADD:
+        return one, one
+    if op == C.OP_SUB:
+        return one, const(-1.0)
+    if op == C.OP_MUL:
+        return y, x
+    if op == C.OP_DIV:
+        return one / y, -f / y
+    if op == C.OP_NEG:
+        return const(-1.0), zero
+    if op == C.OP_EXP:
+        return f, zero
+    if op == C.OP_LOG:
+        return one / x, zero
+    if op == C.OP_POW:
+        return y * power(x, y - one), log(x) * f
+    if op == C.OP_CONSTPOW:
+        return y * power(x, y - one), zero
+    if op == C.OP_SQRT:
+        return one / twice(f), zero
+    if op == C.OP_SQ:
+        return twice(x), zero
+    if op == C.OP_TWICE:
+        return const(2.0), zero
+    if op == C.OP_SIN:
+        return cos(x), zero
+    if op == C.OP_COS:
+        return -sin(x), zero
+    if op == C.OP_TAN:
+        return one / sq(cos(x)), zero
+    if op == C.OP_ASIN:
+        return one / sqrt(one - x * x), zero
+    if op == C.OP_ACOS:
+        return const(-1.0) / sqrt(one - x * x), zero
+    if op == C.OP_ATAN:
+        return one / (one + x * x), zero
+    if op in (C.OP_LT, C.OP_LE, C.OP_EQ, C.OP_NE, C.OP_AND, C.OP_OR):
+        return zero, zero
+    if op in (C.OP_FLOOR, C.OP_CEIL, C.OP_NOT, C.OP_SIGN):
+        return zero, zero
+    if op in (C.OP_FMOD, C.OP_REMAINDER):
+        return one, (f - x) / y
+    if op == C.OP_ERF:
+        return const(2.0 / math.sqrt(math.pi)) * exp(-x * x), zero
+    if op == C.OP_FABS:
+        return sign(x), zero
+    if op == C.OP_COPYSIGN:
+        return copysign(one, y), zero
+    if op == C.OP_FMIN:
+        a, b = x <= y, y <= x
+        c = a + b
+        return a / c, b / c
+    if op == C.OP_FMAX:
+        a, b = y <= x, x <= y
+        c = a + b
+        return a / c, b / c
+    if op == C.OP_INV:
+        return (-f) * f, zero
+    if op == C.OP_SINH:
+        return cosh(x), zero
+    if op == C.OP_COSH:
+        return sinh(x), zero
+    if op == C.OP_TANH:
+        return one - f * f, zero
+    if op == C.OP_ASINH:
+        return one / sqrt(one + x * x), zero
+    if op == C.OP_ACOSH:
+        return one / sqrt(x - one) / sqrt(x + one), zero
+    if op == C.OP_ATANH:
+        return one / (one - x * x), zero
+    if op == C.OP_ERFINV:
+        return const(math.sqrt(math.pi) / 2) * exp(f * f), zero
+    if op == C.OP_LOG1P:
+        return one / (one + x), zero
+    if op == C.OP_EXPM1:
+        return exp(x), zero
+    if op == C.OP_ATAN2:
+        t = x * x + y * y
+        return y / t, -x / t
+    if op == C.OP_IF_ELSE_ZERO:
+        return zero, x
+    if op == C.OP_HYPOT:
+        return x / f, y / f
+    raise ValueError("no symbolic derivative for op %s" % C.OP_NAMES.get(op, op))
+
+
+def reverse(f, aseed):
+    """Adjoint sensitivity expressions of Function ``f`` for one adjoint direction:
+    ``aseed[j]`` gives the seed of every nonzero of output j (numbers or SXElem; None for
+    an unseeded output). Returns one list of SXElem per input. Follows SXFunction::ad_reverse:
+    symbolic partials of every operation in tape order, then a reverse sweep in which each
+    operation passes d0*seed and d1*seed to its operands (if_else_zero(d1, seed) for
+    IF_ELSE_ZERO) and the simplification rules drop structural zeros."""
+    outputs = f.outputs
+    nodes = _sorted_nodes(outputs)
+    der = {}
+    for n in nodes:
+        if n is None or n.is_constant() or n.is_symbolic():
+            continue
+        if n not in der:
+            der[n] = _der_sx(n.op, n.dep0, n.dep1 if n._kind == "b" else n.dep0, n)
+    zero = const(0.0)
+    w = {}
+    out_pos = [(oi, nz) for oi, vec in enumerate(outputs) for nz in range(len(vec))]
+    k_out = len(out_pos)
+    sens_of = {}
+    for n in reversed(nodes):
+        if n is None:
+            k_out -= 1
+            oi, nz = out_pos[k_out]
+            s = aseed[oi]
+            if s is None:
+                continue
+            node = outputs[oi][nz]
+            w[node] = w.get(node, zero) + _sx(s[nz])
+            continue
+        if n.is_constant():
+            w.pop(n, None)
+            continue
+        if n.is_symbolic():
+            sens_of[n] = w.pop(n, zero)
+            continue
+        seed = w.pop(n, zero)
+        d0, d1 = der[n]
+        if n.op == C.OP_IF_ELSE_ZERO:
+            w[n.dep1] = w.get(n.dep1, zero) + if_else_zero(d1, seed)
+        elif n._kind == "b":
+            w[n.dep0] = w.get(n.dep0, zero) + d0 * seed
+            w[n.dep1] = w.get(n.dep1, zero) + d1 * seed
+        else:
+            w[n.dep0] = w.get(n.dep0, zero) + d0 * seed
+    return [[sens_of.get(e, zero) for e in vec] for vec in f.inputs]
+
+
+def gradient(f, out, wrt):
+    """Gradient expressions of the scalar output ``out`` of ``f`` with respect to input
+    ``wrt``: one adjoint sweep seeded with 1 on that output."""
+    seeds = [None] * f.n_out()
+    seeds[out] = [1.0] * len(f.outputs[out])
+    return reverse(f, seeds)[wrt]

@@ -171,6 +171,13 @@ def quad_ode(x, u, p=QUAD):
     return [x[3], x[4], x[5], ax, ay, az, dphi, dth, dpsi, dp, dq, dr]
 
 
+def quad_ms_constraints(intervals=100):
+    """The constraints of :func:`quad_ms_lagrangian` alone: ``g(w, lam, x0bar)`` (``lam`` is
+    unused; same inputs so the same scenario arrays serve both)."""
+    L = quad_ms_lagrangian(intervals)
+    return S.Function("g", L.inputs, [L.outputs[0]])
+
+
 def quad_ms_lagrangian(intervals=100):
     """Multiple-shooting NLP pieces: decision vector w = (x_0, u_0, ..., x_{K-1}, u_{K-1},
     x_K) with 12 + 4 variables per interval, constraints g_k = F(x_k, u_k) - x_{k+1}
@@ -194,3 +201,29 @@ def quad_ms_lagrangian(intervals=100):
     for i, gi in enumerate(g):
         lag = lag + lam[i] * gi
     return S.Function("L", [w, lam, x0bar], [g, [lag]])
+
+
+def quad_ms_inputs(n, intervals=100, seed=0):
+    """Scenario inputs of :func:`quad_ms_lagrangian` for n instances (instance-minor):
+    initial states with positions ~ U(-1, 1) m and angles ~ U(-0.5, 0.5) rad (velocities and
+    rates zero); the decision vector perturbs that state along the horizon (positions
+    U(-1, 1), velocities U(-0.5, 0.5), angles U(-0.5, 0.5), rates U(-0.5, 0.5); thrust
+    m*g + U(-1, 1), torques U(-0.05, 0.05)); multipliers ~ N(0, 1)."""
+    rng = np.random.default_rng(seed)
+    nx, nu, K = 12, 4, intervals
+    lo_x = np.array([-1, -1, -1, -.5, -.5, -.5, -.5, -.5, -.5, -.5, -.5, -.5])
+    hi_x = -lo_x
+    x0 = np.zeros((nx, n))
+    x0[0:3] = rng.uniform(-1, 1, (3, n))
+    x0[6:9] = rng.uniform(-0.5, 0.5, (3, n))
+    w = np.empty((K * (nx + nu) + nx, n))
+    hover = QUAD["m"] * QUAD["g"]
+    for k in range(K + 1):
+        o = k * (nx + nu)
+        w[o:o + nx] = rng.uniform(lo_x[:, None], hi_x[:, None], (nx, n))
+        if k < K:
+            w[o + nx] = hover + rng.uniform(-1, 1, n)
+            w[o + nx + 1:o + nx + nu] = rng.uniform(-0.05, 0.05, (nu - 1, n))
+    lam = rng.standard_normal(((K + 1) * nx, n))
+    return [w, lam, x0]
+

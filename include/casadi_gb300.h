@@ -209,6 +209,40 @@ CASADI_GB300_API int casadi_gb300_tuned_variant(int id, int kind, int* variant);
  * for retuning (-1). */
 CASADI_GB300_API int casadi_gb300_set_variant(int id, int kind, int variant);
 
+/* Colour-compressed Jacobian: n_colors forward directions, direction d seeded with 1 on
+ * every flat input nonzero k with color[k] == d (color: one entry per nonzero of all inputs
+ * in order, -1 = not seeded). comp[j] receives the compressed block of output j, direction-
+ * major as fsens in casadi_gb300_forward. Structural activity is computed per direction, so
+ * a direction walks only the instructions its seeded inputs reach. Replaces the forward
+ * seeding of the reference's coloured jacobian (FunctionInternal::get_partition,
+ * casadi/core/function_internal.cpp:2068-2160, and XFunction::jac,
+ * casadi/core/x_function.hpp:441-840). */
+CASADI_GB300_API int casadi_gb300_jacobian_colored(int id, int64_t n, int64_t ld,
+                           int n_colors, const int* color, const double* const* arg,
+                           double* const* res, double* const* comp, void* scratch,
+                           size_t scratch_bytes, void* stream);
+
+/* Row gather on the device: dst[e*ld + i] = src[src_row[e]*ld + i] for e < count, i < n
+ * (src_row a device array). Recovers sparse Jacobian/Hessian nonzeros from colour-compressed
+ * blocks; replaces the reference's scatter of compressed results into nonzeros
+ * (casadi/core/x_function.hpp:702-826). */
+CASADI_GB300_API int casadi_gb300_gather(int64_t n, int64_t ld, int count,
+                                         const int64_t* src_row, const double* src,
+                                         double* dst, void* stream);
+
+/* Seed colourings for compressed Jacobians and Hessians (host only, no device). Patterns
+ * are compressed-column arrays with sorted rows (CasADi's Sparsity layout). Both write one
+ * colour per column and return the number of colours (or a negative status).
+ *   uni_coloring: columns of one colour share no row (forward-mode seeds of a Jacobian);
+ *     restates SparsityInternal::uni_coloring (casadi/core/sparsity_internal.cpp:2959-3045).
+ *   star_coloring: star colouring of a symmetric pattern (Hessian seeds), ordering 1 =
+ *     largest-first (the reference's default), 0 = index order; restates
+ *     SparsityInternal::star_coloring and ::largest_first (:3398-3509, :3511-3545). */
+CASADI_GB300_API int casadi_gb300_uni_coloring(int nrow, int ncol, const int* colind,
+                                               const int* row, int* color);
+CASADI_GB300_API int casadi_gb300_star_coloring(int n, const int* colind, const int* row,
+                                                int ordering, int* color);
+
 /* Persistent multi-tape batches. A batch is a list of items, each one tape over its own
  * instance range (device pointers, instance-minor layout as above): nadj == 0 runs the value
  * sweep, nadj > 0 the value sweep plus nadj adjoint directions (aseed/asens as in

@@ -1,0 +1,78 @@
+"""Colour-compressed sparse Jacobians and Hessians (coloured forward sweeps + device
+gather) on the multiple-shooting quadcopter NLP: the constraint Jacobian against the dense
+unit-seed Jacobian of the same tape (same bits) and the oracle, the Lagrangian Hessian
+against the oracle's dense Jacobian of the same symbolic gradient, against central
+differences of the oracle's adjoint, and its symmetry."""
+import numpy as np
+import pytest
+
+import oracle as O
+from casadi_gb300 import workloads as W
+
+from helpers import RTOL, assert_close, same_bits
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+INTERVALS = 3
+
+
+def _inputs(n, seed=0):
+    return W.quad_ms_inputs(n, intervals=INTERVALS, seed=seed)
+
+
+def test_colored_constraint_jacobian(gpu_lib):
+    from casadi_gb300.sparse_ad import ColoredJacobian
+    F = W.quad_ms_constraints(INTERVALS)
+    n = 333
+    args = _inputs(n, 1)
+    J = ColoredJacobian(F, out=0, wrt=0)
+    nw = F.tape.nnz_in[0]
+    assert J.n_colors < nw / 4  # the coloring compresses the 12+4 per interval band
+    vals = J([torch.from_numpy(a).cuda() for a in args]).cpu().numpy()
+    rows, cols = J.pattern.row, J.pattern.col()
+    # dense unit-seed Jacobian of the same tape: jac[0] has shape (nnz_in_total, nnz_g, n)
+    _, jac = J.tape.jacobian([torch.from_numpy(a).cuda() for a in args])
+    dense = jac[0].cpu().numpy()[:nw]  # rows: w nonzeros
+    assert same_bits(vals, dense[cols, rows]).all()
+    # and every entry outside the pattern is zero
+    mask = np.ones((nw, dense.shape[1]), bool)
+    mask[cols, rows] = False
+    assert not np.any(dense[mask])
+    _, wjac = O.jacobian(F.tape, args, n)
+    assert_close(vals, wjac[0][cols, rows], "colored constraint Jacobian", rtol=RTOL)
+
+
+def test_colored_lagrangian_hessian(gpu_lib):
+    from casadi_gb300.sparse_ad import ColoredHessian
+    F = W.quad_ms_lagrangian(INTERVALS)
+    n = 257
+    args = _inputs(n, 2)
+    H = ColoredHessian(F, out=1, wrt=0)
+    nw = F.tape.nnz_in[0]
+    assert H.n_colors < nw / 3
+    vals = H([torch.from_numpy(a).cuda() for a in args]).cpu().numpy()
+    # oracle: dense Jacobian of the same gradient tape
+    G = H.gradient_function
+    _, gj = O.jacobian(G.tape, args, n)
+    dense = gj[0][:nw]  # [w nonzero j][gradient entry i][instance] = H[i, j]
+    assert_close(vals, dense[H.cols, H.rows], "colored Hessian vs oracle", rtol=1e-12)
+    # symmetric: H[i, j] == H[j, i] in the oracle's dense Hessian
+    assert_close(dense[H.rows, H.cols], dense[H.cols, H.rows], "symmetry", rtol=1e-12)
+    # central differences of the oracle's adjoint (gradient of the Lagrangian) on 3 instances
+    m, h = 3, 1e-6
+    Hd = np.zeros((nw, nw, m))
+    Hd[H.rows, H.cols] = vals[:, :m]
+    Hd[H.cols, H.rows] = vals[:, :m]
+    sub = [a[:, :m].copy() for a in args]
+    seeds = [np.zeros((1, k, m)) for k in F.tape.nnz_out]
+    seeds[1][:] = 1.0
+    for j in (0, 5, 12, 20, nw - 13):
+        p = [a.copy() for a in sub]
+        q = [a.copy() for a in sub]
+        p[0][j] += h
+        q[0][j] -= h
+        gp = O.reverse(F.tape, p, seeds, m)[1][0][0]
+        gq = O.reverse(F.tape, q, seeds, m)[1][0][0]
+        col = (gp - gq) / (2 * h)  # column j of H, (nw, m)
+        assert np.max(np.abs(Hd[:, j] - col) / np.maximum(np.abs(col), 1.0)) < 1e-5
