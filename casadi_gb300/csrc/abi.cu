@@ -1610,7 +1610,9 @@ struct BatchHost {
     int tape;
     long long n;
     int ndir;
-    std::vector<IoDesc> io;  // 4*kMaxIo
+    bool forward = false;
+    std::vector<int> dirmap;  // forward items: direction of each flat input nonzero (-1: none)
+    std::vector<IoDesc> io;   // 4*kMaxIo
   };
   std::vector<Item> items;
   bool dirty = true;
@@ -1675,7 +1677,18 @@ int batch_prepare(BatchHost& b) {
     bi.n_code = t->n_chunks * kChunk;
     bi.ndir = it.ndir;
     bi.n = it.n;
-    if (it.ndir > 0) {
+    bi.forward = it.forward ? 1 : 0;
+    if (it.ndir > 0 && it.forward) {
+      if (static_cast<unsigned>(t->n_partials) >= kMaxPartials)
+        return fail(CASADI_GB300_ERR_UNSUPPORTED, "batch item %zu records too many partials", k);
+      int err = 0;
+      const TanPlan* tp = tan_plan(*t, it.ndir, 1, 0, true, std::vector<char>(t->n_in, 0),
+                                   it.dirmap, &err);
+      if (!tp) return err;
+      bi.tan_stream = tp->d_stream;
+      bi.tan_chunks = tp->d_chunks;
+      b.pmax = std::max(b.pmax, t->n_partials);
+    } else if (it.ndir > 0) {
       if (static_cast<unsigned>(t->n_partials) >= kMaxPartials)
         return fail(CASADI_GB300_ERR_UNSUPPORTED, "batch item %zu records too many partials", k);
       std::vector<char> seeded(t->n_out);
@@ -1785,6 +1798,39 @@ int casadi_gb300_batch_add(int batch, int id, int64_t n, int64_t ld, int nadj,
     fill_io(it.io.data() + 2 * kMaxIo, t->n_out, vptrs(aseed), t->nnz_out, ld, true);
     fill_io(it.io.data() + 3 * kMaxIo, t->n_in, vptrs(asens), t->nnz_in, ld, true);
   }
+  b->items.push_back(std::move(it));
+  b->dirty = true;
+  return static_cast<int>(b->items.size()) - 1;
+}
+
+int casadi_gb300_batch_add_jacobian_colored(int batch, int id, int64_t n, int64_t ld,
+                                            int n_colors, const int* color,
+                                            const double* const* arg, double* const* res,
+                                            double* const* comp) {
+  BatchHost* b = get_batch(batch);
+  if (!b) return fail(CASADI_GB300_ERR_ID, "no batch %d", batch);
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  if (int rc = check_device(*t)) return rc;
+  if (int rc = check_n(n, ld)) return rc;
+  if (n > (1ll << 36)) return fail(CASADI_GB300_ERR_ARG, "too many instances");
+  int nz = 0;
+  for (int v : t->nnz_in) nz += v;
+  if (!color || n_colors < 1 || n_colors > nz)
+    return fail(CASADI_GB300_ERR_ARG, "bad colouring (%d colours for %d input nonzeros)",
+                n_colors, nz);
+  BatchHost::Item it;
+  it.tape = id;
+  it.n = n;
+  it.ndir = n_colors;
+  it.forward = true;
+  it.dirmap.assign(color, color + nz);
+  for (int v : it.dirmap)
+    if (v < -1 || v >= n_colors) return fail(CASADI_GB300_ERR_ARG, "colour %d out of range", v);
+  it.io.assign(4 * kMaxIo, IoDesc{nullptr, 0, 0, 0});
+  fill_io(it.io.data(), t->n_in, vptrs(arg), t->nnz_in, ld, false);
+  fill_io(it.io.data() + kMaxIo, t->n_out, vptrs(res), t->nnz_out, ld, false);
+  fill_io(it.io.data() + 3 * kMaxIo, t->n_out, vptrs(comp), t->nnz_out, ld, true);
   b->items.push_back(std::move(it));
   b->dirty = true;
   return static_cast<int>(b->items.size()) - 1;

@@ -484,6 +484,164 @@ __device__ __forceinline__ void load_partials_n(const uint4 (&E)[G], const doubl
   }
 }
 
+// Tangent entries of K > 1 directions: x bits 0-18 hold the destination (see k_tangent).
+constexpr unsigned kTanXMask = (1u << 19) - 1;
+
+// One tangent sweep by one warp over its entry stream st (ngr groups of G): IPT tiles (tile j's
+// partials at pt + j*tstride), K directions dir0.. (the union stream of the K directions).
+template <bool kNC, int G, int IPT, int K>
+__device__ __forceinline__ void tangent_walk(const uint4* st, int ngr, const double* pt,
+                                             size_t tstride, const bool (&tok)[IPT],
+                                             unsigned char* wb, const IoDesc* seed,
+                                             const IoDesc* sens, bool identity,
+                                             const bool (&active)[IPT], int dir0, int ndir,
+                                             const long long (&ig)[IPT]) {
+  uint4 E0[G], E1[G];
+  double P0[G][IPT], Q0[G][IPT];
+  load_group<G>(st, 0, ngr, E0);
+  load_group<G>(st, 1, ngr, E1);
+  load_partials_n<kNC, false, G, IPT>(E0, pt, tstride, tok, P0, Q0);
+#pragma unroll 1
+  for (int g = 0; g < ngr; ++g) {
+    uint4 E2[G];
+    double P1[G][IPT], Q1[G][IPT];
+    load_group<G>(st, g + 2, ngr, E2);
+    load_partials_n<kNC, false, G, IPT>(E1, pt, tstride, tok, P1, Q1);
+#pragma unroll
+    for (int i = 0; i < G; ++i) {
+      const uint4 cur = E0[i];
+      const unsigned meta = cur.w;
+      const unsigned xo = K > 1 ? (cur.x & kTanXMask) : cur.x;
+#define CGB_W(off, j, k) wj<IPT * K>(wb, (off), (j) * K + (k))
+#define CGB_JK _Pragma("unroll") for (int j = 0; j < IPT; ++j) _Pragma("unroll") for (int k = 0; k < K; ++k)
+// tangent of one arithmetic entry (kind and flags in `key`) for tile j, direction k
+#define CGB_TAN_CASES(R, j, k)                                                               \
+case (LK_GEN << 2) | 1u: R = __dmul_rn(P0[i][j], CGB_W(cur.y, j, k)); break;               \
+case (LK_GEN << 2) | 2u: R = __dmul_rn(Q0[i][j], CGB_W(cur.z, j, k)); break;               \
+case (LK_GEN << 2) | 3u:                                                                   \
+  R = __dadd_rn(__dmul_rn(P0[i][j], CGB_W(cur.y, j, k)), __dmul_rn(Q0[i][j], CGB_W(cur.z, j, k))); \
+  break;                                                                                   \
+case (LK_ADD << 2) | 1u: R = CGB_W(cur.y, j, k); break;                                    \
+case (LK_ADD << 2) | 2u: R = CGB_W(cur.z, j, k); break;                                    \
+case (LK_ADD << 2) | 3u: R = __dadd_rn(CGB_W(cur.y, j, k), CGB_W(cur.z, j, k)); break;     \
+case (LK_SUB << 2) | 1u: R = CGB_W(cur.y, j, k); break;                                    \
+case (LK_SUB << 2) | 2u: R = d_neg(CGB_W(cur.z, j, k)); break;                             \
+case (LK_SUB << 2) | 3u: R = __dsub_rn(CGB_W(cur.y, j, k), CGB_W(cur.z, j, k)); break;     \
+case (LK_NEG << 2) | 1u: R = d_neg(CGB_W(cur.y, j, k)); break;                             \
+case (LK_TWICE << 2) | 1u: {                                                               \
+  const double xb = CGB_W(cur.y, j, k);                                                    \
+  R = __dadd_rn(xb, xb);                                                                   \
+} break;                                                                                   \
+case (LK_ASSIGN << 2) | 1u: R = CGB_W(cur.y, j, k); break;                                 \
+case (LK_IFZ << 2) | 2u: R = d_iszero(Q0[i][j]) ? 0.0 : CGB_W(cur.z, j, k); break;
+      // one jump-table dispatch on (kind, active operands): every case holds only the FP64
+      // operations it needs, so nothing is computed speculatively (an FP64 instruction holds
+      // a sub-partition's FP64 unit for ~64 cycles on GB300)
+      const unsigned key = (ent_kind(meta) << 2) | (ent_flags(meta) & 3u);
+      double r[IPT][K];
+      switch (key) {
+        case (LK_OUTPUT << 2) | 0u:
+        case (LK_OUTPUT << 2) | 1u: {
+          const IoDesc& d = sens[xo];
+          CGB_JK {
+            if (dir0 + k < ndir && active[j] && d.ptr)
+              static_cast<double*>(d.ptr)[io_off(d, dir0 + k, cur.z, ig[j])] =
+                  (meta & 1u) ? CGB_W(cur.y, j, k) : 0.0;
+          }
+          continue;
+        }
+        case (LK_INPUT << 2) | 1u:
+          if (identity) {
+            CGB_JK r[j][k] = 1.0;
+          } else {
+            const IoDesc& d = seed[cur.y];
+            CGB_JK r[j][k] = (active[j] && dir0 + k < ndir)
+                ? __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir0 + k, cur.z, ig[j]))
+                : 0.0;
+          }
+          break;
+#define CGB_UNIFORM(KEY) \
+case KEY: {            \
+  CGB_JK switch (KEY) { CGB_TAN_CASES(r[j][k], j, k) default: break; } \
+} break;
+        CGB_UNIFORM((LK_GEN << 2) | 1u)
+        CGB_UNIFORM((LK_GEN << 2) | 2u)
+        CGB_UNIFORM((LK_GEN << 2) | 3u)
+        CGB_UNIFORM((LK_ADD << 2) | 1u)
+        CGB_UNIFORM((LK_ADD << 2) | 2u)
+        CGB_UNIFORM((LK_ADD << 2) | 3u)
+        CGB_UNIFORM((LK_SUB << 2) | 1u)
+        CGB_UNIFORM((LK_SUB << 2) | 2u)
+        CGB_UNIFORM((LK_SUB << 2) | 3u)
+        CGB_UNIFORM((LK_NEG << 2) | 1u)
+        CGB_UNIFORM((LK_TWICE << 2) | 1u)
+        CGB_UNIFORM((LK_ASSIGN << 2) | 1u)
+        CGB_UNIFORM((LK_IFZ << 2) | 2u)
+#undef CGB_UNIFORM
+        case (LK_MIXED << 2): {
+          if (K == 1) continue;
+          // directions of the group differ: one dispatch per direction
+          const unsigned rk = (cur.x >> 19) & 15u;
+#pragma unroll
+          for (int k = 0; k < K; ++k) {
+            const unsigned fk = (cur.x >> (24 + 2 * k)) & 3u;
+            if (rk == LK_OUTPUT) {
+              const IoDesc& d = sens[xo];
+#pragma unroll
+              for (int j = 0; j < IPT; ++j)
+                if (dir0 + k < ndir && active[j] && d.ptr)
+                  static_cast<double*>(d.ptr)[io_off(d, dir0 + k, cur.z, ig[j])] =
+                      (fk & 1u) ? CGB_W(cur.y, j, k) : 0.0;
+              continue;
+            }
+            if (!fk) continue;
+            if (rk == LK_INPUT) {
+#pragma unroll
+              for (int j = 0; j < IPT; ++j) {
+                double v = 1.0;
+                if (!identity) {
+                  const IoDesc& d = seed[cur.y];
+                  v = (active[j] && dir0 + k < ndir)
+                      ? __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir0 + k, cur.z, ig[j]))
+                      : 0.0;
+                }
+                CGB_W(xo, j, k) = v;
+              }
+              continue;
+            }
+#pragma unroll
+            for (int j = 0; j < IPT; ++j) {
+              double rr = 0.0;
+              switch ((rk << 2) | fk) {
+                CGB_TAN_CASES(rr, j, k)
+                default: break;
+              }
+              CGB_W(xo, j, k) = rr;
+            }
+          }
+          continue;
+        }
+        default:
+          continue;  // NOP padding
+      }
+      CGB_JK CGB_W(xo, j, k) = r[j][k];
+#undef CGB_TAN_CASES
+#undef CGB_JK
+#undef CGB_W
+    }
+#pragma unroll
+    for (int i = 0; i < G; ++i) {
+      E0[i] = E1[i];
+      E1[i] = E2[i];
+#pragma unroll
+      for (int j = 0; j < IPT; ++j) {
+        P0[i][j] = P1[i][j];
+        Q0[i][j] = Q1[i][j];
+      }
+    }
+  }
+}
+
 // Tangent sweep. A warp takes one work item (IPT tiles, K directions): the work vector holds
 // IPT*K values per slot and lane, w[slot][j*K + k][lane]. With K > 1 the warp walks the
 // union stream of its K directions: recorded partials and entries are loaded once for all K,
@@ -491,7 +649,6 @@ __device__ __forceinline__ void load_partials_n(const uint4 (&E)[G], const doubl
 // every direction of the group is dispatched once ("uniform"); otherwise its kind is
 // LK_MIXED and x carries the real kind (bits 19-22) and the flags of direction k (bits
 // 24+2k, 25+2k), handled one direction at a time.
-constexpr unsigned kTanXMask = (1u << 19) - 1;
 
 template <int G, int MB, int IPT, int K>
 __global__ void __launch_bounds__(32, MB) k_tangent(const __grid_constant__ SweepArgs a) {
@@ -520,150 +677,8 @@ __global__ void __launch_bounds__(32, MB) k_tangent(const __grid_constant__ Swee
     const uint4* st = a.dstream + se.x;
     const int ngr = se.y / G;
     const double* pt = a.partials + static_cast<size_t>(tg * IPT) * tstride + lane;
-    uint4 E0[G], E1[G];
-    double P0[G][IPT], Q0[G][IPT];
-    load_group<G>(st, 0, ngr, E0);
-    load_group<G>(st, 1, ngr, E1);
-    load_partials_n<true, false, G, IPT>(E0, pt, tstride, tok, P0, Q0);
-#pragma unroll 1
-    for (int g = 0; g < ngr; ++g) {
-      uint4 E2[G];
-      double P1[G][IPT], Q1[G][IPT];
-      load_group<G>(st, g + 2, ngr, E2);
-      load_partials_n<true, false, G, IPT>(E1, pt, tstride, tok, P1, Q1);
-#pragma unroll
-      for (int i = 0; i < G; ++i) {
-        const uint4 cur = E0[i];
-        const unsigned meta = cur.w;
-        const unsigned xo = K > 1 ? (cur.x & kTanXMask) : cur.x;
-#define CGB_W(off, j, k) wj<IPT * K>(wb, (off), (j) * K + (k))
-#define CGB_JK _Pragma("unroll") for (int j = 0; j < IPT; ++j) _Pragma("unroll") for (int k = 0; k < K; ++k)
-// tangent of one arithmetic entry (kind and flags in `key`) for tile j, direction k
-#define CGB_TAN_CASES(R, j, k)                                                               \
-  case (LK_GEN << 2) | 1u: R = __dmul_rn(P0[i][j], CGB_W(cur.y, j, k)); break;               \
-  case (LK_GEN << 2) | 2u: R = __dmul_rn(Q0[i][j], CGB_W(cur.z, j, k)); break;               \
-  case (LK_GEN << 2) | 3u:                                                                   \
-    R = __dadd_rn(__dmul_rn(P0[i][j], CGB_W(cur.y, j, k)), __dmul_rn(Q0[i][j], CGB_W(cur.z, j, k))); \
-    break;                                                                                   \
-  case (LK_ADD << 2) | 1u: R = CGB_W(cur.y, j, k); break;                                    \
-  case (LK_ADD << 2) | 2u: R = CGB_W(cur.z, j, k); break;                                    \
-  case (LK_ADD << 2) | 3u: R = __dadd_rn(CGB_W(cur.y, j, k), CGB_W(cur.z, j, k)); break;     \
-  case (LK_SUB << 2) | 1u: R = CGB_W(cur.y, j, k); break;                                    \
-  case (LK_SUB << 2) | 2u: R = d_neg(CGB_W(cur.z, j, k)); break;                             \
-  case (LK_SUB << 2) | 3u: R = __dsub_rn(CGB_W(cur.y, j, k), CGB_W(cur.z, j, k)); break;     \
-  case (LK_NEG << 2) | 1u: R = d_neg(CGB_W(cur.y, j, k)); break;                             \
-  case (LK_TWICE << 2) | 1u: {                                                               \
-    const double xb = CGB_W(cur.y, j, k);                                                    \
-    R = __dadd_rn(xb, xb);                                                                   \
-  } break;                                                                                   \
-  case (LK_ASSIGN << 2) | 1u: R = CGB_W(cur.y, j, k); break;                                 \
-  case (LK_IFZ << 2) | 2u: R = d_iszero(Q0[i][j]) ? 0.0 : CGB_W(cur.z, j, k); break;
-        // one jump-table dispatch on (kind, active operands): every case holds only the FP64
-        // operations it needs, so nothing is computed speculatively (an FP64 instruction holds
-        // a sub-partition's FP64 unit for ~64 cycles on GB300)
-        const unsigned key = (ent_kind(meta) << 2) | (ent_flags(meta) & 3u);
-        double r[IPT][K];
-        switch (key) {
-          case (LK_OUTPUT << 2) | 0u:
-          case (LK_OUTPUT << 2) | 1u: {
-            const IoDesc& d = a.sens[xo];
-            CGB_JK {
-              if (dir0 + k < a.ndir && active[j] && d.ptr)
-                static_cast<double*>(d.ptr)[io_off(d, dir0 + k, cur.z, ig[j])] =
-                    (meta & 1u) ? CGB_W(cur.y, j, k) : 0.0;
-            }
-            continue;
-          }
-          case (LK_INPUT << 2) | 1u:
-            if (a.identity_seed) {
-              CGB_JK r[j][k] = 1.0;
-            } else {
-              const IoDesc& d = a.seed[cur.y];
-              CGB_JK r[j][k] = (active[j] && dir0 + k < a.ndir)
-                  ? __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir0 + k, cur.z, ig[j]))
-                  : 0.0;
-            }
-            break;
-#define CGB_UNIFORM(KEY) \
-  case KEY: {            \
-    CGB_JK switch (KEY) { CGB_TAN_CASES(r[j][k], j, k) default: break; } \
-  } break;
-          CGB_UNIFORM((LK_GEN << 2) | 1u)
-          CGB_UNIFORM((LK_GEN << 2) | 2u)
-          CGB_UNIFORM((LK_GEN << 2) | 3u)
-          CGB_UNIFORM((LK_ADD << 2) | 1u)
-          CGB_UNIFORM((LK_ADD << 2) | 2u)
-          CGB_UNIFORM((LK_ADD << 2) | 3u)
-          CGB_UNIFORM((LK_SUB << 2) | 1u)
-          CGB_UNIFORM((LK_SUB << 2) | 2u)
-          CGB_UNIFORM((LK_SUB << 2) | 3u)
-          CGB_UNIFORM((LK_NEG << 2) | 1u)
-          CGB_UNIFORM((LK_TWICE << 2) | 1u)
-          CGB_UNIFORM((LK_ASSIGN << 2) | 1u)
-          CGB_UNIFORM((LK_IFZ << 2) | 2u)
-#undef CGB_UNIFORM
-          case (LK_MIXED << 2): {
-            if (K == 1) continue;
-            // directions of the group differ: one dispatch per direction
-            const unsigned rk = (cur.x >> 19) & 15u;
-#pragma unroll
-            for (int k = 0; k < K; ++k) {
-              const unsigned fk = (cur.x >> (24 + 2 * k)) & 3u;
-              if (rk == LK_OUTPUT) {
-                const IoDesc& d = a.sens[xo];
-#pragma unroll
-                for (int j = 0; j < IPT; ++j)
-                  if (dir0 + k < a.ndir && active[j] && d.ptr)
-                    static_cast<double*>(d.ptr)[io_off(d, dir0 + k, cur.z, ig[j])] =
-                        (fk & 1u) ? CGB_W(cur.y, j, k) : 0.0;
-                continue;
-              }
-              if (!fk) continue;
-              if (rk == LK_INPUT) {
-#pragma unroll
-                for (int j = 0; j < IPT; ++j) {
-                  double v = 1.0;
-                  if (!a.identity_seed) {
-                    const IoDesc& d = a.seed[cur.y];
-                    v = (active[j] && dir0 + k < a.ndir)
-                        ? __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir0 + k, cur.z, ig[j]))
-                        : 0.0;
-                  }
-                  CGB_W(xo, j, k) = v;
-                }
-                continue;
-              }
-#pragma unroll
-              for (int j = 0; j < IPT; ++j) {
-                double rr = 0.0;
-                switch ((rk << 2) | fk) {
-                  CGB_TAN_CASES(rr, j, k)
-                  default: break;
-                }
-                CGB_W(xo, j, k) = rr;
-              }
-            }
-            continue;
-          }
-          default:
-            continue;  // NOP padding
-        }
-        CGB_JK CGB_W(xo, j, k) = r[j][k];
-#undef CGB_TAN_CASES
-#undef CGB_JK
-#undef CGB_W
-      }
-#pragma unroll
-      for (int i = 0; i < G; ++i) {
-        E0[i] = E1[i];
-        E1[i] = E2[i];
-#pragma unroll
-        for (int j = 0; j < IPT; ++j) {
-          P0[i][j] = P1[i][j];
-          Q0[i][j] = Q1[i][j];
-        }
-      }
-    }
+    tangent_walk<true, G, IPT, K>(st, ngr, pt, tstride, tok, wb, a.seed, a.sens,
+                                  a.identity_seed != 0, active, dir0, a.ndir, ig);
   }
 }
 
@@ -855,9 +870,10 @@ __global__ void __launch_bounds__(32, MB) k_adjoint(const __grid_constant__ Swee
 // ---------------------------------------------------------------------------------------------
 // Persistent multi-tape batch: one launch drains a host-built list of work units
 // (item, 32-instance tile), longest first, through an atomic counter. An item is one tape over
-// its own instance range, either a value sweep or a value+adjoint sweep. Each one-warp CTA
-// grabs a unit, runs the warp-level value (or record) walk for its tile and, for adjoint items,
-// the adjoint walk of every direction, then grabs the next unit. Tapes of any length and
+// its own instance range: a value sweep, a value + adjoint sweep, or a value + tangent sweep
+// with identity (or colour-compressed) seeds. Each one-warp CTA grabs a unit, runs the
+// warp-level value (or record) walk for its tile and then the adjoint or tangent walk of every
+// direction, then grabs the next unit. Tapes of any length and
 // instance count share the GPU in one launch instead of one underfilled launch per tape.
 // ---------------------------------------------------------------------------------------------
 // Warp-level value sweep of one tile; instruction words are read straight from the tape
@@ -930,6 +946,17 @@ __global__ void __launch_bounds__(32, 16) k_batch(const __grid_constant__ BatchA
     primal_walk<true>(it.t, it.n_code, pt, wb, io, io + kMaxIo, active, il);
     // the warp's own partial stores must be visible to its loads below
     __syncwarp();
+    const bool act1[1] = {active}, tok1[1] = {true};
+    const long long ig1[1] = {il};
+    if (it.forward) {
+      for (int dir = 0; dir < it.ndir; ++dir) {
+        const int2 se = __ldg(it.tan_chunks + dir);
+        tangent_walk<false, kBatchGroup, 1, 1>(it.tan_stream + se.x, se.y / kBatchGroup, pt, 0,
+                                               tok1, wb, io + 2 * kMaxIo, io + 3 * kMaxIo, true,
+                                               act1, dir, it.ndir, ig1);
+      }
+      continue;
+    }
     for (int dir = 0; dir < it.ndir; ++dir) {
       for (int q = 0; q < it.t.sz_w; ++q) wreg(wb, q * 256u) = 0.0;
       if (active) {
@@ -939,8 +966,6 @@ __global__ void __launch_bounds__(32, 16) k_batch(const __grid_constant__ BatchA
           if (d.ptr) static_cast<double*>(d.ptr)[io_off(d, dir, jk.y, il)] = 0.0;
         }
       }
-      const bool act1[1] = {active}, tok1[1] = {true};
-      const long long ig1[1] = {il};
       adjoint_walk<false, kBatchGroup, 1>(it.adj_stream, it.adj_ngr, pt, 0, tok1, wb,
                                           io + 2 * kMaxIo, io + 3 * kMaxIo, act1, dir, ig1);
     }

@@ -79,13 +79,16 @@ struct SweepArgs {
 struct BatchItem {
   TapeView t;
   int n_code;
-  int ndir;                 // 0: value sweep only; >0: value + adjoint directions
+  int ndir;                 // 0: value sweep only; >0: value + derivative directions
+  int forward;              // directions are tangent (1, identity-seeded) or adjoint (0)
   long long n;              // instances
-  const IoDesc* io;         // 4*kMaxIo descriptors: inputs, outputs, adjoint seeds, sensitivities
-  const uint4* adj_stream;  // adjoint entry stream (ndir > 0)
+  const IoDesc* io;         // 4*kMaxIo descriptors: inputs, outputs, seeds, sensitivities
+  const uint4* adj_stream;  // adjoint entry stream (ndir > 0, !forward)
   int adj_ngr;              // its groups of kBatchGroup entries
   const int2* zero_in;      // inputs with a structurally zero adjoint
   int n_zero;
+  const uint4* tan_stream;  // tangent entry streams (forward)
+  const int2* tan_chunks;   // per direction: (first entry, entry count)
 };
 
 struct BatchArgs {

@@ -93,6 +93,8 @@ def load(path=None):
         "casadi_gb300_batch_free": (cint, [cint]),
         "casadi_gb300_batch_add": (cint, [cint, cint, i64, i64, cint, vp, vp, vp, vp]),
         "casadi_gb300_batch_scratch_size": (cint, [cint, vp]),
+        "casadi_gb300_batch_add_jacobian_colored": (cint, [cint, cint, i64, i64, cint, vp, vp, vp,
+                                                           vp]),
         "casadi_gb300_batch_run": (cint, [cint, vp, sz, cint, vp]),
     }
     for name, (res, args) in sig.items():
@@ -422,6 +424,24 @@ class Batch:
                                             _ptr_array(asens)))
         self._keep.append((tape, list(args), res, list(aseeds), asens))
         return res, asens
+
+    def add_jacobian_colored(self, tape, args, n_colors, color, outputs=None, n=None):
+        """Queue colour-compressed forward directions (``color``: int32 array, one colour per
+        flat input nonzero, -1 = unseeded). Returns the compressed blocks, one
+        (n_colors, nnz_out, n) tensor per output in ``outputs`` (default: all), None for the
+        others."""
+        import torch
+        n = CudaTape._n(args) if n is None else n
+        color = np.ascontiguousarray(color, dtype=np.int32)
+        comp = [torch.empty((n_colors, k, n), dtype=torch.float64, device="cuda")
+                if outputs is None or j in outputs else None
+                for j, k in enumerate(tape.nnz_out)]
+        res = [None] * len(tape.nnz_out)
+        check(load().casadi_gb300_batch_add_jacobian_colored(
+            self.id, tape.id, n, n, n_colors, color.ctypes.data, _ptr_array(args),
+            _ptr_array(res), _ptr_array(comp)))
+        self._keep.append((tape, list(args), comp, color))
+        return comp
 
     def scratch_bytes(self):
         b = ct.c_size_t()

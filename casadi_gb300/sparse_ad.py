@@ -80,17 +80,27 @@ class _Compressed:
             R._stream_handle(stream)))
         return comp[self.out]
 
-    def __call__(self, args, n=None, stream=None, scratch_limit=None):
-        """Nonzeros of every instance: a (nnz, n) float64 device tensor."""
+    def gather(self, comp, n, out=None, stream=None):
+        """Nonzeros (nnz, n) picked out of a compressed block (n_colors, nnz_out, n)."""
         import torch
-        n = R.CudaTape._n(args) if n is None else n
-        comp = self.compressed(args, n, stream, scratch_limit)
-        vals = torch.empty((self.src_row.numel(), n), dtype=torch.float64, device="cuda")
+        vals = torch.empty((self.src_row.numel(), n), dtype=torch.float64, device="cuda") \
+            if out is None else out
         R.check(R.load().casadi_gb300_gather(
             n, n, self.src_row.numel(), ct.c_void_p(self.src_row.data_ptr()),
             ct.c_void_p(comp.data_ptr()), ct.c_void_p(vals.data_ptr()),
             R._stream_handle(stream)))
         return vals
+
+    def __call__(self, args, n=None, stream=None, scratch_limit=None):
+        """Nonzeros of every instance: a (nnz, n) float64 device tensor."""
+        n = R.CudaTape._n(args) if n is None else n
+        return self.gather(self.compressed(args, n, stream, scratch_limit), n, stream=stream)
+
+    def add_to_batch(self, batch, args, n=None):
+        """Queue the compressed sweeps as an item of a :class:`runtime.Batch`; returns the
+        compressed block that ``batch.run()`` fills (recover with :meth:`gather`)."""
+        return batch.add_jacobian_colored(self.tape, args, self.n_colors, self._flat,
+                                          outputs=[self.out], n=n)[self.out]
 
 
 class ColoredJacobian(_Compressed):

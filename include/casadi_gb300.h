@@ -258,6 +258,11 @@ CASADI_GB300_API int casadi_gb300_batch_free(int batch);
 CASADI_GB300_API int casadi_gb300_batch_add(int batch, int id, int64_t n, int64_t ld, int nadj,
                            const double* const* arg, double* const* res,
                            const double* const* aseed, double* const* asens);
+/* A batch item of colour-compressed forward directions: as casadi_gb300_jacobian_colored
+ * (color, comp), run in the batch's single launch. Returns the item index. */
+CASADI_GB300_API int casadi_gb300_batch_add_jacobian_colored(int batch, int id, int64_t n,
+                           int64_t ld, int n_colors, const int* color,
+                           const double* const* arg, double* const* res, double* const* comp);
 CASADI_GB300_API int casadi_gb300_batch_scratch_size(int batch, size_t* bytes);
 CASADI_GB300_API int casadi_gb300_batch_run(int batch, void* scratch, size_t scratch_bytes,
                            int use_graph, void* stream);

@@ -76,3 +76,25 @@ def test_colored_lagrangian_hessian(gpu_lib):
         gq = O.reverse(F.tape, q, seeds, m)[1][0][0]
         col = (gp - gq) / (2 * h)  # column j of H, (nw, m)
         assert np.max(np.abs(Hd[:, j] - col) / np.maximum(np.abs(col), 1.0)) < 1e-5
+
+
+def test_colored_sweeps_in_one_batch_launch(gpu_lib):
+    """The constraint Jacobian and the Lagrangian Hessian as two items of one persistent
+    batch (replayed from a CUDA graph): the same bits as the separate coloured calls."""
+    from casadi_gb300 import runtime as R
+    from casadi_gb300.sparse_ad import ColoredHessian, ColoredJacobian
+    L = W.quad_ms_lagrangian(INTERVALS)
+    J = ColoredJacobian(W.quad_ms_constraints(INTERVALS), out=0, wrt=0)
+    H = ColoredHessian(L, out=1, wrt=0)
+    n = 1000
+    args = [torch.from_numpy(a).cuda() for a in _inputs(n, 3)]
+    want_j, want_h = J(args).cpu().numpy(), H(args).cpu().numpy()
+    b = R.Batch()
+    cj = J.add_to_batch(b, args)
+    ch = H.add_to_batch(b, args)
+    for _ in range(2):
+        b.run(graph=True)
+        got_j = J.gather(cj, n).cpu().numpy()
+        got_h = H.gather(ch, n).cpu().numpy()
+        assert same_bits(got_j, want_j).all()
+        assert same_bits(got_h, want_h).all()
