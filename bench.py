@@ -512,9 +512,8 @@ def run_native(a):
     ct.sync()
     ms_step = sum(ms) / len(ms)
     if dist:
-        t = torch.tensor([ms_step], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
+        from casadi_gb300 import replicas as RP
+        ms_step = RP.max_over_ranks(ms_step, device="cuda")  # the slowest replica's step
     value = world * n / (ms_step * 1e-3)
 
     # component rates (outside the timed region): eval-only and adjoint-only
