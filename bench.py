@@ -283,14 +283,14 @@ def cpu_baseline(F, args, aseeds, workload, budget_s=12.0):
 
 
 # ---- native arm ----------------------------------------------------------------------------------
-def mixed_component(torch, R, stream, reps=3):
+def mixed_component(torch, R, stream, reps=3, total=1 << 20):
     """Mixed-size batch: eight random-DAG tapes (200..20000 nodes, 64 inputs, 16 outputs)
     and work items with log-normal instance counts (median 4096, sigma 1.5) up to 2^20
     instances, each evaluated with the adjoint of the sum of its outputs: one launch pair per
     item (record + adjoint, one item after the other on one stream) against the persistent
     batch (all items in one launch, replayed from a CUDA graph)."""
     from casadi_gb300 import workloads as W
-    funs, items = W.mixed_batch(n_tapes=8, total=1 << 20, seed=0)
+    funs, items = W.mixed_batch(n_tapes=8, total=total, seed=0)
     tapes = [R.CudaTape(f) for f in funs]
     b = R.Batch()
     plain = []
@@ -433,6 +433,24 @@ def mpc_sparse_component(torch, stream, n=4096, intervals=100, reps=3):
             "ms": ms, "scenarios_per_s": n / (ms * 1e-3),
             "persistent_graph_ms": ms_batch, "persistent_scenarios_per_s": n / (ms_batch * 1e-3),
             "bitwise_equal": same, "host_setup_s": setup_s}
+
+
+def run_mixed(a):
+    """The mixed-size persistent batch alone (profiling captures of k_batch): one line with
+    the persistent batch's rate and the one-launch-pair-per-item comparison."""
+    import torch
+    from casadi_gb300 import runtime as R
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    comp = mixed_component(torch, R, torch.cuda.current_stream(), reps=max(1, a.steps),
+                           total=a.instances or (1 << 20))
+    print(json.dumps({"metric": METRIC, "value": comp["persistent_evals_per_s"], "unit": UNIT,
+                      "n_gpus": 1, "steps": a.steps, "warmup": 1,
+                      "ms_per_step": comp["persistent_ms"], "higher_is_better": True,
+                      "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                      "data": "synthetic",
+                      "config": {"workload": "mixed-size batch: 8 random-DAG tapes, "
+                                             "log-normal item sizes, value + adjoint"},
+                      "components": {"mixed_batch": comp}}), flush=True)
 
 
 def run_native(a):
@@ -683,7 +701,8 @@ def main():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="native", choices=["native", "reference"])
-    p.add_argument("--workload", default="rollout20", choices=["rollout20", "cartpole", "dag"])
+    p.add_argument("--workload", default="rollout20",
+                   choices=["rollout20", "cartpole", "dag", "mixed"])
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     p.add_argument("--instances", type=int, default=None,
                    help="override the workload's instance count (profiling captures)")
@@ -692,6 +711,8 @@ def main():
     a = p.parse_args()
     if a.impl == "reference":
         run_reference(a)
+    elif a.workload == "mixed":
+        run_mixed(a)
     else:
         run_native(a)
 
