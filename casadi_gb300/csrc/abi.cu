@@ -115,6 +115,14 @@ struct Tape {
   int device = 0;
   int n_instr = 0, n_in = 0, n_out = 0, sz_w = 0, n_partials = 0, n_chunks = 0;
   int ref_sz_w = 0;  // the work-vector length the tape came with (sz_w: after scheduling)
+  int residence = 0;  // work vector: 0 shared memory when it fits, 1 global memory
+  // global work vector: per-CTA blocks, grown on demand; uses on different streams are
+  // ordered by gw_event
+  std::mutex gw_mtx;
+  unsigned char* d_gw = nullptr;
+  size_t gw_cap = 0;
+  cudaEvent_t gw_event = nullptr;
+  bool gw_recorded = false;
   std::vector<int> nnz_in, nnz_out;
   std::vector<int2> absent_in;
   std::vector<int> pofs;    // partials recorded before instruction k*kPofsGran
@@ -142,6 +150,9 @@ struct Tape {
     cudaFree(d_consts);
     cudaFree(d_absent);
     cudaFree(d_err);
+    if (gw_event) cudaEventSynchronize(gw_event);
+    cudaFree(d_gw);
+    if (gw_event) cudaEventDestroy(gw_event);
     if (cur != device) cudaSetDevice(cur);
   }
 
@@ -274,6 +285,62 @@ bool g_autotune = true;
 
 bool fits_smem(int sz_w) {
   return smem_primal(sz_w, 32) <= static_cast<size_t>(max_smem_optin());
+}
+
+// Work-vector residence: global memory when asked for or when shared memory cannot hold it.
+bool primal_global(const Tape& t) {
+  return t.residence == 1 || !fits_smem(t.sz_w);
+}
+bool dir_global(const Tape& t) {
+  return t.residence == 1 || smem_lean(t.sz_w, 1, 0) > static_cast<size_t>(max_smem_optin());
+}
+
+constexpr size_t kGwMaxBytes = 4ull << 30;  // global work vectors of one launch
+
+bool capturing(cudaStream_t s) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(s, &cs);
+  return cs != cudaStreamCaptureStatusNone;
+}
+
+// Points a.wglob at a per-CTA block of per_cta bytes for *grid CTAs (grid capped to the
+// byte budget), growing the tape's buffer if needed; orders the launch after the buffer's
+// last use on another stream.
+int gw_prepare(Tape& t, SweepArgs& a, int* grid, size_t per_cta, cudaStream_t s) {
+  const long long max_grid = std::max<long long>(1, static_cast<long long>(kGwMaxBytes / per_cta));
+  *grid = static_cast<int>(std::min<long long>(*grid, max_grid));
+  const size_t need = per_cta * static_cast<size_t>(*grid);
+  std::lock_guard<std::mutex> lk(t.gw_mtx);
+  cudaError_t e;
+  if (!t.gw_event && (e = cudaEventCreateWithFlags(&t.gw_event, cudaEventDisableTiming)) != cudaSuccess)
+    return cuda_fail(e, "work-vector event");
+  if (t.gw_cap < need) {
+    if (capturing(s))
+      return fail(CASADI_GB300_ERR_ARG,
+                  "global work vector must grow (%zu bytes): call once before graph capture", need);
+    if (t.gw_recorded && (e = cudaEventSynchronize(t.gw_event)) != cudaSuccess)
+      return cuda_fail(e, "work-vector wait");
+    cudaFree(t.d_gw);
+    t.d_gw = nullptr;
+    t.gw_cap = 0;
+    if ((e = cudaMalloc(&t.d_gw, need)) != cudaSuccess) return cuda_fail(e, "cudaMalloc(work vectors)");
+    t.gw_cap = need;
+  } else if (t.gw_recorded && !capturing(s)) {
+    if ((e = cudaStreamWaitEvent(s, t.gw_event, 0)) != cudaSuccess)
+      return cuda_fail(e, "work-vector ordering");
+  }
+  a.wglob = t.d_gw;
+  a.wglob_stride = static_cast<long long>(per_cta);
+  return 0;
+}
+
+int gw_done(Tape& t, cudaStream_t s) {
+  if (capturing(s)) return 0;
+  std::lock_guard<std::mutex> lk(t.gw_mtx);
+  cudaError_t e = cudaEventRecord(t.gw_event, s);
+  if (e != cudaSuccess) return cuda_fail(e, "work-vector event record");
+  t.gw_recorded = true;
+  return 0;
 }
 
 int check_device(const Tape& t) {
@@ -569,6 +636,45 @@ int time_once(cudaStream_t s, F fn, float* ms) {
 
 // Values + partials (record sweep) followed by the derivative sweep, in waves of as many
 // instances as the scratch holds. `in/out/seed/sens` address the whole instance range.
+// Value-type sweeps (eval, record, both sparsity sweeps) over one instance range: the shared-
+// memory kernels with the tape's block size, or the global-work-vector kernels.
+enum PrimalKind { PK_EVAL = 0, PK_RECORD, PK_SP_FORWARD, PK_SP_REVERSE };
+
+int primal_launch(Tape& t, SweepArgs& a, long long m, PrimalKind kind, cudaStream_t s) {
+  static const int fam[] = {F_EVAL, F_RECORD, F_SP_FORWARD, F_SP_REVERSE};
+  static const char* what[] = {"eval launch", "record sweep launch", "sp_forward launch",
+                               "sp_reverse launch"};
+  auto go = [&](int grid) {
+    switch (kind) {
+      case PK_EVAL: return launch_eval(a, grid, s);
+      case PK_RECORD: return launch_record(a, grid, s);
+      case PK_SP_FORWARD: return launch_sp_forward(a, grid, s);
+      default: return launch_sp_reverse(a, grid, s);
+    }
+  };
+  const bool global = primal_global(t);
+  int grid;
+  if (global) {
+    a.block = kGwBlock;
+    const int occ = std::max(1, kind >= PK_SP_FORWARD ? occupancy_gw_sp() : occupancy_gw_primal());
+    grid = grid_for((m + kGwBlock - 1) / kGwBlock, occ * sm_count());
+    const size_t elem = 8;  // a double or a bvec_t per slot and instance
+    if (int rc = gw_prepare(t, a, &grid, static_cast<size_t>(std::max(1, t.sz_w)) * kGwBlock * elem, s))
+      return rc;
+  } else {
+    a.block = t.primal_block;
+    a.wglob = nullptr;
+    grid = grid_for((m + a.block - 1) / a.block, t.primal_grid_cap);
+  }
+  cudaError_t e = timed(fam[kind], s, [&] { return go(grid); });
+  if (e != cudaSuccess) return cuda_fail(e, what[kind]);
+  if (global) {
+    a.wglob = nullptr;
+    if (int rc = gw_done(t, s)) return rc;
+  }
+  return 0;
+}
+
 // One derivative sweep after the record sweep: ndir directions, forward (seeded or identity)
 // or adjoint, with its seed and sensitivity descriptors over the whole instance range.
 struct DerivReq {
@@ -647,6 +753,27 @@ int run_deriv(Tape& t, SweepArgs a, long long m, const DerivReq& rq, cudaStream_
     return launch_tangent(a, grid_of(v), v, s);
   };
   const long long work = tiles * ndir;
+  if (dir_global(t)) {
+    // global work vectors: one variant (G=2, 64 registers), one warp per CTA
+    int grid = static_cast<int>(std::max<long long>(
+        1, std::min<long long>(work, static_cast<long long>(sms) *
+                                         std::max(1, occupancy_gw_dir(adjoint)))));
+    if (int rc = gw_prepare(t, a, &grid, static_cast<size_t>(std::max(1, t.sz_w)) * 256, s))
+      return rc;
+    cudaError_t e = timed(adjoint ? F_ADJOINT : F_TANGENT, s, [&] {
+      if (adjoint) return launch_adjoint(a, grid, 0, s);
+      static const std::vector<int> kNoMap;
+      const TanPlan* tp = tan_plan(t, ndir, 1, 0, identity, seeded_in,
+                                   rq.dirmap ? *rq.dirmap : kNoMap, &plan_err);
+      if (!tp) return cudaErrorInvalidValue;
+      a.dstream = tp->d_stream;
+      a.dchunks = tp->d_chunks;
+      return launch_tangent(a, grid, 0, s);
+    });
+    if (plan_err) return plan_err;
+    if (e != cudaSuccess) return cuda_fail(e, "derivative sweep launch");
+    return gw_done(t, s);
+  }
   const int n_variants = adjoint ? AV_COUNT : TV_COUNT;
   int variant = t.tuned[kind];
   if (variant >= 0 && !fits(variant)) variant = -1;
@@ -693,10 +820,6 @@ int run_ad_multi(Tape& t, long long n, const IoDesc* in, const IoDesc* out,
                 scratch_bytes, 32ll * 8ll * t.n_partials);
   bool any = false;
   for (int r = 0; r < nreq; ++r) any = any || reqs[r].ndir > 0;
-  // derivative sweeps: one-warp CTAs, as many per SM as the work vector allows
-  if (any && smem_lean(t.sz_w, 1, 0) > static_cast<size_t>(max_smem_optin()))
-    return fail(CASADI_GB300_ERR_UNSUPPORTED,
-                "work vector of %d slots does not fit the derivative sweeps' shared memory", t.sz_w);
   if (any && static_cast<unsigned>(t.n_partials) >= kMaxPartials)
     return fail(CASADI_GB300_ERR_UNSUPPORTED, "tape records %d partials per instance (max %u)",
                 t.n_partials, kMaxPartials - 1);
@@ -709,11 +832,7 @@ int run_ad_multi(Tape& t, long long n, const IoDesc* in, const IoDesc* out,
     for (int j = 0, off = 0; j < t.n_in; off += t.nnz_in[j], ++j) a.in_off[j] = off;
     std::memcpy(a.in, in, sizeof(IoDesc) * t.n_in);
     std::memcpy(a.out, out, sizeof(IoDesc) * t.n_out);
-    a.block = t.primal_block;
-    cudaError_t e = timed(F_RECORD, s, [&] {
-      return launch_record(a, grid_for((m + a.block - 1) / a.block, t.primal_grid_cap), s);
-    });
-    if (e != cudaSuccess) return cuda_fail(e, "record sweep launch");
+    if (int rc = primal_launch(t, a, m, PK_RECORD, s)) return rc;
     for (int r = 0; r < nreq; ++r)
       if (reqs[r].ndir > 0)
         if (int rc = run_deriv(t, a, m, reqs[r], s)) return rc;
@@ -856,10 +975,6 @@ int casadi_gb300_tape_create(const casadi_gb300_atomic* alg, int n_instr, int n_
   Encoded en;
   const int wlen = encode_and_schedule(alg, n_instr, n_in, nnz_in, n_out, nnz_out, sz_w, en);
   if (wlen < 0) return wlen;
-  if (!fits_smem(wlen))
-    return fail(CASADI_GB300_ERR_UNSUPPORTED,
-                "work vector of %d slots (after scheduling) does not fit shared memory (global "
-                "work vectors are not available in this build)", wlen);
   auto t = std::make_unique<Tape>();
   t->n_instr = n_instr;
   t->n_in = n_in;
@@ -1026,13 +1141,7 @@ int casadi_gb300_eval(int id, int64_t n, int64_t ld, const double* const* arg,
   SweepArgs a = base_args(*t, n, 0);
   fill_io(a.in, t->n_in, vptrs(arg), t->nnz_in, ld, false);
   fill_io(a.out, t->n_out, vptrs(res), t->nnz_out, ld, false);
-  a.block = t->primal_block;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  cudaError_t e = timed(F_EVAL, s, [&] {
-    return launch_eval(a, grid_for((n + a.block - 1) / a.block, t->primal_grid_cap), s);
-  });
-  if (e != cudaSuccess) return cuda_fail(e, "eval launch");
-  return 0;
+  return primal_launch(*t, a, n, PK_EVAL, static_cast<cudaStream_t>(stream));
 }
 
 int casadi_gb300_forward(int id, int64_t n, int64_t ld, int nfwd, const double* const* arg,
@@ -1182,6 +1291,14 @@ int casadi_gb300_tuned_variant(int id, int kind, int* variant) {
   return 0;
 }
 
+int casadi_gb300_set_residence(int id, int mode) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  if (mode != 0 && mode != 1) return fail(CASADI_GB300_ERR_ARG, "residence must be 0 or 1");
+  t->residence = mode;
+  return 0;
+}
+
 int casadi_gb300_set_variant(int id, int kind, int variant) {
   Tape* t = get_tape(id);
   if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
@@ -1225,13 +1342,7 @@ int casadi_gb300_sp_forward(int id, int64_t n, int64_t ld, const uint64_t* const
   SweepArgs a = base_args(*t, n, 0);
   fill_io(a.in, t->n_in, vptrs(arg), t->nnz_in, ld, false);
   fill_io(a.out, t->n_out, vptrs(res), t->nnz_out, ld, false);
-  a.block = t->primal_block;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  cudaError_t e = timed(F_SP_FORWARD, s, [&] {
-    return launch_sp_forward(a, grid_for((n + a.block - 1) / a.block, t->primal_grid_cap), s);
-  });
-  if (e != cudaSuccess) return cuda_fail(e, "sp_forward launch");
-  return 0;
+  return primal_launch(*t, a, n, PK_SP_FORWARD, static_cast<cudaStream_t>(stream));
 }
 
 int casadi_gb300_sp_reverse(int id, int64_t n, int64_t ld, uint64_t* const* arg,
@@ -1244,13 +1355,7 @@ int casadi_gb300_sp_reverse(int id, int64_t n, int64_t ld, uint64_t* const* arg,
   SweepArgs a = base_args(*t, n, 0);
   fill_io(a.in, t->n_in, vptrs(arg), t->nnz_in, ld, false);
   fill_io(a.out, t->n_out, vptrs(res), t->nnz_out, ld, false);
-  a.block = t->primal_block;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  cudaError_t e = timed(F_SP_REVERSE, s, [&] {
-    return launch_sp_reverse(a, grid_for((n + a.block - 1) / a.block, t->primal_grid_cap), s);
-  });
-  if (e != cudaSuccess) return cuda_fail(e, "sp_reverse launch");
-  return 0;
+  return primal_launch(*t, a, n, PK_SP_REVERSE, static_cast<cudaStream_t>(stream));
 }
 
 int casadi_gb300_sync(int id, void* stream) {
@@ -1361,11 +1466,7 @@ int casadi_gb300_map_eval(int id, int mem, int64_t n, const double* const* arg,
   if (int rc = stage_blocks(*m, kMaxIo, t->n_out, t->nnz_out, 1, n,
                             reinterpret_cast<const double* const*>(res), false, a.out, s))
     return rc;
-  a.block = t->primal_block;
-  cudaError_t e = timed(F_EVAL, s, [&] {
-    return launch_eval(a, grid_for((n + a.block - 1) / a.block, t->primal_grid_cap), s);
-  });
-  if (e != cudaSuccess) return cuda_fail(e, "eval launch");
+  if (int rc = primal_launch(*t, a, n, PK_EVAL, s)) return rc;
   if (int rc = fetch_blocks(a.out, t->n_out, t->nnz_out, 1, n, res, s)) return rc;
   return casadi_gb300_sync(id, s);
 }

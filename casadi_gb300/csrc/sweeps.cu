@@ -146,12 +146,16 @@ __device__ __forceinline__ long long io_off(const IoDesc& d, long long dir, long
 // Forward value sweep (RECORD=false) and value + partials sweep (RECORD=true).
 // One thread per instance; BS instances per tile; persistent over tiles.
 // ---------------------------------------------------------------------------------------------
-template <int BS, bool RECORD>
+// GW: the work vector lives in global memory (a per-CTA block of a.wglob, L1/L2-cached)
+// instead of shared memory, for tapes whose work vector does not fit or is worth trading for
+// residency.
+template <int BS, bool RECORD, bool GW = false>
 __global__ void __launch_bounds__(BS) k_primal(const __grid_constant__ SweepArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
   u64* ring = reinterpret_cast<u64*>(smem);
   u64* bars = ring + 2 * kChunk;
-  double* w = reinterpret_cast<double*>(smem + kHeaderBytes);
+  double* w = GW ? reinterpret_cast<double*>(a.wglob + blockIdx.x * a.wglob_stride)
+                 : reinterpret_cast<double*>(smem + kHeaderBytes);
   const int tid = threadIdx.x;
   if (tid == 0) stage_init(bars);
   __syncthreads();
@@ -650,11 +654,11 @@ case KEY: {            \
 // LK_MIXED and x carries the real kind (bits 19-22) and the flags of direction k (bits
 // 24+2k, 25+2k), handled one direction at a time.
 
-template <int G, int MB, int IPT, int K>
+template <int G, int MB, int IPT, int K, bool GW = false>
 __global__ void __launch_bounds__(32, MB) k_tangent(const __grid_constant__ SweepArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x & 31;
-  unsigned char* wb = smem + lane * 8;
+  unsigned char* wb = (GW ? a.wglob + blockIdx.x * a.wglob_stride : smem) + lane * 8;
   const long long ntiles = (a.n + 31) / 32;
   const int ngroups = (a.ndir + K - 1) / K;
   const long long nwork = (ntiles + IPT - 1) / IPT * ngroups;
@@ -828,11 +832,11 @@ __device__ __forceinline__ void adjoint_walk(const uint4* st, int ngr, const dou
 
 // Flags (bits 0-4): 2/4 operand b/c receives a contribution, 8/16 it is the first one
 // (1 marks an entry with work; outputs carry 8 when their seed is the slot's first).
-template <int G, int MB, int IPT>
+template <int G, int MB, int IPT, bool GW = false>
 __global__ void __launch_bounds__(32, MB) k_adjoint(const __grid_constant__ SweepArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x & 31;
-  unsigned char* wb = smem + lane * 8;
+  unsigned char* wb = (GW ? a.wglob + blockIdx.x * a.wglob_stride : smem) + lane * 8;
   const long long ntiles = (a.n + 31) / 32;
   const long long nwork = (ntiles + IPT - 1) / IPT * a.ndir;
   const size_t tstride = static_cast<size_t>(a.t.n_partials) * 32;
@@ -975,12 +979,13 @@ __global__ void __launch_bounds__(32, 16) k_batch(const __grid_constant__ BatchA
 // ---------------------------------------------------------------------------------------------
 // bvec_t sparsity sweeps (uint64 bit sets, 64 directions at once).
 // ---------------------------------------------------------------------------------------------
-template <int BS>
+template <int BS, bool GW = false>
 __global__ void __launch_bounds__(BS) k_sp_forward(const __grid_constant__ SweepArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
   u64* ring = reinterpret_cast<u64*>(smem);
   u64* bars = ring + 2 * kChunk;
-  u64* w = reinterpret_cast<u64*>(smem + kHeaderBytes);
+  u64* w = GW ? reinterpret_cast<u64*>(a.wglob + blockIdx.x * a.wglob_stride)
+              : reinterpret_cast<u64*>(smem + kHeaderBytes);
   const int tid = threadIdx.x;
   if (tid == 0) stage_init(bars);
   __syncthreads();
@@ -1016,12 +1021,13 @@ __global__ void __launch_bounds__(BS) k_sp_forward(const __grid_constant__ Sweep
   }
 }
 
-template <int BS>
+template <int BS, bool GW = false>
 __global__ void __launch_bounds__(BS) k_sp_reverse(const __grid_constant__ SweepArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
   u64* ring = reinterpret_cast<u64*>(smem);
   u64* bars = ring + 2 * kChunk;
-  u64* w = reinterpret_cast<u64*>(smem + kHeaderBytes);
+  u64* w = GW ? reinterpret_cast<u64*>(a.wglob + blockIdx.x * a.wglob_stride)
+              : reinterpret_cast<u64*>(smem + kHeaderBytes);
   const int tid = threadIdx.x;
   if (tid == 0) stage_init(bars);
   __syncthreads();
@@ -1092,6 +1098,17 @@ int max_smem_optin() {
 }
 
 template <class K>
+static int occ_of_k(K kernel, int block, size_t smem) {
+  int n = 0;
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
+    return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, block, smem) != cudaSuccess)
+    return 0;
+  return n;
+}
+
+template <class K>
 static cudaError_t launch_k(K kernel, dim3 grid, int block, size_t smem, const SweepArgs& a,
                             cudaStream_t s) {
   cudaError_t e =
@@ -1110,25 +1127,33 @@ static cudaError_t launch_k(K kernel, dim3 grid, int block, size_t smem, const S
     default: return cudaErrorInvalidValue;                                              \
   }
 
+// With a.wglob set the global-work-vector instance runs (block kGwBlock, ring header only).
 cudaError_t launch_eval(const SweepArgs& a, int grid, cudaStream_t s) {
+  if (a.wglob) return launch_k(k_primal<kGwBlock, false, true>, grid, kGwBlock, kHeaderBytes, a, s);
   const size_t smem = smem_primal(a.t.sz_w, a.block);
   CGB_DISPATCH_BS(k_primal, , false)
 }
 
 cudaError_t launch_record(const SweepArgs& a, int grid, cudaStream_t s) {
+  if (a.wglob) return launch_k(k_primal<kGwBlock, true, true>, grid, kGwBlock, kHeaderBytes, a, s);
   const size_t smem = smem_primal(a.t.sz_w, a.block);
   CGB_DISPATCH_BS(k_primal, , true)
 }
 
 cudaError_t launch_sp_forward(const SweepArgs& a, int grid, cudaStream_t s) {
+  if (a.wglob) return launch_k(k_sp_forward<kGwBlock, true>, grid, kGwBlock, kHeaderBytes, a, s);
   const size_t smem = smem_primal(a.t.sz_w, a.block);
   CGB_DISPATCH_BS(k_sp_forward)
 }
 
 cudaError_t launch_sp_reverse(const SweepArgs& a, int grid, cudaStream_t s) {
+  if (a.wglob) return launch_k(k_sp_reverse<kGwBlock, true>, grid, kGwBlock, kHeaderBytes, a, s);
   const size_t smem = smem_primal(a.t.sz_w, a.block);
   CGB_DISPATCH_BS(k_sp_reverse)
 }
+
+int occupancy_gw_primal() { return occ_of_k(k_primal<kGwBlock, true, true>, kGwBlock, kHeaderBytes); }
+int occupancy_gw_sp() { return occ_of_k(k_sp_reverse<kGwBlock, true>, kGwBlock, kHeaderBytes); }
 
 // Derivative-sweep variants: G entries per software-pipeline group, MB minimum CTAs per SM
 // (register cap), IPT tiles per warp and, for the tangent sweep, K directions per warp.
@@ -1168,6 +1193,7 @@ int adj_variant_ipt(int variant) {
 }
 
 cudaError_t launch_tangent(const SweepArgs& a, int grid, int variant, cudaStream_t s) {
+  if (a.wglob) return launch_k(k_tangent<2, 32, 1, 1, true>, dim3(grid), 32, 0, a, s);
   switch (variant) {
 #define CGB_LAUNCH(V, G, MB, IPT, K)                                                          \
   case V:                                                                                     \
@@ -1180,6 +1206,7 @@ cudaError_t launch_tangent(const SweepArgs& a, int grid, int variant, cudaStream
 }
 
 cudaError_t launch_adjoint(const SweepArgs& a, int grid, int variant, cudaStream_t s) {
+  if (a.wglob) return launch_k(k_adjoint<2, 32, 1, true>, dim3(grid), 32, 0, a, s);
   switch (variant) {
 #define CGB_LAUNCH(V, G, MB, IPT)                                                              \
   case V:                                                                                      \
@@ -1288,6 +1315,10 @@ int occupancy_dense(int dir_warps, size_t smem) {
     case 8: return occ_of(k_adjoint_tape<8, true>, 256, smem);
     default: return 0;
   }
+}
+
+int occupancy_gw_dir(bool adjoint) {
+  return adjoint ? occ_of(k_adjoint<2, 32, 1, true>, 32, 0) : occ_of(k_tangent<2, 32, 1, 1, true>, 32, 0);
 }
 
 int occupancy_dir(int variant, bool adjoint, size_t smem) {

@@ -73,6 +73,9 @@ struct SweepArgs {
   const uint4* dstream;             // entries of all streams
   const int2* dchunks;              // per direction (tangent) or one (adjoint): first entry, count
   const int* dchunk_off;            // unused by the warp-independent sweeps
+  // global work vector (null: shared memory): CTA b uses wglob + b*wglob_stride
+  unsigned char* wglob;
+  long long wglob_stride;
 };
 
 // One item of a persistent batch: a tape over its own instance range.
@@ -100,6 +103,10 @@ struct BatchArgs {
   long long scratch_stride;
 };
 
+constexpr int kGwBlock = 128;   // threads per CTA of the global-work-vector value sweeps
+int occupancy_gw_primal();       // CTAs per SM of the global-work-vector value/record sweep
+int occupancy_gw_sp();           // ... of the sparsity sweeps
+int occupancy_gw_dir(bool adjoint);  // ... of the derivative sweeps (one warp per CTA)
 cudaError_t launch_gather(long long n, long long ld, int count, const long long* src_row,
                           const double* src, double* dst, cudaStream_t s);
 cudaError_t launch_batch(const BatchArgs& b, int grid, size_t smem, cudaStream_t s);

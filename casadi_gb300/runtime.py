@@ -84,6 +84,7 @@ def load(path=None):
         "casadi_gb300_autotune": (cint, [cint]),
         "casadi_gb300_tuned_variant": (cint, [cint, cint, vp]),
         "casadi_gb300_set_variant": (cint, [cint, cint, cint]),
+        "casadi_gb300_set_residence": (cint, [cint, cint]),
         "casadi_gb300_uni_coloring": (cint, [cint, cint, vp, vp, vp]),
         "casadi_gb300_jacobian_colored": (cint, [cint, i64, i64, cint, vp, vp, vp, vp, vp, sz,
                                                  vp]),
@@ -289,6 +290,10 @@ class CudaTape:
 
     def sync(self, stream=None):
         check(load().casadi_gb300_sync(self.id, _stream_handle(stream)))
+
+    def set_residence(self, mode):
+        """Work vectors in shared memory when they fit (0) or always in global memory (1)."""
+        check(load().casadi_gb300_set_residence(self.id, mode))
 
     def set_variant(self, kind, variant):
         """Fix the derivative-sweep variant of one kind (-1: let the autotuner choose)."""

@@ -205,6 +205,12 @@ CASADI_GB300_API int casadi_gb300_map_jacobian_reverse(int id, int mem, int64_t 
  * the reference, whose Map has one code path per parallelization (casadi/core/map.cpp:39-51). */
 CASADI_GB300_API int casadi_gb300_autotune(int enable);
 CASADI_GB300_API int casadi_gb300_tuned_variant(int id, int kind, int* variant);
+/* Work-vector residence of a tape's sweeps: 0 (default) shared memory when the scheduled
+ * work vector fits, global memory (L1/L2-cached per-CTA blocks owned by the tape) when it does
+ * not; 1 always global memory. Results are identical either way. A tape whose global work
+ * vectors must grow cannot be first used inside a CUDA graph capture. No counterpart in the
+ * reference, whose work vector is the caller's w array (casadi/core/function_internal.hpp:414). */
+CASADI_GB300_API int casadi_gb300_set_residence(int id, int mode);
 /* Fixes the variant of one kind on a tape (kinds 0 and 1: 0..4; kind 2: 0..4), or clears it
  * for retuning (-1). */
 CASADI_GB300_API int casadi_gb300_set_variant(int id, int kind, int variant);
