@@ -115,7 +115,9 @@ struct Tape {
   int device = 0;
   int n_instr = 0, n_in = 0, n_out = 0, sz_w = 0, n_partials = 0, n_chunks = 0;
   int ref_sz_w = 0;  // the work-vector length the tape came with (sz_w: after scheduling)
-  int residence = 0;  // work vector: 0 shared memory when it fits, 1 global memory
+  int residence = 0;  // work vector: 0 auto (shared memory when it fits, value sweeps tuned),
+                      // 1 global memory, 2 shared memory whenever it fits
+  int primal_tuned[4] = {-1, -1, -1, -1};  // per PrimalKind: 0 shared, 1 global (autotuned)
   // global work vector: per-CTA blocks, grown on demand; uses on different streams are
   // ordered by gw_event
   std::mutex gw_mtx;
@@ -652,27 +654,49 @@ int primal_launch(Tape& t, SweepArgs& a, long long m, PrimalKind kind, cudaStrea
       default: return launch_sp_reverse(a, grid, s);
     }
   };
-  const bool global = primal_global(t);
-  int grid;
-  if (global) {
-    a.block = kGwBlock;
-    const int occ = std::max(1, kind >= PK_SP_FORWARD ? occupancy_gw_sp() : occupancy_gw_primal());
-    grid = grid_for((m + kGwBlock - 1) / kGwBlock, occ * sm_count());
-    const size_t elem = 8;  // a double or a bvec_t per slot and instance
-    if (int rc = gw_prepare(t, a, &grid, static_cast<size_t>(std::max(1, t.sz_w)) * kGwBlock * elem, s))
-      return rc;
-  } else {
-    a.block = t.primal_block;
-    a.wglob = nullptr;
-    grid = grid_for((m + a.block - 1) / a.block, t.primal_grid_cap);
+  // one launch with the work vector in shared (global = false) or global memory
+  auto run = [&](bool global, bool profile) -> int {
+    int grid;
+    if (global) {
+      a.block = kGwBlock;
+      const int occ =
+          std::max(1, kind >= PK_SP_FORWARD ? occupancy_gw_sp() : occupancy_gw_primal());
+      grid = grid_for((m + kGwBlock - 1) / kGwBlock, occ * sm_count());
+      const size_t elem = 8;  // a double or a bvec_t per slot and instance
+      if (int rc = gw_prepare(t, a, &grid,
+                              static_cast<size_t>(std::max(1, t.sz_w)) * kGwBlock * elem, s))
+        return rc;
+    } else {
+      a.block = t.primal_block;
+      a.wglob = nullptr;
+      grid = grid_for((m + a.block - 1) / a.block, t.primal_grid_cap);
+    }
+    cudaError_t e = profile ? timed(fam[kind], s, [&] { return go(grid); }) : go(grid);
+    if (e != cudaSuccess) return cuda_fail(e, what[kind]);
+    if (global) {
+      a.wglob = nullptr;
+      if (int rc = gw_done(t, s)) return rc;
+    }
+    return 0;
+  };
+  if (primal_global(t)) return run(true, true);
+  if (t.residence == 2) return run(false, true);
+  int choice = t.primal_tuned[kind];
+  // residence is tuned like the derivative variants: time both on a launch that fills the GPU
+  // several times (every sweep here but sp_reverse, which consumes its seeds, can run twice)
+  if (choice < 0 && g_autotune && kind != PK_SP_REVERSE && !capturing(s) &&
+      m >= 16ll * sm_count() * 32) {
+    float ms[2] = {0, 0};
+    for (int g = 0; g < 2; ++g) {
+      int rc = 0;
+      if (int trc = time_once(s, [&] { rc = run(g == 1, false); return cudaSuccess; }, &ms[g]))
+        return trc;
+      if (rc) return rc;
+    }
+    t.primal_tuned[kind] = ms[1] < ms[0] ? 1 : 0;
+    return 0;  // both runs produced the same (complete) results
   }
-  cudaError_t e = timed(fam[kind], s, [&] { return go(grid); });
-  if (e != cudaSuccess) return cuda_fail(e, what[kind]);
-  if (global) {
-    a.wglob = nullptr;
-    if (int rc = gw_done(t, s)) return rc;
-  }
-  return 0;
+  return run(choice == 1, true);
 }
 
 // One derivative sweep after the record sweep: ndir directions, forward (seeded or identity)
@@ -1294,8 +1318,9 @@ int casadi_gb300_tuned_variant(int id, int kind, int* variant) {
 int casadi_gb300_set_residence(int id, int mode) {
   Tape* t = get_tape(id);
   if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
-  if (mode != 0 && mode != 1) return fail(CASADI_GB300_ERR_ARG, "residence must be 0 or 1");
+  if (mode < 0 || mode > 2) return fail(CASADI_GB300_ERR_ARG, "residence must be 0, 1 or 2");
   t->residence = mode;
+  for (int& c : t->primal_tuned) c = -1;
   return 0;
 }
 

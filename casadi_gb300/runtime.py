@@ -292,7 +292,7 @@ class CudaTape:
         check(load().casadi_gb300_sync(self.id, _stream_handle(stream)))
 
     def set_residence(self, mode):
-        """Work vectors in shared memory when they fit (0) or always in global memory (1)."""
+        """Work-vector residence: 0 auto (tuned), 1 global memory, 2 shared memory when it fits."""
         check(load().casadi_gb300_set_residence(self.id, mode))
 
     def set_variant(self, kind, variant):

@@ -207,7 +207,9 @@ CASADI_GB300_API int casadi_gb300_autotune(int enable);
 CASADI_GB300_API int casadi_gb300_tuned_variant(int id, int kind, int* variant);
 /* Work-vector residence of a tape's sweeps: 0 (default) shared memory when the scheduled
  * work vector fits, global memory (L1/L2-cached per-CTA blocks owned by the tape) when it does
- * not; 1 always global memory. Results are identical either way. A tape whose global work
+ * not, and for the value/record/sparsity sweeps the faster of the two, timed by the autotuner
+ * on the first large call; 1 always global memory; 2 shared memory whenever it fits. Results
+ * are identical either way. A tape whose global work
  * vectors must grow cannot be first used inside a CUDA graph capture. No counterpart in the
  * reference, whose work vector is the caller's w array (casadi/core/function_internal.hpp:414). */
 CASADI_GB300_API int casadi_gb300_set_residence(int id, int mode);

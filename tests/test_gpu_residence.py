@@ -49,7 +49,9 @@ def test_forced_global_equals_shared(gpu_lib):
         ct.sync()
         return out
 
-    shared = run(R.CudaTape(F))
+    sh = R.CudaTape(F)
+    sh.set_residence(2)
+    shared = run(sh)
     g = R.CudaTape(F)
     g.set_residence(1)
     glob = run(g)
