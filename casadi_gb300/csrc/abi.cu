@@ -1745,8 +1745,11 @@ struct BatchHost {
   // device side, rebuilt when dirty
   BatchItem* d_items = nullptr;
   IoDesc* d_io = nullptr;
-  int2* d_units = nullptr;
-  unsigned* d_counter = nullptr;
+  int4* d_units = nullptr;
+  unsigned* d_counter = nullptr;  // [0] next unit, [1] error bits
+  unsigned* d_flags = nullptr;    // tile flags of split items
+  size_t n_flags = 0;
+  std::vector<double*> d_tile_partials;  // per split item
   int n_units = 0;
   int szw = 1, pmax = 0, grid = 1;
   size_t smem = 0;
@@ -1761,6 +1764,8 @@ struct BatchHost {
     cudaFree(d_io);
     cudaFree(d_units);
     cudaFree(d_counter);
+    cudaFree(d_flags);
+    for (double* p : d_tile_partials) cudaFree(p);
     if (ev_in) cudaEventDestroy(ev_in);
     if (ev_out) cudaEventDestroy(ev_out);
     if (stream) cudaStreamDestroy(stream);
@@ -1785,12 +1790,19 @@ int batch_prepare(BatchHost& b) {
   cudaFree(b.d_items);
   cudaFree(b.d_io);
   cudaFree(b.d_units);
+  cudaFree(b.d_flags);
+  for (double* p : b.d_tile_partials) cudaFree(p);
+  b.d_tile_partials.clear();
   b.d_items = nullptr;
   b.d_io = nullptr;
   b.d_units = nullptr;
+  b.d_flags = nullptr;
   std::vector<BatchItem> items;
   std::vector<IoDesc> io;
-  std::vector<std::pair<double, int2>> units;
+  // (cost, unit): record and whole units first (longest first), then direction units
+  std::vector<std::pair<double, int4>> units, dir_units;
+  std::vector<std::pair<size_t, size_t>> flag_off;  // (item, first flag) of split items
+  size_t n_flags = 0;
   b.szw = 1;
   b.pmax = 0;
   for (size_t k = 0; k < b.items.size(); ++k) {
@@ -1813,7 +1825,6 @@ int batch_prepare(BatchHost& b) {
       if (!tp) return err;
       bi.tan_stream = tp->d_stream;
       bi.tan_chunks = tp->d_chunks;
-      b.pmax = std::max(b.pmax, t->n_partials);
     } else if (it.ndir > 0) {
       if (static_cast<unsigned>(t->n_partials) >= kMaxPartials)
         return fail(CASADI_GB300_ERR_UNSUPPORTED, "batch item %zu records too many partials", k);
@@ -1829,50 +1840,87 @@ int batch_prepare(BatchHost& b) {
       bi.adj_ngr = se.y / kBatchGroup;
       bi.zero_in = ap->d_zero;
       bi.n_zero = ap->n_zero;
-      b.pmax = std::max(b.pmax, t->n_partials);
     }
     b.szw = std::max(b.szw, t->sz_w);
-    // cost of one tile: instructions x (1 value sweep + directions)
-    const double cost = static_cast<double>(t->n_instr) * (1 + it.ndir);
-    for (long long tile = 0; tile < (it.n + 31) / 32; ++tile)
-      units.push_back({cost, make_int2(static_cast<int>(k), static_cast<int>(tile))});
+    const long long tiles = (it.n + 31) / 32;
+    if (it.ndir >= 2) {
+      // split: one record unit per tile into the item's own partial buffer, then one unit
+      // per (tile, direction), so the directions of a tile run on different SMs
+      double* tp = nullptr;
+      const size_t bytes = static_cast<size_t>(tiles) * t->n_partials * 32 * sizeof(double);
+      cudaError_t e = cudaMalloc(&tp, std::max<size_t>(bytes, 8));
+      if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(batch tile partials)");
+      b.d_tile_partials.push_back(tp);
+      bi.tile_partials = tp;
+      flag_off.push_back({k, n_flags});
+      std::vector<int2> se(it.forward ? it.ndir : 1);
+      if (it.forward &&
+          (e = cudaMemcpy(se.data(), bi.tan_chunks, sizeof(int2) * it.ndir,
+                          cudaMemcpyDeviceToHost)) != cudaSuccess)
+        return cuda_fail(e, "read tangent plan");
+      for (long long tile = 0; tile < tiles; ++tile) {
+        units.push_back({static_cast<double>(t->n_instr),
+                         make_int4(static_cast<int>(k), static_cast<int>(tile), -1, 0)});
+        for (int d = 0; d < it.ndir; ++d) {
+          const double len = it.forward ? se[d].y : bi.adj_ngr * kBatchGroup;
+          dir_units.push_back({len, make_int4(static_cast<int>(k), static_cast<int>(tile), d, 0)});
+        }
+      }
+      n_flags += static_cast<size_t>(tiles);
+    } else {
+      // whole units: value sweep plus the (at most one) direction in one warp
+      const double cost = static_cast<double>(t->n_instr) * (1 + it.ndir);
+      for (long long tile = 0; tile < tiles; ++tile)
+        units.push_back({cost, make_int4(static_cast<int>(k), static_cast<int>(tile), -1, 0)});
+      if (it.ndir > 0) b.pmax = std::max(b.pmax, t->n_partials);
+    }
     items.push_back(bi);
     io.insert(io.end(), it.io.begin(), it.io.end());
   }
-  std::stable_sort(units.begin(), units.end(),
-                   [](const std::pair<double, int2>& x, const std::pair<double, int2>& y) {
-                     return x.first > y.first;
-                   });
-  std::vector<int2> ulist(units.size());
-  for (size_t k = 0; k < units.size(); ++k) ulist[k] = units[k].second;
+  auto longest_first = [](const std::pair<double, int4>& x, const std::pair<double, int4>& y) {
+    return x.first > y.first;
+  };
+  std::stable_sort(units.begin(), units.end(), longest_first);
+  std::stable_sort(dir_units.begin(), dir_units.end(), longest_first);
+  std::vector<int4> ulist;
+  ulist.reserve(units.size() + dir_units.size());
+  for (const auto& u : units) ulist.push_back(u.second);
+  for (const auto& u : dir_units) ulist.push_back(u.second);
   cudaError_t e;
+  if (n_flags && (e = cudaMalloc(&b.d_flags, n_flags * sizeof(unsigned))) != cudaSuccess)
+    return cuda_fail(e, "cudaMalloc(batch flags)");
+  b.n_flags = n_flags;
+  for (const auto& fo : flag_off) items[fo.first].ready = b.d_flags + fo.second;
   if ((e = upload(&b.d_io, io)) != cudaSuccess) return cuda_fail(e, "upload batch I/O");
   for (size_t k = 0; k < items.size(); ++k) items[k].io = b.d_io + k * 4 * kMaxIo;
   if ((e = upload(&b.d_items, items)) != cudaSuccess || (e = upload(&b.d_units, ulist)) != cudaSuccess)
     return cuda_fail(e, "upload batch");
-  if (!b.d_counter && (e = cudaMalloc(&b.d_counter, sizeof(unsigned))) != cudaSuccess)
+  if (!b.d_counter && (e = cudaMalloc(&b.d_counter, 2 * sizeof(unsigned))) != cudaSuccess)
     return cuda_fail(e, "cudaMalloc(counter)");
   b.n_units = static_cast<int>(ulist.size());
   b.smem = static_cast<size_t>(b.szw) * 256;
   if (b.smem > static_cast<size_t>(max_smem_optin()))
     return fail(CASADI_GB300_ERR_UNSUPPORTED, "batch work vector of %d slots does not fit", b.szw);
-  const int occ = std::max(1, occupancy_batch(b.smem));
+  const int occ = std::max(1, occupancy_batch(b.smem, b.n_flags > 0));
   b.grid = std::max(1, std::min(sm_count() * occ, std::max(1, b.n_units)));
   b.dirty = false;
   return 0;
 }
 
 int batch_enqueue(BatchHost& b, void* scratch, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(b.d_counter, 0, sizeof(unsigned), s);
+  cudaError_t e = cudaMemsetAsync(b.d_counter, 0, 2 * sizeof(unsigned), s);
+  if (e == cudaSuccess && b.n_flags)
+    e = cudaMemsetAsync(b.d_flags, 0, b.n_flags * sizeof(unsigned), s);
   if (e != cudaSuccess) return cuda_fail(e, "reset batch counter");
   BatchArgs a;
   a.items = b.d_items;
   a.units = b.d_units;
   a.n_units = b.n_units;
   a.counter = b.d_counter;
+  a.err = b.d_counter + 1;
   a.scratch = static_cast<double*>(scratch);
   a.scratch_stride = static_cast<long long>(b.pmax) * 32;
-  e = launch_batch(a, b.grid, b.smem, s);
+  e = launch_batch(a, b.grid, b.smem, b.n_flags > 0, s);
   if (e != cudaSuccess) return cuda_fail(e, "batch launch");
   return 0;
 }
@@ -1960,6 +2008,19 @@ int casadi_gb300_batch_add_jacobian_colored(int batch, int id, int64_t n, int64_
   b->items.push_back(std::move(it));
   b->dirty = true;
   return static_cast<int>(b->items.size()) - 1;
+}
+
+int casadi_gb300_batch_status(int batch) {
+  BatchHost* b = get_batch(batch);
+  if (!b) return fail(CASADI_GB300_ERR_ID, "no batch %d", batch);
+  if (!b->d_counter) return 0;
+  unsigned w[2] = {0, 0};
+  cudaError_t e = cudaStreamSynchronize(b->stream);
+  if (e == cudaSuccess) e = cudaMemcpy(w, b->d_counter, sizeof(w), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "batch status");
+  if (w[1] & kErrWaitTimeout)
+    return fail(CASADI_GB300_ERR_CUDA, "batch: a direction unit timed out waiting for its tile");
+  return 0;
 }
 
 int casadi_gb300_batch_scratch_size(int batch, size_t* bytes) {

@@ -928,40 +928,83 @@ __device__ __forceinline__ void primal_walk(const TapeView& t, int n_code, doubl
   }
 }
 
+// Bounded wait (lane 0, then shared with the warp) for a split item's tile flag. Every record
+// unit precedes every direction unit in the list, so the unit that sets the flag was taken by
+// a CTA that is already running and waits on nothing: the wait ends unless that CTA faults.
+__device__ __forceinline__ bool wait_tile(const unsigned* flag, unsigned* err) {
+  bool ok = true;
+  if ((threadIdx.x & 31) == 0) {
+    const long long t0 = clock64();
+    for (unsigned k = 0;; ++k) {
+      if (*reinterpret_cast<const volatile unsigned*>(flag)) break;
+      if ((k & 63u) == 63u && clock64() - t0 > kWaitCycles) {
+        ok = false;
+        atomicOr(err, kErrWaitTimeout);
+        break;
+      }
+      __nanosleep(128);
+    }
+  }
+  ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+  __threadfence();  // the partials written before the flag are visible from here on
+  return ok;
+}
+
+// kSplit: the batch has split items (per-tile record units and per-direction units); batches
+// without any run the instance that holds only the whole-unit path.
+template <bool kSplit>
 __global__ void __launch_bounds__(32, 16) k_batch(const __grid_constant__ BatchArgs b) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x;
   unsigned char* wb = smem + lane * 8;
-  double* pt = b.scratch + static_cast<size_t>(blockIdx.x) * b.scratch_stride + lane;
+  double* const pcta = b.scratch + static_cast<size_t>(blockIdx.x) * b.scratch_stride + lane;
   for (;;) {
     unsigned u = 0;
     if (lane == 0) u = atomicAdd(b.counter, 1u);
     u = __shfl_sync(0xffffffffu, u, 0);
     if (u >= static_cast<unsigned>(b.n_units)) break;
-    const int2 unit = __ldg(b.units + u);
+    const int4 unit = __ldg(b.units + u);
     const BatchItem& it = b.items[unit.x];
     const long long il = static_cast<long long>(unit.y) * 32 + lane;
     const bool active = il < it.n;
     const IoDesc* io = it.io;
-    if (it.ndir == 0) {
-      primal_walk<false>(it.t, it.n_code, pt, wb, io, io + kMaxIo, active, il);
-      continue;
+    // partials: the item's per-tile buffer (split items) or this CTA's scratch (whole units)
+    double* pt = (kSplit && it.tile_partials)
+                     ? it.tile_partials + static_cast<size_t>(unit.y) * it.t.n_partials * 32 + lane
+                     : pcta;
+    int d0 = 0, d1 = it.ndir;
+    if (!kSplit || unit.z < 0) {
+      // record (or value) unit
+      if (it.ndir == 0) {
+        primal_walk<false>(it.t, it.n_code, pt, wb, io, io + kMaxIo, active, il);
+        continue;
+      }
+      primal_walk<true>(it.t, it.n_code, pt, wb, io, io + kMaxIo, active, il);
+      if (kSplit && it.tile_partials) {
+        // split item: publish the tile's partials; its directions are separate units
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) atomicExch(it.ready + unit.y, 1u);
+        continue;
+      }
+      // whole unit: the warp's own partial stores must be visible to its loads below
+      __syncwarp();
+    } else {
+      // one direction of a split item, after its tile's record unit
+      if (!wait_tile(it.ready + unit.y, b.err)) continue;
+      d0 = unit.z;
+      d1 = unit.z + 1;
     }
-    primal_walk<true>(it.t, it.n_code, pt, wb, io, io + kMaxIo, active, il);
-    // the warp's own partial stores must be visible to its loads below
-    __syncwarp();
     const bool act1[1] = {active}, tok1[1] = {true};
     const long long ig1[1] = {il};
-    if (it.forward) {
-      for (int dir = 0; dir < it.ndir; ++dir) {
+    for (int dir = d0; dir < d1; ++dir) {
+      if (it.forward) {
         const int2 se = __ldg(it.tan_chunks + dir);
         tangent_walk<false, kBatchGroup, 1, 1>(it.tan_stream + se.x, se.y / kBatchGroup, pt, 0,
                                                tok1, wb, io + 2 * kMaxIo, io + 3 * kMaxIo, true,
                                                act1, dir, it.ndir, ig1);
+        continue;
       }
-      continue;
-    }
-    for (int dir = 0; dir < it.ndir; ++dir) {
       for (int q = 0; q < it.t.sz_w; ++q) wreg(wb, q * 256u) = 0.0;
       if (active) {
         for (int k = 0; k < it.n_zero; ++k) {
@@ -1250,14 +1293,20 @@ cudaError_t launch_gather(long long n, long long ld, int count, const long long*
   return cudaGetLastError();
 }
 
-cudaError_t launch_batch(const BatchArgs& b, int grid, size_t smem, cudaStream_t s) {
+cudaError_t launch_batch(const BatchArgs& b, int grid, size_t smem, bool split, cudaStream_t s) {
   // the attribute is raised once to the device maximum, so a captured graph never depends on
   // a later call lowering it
-  static const cudaError_t set = cudaFuncSetAttribute(
-      k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_optin());
-  if (set != cudaSuccess) return set;
+  static const cudaError_t set0 = cudaFuncSetAttribute(
+      k_batch<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_optin());
+  static const cudaError_t set1 = cudaFuncSetAttribute(
+      k_batch<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_optin());
+  if (set0 != cudaSuccess) return set0;
+  if (set1 != cudaSuccess) return set1;
   if (smem > static_cast<size_t>(max_smem_optin())) return cudaErrorInvalidValue;
-  k_batch<<<grid, 32, smem, s>>>(b);
+  if (split)
+    k_batch<true><<<grid, 32, smem, s>>>(b);
+  else
+    k_batch<false><<<grid, 32, smem, s>>>(b);
   return cudaGetLastError();
 }
 
@@ -1296,13 +1345,19 @@ static int occ_of(K kernel, int block, size_t smem) {
   return n;
 }
 
-int occupancy_batch(size_t smem) {
-  if (cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           max_smem_optin()) != cudaSuccess)
-    return 0;
+int occupancy_batch(size_t smem, bool split) {
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch, 32, smem) != cudaSuccess)
-    return 0;
+  if (split) {
+    if (cudaFuncSetAttribute(k_batch<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             max_smem_optin()) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch<true>, 32, smem) != cudaSuccess)
+      return 0;
+  } else {
+    if (cudaFuncSetAttribute(k_batch<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             max_smem_optin()) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch<false>, 32, smem) != cudaSuccess)
+      return 0;
+  }
   return n;
 }
 

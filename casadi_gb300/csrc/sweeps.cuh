@@ -92,14 +92,21 @@ struct BatchItem {
   int n_zero;
   const uint4* tan_stream;  // tangent entry streams (forward)
   const int2* tan_chunks;   // per direction: (first entry, entry count)
+  // split items (two or more directions): one record unit per tile writes the tile's partials
+  // here, (tile*P + p)*32 + lane, then sets ready[tile]; one unit per (tile, direction) waits
+  // for the flag and walks its direction
+  double* tile_partials;
+  unsigned* ready;
 };
 
 struct BatchArgs {
   const BatchItem* items;
-  const int2* units;        // (item, tile), longest first
+  const int4* units;        // (item, tile, direction or -1, 0): record/whole units longest
+                            // first, then the direction units of split items
   int n_units;
   unsigned* counter;        // next unit (zeroed before each launch)
-  double* scratch;          // partials, scratch_stride doubles per CTA
+  unsigned* err;            // kErr* bits (zeroed before each launch)
+  double* scratch;          // partials of whole units, scratch_stride doubles per CTA
   long long scratch_stride;
 };
 
@@ -109,8 +116,8 @@ int occupancy_gw_sp();           // ... of the sparsity sweeps
 int occupancy_gw_dir(bool adjoint);  // ... of the derivative sweeps (one warp per CTA)
 cudaError_t launch_gather(long long n, long long ld, int count, const long long* src_row,
                           const double* src, double* dst, cudaStream_t s);
-cudaError_t launch_batch(const BatchArgs& b, int grid, size_t smem, cudaStream_t s);
-int occupancy_batch(size_t smem);
+cudaError_t launch_batch(const BatchArgs& b, int grid, size_t smem, bool split, cudaStream_t s);
+int occupancy_batch(size_t smem, bool split);
 
 // Error bits written to TapeView::err.
 constexpr int kErrWaitTimeout = 1;   // a bounded wait on a staged chunk ran out

@@ -94,6 +94,7 @@ def load(path=None):
         "casadi_gb300_batch_free": (cint, [cint]),
         "casadi_gb300_batch_add": (cint, [cint, cint, i64, i64, cint, vp, vp, vp, vp]),
         "casadi_gb300_batch_scratch_size": (cint, [cint, vp]),
+        "casadi_gb300_batch_status": (cint, [cint]),
         "casadi_gb300_batch_add_jacobian_colored": (cint, [cint, cint, i64, i64, cint, vp, vp, vp,
                                                            vp]),
         "casadi_gb300_batch_run": (cint, [cint, vp, sz, cint, vp]),
@@ -452,6 +453,10 @@ class Batch:
         b = ct.c_size_t()
         check(load().casadi_gb300_batch_scratch_size(self.id, ct.byref(b)))
         return b.value
+
+    def status(self):
+        """Wait for the last run and raise if a unit of it failed on the device."""
+        check(load().casadi_gb300_batch_status(self.id))
 
     def run(self, graph=False, stream=None):
         import torch

@@ -259,8 +259,12 @@ CASADI_GB300_API int casadi_gb300_star_coloring(int n, const int* colind, const 
  * uneven length and instance count keep the GPU full. With use_graph the launch is captured
  * once into a CUDA graph (on a stream the batch owns, ordered after and before the caller's
  * stream) and replayed; adding items or changing the scratch buffer re-captures it.
- * casadi_gb300_batch_add returns the item index. No counterpart in the reference: a CasADi
- * Map evaluates one Function per call (casadi/core/map.cpp:141-157). */
+ * casadi_gb300_batch_add returns the item index. An item with two or more directions is
+ * split: one unit per tile records its partials into a buffer the batch owns, and one unit
+ * per (tile, direction) walks that direction after the tile's record unit has finished (a
+ * bounded wait on a per-tile flag; record units precede direction units in the list), so the
+ * directions of a tile run in parallel. No counterpart in the reference: a CasADi Map
+ * evaluates one Function per call (casadi/core/map.cpp:141-157). */
 CASADI_GB300_API int casadi_gb300_batch_create(void);
 CASADI_GB300_API int casadi_gb300_batch_free(int batch);
 CASADI_GB300_API int casadi_gb300_batch_add(int batch, int id, int64_t n, int64_t ld, int nadj,
@@ -272,6 +276,9 @@ CASADI_GB300_API int casadi_gb300_batch_add_jacobian_colored(int batch, int id, 
                            int64_t ld, int n_colors, const int* color,
                            const double* const* arg, double* const* res, double* const* comp);
 CASADI_GB300_API int casadi_gb300_batch_scratch_size(int batch, size_t* bytes);
+/* Waits for the batch's stream and reports a device-side failure of its last run (a
+ * direction unit whose tile's record unit did not finish within its bounded wait). */
+CASADI_GB300_API int casadi_gb300_batch_status(int batch);
 CASADI_GB300_API int casadi_gb300_batch_run(int batch, void* scratch, size_t scratch_bytes,
                            int use_graph, void* stream);
 

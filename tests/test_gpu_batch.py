@@ -56,6 +56,7 @@ def test_batch_matches_per_tape_sweeps(gpu_lib, graph):
     b.run(graph=graph)
     if graph:
         b.run(graph=True)  # replay
+    b.status()
     for t, dargs, dseeds, res, asens in queued:
         t.sync()
         if dseeds is None:
@@ -81,6 +82,7 @@ def test_batch_matches_oracle(gpu_lib):
                            [_cuda(s) for s in seeds] if seeds else None)
         queued.append((f, n, args, seeds, res, asens, t))
     b.run()
+    b.status()
     for k, (f, n, args, seeds, res, asens, t) in enumerate(queued):
         t.sync()
         # thousands of sin/cos/exp/tanh nodes carry the <= 1-ulp differences between CUDA's and

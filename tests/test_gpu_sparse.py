@@ -94,6 +94,7 @@ def test_colored_sweeps_in_one_batch_launch(gpu_lib):
     ch = H.add_to_batch(b, args)
     for _ in range(2):
         b.run(graph=True)
+        b.status()
         got_j = J.gather(cj, n).cpu().numpy()
         got_h = H.gather(ch, n).cpu().numpy()
         assert same_bits(got_j, want_j).all()
