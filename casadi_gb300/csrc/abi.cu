@@ -137,6 +137,7 @@ struct Tape {
   int primal_block = 128, primal_grid_cap = 1;
   std::mutex shape_mtx;
   int tuned[3] = {-1, -1, -1};  // derivative-sweep variant per kind (seeded/identity tangent, adjoint)
+  std::vector<double> h_consts;  // constant pool (host copy, for inlining into callers)
   std::vector<u64> h_code;                            // padded instruction stream
   std::vector<std::unique_ptr<TanPlan>> tan_plans;
   std::vector<std::unique_ptr<AdjPlan>> adj_plans;
@@ -930,7 +931,8 @@ int encode_tape(const casadi_gb300_atomic* alg, int n_instr, int n_in, const int
     if (op == kOpParameter)
       return fail(CASADI_GB300_ERR_UNSUPPORTED, "instruction %d: free parameter (OP_PARAMETER)", k);
     if (op == kOpCall)
-      return fail(CASADI_GB300_ERR_UNSUPPORTED, "instruction %d: OP_CALL is not supported", k);
+      return fail(CASADI_GB300_ERR_UNSUPPORTED,
+                  "instruction %d: OP_CALL needs its callees (casadi_gb300_tape_create_calls)", k);
     const int dop = device_opcode(op);
     if (dop < 0) return fail(CASADI_GB300_ERR_UNSUPPORTED, "instruction %d: unknown op %d", k, op);
     if (dop == D_CONST) {
@@ -1010,6 +1012,7 @@ int casadi_gb300_tape_create(const casadi_gb300_atomic* alg, int n_instr, int n_
   t->absent_in = en.absent_in;
   std::vector<u64>& code = en.code;
   std::vector<double>& consts = en.consts;
+  t->h_consts = consts;
   const long long n_partials = en.n_partials;
   t->n_partials = static_cast<int>(n_partials);
   t->n_chunks = std::max(1, (n_instr + kChunk - 1) / kChunk);
@@ -1117,6 +1120,92 @@ int casadi_gb300_star_coloring(int n, const int* colind, const int* row, int ord
   if (n > 0 && !color) return fail(CASADI_GB300_ERR_ARG, "missing color array");
   if (ordering != 0 && ordering != 1) return fail(CASADI_GB300_ERR_ARG, "ordering must be 0 or 1");
   return star_coloring_ccs(n, colind, row, ordering, color);
+}
+
+int casadi_gb300_tape_create_calls(const casadi_gb300_atomic* alg, int n_instr, int n_in,
+                                   const int* nnz_in, int n_out, const int* nnz_out, int sz_w,
+                                   int n_calls, const int* call_tape,
+                                   const int* const* call_dep, const int* const* call_res) {
+  if (n_instr < 0 || (n_instr > 0 && !alg)) return fail(CASADI_GB300_ERR_ARG, "no instructions");
+  if (n_calls < 0 || (n_calls > 0 && (!call_tape || !call_dep || !call_res)))
+    return fail(CASADI_GB300_ERR_ARG, "missing call tables");
+  if (sz_w < 0) return fail(CASADI_GB300_ERR_ARG, "negative size");
+  // Inline every OP_CALL: the callee's instructions with their slots moved past the caller's
+  // work vector, its inputs copied in from the call's dep slots and its outputs copied out to
+  // the res slots (SXFunction::call_fwd, casadi/core/sx_function.cpp:1595-1621)
+  std::vector<casadi_gb300_atomic> out;
+  out.reserve(n_instr);
+  long long wlen = sz_w;
+  for (int k = 0; k < n_instr; ++k) {
+    const casadi_gb300_atomic& e = alg[k];
+    if (e.op != kOpCall) {
+      out.push_back(e);
+      continue;
+    }
+    const int ci = e.a.i[0];
+    if (ci < 0 || ci >= n_calls)
+      return fail(CASADI_GB300_ERR_ARG, "instruction %d: call index %d out of range", k, ci);
+    Tape* f = get_tape(call_tape[ci]);
+    if (!f) return fail(CASADI_GB300_ERR_ID, "call %d: no tape with id %d", ci, call_tape[ci]);
+    const int* dep = call_dep[ci];
+    const int* res = call_res[ci];
+    int nzi = 0, nzo = 0;
+    for (int v : f->nnz_in) nzi += v;
+    for (int v : f->nnz_out) nzo += v;
+    if ((nzi > 0 && !dep) || (nzo > 0 && !res))
+      return fail(CASADI_GB300_ERR_ARG, "call %d: missing dep/res slots", ci);
+    for (int i = 0; i < nzi; ++i)
+      if (dep[i] < 0 || dep[i] >= sz_w)
+        return fail(CASADI_GB300_ERR_ARG, "call %d: dep slot out of range", ci);
+    for (int i = 0; i < nzo; ++i)
+      if (res[i] < -1 || res[i] >= sz_w)
+        return fail(CASADI_GB300_ERR_ARG, "call %d: res slot out of range", ci);
+    std::vector<int> off_in(f->n_in + 1, 0), off_out(f->n_out + 1, 0);
+    for (int j = 0; j < f->n_in; ++j) off_in[j + 1] = off_in[j] + f->nnz_in[j];
+    for (int j = 0; j < f->n_out; ++j) off_out[j + 1] = off_out[j] + f->nnz_out[j];
+    const long long base = wlen;
+    wlen += std::max(1, f->sz_w);
+    if (wlen > kFieldMax)
+      return fail(CASADI_GB300_ERR_UNSUPPORTED, "inlined work vector exceeds %u slots", kFieldMax);
+    auto emit = [&](int op, long long i0, int i1, int i2, double d) {
+      casadi_gb300_atomic a;
+      std::memset(&a, 0, sizeof(a));
+      a.op = op;
+      a.i0 = static_cast<int>(i0);
+      if (op == kOpConst) {
+        a.a.d = d;
+      } else {
+        a.a.i[0] = i1;
+        a.a.i[1] = i2;
+      }
+      out.push_back(a);
+    };
+    for (u64 w : f->h_code) {
+      const unsigned op = dec_op(w), A = dec_a(w), B = dec_b(w), C = dec_c(w);
+      switch (op) {
+        case D_NOP:
+          break;
+        case D_INPUT: {
+          const int slot = dep[off_in[B] + static_cast<int>(C)];
+          emit(0 /* OP_ASSIGN */, base + A, slot, slot, 0.0);
+        } break;
+        case D_OUTPUT: {
+          const int r = res[off_out[A] + static_cast<int>(C)];
+          if (r >= 0) emit(0 /* OP_ASSIGN */, r, static_cast<int>(base + B), static_cast<int>(base + B), 0.0);
+        } break;
+        case D_CONST:
+          emit(kOpConst, base + A, 0, 0, f->h_consts[B]);
+          break;
+        default:
+          emit(reference_opcode(op), base + A, static_cast<int>(base + B),
+               static_cast<int>(base + C), 0.0);
+      }
+    }
+  }
+  if (out.size() > static_cast<size_t>(0x7fffffff))
+    return fail(CASADI_GB300_ERR_UNSUPPORTED, "inlined tape too long");
+  return casadi_gb300_tape_create(out.data(), static_cast<int>(out.size()), n_in, nnz_in, n_out,
+                                  nnz_out, static_cast<int>(wlen));
 }
 
 int casadi_gb300_tape_free(int id) {

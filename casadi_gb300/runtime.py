@@ -59,6 +59,8 @@ def load(path=None):
         "casadi_gb300_version": (ct.c_char_p, []),
         "casadi_gb300_tape_create": (cint, [vp, cint, cint, vp, cint, vp, cint]),
         "casadi_gb300_tape_free": (cint, [cint]),
+        "casadi_gb300_tape_create_calls": (cint, [vp, cint, cint, vp, cint, vp, cint, cint, vp, vp,
+                                                  vp]),
         "casadi_gb300_tape_schedule": (cint, [vp, cint, cint, vp, cint, vp, cint, vp, vp]),
         "casadi_gb300_tape_info": (cint, [cint, vp, vp, vp, vp, vp]),
         "casadi_gb300_scratch_size": (cint, [cint, i64, vp]),
@@ -150,7 +152,10 @@ def schedule(tape):
 class CudaTape:
     """A tape registered with the GPU library (one CUDA device)."""
 
-    def __init__(self, tape):
+    def __init__(self, tape, calls=None):
+        """``tape``: an :class:`sx.Function` or :class:`sx.Tape`. ``calls``: for tapes with
+        OP_CALL instructions (call index in ``i1``), a list of ``(callee CudaTape, dep slots,
+        res slots)``; the calls are inlined by the library."""
         if isinstance(tape, _sx.Function):
             tape = tape.tape
         self.tape = tape
@@ -158,9 +163,21 @@ class CudaTape:
         atoms = tape.atomic_array()
         self._nnz_in = np.ascontiguousarray(tape.nnz_in, dtype=np.int32)
         self._nnz_out = np.ascontiguousarray(tape.nnz_out, dtype=np.int32)
-        self.id = check(lib.casadi_gb300_tape_create(
-            atoms.ctypes.data, tape.n_instr, len(tape.nnz_in), self._nnz_in.ctypes.data,
-            len(tape.nnz_out), self._nnz_out.ctypes.data, tape.sz_w))
+        if calls:
+            ids = np.ascontiguousarray([c[0].id for c in calls], dtype=np.int32)
+            deps = [np.ascontiguousarray(c[1], dtype=np.int32) for c in calls]
+            ress = [np.ascontiguousarray(c[2], dtype=np.int32) for c in calls]
+            dptr = (ct.c_void_p * len(calls))(*[d.ctypes.data for d in deps])
+            rptr = (ct.c_void_p * len(calls))(*[x.ctypes.data for x in ress])
+            self._callees = [c[0] for c in calls]  # keep the callee tapes registered
+            self.id = check(lib.casadi_gb300_tape_create_calls(
+                atoms.ctypes.data, tape.n_instr, len(tape.nnz_in), self._nnz_in.ctypes.data,
+                len(tape.nnz_out), self._nnz_out.ctypes.data, tape.sz_w, len(calls),
+                ids.ctypes.data, dptr, rptr))
+        else:
+            self.id = check(lib.casadi_gb300_tape_create(
+                atoms.ctypes.data, tape.n_instr, len(tape.nnz_in), self._nnz_in.ctypes.data,
+                len(tape.nnz_out), self._nnz_out.ctypes.data, tape.sz_w))
         vals = [ct.c_int() for _ in range(5)]
         check(lib.casadi_gb300_tape_info(self.id, *[ct.byref(v) for v in vals]))
         self.n_instr, self.n_in, self.n_out, self.sz_w, self.n_partials = [v.value for v in vals]

@@ -85,6 +85,19 @@ CASADI_GB300_API int casadi_gb300_tape_create(const casadi_gb300_atomic* alg, in
 /* Release a tape and its device memory. Cf. casadi_c_decref_id (casadi_c.h:113). */
 CASADI_GB300_API int casadi_gb300_tape_free(int id);
 
+/* A tape with OP_CALL instructions (nested Functions): instruction k with op OP_CALL (48)
+ * names call a.i[0]; call c evaluates the registered tape call_tape[c] with its input
+ * nonzeros read from the caller's work-vector slots call_dep[c][0 .. nnz_in-1] and its output
+ * nonzeros written to call_res[c][0 .. nnz_out-1] (-1: not needed) — the reference's
+ * ExtendedAlgEl dep/res (casadi/core/sx_function.cpp:630-661) and call_fwd (:1595-1621).
+ * The calls are inlined on the host (callee slots placed past the caller's work vector, input
+ * and output copies as OP_ASSIGN), then the tape is created as by casadi_gb300_tape_create, so
+ * every sweep and derivative supports them. Returns the new tape id. */
+CASADI_GB300_API int casadi_gb300_tape_create_calls(const casadi_gb300_atomic* alg,
+                           int n_instr, int n_in, const int* nnz_in, int n_out,
+                           const int* nnz_out, int sz_w, int n_calls, const int* call_tape,
+                           const int* const* call_dep, const int* const* call_res);
+
 /* The tape as the GPU sweeps run it: casadi_gb300_tape_create reorders the instructions so
  * fewer values are live at once (the work vector of every 32-instance tile sits in shared
  * memory, and its length decides how many tiles an SM runs at a time) and reassigns the slots.
