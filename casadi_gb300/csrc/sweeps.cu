@@ -210,43 +210,33 @@ __global__ void __launch_bounds__(BS) k_primal(const __grid_constant__ SweepArgs
 }
 
 // ---------------------------------------------------------------------------------------------
-// Derivative sweeps from recorded partials.
+// Plan-free adjoint sweep (the allocation-free entry point).
 //
 // The record sweep stores partials tile-major: for the 32-instance tile T of a wave,
 // partial p of lane l is at partials[(T*P + p)*32 + l]. The partials an instruction chunk
-// consumes for one tile are therefore one contiguous block. Each chunk is staged with three
-// TMA bulk copies on one mbarrier: its instruction words, its partial block, and its
-// activity plan. A CTA works on one tile with DW warps, one direction per warp; consecutive
-// CTAs take the direction groups of the same tile, so a tile's partial block is read from
-// HBM once and from L2 for the other groups.
-//
-// Activity plan: which derivatives are structurally zero does not depend on the instance,
-// only on the tape and the seed pattern, so the host precomputes it. For the tangent sweep
-// each instruction carries two bits per direction of the group (operand b carries a
-// derivative, operand c carries one); chunks in which no direction of the group does any
-// work are left out of the group's chunk list and never fetched. For the adjoint sweep each
-// instruction carries five bits shared by all directions (its adjoint is nonzero, operand b
-// / c receives a contribution, that contribution is the first one to b / c).
+// consumes for one tile are therefore one contiguous block. This CTA-level adjoint sweep
+// stages each chunk, last first, with TMA bulk copies on one mbarrier (instruction words and
+// partial block) and treats every instruction as active, so it needs no host-built plan and
+// no plan memory. The regular derivative sweeps (warp-independent entry streams) follow
+// further below.
 // ---------------------------------------------------------------------------------------------
 struct DirSmem {
   u64* ring;      // 2 x chunk instruction words
   double* pbuf;   // 2 x (2*chunk partials x 32 lanes)
-  unsigned char* abuf;  // 2 x chunk activity entries (2 bytes each for the tangent sweep)
   u64* bars;      // 2 mbarriers
-  double* wd;     // sz_w x (32*DW) tangents/adjoints
+  double* wd;     // sz_w x (32*DW) adjoints
 };
 
 __host__ __device__ __forceinline__ size_t dir_header_bytes(int ch) {
   return static_cast<size_t>(2 * ch) * sizeof(u64) + static_cast<size_t>(4 * ch * 32) * 8 +
-         static_cast<size_t>(2 * ch) * 2 + 2 * sizeof(u64);
+         2 * sizeof(u64);
 }
 
 __device__ __forceinline__ DirSmem dir_smem(unsigned char* smem, int ch) {
   DirSmem s;
   s.ring = reinterpret_cast<u64*>(smem);
   s.pbuf = reinterpret_cast<double*>(smem + 2 * ch * sizeof(u64));
-  s.abuf = reinterpret_cast<unsigned char*>(s.pbuf + 2 * (2 * ch * 32));
-  s.bars = reinterpret_cast<u64*>(s.abuf + 2 * ch * 2);
+  s.bars = reinterpret_cast<u64*>(s.pbuf + 2 * (2 * ch * 32));
   s.wd = reinterpret_cast<double*>(s.bars + 2);
   return s;
 }
@@ -263,33 +253,28 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
       : "memory");
 }
 
-// Stage chunk c (instructions, partial block of wave-local tile tl, activity entries of
-// `abytes_per` bytes from plan `plan`) into slot seq&1.
+// Stage chunk c (instructions and the partial block of wave-local tile tl) into slot seq&1.
 __device__ __forceinline__ void stage_dir(const SweepArgs& a, const DirSmem& s, unsigned seq,
-                                          int c, long long tl, const unsigned char* plan,
-                                          unsigned abytes_per) {
+                                          int c, long long tl) {
   const int ch = a.chunk;
   const int p0 = chunk_p0(a, c), p1 = chunk_p0(a, c + 1);
   const unsigned ibytes = ch * sizeof(u64);
   const unsigned pbytes = static_cast<unsigned>(p1 - p0) * 32u * sizeof(double);
-  const unsigned abytes = ch * abytes_per;
   const unsigned slot = seq & 1u;
   u64* bar = s.bars + slot;
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-               "r"(ibytes + pbytes + abytes)
+               "r"(ibytes + pbytes)
                : "memory");
   bulk_g2s(s.ring + slot * ch, a.t.code + static_cast<size_t>(c) * ch, ibytes, bar);
-  bulk_g2s(s.abuf + slot * ch * 2, plan + static_cast<size_t>(c) * ch * abytes_per, abytes, bar);
   if (pbytes)
     bulk_g2s(s.pbuf + slot * (2 * ch * 32), a.partials + (tl * a.t.n_partials + p0) * 32, pbytes,
              bar);
 }
 
 // Adjoint sweep over the 8-byte instruction stream (seed = w'[i0]; w'[i0] = 0;
-// w'[i1] += d0*seed; w'[i2] += d1*seed, sx_function.cpp:1454-1560). With kDense it needs no
-// activity plan (every chunk, every instruction active, contributions always added to a
-// zeroed adjoint) and so no plan memory; the allocation-free entry point uses that variant.
-template <int DW, bool kDense>
+// w'[i1] += d0*seed; w'[i2] += d1*seed, sx_function.cpp:1454-1560): every chunk, every
+// instruction active, contributions always added to a zeroed adjoint; DW directions per CTA.
+template <int DW>
 __global__ void __launch_bounds__(32 * DW) k_adjoint_tape(const __grid_constant__ SweepArgs a) {
   constexpr int BS = 32 * DW;
   extern __shared__ __align__(128) unsigned char smem[];
@@ -303,7 +288,7 @@ __global__ void __launch_bounds__(32 * DW) k_adjoint_tape(const __grid_constant_
   const long long dir = static_cast<long long>(group) * DW + warp;
   const bool dir_ok = dir < a.ndir;
   const int ch = a.chunk;
-  const int nlist = kDense ? a.n_code / ch : __ldg(a.chunk_list_off + 1);
+  const int nlist = a.n_code / ch;
   const long long ntiles = (a.n + 31) / 32;
   const long long tstride = gridDim.x / ngroups;
   unsigned seq = 0;
@@ -314,8 +299,8 @@ __global__ void __launch_bounds__(32 * DW) k_adjoint_tape(const __grid_constant_
     const long long ig = a.i_begin + il;
     if (active) {
       // input nonzeros whose adjoint is structurally zero (or never read) get a zero
-      const int nz = kDense ? a.t.n_absent_in : a.n_zero;
-      const int2* zl = kDense ? a.t.absent_in : a.zero_in;
+      const int nz = a.t.n_absent_in;
+      const int2* zl = a.t.absent_in;
       for (int k = 0; k < nz; ++k) {
         const int2 jk = __ldg(zl + k);
         const IoDesc& d = a.sens[jk.x];
@@ -323,39 +308,29 @@ __global__ void __launch_bounds__(32 * DW) k_adjoint_tape(const __grid_constant_
       }
     }
     if (nlist == 0) continue;
-    // the dense variant stages instruction bytes in place of plan bytes (never read)
-    const unsigned char* plan = kDense ? reinterpret_cast<const unsigned char*>(a.t.code) : a.adj_bits;
-    if (tid == 0)
-      stage_dir(a, s, seq, kDense ? nlist - 1 : __ldg(a.chunk_list + nlist - 1), tile, plan, 1);
+    if (tid == 0) stage_dir(a, s, seq, nlist - 1, tile);
 #pragma unroll 1
     for (int idx = nlist - 1; idx >= 0; --idx) {
       const bool more = idx > 0;
-      if (tid == 0 && more)
-        stage_dir(a, s, seq + 1, kDense ? idx - 1 : __ldg(a.chunk_list + idx - 1), tile, plan, 1);
+      if (tid == 0 && more) stage_dir(a, s, seq + 1, idx - 1, tile);
       const bool ok = stage_wait(s.bars, seq);
       if (!__syncthreads_and(ok)) {
         stage_abort(a.t, s.bars, seq, more);
         return;
       }
-      const int c = kDense ? idx : __ldg(a.chunk_list + idx);
+      const int c = idx;
       const u64* code = s.ring + (seq & 1u) * ch;
       const double* pb = s.pbuf + (seq & 1u) * (2 * ch * 32) + lane;
-      const unsigned char* bits = s.abuf + (seq & 1u) * ch * 2;
       int pl = chunk_p0(a, c + 1) - chunk_p0(a, c);
 #pragma unroll 1
       for (int k = ch - 1; k >= 0; --k) {
         const u64 ins = code[k];
         const unsigned op = dec_op(ins), A = dec_a(ins), B = dec_b(ins), C = dec_c(ins);
         const unsigned m = dec_pmask(ins);
-        unsigned f;
-        if (kDense) {
-          f = op == D_OUTPUT ? 32u
-                             : (op == D_NOP ? 0u
-                                            : 1u | (carries_d0(op) ? 2u : 0u) |
-                                                  (carries_d1(op) ? 4u : 0u));
-        } else {
-          f = bits[k];
-        }
+        const unsigned f = op == D_OUTPUT ? 32u
+                           : (op == D_NOP ? 0u
+                                          : 1u | (carries_d0(op) ? 2u : 0u) |
+                                                (carries_d1(op) ? 4u : 0u));
         double d0 = 1.0, d1 = 0.0;
         if (m & 2u) d1 = pb[32 * --pl];
         if (m & 1u) d0 = pb[32 * --pl];
@@ -1263,11 +1238,11 @@ cudaError_t launch_adjoint(const SweepArgs& a, int grid, int variant, cudaStream
 cudaError_t launch_adjoint_dense(const SweepArgs& a, int grid, cudaStream_t s) {
   const size_t smem = smem_dir(a.t.sz_w, a.block / 32, a.chunk);
   switch (a.block / 32) {
-    case 1: return launch_k(k_adjoint_tape<1, true>, dim3(grid), 32, smem, a, s);
-    case 2: return launch_k(k_adjoint_tape<2, true>, dim3(grid), 64, smem, a, s);
-    case 4: return launch_k(k_adjoint_tape<4, true>, dim3(grid), 128, smem, a, s);
-    case 6: return launch_k(k_adjoint_tape<6, true>, dim3(grid), 192, smem, a, s);
-    case 8: return launch_k(k_adjoint_tape<8, true>, dim3(grid), 256, smem, a, s);
+    case 1: return launch_k(k_adjoint_tape<1>, dim3(grid), 32, smem, a, s);
+    case 2: return launch_k(k_adjoint_tape<2>, dim3(grid), 64, smem, a, s);
+    case 4: return launch_k(k_adjoint_tape<4>, dim3(grid), 128, smem, a, s);
+    case 6: return launch_k(k_adjoint_tape<6>, dim3(grid), 192, smem, a, s);
+    case 8: return launch_k(k_adjoint_tape<8>, dim3(grid), 256, smem, a, s);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -1363,11 +1338,11 @@ int occupancy_batch(size_t smem, bool split) {
 
 int occupancy_dense(int dir_warps, size_t smem) {
   switch (dir_warps) {
-    case 1: return occ_of(k_adjoint_tape<1, true>, 32, smem);
-    case 2: return occ_of(k_adjoint_tape<2, true>, 64, smem);
-    case 4: return occ_of(k_adjoint_tape<4, true>, 128, smem);
-    case 6: return occ_of(k_adjoint_tape<6, true>, 192, smem);
-    case 8: return occ_of(k_adjoint_tape<8, true>, 256, smem);
+    case 1: return occ_of(k_adjoint_tape<1>, 32, smem);
+    case 2: return occ_of(k_adjoint_tape<2>, 64, smem);
+    case 4: return occ_of(k_adjoint_tape<4>, 128, smem);
+    case 6: return occ_of(k_adjoint_tape<6>, 192, smem);
+    case 8: return occ_of(k_adjoint_tape<8>, 256, smem);
     default: return 0;
   }
 }

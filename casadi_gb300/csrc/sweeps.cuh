@@ -20,7 +20,6 @@ enum LeanKind : unsigned {
   LK_CONST, LK_MIXED
 };
 constexpr int kMaxIo = 64;       // inputs/outputs per tape handled by one launch
-constexpr int kDirWarps = 4;     // directions per CTA in the derivative sweeps (one per warp)
 
 // One input/output block: element (direction d, nonzero k, instance i) lives at
 // ptr[d*dir_stride + k*nz_stride + i*inst_stride].
@@ -62,17 +61,11 @@ struct SweepArgs {
   IoDesc seed[kMaxIo];      // forward: input seeds / adjoint: output seeds
   IoDesc sens[kMaxIo];      // forward: output sensitivities / adjoint: input sensitivities
   int in_off[kMaxIo];       // flat offset of each input's first nonzero (identity seeds)
-  // activity plans (host-computed; see the derivative sweeps)
-  const unsigned short* tan_bits;   // [group][n_code]: 2 bits per direction of the group
-  const unsigned char* adj_bits;    // [n_code]: adjoint activity flags
-  const int* chunk_list;            // chunk indices to process, per group (tangent) or one list
-  const int* chunk_list_off;        // offsets into chunk_list, groups + 1 entries
   const int2* zero_in;              // adjoint: (input, nonzero) pairs with a zero sensitivity
   int n_zero;
   // derivative entry streams (host-compiled; see the derivative sweeps)
   const uint4* dstream;             // entries of all streams
   const int2* dchunks;              // per direction (tangent) or one (adjoint): first entry, count
-  const int* dchunk_off;            // unused by the warp-independent sweeps
   // global work vector (null: shared memory): CTA b uses wglob + b*wglob_stride
   unsigned char* wglob;
   long long wglob_stride;

@@ -415,3 +415,30 @@ def test_jacobian_reverse_equals_the_two_calls(gpu_lib):
     # host layout agrees with the device layout
     assert_bitexact(np.transpose(hj2[0], (1, 2, 0)), host(jac2)[0], "layouts")
     ct.sync()
+
+
+def test_sweeps_replay_from_a_cuda_graph(gpu_lib):
+    """After one warm-up call (plans built, variants tuned), the derivative entry points can
+    be captured into a CUDA graph and replayed: the replays read the inputs' current contents
+    and give the same bits as direct calls."""
+    F = W.cartpole_rollout(4)
+    n = 4096
+    ct = CudaTape(F)
+    args = dev(W.cartpole_inputs(n, steps=4, seed=51))
+    aseeds = dev([np.zeros((1, 4, n)), np.ones((1, 1, n))])
+    res, jac, asens = ct.jacobian_reverse(args, aseeds)  # warm-up
+    torch.cuda.synchronize()
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        ct.jacobian_reverse(args, aseeds, res=res, jac=jac, asens=asens, stream=s)
+    for seed in (52, 53):
+        for a, v in zip(args, dev(W.cartpole_inputs(n, steps=4, seed=seed))):
+            a.copy_(v)
+        g.replay()
+        torch.cuda.synchronize()
+        want_r, want_j, want_a = ct.jacobian_reverse(args, aseeds)
+        for x, y in zip(host(res) + host(jac) + host(asens),
+                        host(want_r) + host(want_j) + host(want_a)):
+            assert_bitexact(x, y, "graph replay")
+    ct.sync()
