@@ -361,7 +361,7 @@ __global__ void __launch_bounds__(32 * DW) k_adjoint_tape(const __grid_constant_
           switch (op) {
             case D_ADD: case D_SUB: case D_ASSIGN: c0 = seed; break;
             case D_NEG: c0 = d_neg(seed); break;
-            case D_TWICE: c0 = __dadd_rn(seed, seed); break;
+            case D_TWICE: c0 = d_twice(seed); break;
             default: c0 = __dmul_rn(d0, seed);
           }
           double* w1 = wb + B * BS + tid;
@@ -509,7 +509,7 @@ case (LK_SUB << 2) | 3u: R = __dsub_rn(CGB_W(cur.y, j, k), CGB_W(cur.z, j, k)); 
 case (LK_NEG << 2) | 1u: R = d_neg(CGB_W(cur.y, j, k)); break;                             \
 case (LK_TWICE << 2) | 1u: {                                                               \
   const double xb = CGB_W(cur.y, j, k);                                                    \
-  R = __dadd_rn(xb, xb);                                                                   \
+  R = d_twice(xb);                                                                         \
 } break;                                                                                   \
 case (LK_ASSIGN << 2) | 1u: R = CGB_W(cur.y, j, k); break;                                 \
 case (LK_IFZ << 2) | 2u: R = d_iszero(Q0[i][j]) ? 0.0 : CGB_W(cur.z, j, k); break;
@@ -748,10 +748,10 @@ __device__ __forceinline__ void adjoint_walk(const uint4* st, int ngr, const dou
             case (LK_TWICE << 2) | 1u:
               CGB_J {
                 double& w1 = wj<IPT>(wb, cur.y, j);
-                w1 = __dadd_rn(w1, __dadd_rn(sd[j], sd[j]));
+                w1 = __dadd_rn(w1, d_twice(sd[j]));
               }
               break;
-            case (LK_TWICE << 2) | 3u: CGB_J wj<IPT>(wb, cur.y, j) = __dadd_rn(sd[j], sd[j]); break;
+            case (LK_TWICE << 2) | 3u: CGB_J wj<IPT>(wb, cur.y, j) = d_twice(sd[j]); break;
             default: break;  // operand b receives nothing
           }
           // contribution to operand c
