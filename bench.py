@@ -283,7 +283,22 @@ def cpu_baseline(F, args, aseeds, workload, budget_s=12.0):
 
 
 # ---- native arm ----------------------------------------------------------------------------------
-def mixed_component(torch, R, stream, reps=3, total=1 << 20):
+def _seed_block(nnz_in, flat_color, n_colors, m):
+    """Dense forward seeds of a colouring for the oracle: one (n_colors, nnz, m) array per
+    input, direction d = 1 on the nonzeros of colour d."""
+    out, off = [], 0
+    for k in nnz_in:
+        blk = np.zeros((n_colors, k, m))
+        for q in range(k):
+            c = flat_color[off + q]
+            if c >= 0:
+                blk[c, q, :] = 1.0
+        out.append(blk)
+        off += k
+    return out
+
+
+def mixed_component(torch, R, stream, reps=3, total=1 << 20, cpu=False):
     """Mixed-size batch: eight random-DAG tapes (200..20000 nodes, 64 inputs, 16 outputs)
     and work items with log-normal instance counts (median 4096, sigma 1.5) up to 2^20
     instances, each evaluated with the adjoint of the sum of its outputs: one launch pair per
@@ -335,7 +350,22 @@ def mixed_component(torch, R, stream, reps=3, total=1 << 20):
         t.sync()
         t._scratch = None
     counts = [n for _, n, _ in items]
-    return {"instances": total, "items": len(items),
+    cpu_rate = None
+    if cpu:
+        # the oracle port on the host cores: every item on 1/64 of its instances
+        import oracle as O
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        sampled = 0
+        for k, n, sd in items:
+            m = max(1, n // 64)
+            args = W.dag_inputs(m, n_in=64, seed=sd)
+            O.reverse(funs[k].tape, args, [np.ones((1, 16, m))], m, threads)
+            sampled += m
+        cpu_rate = {"value": sampled / (time.perf_counter() - t0), "unit": UNIT,
+                    "cores": threads, "kind": "port",
+                    "sample": "1/64 of every item's instances (%d), value + adjoint" % sampled}
+    return {"instances": total, "items": len(items), "cpu_port": cpu_rate,
             "tape_instructions": [f.tape.n_instr for f in funs],
             "item_instances_median": int(np.median(counts)), "item_instances_max": max(counts),
             "plain_ms": ms_plain, "persistent_ms": ms_batch,
@@ -378,7 +408,7 @@ def rollout_autograd_component(torch, stream, n=1 << 20, reps=2):
             "peak_device_gb": torch.cuda.max_memory_allocated() / 1e9}
 
 
-def mpc_sparse_component(torch, stream, n=4096, intervals=100, reps=3):
+def mpc_sparse_component(torch, stream, n=4096, intervals=100, reps=3, cpu=False):
     """Scenario MPC: the quadcopter multiple-shooting NLP (100 intervals, 1612 decision
     variables, 1212 constraints) over 4096 scenarios: the constraint Jacobian by uni-coloured
     forward sweeps and the Lagrangian Hessian by star-coloured forward sweeps over the
@@ -425,7 +455,23 @@ def mpc_sparse_component(torch, stream, n=4096, intervals=100, reps=3):
     ms_batch = timeit(step_batch)
     same = bool(torch.equal(vj.view(torch.int64), J(args, stream=stream).view(torch.int64)) and
                 torch.equal(vh.view(torch.int64), H(args, stream=stream).view(torch.int64)))
+    cpu_rate = None
+    if cpu:
+        # the oracle port on the host cores: the same coloured forward sweeps on 64 scenarios
+        import oracle as O
+        threads = os.cpu_count() or 1
+        m = 64
+        sub = [a[:, :m].cpu().numpy() for a in args]
+        sj = _seed_block(J.tape.nnz_in, J._flat, J.n_colors, m)
+        sh = _seed_block(H.tape.nnz_in, H._flat, H.n_colors, m)
+        t0 = time.perf_counter()
+        O.forward(J.tape.tape, sub, sj, m, threads)
+        O.forward(H.tape.tape, sub, sh, m, threads)
+        cpu_rate = {"value": m / (time.perf_counter() - t0), "unit": "scenarios/s",
+                    "cores": threads, "kind": "port",
+                    "sample": "%d scenarios, same coloured forward sweeps" % m}
     return {"scenarios": n, "intervals": intervals, "decision_variables": F.tape.nnz_in[0],
+            "cpu_port": cpu_rate,
             "constraints": F.tape.nnz_out[0], "lagrangian_instructions": F.tape.n_instr,
             "gradient_instructions": H.gradient_function.tape.n_instr,
             "jacobian_nnz": J.pattern.nnz, "jacobian_colors": J.n_colors,
@@ -557,9 +603,10 @@ def run_native(a):
     ct.sync()
 
     if not a.no_mixed:
-        comps["mixed_batch"] = mixed_component(torch, R, stream)
+        cpu = not a.no_cpu and rank == 0
+        comps["mixed_batch"] = mixed_component(torch, R, stream, cpu=cpu)
         comps["rollout100_autograd"] = rollout_autograd_component(torch, stream)
-        comps["mpc_sparse_hessian"] = mpc_sparse_component(torch, stream)
+        comps["mpc_sparse_hessian"] = mpc_sparse_component(torch, stream, cpu=cpu)
 
     # roofline of the dominant kernel family (device time from the per-launch events)
     weights = load_weights()
