@@ -1842,6 +1842,11 @@ struct BatchHost {
   int n_units = 0;
   int szw = 1, pmax = 0, grid = 1;
   size_t smem = 0;
+  // work-vector residence: 0 shared memory, 1 global memory (grid_gw CTAs), -1 not tuned yet
+  int residence = -1;
+  int forced = 0;  // 0 tune, 1 global memory, 2 shared memory
+  int grid_gw = 1;
+  unsigned char* d_gw = nullptr;
   int device = 0;
   cudaStream_t stream = nullptr;  // owned: graph capture needs a non-legacy stream
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
@@ -1854,6 +1859,7 @@ struct BatchHost {
     cudaFree(d_units);
     cudaFree(d_counter);
     cudaFree(d_flags);
+    cudaFree(d_gw);
     for (double* p : d_tile_partials) cudaFree(p);
     if (ev_in) cudaEventDestroy(ev_in);
     if (ev_out) cudaEventDestroy(ev_out);
@@ -1988,15 +1994,25 @@ int batch_prepare(BatchHost& b) {
     return cuda_fail(e, "cudaMalloc(counter)");
   b.n_units = static_cast<int>(ulist.size());
   b.smem = static_cast<size_t>(b.szw) * 256;
-  if (b.smem > static_cast<size_t>(max_smem_optin()))
-    return fail(CASADI_GB300_ERR_UNSUPPORTED, "batch work vector of %d slots does not fit", b.szw);
-  const int occ = std::max(1, occupancy_batch(b.smem, b.n_flags > 0));
+  const int occ = b.smem <= static_cast<size_t>(max_smem_optin())
+                      ? std::max(1, occupancy_batch(b.smem, b.n_flags > 0, false))
+                      : 1;
   b.grid = std::max(1, std::min(sm_count() * occ, std::max(1, b.n_units)));
+  // global-memory work vectors: residency capped by registers (and at 8 CTAs per SM, which
+  // bounds the per-CTA partial scratch the caller provides)
+  const int occ_gw = std::max(1, std::min(8, occupancy_batch(0, b.n_flags > 0, true)));
+  b.grid_gw = std::max(1, std::min(sm_count() * occ_gw, std::max(1, b.n_units)));
+  cudaFree(b.d_gw);
+  b.d_gw = nullptr;
+  const size_t gw_bytes = static_cast<size_t>(b.grid_gw) * b.szw * 256;
+  if ((e = cudaMalloc(&b.d_gw, std::max<size_t>(gw_bytes, 256))) != cudaSuccess)
+    return cuda_fail(e, "cudaMalloc(batch work vectors)");
+  b.residence = b.forced == 1 ? 1 : (b.forced == 2 ? 0 : -1);
   b.dirty = false;
   return 0;
 }
 
-int batch_enqueue(BatchHost& b, void* scratch, cudaStream_t s) {
+int batch_enqueue(BatchHost& b, void* scratch, cudaStream_t s, bool gw) {
   cudaError_t e = cudaMemsetAsync(b.d_counter, 0, 2 * sizeof(unsigned), s);
   if (e == cudaSuccess && b.n_flags)
     e = cudaMemsetAsync(b.d_flags, 0, b.n_flags * sizeof(unsigned), s);
@@ -2009,7 +2025,9 @@ int batch_enqueue(BatchHost& b, void* scratch, cudaStream_t s) {
   a.err = b.d_counter + 1;
   a.scratch = static_cast<double*>(scratch);
   a.scratch_stride = static_cast<long long>(b.pmax) * 32;
-  e = launch_batch(a, b.grid, b.smem, b.n_flags > 0, s);
+  a.wglob = gw ? b.d_gw : nullptr;
+  a.wglob_stride = static_cast<long long>(b.szw) * 256;
+  e = launch_batch(a, gw ? b.grid_gw : b.grid, b.smem, b.n_flags > 0, gw, s);
   if (e != cudaSuccess) return cuda_fail(e, "batch launch");
   return 0;
 }
@@ -2099,6 +2117,19 @@ int casadi_gb300_batch_add_jacobian_colored(int batch, int id, int64_t n, int64_
   return static_cast<int>(b->items.size()) - 1;
 }
 
+int casadi_gb300_batch_set_residence(int batch, int mode) {
+  BatchHost* b = get_batch(batch);
+  if (!b) return fail(CASADI_GB300_ERR_ID, "no batch %d", batch);
+  if (mode < 0 || mode > 2) return fail(CASADI_GB300_ERR_ARG, "residence must be 0, 1 or 2");
+  b->forced = mode;
+  b->residence = mode == 1 ? 1 : (mode == 2 ? 0 : -1);
+  if (b->exec) {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  return 0;
+}
+
 int casadi_gb300_batch_status(int batch) {
   BatchHost* b = get_batch(batch);
   if (!b) return fail(CASADI_GB300_ERR_ID, "no batch %d", batch);
@@ -2117,7 +2148,7 @@ int casadi_gb300_batch_scratch_size(int batch, size_t* bytes) {
   if (!b) return fail(CASADI_GB300_ERR_ID, "no batch %d", batch);
   if (!bytes) return fail(CASADI_GB300_ERR_ARG, "bad arguments");
   if (int rc = batch_prepare(*b)) return rc;
-  *bytes = static_cast<size_t>(b->grid) * b->pmax * 32 * 8;
+  *bytes = static_cast<size_t>(std::max(b->grid, b->grid_gw)) * b->pmax * 32 * 8;
   return 0;
 }
 
@@ -2129,7 +2160,7 @@ int casadi_gb300_batch_run(int batch, void* scratch, size_t scratch_bytes, int u
   cudaGetDevice(&cur);
   if (cur != b->device) return fail(CASADI_GB300_ERR_ARG, "batch lives on device %d", b->device);
   if (int rc = batch_prepare(*b)) return rc;
-  const size_t need = static_cast<size_t>(b->grid) * b->pmax * 32 * 8;
+  const size_t need = static_cast<size_t>(std::max(b->grid, b->grid_gw)) * b->pmax * 32 * 8;
   if (need > 0 && (!scratch || scratch_bytes < need))
     return fail(CASADI_GB300_ERR_SCRATCH, "batch needs %zu bytes of scratch, got %zu", need,
                 scratch_bytes);
@@ -2138,6 +2169,29 @@ int casadi_gb300_batch_run(int batch, void* scratch, size_t scratch_bytes, int u
   cudaError_t e = cudaEventRecord(b->ev_in, caller);
   if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->ev_in, 0);
   if (e != cudaSuccess) return cuda_fail(e, "batch ordering");
+  if (b->residence < 0) {
+    // tune the work-vector residence once per batch layout: both runs produce the results
+    if (g_autotune && !capturing(caller)) {
+      float ms[2] = {0, 0};
+      for (int gw = 0; gw < 2; ++gw) {
+        if (gw == 0 && b->smem > static_cast<size_t>(max_smem_optin())) {
+          ms[0] = 3.0e38f;  // the shared-memory instance cannot hold this batch
+          continue;
+        }
+        int rc = 0;
+        if (int trc = time_once(b->stream, [&] {
+              rc = batch_enqueue(*b, scratch, b->stream, gw == 1);
+              return cudaSuccess;
+            }, &ms[gw]))
+          return trc;
+        if (rc) return rc;
+      }
+      b->residence = ms[1] < ms[0] ? 1 : 0;
+    } else {
+      b->residence = b->smem <= static_cast<size_t>(max_smem_optin()) ? 0 : 1;
+    }
+  }
+  const bool gw = b->residence == 1;
   if (use_graph) {
     if (b->exec && b->exec_scratch != scratch) {
       cudaGraphExecDestroy(b->exec);
@@ -2147,7 +2201,7 @@ int casadi_gb300_batch_run(int batch, void* scratch, size_t scratch_bytes, int u
       cudaGraph_t g = nullptr;
       e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
       if (e != cudaSuccess) return cuda_fail(e, "begin capture");
-      int rc = batch_enqueue(*b, scratch, b->stream);
+      int rc = batch_enqueue(*b, scratch, b->stream, gw);
       e = cudaStreamEndCapture(b->stream, &g);
       if (rc) {
         if (g) cudaGraphDestroy(g);
@@ -2164,7 +2218,7 @@ int casadi_gb300_batch_run(int batch, void* scratch, size_t scratch_bytes, int u
   } else {
     int rc = 0;
     e = timed(F_BATCH, b->stream, [&] {
-      rc = batch_enqueue(*b, scratch, b->stream);
+      rc = batch_enqueue(*b, scratch, b->stream, gw);
       return cudaSuccess;
     });
     if (rc) return rc;

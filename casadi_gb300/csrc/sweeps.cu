@@ -926,12 +926,14 @@ __device__ __forceinline__ bool wait_tile(const unsigned* flag, unsigned* err) {
 }
 
 // kSplit: the batch has split items (per-tile record units and per-direction units); batches
-// without any run the instance that holds only the whole-unit path.
-template <bool kSplit>
+// without any run the instance that holds only the whole-unit path. GW: the work vector lives
+// in global memory (per-CTA blocks) instead of shared memory, so residency is not capped by
+// the longest tape's work vector.
+template <bool kSplit, bool GW>
 __global__ void __launch_bounds__(32, 16) k_batch(const __grid_constant__ BatchArgs b) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x;
-  unsigned char* wb = smem + lane * 8;
+  unsigned char* wb = (GW ? b.wglob + blockIdx.x * b.wglob_stride : smem) + lane * 8;
   double* const pcta = b.scratch + static_cast<size_t>(blockIdx.x) * b.scratch_stride + lane;
   for (;;) {
     unsigned u = 0;
@@ -1268,20 +1270,27 @@ cudaError_t launch_gather(long long n, long long ld, int count, const long long*
   return cudaGetLastError();
 }
 
-cudaError_t launch_batch(const BatchArgs& b, int grid, size_t smem, bool split, cudaStream_t s) {
+cudaError_t launch_batch(const BatchArgs& b, int grid, size_t smem, bool split, bool gw,
+                         cudaStream_t s) {
   // the attribute is raised once to the device maximum, so a captured graph never depends on
   // a later call lowering it
   static const cudaError_t set0 = cudaFuncSetAttribute(
-      k_batch<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_optin());
+      k_batch<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_optin());
   static const cudaError_t set1 = cudaFuncSetAttribute(
-      k_batch<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_optin());
+      k_batch<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_optin());
   if (set0 != cudaSuccess) return set0;
   if (set1 != cudaSuccess) return set1;
   if (smem > static_cast<size_t>(max_smem_optin())) return cudaErrorInvalidValue;
-  if (split)
-    k_batch<true><<<grid, 32, smem, s>>>(b);
-  else
-    k_batch<false><<<grid, 32, smem, s>>>(b);
+  if (gw) {
+    if (split)
+      k_batch<true, true><<<grid, 32, 0, s>>>(b);
+    else
+      k_batch<false, true><<<grid, 32, 0, s>>>(b);
+  } else if (split) {
+    k_batch<true, false><<<grid, 32, smem, s>>>(b);
+  } else {
+    k_batch<false, false><<<grid, 32, smem, s>>>(b);
+  }
   return cudaGetLastError();
 }
 
@@ -1320,17 +1329,20 @@ static int occ_of(K kernel, int block, size_t smem) {
   return n;
 }
 
-int occupancy_batch(size_t smem, bool split) {
+int occupancy_batch(size_t smem, bool split, bool gw) {
+  if (gw) return split ? occ_of(k_batch<true, true>, 32, 0) : occ_of(k_batch<false, true>, 32, 0);
   int n = 0;
   if (split) {
-    if (cudaFuncSetAttribute(k_batch<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (cudaFuncSetAttribute(k_batch<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              max_smem_optin()) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch<true>, 32, smem) != cudaSuccess)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch<true, false>, 32, smem) !=
+            cudaSuccess)
       return 0;
   } else {
-    if (cudaFuncSetAttribute(k_batch<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (cudaFuncSetAttribute(k_batch<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              max_smem_optin()) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch<false>, 32, smem) != cudaSuccess)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch<false, false>, 32, smem) !=
+            cudaSuccess)
       return 0;
   }
   return n;

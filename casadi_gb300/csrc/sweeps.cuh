@@ -101,6 +101,8 @@ struct BatchArgs {
   unsigned* err;            // kErr* bits (zeroed before each launch)
   double* scratch;          // partials of whole units, scratch_stride doubles per CTA
   long long scratch_stride;
+  unsigned char* wglob;     // global work vectors (GW instance): CTA b at wglob + b*wglob_stride
+  long long wglob_stride;
 };
 
 constexpr int kGwBlock = 128;   // threads per CTA of the global-work-vector value sweeps
@@ -109,8 +111,9 @@ int occupancy_gw_sp();           // ... of the sparsity sweeps
 int occupancy_gw_dir(bool adjoint);  // ... of the derivative sweeps (one warp per CTA)
 cudaError_t launch_gather(long long n, long long ld, int count, const long long* src_row,
                           const double* src, double* dst, cudaStream_t s);
-cudaError_t launch_batch(const BatchArgs& b, int grid, size_t smem, bool split, cudaStream_t s);
-int occupancy_batch(size_t smem, bool split);
+cudaError_t launch_batch(const BatchArgs& b, int grid, size_t smem, bool split, bool gw,
+                         cudaStream_t s);
+int occupancy_batch(size_t smem, bool split, bool gw);
 
 // Error bits written to TapeView::err.
 constexpr int kErrWaitTimeout = 1;   // a bounded wait on a staged chunk ran out

@@ -97,6 +97,7 @@ def load(path=None):
         "casadi_gb300_batch_add": (cint, [cint, cint, i64, i64, cint, vp, vp, vp, vp]),
         "casadi_gb300_batch_scratch_size": (cint, [cint, vp]),
         "casadi_gb300_batch_status": (cint, [cint]),
+        "casadi_gb300_batch_set_residence": (cint, [cint, cint]),
         "casadi_gb300_batch_add_jacobian_colored": (cint, [cint, cint, i64, i64, cint, vp, vp, vp,
                                                            vp]),
         "casadi_gb300_batch_run": (cint, [cint, vp, sz, cint, vp]),
@@ -470,6 +471,10 @@ class Batch:
         b = ct.c_size_t()
         check(load().casadi_gb300_batch_scratch_size(self.id, ct.byref(b)))
         return b.value
+
+    def set_residence(self, mode):
+        """Work vectors: 0 tuned (default), 1 global memory, 2 shared memory."""
+        check(load().casadi_gb300_batch_set_residence(self.id, mode))
 
     def status(self):
         """Wait for the last run and raise if a unit of it failed on the device."""

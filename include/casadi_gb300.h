@@ -289,6 +289,9 @@ CASADI_GB300_API int casadi_gb300_batch_add_jacobian_colored(int batch, int id, 
                            int64_t ld, int n_colors, const int* color,
                            const double* const* arg, double* const* res, double* const* comp);
 CASADI_GB300_API int casadi_gb300_batch_scratch_size(int batch, size_t* bytes);
+/* Work-vector residence of a batch's launch: 0 (default) the faster of shared and global
+ * memory, timed on the first run; 1 global memory; 2 shared memory. Same results either way. */
+CASADI_GB300_API int casadi_gb300_batch_set_residence(int batch, int mode);
 /* Waits for the batch's stream and reports a device-side failure of its last run (a
  * direction unit whose tile's record unit did not finish within its bounded wait). */
 CASADI_GB300_API int casadi_gb300_batch_status(int batch);

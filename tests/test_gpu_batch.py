@@ -131,3 +131,29 @@ def test_batch_rejects_small_scratch_and_bad_ids(gpu_lib):
     st = lib.casadi_gb300_batch_run(b.id, None, 0, 0, ct.c_void_p(0))
     assert st == -5
     assert lib.casadi_gb300_batch_add(b.id, 999999, 1, 1, 0, None, None, None, None) == -1
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_batch_residence_gives_the_same_bits(gpu_lib, mode):
+    """The batch with its work vectors forced into global (1) or shared (2) memory."""
+    items = _items()
+    tapes = {}
+    b = R.Batch()
+    b.set_residence(mode)
+    queued = []
+    for k, (f, n, nadj, args) in enumerate(items):
+        t = tapes.setdefault(id(f), R.CudaTape(f))
+        dargs = [_cuda(a) for a in args]
+        dseeds = [_cuda(s) for s in _seeds(f, n, nadj, k)] if nadj else None
+        res, asens = b.add(t, dargs, dseeds)
+        queued.append((t, dargs, dseeds, res, asens))
+    b.run(graph=True)
+    b.status()
+    for t, dargs, dseeds, res, asens in queued:
+        if dseeds is None:
+            for g, w in zip(res, t.eval(dargs)):
+                assert same_bits(g.cpu().numpy(), w.cpu().numpy()).all()
+        else:
+            want_r, want_s = t.reverse(dargs, dseeds)
+            for g, w in zip(res + asens, want_r + want_s):
+                assert same_bits(g.cpu().numpy(), w.cpu().numpy()).all()
