@@ -117,7 +117,7 @@ struct Tape {
   int ref_sz_w = 0;  // the work-vector length the tape came with (sz_w: after scheduling)
   int residence = 0;  // work vector: 0 auto (shared memory when it fits, value sweeps tuned),
                       // 1 global memory, 2 shared memory whenever it fits
-  int primal_tuned[4] = {-1, -1, -1, -1};  // per PrimalKind: 0 shared, 1 global (autotuned)
+  int primal_tuned[5] = {-1, -1, -1, -1, -1};  // per PrimalKind: 0 shared, 1 global (tuned)
   // global work vector: per-CTA blocks, grown on demand; uses on different streams are
   // ordered by gw_event
   std::mutex gw_mtx;
@@ -206,7 +206,7 @@ std::vector<std::unique_ptr<Mem>> g_mems;
 
 // ---- optional per-launch timing (CUDA events on the launch stream) -------------------------
 enum Family { F_EVAL = 0, F_RECORD, F_TANGENT, F_ADJOINT, F_SP_FORWARD, F_SP_REVERSE, F_BATCH,
-              F_COUNT };
+              F_ACTIVITY, F_COUNT };
 struct ProfEntry {
   int family;
   cudaEvent_t start, stop;
@@ -641,17 +641,18 @@ int time_once(cudaStream_t s, F fn, float* ms) {
 // instances as the scratch holds. `in/out/seed/sens` address the whole instance range.
 // Value-type sweeps (eval, record, both sparsity sweeps) over one instance range: the shared-
 // memory kernels with the tape's block size, or the global-work-vector kernels.
-enum PrimalKind { PK_EVAL = 0, PK_RECORD, PK_SP_FORWARD, PK_SP_REVERSE };
+enum PrimalKind { PK_EVAL = 0, PK_RECORD, PK_SP_FORWARD, PK_SP_REVERSE, PK_ACTIVITY };
 
 int primal_launch(Tape& t, SweepArgs& a, long long m, PrimalKind kind, cudaStream_t s) {
-  static const int fam[] = {F_EVAL, F_RECORD, F_SP_FORWARD, F_SP_REVERSE};
+  static const int fam[] = {F_EVAL, F_RECORD, F_SP_FORWARD, F_SP_REVERSE, F_ACTIVITY};
   static const char* what[] = {"eval launch", "record sweep launch", "sp_forward launch",
-                               "sp_reverse launch"};
+                               "sp_reverse launch", "activity launch"};
   auto go = [&](int grid) {
     switch (kind) {
       case PK_EVAL: return launch_eval(a, grid, s);
       case PK_RECORD: return launch_record(a, grid, s);
       case PK_SP_FORWARD: return launch_sp_forward(a, grid, s);
+      case PK_ACTIVITY: return launch_activity(a, grid, s);
       default: return launch_sp_reverse(a, grid, s);
     }
   };
@@ -1457,6 +1458,19 @@ int casadi_gb300_sp_forward(int id, int64_t n, int64_t ld, const uint64_t* const
   fill_io(a.in, t->n_in, vptrs(arg), t->nnz_in, ld, false);
   fill_io(a.out, t->n_out, vptrs(res), t->nnz_out, ld, false);
   return primal_launch(*t, a, n, PK_SP_FORWARD, static_cast<cudaStream_t>(stream));
+}
+
+int casadi_gb300_eval_activity(int id, int64_t n, int64_t ld, const uint64_t* const* arg,
+                               uint64_t* const* res, void* stream) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  if (int rc = check_device(*t)) return rc;
+  if (int rc = check_n(n, ld)) return rc;
+  if (n == 0) return 0;
+  SweepArgs a = base_args(*t, n, 0);
+  fill_io(a.in, t->n_in, vptrs(arg), t->nnz_in, ld, false);
+  fill_io(a.out, t->n_out, vptrs(res), t->nnz_out, ld, false);
+  return primal_launch(*t, a, n, PK_ACTIVITY, static_cast<cudaStream_t>(stream));
 }
 
 int casadi_gb300_sp_reverse(int id, int64_t n, int64_t ld, uint64_t* const* arg,

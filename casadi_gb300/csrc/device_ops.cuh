@@ -110,6 +110,42 @@ __host__ __device__ __forceinline__ bool carries_d1(unsigned op) {
   return is_binary(op) && ((partial_mask(op) & 2u) || const_d1(op) != 0.0);
 }
 
+// Activity analysis (SXFunction::eval_activity, casadi/core/sx_function.cpp:1684-1718): a
+// result is inactive (0) only when the op is known to give zero for its zero operands, else
+// active (all bits set). One bit per device opcode, from the reference's zero checkers
+// (calculus.hpp:485-540):
+//   kZeroFirst   f(0, y) == 0 for every y (F0XChecker)
+//   kZeroSecond  f(x, 0) == 0 for every x (FX0Checker)
+//   kZeroBoth    f(0, 0) == 0 (F00Checker: either of the above, or ADD SUB FMIN FMAX AND OR
+//                COPYSIGN LT HYPOT)
+constexpr u64 op_bit(unsigned op) { return 1ull << op; }
+constexpr u64 kZeroFirst =
+    op_bit(D_ASSIGN) | op_bit(D_MUL) | op_bit(D_DIV) | op_bit(D_NEG) | op_bit(D_SQRT) |
+    op_bit(D_SQ) | op_bit(D_TWICE) | op_bit(D_SIN) | op_bit(D_TAN) | op_bit(D_ATAN) |
+    op_bit(D_ASIN) | op_bit(D_FLOOR) | op_bit(D_CEIL) | op_bit(D_FMOD) | op_bit(D_REMAINDER) |
+    op_bit(D_FABS) | op_bit(D_SIGN) | op_bit(D_COPYSIGN) | op_bit(D_ERF) | op_bit(D_SINH) |
+    op_bit(D_TANH) | op_bit(D_ASINH) | op_bit(D_ATANH) | op_bit(D_ERFINV) | op_bit(D_AND) |
+    op_bit(D_IF_ELSE_ZERO) | op_bit(D_LOG1P) | op_bit(D_EXPM1);
+constexpr u64 kZeroSecond = op_bit(D_MUL) | op_bit(D_AND) | op_bit(D_IF_ELSE_ZERO);
+constexpr u64 kZeroBoth = kZeroFirst | kZeroSecond | op_bit(D_ADD) | op_bit(D_SUB) |
+                          op_bit(D_FMIN) | op_bit(D_FMAX) | op_bit(D_OR) | op_bit(D_COPYSIGN) |
+                          op_bit(D_LT) | op_bit(D_HYPOT);
+
+// Activity of an arithmetic result from its operands' activity words x (first) and y (second;
+// ignored for unary ops).
+__host__ __device__ __forceinline__ u64 activity_of(unsigned op, bool binary, u64 x, u64 y) {
+  u64 zero_if;
+  if (!binary) {
+    if (x) return ~0ull;
+    zero_if = kZeroFirst;
+  } else if (x && y) {
+    return ~0ull;
+  } else {
+    zero_if = x ? kZeroSecond : y ? kZeroFirst : kZeroBoth;
+  }
+  return ((zero_if >> op) & 1ull) ? 0ull : ~0ull;
+}
+
 #ifdef __CUDACC__
 constexpr unsigned long long kSignBit = 0x8000000000000000ull;
 

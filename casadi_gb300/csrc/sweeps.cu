@@ -17,6 +17,7 @@
 //   k_tangent<DW>       forward-mode directions       ad_forward, numeric (sx_function.cpp:1318-1364)
 //   k_adjoint<DW>       adjoint directions            ad_reverse, numeric (sx_function.cpp:1454-1560)
 //   k_sp_forward<BS>    bvec_t OR-propagation         sp_forward (sx_function.cpp:1657-1682)
+//   k_sp_forward<BS,GW,true>  activity propagation    eval_activity (sx_function.cpp:1684-1718)
 //   k_sp_reverse<BS>    bvec_t reverse propagation    sp_reverse (sx_function.cpp:1742-1782)
 //
 // Waits on the staging barriers are bounded: after ~1 s without completion a kernel sets
@@ -999,7 +1000,9 @@ __global__ void __launch_bounds__(32, 16) k_batch(const __grid_constant__ BatchA
 // ---------------------------------------------------------------------------------------------
 // bvec_t sparsity sweeps (uint64 bit sets, 64 directions at once).
 // ---------------------------------------------------------------------------------------------
-template <int BS, bool GW = false>
+// ACT: the activity sweep (SXFunction::eval_activity, sx_function.cpp:1684-1718) on the same
+// walk: constants are active when nonzero, arithmetic results follow activity_of.
+template <int BS, bool GW = false, bool ACT = false>
 __global__ void __launch_bounds__(BS) k_sp_forward(const __grid_constant__ SweepArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
   u64* ring = reinterpret_cast<u64*>(smem);
@@ -1021,7 +1024,7 @@ __global__ void __launch_bounds__(BS) k_sp_forward(const __grid_constant__ Sweep
         case D_NOP:
           break;
         case D_CONST:
-          w[A * BS + tid] = 0;
+          w[A * BS + tid] = ACT && __ldg(a.t.consts + B) != 0.0 ? ~0ull : 0ull;
           break;
         case D_INPUT: {
           const IoDesc& d = a.in[B];
@@ -1034,7 +1037,10 @@ __global__ void __launch_bounds__(BS) k_sp_forward(const __grid_constant__ Sweep
           if (active && d.ptr) static_cast<u64*>(d.ptr)[io_off(d, 0, C, ig)] = w[B * BS + tid];
         } break;
         default:
-          w[A * BS + tid] = w[B * BS + tid] | w[C * BS + tid];
+          if (ACT)
+            w[A * BS + tid] = activity_of(op, dec_binary(ins), w[B * BS + tid], w[C * BS + tid]);
+          else
+            w[A * BS + tid] = w[B * BS + tid] | w[C * BS + tid];
       }
     });
     if (!ok) return;
@@ -1164,6 +1170,13 @@ cudaError_t launch_sp_forward(const SweepArgs& a, int grid, cudaStream_t s) {
   if (a.wglob) return launch_k(k_sp_forward<kGwBlock, true>, grid, kGwBlock, kHeaderBytes, a, s);
   const size_t smem = smem_primal(a.t.sz_w, a.block);
   CGB_DISPATCH_BS(k_sp_forward)
+}
+
+cudaError_t launch_activity(const SweepArgs& a, int grid, cudaStream_t s) {
+  if (a.wglob)
+    return launch_k(k_sp_forward<kGwBlock, true, true>, grid, kGwBlock, kHeaderBytes, a, s);
+  const size_t smem = smem_primal(a.t.sz_w, a.block);
+  CGB_DISPATCH_BS(k_sp_forward, , false, true)
 }
 
 cudaError_t launch_sp_reverse(const SweepArgs& a, int grid, cudaStream_t s) {

@@ -144,6 +144,7 @@ cudaError_t launch_adjoint(const SweepArgs& a, int grid, int variant, cudaStream
 cudaError_t launch_adjoint_dense(const SweepArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_sp_forward(const SweepArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_sp_reverse(const SweepArgs& a, int grid, cudaStream_t s);
+cudaError_t launch_activity(const SweepArgs& a, int grid, cudaStream_t s);
 
 // Resident CTAs per SM for a given kernel family and shared-memory footprint.
 int occupancy_primal(int block, size_t smem);

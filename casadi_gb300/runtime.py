@@ -70,6 +70,7 @@ def load(path=None):
         "casadi_gb300_reverse": (cint, [cint, i64, i64, cint, vp, vp, vp, vp, vp, sz, vp]),
         "casadi_gb300_sp_forward": (cint, [cint, i64, i64, vp, vp, vp]),
         "casadi_gb300_sp_reverse": (cint, [cint, i64, i64, vp, vp, vp]),
+        "casadi_gb300_eval_activity": (cint, [cint, i64, i64, vp, vp, vp]),
         "casadi_gb300_sync": (cint, [cint, vp]),
         "casadi_gb300_checkout": (cint, []),
         "casadi_gb300_release": (cint, [cint]),
@@ -300,6 +301,35 @@ class CudaTape:
                                              _stream_handle(stream)))
         return res
 
+    def eval_activity(self, args, n=None, stream=None):
+        """Activity words of the outputs (SXFunction::eval_activity): args are int64 tensors
+        (nnz, n) of input activity words (nonzero: possibly nonzero input)."""
+        import torch
+        n = self._n(args) if n is None else n
+        res = self._outs(self.nnz_out, n, dtype=torch.int64)
+        check(load().casadi_gb300_eval_activity(self.id, n, n, _ptr_array(args),
+                                                _ptr_array(res), _stream_handle(stream)))
+        return res
+
+    def activity(self, masks):
+        """Function::activity over instances (casadi/core/function.cpp:1269-1294): ``masks``
+        is a bool array (nnz_in_total, n) of possibly-nonzero inputs; returns a bool array
+        (nnz_out_total, n) of possibly-nonzero outputs."""
+        import torch
+        masks = np.asarray(masks, dtype=bool)
+        if masks.ndim != 2 or masks.shape[0] != sum(self.nnz_in):
+            raise ValueError("activity: expected a mask of %d input nonzeros per instance"
+                             % sum(self.nnz_in))
+        n = masks.shape[1]
+        words = torch.from_numpy(np.where(masks, -1, 0).astype(np.int64)).cuda()
+        args, off = [], 0
+        for k in self.nnz_in:
+            args.append(words[off:off + k])
+            off += k
+        res = self.eval_activity(args, n=n)
+        return np.concatenate([r.cpu().numpy() != 0 for r in res], axis=0) if res else \
+            np.zeros((0, n), dtype=bool)
+
     def sp_reverse(self, args, res, n=None, stream=None):
         """In place: args |= propagated bits, res cleared (SXFunction::sp_reverse)."""
         n = self._n(args + res) if n is None else n
@@ -493,7 +523,8 @@ class Batch:
 N_TAN_VARIANTS = 5  # tangent-sweep kernel variants (forward, Jacobian)
 N_ADJ_VARIANTS = 5  # adjoint-sweep kernel variants
 
-FAMILIES = ("eval", "record", "tangent", "adjoint", "sp_forward", "sp_reverse", "batch")
+FAMILIES = ("eval", "record", "tangent", "adjoint", "sp_forward", "sp_reverse", "batch",
+            "activity")
 
 
 def profile(enable=True):

@@ -177,6 +177,15 @@ CASADI_GB300_API int casadi_gb300_sp_forward(int id, int64_t n, int64_t ld, cons
 CASADI_GB300_API int casadi_gb300_sp_reverse(int id, int64_t n, int64_t ld, uint64_t* const* arg,
                             uint64_t* const* res, void* stream);
 
+/* Activity analysis over n instances (SXFunction::eval_activity, sx_function.cpp:1684-1718;
+ * Function::eval_activity, function.cpp:1260-1267): arg words are the inputs' activity (a set
+ * bit: possibly nonzero), res receives the outputs'. A constant is active when nonzero; an
+ * arithmetic result is inactive only when its op gives zero for its inactive operands
+ * (F0X/FX0/F00 checkers, calculus.hpp:485-540), else all bits are set. Null arg reads zeros,
+ * null res is skipped. Layout as casadi_gb300_sp_forward. */
+CASADI_GB300_API int casadi_gb300_eval_activity(int id, int64_t n, int64_t ld,
+                            const uint64_t* const* arg, uint64_t* const* res, void* stream);
+
 /* Wait for all work on `stream` and report device-side error flags raised by sweeps of this
  * tape (bounded waits that ran out, malformed instructions). Clears the flags. */
 CASADI_GB300_API int casadi_gb300_sync(int id, void* stream);

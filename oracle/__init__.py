@@ -49,7 +49,7 @@ def lib():
         _lib.sxo_fun.argtypes = [ct.c_int, ct.c_double, ct.c_double]
         _lib.sxo_der.argtypes = [ct.c_int, ct.c_double, ct.c_double, ct.c_double, ct.c_void_p]
         for name in ("sxo_eval", "sxo_forward", "sxo_jacobian", "sxo_reverse",
-                     "sxo_sp_forward", "sxo_sp_reverse"):
+                     "sxo_sp_forward", "sxo_sp_reverse", "sxo_activity", "sxo_zero_checker"):
             getattr(_lib, name).restype = ct.c_int
     return _lib
 
@@ -191,6 +191,23 @@ def sp_reverse(tape, args, res, n, nthreads=1):
     return args, res
 
 
+def activity(tape, args, n, nthreads=1):
+    """SXFunction::eval_activity over n instances: uint64 activity words (nnz, n)."""
+    t = TapeArrays(tape)
+    args = _prep(args, np.uint64)
+    _check(args, tape.nnz_in, n, "activity words")
+    res = _outs(tape.nnz_out, n, dtype=np.uint64)
+    rc = lib().sxo_activity(ct.byref(t.struct), ct.c_long(n), _ptrs(args), _ptrs(res),
+                            ct.c_int(nthreads))
+    assert rc == 0
+    return res
+
+
+def zero_checker(which, op):
+    """0: f(0, y) == 0; 1: f(x, 0) == 0; 2: f(0, 0) == 0 (calculus.hpp:485-540)."""
+    return bool(lib().sxo_zero_checker(which, op))
+
+
 def fun(op, x, y):
     return lib().sxo_fun(op, x, y)
 
@@ -210,6 +227,22 @@ def ref_der(op, x, y, f):
     d = np.zeros(2)
     ref().ref_der(op, x, y, f, d.ctypes.data)
     return d
+
+
+def ref_zero_checker(which, op):
+    return bool(ref().ref_zero_checker(which, op))
+
+
+def ref_activity(tape, args, n):
+    t = TapeArrays(tape)
+    args = _prep(args, np.uint64)
+    res = _outs(tape.nnz_out, n, dtype=np.uint64)
+    rc = ref().ref_activity(ct.c_int(tape.n_instr), t.op.ctypes.data_as(ct.c_void_p),
+                            t.i0.ctypes.data_as(ct.c_void_p), t.i1.ctypes.data_as(ct.c_void_p),
+                            t.i2.ctypes.data_as(ct.c_void_p), t.d.ctypes.data_as(ct.c_void_p),
+                            ct.c_int(tape.sz_w), ct.c_long(n), _ptrs(args), _ptrs(res))
+    assert rc == 0
+    return res
 
 
 def ref_eval(tape, args, n):

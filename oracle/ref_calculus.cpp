@@ -6,6 +6,10 @@
 //   ref_fun / ref_der   casadi_math<double>::fun / der (calculus.hpp:1299-1439)
 //   ref_ndeps           casadi_math<double>::ndeps (calculus.hpp:1632-1647)
 //   ref_op_id           the numeric value of enum Operation members (calculus.hpp:60-218)
+//   ref_zero_checker    operation_checker<F0XChecker / FX0Checker / F00Checker>
+//                       (calculus.hpp:485-540, :1128-1131)
+//   ref_activity        SXFunction::eval_activity's instruction loop (sx_function.cpp:
+//                       1684-1718) driving the reference's own checkers
 //   ref_eval            SXFunction::eval's instruction loop (casadi/core/sx_function.cpp:110-124)
 //                       driving the reference's own CASADI_MATH_FUN_BUILTIN dispatch macro
 //   ref_forward / ref_jacobian / ref_reverse
@@ -55,6 +59,41 @@ int ref_op_id(const char* name) {
   ID(OP_REMAINDER)
 #undef ID
   return -1;
+}
+
+int ref_zero_checker(int which, int op) {
+  if (which == 0) return operation_checker<F0XChecker>(op) ? 1 : 0;
+  if (which == 1) return operation_checker<FX0Checker>(op) ? 1 : 0;
+  return operation_checker<F00Checker>(op) ? 1 : 0;
+}
+
+// Instance-minor layout as ref_eval.
+int ref_activity(int n_instr, const int* op, const int* i0, const int* i1, const int* i2,
+                 const double* d, int sz_w, long n, const uint64_t* const* arg,
+                 uint64_t* const* res) {
+  const uint64_t nz = ~static_cast<uint64_t>(0);
+  std::vector<uint64_t> w(sz_w > 0 ? sz_w : 1);
+  for (long i = 0; i < n; ++i) {
+    for (int k = 0; k < n_instr; ++k) {
+      switch (op[k]) {
+        case OP_CONST: w[i0[k]] = d[k] != 0 ? nz : 0; break;
+        case OP_PARAMETER: w[i0[k]] = nz; break;
+        case OP_INPUT: w[i0[k]] = arg[i1[k]] != nullptr ? arg[i1[k]][i2[k] * n + i] : 0; break;
+        case OP_OUTPUT: if (res[i0[k]] != nullptr) res[i0[k]][i2[k] * n + i] = w[i1[k]]; break;
+        default:
+          if (casadi_math<double>::ndeps(op[k]) == 1) {
+            w[i0[k]] = w[i1[k]] ? nz : (operation_checker<F0XChecker>(op[k]) ? 0 : nz);
+          } else {
+            const bool z0 = w[i1[k]] != 0, z1 = w[i2[k]] != 0;
+            if (!z0 && !z1) w[i0[k]] = operation_checker<F00Checker>(op[k]) ? 0 : nz;
+            else if (!z0) w[i0[k]] = operation_checker<F0XChecker>(op[k]) ? 0 : nz;
+            else if (!z1) w[i0[k]] = operation_checker<FX0Checker>(op[k]) ? 0 : nz;
+            else w[i0[k]] = nz;
+          }
+      }
+    }
+  }
+  return 0;
 }
 
 // Instance-minor layout: arg[j][k*n + i]; see oracle/sxvm.c.

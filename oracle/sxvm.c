@@ -14,6 +14,8 @@
  *   sxo_reverse         numeric analogue of SXFunction::ad_reverse (sx_function.cpp:1418-1560)
  *   sxo_sp_forward      SXFunction::sp_forward           (sx_function.cpp:1657-1682)
  *   sxo_sp_reverse      SXFunction::sp_reverse           (sx_function.cpp:1742-1782)
+ *   sxo_activity        SXFunction::eval_activity        (sx_function.cpp:1684-1718) with
+ *                       the zero checkers of calculus.hpp:485-540 (sxo_zero_checker)
  *
  * Data layout (the layout the CUDA sweeps use): instance-minor. Input j of instance i,
  * nonzero k lives at arg[j][k*n + i]; outputs likewise. A null arg[j] reads zeros, a null
@@ -493,6 +495,77 @@ int sxo_sp_reverse(const sxo_tape* t, long n, uint64_t* const* arg, uint64_t* co
               seed = w[i0]; w[i0] = 0;
               w[i1] |= seed;
               w[i2] |= seed;
+          }
+        }
+      }
+    }
+    free(w);
+  }
+  return err;
+}
+
+/* The reference's zero checkers (calculus.hpp:485-540). which = 0: f(0, y) == 0 for every y
+ * (F0XChecker); 1: f(x, 0) == 0 for every x (FX0Checker); 2: f(0, 0) == 0 (F00Checker). */
+int sxo_zero_checker(int which, int op) {
+  int first = 0, second = 0, both = 0;
+  switch (op) {
+    case SXO_ASSIGN: case SXO_DIV: case SXO_NEG: case SXO_SQRT: case SXO_SQ: case SXO_TWICE:
+    case SXO_SIN: case SXO_TAN: case SXO_ATAN: case SXO_ASIN: case SXO_FLOOR: case SXO_CEIL:
+    case SXO_FMOD: case SXO_REMAINDER: case SXO_FABS: case SXO_SIGN: case SXO_ERF:
+    case SXO_SINH: case SXO_TANH: case SXO_ASINH: case SXO_ATANH: case SXO_ERFINV:
+    case SXO_LOG1P: case SXO_EXPM1:
+      first = 1;
+      break;
+    case SXO_COPYSIGN:
+      first = both = 1;
+      break;
+    case SXO_MUL: case SXO_IF_ELSE_ZERO:
+      first = second = 1;
+      break;
+    case SXO_AND:
+      first = second = both = 1;
+      break;
+    case SXO_ADD: case SXO_SUB: case SXO_FMIN: case SXO_FMAX: case SXO_OR: case SXO_LT:
+    case SXO_HYPOT:
+      both = 1;
+      break;
+    default:
+      break;
+  }
+  if (which == 0) return first;
+  if (which == 1) return second;
+  return both || first || second;
+}
+
+int sxo_activity(const sxo_tape* t, long n, const uint64_t* const* arg, uint64_t* const* res,
+                 int nthreads) {
+  const uint64_t all = ~(uint64_t)0;
+  int err = 0;
+#pragma omp parallel num_threads(nthreads > 0 ? nthreads : 1)
+  {
+    uint64_t* w = (uint64_t*)malloc(sizeof(uint64_t) * (t->sz_w > 0 ? t->sz_w : 1));
+    if (!w) {
+#pragma omp atomic write
+      err = 1;
+    } else {
+#pragma omp for schedule(static)
+      for (long i = 0; i < n; ++i) {
+        for (int k = 0; k < t->n_instr; ++k) {
+          int op = t->op[k], i0 = t->i0[k], i1 = t->i1[k], i2 = t->i2[k];
+          switch (op) {
+            case SXO_CONST: w[i0] = t->d[k] != 0 ? all : 0; break;
+            case SXO_PARAMETER: w[i0] = all; break;
+            case SXO_INPUT: w[i0] = arg[i1] ? arg[i1][(long)i2 * n + i] : 0; break;
+            case SXO_OUTPUT: if (res[i0]) res[i0][(long)i2 * n + i] = w[i1]; break;
+            default:
+              if (sxo_ndeps(op) == 1) {
+                w[i0] = w[i1] ? all : (sxo_zero_checker(0, op) ? 0 : all);
+              } else {
+                int a = w[i1] != 0, b = w[i2] != 0;
+                int zero = a && b ? 0 : a ? sxo_zero_checker(1, op)
+                                          : b ? sxo_zero_checker(0, op) : sxo_zero_checker(2, op);
+                w[i0] = zero ? 0 : all;
+              }
           }
         }
       }

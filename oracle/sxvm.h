@@ -48,4 +48,7 @@ int sxo_sp_forward(const sxo_tape* t, long n, const uint64_t* const* arg, uint64
                    int nthreads);
 int sxo_sp_reverse(const sxo_tape* t, long n, uint64_t* const* arg, uint64_t* const* res,
                    int nthreads);
+int sxo_zero_checker(int which, int op);
+int sxo_activity(const sxo_tape* t, long n, const uint64_t* const* arg, uint64_t* const* res,
+                 int nthreads);
 #endif

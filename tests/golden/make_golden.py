@@ -3,13 +3,19 @@
 Run where the reference source tree is available (it builds oracle/_ref from the reference's
 casadi/core/calculus.hpp):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [ops] [enum] [tapes] [activity]   # default: all
 
 Fixtures:
   ops.npz        value and partials of every scalar op over a grid of special and ordinary
                  arguments: casadi_math<double>::fun/der (calculus.hpp:1299-1439) as compiled
                  from the reference header.
   enum.npz       the numeric ids of enum Operation (calculus.hpp:60-218).
+  activity.npz   the zero checkers of every op (operation_checker<F0XChecker/FX0Checker/
+                 F00Checker>, calculus.hpp:485-540, :1128-1131, as compiled) and the
+                 activity words of SXFunction::eval_activity's loop (sx_function.cpp:
+                 1684-1718) driving those checkers, on a tape that applies every op to every
+                 pair of active/inactive operands and on the tapes of tapes.npz, for seeded
+                 input activity words (zero, all ones and partial bit patterns).
   tapes.npz      the cart-pole step, the 20-step rollout and a small random DAG as tapes, with
                  seeded inputs, forward seeds and adjoint seeds, and the reference harness's
                  outputs: values (SXFunction::eval's loop over CASADI_MATH_FUN_BUILTIN),
@@ -29,6 +35,7 @@ sys.path.insert(0, ROOT)
 
 import oracle as O  # noqa: E402
 from casadi_gb300 import calculus as C  # noqa: E402
+from casadi_gb300 import sx as S  # noqa: E402
 from casadi_gb300 import workloads as W  # noqa: E402
 
 SPECIAL = [0.0, -0.0, 1.0, -1.0, 0.5, -0.5, 2.0, -2.0, 3.7, -3.7, 1e-300, -1e-300, 5e-324,
@@ -89,14 +96,113 @@ def tape_case(name, fun, args, nfwd_seed_dirs=None, nadj=1, seed=7):
     return out
 
 
-def main():
+def activity_ops_tape(seed=5, layer2=400):
+    """Every arithmetic op applied to every pair drawn from two inputs and the constants 0,
+    1.5, -0 and NaN, then ``layer2`` random ops over those results; every result is an
+    output nonzero, and the two inputs pass straight to a second output."""
+    rng = np.random.default_rng(seed)
+    ops, i0, i1, i2, d = [], [], [], [], []
+
+    def emit(op, a, b=0, c=0, v=0.0):
+        ops.append(op); i0.append(a); i1.append(b); i2.append(c); d.append(v)
+
+    emit(C.OP_INPUT, 0, 0, 0)
+    emit(C.OP_INPUT, 1, 0, 1)
+    for slot, v in ((2, 0.0), (3, 1.5), (4, -0.0), (5, math.nan)):
+        emit(C.OP_CONST, slot, v=v)
+    pool = list(range(6))
+    results = []
+    slot = 6
+    for op in sorted(C.ARITH_OPS):
+        pairs = [(a, b) for a in pool for b in pool] if op in C.BINARY_OPS else \
+            [(a, a) for a in pool]
+        for a, b in pairs:
+            emit(op, slot, a, b)
+            results.append(slot)
+            slot += 1
+    arith = sorted(C.ARITH_OPS)
+    for _ in range(layer2):
+        op = int(arith[rng.integers(len(arith))])
+        a = int(results[rng.integers(len(results))])
+        b = int(results[rng.integers(len(results))]) if op in C.BINARY_OPS else a
+        emit(op, slot, a, b)
+        results.append(slot)
+        slot += 1
+    for k, r in enumerate(results):
+        emit(C.OP_OUTPUT, 0, r, k)
+    emit(C.OP_OUTPUT, 1, 0, 0)
+    emit(C.OP_OUTPUT, 1, 1, 1)
+    return S.Tape(ops, i0, i1, i2, d, [2], [len(results), 2], slot)
+
+
+def activity_words(nnz, n, rng):
+    """Seeded activity words: zero, all ones, single bits and random partial patterns."""
+    kinds = rng.integers(0, 5, size=(nnz, n))
+    rand = rng.integers(0, 2**63, size=(nnz, n), dtype=np.int64).view(np.uint64)
+    out = np.zeros((nnz, n), np.uint64)
+    out[kinds == 1] = np.uint64(0xFFFFFFFFFFFFFFFF)
+    out[kinds == 2] = np.uint64(1)
+    out[kinds == 3] = np.uint64(1) << np.uint64(63)
+    out[kinds == 4] = rand[kinds == 4] | np.uint64(4)
+    return out
+
+
+def activity_case():
+    out = {}
+    ops = sorted(C.ARITH_OPS)
+    out["checker/op"] = np.array(ops, np.int32)
+    for w, name in enumerate(("zero_first", "zero_second", "zero_both")):
+        out["checker/" + name] = np.array([O.ref_zero_checker(w, op) for op in ops], bool)
+    rng = np.random.default_rng(77)
+    t = activity_ops_tape()
+    out.update({"ops/op": t.op, "ops/i0": t.i0, "ops/i1": t.i1, "ops/i2": t.i2, "ops/d": t.d,
+                "ops/nnz_in": np.array(t.nnz_in), "ops/nnz_out": np.array(t.nnz_out),
+                "ops/sz_w": np.array(t.sz_w)})
+    cases = [("ops", t, 300)]
+    z = np.load(os.path.join(HERE, "tapes.npz"))
+    for name in ("cartpole", "rollout", "dag"):
+        tt = S.Tape(z[name + "/op"], z[name + "/i0"], z[name + "/i1"], z[name + "/i2"],
+                    z[name + "/d"], z[name + "/nnz_in"].tolist(), z[name + "/nnz_out"].tolist(),
+                    int(z[name + "/sz_w"]))
+        cases.append((name, tt, 64))
+    for name, tt, n in cases:
+        args = [activity_words(k, n, rng) for k in tt.nnz_in]
+        # some instances with every input inactive
+        for a in args:
+            a[:, :3] = 0
+        res = O.ref_activity(tt, args, n)
+        for j, a in enumerate(args):
+            out["%s/act_arg%d" % (name, j)] = a
+        for j, r in enumerate(res):
+            out["%s/act_res%d" % (name, j)] = r
+    return out
+
+
+def main(which=None):
+    which = set(which or ("ops", "enum", "tapes", "activity"))
     O.build(ref=True)
     if not O.ref_available():
         raise SystemExit("the reference harness could not be built")
-    np.savez_compressed(os.path.join(HERE, "ops.npz"), **op_grid())
-    names = sorted(C.OP_NAMES.values())
-    ids = np.array([O.ref().ref_op_id(("OP_" + s).encode()) for s in names], np.int32)
-    np.savez_compressed(os.path.join(HERE, "enum.npz"), names=np.array(names), ids=ids)
+    written = []
+    if "ops" in which:
+        np.savez_compressed(os.path.join(HERE, "ops.npz"), **op_grid())
+        written.append("ops.npz")
+    if "enum" in which:
+        names = sorted(C.OP_NAMES.values())
+        ids = np.array([O.ref().ref_op_id(("OP_" + s).encode()) for s in names], np.int32)
+        np.savez_compressed(os.path.join(HERE, "enum.npz"), names=np.array(names), ids=ids)
+        written.append("enum.npz")
+    if "tapes" in which:
+        write_tapes()
+        written.append("tapes.npz")
+    if "activity" in which:
+        np.savez_compressed(os.path.join(HERE, "activity.npz"), **activity_case())
+        written.append("activity.npz")
+    for f in written:
+        print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")
+
+
+def write_tapes():
     tapes = {}
     tapes.update(tape_case("cartpole", W.cartpole_step(), W.cartpole_inputs(96, steps=1, seed=0),
                            nfwd_seed_dirs=3))
@@ -106,9 +212,7 @@ def main():
     tapes.update(tape_case("dag", W.random_dag(n_in=16, n_nodes=800, n_out=6, seed=3),
                            W.dag_inputs(40, n_in=16, seed=2), nfwd_seed_dirs=2))
     np.savez_compressed(os.path.join(HERE, "tapes.npz"), **tapes)
-    for f in ("ops.npz", "enum.npz", "tapes.npz"):
-        print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -136,3 +136,56 @@ def test_oracle_matches_reference_harness_exactly():
 
 def test_rtol_is_the_documented_tolerance():
     assert RTOL == 1e-13 and math.isfinite(RTOL)
+
+
+# ---- activity analysis (SXFunction::eval_activity) ------------------------------------------
+ACTIVITY_CASES = ("ops", "cartpole", "rollout", "dag")
+
+
+def _activity_tape(name):
+    if name == "ops":
+        return golden_tape(load_npz("activity.npz"), "ops")
+    return golden_tape(load_npz("tapes.npz"), name)
+
+
+def test_oracle_zero_checkers_vs_golden():
+    """The oracle's F0X/FX0/F00 tables equal the reference's operation_checker templates."""
+    z = load_npz("activity.npz")
+    for w, name in enumerate(("zero_first", "zero_second", "zero_both")):
+        for op, want in zip(z["checker/op"], z["checker/" + name]):
+            assert O.zero_checker(w, int(op)) == bool(want), (name, C.OP_NAMES[int(op)])
+
+
+@pytest.mark.parametrize("name", ACTIVITY_CASES)
+def test_oracle_activity_vs_golden(name):
+    z = load_npz("activity.npz")
+    t = _activity_tape(name)
+    args = golden_list(z, name, "act_arg", len(t.nnz_in))
+    want = golden_list(z, name, "act_res", len(t.nnz_out))
+    n = args[0].shape[1]
+    got = O.activity(t, args, n, nthreads=2)
+    for g, w in zip(got, want):
+        assert np.array_equal(g, w)
+
+
+def test_activity_fixture_is_not_trivial():
+    """The op tape's golden outputs hold inactive and active results, and the pass-through
+    output keeps partial bit patterns (words other than 0 and all ones)."""
+    z = load_npz("activity.npz")
+    r0, r1 = z["ops/act_res0"], z["ops/act_res1"]
+    assert (r0 == 0).mean() > 0.1 and (r0 != 0).mean() > 0.5
+    full = np.uint64(0xFFFFFFFFFFFFFFFF)
+    assert ((r1 != 0) & (r1 != full)).any()
+    assert set(np.unique(r0).tolist()) <= {0, int(full)}
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="reference harness not built on this host")
+def test_oracle_activity_matches_reference_harness():
+    from casadi_gb300 import workloads as W
+    t = W.random_dag(n_in=16, n_nodes=700, n_out=6, seed=9).tape
+    rng = np.random.default_rng(3)
+    n = 50
+    args = [np.where(rng.random((16, n)) < 0.5, np.uint64(0), np.uint64(2**64 - 1))]
+    got = O.activity(t, args, n)
+    want = O.ref_activity(t, args, n)
+    assert np.array_equal(got[0], want[0])
