@@ -19,6 +19,7 @@
 #include "../../include/casadi_gb300.h"
 #include "coloring.cuh"
 #include "schedule.cuh"
+#include "reduce.cuh"
 #include "sweeps.cuh"
 
 using namespace cgb;
@@ -2240,6 +2241,366 @@ int casadi_gb300_batch_run(int batch, void* scratch, size_t scratch_bytes, int u
   e = cudaEventRecord(b->ev_out, b->stream);
   if (e == cudaSuccess) e = cudaStreamWaitEvent(caller, b->ev_out, 0);
   if (e != cudaSuccess) return cuda_fail(e, "batch ordering");
+  return 0;
+}
+
+}  // extern "C"
+
+// ---- MapSum: shared inputs and instance-summed outputs (casadi/core/mapsum.cpp) -------------
+namespace {
+
+// Bump allocator over the caller's scratch (256-byte aligned regions).
+struct Arena {
+  char* p = nullptr;
+  size_t left = 0;
+  Arena(void* base, size_t bytes) {
+    const uintptr_t b = reinterpret_cast<uintptr_t>(base);
+    const uintptr_t a = (b + 255) & ~static_cast<uintptr_t>(255);
+    if (base && bytes >= a - b) {
+      p = reinterpret_cast<char*>(a);
+      left = bytes - (a - b);
+    }
+  }
+  void* take(size_t bytes) {
+    const size_t b = (bytes + 255) & ~static_cast<size_t>(255);
+    if (!p || b > left) return nullptr;
+    void* r = p;
+    p += b;
+    left -= b;
+    return r;
+  }
+};
+
+struct SumFlags {
+  bool shared[kMaxIo] = {};
+  bool summed[kMaxIo] = {};
+  int order = 0;
+};
+
+int sum_flags(const Tape& t, const casadi_gb300_mapsum_spec* spec, SumFlags* f) {
+  if (!spec) return fail(CASADI_GB300_ERR_ARG, "missing MapSum spec");
+  if (spec->order != 0 && spec->order != 1)
+    return fail(CASADI_GB300_ERR_ARG, "MapSum order must be 0 (instance order) or 1 (tree)");
+  for (int j = 0; j < t.n_in; ++j) f->shared[j] = spec->reduce_in && spec->reduce_in[j] != 0;
+  for (int j = 0; j < t.n_out; ++j) f->summed[j] = spec->reduce_out && spec->reduce_out[j] != 0;
+  f->order = spec->order;
+  return 0;
+}
+
+// An input (or seed) shared by every instance: ptr[d*nnz + k].
+IoDesc shared_io(const void* ptr, int nnz) {
+  return IoDesc{const_cast<void*>(ptr), 1, 0, static_cast<long long>(nnz)};
+}
+// Rows of n instances: ptr[(d*nnz + k)*n + i] (the per-instance values of a summed output).
+IoDesc rows_io(void* ptr, int nnz, long long n) {
+  return IoDesc{ptr, n, 1, static_cast<long long>(nnz) * n};
+}
+// The ordinary instance-minor layout with leading dimension ld.
+IoDesc plain_io(const void* ptr, int nnz, long long ld, bool dir_major) {
+  return IoDesc{const_cast<void*>(ptr), ld, 1, dir_major ? static_cast<long long>(nnz) * ld : 0};
+}
+
+template <class T>
+const void* at(T* const* p, int j) {
+  return p ? static_cast<const void*>(p[j]) : nullptr;
+}
+
+// Scratch the reductions of one call need besides the derivative sweeps: the per-instance rows
+// of every summed output (values and ndir directions) and shared input (ndir sensitivity
+// directions, or the sparsity bits), and the tree's level buffers.
+size_t sum_bytes(const Tape& t, long long n, int ndir, const SumFlags& f) {
+  const long long nd = std::max(1, ndir);
+  size_t bytes = 0;
+  long long max_rows = 0;
+  for (int j = 0; j < t.n_out; ++j) {
+    if (!f.summed[j]) continue;
+    const long long k = t.nnz_out[j];
+    bytes += ((8 * k * n + 255) / 256) * 256 + ((8 * k * nd * n + 255) / 256) * 256;
+    max_rows = std::max(max_rows, k * nd);
+  }
+  for (int j = 0; j < t.n_in; ++j) {
+    if (!f.shared[j]) continue;
+    const long long k = t.nnz_in[j];
+    bytes += ((8 * k * nd * n + 255) / 256) * 256;
+    max_rows = std::max(max_rows, k * nd);
+  }
+  return bytes + ((reduce_scratch_bytes(max_rows, n, f.order) + 255) / 256) * 256 + 256;
+}
+
+// Largest row count one reduction of the call handles (its tree buffers are reused).
+long long max_sum_rows(const Tape& t, int ndir, const SumFlags& f) {
+  const long long nd = std::max(1, ndir);
+  long long m = 0;
+  for (int j = 0; j < t.n_out; ++j)
+    if (f.summed[j]) m = std::max(m, static_cast<long long>(t.nnz_out[j]) * nd);
+  for (int j = 0; j < t.n_in; ++j)
+    if (f.shared[j]) m = std::max(m, static_cast<long long>(t.nnz_in[j]) * nd);
+  return m;
+}
+
+int scratch_short(const char* what) {
+  return fail(CASADI_GB300_ERR_SCRATCH,
+              "MapSum scratch too small for the %s (see casadi_gb300_mapsum_scratch_size)", what);
+}
+
+int take_tree(Arena& ar, const Tape& t, long long n, int ndir, const SumFlags& f, double** tree) {
+  const size_t b = reduce_scratch_bytes(max_sum_rows(t, ndir, f), n, f.order);
+  *tree = nullptr;
+  if (b == 0) return 0;
+  *tree = static_cast<double*>(ar.take(b));
+  return *tree ? 0 : scratch_short("summation tree");
+}
+
+int sum_rows(long long rows, long long n, const double* src, double* dst, int order,
+             double* tree, cudaStream_t s) {
+  cudaError_t e = reduce_sum(rows, n, src, n, dst, order, tree, s);
+  return e == cudaSuccess ? 0 : cuda_fail(e, "MapSum reduction");
+}
+
+}  // namespace
+
+extern "C" {
+
+int casadi_gb300_mapsum_scratch_size(int id, int64_t n, int ndir,
+                                     const casadi_gb300_mapsum_spec* spec, size_t* bytes) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  if (!bytes || n < 0 || ndir < 0) return fail(CASADI_GB300_ERR_ARG, "bad arguments");
+  SumFlags f;
+  if (int rc = sum_flags(*t, spec, &f)) return rc;
+  const size_t sweep =
+      ndir > 0 ? static_cast<size_t>(8) * t->n_partials * static_cast<size_t>(((n + 31) / 32) * 32)
+               : 0;
+  *bytes = sum_bytes(*t, n, ndir, f) + sweep + 256;
+  return 0;
+}
+
+int casadi_gb300_mapsum_eval(int id, int64_t n, int64_t ld, const casadi_gb300_mapsum_spec* spec,
+                             const double* const* arg, double* const* res, void* scratch,
+                             size_t scratch_bytes, void* stream) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  if (int rc = check_device(*t)) return rc;
+  if (int rc = check_n(n, ld)) return rc;
+  SumFlags f;
+  if (int rc = sum_flags(*t, spec, &f)) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  Arena ar(scratch, scratch_bytes);
+  SweepArgs a = base_args(*t, n, 0);
+  double* rows[kMaxIo] = {};
+  for (int j = 0; j < t->n_in; ++j)
+    a.in[j] = f.shared[j] ? shared_io(at(arg, j), t->nnz_in[j])
+                          : plain_io(at(arg, j), t->nnz_in[j], ld, false);
+  for (int j = 0; j < t->n_out; ++j) {
+    if (f.summed[j] && at(res, j)) {
+      rows[j] = static_cast<double*>(ar.take(8 * static_cast<size_t>(t->nnz_out[j]) * n));
+      if (!rows[j]) return scratch_short("summed outputs");
+      a.out[j] = rows_io(rows[j], t->nnz_out[j], n);
+    } else {
+      a.out[j] = plain_io(at(res, j), t->nnz_out[j], ld, false);
+    }
+  }
+  double* tree = nullptr;
+  if (int rc = take_tree(ar, *t, n, 0, f, &tree)) return rc;
+  if (n > 0)
+    if (int rc = primal_launch(*t, a, n, PK_EVAL, s)) return rc;
+  for (int j = 0; j < t->n_out; ++j)
+    if (rows[j])
+      if (int rc = sum_rows(t->nnz_out[j], n, rows[j], res[j], f.order, tree, s)) return rc;
+  return 0;
+}
+
+int casadi_gb300_mapsum_forward(int id, int64_t n, int64_t ld,
+                                const casadi_gb300_mapsum_spec* spec, int nfwd,
+                                const double* const* arg, double* const* res,
+                                const double* const* fseed, double* const* fsens, void* scratch,
+                                size_t scratch_bytes, void* stream) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  if (int rc = check_device(*t)) return rc;
+  if (int rc = check_n(n, ld)) return rc;
+  if (nfwd < 0 || nfwd > 65535) return fail(CASADI_GB300_ERR_ARG, "bad direction count %d", nfwd);
+  SumFlags f;
+  if (int rc = sum_flags(*t, spec, &f)) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  Arena ar(scratch, scratch_bytes);
+  IoDesc in[kMaxIo], out[kMaxIo], seed[kMaxIo], sens[kMaxIo];
+  double* rows[kMaxIo] = {};
+  double* srows[kMaxIo] = {};
+  for (int j = 0; j < t->n_in; ++j) {
+    const int k = t->nnz_in[j];
+    in[j] = f.shared[j] ? shared_io(at(arg, j), k) : plain_io(at(arg, j), k, ld, false);
+    seed[j] = f.shared[j] ? shared_io(at(fseed, j), k) : plain_io(at(fseed, j), k, ld, true);
+  }
+  for (int j = 0; j < t->n_out; ++j) {
+    const int k = t->nnz_out[j];
+    out[j] = plain_io(at(res, j), k, ld, false);
+    sens[j] = plain_io(at(fsens, j), k, ld, true);
+    if (!f.summed[j]) continue;
+    if (at(res, j)) {
+      rows[j] = static_cast<double*>(ar.take(8 * static_cast<size_t>(k) * n));
+      if (!rows[j]) return scratch_short("summed outputs");
+      out[j] = rows_io(rows[j], k, n);
+    }
+    if (at(fsens, j) && nfwd > 0) {
+      srows[j] = static_cast<double*>(ar.take(8 * static_cast<size_t>(k) * nfwd * n));
+      if (!srows[j]) return scratch_short("summed sensitivities");
+      sens[j] = rows_io(srows[j], k, n);
+    }
+  }
+  double* tree = nullptr;
+  if (int rc = take_tree(ar, *t, n, nfwd, f, &tree)) return rc;
+  if (int rc = run_ad(*t, n, in, out, seed, sens, nfwd, false, false, ar.p, ar.left, s))
+    return rc;
+  for (int j = 0; j < t->n_out; ++j) {
+    if (rows[j])
+      if (int rc = sum_rows(t->nnz_out[j], n, rows[j], res[j], f.order, tree, s)) return rc;
+    if (srows[j])
+      if (int rc = sum_rows(static_cast<long long>(t->nnz_out[j]) * nfwd, n, srows[j], fsens[j],
+                            f.order, tree, s))
+        return rc;
+  }
+  return 0;
+}
+
+int casadi_gb300_mapsum_reverse(int id, int64_t n, int64_t ld,
+                                const casadi_gb300_mapsum_spec* spec, int nadj,
+                                const double* const* arg, double* const* res,
+                                const double* const* aseed, double* const* asens, void* scratch,
+                                size_t scratch_bytes, void* stream) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  if (int rc = check_device(*t)) return rc;
+  if (int rc = check_n(n, ld)) return rc;
+  if (nadj < 0 || nadj > 65535) return fail(CASADI_GB300_ERR_ARG, "bad direction count %d", nadj);
+  SumFlags f;
+  if (int rc = sum_flags(*t, spec, &f)) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  Arena ar(scratch, scratch_bytes);
+  IoDesc in[kMaxIo], out[kMaxIo], seed[kMaxIo], sens[kMaxIo];
+  double* rows[kMaxIo] = {};
+  double* srows[kMaxIo] = {};
+  for (int j = 0; j < t->n_out; ++j) {
+    const int k = t->nnz_out[j];
+    out[j] = plain_io(at(res, j), k, ld, false);
+    seed[j] = f.summed[j] ? shared_io(at(aseed, j), k) : plain_io(at(aseed, j), k, ld, true);
+    if (f.summed[j] && at(res, j)) {
+      rows[j] = static_cast<double*>(ar.take(8 * static_cast<size_t>(k) * n));
+      if (!rows[j]) return scratch_short("summed outputs");
+      out[j] = rows_io(rows[j], k, n);
+    }
+  }
+  for (int j = 0; j < t->n_in; ++j) {
+    const int k = t->nnz_in[j];
+    in[j] = f.shared[j] ? shared_io(at(arg, j), k) : plain_io(at(arg, j), k, ld, false);
+    sens[j] = plain_io(at(asens, j), k, ld, true);
+    if (f.shared[j] && at(asens, j) && nadj > 0) {
+      srows[j] = static_cast<double*>(ar.take(8 * static_cast<size_t>(k) * nadj * n));
+      if (!srows[j]) return scratch_short("summed sensitivities");
+      sens[j] = rows_io(srows[j], k, n);
+    }
+  }
+  double* tree = nullptr;
+  if (int rc = take_tree(ar, *t, n, nadj, f, &tree)) return rc;
+  if (int rc = run_ad(*t, n, in, out, seed, sens, nadj, true, false, ar.p, ar.left, s)) return rc;
+  for (int j = 0; j < t->n_out; ++j)
+    if (rows[j])
+      if (int rc = sum_rows(t->nnz_out[j], n, rows[j], res[j], f.order, tree, s)) return rc;
+  for (int j = 0; j < t->n_in; ++j)
+    if (srows[j])
+      if (int rc = sum_rows(static_cast<long long>(t->nnz_in[j]) * nadj, n, srows[j], asens[j],
+                            f.order, tree, s))
+        return rc;
+  return 0;
+}
+
+int casadi_gb300_mapsum_sp_forward(int id, int64_t n, int64_t ld,
+                                   const casadi_gb300_mapsum_spec* spec,
+                                   const uint64_t* const* arg, uint64_t* const* res,
+                                   void* scratch, size_t scratch_bytes, void* stream) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  if (int rc = check_device(*t)) return rc;
+  if (int rc = check_n(n, ld)) return rc;
+  SumFlags f;
+  if (int rc = sum_flags(*t, spec, &f)) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  Arena ar(scratch, scratch_bytes);
+  SweepArgs a = base_args(*t, n, 0);
+  u64* rows[kMaxIo] = {};
+  for (int j = 0; j < t->n_in; ++j)
+    a.in[j] = f.shared[j] ? shared_io(at(arg, j), t->nnz_in[j])
+                          : plain_io(at(arg, j), t->nnz_in[j], ld, false);
+  for (int j = 0; j < t->n_out; ++j) {
+    if (f.summed[j] && at(res, j)) {
+      rows[j] = static_cast<u64*>(ar.take(8 * static_cast<size_t>(t->nnz_out[j]) * n));
+      if (!rows[j]) return scratch_short("summed outputs");
+      a.out[j] = rows_io(rows[j], t->nnz_out[j], n);
+    } else {
+      a.out[j] = plain_io(at(res, j), t->nnz_out[j], ld, false);
+    }
+  }
+  if (n > 0)
+    if (int rc = primal_launch(*t, a, n, PK_SP_FORWARD, s)) return rc;
+  for (int j = 0; j < t->n_out; ++j) {
+    if (!rows[j]) continue;
+    cudaError_t e = reduce_or(t->nnz_out[j], n, rows[j], n, reinterpret_cast<u64*>(res[j]), false, s);
+    if (e != cudaSuccess) return cuda_fail(e, "MapSum OR reduction");
+  }
+  return 0;
+}
+
+int casadi_gb300_mapsum_sp_reverse(int id, int64_t n, int64_t ld,
+                                   const casadi_gb300_mapsum_spec* spec, uint64_t* const* arg,
+                                   uint64_t* const* res, void* scratch, size_t scratch_bytes,
+                                   void* stream) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  if (int rc = check_device(*t)) return rc;
+  if (int rc = check_n(n, ld)) return rc;
+  SumFlags f;
+  if (int rc = sum_flags(*t, spec, &f)) return rc;
+  if (n == 0) return 0;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  Arena ar(scratch, scratch_bytes);
+  SweepArgs a = base_args(*t, n, 0);
+  u64* arows[kMaxIo] = {};
+  u64* srows[kMaxIo] = {};
+  cudaError_t e = cudaSuccess;
+  for (int j = 0; j < t->n_in; ++j) {
+    const int k = t->nnz_in[j];
+    a.in[j] = plain_io(at(arg, j), k, ld, false);
+    if (f.shared[j] && at(arg, j)) {
+      // every instance ORs its bits into its own row; the rows are OR-ed into arg[j] after
+      arows[j] = static_cast<u64*>(ar.take(8 * static_cast<size_t>(k) * n));
+      if (!arows[j]) return scratch_short("shared inputs");
+      if ((e = cudaMemsetAsync(arows[j], 0, 8 * static_cast<size_t>(k) * n, s)) != cudaSuccess)
+        return cuda_fail(e, "MapSum clear");
+      a.in[j] = rows_io(arows[j], k, n);
+    }
+  }
+  for (int j = 0; j < t->n_out; ++j) {
+    const int k = t->nnz_out[j];
+    a.out[j] = plain_io(at(res, j), k, ld, false);
+    if (f.summed[j] && at(res, j)) {
+      // the summed output's seed reaches every instance (MapSum restores it before each one)
+      srows[j] = static_cast<u64*>(ar.take(8 * static_cast<size_t>(k) * n));
+      if (!srows[j]) return scratch_short("summed outputs");
+      if ((e = broadcast_rows(k, n, reinterpret_cast<const u64*>(res[j]), srows[j], n, s)) !=
+          cudaSuccess)
+        return cuda_fail(e, "MapSum seed broadcast");
+      a.out[j] = rows_io(srows[j], k, n);
+    }
+  }
+  if (int rc = primal_launch(*t, a, n, PK_SP_REVERSE, s)) return rc;
+  for (int j = 0; j < t->n_in; ++j)
+    if (arows[j] && (e = reduce_or(t->nnz_in[j], n, arows[j], n,
+                                   reinterpret_cast<u64*>(arg[j]), true, s)) != cudaSuccess)
+      return cuda_fail(e, "MapSum OR reduction");
+  for (int j = 0; j < t->n_out; ++j)
+    if (srows[j] &&
+        (e = cudaMemsetAsync(res[j], 0, 8 * static_cast<size_t>(t->nnz_out[j]), s)) != cudaSuccess)
+      return cuda_fail(e, "MapSum clear");
   return 0;
 }
 

@@ -71,6 +71,14 @@ def load(path=None):
         "casadi_gb300_sp_forward": (cint, [cint, i64, i64, vp, vp, vp]),
         "casadi_gb300_sp_reverse": (cint, [cint, i64, i64, vp, vp, vp]),
         "casadi_gb300_eval_activity": (cint, [cint, i64, i64, vp, vp, vp]),
+        "casadi_gb300_mapsum_scratch_size": (cint, [cint, i64, cint, vp, vp]),
+        "casadi_gb300_mapsum_eval": (cint, [cint, i64, i64, vp, vp, vp, vp, sz, vp]),
+        "casadi_gb300_mapsum_forward": (cint, [cint, i64, i64, vp, cint, vp, vp, vp, vp, vp, sz,
+                                               vp]),
+        "casadi_gb300_mapsum_reverse": (cint, [cint, i64, i64, vp, cint, vp, vp, vp, vp, vp, sz,
+                                               vp]),
+        "casadi_gb300_mapsum_sp_forward": (cint, [cint, i64, i64, vp, vp, vp, vp, sz, vp]),
+        "casadi_gb300_mapsum_sp_reverse": (cint, [cint, i64, i64, vp, vp, vp, vp, sz, vp]),
         "casadi_gb300_sync": (cint, [cint, vp]),
         "casadi_gb300_checkout": (cint, []),
         "casadi_gb300_release": (cint, [cint]),
@@ -353,6 +361,111 @@ class CudaTape:
         v = ct.c_int()
         check(load().casadi_gb300_tuned_variant(self.id, kind, ct.byref(v)))
         return v.value
+
+
+class _MapSumSpec(ct.Structure):
+    _fields_ = [("reduce_in", ct.c_void_p), ("reduce_out", ct.c_void_p), ("order", ct.c_int)]
+
+
+class CudaMapSum:
+    """``f.map(name, "cuda", n, reduce_in, reduce_out)``: MapSum over n instances
+    (casadi/core/mapsum.cpp) on device tensors. A shared input (``reduce_in``) is one column,
+    shape (nnz,), used by every instance; a summed output (``reduce_out``) is returned as its
+    sum over the instances, shape (nnz,). Other inputs/outputs are (nnz, n) as in
+    :class:`CudaTape`. Seeds of shared inputs and sensitivities of summed outputs carry a
+    leading direction axis: (ndir, nnz).
+
+    ``order=0`` sums in instance order (MapSum's own order, the reference's bits);
+    ``order=1`` uses a fixed blocked tree that does not chain n dependent adds."""
+
+    class_name = "MapSum"
+    parallelization = "cuda"
+
+    def __init__(self, f, n, reduce_in=None, reduce_out=None, order=0):
+        self.tape = f if isinstance(f, CudaTape) else CudaTape(f)
+        self.n = int(n)
+        nin, nout = len(self.tape.nnz_in), len(self.tape.nnz_out)
+        self.reduce_in = [bool(v) for v in (reduce_in or [False] * nin)]
+        self.reduce_out = [bool(v) for v in (reduce_out or [False] * nout)]
+        if len(self.reduce_in) != nin or len(self.reduce_out) != nout:
+            raise ValueError("reduce_in/reduce_out: one flag per input/output")
+        self._rin = np.ascontiguousarray(self.reduce_in, dtype=np.int32)
+        self._rout = np.ascontiguousarray(self.reduce_out, dtype=np.int32)
+        self._spec = _MapSumSpec(self._rin.ctypes.data, self._rout.ctypes.data, int(order))
+        self._scratch = None
+        self.name = "mapsum%d_%s" % (self.n, getattr(f, "name", "f"))
+
+    @property
+    def order(self):
+        return self._spec.order
+
+    def scratch(self, ndir=0):
+        import torch
+        b = ct.c_size_t()
+        check(load().casadi_gb300_mapsum_scratch_size(self.tape.id, self.n, ndir,
+                                                      ct.byref(self._spec), ct.byref(b)))
+        if self._scratch is None or self._scratch.numel() < b.value:
+            self._scratch = torch.empty(max(b.value, 8), dtype=torch.uint8, device="cuda")
+        return self._scratch
+
+    def _res(self, nnz, summed, ndir=None, dtype=None):
+        import torch
+        dtype = dtype or torch.float64
+        out = []
+        for k, red in zip(nnz, summed):
+            shape = (k,) if red else (k, self.n)
+            if ndir is not None:
+                shape = (ndir,) + shape
+            out.append(torch.empty(shape, dtype=dtype, device="cuda"))
+        return out
+
+    def _call(self, name, *args):
+        check(getattr(load(), name)(self.tape.id, self.n, self.n, ct.byref(self._spec), *args))
+
+    def __call__(self, args, stream=None):
+        return self.eval(args, stream=stream)
+
+    def eval(self, args, res=None, stream=None):
+        res = self._res(self.tape.nnz_out, self.reduce_out) if res is None else res
+        sc = self.scratch(0)
+        self._call("casadi_gb300_mapsum_eval", _ptr_array(args), _ptr_array(res),
+                   ct.c_void_p(sc.data_ptr()), sc.numel(), _stream_handle(stream))
+        return res
+
+    def forward(self, args, fseeds, res=None, fsens=None, stream=None):
+        nfwd = next(s.shape[0] for s in fseeds if s is not None)
+        res = self._res(self.tape.nnz_out, self.reduce_out) if res is None else res
+        fsens = self._res(self.tape.nnz_out, self.reduce_out, nfwd) if fsens is None else fsens
+        sc = self.scratch(nfwd)
+        self._call("casadi_gb300_mapsum_forward", nfwd, _ptr_array(args), _ptr_array(res),
+                   _ptr_array(fseeds), _ptr_array(fsens), ct.c_void_p(sc.data_ptr()),
+                   sc.numel(), _stream_handle(stream))
+        return res, fsens
+
+    def reverse(self, args, aseeds, res=None, asens=None, stream=None):
+        nadj = next(s.shape[0] for s in aseeds if s is not None)
+        res = self._res(self.tape.nnz_out, self.reduce_out) if res is None else res
+        asens = self._res(self.tape.nnz_in, self.reduce_in, nadj) if asens is None else asens
+        sc = self.scratch(nadj)
+        self._call("casadi_gb300_mapsum_reverse", nadj, _ptr_array(args), _ptr_array(res),
+                   _ptr_array(aseeds), _ptr_array(asens), ct.c_void_p(sc.data_ptr()),
+                   sc.numel(), _stream_handle(stream))
+        return res, asens
+
+    def sp_forward(self, args, stream=None):
+        import torch
+        res = self._res(self.tape.nnz_out, self.reduce_out, dtype=torch.int64)
+        sc = self.scratch(0)
+        self._call("casadi_gb300_mapsum_sp_forward", _ptr_array(args), _ptr_array(res),
+                   ct.c_void_p(sc.data_ptr()), sc.numel(), _stream_handle(stream))
+        return res
+
+    def sp_reverse(self, args, res, stream=None):
+        """In place, like MapSum::sp_reverse: args |= propagated bits, res seeds cleared."""
+        sc = self.scratch(0)
+        self._call("casadi_gb300_mapsum_sp_reverse", _ptr_array(args), _ptr_array(res),
+                   ct.c_void_p(sc.data_ptr()), sc.numel(), _stream_handle(stream))
+        return args, res
 
 
 class MapMemory:

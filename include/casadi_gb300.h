@@ -186,6 +186,57 @@ CASADI_GB300_API int casadi_gb300_sp_reverse(int id, int64_t n, int64_t ld, uint
 CASADI_GB300_API int casadi_gb300_eval_activity(int id, int64_t n, int64_t ld,
                             const uint64_t* const* arg, uint64_t* const* res, void* stream);
 
+/* MapSum over n instances (MapSum::eval_gen, casadi/core/mapsum.cpp:153-181; created by
+ * Function::map(name, parallelization, n, reduce_in, reduce_out), function.cpp:787-827).
+ * reduce_in[j] != 0: input j is shared by every instance, arg[j] holds nnz_in[j] values
+ * (seeds of a shared input: (ndir, nnz_in[j]) values). reduce_out[j] != 0: output j is summed
+ * over the instances, res[j] receives nnz_out[j] values (sensitivities: (ndir, nnz_out[j])).
+ * Null flag arrays mean no flags. Every other input/output uses the instance-minor layout of
+ * casadi_gb300_eval with leading dimension ld. order 0 sums in instance order starting from
+ * zero, MapSum's own order (the reference's bits); order 1 sums by a fixed blocked tree
+ * (256-instance blocks, then their sums, until one value; the bits do not depend on the
+ * launch), which does not form a chain of n dependent adds. */
+typedef struct casadi_gb300_mapsum_spec {
+  const int* reduce_in;  /* n_in flags, or null */
+  const int* reduce_out; /* n_out flags, or null */
+  int order;             /* 0: instance order, 1: blocked tree */
+} casadi_gb300_mapsum_spec;
+
+/* Device scratch the MapSum calls below need for n instances and up to ndir directions
+ * (0 for eval and the sparsity sweeps): per-instance rows of the summed outputs and shared
+ * inputs' sensitivities, the tree's level buffers and the derivative sweeps' partials. */
+CASADI_GB300_API int casadi_gb300_mapsum_scratch_size(int id, int64_t n, int ndir,
+                            const casadi_gb300_mapsum_spec* spec, size_t* bytes);
+CASADI_GB300_API int casadi_gb300_mapsum_eval(int id, int64_t n, int64_t ld,
+                            const casadi_gb300_mapsum_spec* spec, const double* const* arg,
+                            double* const* res, void* scratch, size_t scratch_bytes,
+                            void* stream);
+/* Forward mode of a MapSum (MapSum::get_forward, mapsum.cpp:255-349): the seeds of shared
+ * inputs are shared, the sensitivities of summed outputs are summed. */
+CASADI_GB300_API int casadi_gb300_mapsum_forward(int id, int64_t n, int64_t ld,
+                            const casadi_gb300_mapsum_spec* spec, int nfwd,
+                            const double* const* arg, double* const* res,
+                            const double* const* fseed, double* const* fsens, void* scratch,
+                            size_t scratch_bytes, void* stream);
+/* Reverse mode of a MapSum (MapSum::get_reverse, mapsum.cpp:351-413): the adjoint seeds of
+ * summed outputs are shared, the adjoint sensitivities of shared inputs are summed. */
+CASADI_GB300_API int casadi_gb300_mapsum_reverse(int id, int64_t n, int64_t ld,
+                            const casadi_gb300_mapsum_spec* spec, int nadj,
+                            const double* const* arg, double* const* res,
+                            const double* const* aseed, double* const* asens, void* scratch,
+                            size_t scratch_bytes, void* stream);
+/* Sparsity of a MapSum (MapSum::sp_forward / sp_reverse, mapsum.cpp:190-232): summed outputs
+ * OR over the instances; in reverse, a summed output's seed bits reach every instance and are
+ * cleared afterwards, and a shared input receives (|=) the OR of every instance's bits. */
+CASADI_GB300_API int casadi_gb300_mapsum_sp_forward(int id, int64_t n, int64_t ld,
+                            const casadi_gb300_mapsum_spec* spec, const uint64_t* const* arg,
+                            uint64_t* const* res, void* scratch, size_t scratch_bytes,
+                            void* stream);
+CASADI_GB300_API int casadi_gb300_mapsum_sp_reverse(int id, int64_t n, int64_t ld,
+                            const casadi_gb300_mapsum_spec* spec, uint64_t* const* arg,
+                            uint64_t* const* res, void* scratch, size_t scratch_bytes,
+                            void* stream);
+
 /* Wait for all work on `stream` and report device-side error flags raised by sweeps of this
  * tape (bounded waits that ran out, malformed instructions). Clears the flags. */
 CASADI_GB300_API int casadi_gb300_sync(int id, void* stream);

@@ -203,6 +203,86 @@ def activity(tape, args, n, nthreads=1):
     return res
 
 
+# ---- MapSum (casadi/core/mapsum.cpp) -------------------------------------------------------
+def _broadcast(a, n, shared, ndir=False):
+    """A shared input (nnz,) or seed (ndir, nnz) repeated for every instance."""
+    if a is None or not shared:
+        return a
+    a = np.asarray(a)
+    return np.ascontiguousarray(np.repeat(a[..., None], n, axis=-1))
+
+
+def ordered_sum(rows):
+    """Sum over the last (instance) axis in instance order starting from zero: MapSum's
+    casadi_clear then one casadi_add per instance (mapsum.cpp:141-146, :160-178)."""
+    rows = np.asarray(rows, dtype=np.float64)
+    acc = np.zeros(rows.shape[:-1])
+    for i in range(rows.shape[-1]):
+        acc = acc + rows[..., i]
+    return acc
+
+
+def _or_all(rows):
+    rows = np.asarray(rows, dtype=np.uint64)
+    return np.bitwise_or.reduce(rows, axis=-1) if rows.shape[-1] else \
+        np.zeros(rows.shape[:-1], np.uint64)
+
+
+def mapsum_eval(tape, args, n, reduce_in, reduce_out, nthreads=1):
+    """MapSum::eval_gen (mapsum.cpp:153-181): shared inputs are (nnz,), summed outputs (nnz,)."""
+    full = [_broadcast(a, n, r) for a, r in zip(args, reduce_in)]
+    res = eval(tape, full, n, nthreads)
+    return [ordered_sum(r) if red else r for r, red in zip(res, reduce_out)]
+
+
+def mapsum_forward(tape, args, fseeds, n, reduce_in, reduce_out, nthreads=1):
+    """MapSum::get_forward (mapsum.cpp:255-349): shared seeds (nfwd, nnz), summed
+    sensitivities (nfwd, nnz)."""
+    full = [_broadcast(a, n, r) for a, r in zip(args, reduce_in)]
+    seeds = [_broadcast(a, n, r) for a, r in zip(fseeds, reduce_in)]
+    res, fsens = forward(tape, full, seeds, n, nthreads)
+    res = [ordered_sum(r) if red else r for r, red in zip(res, reduce_out)]
+    fsens = [ordered_sum(r) if red else r for r, red in zip(fsens, reduce_out)]
+    return res, fsens
+
+
+def mapsum_reverse(tape, args, aseeds, n, reduce_in, reduce_out, nthreads=1):
+    """MapSum::get_reverse (mapsum.cpp:351-413): the seeds of summed outputs are shared, the
+    sensitivities of shared inputs summed."""
+    full = [_broadcast(a, n, r) for a, r in zip(args, reduce_in)]
+    seeds = [_broadcast(a, n, r) for a, r in zip(aseeds, reduce_out)]
+    res, asens = reverse(tape, full, seeds, n, nthreads)
+    res = [ordered_sum(r) if red else r for r, red in zip(res, reduce_out)]
+    asens = [ordered_sum(r) if red else r for r, red in zip(asens, reduce_in)]
+    return res, asens
+
+
+def mapsum_sp_forward(tape, args, n, reduce_in, reduce_out):
+    """MapSum::sp_forward (mapsum.cpp:190-193 with the bvec_t casadi_add, :148-152)."""
+    full = [_broadcast(a, n, r) for a, r in zip(args, reduce_in)]
+    res = sp_forward(tape, full, n)
+    return [_or_all(r) if red else r for r, red in zip(res, reduce_out)]
+
+
+def mapsum_sp_reverse(tape, args, res, n, reduce_in, reduce_out):
+    """MapSum::sp_reverse (mapsum.cpp:196-232), in place: every instance sees the seed of a
+    summed output (cleared at the end); a shared input ORs in every instance's bits."""
+    if n == 0:
+        return args, res
+    work_args = [np.zeros((a.shape[0], n), np.uint64) if (a is not None and r) else a
+                 for a, r in zip(args, reduce_in)]
+    work_res = [_broadcast(s, n, r).astype(np.uint64) if (s is not None and r) else s
+                for s, r in zip(res, reduce_out)]
+    sp_reverse(tape, work_args, work_res, n)
+    for j, r in enumerate(reduce_in):
+        if r and args[j] is not None:
+            args[j] |= _or_all(work_args[j])
+    for j, r in enumerate(reduce_out):
+        if r and res[j] is not None:
+            res[j][...] = 0
+    return args, res
+
+
 def zero_checker(which, op):
     """0: f(0, y) == 0; 1: f(x, 0) == 0; 2: f(0, 0) == 0 (calculus.hpp:485-540)."""
     return bool(lib().sxo_zero_checker(which, op))

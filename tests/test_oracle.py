@@ -189,3 +189,31 @@ def test_oracle_activity_matches_reference_harness():
     got = O.activity(t, args, n)
     want = O.ref_activity(t, args, n)
     assert np.array_equal(got[0], want[0])
+
+
+# ---- MapSum restatement ----------------------------------------------------------------------
+def test_oracle_mapsum_matches_unrolled_instances():
+    """The oracle's MapSum equals an explicit loop over instances: shared inputs repeated,
+    summed outputs accumulated from zero in instance order (mapsum.cpp:153-181)."""
+    from casadi_gb300 import workloads as W
+    f = W.cartpole_rollout(3)
+    n = 7
+    x0, U = W.cartpole_inputs(n, steps=3, seed=2)
+    shared_u = np.ascontiguousarray(U[:, 0])
+    res = O.mapsum_eval(f.tape, [x0, shared_u], n, [False, True], [True, False])
+    acc = np.zeros(4)
+    xs = []
+    for i in range(n):
+        r = O.eval(f.tape, [x0[:, i:i + 1].copy(), shared_u[:, None].copy()], 1)
+        acc = acc + r[0][:, 0]
+        xs.append(r[1][:, 0])
+    assert np.array_equal(res[0], acc)
+    assert np.array_equal(res[1], np.array(xs).T)
+    # sparsity: a shared input's reverse bits are the OR over the instances
+    t = W.random_dag(n_in=8, n_nodes=200, n_out=3, seed=1).tape
+    arg = [np.zeros(8, np.uint64)]
+    seed = [np.array([1, 2, 4], np.uint64)]
+    O.mapsum_sp_reverse(t, arg, seed, 5, [True], [True])
+    one = [np.zeros((8, 1), np.uint64)]
+    O.sp_reverse(t, one, [np.array([[1], [2], [4]], np.uint64)], 1)
+    assert np.array_equal(arg[0], one[0][:, 0]) and not seed[0].any()
