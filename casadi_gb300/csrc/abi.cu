@@ -118,7 +118,15 @@ struct Tape {
   int ref_sz_w = 0;  // the work-vector length the tape came with (sz_w: after scheduling)
   int residence = 0;  // work vector: 0 auto (shared memory when it fits, value sweeps tuned),
                       // 1 global memory, 2 shared memory whenever it fits
-  int primal_tuned[5] = {-1, -1, -1, -1, -1};  // per PrimalKind: 0 shared, 1 global (tuned)
+  // per PrimalKind and launch size class (0: at most 16 tiles per SM): 0 shared, 1 global,
+  // 2 cooperative level sweep (autotuned)
+  int primal_tuned[5][2] = {{-1, -1}, {-1, -1}, {-1, -1}, {-1, -1}, {-1, -1}};
+  // level schedule of the cooperative value/record sweeps, built on first use
+  int lv_state = 0;  // 0 not built, 1 built, -1 unavailable
+  u64* d_lcode = nullptr;
+  int* d_lbegin = nullptr;
+  int* d_lpidx = nullptr;
+  int n_levels = 0, lv_sz_w = 0;
   // global work vector: per-CTA blocks, grown on demand; uses on different streams are
   // ordered by gw_event
   std::mutex gw_mtx;
@@ -154,6 +162,9 @@ struct Tape {
     cudaFree(d_consts);
     cudaFree(d_absent);
     cudaFree(d_err);
+    cudaFree(d_lcode);
+    cudaFree(d_lbegin);
+    cudaFree(d_lpidx);
     if (gw_event) cudaEventSynchronize(gw_event);
     cudaFree(d_gw);
     if (gw_event) cudaEventDestroy(gw_event);
@@ -171,6 +182,11 @@ struct Tape {
     v.sz_w = sz_w;
     v.n_partials = n_partials;
     v.err = d_err;
+    v.lcode = d_lcode;
+    v.lbegin = d_lbegin;
+    v.lpidx = d_lpidx;
+    v.n_levels = n_levels;
+    v.lv_sz_w = lv_sz_w;
     return v;
   }
 };
@@ -644,10 +660,56 @@ int time_once(cudaStream_t s, F fn, float* ms) {
 // memory kernels with the tape's block size, or the global-work-vector kernels.
 enum PrimalKind { PK_EVAL = 0, PK_RECORD, PK_SP_FORWARD, PK_SP_REVERSE, PK_ACTIVITY };
 
+// Level schedule of the cooperative sweeps (host scheduling + upload, once per tape). Returns
+// whether it is available; never called while the stream is being captured.
+constexpr int kLevelWidth = 64;      // instructions per level
+constexpr int kCoopThreads = 256;    // warps of a cooperative CTA x 32
+bool ensure_levels(Tape& t) {
+  std::lock_guard<std::mutex> lk(t.shape_mtx);
+  if (t.lv_state != 0) return t.lv_state > 0;
+  t.lv_state = -1;
+  Levels lv;
+  std::string err;
+  const int cap = t.sz_w <= 400 ? 400 : t.sz_w + kLevelWidth;
+  const int nl = level_schedule(t.h_code, kLevelWidth, cap, lv, err);
+  if (nl <= 0 || lv.code.empty()) return false;
+  u64* code = nullptr;
+  int *begin = nullptr, *pidx = nullptr;
+  bool ok = cudaMalloc(&code, lv.code.size() * sizeof(u64)) == cudaSuccess &&
+            cudaMalloc(&begin, lv.begin.size() * sizeof(int)) == cudaSuccess &&
+            cudaMalloc(&pidx, lv.pidx.size() * sizeof(int)) == cudaSuccess;
+  ok = ok &&
+       cudaMemcpy(code, lv.code.data(), lv.code.size() * sizeof(u64), cudaMemcpyHostToDevice) ==
+           cudaSuccess &&
+       cudaMemcpy(begin, lv.begin.data(), lv.begin.size() * sizeof(int),
+                  cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(pidx, lv.pidx.data(), lv.pidx.size() * sizeof(int), cudaMemcpyHostToDevice) ==
+           cudaSuccess;
+  if (!ok) {
+    cudaFree(code);
+    cudaFree(begin);
+    cudaFree(pidx);
+    cudaGetLastError();
+    return false;
+  }
+  t.d_lcode = code;
+  t.d_lbegin = begin;
+  t.d_lpidx = pidx;
+  t.n_levels = nl;
+  t.lv_sz_w = lv.sz_w;
+  t.lv_state = 1;
+  return true;
+}
+
+void reset_primal_tuning(Tape& t) {
+  for (auto& k : t.primal_tuned) k[0] = k[1] = -1;
+}
+
 int primal_launch(Tape& t, SweepArgs& a, long long m, PrimalKind kind, cudaStream_t s) {
   static const int fam[] = {F_EVAL, F_RECORD, F_SP_FORWARD, F_SP_REVERSE, F_ACTIVITY};
   static const char* what[] = {"eval launch", "record sweep launch", "sp_forward launch",
                                "sp_reverse launch", "activity launch"};
+  enum { M_SHARED = 0, M_GLOBAL = 1, M_COOP = 2 };
   auto go = [&](int grid) {
     switch (kind) {
       case PK_EVAL: return launch_eval(a, grid, s);
@@ -657,10 +719,21 @@ int primal_launch(Tape& t, SweepArgs& a, long long m, PrimalKind kind, cudaStrea
       default: return launch_sp_reverse(a, grid, s);
     }
   };
-  // one launch with the work vector in shared (global = false) or global memory
-  auto run = [&](bool global, bool profile) -> int {
+  // one launch: work vector in shared or global memory, or the cooperative level sweep
+  auto run = [&](int mode, bool profile) -> int {
     int grid;
-    if (global) {
+    bool global = mode == M_GLOBAL;
+    if (mode == M_COOP) {
+      a.block = kCoopThreads;
+      a.t = t.view();
+      const size_t sm = smem_coop(t.lv_sz_w);
+      global = sm > static_cast<size_t>(max_smem_optin());
+      const int occ = std::max(1, occupancy_coop(kCoopThreads, sm, global));
+      grid = grid_for((m + 31) / 32, occ * sm_count());
+      a.wglob = nullptr;
+      if (global)
+        if (int rc = gw_prepare(t, a, &grid, static_cast<size_t>(t.lv_sz_w) * 32 * 8, s)) return rc;
+    } else if (global) {
       a.block = kGwBlock;
       const int occ =
           std::max(1, kind >= PK_SP_FORWARD ? occupancy_gw_sp() : occupancy_gw_primal());
@@ -674,7 +747,10 @@ int primal_launch(Tape& t, SweepArgs& a, long long m, PrimalKind kind, cudaStrea
       a.wglob = nullptr;
       grid = grid_for((m + a.block - 1) / a.block, t.primal_grid_cap);
     }
-    cudaError_t e = profile ? timed(fam[kind], s, [&] { return go(grid); }) : go(grid);
+    auto launch = [&] {
+      return mode == M_COOP ? launch_coop(a, kind == PK_RECORD, grid, s) : go(grid);
+    };
+    cudaError_t e = profile ? timed(fam[kind], s, launch) : launch();
     if (e != cudaSuccess) return cuda_fail(e, what[kind]);
     if (global) {
       a.wglob = nullptr;
@@ -682,24 +758,42 @@ int primal_launch(Tape& t, SweepArgs& a, long long m, PrimalKind kind, cudaStrea
     }
     return 0;
   };
-  if (primal_global(t)) return run(true, true);
-  if (t.residence == 2) return run(false, true);
-  int choice = t.primal_tuned[kind];
-  // residence is tuned like the derivative variants: time both on a launch that fills the GPU
-  // several times (every sweep here but sp_reverse, which consumes its seeds, can run twice)
-  if (choice < 0 && g_autotune && kind != PK_SP_REVERSE && !capturing(s) &&
-      m >= 16ll * sm_count() * 32) {
-    float ms[2] = {0, 0};
-    for (int g = 0; g < 2; ++g) {
+  const bool coop_kind = kind == PK_EVAL || kind == PK_RECORD;
+  const int cls = (m + 31) / 32 <= 16ll * sm_count() ? 0 : 1;
+  // the cooperative sweep is a candidate for launches of few tiles (or when forced)
+  const bool want_coop = coop_kind && (cls == 0 || t.residence == 3);
+  const bool can_coop = want_coop && (capturing(s) ? t.lv_state > 0 : ensure_levels(t));
+  if (t.residence == 3 && coop_kind && can_coop) return run(M_COOP, true);
+  if (t.residence == 1 || !fits_smem(t.sz_w)) {
+    if (!(coop_kind && can_coop && cls == 0 && t.residence != 1)) return run(M_GLOBAL, true);
+  } else if (t.residence == 2) {
+    return run(M_SHARED, true);
+  }
+  int cand[3], nc = 0;
+  if (fits_smem(t.sz_w)) cand[nc++] = M_SHARED;
+  cand[nc++] = M_GLOBAL;
+  if (coop_kind && can_coop && (cls == 0 || t.residence == 3)) cand[nc++] = M_COOP;
+  int& choice = t.primal_tuned[kind][cls];
+  // residence is tuned like the derivative variants: every candidate timed once on the first
+  // call of each kind and size class (every sweep here but sp_reverse, which consumes its
+  // seeds, can run twice with the same results)
+  if (choice < 0 && nc > 1 && g_autotune && kind != PK_SP_REVERSE && !capturing(s)) {
+    float ms[3] = {0, 0, 0};
+    for (int c = 0; c < nc; ++c) {
       int rc = 0;
-      if (int trc = time_once(s, [&] { rc = run(g == 1, false); return cudaSuccess; }, &ms[g]))
+      if (int trc = time_once(s, [&] { rc = run(cand[c], false); return cudaSuccess; }, &ms[c]))
         return trc;
       if (rc) return rc;
     }
-    t.primal_tuned[kind] = ms[1] < ms[0] ? 1 : 0;
-    return 0;  // both runs produced the same (complete) results
+    int best = 0;
+    for (int c = 1; c < nc; ++c)
+      if (ms[c] < ms[best]) best = c;
+    choice = cand[best];
+    return 0;  // every run produced the same (complete) results
   }
-  return run(choice == 1, true);
+  if (choice >= 0 && (choice != M_COOP || can_coop) && (choice != M_SHARED || fits_smem(t.sz_w)))
+    return run(choice, true);
+  return run(cand[0], true);
 }
 
 // One derivative sweep after the record sweep: ndir directions, forward (seeded or identity)
@@ -1093,6 +1187,42 @@ int casadi_gb300_tape_schedule(const casadi_gb300_atomic* alg, int n_instr, int 
   return 0;
 }
 
+int casadi_gb300_tape_levels(const casadi_gb300_atomic* alg, int n_instr, int n_in,
+                             const int* nnz_in, int n_out, const int* nnz_out, int sz_w,
+                             int width, int slot_cap, casadi_gb300_atomic* out, int* source,
+                             int* level_begin, int* n_levels, int* sz_w_out) {
+  if (!n_levels || !sz_w_out || width < 1 || slot_cap < 1)
+    return fail(CASADI_GB300_ERR_ARG, "bad arguments");
+  Encoded en;
+  const int wlen = encode_and_schedule(alg, n_instr, n_in, nnz_in, n_out, nnz_out, sz_w, en);
+  if (wlen < 0) return wlen;
+  Levels lv;
+  std::string err;
+  const int nl = level_schedule(en.code, width, slot_cap, lv, err);
+  if (nl < 0) return fail(CASADI_GB300_ERR_ARG, "%s", err.c_str());
+  *n_levels = nl;
+  *sz_w_out = lv.sz_w;
+  if (level_begin)
+    for (int l = 0; l <= nl; ++l) level_begin[l] = lv.begin[l];
+  for (size_t k = 0; k < lv.code.size(); ++k) {
+    if (source) source[k] = lv.src[k];
+    if (!out) continue;
+    const u64 w = lv.code[k];
+    const unsigned op = dec_op(w);
+    casadi_gb300_atomic& e = out[k];
+    std::memset(&e, 0, sizeof(e));
+    e.op = reference_opcode(op);
+    e.i0 = static_cast<int>(dec_a(w));
+    if (op == D_CONST) {
+      e.a.d = en.consts[dec_b(w)];
+    } else {
+      e.a.i[0] = static_cast<int>(dec_b(w));
+      e.a.i[1] = static_cast<int>(dec_c(w));
+    }
+  }
+  return 0;
+}
+
 static int check_ccs(int nrow, int ncol, const int* colind, const int* row) {
   if (nrow < 0 || ncol < 0 || !colind) return fail(CASADI_GB300_ERR_ARG, "bad pattern size");
   if (colind[0] != 0) return fail(CASADI_GB300_ERR_ARG, "colind[0] must be 0");
@@ -1409,9 +1539,9 @@ int casadi_gb300_tuned_variant(int id, int kind, int* variant) {
 int casadi_gb300_set_residence(int id, int mode) {
   Tape* t = get_tape(id);
   if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
-  if (mode < 0 || mode > 2) return fail(CASADI_GB300_ERR_ARG, "residence must be 0, 1 or 2");
+  if (mode < 0 || mode > 3) return fail(CASADI_GB300_ERR_ARG, "residence must be 0, 1, 2 or 3");
   t->residence = mode;
-  for (int& c : t->primal_tuned) c = -1;
+  reset_primal_tuning(*t);
   return 0;
 }
 

@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <queue>
 #include <tuple>
+#include <unordered_map>
 
 #include "schedule.cuh"
 
@@ -211,6 +212,154 @@ int schedule_code(const std::vector<u64>& in, std::vector<u64>& out, std::string
     return w_orig;
   }
   return w_sched;
+}
+
+int level_schedule(const std::vector<u64>& in, int width, int slot_cap, Levels& out,
+                   std::string& err) {
+  const int n = static_cast<int>(in.size());
+  out = Levels();
+  out.begin.push_back(0);
+  if (width < 1) width = 1;
+  // value graph (dep0/dep1: defining instruction of each operand) and recorded-partial indices
+  std::vector<int> dep0(n, -1), dep1(n, -1), after(n, -1), pidx(n, 0);
+  std::vector<int> cur;                      // slot -> defining instruction of its value
+  std::unordered_map<long long, int> last_out;  // (output, nonzero) -> last OUTPUT writing it
+  int np = 0;
+  for (int k = 0; k < n; ++k) {
+    const u64 w = in[k];
+    const unsigned op = dec_op(w);
+    pidx[k] = np;
+    if (op == D_NOP) continue;
+    auto def_of = [&](unsigned slot, int* d) {
+      if (slot >= cur.size() || cur[slot] < 0) {
+        char buf[128];
+        std::snprintf(buf, sizeof(buf), "instruction %d reads slot %u before it is written", k,
+                      slot);
+        err = buf;
+        return false;
+      }
+      *d = cur[slot];
+      return true;
+    };
+    if (op == D_OUTPUT) {
+      if (!def_of(dec_b(w), &dep0[k])) return -1;
+      // two writes of one output nonzero keep their order
+      const long long key = (static_cast<long long>(dec_a(w)) << 32) | dec_c(w);
+      auto it = last_out.find(key);
+      if (it != last_out.end()) {
+        after[k] = it->second;
+        it->second = k;
+      } else {
+        last_out.emplace(key, k);
+      }
+    } else if (op != D_CONST && op != D_INPUT) {
+      if (!def_of(dec_b(w), &dep0[k])) return -1;
+      if (is_binary(op)) {
+        int d = -1;
+        if (!def_of(dec_c(w), &d)) return -1;
+        if (d != dep0[k]) dep1[k] = d;
+      }
+      const unsigned m = partial_mask(op);
+      np += static_cast<int>((m & 1u) + ((m >> 1) & 1u));
+    }
+    if (defines_value(op)) {
+      const unsigned a = dec_a(w);
+      if (a >= cur.size()) cur.resize(a + 1, -1);
+      cur[a] = k;
+    }
+  }
+  // successors, predecessor counts, remaining uses
+  std::vector<std::vector<int>> succ(n);
+  std::vector<int> npred(n, 0), uses(n, 0);
+  for (int k = 0; k < n; ++k)
+    for (int d : {dep0[k], dep1[k], after[k]})
+      if (d >= 0) {
+        succ[d].push_back(k);
+        ++npred[k];
+      }
+  for (int k = 0; k < n; ++k)
+    for (int d : {dep0[k], dep1[k]})
+      if (d >= 0) ++uses[d];
+
+  // Priority: position in `in` (the register-pressure order). The earliest ready instruction
+  // of each level always runs -- that is the sequential order's own progress, which needs no
+  // more slots than the order itself -- and later ready instructions fill the level only
+  // while fewer than `slot_cap` values are live or a slot is free, so looking ahead for
+  // parallel work never grows the work vector much past the cap.
+  typedef int Entry;
+  std::priority_queue<Entry, std::vector<Entry>, std::greater<Entry>> ready;
+  for (int k = 0; k < n; ++k)
+    if (dec_op(in[k]) != D_NOP && npred[k] == 0) ready.push(k);
+  std::vector<int> slot(n, -1), free_slots;  // free_slots: usable in the current level
+  int n_slots = 0, live = 0, placed = 0, total = 0;
+  for (int k = 0; k < n; ++k) total += dec_op(in[k]) != D_NOP;
+  std::vector<int> chosen, deferred, freed;
+  const int max_deferred = 4 * width;
+  while (placed < total) {
+    chosen.clear();
+    deferred.clear();
+    while (!ready.empty() && static_cast<int>(chosen.size()) < width &&
+           static_cast<int>(deferred.size()) < max_deferred) {
+      const int k = ready.top();
+      ready.pop();
+      if (defines_value(dec_op(in[k]))) {
+        if (!chosen.empty() && free_slots.empty() && live >= slot_cap) {
+          deferred.push_back(k);
+          continue;
+        }
+        if (free_slots.empty()) {
+          slot[k] = n_slots++;
+        } else {
+          slot[k] = free_slots.back();
+          free_slots.pop_back();
+        }
+        ++live;
+      }
+      chosen.push_back(k);
+    }
+    if (chosen.empty()) {
+      err = "tape has a dependence cycle";
+      return -1;
+    }
+    for (int k : deferred) ready.push(k);
+    // emit the level
+    freed.clear();
+    for (int k : chosen) {
+      const u64 w = in[k];
+      const unsigned op = dec_op(w);
+      switch (op) {
+        case D_CONST:
+        case D_INPUT:
+          out.code.push_back(enc(op, slot[k], dec_b(w), dec_c(w)));
+          break;
+        case D_OUTPUT:
+          out.code.push_back(enc(op, dec_a(w), slot[dep0[k]], dec_c(w)));
+          break;
+        default: {
+          const int b = slot[dep0[k]];
+          const int c = is_binary(op) ? slot[dep1[k] >= 0 ? dep1[k] : dep0[k]] : b;
+          out.code.push_back(enc(op, slot[k], b, c));
+        }
+      }
+      out.pidx.push_back(pidx[k]);
+      out.src.push_back(k);
+      for (int d : {dep0[k], dep1[k]})
+        if (d >= 0 && --uses[d] == 0) freed.push_back(d);
+      if (defines_value(op) && uses[k] == 0) freed.push_back(k);  // never read
+    }
+    out.begin.push_back(static_cast<int>(out.code.size()));
+    placed += static_cast<int>(chosen.size());
+    // slots of values whose last use was in this level are free from the next level on
+    for (int d : freed) {
+      free_slots.push_back(slot[d]);
+      --live;
+    }
+    for (int k : chosen)
+      for (int s : succ[k])
+        if (--npred[s] == 0) ready.push(s);
+  }
+  out.sz_w = n_slots;
+  return static_cast<int>(out.begin.size()) - 1;
 }
 
 }  // namespace cgb

@@ -211,6 +211,74 @@ __global__ void __launch_bounds__(BS) k_primal(const __grid_constant__ SweepArgs
 }
 
 // ---------------------------------------------------------------------------------------------
+// Cooperative value / record sweep for launches with few instances.
+//
+// One 32-instance tile per CTA (lane = instance) and several warps per CTA: the host's level
+// schedule groups the tape into levels of independent instructions; the warps of the CTA split
+// each level between them and meet at a barrier before the next, so a tile's sweep advances
+// by a whole level of independent instructions per step instead of one instruction. Each
+// instruction is the same operation on the same operand values as in the sequential sweep
+// (identical bits), and writes its partials at its index of the sequential order.
+// ---------------------------------------------------------------------------------------------
+template <bool RECORD, bool GW>
+__global__ void __launch_bounds__(kCoopMaxThreads) k_coop(const __grid_constant__ SweepArgs a) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  double* w = GW ? reinterpret_cast<double*>(a.wglob + blockIdx.x * a.wglob_stride)
+                 : reinterpret_cast<double*>(smem);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const long long ntiles = (a.n + 31) / 32;
+  const int nl = a.t.n_levels;
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const long long il = tile * 32 + lane;
+    const bool active = il < a.n;
+    const long long ig = a.i_begin + il;
+    double* pt = RECORD ? a.partials + static_cast<size_t>(tile) * a.t.n_partials * 32 + lane
+                        : nullptr;
+    int end = __ldg(a.t.lbegin);
+    for (int l = 0; l < nl; ++l) {
+      const int beg = end;
+      end = __ldg(a.t.lbegin + l + 1);
+      for (int i = beg + warp; i < end; i += nw) {
+        const u64 ins = __ldg(a.t.lcode + i);
+        const unsigned op = dec_op(ins), A = dec_a(ins), B = dec_b(ins), C = dec_c(ins);
+        switch (op) {
+          case D_CONST:
+            w[A * 32 + lane] = __ldg(a.t.consts + B);
+            break;
+          case D_INPUT: {
+            const IoDesc& d = a.in[B];
+            double v = 0.0;
+            if (active && d.ptr) v = __ldg(static_cast<const double*>(d.ptr) + io_off(d, 0, C, ig));
+            w[A * 32 + lane] = v;
+          } break;
+          case D_OUTPUT: {
+            const IoDesc& d = a.out[A];
+            if (active && d.ptr) static_cast<double*>(d.ptr)[io_off(d, 0, C, ig)] = w[B * 32 + lane];
+          } break;
+          default: {
+            const double x = w[B * 32 + lane], y = w[C * 32 + lane];
+            if (RECORD) {
+              const unsigned m = partial_mask(op);
+              double d0 = 0.0, d1 = 0.0;
+              const double f = dev_fun_der(op, x, y, d0, d1);
+              if (m && active) {
+                const size_t p = static_cast<size_t>(__ldg(a.t.lpidx + i));
+                if (m & 1u) pt[p * 32] = d0;
+                if (m & 2u) pt[(p + (m & 1u)) * 32] = d1;
+              }
+              w[A * 32 + lane] = f;
+            } else {
+              w[A * 32 + lane] = dev_fun(op, x, y);
+            }
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
 // Plan-free adjoint sweep (the allocation-free entry point).
 //
 // The record sweep stores partials tile-major: for the 32-instance tile T of a wave,
@@ -1177,6 +1245,23 @@ cudaError_t launch_activity(const SweepArgs& a, int grid, cudaStream_t s) {
     return launch_k(k_sp_forward<kGwBlock, true, true>, grid, kGwBlock, kHeaderBytes, a, s);
   const size_t smem = smem_primal(a.t.sz_w, a.block);
   CGB_DISPATCH_BS(k_sp_forward, , false, true)
+}
+
+size_t smem_coop(int lv_sz_w) { return static_cast<size_t>(lv_sz_w > 0 ? lv_sz_w : 1) * 32 * 8; }
+
+cudaError_t launch_coop(const SweepArgs& a, bool record, int grid, cudaStream_t s) {
+  if (a.block < 32 || a.block > kCoopMaxThreads || a.block % 32) return cudaErrorInvalidValue;
+  if (a.wglob)
+    return record ? launch_k(k_coop<true, true>, grid, a.block, 0, a, s)
+                  : launch_k(k_coop<false, true>, grid, a.block, 0, a, s);
+  const size_t smem = smem_coop(a.t.lv_sz_w);
+  return record ? launch_k(k_coop<true, false>, grid, a.block, smem, a, s)
+                : launch_k(k_coop<false, false>, grid, a.block, smem, a, s);
+}
+
+int occupancy_coop(int threads, size_t smem, bool global) {
+  return global ? occ_of_k(k_coop<true, true>, threads, 0)
+                : occ_of_k(k_coop<true, false>, threads, smem);
 }
 
 cudaError_t launch_sp_reverse(const SweepArgs& a, int grid, cudaStream_t s) {

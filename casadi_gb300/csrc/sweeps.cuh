@@ -41,6 +41,12 @@ struct TapeView {
   int sz_w;
   int n_partials;           // partials recorded per instance
   int* err;                 // device error word
+  // level schedule of the cooperative value/record sweeps (null until first needed)
+  const u64* lcode;         // instructions level by level, slots renamed
+  const int* lbegin;        // level l is lcode[lbegin[l] .. lbegin[l+1])
+  const int* lpidx;         // first recorded partial of each lcode instruction
+  int n_levels;
+  int lv_sz_w;              // work-vector length of the renamed slots
 };
 
 struct SweepArgs {
@@ -145,6 +151,13 @@ cudaError_t launch_adjoint_dense(const SweepArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_sp_forward(const SweepArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_sp_reverse(const SweepArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_activity(const SweepArgs& a, int grid, cudaStream_t s);
+// Cooperative value (record = false) or record sweep: a.block threads (a multiple of 32, at
+// most kCoopMaxThreads) share one 32-instance tile and run its level schedule; the work vector
+// in shared memory (lv_sz_w x 32 doubles), or in a.wglob blocks when set.
+constexpr int kCoopMaxThreads = 512;
+cudaError_t launch_coop(const SweepArgs& a, bool record, int grid, cudaStream_t s);
+size_t smem_coop(int lv_sz_w);
+int occupancy_coop(int threads, size_t smem, bool global);
 
 // Resident CTAs per SM for a given kernel family and shared-memory footprint.
 int occupancy_primal(int block, size_t smem);

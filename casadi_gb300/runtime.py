@@ -63,6 +63,8 @@ def load(path=None):
                                                   vp]),
         "casadi_gb300_tape_schedule": (cint, [vp, cint, cint, vp, cint, vp, cint, vp, vp]),
         "casadi_gb300_tape_info": (cint, [cint, vp, vp, vp, vp, vp]),
+        "casadi_gb300_tape_levels": (cint, [vp, cint, cint, vp, cint, vp, cint, cint, cint, vp,
+                                             vp, vp, vp, vp]),
         "casadi_gb300_scratch_size": (cint, [cint, i64, vp]),
         "casadi_gb300_scratch_min": (cint, [cint, vp]),
         "casadi_gb300_eval": (cint, [cint, i64, i64, vp, vp, vp]),
@@ -157,6 +159,29 @@ def schedule(tape):
                                          nnz_out.ctypes.data, tape.sz_w, out.ctypes.data,
                                          ct.byref(szw)))
     return _sx.Tape.from_atomic_array(out, tape.nnz_in, tape.nnz_out, szw.value)
+
+
+def levels(tape, width=32, slot_cap=None):
+    """The level schedule of the cooperative sweeps (host only): returns (leveled tape,
+    source index of each instruction in :func:`schedule`'s tape, level offsets)."""
+    if isinstance(tape, _sx.Function):
+        tape = tape.tape
+    lib = load()
+    atoms = tape.atomic_array()
+    nnz_in = np.ascontiguousarray(tape.nnz_in, dtype=np.int32)
+    nnz_out = np.ascontiguousarray(tape.nnz_out, dtype=np.int32)
+    out = np.zeros_like(atoms)
+    src = np.zeros(max(1, tape.n_instr), dtype=np.int32)
+    begin = np.zeros(tape.n_instr + 1, dtype=np.int32)
+    nl, szw = ct.c_int(), ct.c_int()
+    cap = slot_cap if slot_cap is not None else 1 << 30
+    check(lib.casadi_gb300_tape_levels(atoms.ctypes.data, tape.n_instr, len(tape.nnz_in),
+                                       nnz_in.ctypes.data, len(tape.nnz_out),
+                                       nnz_out.ctypes.data, tape.sz_w, width, cap,
+                                       out.ctypes.data, src.ctypes.data, begin.ctypes.data,
+                                       ct.byref(nl), ct.byref(szw)))
+    lt = _sx.Tape.from_atomic_array(out, tape.nnz_in, tape.nnz_out, szw.value)
+    return lt, src[:tape.n_instr], begin[:nl.value + 1]
 
 
 class CudaTape:
@@ -349,7 +374,8 @@ class CudaTape:
         check(load().casadi_gb300_sync(self.id, _stream_handle(stream)))
 
     def set_residence(self, mode):
-        """Work-vector residence: 0 auto (tuned), 1 global memory, 2 shared memory when it fits."""
+        """Work-vector residence: 0 auto (tuned), 1 global memory, 2 shared memory when it fits,
+        3 the cooperative level sweep for value/record sweeps."""
         check(load().casadi_gb300_set_residence(self.id, mode))
 
     def set_variant(self, kind, variant):

@@ -115,6 +115,19 @@ CASADI_GB300_API int casadi_gb300_tape_schedule(const casadi_gb300_atomic* alg, 
 /* Shape queries. Cf. casadi_c_n_in_id/casadi_c_n_out_id/casadi_c_work_id (casadi_c.h:115-124):
  * sz_w is the tape's work-vector length; n_partials the partial derivatives one instance
  * records for the AD sweeps. */
+/* Host only (no device needed): the level schedule the cooperative value/record sweeps run
+ * for this tape (after the scheduling of casadi_gb300_tape_schedule): instructions grouped
+ * into levels of at most `width` mutually independent instructions, slots renamed (a slot
+ * freed at a value's last use is reused from the next level on), the scheduler deferring new
+ * values while `slot_cap` slots are live. out (n_instr entries, optional): the leveled tape in
+ * the reference's format; source (optional): each one's index in the scheduled tape;
+ * level_begin (n_levels + 1 entries, optional): level l is out[level_begin[l] ..
+ * level_begin[l+1]). Executed in order it gives the same results as the tape. */
+CASADI_GB300_API int casadi_gb300_tape_levels(const casadi_gb300_atomic* alg, int n_instr,
+                            int n_in, const int* nnz_in, int n_out, const int* nnz_out,
+                            int sz_w, int width, int slot_cap, casadi_gb300_atomic* out,
+                            int* source, int* level_begin, int* n_levels, int* sz_w_out);
+
 CASADI_GB300_API int casadi_gb300_tape_info(int id, int* n_instr, int* n_in, int* n_out, int* sz_w,
                            int* n_partials);
 
@@ -280,11 +293,15 @@ CASADI_GB300_API int casadi_gb300_autotune(int enable);
 CASADI_GB300_API int casadi_gb300_tuned_variant(int id, int kind, int* variant);
 /* Work-vector residence of a tape's sweeps: 0 (default) shared memory when the scheduled
  * work vector fits, global memory (L1/L2-cached per-CTA blocks owned by the tape) when it does
- * not, and for the value/record/sparsity sweeps the faster of the two, timed by the autotuner
- * on the first large call; 1 always global memory; 2 shared memory whenever it fits. Results
- * are identical either way. A tape whose global work
- * vectors must grow cannot be first used inside a CUDA graph capture. No counterpart in the
- * reference, whose work vector is the caller's w array (casadi/core/function_internal.hpp:414). */
+ * not, and for the value/record/sparsity sweeps the fastest candidate, timed by the autotuner
+ * on the first call of each sweep kind and launch size (at most 16 tiles of 32 instances per
+ * SM, or more): shared, global, and for value/record sweeps of the smaller launches the
+ * cooperative level sweep (several warps share a tile and run the tape's independent
+ * instructions level by level; casadi_gb300_tape_levels shows the schedule); 1 always global
+ * memory; 2 shared memory whenever it fits; 3 the cooperative sweep for value/record sweeps.
+ * Results are identical in every mode. A tape whose global work vectors must grow cannot be
+ * first used inside a CUDA graph capture. No counterpart in the reference, whose work vector
+ * is the caller's w array (casadi/core/function_internal.hpp:414). */
 CASADI_GB300_API int casadi_gb300_set_residence(int id, int mode);
 /* Fixes the variant of one kind on a tape (kinds 0 and 1: 0..4; kind 2: 0..4), or clears it
  * for retuning (-1). */

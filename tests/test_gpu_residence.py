@@ -2,7 +2,8 @@
 global memory instead of shared memory. Forced on a small tape, every result must equal the
 shared-memory path bit for bit; on a tape whose scheduled work vector does not fit shared
 memory (the quadcopter NLP's Lagrangian with both outputs, 1447 slots) the path is taken
-automatically and checked against the oracle."""
+automatically and checked against the oracle. The cooperative level sweep (residence 3: several
+warps share a tile and run the tape level by level) must give the same bits as well."""
 import numpy as np
 import pytest
 
@@ -24,7 +25,8 @@ def _host(ts):
     return [t.cpu().numpy() for t in ts]
 
 
-def test_forced_global_equals_shared(gpu_lib):
+@pytest.mark.parametrize("mode", [1, 3])
+def test_forced_residence_equals_shared(gpu_lib, mode):
     F = W.cartpole_rollout(6)
     n = 3001
     args = _dev(W.cartpole_inputs(n, steps=6, seed=41))
@@ -53,14 +55,14 @@ def test_forced_global_equals_shared(gpu_lib):
     sh.set_residence(2)
     shared = run(sh)
     g = R.CudaTape(F)
-    g.set_residence(1)
+    g.set_residence(mode)
     glob = run(g)
     for a, b in zip(shared, glob):
         for x, y in zip(a, b):
             if x.dtype == np.int64:
                 assert np.array_equal(x, y)
             else:
-                assert_bitexact(x, y, "global work vector")
+                assert_bitexact(x, y, "residence %d" % mode)
 
 
 def test_tape_larger_than_shared_memory(gpu_lib):
@@ -80,3 +82,38 @@ def test_tape_larger_than_shared_memory(gpu_lib):
     for g, w in zip(_host(asens), was):
         assert_close(g, w, "adjoint of the Lagrangian", rtol=RTOL)
     ct.sync()
+
+
+@pytest.mark.parametrize("n", [1, 31, 4096, 100000])
+def test_cooperative_sweeps_on_wide_tapes(gpu_lib, n):
+    """The quadcopter multiple-shooting constraints (34156 instructions, wide levels) and the
+    random DAG: values, the unit-seed Jacobian and the adjoint with the cooperative value and
+    record sweeps equal the sequential sweeps bit for bit (and the oracle within tolerance);
+    100000 instances is past the launch size where the autotuner considers the cooperative
+    sweep, so there it runs only because it is forced."""
+    cases = [(W.random_dag(), W.dag_inputs(n, seed=3))]
+    if n <= 4096:
+        cases.append((W.quad_ms_constraints(100), W.quad_ms_inputs(n, intervals=100, seed=3)))
+    for F, args_h in cases:
+        args = _dev(args_h)
+        rng = np.random.default_rng(n)
+        aseeds = _dev([rng.standard_normal((1, k, n)) for k in F.tape.nnz_out])
+        out = {}
+        for mode in (2, 1, 3):
+            ct = R.CudaTape(F)
+            ct.set_residence(mode)
+            r = [_host(ct.eval(args))]
+            r.append(_host(ct.reverse(args, aseeds)[1]))
+            if F.tape.n_instr < 20000:
+                r.append(_host(ct.jacobian(args)[1]))
+            ct.sync()
+            out[mode] = r
+        for mode in (1, 3):
+            for a, b in zip(out[2], out[mode]):
+                for x, y in zip(a, b):
+                    assert_bitexact(x, y, "residence %d" % mode)
+        if n <= 4096:
+            m = min(n, 64)
+            want = O.eval(F.tape, [a[:, :m].copy() for a in args_h], m)
+            for g, w in zip(out[3][0], want):
+                assert_close(g[:, :m], w, "values", rtol=RTOL)

@@ -88,3 +88,67 @@ def test_schedule_is_idempotent_on_its_output():
     s1 = R.schedule(t)
     s2 = R.schedule(s1)
     assert s2.sz_w <= s1.sz_w
+
+
+# ---- level schedule of the cooperative sweeps (casadi_gb300_tape_levels) -------------------
+def _reads_writes(op, i0, i1, i2):
+    """Slots an instruction reads and the slot it writes (None for OUTPUT)."""
+    if op == C.OP_OUTPUT:
+        return {int(i1)}, None
+    if op in (C.OP_CONST, C.OP_INPUT):
+        return set(), int(i0)
+    return ({int(i1), int(i2)} if op in C.BINARY_OPS else {int(i1)}), int(i0)
+
+
+LEVEL_CASES = CASES + [
+    ("quad_constraints", lambda: W.quad_ms_constraints(6),
+     lambda n: W.quad_ms_inputs(n, intervals=6, seed=2)),
+]
+
+
+@pytest.mark.parametrize("name,make,inputs", LEVEL_CASES, ids=[c[0] for c in LEVEL_CASES])
+@pytest.mark.parametrize("width,cap", [(8, 16), (64, 400)])
+def test_levels_are_independent_and_keep_every_bit(name, make, inputs, width, cap):
+    t = make().tape
+    s = R.schedule(t)
+    lt, src, begin = R.levels(t, width=width, slot_cap=cap)
+    # every instruction of the scheduled tape exactly once, with its own operation
+    assert sorted(src.tolist()) == list(range(s.n_instr))
+    assert np.array_equal(lt.op, s.op[src])
+    assert np.all(np.diff(begin) >= 1) and np.all(np.diff(begin) <= width)
+    assert begin[0] == 0 and begin[-1] == lt.n_instr
+    # members of a level are independent: nobody reads or writes what another member writes
+    for l in range(len(begin) - 1):
+        writes, reads = [], []
+        for k in range(begin[l], begin[l + 1]):
+            r, w = _reads_writes(lt.op[k], lt.i0[k], lt.i1[k], lt.i2[k])
+            reads.append(r)
+            writes.append(w)
+        ws = [w for w in writes if w is not None]
+        assert len(ws) == len(set(ws)), "two writes of one slot in level %d" % l
+        for a, w in enumerate(writes):
+            if w is None:
+                continue
+            for b, r in enumerate(reads):
+                assert a == b or w not in r, "level %d reads a slot it writes" % l
+    # executed in order, the leveled tape gives the same bits
+    n = 23
+    args = inputs(n)
+    _all_bits_equal(O.eval(lt, args, n), O.eval(t, args, n), "values")
+    bits = [np.full((k, n), np.uint64(0), np.uint64) for k in t.nnz_in]
+    for j, b in enumerate(bits):
+        for k in range(b.shape[0]):
+            b[k, :] = np.uint64(1) << np.uint64((j * 5 + k) % 64)
+    _all_bits_equal(O.sp_forward(lt, bits, n), O.sp_forward(t, bits, n), "sp_forward")
+
+
+def test_levels_expose_parallel_work():
+    """The 10000-node random DAG runs in a few hundred levels, the quadcopter multiple-shooting
+    constraints in far fewer levels than instructions, with a bounded work vector."""
+    dag = W.random_dag().tape
+    _, _, begin = R.levels(dag, width=64, slot_cap=400)
+    assert len(begin) - 1 < dag.n_instr / 25
+    q = W.quad_ms_constraints(100).tape
+    lt, _, begin = R.levels(q, width=64, slot_cap=400)
+    assert len(begin) - 1 < q.n_instr / 30
+    assert lt.sz_w <= 400 + 64
