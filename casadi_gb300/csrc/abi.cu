@@ -90,9 +90,11 @@ struct TanPlan {
   int groups = 0;
   uint4* d_stream = nullptr;  // entry streams of all directions
   int2* d_chunks = nullptr;   // per direction: (first entry, entry count)
+  int* d_dirmap = nullptr;    // identity mode with a dirmap: its device copy
   ~TanPlan() {
     cudaFree(d_stream);
     cudaFree(d_chunks);
+    cudaFree(d_dirmap);
   }
 };
 
@@ -145,7 +147,9 @@ struct Tape {
   // launch shapes
   int primal_block = 128, primal_grid_cap = 1;
   std::mutex shape_mtx;
-  int tuned[3] = {-1, -1, -1};  // derivative-sweep variant per kind (seeded/identity tangent, adjoint)
+  // derivative-sweep variant per kind (seeded/identity tangent, adjoint) and launch size class
+  // (0: at most 16 tiles per SM); tangent kinds may keep the cooperative sweep (TV_COUNT)
+  int tuned[3][2] = {{-1, -1}, {-1, -1}, {-1, -1}};
   std::vector<double> h_consts;  // constant pool (host copy, for inlining into callers)
   std::vector<u64> h_code;                            // padded instruction stream
   std::vector<std::unique_ptr<TanPlan>> tan_plans;
@@ -560,7 +564,8 @@ const TanPlan* tan_plan(Tape& t, int ndir, int dw, int ch, bool identity,
   }
   cudaError_t e;
   if ((e = upload(&p->d_stream, all)) != cudaSuccess ||
-      (e = upload(&p->d_chunks, se)) != cudaSuccess) {
+      (e = upload(&p->d_chunks, se)) != cudaSuccess ||
+      (identity && !dirmap.empty() && (e = upload(&p->d_dirmap, dirmap)) != cudaSuccess)) {
     *err = cuda_fail(e, "upload tangent plan");
     return nullptr;
   }
@@ -874,6 +879,29 @@ int run_deriv(Tape& t, SweepArgs a, long long m, const DerivReq& rq, cudaStream_
     return launch_tangent(a, grid_of(v), v, s);
   };
   const long long work = tiles * ndir;
+  const int cls = tiles <= 16ll * sms ? 0 : 1;
+  // the cooperative tangent sweep: a candidate for launches of few tiles whose level schedule
+  // (tangents + activity bytes) fits shared memory
+  const bool coop_ok =
+      !adjoint && cls == 0 && (capturing(s) ? t.lv_state > 0 : ensure_levels(t)) &&
+      smem_tangent_coop(t.lv_sz_w, false) <= static_cast<size_t>(max_smem_optin());
+  const int kCoop = TV_COUNT;
+  auto launch_coop_tan = [&]() -> cudaError_t {
+    static const std::vector<int> kNoMap;
+    const TanPlan* tp =
+        tan_plan(t, ndir, 1, 0, identity, seeded_in, rq.dirmap ? *rq.dirmap : kNoMap, &plan_err);
+    if (!tp) return cudaErrorInvalidValue;
+    SweepArgs c = a;
+    c.t = t.view();
+    c.block = kCoopTanThreads;
+    c.wglob = nullptr;
+    c.dirmap = tp->d_dirmap;
+    const size_t sm = smem_tangent_coop(t.lv_sz_w, false);
+    const int occ = std::max(1, occupancy_tangent_coop(sm, false));
+    const int grid = static_cast<int>(std::max<long long>(
+        1, std::min<long long>(work, static_cast<long long>(sms) * occ)));
+    return launch_tangent_coop(c, grid, s);
+  };
   if (dir_global(t)) {
     // global work vectors: one variant (G=2, 64 registers), one warp per CTA
     int grid = static_cast<int>(std::max<long long>(
@@ -896,24 +924,26 @@ int run_deriv(Tape& t, SweepArgs a, long long m, const DerivReq& rq, cudaStream_
     return gw_done(t, s);
   }
   const int n_variants = adjoint ? AV_COUNT : TV_COUNT;
-  int variant = t.tuned[kind];
-  if (variant >= 0 && !fits(variant)) variant = -1;
+  auto usable = [&](int v) { return v == kCoop ? (!adjoint && coop_ok) : fits(v); };
+  auto run_v = [&](int v) { return v == kCoop ? launch_coop_tan() : launch(v); };
+  int& kept = t.tuned[kind][cls];
+  int variant = kept;
+  if (variant >= 0 && !usable(variant)) variant = -1;
   if (variant < 0) {
-    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    cudaStreamIsCapturing(s, &cs);
-    // tune on waves that fill the GPU at least twice at 8 warps per SM, outside capture
-    if (g_autotune && cs == cudaStreamCaptureStatusNone && work >= 2ll * sms * 8) {
+    // tune outside capture: on waves that fill the GPU at least twice at 8 warps per SM, and
+    // on every small launch, where the cooperative sweep is a candidate too
+    if (g_autotune && !capturing(s) && (work >= 2ll * sms * 8 || cls == 0)) {
       float best = 0;
-      for (int v = 0; v < n_variants; ++v) {
-        if (!fits(v)) continue;
+      for (int v = 0; v <= n_variants; ++v) {
+        if (!usable(v)) continue;
         float ms = 0;
-        if (int rc = time_once(s, [&] { return launch(v); }, &ms)) return plan_err ? plan_err : rc;
+        if (int rc = time_once(s, [&] { return run_v(v); }, &ms)) return plan_err ? plan_err : rc;
         if (variant < 0 || ms < best) {
           best = ms;
           variant = v;
         }
       }
-      t.tuned[kind] = variant;
+      kept = variant;
       return 0;  // every variant's run produced this wave's (identical) results
     }
     variant = 0;  // the first variant of each list: fastest on the tapes measured
@@ -921,7 +951,7 @@ int run_deriv(Tape& t, SweepArgs a, long long m, const DerivReq& rq, cudaStream_
     if (variant == n_variants)
       return fail(CASADI_GB300_ERR_UNSUPPORTED, "no derivative-sweep variant fits");
   }
-  cudaError_t e = timed(adjoint ? F_ADJOINT : F_TANGENT, s, [&] { return launch(variant); });
+  cudaError_t e = timed(adjoint ? F_ADJOINT : F_TANGENT, s, [&] { return run_v(variant); });
   if (plan_err) return plan_err;
   if (e != cudaSuccess) return cuda_fail(e, "derivative sweep launch");
   return 0;
@@ -1532,7 +1562,7 @@ int casadi_gb300_tuned_variant(int id, int kind, int* variant) {
   Tape* t = get_tape(id);
   if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
   if (kind < 0 || kind > 2 || !variant) return fail(CASADI_GB300_ERR_ARG, "bad arguments");
-  *variant = t->tuned[kind];
+  *variant = t->tuned[kind][1] >= 0 ? t->tuned[kind][1] : t->tuned[kind][0];
   return 0;
 }
 
@@ -1548,9 +1578,9 @@ int casadi_gb300_set_residence(int id, int mode) {
 int casadi_gb300_set_variant(int id, int kind, int variant) {
   Tape* t = get_tape(id);
   if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
-  if (kind < 0 || kind > 2 || variant < -1 || variant >= (kind == 2 ? AV_COUNT : TV_COUNT))
+  if (kind < 0 || kind > 2 || variant < -1 || variant > (kind == 2 ? AV_COUNT - 1 : TV_COUNT))
     return fail(CASADI_GB300_ERR_ARG, "bad arguments");
-  t->tuned[kind] = variant;
+  t->tuned[kind][0] = t->tuned[kind][1] = variant;
   return 0;
 }
 

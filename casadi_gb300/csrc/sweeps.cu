@@ -278,6 +278,143 @@ __global__ void __launch_bounds__(kCoopMaxThreads) k_coop(const __grid_constant_
   }
 }
 
+// Cooperative tangent sweep: one CTA per (tile, direction) item runs the level schedule of
+// the forward-mode sweep over the partials the record sweep stored. Activity is structural
+// (the same for every lane), so it is kept per slot in shared memory (act) and an instruction
+// whose operands carry no derivative is skipped exactly where the sequential sweep's entry
+// stream has no entry; the arithmetic of every case is the sequential sweep's (same
+// operations, same order), so the sensitivities are the same bits. Each warp takes up to Q
+// instructions of a level at a time, loading all their operands and partials before any
+// arithmetic so the loads overlap.
+__device__ __forceinline__ bool is_arith(unsigned op) {
+  return op < D_CONST || (op >= D_ERFINV && op != D_NOP);
+}
+
+template <int Q, bool GW>
+__global__ void __launch_bounds__(kCoopMaxThreads)
+    k_tangent_coop(const __grid_constant__ SweepArgs a) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int lv = a.t.lv_sz_w;
+  double* wd = GW ? reinterpret_cast<double*>(a.wglob + blockIdx.x * a.wglob_stride)
+                  : reinterpret_cast<double*>(smem);
+  unsigned char* act = GW ? smem : smem + static_cast<size_t>(lv) * 256;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const long long ntiles = (a.n + 31) / 32;
+  const long long items = ntiles * a.ndir;
+  const int nl = a.t.n_levels;
+  const u64 nop = static_cast<u64>(D_NOP);
+  for (long long item = blockIdx.x; item < items; item += gridDim.x) {
+    const long long tile = item / a.ndir;
+    const int dir = static_cast<int>(item - tile * a.ndir);
+    const long long il = tile * 32 + lane;
+    const bool active = il < a.n;
+    const long long ig = a.i_begin + il;
+    const double* pt = a.partials + static_cast<size_t>(tile) * a.t.n_partials * 32 + lane;
+    int end = __ldg(a.t.lbegin);
+    for (int l = 0; l < nl; ++l) {
+      const int beg = end;
+      end = __ldg(a.t.lbegin + l + 1);
+      for (int base = beg + warp; base < end; base += Q * nw) {
+        u64 ins[Q];
+        unsigned fl[Q];
+        double p0[Q], p1[Q], xb[Q], xc[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+          const int i = base + q * nw;
+          ins[q] = i < end ? __ldg(a.t.lcode + i) : nop;
+          fl[q] = 0;
+          p0[q] = 1.0;
+          p1[q] = 0.0;
+          xb[q] = 0.0;
+          xc[q] = 0.0;
+          const unsigned op = dec_op(ins[q]), B = dec_b(ins[q]), C = dec_c(ins[q]);
+          if (is_arith(op)) {
+            const bool fb = act[B] && carries_d0(op);
+            const bool fc = act[C] && carries_d1(op);
+            fl[q] = (fb ? 1u : 0u) | (fc ? 2u : 0u);
+            const unsigned m = partial_mask(op);
+            if (m & fl[q]) {
+              const size_t pk = static_cast<size_t>(__ldg(a.t.lpidx + i));
+              if (m & fl[q] & 1u) p0[q] = __ldg(pt + pk * 32);
+              if (m & fl[q] & 2u) p1[q] = __ldg(pt + (pk + (m & 1u)) * 32);
+            }
+            if (fb) xb[q] = wd[B * 32 + lane];
+            if (fc) xc[q] = wd[C * 32 + lane];
+          } else if (op == D_OUTPUT) {
+            fl[q] = act[B] ? 1u : 0u;
+            if (fl[q]) xb[q] = wd[B * 32 + lane];
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+          const unsigned op = dec_op(ins[q]), A = dec_a(ins[q]), B = dec_b(ins[q]),
+                         C = dec_c(ins[q]);
+          const unsigned f = fl[q];
+          if (op == D_NOP) continue;
+          if (op == D_CONST) {
+            if (lane == 0) act[A] = 0;
+            continue;
+          }
+          if (op == D_INPUT) {
+            bool on;
+            double v = 0.0;
+            if (a.identity_seed) {
+              const int flat = a.in_off[B] + static_cast<int>(C);
+              on = (a.dirmap ? __ldg(a.dirmap + flat) : flat) == dir;
+              v = 1.0;
+            } else {
+              const IoDesc& d = a.seed[B];
+              on = d.ptr != nullptr;
+              if (on && active)
+                v = __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir, C, ig));
+            }
+            if (on) wd[A * 32 + lane] = v;
+            if (lane == 0) act[A] = on ? 1 : 0;
+            continue;
+          }
+          if (op == D_OUTPUT) {
+            const IoDesc& d = a.sens[A];
+            if (active && d.ptr)
+              static_cast<double*>(d.ptr)[io_off(d, dir, C, ig)] = f ? xb[q] : 0.0;
+            continue;
+          }
+          if (!f) {
+            if (lane == 0) act[A] = 0;
+            continue;
+          }
+          double r;
+          switch (op) {
+            case D_ADD:
+              r = f == 3u ? __dadd_rn(xb[q], xc[q]) : (f == 1u ? xb[q] : xc[q]);
+              break;
+            case D_SUB:
+              r = f == 3u ? __dsub_rn(xb[q], xc[q]) : (f == 1u ? xb[q] : d_neg(xc[q]));
+              break;
+            case D_NEG:
+              r = d_neg(xb[q]);
+              break;
+            case D_TWICE:
+              r = d_twice(xb[q]);
+              break;
+            case D_ASSIGN:
+              r = xb[q];
+              break;
+            case D_IF_ELSE_ZERO:
+              r = d_iszero(p1[q]) ? 0.0 : xc[q];
+              break;
+            default:
+              r = f == 3u ? __dadd_rn(__dmul_rn(p0[q], xb[q]), __dmul_rn(p1[q], xc[q]))
+                          : (f == 1u ? __dmul_rn(p0[q], xb[q]) : __dmul_rn(p1[q], xc[q]));
+          }
+          wd[A * 32 + lane] = r;
+          if (lane == 0) act[A] = 1;
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------------------------
 // Plan-free adjoint sweep (the allocation-free entry point).
 //
@@ -1257,6 +1394,23 @@ cudaError_t launch_coop(const SweepArgs& a, bool record, int grid, cudaStream_t 
   const size_t smem = smem_coop(a.t.lv_sz_w);
   return record ? launch_k(k_coop<true, false>, grid, a.block, smem, a, s)
                 : launch_k(k_coop<false, false>, grid, a.block, smem, a, s);
+}
+
+size_t smem_tangent_coop(int lv_sz_w, bool global) {
+  const size_t slots = static_cast<size_t>(lv_sz_w > 0 ? lv_sz_w : 1);
+  return (global ? 0 : slots * 256) + ((slots + 15) / 16) * 16;
+}
+
+cudaError_t launch_tangent_coop(const SweepArgs& a, int grid, cudaStream_t s) {
+  if (a.block != kCoopTanThreads) return cudaErrorInvalidValue;
+  const size_t smem = smem_tangent_coop(a.t.lv_sz_w, a.wglob != nullptr);
+  return a.wglob ? launch_k(k_tangent_coop<kCoopTanQ, true>, grid, a.block, smem, a, s)
+                 : launch_k(k_tangent_coop<kCoopTanQ, false>, grid, a.block, smem, a, s);
+}
+
+int occupancy_tangent_coop(size_t smem, bool global) {
+  return global ? occ_of_k(k_tangent_coop<kCoopTanQ, true>, kCoopTanThreads, smem)
+                : occ_of_k(k_tangent_coop<kCoopTanQ, false>, kCoopTanThreads, smem);
 }
 
 int occupancy_coop(int threads, size_t smem, bool global) {

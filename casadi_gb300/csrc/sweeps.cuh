@@ -75,6 +75,7 @@ struct SweepArgs {
   // global work vector (null: shared memory): CTA b uses wglob + b*wglob_stride
   unsigned char* wglob;
   long long wglob_stride;
+  const int* dirmap;                // cooperative tangent, identity seeds (see launch_tangent_coop)
 };
 
 // One item of a persistent batch: a tape over its own instance range.
@@ -156,6 +157,14 @@ cudaError_t launch_activity(const SweepArgs& a, int grid, cudaStream_t s);
 // in shared memory (lv_sz_w x 32 doubles), or in a.wglob blocks when set.
 constexpr int kCoopMaxThreads = 512;
 cudaError_t launch_coop(const SweepArgs& a, bool record, int grid, cudaStream_t s);
+// Cooperative tangent sweep over recorded partials: one CTA of kCoopTanThreads threads per
+// (tile, direction) item; identity seeds use a.dirmap (flat input nonzero -> direction, null:
+// the nonzero's own index) and a.in_off. Shared memory: smem_tangent_coop.
+constexpr int kCoopTanThreads = 512;
+constexpr int kCoopTanQ = 4;  // instructions per warp and level handled at once
+cudaError_t launch_tangent_coop(const SweepArgs& a, int grid, cudaStream_t s);
+size_t smem_tangent_coop(int lv_sz_w, bool global);
+int occupancy_tangent_coop(size_t smem, bool global);
 size_t smem_coop(int lv_sz_w);
 int occupancy_coop(int threads, size_t smem, bool global);
 

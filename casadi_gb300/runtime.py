@@ -659,7 +659,8 @@ class Batch:
                                             _stream_handle(stream)))
 
 
-N_TAN_VARIANTS = 5  # tangent-sweep kernel variants (forward, Jacobian)
+N_TAN_VARIANTS = 6  # tangent-sweep kernel variants (forward, Jacobian); the last one is the
+#                     cooperative level sweep, used only by launches of few tiles
 N_ADJ_VARIANTS = 5  # adjoint-sweep kernel variants
 
 FAMILIES = ("eval", "record", "tangent", "adjoint", "sp_forward", "sp_reverse", "batch",

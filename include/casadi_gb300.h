@@ -283,9 +283,11 @@ CASADI_GB300_API int casadi_gb300_map_jacobian_reverse(int id, int mem, int64_t 
                            int nadj, const double* const* aseed, double* const* asens);
 
 /* Autotuning of the derivative sweeps (on by default): the first call of each kind
- * (0 seeded forward, 1 Jacobian, 2 adjoint) on a tape whose wave fills the GPU several times
- * runs each kernel variant once on that wave, keeps the fastest for the tape and synchronizes
- * the stream once; it is skipped while the stream is being captured into a CUDA graph.
+ * (0 seeded forward, 1 Jacobian, 2 adjoint) and launch size (at most 16 tiles per SM, or more)
+ * on a tape runs each kernel variant once on that wave (large launches: those that fill the
+ * GPU several times; small launches also try the cooperative level sweep), keeps the fastest
+ * for the tape and synchronizes the stream once; it is skipped while the stream is being
+ * captured into a CUDA graph.
  * Variants differ only in speed: every variant does the same arithmetic in the same order.
  * casadi_gb300_tuned_variant reports the kept variant (-1: not tuned yet). No counterpart in
  * the reference, whose Map has one code path per parallelization (casadi/core/map.cpp:39-51). */
@@ -303,8 +305,9 @@ CASADI_GB300_API int casadi_gb300_tuned_variant(int id, int kind, int* variant);
  * first used inside a CUDA graph capture. No counterpart in the reference, whose work vector
  * is the caller's w array (casadi/core/function_internal.hpp:414). */
 CASADI_GB300_API int casadi_gb300_set_residence(int id, int mode);
-/* Fixes the variant of one kind on a tape (kinds 0 and 1: 0..4; kind 2: 0..4), or clears it
- * for retuning (-1). */
+/* Fixes the variant of one kind on a tape (kinds 0 and 1: 0..5, 5 = the cooperative level
+ * sweep, which only launches of at most 16 tiles per SM use; kind 2: 0..4), or clears it for
+ * retuning (-1). */
 CASADI_GB300_API int casadi_gb300_set_variant(int id, int kind, int variant);
 
 /* Colour-compressed Jacobian: n_colors forward directions, direction d seeded with 1 on
