@@ -99,3 +99,23 @@ def test_colored_sweeps_in_one_batch_launch(gpu_lib):
         got_h = H.gather(ch, n).cpu().numpy()
         assert same_bits(got_j, want_j).all()
         assert same_bits(got_h, want_h).all()
+
+
+@pytest.mark.parametrize("variant", [0, 5])
+def test_colored_sweeps_same_bits_in_every_tangent_variant(gpu_lib, variant):
+    """Coloured seeding (identity directions through a colour map) with the sequential
+    tangent sweep (variant 0) and the cooperative level sweep (variant 5): the same bits as
+    the autotuned call."""
+    from casadi_gb300.sparse_ad import ColoredHessian, ColoredJacobian
+    L = W.quad_ms_lagrangian(INTERVALS)
+    J = ColoredJacobian(W.quad_ms_constraints(INTERVALS), out=0, wrt=0)
+    H = ColoredHessian(L, out=1, wrt=0)
+    n = 777
+    args = [torch.from_numpy(a).cuda() for a in _inputs(n, 4)]
+    want_j, want_h = J(args).cpu().numpy(), H(args).cpu().numpy()
+    J.tape.set_variant(1, variant)
+    H.tape.set_variant(1, variant)
+    got_j, got_h = J(args).cpu().numpy(), H(args).cpu().numpy()
+    assert same_bits(got_j, want_j).all()
+    assert same_bits(got_h, want_h).all()
+    J.tape.sync()
