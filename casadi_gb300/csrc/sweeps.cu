@@ -1435,13 +1435,16 @@ int occupancy_gw_sp() { return occ_of_k(k_sp_reverse<kGwBlock, true>, kGwBlock, 
   X(TV_G2_R64, 2, 32, 1, 1)    \
   X(TV_G1_R64, 1, 32, 1, 1)    \
   X(TV_G2_K2, 2, 16, 1, 2)     \
-  X(TV_G2_K4, 2, 8, 1, 4)
+  X(TV_G2_K4, 2, 8, 1, 4)      \
+  X(TV_G4_R128, 4, 16, 1, 1)   \
+  X(TV_G8_R256, 8, 8, 1, 1)
 #define CGB_ADJ_VARIANTS(X)    \
   X(AV_G2_R80, 2, 24, 1)       \
   X(AV_G1_R64, 1, 32, 1)       \
   X(AV_G2_R64, 2, 32, 1)       \
   X(AV_G2_I2_R128, 2, 16, 2)   \
-  X(AV_G4_R128, 4, 16, 1)
+  X(AV_G4_R128, 4, 16, 1)      \
+  X(AV_G8_R256, 8, 8, 1)
 
 void tan_variant_shape(int variant, int* ipt, int* k) {
   *ipt = 1;

@@ -141,8 +141,13 @@ cudaError_t launch_record(const SweepArgs& a, int grid, cudaStream_t s);
 // and, for the tangent sweep, directions per warp (K, walking the union stream of K
 // directions). All variants do the same arithmetic in the same order; only speed differs, so
 // the host may pick any. A variant's work vector takes smem_lean(sz_w, IPT*K, 0) bytes.
-enum TanVariant : int { TV_G2_R80 = 0, TV_G2_R64, TV_G1_R64, TV_G2_K2, TV_G2_K4, TV_COUNT };
-enum AdjVariant : int { AV_G2_R80 = 0, AV_G1_R64, AV_G2_R64, AV_G2_I2_R128, AV_G4_R128, AV_COUNT };
+// G8/G4 variants keep more partial loads in flight per warp: for launches with few warps per SM
+enum TanVariant : int {
+  TV_G2_R80 = 0, TV_G2_R64, TV_G1_R64, TV_G2_K2, TV_G2_K4, TV_G4_R128, TV_G8_R256, TV_COUNT
+};
+enum AdjVariant : int {
+  AV_G2_R80 = 0, AV_G1_R64, AV_G2_R64, AV_G2_I2_R128, AV_G4_R128, AV_G8_R256, AV_COUNT
+};
 void tan_variant_shape(int variant, int* ipt, int* k);
 int adj_variant_ipt(int variant);
 cudaError_t launch_tangent(const SweepArgs& a, int grid, int variant, cudaStream_t s);

@@ -659,9 +659,9 @@ class Batch:
                                             _stream_handle(stream)))
 
 
-N_TAN_VARIANTS = 6  # tangent-sweep kernel variants (forward, Jacobian); the last one is the
+N_TAN_VARIANTS = 8  # tangent-sweep kernel variants (forward, Jacobian); the last one is the
 #                     cooperative level sweep, used only by launches of few tiles
-N_ADJ_VARIANTS = 5  # adjoint-sweep kernel variants
+N_ADJ_VARIANTS = 6  # adjoint-sweep kernel variants
 
 FAMILIES = ("eval", "record", "tangent", "adjoint", "sp_forward", "sp_reverse", "batch",
             "activity")

@@ -305,8 +305,8 @@ CASADI_GB300_API int casadi_gb300_tuned_variant(int id, int kind, int* variant);
  * first used inside a CUDA graph capture. No counterpart in the reference, whose work vector
  * is the caller's w array (casadi/core/function_internal.hpp:414). */
 CASADI_GB300_API int casadi_gb300_set_residence(int id, int mode);
-/* Fixes the variant of one kind on a tape (kinds 0 and 1: 0..5, 5 = the cooperative level
- * sweep, which only launches of at most 16 tiles per SM use; kind 2: 0..4), or clears it for
+/* Fixes the variant of one kind on a tape (kinds 0 and 1: 0..7, 7 = the cooperative level
+ * sweep, which only launches of at most 16 tiles per SM use; kind 2: 0..5), or clears it for
  * retuning (-1). */
 CASADI_GB300_API int casadi_gb300_set_variant(int id, int kind, int variant);
 

@@ -101,10 +101,10 @@ def test_colored_sweeps_in_one_batch_launch(gpu_lib):
         assert same_bits(got_h, want_h).all()
 
 
-@pytest.mark.parametrize("variant", [0, 5])
+@pytest.mark.parametrize("variant", [0, 6, 7])
 def test_colored_sweeps_same_bits_in_every_tangent_variant(gpu_lib, variant):
     """Coloured seeding (identity directions through a colour map) with the sequential
-    tangent sweep (variant 0) and the cooperative level sweep (variant 5): the same bits as
+    tangent sweep (variants 0 and 6) and the cooperative level sweep (variant 7): the same bits as
     the autotuned call."""
     from casadi_gb300.sparse_ad import ColoredHessian, ColoredJacobian
     L = W.quad_ms_lagrangian(INTERVALS)
