@@ -924,7 +924,9 @@ int run_deriv(Tape& t, SweepArgs a, long long m, const DerivReq& rq, cudaStream_
     return gw_done(t, s);
   }
   const int n_variants = adjoint ? AV_COUNT : TV_COUNT;
-  auto usable = [&](int v) { return v == kCoop ? (!adjoint && coop_ok) : fits(v); };
+  auto usable = [&](int v) {
+    return v == kCoop ? (!adjoint && coop_ok) : (v >= 0 && v < n_variants && fits(v));
+  };
   auto run_v = [&](int v) { return v == kCoop ? launch_coop_tan() : launch(v); };
   int& kept = t.tuned[kind][cls];
   int variant = kept;
@@ -934,8 +936,10 @@ int run_deriv(Tape& t, SweepArgs a, long long m, const DerivReq& rq, cudaStream_
     // on every small launch, where the cooperative sweep is a candidate too
     if (g_autotune && !capturing(s) && (work >= 2ll * sms * 8 || cls == 0)) {
       float best = 0;
-      for (int v = 0; v <= n_variants; ++v) {
-        if (!usable(v)) continue;
+      for (int c = 0; c <= n_variants; ++c) {
+        // the variants of the kind, then (tangents) the cooperative sweep
+        const int v = c < n_variants ? c : kCoop;
+        if ((c == n_variants && adjoint) || !usable(v)) continue;
         float ms = 0;
         if (int rc = time_once(s, [&] { return run_v(v); }, &ms)) return plan_err ? plan_err : rc;
         if (variant < 0 || ms < best) {
