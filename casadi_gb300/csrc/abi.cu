@@ -2018,6 +2018,16 @@ struct BatchHost {
   unsigned* d_flags = nullptr;    // tile flags of split items
   size_t n_flags = 0;
   std::vector<double*> d_tile_partials;  // per split item
+  // split items whose record sweep runs as a cooperative level sweep before the persistent
+  // launch (few tiles: the per-tile record units would leave the GPU idle), their flags set
+  // once it is done
+  struct PreRecord {
+    int item;
+    size_t flag0;
+    long long tiles;
+    double* partials;
+  };
+  std::vector<PreRecord> pre;
   int n_units = 0;
   int szw = 1, pmax = 0, grid = 1;
   size_t smem = 0;
@@ -2077,6 +2087,7 @@ int batch_prepare(BatchHost& b) {
   std::vector<std::pair<double, int4>> units, dir_units;
   std::vector<std::pair<size_t, size_t>> flag_off;  // (item, first flag) of split items
   size_t n_flags = 0;
+  b.pre.clear();
   b.szw = 1;
   b.pmax = 0;
   for (size_t k = 0; k < b.items.size(); ++k) {
@@ -2132,9 +2143,18 @@ int batch_prepare(BatchHost& b) {
           (e = cudaMemcpy(se.data(), bi.tan_chunks, sizeof(int2) * it.ndir,
                           cudaMemcpyDeviceToHost)) != cudaSuccess)
         return cuda_fail(e, "read tangent plan");
+      // few tiles: the record sweep runs cooperatively (several warps per tile) before the
+      // persistent launch instead of as one-warp record units
+      const bool pre = tiles <= 4ll * sm_count() && ensure_levels(*t) &&
+                       smem_coop(t->lv_sz_w) <= static_cast<size_t>(max_smem_optin());
+      if (pre) {
+        b.pre.push_back({static_cast<int>(k), n_flags, tiles, tp});
+        bi.t = t->view();
+      }
       for (long long tile = 0; tile < tiles; ++tile) {
-        units.push_back({static_cast<double>(t->n_instr),
-                         make_int4(static_cast<int>(k), static_cast<int>(tile), -1, 0)});
+        if (!pre)
+          units.push_back({static_cast<double>(t->n_instr),
+                           make_int4(static_cast<int>(k), static_cast<int>(tile), -1, 0)});
         for (int d = 0; d < it.ndir; ++d) {
           const double len = it.forward ? se[d].y : bi.adj_ngr * kBatchGroup;
           dir_units.push_back({len, make_int4(static_cast<int>(k), static_cast<int>(tile), d, 0)});
@@ -2196,6 +2216,24 @@ int batch_enqueue(BatchHost& b, void* scratch, cudaStream_t s, bool gw) {
   if (e == cudaSuccess && b.n_flags)
     e = cudaMemsetAsync(b.d_flags, 0, b.n_flags * sizeof(unsigned), s);
   if (e != cudaSuccess) return cuda_fail(e, "reset batch counter");
+  for (const auto& pr : b.pre) {
+    const auto& it = b.items[pr.item];
+    Tape* t = get_tape(it.tape);
+    if (!t) return fail(CASADI_GB300_ERR_ID, "batch item %d: tape %d is gone", pr.item, it.tape);
+    SweepArgs a = base_args(*t, it.n, 0);
+    for (int j = 0; j < t->n_in; ++j) a.in[j] = it.io[j];
+    for (int j = 0; j < t->n_out; ++j) a.out[j] = it.io[kMaxIo + j];
+    a.partials = pr.partials;
+    a.block = kCoopThreads;
+    const size_t sm = smem_coop(t->lv_sz_w);
+    const int occ = std::max(1, occupancy_coop(kCoopThreads, sm, false));
+    const int grid = static_cast<int>(std::min<long long>(pr.tiles, 1ll * occ * sm_count()));
+    if ((e = launch_coop(a, true, grid, s)) != cudaSuccess) return cuda_fail(e, "batch record");
+    // every tile of the item is recorded: its direction units need not wait
+    if ((e = cudaMemsetAsync(b.d_flags + pr.flag0, 0xff, pr.tiles * sizeof(unsigned), s)) !=
+        cudaSuccess)
+      return cuda_fail(e, "batch flags");
+  }
   BatchArgs a;
   a.items = b.d_items;
   a.units = b.d_units;

@@ -22,11 +22,15 @@ def _cuda(a):
 
 def _items():
     """(Function, n, nadj, inputs) covering eval-only and adjoint items, ragged tiles, a
-    one-instance item and two tapes of very different length."""
+    one-instance item, two tapes of very different length, and split items (two or more
+    directions) recorded cooperatively before the launch (few tiles) or by record units."""
     out = []
     f = W.cartpole_rollout(4)
     out.append((f, 1000, 1, W.cartpole_inputs(1000, steps=4, seed=1)))
     out.append((f, 33, 2, W.cartpole_inputs(33, steps=4, seed=2)))
+    # two directions over more tiles than the cooperative pre-record takes: per-tile record
+    # units inside the persistent launch
+    out.append((f, 20000, 2, W.cartpole_inputs(20000, steps=4, seed=7)))
     g = W.random_dag(n_in=16, n_nodes=3000, n_out=4, seed=3, window=64, bounded=True)
     out.append((g, 5000, 1, W.dag_inputs(5000, n_in=16, seed=3)))
     out.append((g, 1, 0, W.dag_inputs(1, n_in=16, seed=4)))
