@@ -129,6 +129,12 @@ struct Tape {
   int* d_lbegin = nullptr;
   int* d_lpidx = nullptr;
   int n_levels = 0, lv_sz_w = 0;
+  // the reverse sweep's level schedule (users of each value in order), built on first use
+  int rlv_state = 0;
+  u64* d_rcode = nullptr;
+  int* d_rbegin = nullptr;
+  int* d_rpidx = nullptr;
+  int n_rlevels = 0, rlv_sz_w = 0;
   // global work vector: per-CTA blocks, grown on demand; uses on different streams are
   // ordered by gw_event
   std::mutex gw_mtx;
@@ -169,6 +175,9 @@ struct Tape {
     cudaFree(d_lcode);
     cudaFree(d_lbegin);
     cudaFree(d_lpidx);
+    cudaFree(d_rcode);
+    cudaFree(d_rbegin);
+    cudaFree(d_rpidx);
     if (gw_event) cudaEventSynchronize(gw_event);
     cudaFree(d_gw);
     if (gw_event) cudaEventDestroy(gw_event);
@@ -191,6 +200,11 @@ struct Tape {
     v.lpidx = d_lpidx;
     v.n_levels = n_levels;
     v.lv_sz_w = lv_sz_w;
+    v.rcode = d_rcode;
+    v.rbegin = d_rbegin;
+    v.rpidx = d_rpidx;
+    v.n_rlevels = n_rlevels;
+    v.rlv_sz_w = rlv_sz_w;
     return v;
   }
 };
@@ -669,14 +683,15 @@ enum PrimalKind { PK_EVAL = 0, PK_RECORD, PK_SP_FORWARD, PK_SP_REVERSE, PK_ACTIV
 // whether it is available; never called while the stream is being captured.
 constexpr int kLevelWidth = 64;      // instructions per level
 constexpr int kCoopThreads = 256;    // warps of a cooperative CTA x 32
-bool ensure_levels(Tape& t) {
+bool ensure_levels(Tape& t, bool reverse = false) {
   std::lock_guard<std::mutex> lk(t.shape_mtx);
-  if (t.lv_state != 0) return t.lv_state > 0;
-  t.lv_state = -1;
+  int& state = reverse ? t.rlv_state : t.lv_state;
+  if (state != 0) return state > 0;
+  state = -1;
   Levels lv;
   std::string err;
   const int cap = t.sz_w <= 400 ? 400 : t.sz_w + kLevelWidth;
-  const int nl = level_schedule(t.h_code, kLevelWidth, cap, lv, err);
+  const int nl = level_schedule(t.h_code, kLevelWidth, cap, lv, err, reverse);
   if (nl <= 0 || lv.code.empty()) return false;
   u64* code = nullptr;
   int *begin = nullptr, *pidx = nullptr;
@@ -697,12 +712,20 @@ bool ensure_levels(Tape& t) {
     cudaGetLastError();
     return false;
   }
-  t.d_lcode = code;
-  t.d_lbegin = begin;
-  t.d_lpidx = pidx;
-  t.n_levels = nl;
-  t.lv_sz_w = lv.sz_w;
-  t.lv_state = 1;
+  if (reverse) {
+    t.d_rcode = code;
+    t.d_rbegin = begin;
+    t.d_rpidx = pidx;
+    t.n_rlevels = nl;
+    t.rlv_sz_w = lv.sz_w;
+  } else {
+    t.d_lcode = code;
+    t.d_lbegin = begin;
+    t.d_lpidx = pidx;
+    t.n_levels = nl;
+    t.lv_sz_w = lv.sz_w;
+  }
+  state = 1;
   return true;
 }
 
@@ -883,9 +906,22 @@ int run_deriv(Tape& t, SweepArgs a, long long m, const DerivReq& rq, cudaStream_
   // the cooperative tangent sweep: a candidate for launches of few tiles whose level schedule
   // (tangents + activity bytes) fits shared memory
   const bool coop_ok =
-      !adjoint && cls == 0 && (capturing(s) ? t.lv_state > 0 : ensure_levels(t)) &&
-      smem_tangent_coop(t.lv_sz_w, false) <= static_cast<size_t>(max_smem_optin());
-  const int kCoop = TV_COUNT;
+      cls == 0 &&
+      (capturing(s) ? (adjoint ? t.rlv_state : t.lv_state) > 0 : ensure_levels(t, adjoint)) &&
+      smem_tangent_coop(adjoint ? t.rlv_sz_w : t.lv_sz_w, false) <=
+          static_cast<size_t>(max_smem_optin());
+  const int kCoop = adjoint ? AV_COUNT : TV_COUNT;
+  auto launch_coop_adj = [&]() -> cudaError_t {
+    SweepArgs c = a;
+    c.t = t.view();
+    c.block = kCoopTanThreads;
+    c.wglob = nullptr;
+    const int occ =
+        std::max(1, occupancy_adjoint_coop(smem_tangent_coop(t.rlv_sz_w, false)));
+    const int grid = static_cast<int>(std::max<long long>(
+        1, std::min<long long>(work, static_cast<long long>(sms) * occ)));
+    return launch_adjoint_coop(c, grid, s);
+  };
   auto launch_coop_tan = [&]() -> cudaError_t {
     static const std::vector<int> kNoMap;
     const TanPlan* tp =
@@ -925,9 +961,11 @@ int run_deriv(Tape& t, SweepArgs a, long long m, const DerivReq& rq, cudaStream_
   }
   const int n_variants = adjoint ? AV_COUNT : TV_COUNT;
   auto usable = [&](int v) {
-    return v == kCoop ? (!adjoint && coop_ok) : (v >= 0 && v < n_variants && fits(v));
+    return v == kCoop ? coop_ok : (v >= 0 && v < n_variants && fits(v));
   };
-  auto run_v = [&](int v) { return v == kCoop ? launch_coop_tan() : launch(v); };
+  auto run_v = [&](int v) {
+    return v == kCoop ? (adjoint ? launch_coop_adj() : launch_coop_tan()) : launch(v);
+  };
   int& kept = t.tuned[kind][cls];
   int variant = kept;
   if (variant >= 0 && !usable(variant)) variant = -1;
@@ -939,7 +977,7 @@ int run_deriv(Tape& t, SweepArgs a, long long m, const DerivReq& rq, cudaStream_
       for (int c = 0; c <= n_variants; ++c) {
         // the variants of the kind, then (tangents) the cooperative sweep
         const int v = c < n_variants ? c : kCoop;
-        if ((c == n_variants && adjoint) || !usable(v)) continue;
+        if (!usable(v)) continue;
         float ms = 0;
         if (int rc = time_once(s, [&] { return run_v(v); }, &ms)) return plan_err ? plan_err : rc;
         if (variant < 0 || ms < best) {
@@ -1225,14 +1263,17 @@ int casadi_gb300_tape_levels(const casadi_gb300_atomic* alg, int n_instr, int n_
                              const int* nnz_in, int n_out, const int* nnz_out, int sz_w,
                              int width, int slot_cap, casadi_gb300_atomic* out, int* source,
                              int* level_begin, int* n_levels, int* sz_w_out) {
-  if (!n_levels || !sz_w_out || width < 1 || slot_cap < 1)
+  if (!n_levels || !sz_w_out || width == 0 || width < -(1 << 20) || slot_cap < 1)
     return fail(CASADI_GB300_ERR_ARG, "bad arguments");
+  // a negative width asks for the schedule of the cooperative reverse sweep (ordered users)
+  const bool ordered = width < 0;
+  if (ordered) width = -width;
   Encoded en;
   const int wlen = encode_and_schedule(alg, n_instr, n_in, nnz_in, n_out, nnz_out, sz_w, en);
   if (wlen < 0) return wlen;
   Levels lv;
   std::string err;
-  const int nl = level_schedule(en.code, width, slot_cap, lv, err);
+  const int nl = level_schedule(en.code, width, slot_cap, lv, err, ordered);
   if (nl < 0) return fail(CASADI_GB300_ERR_ARG, "%s", err.c_str());
   *n_levels = nl;
   *sz_w_out = lv.sz_w;
@@ -1582,7 +1623,7 @@ int casadi_gb300_set_residence(int id, int mode) {
 int casadi_gb300_set_variant(int id, int kind, int variant) {
   Tape* t = get_tape(id);
   if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
-  if (kind < 0 || kind > 2 || variant < -1 || variant > (kind == 2 ? AV_COUNT - 1 : TV_COUNT))
+  if (kind < 0 || kind > 2 || variant < -1 || variant > (kind == 2 ? AV_COUNT : TV_COUNT))
     return fail(CASADI_GB300_ERR_ARG, "bad arguments");
   t->tuned[kind][0] = t->tuned[kind][1] = variant;
   return 0;

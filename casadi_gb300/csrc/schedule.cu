@@ -215,7 +215,7 @@ int schedule_code(const std::vector<u64>& in, std::vector<u64>& out, std::string
 }
 
 int level_schedule(const std::vector<u64>& in, int width, int slot_cap, Levels& out,
-                   std::string& err) {
+                   std::string& err, bool ordered_users) {
   const int n = static_cast<int>(in.size());
   out = Levels();
   out.begin.push_back(0);
@@ -280,6 +280,20 @@ int level_schedule(const std::vector<u64>& in, int width, int slot_cap, Levels& 
   for (int k = 0; k < n; ++k)
     for (int d : {dep0[k], dep1[k]})
       if (d >= 0) ++uses[d];
+  if (ordered_users) {
+    // consecutive users of each non-constant value in consecutive levels: the reverse sweep
+    // then adds the contributions to every adjoint in the order of `in` (last user first)
+    std::vector<int> last_user(n, -1);
+    for (int k = 0; k < n; ++k)
+      for (int d : {dep0[k], dep1[k]}) {
+        if (d < 0 || dec_op(in[d]) == D_CONST) continue;
+        if (last_user[d] >= 0 && last_user[d] != k) {
+          succ[last_user[d]].push_back(k);
+          ++npred[k];
+        }
+        last_user[d] = k;
+      }
+  }
 
   // Priority: position in `in` (the register-pressure order). The earliest ready instruction
   // of each level always runs -- that is the sequential order's own progress, which needs no

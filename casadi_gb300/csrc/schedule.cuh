@@ -38,7 +38,9 @@ struct Levels {
 // ready instruction always runs, later ones join a level only while fewer than `slot_cap`
 // values are live or a slot is free.
 // Returns the number of levels, or -1 with `err` set.
+// With `ordered_users` the users of every non-constant value also keep their order of `in`
+// across levels (no two in one level), as the cooperative reverse sweep needs.
 int level_schedule(const std::vector<u64>& in, int width, int slot_cap, Levels& out,
-                   std::string& err);
+                   std::string& err, bool ordered_users = false);
 
 }  // namespace cgb

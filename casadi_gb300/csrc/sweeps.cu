@@ -415,6 +415,161 @@ __global__ void __launch_bounds__(kCoopMaxThreads)
   }
 }
 
+// Cooperative adjoint sweep: one CTA per (tile, direction) item walks the reverse level
+// schedule (whose levels also keep the users of every value in order, so each adjoint
+// receives its contributions in the order of the sequential sweep, last user first). The
+// activity of each slot's adjoint lives in shared memory (act) and decides, like the
+// sequential sweep's plan, whether a contribution is the first (assigned) or added; the
+// arithmetic of every case is the sequential sweep's, so the sensitivities are the same bits.
+template <int Q>
+__global__ void __launch_bounds__(kCoopMaxThreads)
+    k_adjoint_coop(const __grid_constant__ SweepArgs a) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int lv = a.t.rlv_sz_w;
+  double* wd = reinterpret_cast<double*>(smem);
+  unsigned char* act = smem + static_cast<size_t>(lv) * 256;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const long long ntiles = (a.n + 31) / 32;
+  const long long items = ntiles * a.ndir;
+  const int nl = a.t.n_rlevels;
+  const u64 nop = static_cast<u64>(D_NOP);
+  for (long long item = blockIdx.x; item < items; item += gridDim.x) {
+    const long long tile = item / a.ndir;
+    const int dir = static_cast<int>(item - tile * a.ndir);
+    const long long il = tile * 32 + lane;
+    const bool active = il < a.n;
+    const long long ig = a.i_begin + il;
+    const double* pt = a.partials + static_cast<size_t>(tile) * a.t.n_partials * 32 + lane;
+    for (int k = threadIdx.x; k < lv; k += blockDim.x) act[k] = 0;
+    for (int k = warp; k < a.n_zero; k += nw) {
+      const int2 jk = __ldg(a.zero_in + k);
+      const IoDesc& d = a.sens[jk.x];
+      if (active && d.ptr) static_cast<double*>(d.ptr)[io_off(d, dir, jk.y, ig)] = 0.0;
+    }
+    __syncthreads();
+    int beg = __ldg(a.t.rbegin + nl);
+    for (int l = nl - 1; l >= 0; --l) {
+      const int end = beg;
+      beg = __ldg(a.t.rbegin + l);
+      for (int base = beg + warp; base < end; base += Q * nw) {
+        u64 ins[Q];
+        unsigned fl[Q];  // 1 result active, 2/4 b/c receives, 8/16 first to b/c
+        double sd[Q], p0[Q], p1[Q], ob[Q], oc[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+          const int i = base + q * nw;
+          ins[q] = i < end ? __ldg(a.t.rcode + i) : nop;
+          fl[q] = 0;
+          sd[q] = 0.0;
+          p0[q] = 1.0;
+          p1[q] = 0.0;
+          ob[q] = 0.0;
+          oc[q] = 0.0;
+          const unsigned op = dec_op(ins[q]), A = dec_a(ins[q]), B = dec_b(ins[q]),
+                         C = dec_c(ins[q]);
+          if (op == D_OUTPUT) {
+            const IoDesc& d = a.seed[A];
+            if (d.ptr) {
+              fl[q] = act[B] ? 1u : 9u;
+              if (active) sd[q] = __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir, C, ig));
+              if (!(fl[q] & 8u)) ob[q] = wd[B * 32 + lane];
+            }
+          } else if (op == D_INPUT || op == D_CONST) {
+            if (act[A]) {
+              fl[q] = 1u;
+              if (op == D_INPUT) sd[q] = wd[A * 32 + lane];
+            }
+          } else if (op != D_NOP && act[A]) {
+            unsigned f = 1u;
+            sd[q] = wd[A * 32 + lane];
+            const bool cb = carries_d0(op), cc = carries_d1(op);
+            if (cb) {
+              f |= 2u | (act[B] ? 0u : 8u);
+              if (!(f & 8u)) ob[q] = wd[B * 32 + lane];
+            }
+            if (cc) {
+              // c == b: c's contribution follows b's, which has just activated the slot
+              const bool first_c = (cb && C == B) ? false : !act[C];
+              f |= 4u | (first_c ? 16u : 0u);
+              if (!first_c && !(cb && C == B)) oc[q] = wd[C * 32 + lane];
+            }
+            fl[q] = f;
+            const unsigned m = partial_mask(op);
+            const unsigned use = (f >> 1) & 3u;
+            if (m & use) {
+              const size_t pk = static_cast<size_t>(__ldg(a.t.rpidx + i));
+              if (m & use & 1u) p0[q] = __ldg(pt + pk * 32);
+              if (m & use & 2u) p1[q] = __ldg(pt + (pk + (m & 1u)) * 32);
+            }
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+          const unsigned op = dec_op(ins[q]), A = dec_a(ins[q]), B = dec_b(ins[q]),
+                         C = dec_c(ins[q]);
+          const unsigned f = fl[q];
+          if (!f) continue;
+          if (op == D_OUTPUT) {
+            wd[B * 32 + lane] = (f & 8u) ? sd[q] : __dadd_rn(ob[q], sd[q]);
+            if (lane == 0) act[B] = 1;
+            continue;
+          }
+          if (op == D_INPUT) {
+            const IoDesc& d = a.sens[B];
+            if (active && d.ptr) static_cast<double*>(d.ptr)[io_off(d, dir, C, ig)] = sd[q];
+            if (lane == 0) act[A] = 0;
+            continue;
+          }
+          if (lane == 0) act[A] = 0;
+          if (op == D_CONST) continue;
+          const double s = sd[q];
+          double nb = ob[q];
+          if (f & 2u) {
+            const bool first = f & 8u;
+            switch (op) {
+              case D_ADD: case D_SUB: case D_ASSIGN:
+                nb = first ? s : __dadd_rn(ob[q], s);
+                break;
+              case D_NEG:
+                nb = first ? d_neg(s) : __dsub_rn(ob[q], s);
+                break;
+              case D_TWICE:
+                nb = first ? d_twice(s) : __dadd_rn(ob[q], d_twice(s));
+                break;
+              default:
+                nb = first ? __dmul_rn(p0[q], s) : __dadd_rn(ob[q], __dmul_rn(p0[q], s));
+            }
+            wd[B * 32 + lane] = nb;
+            if (lane == 0) act[B] = 1;
+          }
+          if (f & 4u) {
+            const bool first = f & 16u;
+            const double old = (f & 2u) && C == B ? nb : oc[q];
+            double nc;
+            switch (op) {
+              case D_ADD:
+                nc = first ? s : __dadd_rn(old, s);
+                break;
+              case D_SUB:
+                nc = first ? d_neg(s) : __dsub_rn(old, s);
+                break;
+              case D_IF_ELSE_ZERO:
+                nc = first ? (d_iszero(p1[q]) ? 0.0 : s)
+                           : (d_iszero(p1[q]) ? __dadd_rn(old, 0.0) : __dadd_rn(old, s));
+                break;
+              default:
+                nc = first ? __dmul_rn(p1[q], s) : __dadd_rn(old, __dmul_rn(p1[q], s));
+            }
+            wd[C * 32 + lane] = nc;
+            if (lane == 0) act[C] = 1;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------------------------
 // Plan-free adjoint sweep (the allocation-free entry point).
 //
@@ -1411,6 +1566,16 @@ cudaError_t launch_tangent_coop(const SweepArgs& a, int grid, cudaStream_t s) {
 int occupancy_tangent_coop(size_t smem, bool global) {
   return global ? occ_of_k(k_tangent_coop<kCoopTanQ, true>, kCoopTanThreads, smem)
                 : occ_of_k(k_tangent_coop<kCoopTanQ, false>, kCoopTanThreads, smem);
+}
+
+cudaError_t launch_adjoint_coop(const SweepArgs& a, int grid, cudaStream_t s) {
+  if (a.block != kCoopTanThreads) return cudaErrorInvalidValue;
+  return launch_k(k_adjoint_coop<kCoopTanQ>, grid, a.block,
+                  smem_tangent_coop(a.t.rlv_sz_w, false), a, s);
+}
+
+int occupancy_adjoint_coop(size_t smem) {
+  return occ_of_k(k_adjoint_coop<kCoopTanQ>, kCoopTanThreads, smem);
 }
 
 int occupancy_coop(int threads, size_t smem, bool global) {

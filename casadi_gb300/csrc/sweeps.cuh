@@ -47,6 +47,12 @@ struct TapeView {
   const int* lpidx;         // first recorded partial of each lcode instruction
   int n_levels;
   int lv_sz_w;              // work-vector length of the renamed slots
+  // level schedule of the cooperative reverse sweep (users of each value in order)
+  const u64* rcode;
+  const int* rbegin;
+  const int* rpidx;
+  int n_rlevels;
+  int rlv_sz_w;
 };
 
 struct SweepArgs {
@@ -170,6 +176,12 @@ constexpr int kCoopTanQ = 4;  // instructions per warp and level handled at once
 cudaError_t launch_tangent_coop(const SweepArgs& a, int grid, cudaStream_t s);
 size_t smem_tangent_coop(int lv_sz_w, bool global);
 int occupancy_tangent_coop(size_t smem, bool global);
+// Cooperative adjoint sweep over recorded partials: one CTA of kCoopTanThreads threads per
+// (tile, direction) item walks the reverse level schedule last level first; a.zero_in lists
+// the inputs whose sensitivity is a structural zero. Shared memory: smem_tangent_coop of the
+// reverse schedule's work-vector length.
+cudaError_t launch_adjoint_coop(const SweepArgs& a, int grid, cudaStream_t s);
+int occupancy_adjoint_coop(size_t smem);
 size_t smem_coop(int lv_sz_w);
 int occupancy_coop(int threads, size_t smem, bool global);
 

@@ -661,7 +661,8 @@ class Batch:
 
 N_TAN_VARIANTS = 8  # tangent-sweep kernel variants (forward, Jacobian); the last one is the
 #                     cooperative level sweep, used only by launches of few tiles
-N_ADJ_VARIANTS = 6  # adjoint-sweep kernel variants
+N_ADJ_VARIANTS = 7  # adjoint-sweep kernel variants; the last one is the cooperative level
+#                     sweep, used only by launches of few tiles
 
 FAMILIES = ("eval", "record", "tangent", "adjoint", "sp_forward", "sp_reverse", "batch",
             "activity")

@@ -87,8 +87,9 @@ def test_tape_larger_than_shared_memory(gpu_lib):
 @pytest.mark.parametrize("n", [1, 31, 4096, 100000])
 def test_cooperative_sweeps_on_wide_tapes(gpu_lib, n):
     """The quadcopter multiple-shooting constraints (34156 instructions, wide levels) and the
-    random DAG: values, the unit-seed Jacobian and the adjoint with the cooperative value and
-    record sweeps equal the sequential sweeps bit for bit (and the oracle within tolerance);
+    random DAG: values, the unit-seed Jacobian and the adjoint with the cooperative value,
+    record, tangent and adjoint sweeps equal the sequential sweeps bit for bit (and the oracle
+    within tolerance);
     100000 instances is past the launch size where the autotuner considers the cooperative
     sweep, so there it runs only because it is forced."""
     cases = [(W.random_dag(), W.dag_inputs(n, seed=3))]
@@ -102,6 +103,10 @@ def test_cooperative_sweeps_on_wide_tapes(gpu_lib, n):
         for mode in (2, 1, 3):
             ct = R.CudaTape(F)
             ct.set_residence(mode)
+            if mode == 3:
+                # the cooperative tangent and adjoint sweeps too
+                ct.set_variant(1, R.N_TAN_VARIANTS - 1)
+                ct.set_variant(2, R.N_ADJ_VARIANTS - 1)
             r = [_host(ct.eval(args))]
             r.append(_host(ct.reverse(args, aseeds)[1]))
             if F.tape.n_instr < 20000:

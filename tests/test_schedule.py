@@ -152,3 +152,37 @@ def test_levels_expose_parallel_work():
     lt, _, begin = R.levels(q, width=64, slot_cap=400)
     assert len(begin) - 1 < q.n_instr / 30
     assert lt.sz_w <= 400 + 64
+
+
+@pytest.mark.parametrize("name,make,inputs", LEVEL_CASES, ids=[c[0] for c in LEVEL_CASES])
+def test_reverse_levels_keep_the_users_of_each_value_in_order(name, make, inputs):
+    """The cooperative reverse sweep's schedule (negative width): besides independence, no
+    two users of a non-constant value share a level and the users of each value follow the
+    scheduled tape's order, so adjoints sum their contributions in the sequential order."""
+    t = make().tape
+    lt, src, begin = R.levels(t, width=-64, slot_cap=400)
+    definer = {}  # slot -> (defining op, value id)
+    users = {}    # value id -> source indices of its users in level order
+    for l in range(len(begin) - 1):
+        level_reads = {}
+        for k in range(begin[l], begin[l + 1]):
+            r, _ = _reads_writes(lt.op[k], lt.i0[k], lt.i1[k], lt.i2[k])
+            for slot in r:
+                op, vid = definer[slot]
+                if op != C.OP_CONST:
+                    assert slot not in level_reads, "two users of one value in level %d" % l
+                    level_reads[slot] = k
+                    users.setdefault(vid, []).append(int(src[k]))
+        for k in range(begin[l], begin[l + 1]):
+            _, w = _reads_writes(lt.op[k], lt.i0[k], lt.i1[k], lt.i2[k])
+            if w is not None:
+                definer[w] = (int(lt.op[k]), k)
+    for vid, u in users.items():
+        assert u == sorted(u), "users of value %d out of order" % vid
+    n = 19
+    args = inputs(n)
+    _all_bits_equal(O.eval(lt, args, n), O.eval(t, args, n), "values")
+    rng = np.random.default_rng(3)
+    aseeds = [rng.standard_normal((1, k, n)) for k in t.nnz_out]
+    _all_bits_equal(O.reverse(lt, args, aseeds, n)[1], O.reverse(R.schedule(t), args, aseeds,
+                                                                  n)[1], "adjoint")
