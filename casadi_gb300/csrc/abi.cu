@@ -738,6 +738,7 @@ int primal_launch(Tape& t, SweepArgs& a, long long m, PrimalKind kind, cudaStrea
   static const char* what[] = {"eval launch", "record sweep launch", "sp_forward launch",
                                "sp_reverse launch", "activity launch"};
   enum { M_SHARED = 0, M_GLOBAL = 1, M_COOP = 2 };
+  const bool sp_kind = kind == PK_SP_FORWARD || kind == PK_SP_REVERSE;
   auto go = [&](int grid) {
     switch (kind) {
       case PK_EVAL: return launch_eval(a, grid, s);
@@ -751,7 +752,13 @@ int primal_launch(Tape& t, SweepArgs& a, long long m, PrimalKind kind, cudaStrea
   auto run = [&](int mode, bool profile) -> int {
     int grid;
     bool global = mode == M_GLOBAL;
-    if (mode == M_COOP) {
+    if (mode == M_COOP && sp_kind) {
+      a.block = kCoopThreads;
+      a.t = t.view();
+      a.wglob = nullptr;
+      const size_t sm = smem_coop(kind == PK_SP_REVERSE ? t.rlv_sz_w : t.lv_sz_w);
+      grid = grid_for((m + 31) / 32, std::max(1, occupancy_coop_sp(kCoopThreads, sm)) * sm_count());
+    } else if (mode == M_COOP) {
       a.block = kCoopThreads;
       a.t = t.view();
       const size_t sm = smem_coop(t.lv_sz_w);
@@ -776,7 +783,10 @@ int primal_launch(Tape& t, SweepArgs& a, long long m, PrimalKind kind, cudaStrea
       grid = grid_for((m + a.block - 1) / a.block, t.primal_grid_cap);
     }
     auto launch = [&] {
-      return mode == M_COOP ? launch_coop(a, kind == PK_RECORD, grid, s) : go(grid);
+      if (mode == M_COOP)
+        return sp_kind ? launch_coop_sp(a, kind == PK_SP_REVERSE, grid, s)
+                       : launch_coop(a, kind == PK_RECORD, grid, s);
+      return go(grid);
     };
     cudaError_t e = profile ? timed(fam[kind], s, launch) : launch();
     if (e != cudaSuccess) return cuda_fail(e, what[kind]);
@@ -786,11 +796,16 @@ int primal_launch(Tape& t, SweepArgs& a, long long m, PrimalKind kind, cudaStrea
     }
     return 0;
   };
-  const bool coop_kind = kind == PK_EVAL || kind == PK_RECORD;
+  const bool coop_kind = kind == PK_EVAL || kind == PK_RECORD || sp_kind;
+  const bool rev = kind == PK_SP_REVERSE;
   const int cls = (m + 31) / 32 <= 16ll * sm_count() ? 0 : 1;
-  // the cooperative sweep is a candidate for launches of few tiles (or when forced)
+  // the cooperative sweep is a candidate for launches of few tiles (or when forced); the
+  // sparsity sweeps' version needs its schedule's work vector in shared memory
   const bool want_coop = coop_kind && (cls == 0 || t.residence == 3);
-  const bool can_coop = want_coop && (capturing(s) ? t.lv_state > 0 : ensure_levels(t));
+  bool can_coop = want_coop && (capturing(s) ? (rev ? t.rlv_state : t.lv_state) > 0
+                                             : ensure_levels(t, rev));
+  if (can_coop && sp_kind)
+    can_coop = smem_coop(rev ? t.rlv_sz_w : t.lv_sz_w) <= static_cast<size_t>(max_smem_optin());
   if (t.residence == 3 && coop_kind && can_coop) return run(M_COOP, true);
   if (t.residence == 1 || !fits_smem(t.sz_w)) {
     if (!(coop_kind && can_coop && cls == 0 && t.residence != 1)) return run(M_GLOBAL, true);
@@ -802,6 +817,9 @@ int primal_launch(Tape& t, SweepArgs& a, long long m, PrimalKind kind, cudaStrea
   cand[nc++] = M_GLOBAL;
   if (coop_kind && can_coop && (cls == 0 || t.residence == 3)) cand[nc++] = M_COOP;
   int& choice = t.primal_tuned[kind][cls];
+  // sp_reverse consumes its seeds and cannot be timed twice: it follows sp_forward's choice
+  if (rev && choice < 0 && t.primal_tuned[PK_SP_FORWARD][cls] >= 0)
+    choice = t.primal_tuned[PK_SP_FORWARD][cls];
   // residence is tuned like the derivative variants: every candidate timed once on the first
   // call of each kind and size class (every sweep here but sp_reverse, which consumes its
   // seeds, can run twice with the same results)

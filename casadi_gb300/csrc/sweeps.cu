@@ -278,6 +278,78 @@ __global__ void __launch_bounds__(kCoopMaxThreads) k_coop(const __grid_constant_
   }
 }
 
+// Cooperative bvec_t sparsity sweeps (SXFunction::sp_forward / sp_reverse): the value
+// sweep's level walk with OR instead of arithmetic; the reverse sweep walks the reverse level
+// schedule last level first (no two users of a value in one level, so no two instructions of
+// a level OR into one slot). OR does not depend on order: the same bits as the sequential
+// sweeps.
+template <bool REV>
+__global__ void __launch_bounds__(kCoopMaxThreads) k_coop_sp(const __grid_constant__ SweepArgs a) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  u64* w = reinterpret_cast<u64*>(smem);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const long long ntiles = (a.n + 31) / 32;
+  const int nl = REV ? a.t.n_rlevels : a.t.n_levels;
+  const u64* code = REV ? a.t.rcode : a.t.lcode;
+  const int* lb = REV ? a.t.rbegin : a.t.lbegin;
+  const int lv = REV ? a.t.rlv_sz_w : a.t.lv_sz_w;
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const long long il = tile * 32 + lane;
+    const bool active = il < a.n;
+    const long long ig = a.i_begin + il;
+    if (REV) {
+      for (int k = warp; k < lv; k += nw) w[k * 32 + lane] = 0;
+      __syncthreads();
+    }
+    for (int step = 0; step < nl; ++step) {
+      const int l = REV ? nl - 1 - step : step;
+      const int beg = __ldg(lb + l), end = __ldg(lb + l + 1);
+      for (int i = beg + warp; i < end; i += nw) {
+        const u64 ins = __ldg(code + i);
+        const unsigned op = dec_op(ins), A = dec_a(ins), B = dec_b(ins), C = dec_c(ins);
+        switch (op) {
+          case D_CONST:
+            w[A * 32 + lane] = 0;
+            break;
+          case D_INPUT: {
+            const IoDesc& d = a.in[B];
+            if (REV) {
+              if (active && d.ptr) static_cast<u64*>(d.ptr)[io_off(d, 0, C, ig)] |= w[A * 32 + lane];
+              w[A * 32 + lane] = 0;
+            } else {
+              u64 v = 0;
+              if (active && d.ptr) v = __ldg(static_cast<const u64*>(d.ptr) + io_off(d, 0, C, ig));
+              w[A * 32 + lane] = v;
+            }
+          } break;
+          case D_OUTPUT: {
+            const IoDesc& d = a.out[A];
+            if (REV) {
+              if (active && d.ptr) {
+                u64* p = static_cast<u64*>(d.ptr) + io_off(d, 0, C, ig);
+                w[B * 32 + lane] |= *p;
+                *p = 0;
+              }
+            } else if (active && d.ptr) {
+              static_cast<u64*>(d.ptr)[io_off(d, 0, C, ig)] = w[B * 32 + lane];
+            }
+          } break;
+          default:
+            if (REV) {
+              const u64 seed = w[A * 32 + lane];
+              w[A * 32 + lane] = 0;
+              w[B * 32 + lane] |= seed;
+              w[C * 32 + lane] |= seed;
+            } else {
+              w[A * 32 + lane] = w[B * 32 + lane] | w[C * 32 + lane];
+            }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
 // Cooperative tangent sweep: one CTA per (tile, direction) item runs the level schedule of
 // the forward-mode sweep over the partials the record sweep stored. Activity is structural
 // (the same for every lane), so it is kept per slot in shared memory (act) and an instruction
@@ -1566,6 +1638,17 @@ cudaError_t launch_tangent_coop(const SweepArgs& a, int grid, cudaStream_t s) {
 int occupancy_tangent_coop(size_t smem, bool global) {
   return global ? occ_of_k(k_tangent_coop<kCoopTanQ, true>, kCoopTanThreads, smem)
                 : occ_of_k(k_tangent_coop<kCoopTanQ, false>, kCoopTanThreads, smem);
+}
+
+cudaError_t launch_coop_sp(const SweepArgs& a, bool reverse, int grid, cudaStream_t s) {
+  if (a.block < 32 || a.block > kCoopMaxThreads || a.block % 32) return cudaErrorInvalidValue;
+  const size_t smem = smem_coop(reverse ? a.t.rlv_sz_w : a.t.lv_sz_w);
+  return reverse ? launch_k(k_coop_sp<true>, grid, a.block, smem, a, s)
+                 : launch_k(k_coop_sp<false>, grid, a.block, smem, a, s);
+}
+
+int occupancy_coop_sp(int threads, size_t smem) {
+  return occ_of_k(k_coop_sp<false>, threads, smem);
 }
 
 cudaError_t launch_adjoint_coop(const SweepArgs& a, int grid, cudaStream_t s) {

@@ -168,6 +168,10 @@ cudaError_t launch_activity(const SweepArgs& a, int grid, cudaStream_t s);
 // in shared memory (lv_sz_w x 32 doubles), or in a.wglob blocks when set.
 constexpr int kCoopMaxThreads = 512;
 cudaError_t launch_coop(const SweepArgs& a, bool record, int grid, cudaStream_t s);
+// Cooperative sparsity sweeps (forward: the value sweep's levels; reverse: the reverse
+// schedule's levels, last first); shared memory smem_coop of the schedule's work vector.
+cudaError_t launch_coop_sp(const SweepArgs& a, bool reverse, int grid, cudaStream_t s);
+int occupancy_coop_sp(int threads, size_t smem);
 // Cooperative tangent sweep over recorded partials: one CTA of kCoopTanThreads threads per
 // (tile, direction) item; identity seeds use a.dirmap (flat input nonzero -> direction, null:
 // the nonzero's own index) and a.in_off. Shared memory: smem_tangent_coop.

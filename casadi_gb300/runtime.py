@@ -375,7 +375,7 @@ class CudaTape:
 
     def set_residence(self, mode):
         """Work-vector residence: 0 auto (tuned), 1 global memory, 2 shared memory when it fits,
-        3 the cooperative level sweep for value/record sweeps."""
+        3 the cooperative level sweep for value/record/sparsity sweeps."""
         check(load().casadi_gb300_set_residence(self.id, mode))
 
     def set_variant(self, kind, variant):

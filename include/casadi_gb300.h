@@ -297,10 +297,11 @@ CASADI_GB300_API int casadi_gb300_tuned_variant(int id, int kind, int* variant);
  * work vector fits, global memory (L1/L2-cached per-CTA blocks owned by the tape) when it does
  * not, and for the value/record/sparsity sweeps the fastest candidate, timed by the autotuner
  * on the first call of each sweep kind and launch size (at most 16 tiles of 32 instances per
- * SM, or more): shared, global, and for value/record sweeps of the smaller launches the
- * cooperative level sweep (several warps share a tile and run the tape's independent
- * instructions level by level; casadi_gb300_tape_levels shows the schedule); 1 always global
- * memory; 2 shared memory whenever it fits; 3 the cooperative sweep for value/record sweeps.
+ * SM, or more): shared, global, and for value/record/sparsity sweeps of the smaller launches
+ * the cooperative level sweep (several warps share a tile and run the tape's independent
+ * instructions level by level; casadi_gb300_tape_levels shows the schedule; sp_reverse, which
+ * consumes its seeds, follows sp_forward's choice); 1 always global memory; 2 shared memory
+ * whenever it fits; 3 the cooperative sweep for value/record/sparsity sweeps.
  * Results are identical in every mode. A tape whose global work vectors must grow cannot be
  * first used inside a CUDA graph capture. No counterpart in the reference, whose work vector
  * is the caller's w array (casadi/core/function_internal.hpp:414). */
