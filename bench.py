@@ -9,7 +9,7 @@ resident in HBM; `e2e` is the same step through the C ABI's host-buffer Map entr
 copies inside the timed region.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl native|reference]
-                       [--workload rollout20|cartpole|dag]
+                       [--workload rollout20|cartpole|dag|mixed|mpc]
 For N > 1 (torchrun) every rank runs an independent replica on its own instances (the path
 has no exchange step); rank 0 prints the max-over-ranks time.
 """
@@ -508,6 +508,24 @@ def run_mixed(a):
                       "components": {"mixed_batch": comp}}), flush=True)
 
 
+def run_mpc(a):
+    """The scenario-MPC component alone (profiling captures of its kernels): the coloured
+    constraint Jacobian and Lagrangian Hessian over the scenarios, separate calls and the
+    persistent batch graph."""
+    import torch
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    comp = mpc_sparse_component(torch, torch.cuda.current_stream(), n=a.instances or 4096,
+                                reps=max(1, a.steps))
+    print(json.dumps({"metric": METRIC, "value": comp["persistent_scenarios_per_s"],
+                      "unit": "scenarios/s", "n_gpus": 1, "steps": a.steps, "warmup": 1,
+                      "ms_per_step": comp["persistent_graph_ms"], "higher_is_better": True,
+                      "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                      "data": "synthetic",
+                      "config": {"workload": "scenario MPC: quadcopter multiple shooting, "
+                                             "100 intervals, coloured Jacobian + Hessian"},
+                      "components": {"mpc_sparse_hessian": comp}}), flush=True)
+
+
 def run_native(a):
     import torch
     from casadi_gb300 import runtime as R
@@ -758,7 +776,7 @@ def main():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="native", choices=["native", "reference"])
     p.add_argument("--workload", default="rollout20",
-                   choices=["rollout20", "cartpole", "dag", "mixed"])
+                   choices=["rollout20", "cartpole", "dag", "mixed", "mpc"])
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     p.add_argument("--instances", type=int, default=None,
                    help="override the workload's instance count (profiling captures)")
@@ -769,6 +787,8 @@ def main():
         run_reference(a)
     elif a.workload == "mixed":
         run_mixed(a)
+    elif a.workload == "mpc":
+        run_mpc(a)
     else:
         run_native(a)
 
