@@ -363,7 +363,7 @@ __device__ __forceinline__ bool is_arith(unsigned op) {
 }
 
 template <int Q, bool GW>
-__global__ void __launch_bounds__(kCoopMaxThreads)
+__global__ void __launch_bounds__(kCoopTanThreads)
     k_tangent_coop(const __grid_constant__ SweepArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int lv = a.t.lv_sz_w;
@@ -494,7 +494,7 @@ __global__ void __launch_bounds__(kCoopMaxThreads)
 // sequential sweep's plan, whether a contribution is the first (assigned) or added; the
 // arithmetic of every case is the sequential sweep's, so the sensitivities are the same bits.
 template <int Q>
-__global__ void __launch_bounds__(kCoopMaxThreads)
+__global__ void __launch_bounds__(kCoopTanThreads)
     k_adjoint_coop(const __grid_constant__ SweepArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int lv = a.t.rlv_sz_w;

@@ -166,7 +166,7 @@ cudaError_t launch_activity(const SweepArgs& a, int grid, cudaStream_t s);
 // Cooperative value (record = false) or record sweep: a.block threads (a multiple of 32, at
 // most kCoopMaxThreads) share one 32-instance tile and run its level schedule; the work vector
 // in shared memory (lv_sz_w x 32 doubles), or in a.wglob blocks when set.
-constexpr int kCoopMaxThreads = 512;
+constexpr int kCoopMaxThreads = 1024;
 cudaError_t launch_coop(const SweepArgs& a, bool record, int grid, cudaStream_t s);
 // Cooperative sparsity sweeps (forward: the value sweep's levels; reverse: the reverse
 // schedule's levels, last first); shared memory smem_coop of the schedule's work vector.
