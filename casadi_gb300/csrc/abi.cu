@@ -682,7 +682,12 @@ enum PrimalKind { PK_EVAL = 0, PK_RECORD, PK_SP_FORWARD, PK_SP_REVERSE, PK_ACTIV
 // Level schedule of the cooperative sweeps (host scheduling + upload, once per tape). Returns
 // whether it is available; never called while the stream is being captured.
 constexpr int kLevelWidth = 64;      // instructions per level
-constexpr int kCoopThreads = 256;    // warps of a cooperative CTA x 32
+// CTA size of the cooperative value/record/sparsity sweeps: 256, 512 or 1024 threads (tuned);
+// without tuning, enough warps per tile that the tiles of the launch fill the GPU
+int coop_threads_for(long long tiles) {
+  const long long want = static_cast<long long>(sm_count()) * 32 / std::max(1ll, tiles);
+  return want >= 32 ? 1024 : (want >= 16 ? 512 : 256);
+}
 bool ensure_levels(Tape& t, bool reverse = false) {
   std::lock_guard<std::mutex> lk(t.shape_mtx);
   int& state = reverse ? t.rlv_state : t.lv_state;
@@ -737,7 +742,9 @@ int primal_launch(Tape& t, SweepArgs& a, long long m, PrimalKind kind, cudaStrea
   static const int fam[] = {F_EVAL, F_RECORD, F_SP_FORWARD, F_SP_REVERSE, F_ACTIVITY};
   static const char* what[] = {"eval launch", "record sweep launch", "sp_forward launch",
                                "sp_reverse launch", "activity launch"};
-  enum { M_SHARED = 0, M_GLOBAL = 1, M_COOP = 2 };
+  // modes: shared, global, cooperative with 256, 512 or 1024 threads per CTA
+  enum { M_SHARED = 0, M_GLOBAL = 1, M_COOP = 2, M_COOP_LAST = 4 };
+  auto coop_threads = [](int mode) { return 256 << (mode - M_COOP); };
   const bool sp_kind = kind == PK_SP_FORWARD || kind == PK_SP_REVERSE;
   auto go = [&](int grid) {
     switch (kind) {
@@ -752,18 +759,18 @@ int primal_launch(Tape& t, SweepArgs& a, long long m, PrimalKind kind, cudaStrea
   auto run = [&](int mode, bool profile) -> int {
     int grid;
     bool global = mode == M_GLOBAL;
-    if (mode == M_COOP && sp_kind) {
-      a.block = kCoopThreads;
+    if (mode >= M_COOP && sp_kind) {
+      a.block = coop_threads(mode);
       a.t = t.view();
       a.wglob = nullptr;
       const size_t sm = smem_coop(kind == PK_SP_REVERSE ? t.rlv_sz_w : t.lv_sz_w);
-      grid = grid_for((m + 31) / 32, std::max(1, occupancy_coop_sp(kCoopThreads, sm)) * sm_count());
-    } else if (mode == M_COOP) {
-      a.block = kCoopThreads;
+      grid = grid_for((m + 31) / 32, std::max(1, occupancy_coop_sp(a.block, sm)) * sm_count());
+    } else if (mode >= M_COOP) {
+      a.block = coop_threads(mode);
       a.t = t.view();
       const size_t sm = smem_coop(t.lv_sz_w);
       global = sm > static_cast<size_t>(max_smem_optin());
-      const int occ = std::max(1, occupancy_coop(kCoopThreads, sm, global));
+      const int occ = std::max(1, occupancy_coop(a.block, sm, global));
       grid = grid_for((m + 31) / 32, occ * sm_count());
       a.wglob = nullptr;
       if (global)
@@ -783,7 +790,7 @@ int primal_launch(Tape& t, SweepArgs& a, long long m, PrimalKind kind, cudaStrea
       grid = grid_for((m + a.block - 1) / a.block, t.primal_grid_cap);
     }
     auto launch = [&] {
-      if (mode == M_COOP)
+      if (mode >= M_COOP)
         return sp_kind ? launch_coop_sp(a, kind == PK_SP_REVERSE, grid, s)
                        : launch_coop(a, kind == PK_RECORD, grid, s);
       return go(grid);
@@ -806,16 +813,19 @@ int primal_launch(Tape& t, SweepArgs& a, long long m, PrimalKind kind, cudaStrea
                                              : ensure_levels(t, rev));
   if (can_coop && sp_kind)
     can_coop = smem_coop(rev ? t.rlv_sz_w : t.lv_sz_w) <= static_cast<size_t>(max_smem_optin());
-  if (t.residence == 3 && coop_kind && can_coop) return run(M_COOP, true);
+  const int coop_default = M_COOP + (coop_threads_for((m + 31) / 32) == 1024
+                                         ? 2 : coop_threads_for((m + 31) / 32) == 512 ? 1 : 0);
+  if (t.residence == 3 && coop_kind && can_coop) return run(coop_default, true);
   if (t.residence == 1 || !fits_smem(t.sz_w)) {
     if (!(coop_kind && can_coop && cls == 0 && t.residence != 1)) return run(M_GLOBAL, true);
   } else if (t.residence == 2) {
     return run(M_SHARED, true);
   }
-  int cand[3], nc = 0;
+  int cand[5], nc = 0;
   if (fits_smem(t.sz_w)) cand[nc++] = M_SHARED;
   cand[nc++] = M_GLOBAL;
-  if (coop_kind && can_coop && (cls == 0 || t.residence == 3)) cand[nc++] = M_COOP;
+  if (coop_kind && can_coop && (cls == 0 || t.residence == 3))
+    for (int c = M_COOP; c <= M_COOP_LAST; ++c) cand[nc++] = c;
   int& choice = t.primal_tuned[kind][cls];
   // sp_reverse consumes its seeds and cannot be timed twice: it follows sp_forward's choice
   if (rev && choice < 0 && t.primal_tuned[PK_SP_FORWARD][cls] >= 0)
@@ -824,7 +834,7 @@ int primal_launch(Tape& t, SweepArgs& a, long long m, PrimalKind kind, cudaStrea
   // call of each kind and size class (every sweep here but sp_reverse, which consumes its
   // seeds, can run twice with the same results)
   if (choice < 0 && nc > 1 && g_autotune && kind != PK_SP_REVERSE && !capturing(s)) {
-    float ms[3] = {0, 0, 0};
+    float ms[5] = {0, 0, 0, 0, 0};
     for (int c = 0; c < nc; ++c) {
       int rc = 0;
       if (int trc = time_once(s, [&] { rc = run(cand[c], false); return cudaSuccess; }, &ms[c]))
@@ -837,7 +847,7 @@ int primal_launch(Tape& t, SweepArgs& a, long long m, PrimalKind kind, cudaStrea
     choice = cand[best];
     return 0;  // every run produced the same (complete) results
   }
-  if (choice >= 0 && (choice != M_COOP || can_coop) && (choice != M_SHARED || fits_smem(t.sz_w)))
+  if (choice >= 0 && (choice < M_COOP || can_coop) && (choice != M_SHARED || fits_smem(t.sz_w)))
     return run(choice, true);
   return run(cand[0], true);
 }
@@ -2283,9 +2293,9 @@ int batch_enqueue(BatchHost& b, void* scratch, cudaStream_t s, bool gw) {
     for (int j = 0; j < t->n_in; ++j) a.in[j] = it.io[j];
     for (int j = 0; j < t->n_out; ++j) a.out[j] = it.io[kMaxIo + j];
     a.partials = pr.partials;
-    a.block = kCoopThreads;
+    a.block = coop_threads_for(pr.tiles);
     const size_t sm = smem_coop(t->lv_sz_w);
-    const int occ = std::max(1, occupancy_coop(kCoopThreads, sm, false));
+    const int occ = std::max(1, occupancy_coop(a.block, sm, false));
     const int grid = static_cast<int>(std::min<long long>(pr.tiles, 1ll * occ * sm_count()));
     if ((e = launch_coop(a, true, grid, s)) != cudaSuccess) return cuda_fail(e, "batch record");
     // every tile of the item is recorded: its direction units need not wait
