@@ -2876,3 +2876,241 @@ int casadi_gb300_mapsum_sp_reverse(int id, int64_t n, int64_t ld,
 }
 
 }  // extern "C"
+
+// ---- Mapaccum: N chained calls of one tape (Function::mapaccum, casadi/core/function.cpp) ----
+namespace {
+
+int accum_check(const Tape& t, int N, int n_accum) {
+  if (N < 1) return fail(CASADI_GB300_ERR_ARG, "mapaccum: N must be positive");
+  if (n_accum < 0 || n_accum > std::min(t.n_in, t.n_out))
+    return fail(CASADI_GB300_ERR_ARG, "mapaccum: %d accumulators for %d inputs and %d outputs",
+                n_accum, t.n_in, t.n_out);
+  for (int i = 0; i < n_accum; ++i)
+    if (t.nnz_in[i] != t.nnz_out[i])
+      return fail(CASADI_GB300_ERR_ARG,
+                  "mapaccum: accumulator %d has %d input but %d output nonzeros", i,
+                  t.nnz_in[i], t.nnz_out[i]);
+  return 0;
+}
+
+// Block k of a stacked input/output: nonzeros [k*nnz, (k+1)*nnz) of an (nnz*N, ld) array, and
+// of each direction of an (ndir, nnz*N, ld) one.
+IoDesc step_io(const void* base, int nnz, int N, int k, long long ld) {
+  if (!base) return IoDesc{nullptr, ld, 1, 0};
+  return IoDesc{const_cast<char*>(static_cast<const char*>(base)) +
+                    static_cast<size_t>(k) * nnz * ld * sizeof(double),
+                ld, 1, static_cast<long long>(nnz) * N * ld};
+}
+// A contiguous (ndir, nnz, n) block of the scratch.
+IoDesc block_io(void* p, int nnz, long long n) {
+  return IoDesc{p, n, 1, static_cast<long long>(nnz) * n};
+}
+
+size_t bytes_of(long long count) { return ((static_cast<size_t>(count) * 8 + 255) / 256) * 256; }
+
+// Accumulator values of step k-1 (the input of step k > 0): the caller's output block, or the
+// scratch copy (history: every step kept, for the reverse sweep; else two alternating blocks).
+struct AccumValues {
+  const double* const* res;
+  double* keep[kMaxIo] = {};
+  bool history = false;
+  IoDesc value(int i, int nnz, int N, int k, long long n, long long ld) const {
+    if (res && res[i]) return step_io(res[i], nnz, N, k, ld);
+    double* p = keep[i] + static_cast<size_t>(history ? k : (k & 1)) * nnz * n;
+    return IoDesc{p, n, 1, 0};
+  }
+};
+
+int accum_values(const Tape& t, int N, int n_accum, long long n, const double* const* res,
+                 bool history, Arena& ar, AccumValues* v) {
+  v->res = res;
+  v->history = history;
+  for (int i = 0; i < n_accum; ++i) {
+    if (res && res[i]) continue;
+    v->keep[i] = static_cast<double*>(
+        ar.take(bytes_of(static_cast<long long>(t.nnz_out[i]) * n * (history ? N : 2))));
+    if (!v->keep[i])
+      return fail(CASADI_GB300_ERR_SCRATCH,
+                  "mapaccum scratch too small (see casadi_gb300_mapaccum_scratch_size)");
+  }
+  return 0;
+}
+
+// The value sweep of every step: inputs of step k from arg / the previous step's outputs.
+int accum_forward_values(Tape& t, int N, int n_accum, long long n, long long ld,
+                         const double* const* arg, double* const* res, const AccumValues& v,
+                         cudaStream_t s) {
+  for (int k = 0; k < N; ++k) {
+    SweepArgs a = base_args(t, n, 0);
+    for (int j = 0; j < t.n_in; ++j) {
+      const int nz = t.nnz_in[j];
+      if (j < n_accum)
+        a.in[j] = k == 0 ? plain_io(at(arg, j), nz, ld, false) : v.value(j, nz, N, k - 1, n, ld);
+      else
+        a.in[j] = step_io(at(arg, j), nz, N, k, ld);
+    }
+    for (int j = 0; j < t.n_out; ++j)
+      a.out[j] = j < n_accum ? v.value(j, t.nnz_out[j], N, k, n, ld)
+                             : step_io(res ? res[j] : nullptr, t.nnz_out[j], N, k, ld);
+    if (int rc = primal_launch(t, a, n, PK_EVAL, s)) return rc;
+  }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int casadi_gb300_mapaccum_scratch_size(int id, int N, int n_accum, int64_t n, int ndir,
+                                       size_t* bytes) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  if (!bytes || n < 0 || ndir < 0) return fail(CASADI_GB300_ERR_ARG, "bad arguments");
+  if (int rc = accum_check(*t, N, n_accum)) return rc;
+  size_t b = 512;
+  for (int i = 0; i < n_accum; ++i) {
+    const long long nz = t->nnz_out[i];
+    b += bytes_of(nz * n * std::max(N, 2));                // accumulator values
+    b += 3 * bytes_of(static_cast<long long>(std::max(ndir, 1)) * nz * n);  // tangents/adjoints
+  }
+  b += static_cast<size_t>(8) * t->n_partials * static_cast<size_t>(((n + 31) / 32) * 32);
+  *bytes = b;
+  return 0;
+}
+
+int casadi_gb300_mapaccum_eval(int id, int N, int n_accum, int64_t n, int64_t ld,
+                               const double* const* arg, double* const* res, void* scratch,
+                               size_t scratch_bytes, void* stream) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  if (int rc = check_device(*t)) return rc;
+  if (int rc = check_n(n, ld)) return rc;
+  if (int rc = accum_check(*t, N, n_accum)) return rc;
+  if (n == 0) return 0;
+  Arena ar(scratch, scratch_bytes);
+  AccumValues v;
+  if (int rc = accum_values(*t, N, n_accum, n, res, false, ar, &v)) return rc;
+  return accum_forward_values(*t, N, n_accum, n, ld, arg, res, v,
+                              static_cast<cudaStream_t>(stream));
+}
+
+int casadi_gb300_mapaccum_forward(int id, int N, int n_accum, int64_t n, int64_t ld, int nfwd,
+                                  const double* const* arg, double* const* res,
+                                  const double* const* fseed, double* const* fsens,
+                                  void* scratch, size_t scratch_bytes, void* stream) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  if (int rc = check_device(*t)) return rc;
+  if (int rc = check_n(n, ld)) return rc;
+  if (int rc = accum_check(*t, N, n_accum)) return rc;
+  if (nfwd < 1 || nfwd > 65535) return fail(CASADI_GB300_ERR_ARG, "bad direction count %d", nfwd);
+  if (n == 0) return 0;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  Arena ar(scratch, scratch_bytes);
+  AccumValues v;
+  if (int rc = accum_values(*t, N, n_accum, n, res, false, ar, &v)) return rc;
+  // accumulator tangents the caller does not keep: two alternating blocks
+  double* ttmp[kMaxIo] = {};
+  for (int i = 0; i < n_accum; ++i) {
+    if (fsens && fsens[i]) continue;
+    ttmp[i] = static_cast<double*>(ar.take(bytes_of(2ll * nfwd * t->nnz_out[i] * n)));
+    if (!ttmp[i])
+      return fail(CASADI_GB300_ERR_SCRATCH,
+                  "mapaccum scratch too small (see casadi_gb300_mapaccum_scratch_size)");
+  }
+  auto tangent = [&](int i, int k) -> IoDesc {
+    const int nz = t->nnz_out[i];
+    if (fsens && fsens[i]) return step_io(fsens[i], nz, N, k, ld);
+    return block_io(ttmp[i] + static_cast<size_t>(k & 1) * nfwd * nz * n, nz, n);
+  };
+  for (int k = 0; k < N; ++k) {
+    IoDesc in[kMaxIo], out[kMaxIo], seed[kMaxIo], sens[kMaxIo];
+    for (int j = 0; j < t->n_in; ++j) {
+      const int nz = t->nnz_in[j];
+      if (j < n_accum) {
+        in[j] = k == 0 ? plain_io(at(arg, j), nz, ld, false) : v.value(j, nz, N, k - 1, n, ld);
+        seed[j] = k == 0 ? plain_io(at(fseed, j), nz, ld, true) : tangent(j, k - 1);
+      } else {
+        in[j] = step_io(at(arg, j), nz, N, k, ld);
+        seed[j] = step_io(at(fseed, j), nz, N, k, ld);
+      }
+    }
+    for (int j = 0; j < t->n_out; ++j) {
+      const int nz = t->nnz_out[j];
+      out[j] = j < n_accum ? v.value(j, nz, N, k, n, ld)
+                           : step_io(res ? res[j] : nullptr, nz, N, k, ld);
+      sens[j] = j < n_accum ? tangent(j, k) : step_io(fsens ? fsens[j] : nullptr, nz, N, k, ld);
+    }
+    if (int rc = run_ad(*t, n, in, out, seed, sens, nfwd, false, false, ar.p, ar.left, s))
+      return rc;
+  }
+  return 0;
+}
+
+int casadi_gb300_mapaccum_reverse(int id, int N, int n_accum, int64_t n, int64_t ld, int nadj,
+                                  const double* const* arg, double* const* res,
+                                  const double* const* aseed, double* const* asens,
+                                  void* scratch, size_t scratch_bytes, void* stream) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  if (int rc = check_device(*t)) return rc;
+  if (int rc = check_n(n, ld)) return rc;
+  if (int rc = accum_check(*t, N, n_accum)) return rc;
+  if (nadj < 1 || nadj > 65535) return fail(CASADI_GB300_ERR_ARG, "bad direction count %d", nadj);
+  if (n == 0) return 0;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  Arena ar(scratch, scratch_bytes);
+  // every step's accumulator values are kept (the caller's outputs or a scratch history): the
+  // reverse sweep of step k records it again from its inputs
+  AccumValues v;
+  if (int rc = accum_values(*t, N, n_accum, n, res, true, ar, &v)) return rc;
+  if (int rc = accum_forward_values(*t, N, n_accum, n, ld, arg, res, v, s)) return rc;
+  // adjoints of the accumulator inputs, carried from step k+1 to step k, and the combined
+  // seeds of the accumulator outputs
+  double* carry[kMaxIo] = {};
+  double* cseed[kMaxIo] = {};
+  for (int i = 0; i < n_accum; ++i) {
+    const long long blk = static_cast<long long>(nadj) * t->nnz_out[i] * n;
+    carry[i] = static_cast<double*>(ar.take(bytes_of(2 * blk)));
+    cseed[i] = static_cast<double*>(ar.take(bytes_of(blk)));
+    if (!carry[i] || !cseed[i])
+      return fail(CASADI_GB300_ERR_SCRATCH,
+                  "mapaccum scratch too small (see casadi_gb300_mapaccum_scratch_size)");
+  }
+  for (int k = N - 1; k >= 0; --k) {
+    IoDesc in[kMaxIo], out[kMaxIo], seed[kMaxIo], sens[kMaxIo];
+    for (int j = 0; j < t->n_out; ++j) {
+      const int nz = t->nnz_out[j];
+      out[j] = IoDesc{nullptr, ld, 1, 0};  // the values were written by the value sweeps
+      if (j < n_accum) {
+        // seed of x_{k+1}: its own adjoint seed plus what step k+1 passed back
+        const double* a_blk = aseed && aseed[j] ? aseed[j] + static_cast<size_t>(k) * nz * ld
+                                                : nullptr;
+        const double* prev = k < N - 1 ? carry[j] + static_cast<size_t>((k + 1) & 1) * nadj * nz * n
+                                       : nullptr;
+        cudaError_t e = add_blocks(nadj, nz, n, a_blk, ld, static_cast<long long>(nz) * N * ld,
+                                   prev, cseed[j], s);
+        if (e != cudaSuccess) return cuda_fail(e, "mapaccum seeds");
+        seed[j] = block_io(cseed[j], nz, n);
+      } else {
+        seed[j] = step_io(at(aseed, j), nz, N, k, ld);
+      }
+    }
+    for (int j = 0; j < t->n_in; ++j) {
+      const int nz = t->nnz_in[j];
+      if (j < n_accum) {
+        in[j] = k == 0 ? plain_io(at(arg, j), nz, ld, false) : v.value(j, nz, N, k - 1, n, ld);
+        sens[j] = k == 0 ? plain_io(asens ? asens[j] : nullptr, nz, ld, true)
+                         : block_io(carry[j] + static_cast<size_t>(k & 1) * nadj * nz * n, nz, n);
+      } else {
+        in[j] = step_io(at(arg, j), nz, N, k, ld);
+        sens[j] = step_io(asens ? asens[j] : nullptr, nz, N, k, ld);
+      }
+    }
+    if (int rc = run_ad(*t, n, in, out, seed, sens, nadj, true, false, ar.p, ar.left, s))
+      return rc;
+  }
+  return 0;
+}
+
+}  // extern "C"

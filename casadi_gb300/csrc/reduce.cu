@@ -77,6 +77,23 @@ __global__ void k_broadcast_rows(long long rows, long long n,
   }
 }
 
+__global__ void k_add_blocks(long long ndir, long long nnz, long long n,
+                             const double* __restrict__ a, long long a_nz, long long a_dir,
+                             const double* __restrict__ b, double* __restrict__ dst) {
+  const long long total = ndir * nnz * n;
+  for (long long q = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; q < total;
+       q += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const long long i = q % n, r = q / n, k = r % nnz, d = r / nnz;
+    const double* pa = a ? a + d * a_dir + k * a_nz + i : nullptr;
+    double v;
+    if (pa && b) v = __dadd_rn(__ldg(pa), __ldg(b + q));
+    else if (pa) v = __ldg(pa);
+    else if (b) v = __ldg(b + q);
+    else v = 0.0;
+    dst[q] = v;
+  }
+}
+
 unsigned blocks_for(long long items) {
   const long long b = (items + kWarpsPerCta - 1) / kWarpsPerCta;
   return static_cast<unsigned>(std::max<long long>(1, b));
@@ -137,6 +154,15 @@ cudaError_t broadcast_rows(long long rows, long long n, const unsigned long long
   const long long total = rows * n;
   const unsigned grid = static_cast<unsigned>(std::min<long long>((total + 255) / 256, 4096));
   k_broadcast_rows<<<grid, 256, 0, s>>>(rows, n, src, dst, ld);
+  return cudaGetLastError();
+}
+
+cudaError_t add_blocks(long long ndir, long long nnz, long long n, const double* a, long long a_nz,
+                       long long a_dir, const double* b, double* dst, cudaStream_t s) {
+  const long long total = ndir * nnz * n;
+  if (total <= 0) return cudaSuccess;
+  const unsigned grid = static_cast<unsigned>(std::min<long long>((total + 255) / 256, 8192));
+  k_add_blocks<<<grid, 256, 0, s>>>(ndir, nnz, n, a, a_nz, a_dir, b, dst);
   return cudaGetLastError();
 }
 

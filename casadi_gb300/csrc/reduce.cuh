@@ -36,4 +36,9 @@ cudaError_t reduce_or(long long rows, long long n, const unsigned long long* src
 cudaError_t broadcast_rows(long long rows, long long n, const unsigned long long* src,
                            unsigned long long* dst, long long ld, cudaStream_t s);
 
+// dst[(d*nnz + k)*n + i] = a[d*a_dir + k*a_nz + i] + b[(d*nnz + k)*n + i] over ndir x nnz x n;
+// a null operand contributes nothing (the other is copied), both null give zeros.
+cudaError_t add_blocks(long long ndir, long long nnz, long long n, const double* a, long long a_nz,
+                       long long a_dir, const double* b, double* dst, cudaStream_t s);
+
 }  // namespace cgb

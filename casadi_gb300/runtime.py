@@ -74,6 +74,12 @@ def load(path=None):
         "casadi_gb300_sp_reverse": (cint, [cint, i64, i64, vp, vp, vp]),
         "casadi_gb300_eval_activity": (cint, [cint, i64, i64, vp, vp, vp]),
         "casadi_gb300_mapsum_scratch_size": (cint, [cint, i64, cint, vp, vp]),
+        "casadi_gb300_mapaccum_scratch_size": (cint, [cint, cint, cint, i64, cint, vp]),
+        "casadi_gb300_mapaccum_eval": (cint, [cint, cint, cint, i64, i64, vp, vp, vp, sz, vp]),
+        "casadi_gb300_mapaccum_forward": (cint, [cint, cint, cint, i64, i64, cint, vp, vp, vp,
+                                                 vp, vp, sz, vp]),
+        "casadi_gb300_mapaccum_reverse": (cint, [cint, cint, cint, i64, i64, cint, vp, vp, vp,
+                                                 vp, vp, sz, vp]),
         "casadi_gb300_mapsum_eval": (cint, [cint, i64, i64, vp, vp, vp, vp, sz, vp]),
         "casadi_gb300_mapsum_forward": (cint, [cint, i64, i64, vp, cint, vp, vp, vp, vp, vp, sz,
                                                vp]),
@@ -492,6 +498,81 @@ class CudaMapSum:
         self._call("casadi_gb300_mapsum_sp_reverse", _ptr_array(args), _ptr_array(res),
                    ct.c_void_p(sc.data_ptr()), sc.numel(), _stream_handle(stream))
         return args, res
+
+
+class CudaMapaccum:
+    """``f.mapaccum(N, n_accum)`` (casadi/core/function.cpp:668-747) over n instances on
+    device tensors: N chained calls of one tape, the first ``n_accum`` outputs of each call
+    feeding the first ``n_accum`` inputs of the next. Accumulator inputs are (nnz, n); other
+    inputs and every output stack the N calls: (nnz*N, n), call k's block at rows
+    [k*nnz, (k+1)*nnz). Seeds and sensitivities add a leading direction axis."""
+
+    class_name = "Mapaccum"
+
+    def __init__(self, f, N, n_accum=1):
+        self.tape = f if isinstance(f, CudaTape) else CudaTape(f)
+        self.N, self.n_accum = int(N), int(n_accum)
+        self._scratch = None
+        self.name = "mapaccum_%s" % getattr(f, "name", "f")
+
+    def _in_rows(self, j):
+        k = self.tape.nnz_in[j]
+        return k if j < self.n_accum else k * self.N
+
+    def scratch(self, n, ndir=0):
+        import torch
+        b = ct.c_size_t()
+        check(load().casadi_gb300_mapaccum_scratch_size(self.tape.id, self.N, self.n_accum, n,
+                                                        ndir, ct.byref(b)))
+        if self._scratch is None or self._scratch.numel() < b.value:
+            self._scratch = torch.empty(max(b.value, 8), dtype=torch.uint8, device="cuda")
+        return self._scratch
+
+    def _outs(self, n, ndir=None, keep=None):
+        import torch
+        out = []
+        for j, k in enumerate(self.tape.nnz_out):
+            if keep is not None and not keep[j]:
+                out.append(None)
+                continue
+            shape = (k * self.N, n) if ndir is None else (ndir, k * self.N, n)
+            out.append(torch.empty(shape, dtype=torch.float64, device="cuda"))
+        return out
+
+    def eval(self, args, n=None, keep=None, stream=None):
+        """``keep``: per output, whether to return it (accumulators not kept live in scratch)."""
+        n = CudaTape._n(args) if n is None else n
+        res = self._outs(n, keep=keep)
+        sc = self.scratch(n)
+        check(load().casadi_gb300_mapaccum_eval(
+            self.tape.id, self.N, self.n_accum, n, n, _ptr_array(args), _ptr_array(res),
+            ct.c_void_p(sc.data_ptr()), sc.numel(), _stream_handle(stream)))
+        return res
+
+    def forward(self, args, fseeds, n=None, stream=None):
+        n = CudaTape._n(args) if n is None else n
+        nfwd = next(s.shape[0] for s in fseeds if s is not None)
+        res, fsens = self._outs(n), self._outs(n, nfwd)
+        sc = self.scratch(n, nfwd)
+        check(load().casadi_gb300_mapaccum_forward(
+            self.tape.id, self.N, self.n_accum, n, n, nfwd, _ptr_array(args), _ptr_array(res),
+            _ptr_array(fseeds), _ptr_array(fsens), ct.c_void_p(sc.data_ptr()), sc.numel(),
+            _stream_handle(stream)))
+        return res, fsens
+
+    def reverse(self, args, aseeds, n=None, keep=None, stream=None):
+        import torch
+        n = CudaTape._n(args) if n is None else n
+        nadj = next(s.shape[0] for s in aseeds if s is not None)
+        res = self._outs(n, keep=keep)
+        asens = [torch.empty((nadj, self._in_rows(j), n), dtype=torch.float64, device="cuda")
+                 for j in range(len(self.tape.nnz_in))]
+        sc = self.scratch(n, nadj)
+        check(load().casadi_gb300_mapaccum_reverse(
+            self.tape.id, self.N, self.n_accum, n, n, nadj, _ptr_array(args), _ptr_array(res),
+            _ptr_array(aseeds), _ptr_array(asens), ct.c_void_p(sc.data_ptr()), sc.numel(),
+            _stream_handle(stream)))
+        return res, asens
 
 
 class MapMemory:

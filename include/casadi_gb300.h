@@ -250,6 +250,37 @@ CASADI_GB300_API int casadi_gb300_mapsum_sp_reverse(int id, int64_t n, int64_t l
                             uint64_t* const* res, void* scratch, size_t scratch_bytes,
                             void* stream);
 
+/* Mapaccum over n instances (Function::mapaccum(name, N, n_accum), casadi/core/
+ * function.cpp:668-747): the tape is called N times; the first n_accum outputs of call k are
+ * the first n_accum inputs of call k+1 (call 0 reads them from arg, nnz_in[i] per instance);
+ * every other input j of call k is nonzeros [k*nnz_in[j], (k+1)*nnz_in[j]) of arg[j], and
+ * output j of call k is nonzeros [k*nnz_out[j], (k+1)*nnz_out[j]) of res[j] (the horzcat of
+ * the N calls). Instance-minor layout with leading dimension ld. An accumulator input and its
+ * output have the same nonzeros. Accumulator outputs that res does not keep (null) live in
+ * the scratch (casadi_gb300_mapaccum_scratch_size: enough for every call below with up to
+ * ndir directions). Nothing is unrolled: one tape, N launches, outputs fed back in place. */
+CASADI_GB300_API int casadi_gb300_mapaccum_scratch_size(int id, int N, int n_accum, int64_t n,
+                            int ndir, size_t* bytes);
+CASADI_GB300_API int casadi_gb300_mapaccum_eval(int id, int N, int n_accum, int64_t n,
+                            int64_t ld, const double* const* arg, double* const* res,
+                            void* scratch, size_t scratch_bytes, void* stream);
+/* Forward mode: seeds as arg with a leading direction axis ((nfwd, nnz, ld) for accumulators,
+ * (nfwd, nnz*N, ld) otherwise), sensitivities as res; the tangents of call k's accumulator
+ * outputs seed call k+1. */
+CASADI_GB300_API int casadi_gb300_mapaccum_forward(int id, int N, int n_accum, int64_t n,
+                            int64_t ld, int nfwd, const double* const* arg, double* const* res,
+                            const double* const* fseed, double* const* fsens, void* scratch,
+                            size_t scratch_bytes, void* stream);
+/* Reverse mode: adjoint seeds for every call's outputs ((nadj, nnz_out*N, ld)), sensitivities
+ * of x0 ((nadj, nnz, ld)) and of the stacked inputs ((nadj, nnz*N, ld)). The value sweeps of
+ * all calls run first (keeping every accumulator value), then call k = N-1 .. 0 records again
+ * from its stored inputs and runs its adjoint with the seed of its accumulator outputs plus
+ * the adjoint call k+1 returned for them: checkpointing at every call boundary. */
+CASADI_GB300_API int casadi_gb300_mapaccum_reverse(int id, int N, int n_accum, int64_t n,
+                            int64_t ld, int nadj, const double* const* arg, double* const* res,
+                            const double* const* aseed, double* const* asens, void* scratch,
+                            size_t scratch_bytes, void* stream);
+
 /* Wait for all work on `stream` and report device-side error flags raised by sweeps of this
  * tape (bounded waits that ran out, malformed instructions). Clears the flags. */
 CASADI_GB300_API int casadi_gb300_sync(int id, void* stream);
