@@ -28,13 +28,34 @@ from . import runtime as R
 from . import sx as S
 
 
-def jacobian_pattern(tape, out, wrt):
-    """Sparsity of d output[out] / d input[wrt] of a :class:`runtime.CudaTape` as a
-    :class:`coloring.Pattern` (rows: output nonzeros, columns: input nonzeros), from one
-    forward sparsity sweep on the device."""
+def _bit_seeds(count):
+    """One bit per nonzero: nonzero k is bit k % 64 of chunk k // 64, shape (count, chunks)."""
     import torch
+    nchunk = max(1, (count + 63) // 64)
+    bits = torch.zeros((max(count, 1), nchunk), dtype=torch.int64)
+    for k in range(count):
+        b = k % 64
+        bits[k, k // 64] = (1 << b) if b < 63 else -(1 << 63)
+    return bits, nchunk
+
+
+def jacobian_pattern(tape, out, wrt, mode="auto"):
+    """Sparsity of d output[out] / d input[wrt] of a :class:`runtime.CudaTape` as a
+    :class:`coloring.Pattern` (rows: output nonzeros, columns: input nonzeros), from
+    bvec_t sparsity sweeps on the device: ``forward`` seeds one bit per input nonzero
+    (ceil(ncol/64) instances of one sp_forward launch), ``reverse`` one bit per output
+    nonzero (ceil(nrow/64) instances of one sp_reverse launch); ``auto`` takes the one with
+    fewer instances, as the reference picks the mode with fewer sweeps
+    (FunctionInternal::get_jac_sparsity, casadi/core/function_internal.cpp:1928-1975)."""
     ncol = tape.nnz_in[wrt]
     nrow = tape.nnz_out[out]
+    if mode == "auto":
+        mode = "forward" if (ncol + 63) // 64 <= (nrow + 63) // 64 else "reverse"
+    if mode == "reverse":
+        return _jacobian_pattern_reverse(tape, out, wrt)
+    if mode != "forward":
+        raise ValueError("mode must be 'forward', 'reverse' or 'auto'")
+    import torch
     nchunk = max(1, (ncol + 63) // 64)
     bits = torch.zeros((max(ncol, 1), nchunk), dtype=torch.int64)
     for k in range(ncol):
@@ -48,6 +69,23 @@ def jacobian_pattern(tape, out, wrt):
     for c in range(nchunk):
         for b in range(min(64, ncol - 64 * c)):
             mask[:, 64 * c + b] = (ob[:, c] >> np.uint64(b)) & np.uint64(1) != 0
+    return K.Pattern.from_dense(mask)
+
+
+def _jacobian_pattern_reverse(tape, out, wrt):
+    import torch
+    ncol = tape.nnz_in[wrt]
+    nrow = tape.nnz_out[out]
+    seeds, nchunk = _bit_seeds(nrow)
+    args = [torch.zeros((k, nchunk), dtype=torch.int64, device="cuda") for k in tape.nnz_in]
+    res = [None] * len(tape.nnz_out)
+    res[out] = seeds.cuda()
+    tape.sp_reverse(args, res, n=nchunk)
+    ib = args[wrt].cpu().numpy().view(np.uint64)  # (ncol, nchunk)
+    mask = np.zeros((nrow, ncol), dtype=bool)
+    for c in range(nchunk):
+        for b in range(min(64, nrow - 64 * c)):
+            mask[64 * c + b, :] = (ib[:, c] >> np.uint64(b)) & np.uint64(1) != 0
     return K.Pattern.from_dense(mask)
 
 

@@ -119,3 +119,19 @@ def test_colored_sweeps_same_bits_in_every_tangent_variant(gpu_lib, variant):
     assert same_bits(got_j, want_j).all()
     assert same_bits(got_h, want_h).all()
     J.tape.sync()
+
+
+def test_jacobian_pattern_forward_equals_reverse(gpu_lib):
+    """The Jacobian sparsity from forward bit sweeps (one bit per input nonzero) and from
+    reverse bit sweeps (one bit per output nonzero) are the same pattern."""
+    from casadi_gb300 import runtime as R
+    from casadi_gb300.sparse_ad import jacobian_pattern
+    for f, out in ((W.quad_ms_constraints(INTERVALS), 0), (W.random_dag(n_in=70, n_nodes=900,
+                                                                        n_out=130, seed=8), 0)):
+        ct = R.CudaTape(f)
+        pf = jacobian_pattern(ct, out, 0, mode="forward")
+        pr = jacobian_pattern(ct, out, 0, mode="reverse")
+        assert np.array_equal(pf.dense(), pr.dense())
+        pa = jacobian_pattern(ct, out, 0)
+        assert np.array_equal(pa.dense(), pf.dense())
+        ct.sync()
