@@ -467,6 +467,34 @@ uint4 dir_entry(u64 w, unsigned flags, int pk) {
   return e;
 }
 
+// Operand forwarding in a one-direction tangent stream: an operand that is the value the
+// previous value-writing entry just computed is marked (bit 31 of its slot offset) and the
+// sweep takes it from a register instead of reading it back from shared memory.
+constexpr unsigned kFwdBit = 1u << 31;
+void forward_operands(std::vector<uint4>& ents) {
+  bool have = false;
+  unsigned last = 0;  // slot byte offset the previous value-writing entry wrote
+  for (uint4& e : ents) {
+    const unsigned kind = (e.w >> 5) & 15u, f = e.w & 3u;
+    if (kind == LK_OUTPUT) {
+      if (have && (f & 1u) && e.y == last) e.y |= kFwdBit;
+      continue;
+    }
+    if (kind == LK_INPUT) {
+      if (f & 1u) {
+        have = true;
+        last = e.x;
+      }
+      continue;
+    }
+    if (kind == LK_NOP || kind == LK_CONST || !f) continue;
+    if (have && (f & 1u) && e.y == last) e.y |= kFwdBit;
+    if (have && (f & 2u) && e.z == last) e.z |= kFwdBit;
+    have = true;
+    last = e.x;
+  }
+}
+
 // Appends one stream, padded with NOP entries to whole groups; returns (first, count).
 int2 push_stream(std::vector<uint4>& all, const std::vector<uint4>& ents) {
   const int first = static_cast<int>(all.size());
@@ -574,6 +602,7 @@ const TanPlan* tan_plan(Tape& t, int ndir, int dw, int ch, bool identity,
         ents.push_back(e);
       }
     }
+    if (dw == 1) forward_operands(ents);
     se[g] = push_stream(all, ents);
   }
   cudaError_t e;

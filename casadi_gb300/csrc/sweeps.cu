@@ -910,6 +910,11 @@ __device__ __forceinline__ void tangent_walk(const uint4* st, int ngr, const dou
                                              const long long (&ig)[IPT]) {
   uint4 E0[G], E1[G];
   double P0[G][IPT], Q0[G][IPT];
+  // one-direction streams mark operands that are the previous written value (bit 31 of the
+  // slot offset): they come from `last` instead of shared memory
+  double last[IPT];
+#pragma unroll
+  for (int j = 0; j < IPT; ++j) last[j] = 0.0;
   load_group<G>(st, 0, ngr, E0);
   load_group<G>(st, 1, ngr, E1);
   load_partials_n<kNC, false, G, IPT>(E0, pt, tstride, tok, P0, Q0);
@@ -925,27 +930,31 @@ __device__ __forceinline__ void tangent_walk(const uint4* st, int ngr, const dou
       const unsigned meta = cur.w;
       const unsigned xo = K > 1 ? (cur.x & kTanXMask) : cur.x;
 #define CGB_W(off, j, k) wj<IPT * K>(wb, (off), (j) * K + (k))
+// operand at slot offset `off` of tile j, direction k (forwarded from `last` when marked;
+// only one-direction streams carry marks)
+#define CGB_OP(off, j, k) \
+  ((K == 1 && ((off) & 0x80000000u)) ? last[j] : CGB_W((off) & 0x7fffffffu, j, k))
 #define CGB_JK _Pragma("unroll") for (int j = 0; j < IPT; ++j) _Pragma("unroll") for (int k = 0; k < K; ++k)
 // tangent of one arithmetic entry (kind and flags in `key`) for tile j, direction k
 #define CGB_TAN_CASES(R, j, k)                                                               \
-case (LK_GEN << 2) | 1u: R = __dmul_rn(P0[i][j], CGB_W(cur.y, j, k)); break;               \
-case (LK_GEN << 2) | 2u: R = __dmul_rn(Q0[i][j], CGB_W(cur.z, j, k)); break;               \
+case (LK_GEN << 2) | 1u: R = __dmul_rn(P0[i][j], CGB_OP(cur.y, j, k)); break;              \
+case (LK_GEN << 2) | 2u: R = __dmul_rn(Q0[i][j], CGB_OP(cur.z, j, k)); break;              \
 case (LK_GEN << 2) | 3u:                                                                   \
-  R = __dadd_rn(__dmul_rn(P0[i][j], CGB_W(cur.y, j, k)), __dmul_rn(Q0[i][j], CGB_W(cur.z, j, k))); \
+  R = __dadd_rn(__dmul_rn(P0[i][j], CGB_OP(cur.y, j, k)), __dmul_rn(Q0[i][j], CGB_OP(cur.z, j, k))); \
   break;                                                                                   \
-case (LK_ADD << 2) | 1u: R = CGB_W(cur.y, j, k); break;                                    \
-case (LK_ADD << 2) | 2u: R = CGB_W(cur.z, j, k); break;                                    \
-case (LK_ADD << 2) | 3u: R = __dadd_rn(CGB_W(cur.y, j, k), CGB_W(cur.z, j, k)); break;     \
-case (LK_SUB << 2) | 1u: R = CGB_W(cur.y, j, k); break;                                    \
-case (LK_SUB << 2) | 2u: R = d_neg(CGB_W(cur.z, j, k)); break;                             \
-case (LK_SUB << 2) | 3u: R = __dsub_rn(CGB_W(cur.y, j, k), CGB_W(cur.z, j, k)); break;     \
-case (LK_NEG << 2) | 1u: R = d_neg(CGB_W(cur.y, j, k)); break;                             \
+case (LK_ADD << 2) | 1u: R = CGB_OP(cur.y, j, k); break;                                   \
+case (LK_ADD << 2) | 2u: R = CGB_OP(cur.z, j, k); break;                                   \
+case (LK_ADD << 2) | 3u: R = __dadd_rn(CGB_OP(cur.y, j, k), CGB_OP(cur.z, j, k)); break;   \
+case (LK_SUB << 2) | 1u: R = CGB_OP(cur.y, j, k); break;                                   \
+case (LK_SUB << 2) | 2u: R = d_neg(CGB_OP(cur.z, j, k)); break;                            \
+case (LK_SUB << 2) | 3u: R = __dsub_rn(CGB_OP(cur.y, j, k), CGB_OP(cur.z, j, k)); break;   \
+case (LK_NEG << 2) | 1u: R = d_neg(CGB_OP(cur.y, j, k)); break;                            \
 case (LK_TWICE << 2) | 1u: {                                                               \
-  const double xb = CGB_W(cur.y, j, k);                                                    \
+  const double xb = CGB_OP(cur.y, j, k);                                                   \
   R = d_twice(xb);                                                                         \
 } break;                                                                                   \
-case (LK_ASSIGN << 2) | 1u: R = CGB_W(cur.y, j, k); break;                                 \
-case (LK_IFZ << 2) | 2u: R = d_iszero(Q0[i][j]) ? 0.0 : CGB_W(cur.z, j, k); break;
+case (LK_ASSIGN << 2) | 1u: R = CGB_OP(cur.y, j, k); break;                                \
+case (LK_IFZ << 2) | 2u: R = d_iszero(Q0[i][j]) ? 0.0 : CGB_OP(cur.z, j, k); break;
       // one jump-table dispatch on (kind, active operands): every case holds only the FP64
       // operations it needs, so nothing is computed speculatively (an FP64 instruction holds
       // a sub-partition's FP64 unit for ~64 cycles on GB300)
@@ -958,7 +967,7 @@ case (LK_IFZ << 2) | 2u: R = d_iszero(Q0[i][j]) ? 0.0 : CGB_W(cur.z, j, k); brea
           CGB_JK {
             if (dir0 + k < ndir && active[j] && d.ptr)
               static_cast<double*>(d.ptr)[io_off(d, dir0 + k, cur.z, ig[j])] =
-                  (meta & 1u) ? CGB_W(cur.y, j, k) : 0.0;
+                  (meta & 1u) ? CGB_OP(cur.y, j, k) : 0.0;
           }
           continue;
         }
@@ -1037,8 +1046,13 @@ case KEY: {            \
           continue;  // NOP padding
       }
       CGB_JK CGB_W(xo, j, k) = r[j][k];
+      if (K == 1) {
+#pragma unroll
+        for (int j = 0; j < IPT; ++j) last[j] = r[j][0];
+      }
 #undef CGB_TAN_CASES
 #undef CGB_JK
+#undef CGB_OP
 #undef CGB_W
     }
 #pragma unroll
