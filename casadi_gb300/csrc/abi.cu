@@ -209,13 +209,38 @@ struct Tape {
   }
 };
 
+constexpr int kMaxChunks = 4;  // host-buffer calls: instance chunks pipelined over copy engines
+
 struct Mem {
   cudaStream_t stream = nullptr;
+  // copy streams and events of the pipelined host-buffer calls (created on first use)
+  cudaStream_t s_in = nullptr, s_out = nullptr;
+  cudaEvent_t ev_in[kMaxChunks] = {}, ev_done[kMaxChunks] = {}, ev_out = nullptr;
   std::vector<void*> bufs;   // device staging buffers, grown on demand
   std::vector<size_t> caps;
   ~Mem() {
     for (void* p : bufs) cudaFree(p);
+    for (int k = 0; k < kMaxChunks; ++k) {
+      if (ev_in[k]) cudaEventDestroy(ev_in[k]);
+      if (ev_done[k]) cudaEventDestroy(ev_done[k]);
+    }
+    if (ev_out) cudaEventDestroy(ev_out);
+    if (s_in) cudaStreamDestroy(s_in);
+    if (s_out) cudaStreamDestroy(s_out);
     if (stream) cudaStreamDestroy(stream);
+  }
+  cudaError_t pipe() {
+    if (s_in) return cudaSuccess;
+    cudaError_t e;
+    if ((e = cudaStreamCreateWithFlags(&s_in, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&s_out, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming)) != cudaSuccess)
+      return e;
+    for (int k = 0; k < kMaxChunks; ++k)
+      if ((e = cudaEventCreateWithFlags(&ev_in[k], cudaEventDisableTiming)) != cudaSuccess ||
+          (e = cudaEventCreateWithFlags(&ev_done[k], cudaEventDisableTiming)) != cudaSuccess)
+        return e;
+    return cudaSuccess;
   }
   // device buffer k of at least `bytes`
   void* buf(size_t k, size_t bytes, cudaError_t* e) {
@@ -1816,16 +1841,75 @@ static int stage_blocks(Mem& m, size_t first_buf, int count, const std::vector<i
   return 0;
 }
 
-static int fetch_blocks(const IoDesc* desc, int count, const std::vector<int>& nnz, int ndir,
-                        long long n, double* const* host, cudaStream_t s) {
+extern "C++" {
+namespace {
+// Host blocks of a host-buffer call: each device descriptor (instance-major staging buffer,
+// desc->inst_stride doubles per instance) with the host array it is uploaded from or
+// downloaded to.
+struct HostBlock {
+  const IoDesc* desc;
+  const double* up;  // upload source (inputs, seeds) or null
+  double* down;      // download target (outputs, sensitivities) or null
+};
+
+void collect_blocks(std::vector<HostBlock>& v, const IoDesc* desc, int count, const double* const* up,
+                double* const* down) {
+  for (int j = 0; j < count; ++j)
+    if (desc[j].ptr) v.push_back({&desc[j], up ? up[j] : nullptr, down ? down[j] : nullptr});
+}
+
+// Descriptors of instances [i0, ...) of instance-major staging descriptors.
+void shift_io(const IoDesc* src, int count, long long i0, IoDesc* dst) {
   for (int j = 0; j < count; ++j) {
-    if (!host || !host[j] || !desc[j].ptr) continue;
-    const size_t bytes = sizeof(double) * static_cast<size_t>(n) * nnz[j] * std::max(1, ndir);
-    cudaError_t e = cudaMemcpyAsync(host[j], desc[j].ptr, bytes, cudaMemcpyDeviceToHost, s);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(D2H)");
+    dst[j] = src[j];
+    if (src[j].ptr)
+      dst[j].ptr = static_cast<double*>(src[j].ptr) + i0 * src[j].inst_stride;
   }
+}
+
+// Host-buffer call over n instances in up to kMaxChunks chunks: the upload of chunk c+1 (copy
+// stream s_in) and the download of chunk c-1 (s_out) overlap the sweeps of chunk c (the
+// memory object's stream). `compute(i0, count)` enqueues one chunk's sweeps on m.stream.
+template <class F>
+int run_pipelined(Mem& m, long long n, const std::vector<HostBlock>& blocks, F compute) {
+  cudaError_t e = m.pipe();
+  if (e != cudaSuccess) return cuda_fail(e, "copy streams");
+  int chunks = n >= 4 * 32768 ? 4 : (n >= 2 * 32768 ? 2 : 1);
+  const long long per = ((n + chunks - 1) / chunks + 31) / 32 * 32;
+  chunks = static_cast<int>((n + per - 1) / per);
+  for (int c = 0; c < chunks; ++c) {
+    const long long i0 = c * per, cnt = std::min(per, n - i0);
+    for (const auto& b : blocks) {
+      if (!b.up) continue;
+      const size_t bytes = sizeof(double) * static_cast<size_t>(b.desc->inst_stride);
+      if ((e = cudaMemcpyAsync(static_cast<double*>(b.desc->ptr) + i0 * b.desc->inst_stride,
+                               b.up + i0 * b.desc->inst_stride, bytes * cnt,
+                               cudaMemcpyHostToDevice, m.s_in)) != cudaSuccess)
+        return cuda_fail(e, "cudaMemcpyAsync(H2D)");
+    }
+    if ((e = cudaEventRecord(m.ev_in[c], m.s_in)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(m.stream, m.ev_in[c], 0)) != cudaSuccess)
+      return cuda_fail(e, "chunk ordering");
+    if (int rc = compute(i0, cnt)) return rc;
+    if ((e = cudaEventRecord(m.ev_done[c], m.stream)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(m.s_out, m.ev_done[c], 0)) != cudaSuccess)
+      return cuda_fail(e, "chunk ordering");
+    for (const auto& b : blocks) {
+      if (!b.down) continue;
+      const size_t bytes = sizeof(double) * static_cast<size_t>(b.desc->inst_stride);
+      if ((e = cudaMemcpyAsync(b.down + i0 * b.desc->inst_stride,
+                               static_cast<double*>(b.desc->ptr) + i0 * b.desc->inst_stride,
+                               bytes * cnt, cudaMemcpyDeviceToHost, m.s_out)) != cudaSuccess)
+        return cuda_fail(e, "cudaMemcpyAsync(D2H)");
+    }
+  }
+  if ((e = cudaEventRecord(m.ev_out, m.s_out)) != cudaSuccess ||
+      (e = cudaStreamWaitEvent(m.stream, m.ev_out, 0)) != cudaSuccess)
+    return cuda_fail(e, "chunk ordering");
   return 0;
 }
+}  // namespace
+}  // extern "C++"
 
 // Partials scratch of a memory object for the host-buffer AD paths; waves keep it <= 8 GiB.
 static int map_scratch(const Tape& t, Mem& m, long long n, void** scratch, size_t* bytes) {
@@ -1852,13 +1936,21 @@ int casadi_gb300_map_eval(int id, int mem, int64_t n, const double* const* arg,
   if (n < 0) return fail(CASADI_GB300_ERR_ARG, "negative instance count");
   if (n == 0) return 0;
   cudaStream_t s = m->stream;
-  SweepArgs a = base_args(*t, n, 0);
-  if (int rc = stage_blocks(*m, 0, t->n_in, t->nnz_in, 1, n, arg, true, a.in, s)) return rc;
+  IoDesc in[kMaxIo], out[kMaxIo];
+  if (int rc = stage_blocks(*m, 0, t->n_in, t->nnz_in, 1, n, arg, false, in, s)) return rc;
   if (int rc = stage_blocks(*m, kMaxIo, t->n_out, t->nnz_out, 1, n,
-                            reinterpret_cast<const double* const*>(res), false, a.out, s))
+                            reinterpret_cast<const double* const*>(res), false, out, s))
     return rc;
-  if (int rc = primal_launch(*t, a, n, PK_EVAL, s)) return rc;
-  if (int rc = fetch_blocks(a.out, t->n_out, t->nnz_out, 1, n, res, s)) return rc;
+  std::vector<HostBlock> blocks;
+  collect_blocks(blocks, in, t->n_in, arg, nullptr);
+  collect_blocks(blocks, out, t->n_out, nullptr, res);
+  if (int rc = run_pipelined(*m, n, blocks, [&](long long i0, long long cnt) {
+        SweepArgs a = base_args(*t, cnt, 0);
+        shift_io(in, t->n_in, i0, a.in);
+        shift_io(out, t->n_out, i0, a.out);
+        return primal_launch(*t, a, cnt, PK_EVAL, s);
+      }))
+    return rc;
   return casadi_gb300_sync(id, s);
 }
 
@@ -1876,7 +1968,7 @@ int casadi_gb300_map_jacobian(int id, int mem, int64_t n, const double* const* a
   if (nz == 0) return fail(CASADI_GB300_ERR_ARG, "tape has no input nonzeros");
   cudaStream_t s = m->stream;
   IoDesc in[kMaxIo], out[kMaxIo], sens[kMaxIo];
-  if (int rc = stage_blocks(*m, 0, t->n_in, t->nnz_in, 1, n, arg, true, in, s)) return rc;
+  if (int rc = stage_blocks(*m, 0, t->n_in, t->nnz_in, 1, n, arg, false, in, s)) return rc;
   if (int rc = stage_blocks(*m, kMaxIo, t->n_out, t->nnz_out, 1, n,
                             reinterpret_cast<const double* const*>(res), false, out, s))
     return rc;
@@ -1888,9 +1980,18 @@ int casadi_gb300_map_jacobian(int id, int mem, int64_t n, const double* const* a
   if (int rc = map_scratch(*t, *m, n, &scratch, &bytes)) return rc;
   IoDesc seed[kMaxIo];
   std::memset(seed, 0, sizeof(seed));
-  if (int rc = run_ad(*t, n, in, out, seed, sens, nz, false, true, scratch, bytes, s)) return rc;
-  if (int rc = fetch_blocks(out, t->n_out, t->nnz_out, 1, n, res, s)) return rc;
-  if (int rc = fetch_blocks(sens, t->n_out, t->nnz_out, nz, n, jac, s)) return rc;
+  std::vector<HostBlock> blocks;
+  collect_blocks(blocks, in, t->n_in, arg, nullptr);
+  collect_blocks(blocks, out, t->n_out, nullptr, res);
+  collect_blocks(blocks, sens, t->n_out, nullptr, jac);
+  if (int rc = run_pipelined(*m, n, blocks, [&](long long i0, long long cnt) {
+        IoDesc in_c[kMaxIo], out_c[kMaxIo], sens_c[kMaxIo];
+        shift_io(in, t->n_in, i0, in_c);
+        shift_io(out, t->n_out, i0, out_c);
+        shift_io(sens, t->n_out, i0, sens_c);
+        return run_ad(*t, cnt, in_c, out_c, seed, sens_c, nz, false, true, scratch, bytes, s);
+      }))
+    return rc;
   return casadi_gb300_sync(id, s);
 }
 
@@ -1906,11 +2007,11 @@ int casadi_gb300_map_reverse(int id, int mem, int64_t n, int nadj, const double*
   if (n == 0) return 0;
   cudaStream_t s = m->stream;
   IoDesc in[kMaxIo], out[kMaxIo], seed[kMaxIo], sens[kMaxIo];
-  if (int rc = stage_blocks(*m, 0, t->n_in, t->nnz_in, 1, n, arg, true, in, s)) return rc;
+  if (int rc = stage_blocks(*m, 0, t->n_in, t->nnz_in, 1, n, arg, false, in, s)) return rc;
   if (int rc = stage_blocks(*m, kMaxIo, t->n_out, t->nnz_out, 1, n,
                             reinterpret_cast<const double* const*>(res), false, out, s))
     return rc;
-  if (int rc = stage_blocks(*m, 2 * kMaxIo, t->n_out, t->nnz_out, nadj, n, aseed, true, seed, s))
+  if (int rc = stage_blocks(*m, 2 * kMaxIo, t->n_out, t->nnz_out, nadj, n, aseed, false, seed, s))
     return rc;
   if (int rc = stage_blocks(*m, 3 * kMaxIo, t->n_in, t->nnz_in, nadj, n,
                             reinterpret_cast<const double* const*>(asens), false, sens, s))
@@ -1918,9 +2019,20 @@ int casadi_gb300_map_reverse(int id, int mem, int64_t n, int nadj, const double*
   void* scratch = nullptr;
   size_t bytes = 0;
   if (int rc = map_scratch(*t, *m, n, &scratch, &bytes)) return rc;
-  if (int rc = run_ad(*t, n, in, out, seed, sens, nadj, true, false, scratch, bytes, s)) return rc;
-  if (int rc = fetch_blocks(out, t->n_out, t->nnz_out, 1, n, res, s)) return rc;
-  if (int rc = fetch_blocks(sens, t->n_in, t->nnz_in, nadj, n, asens, s)) return rc;
+  std::vector<HostBlock> blocks;
+  collect_blocks(blocks, in, t->n_in, arg, nullptr);
+  collect_blocks(blocks, seed, t->n_out, aseed, nullptr);
+  collect_blocks(blocks, out, t->n_out, nullptr, res);
+  collect_blocks(blocks, sens, t->n_in, nullptr, asens);
+  if (int rc = run_pipelined(*m, n, blocks, [&](long long i0, long long cnt) {
+        IoDesc in_c[kMaxIo], out_c[kMaxIo], seed_c[kMaxIo], sens_c[kMaxIo];
+        shift_io(in, t->n_in, i0, in_c);
+        shift_io(out, t->n_out, i0, out_c);
+        shift_io(seed, t->n_out, i0, seed_c);
+        shift_io(sens, t->n_in, i0, sens_c);
+        return run_ad(*t, cnt, in_c, out_c, seed_c, sens_c, nadj, true, false, scratch, bytes, s);
+      }))
+    return rc;
   return casadi_gb300_sync(id, s);
 }
 
@@ -1940,11 +2052,13 @@ int casadi_gb300_map_jacobian_reverse(int id, int mem, int64_t n, const double* 
   cudaStream_t s = m->stream;
   IoDesc in[kMaxIo], out[kMaxIo], fsens[kMaxIo], aseedd[kMaxIo], asensd[kMaxIo], fseed[kMaxIo];
   std::memset(fseed, 0, sizeof(fseed));
-  if (int rc = stage_blocks(*m, 0, t->n_in, t->nnz_in, 1, n, arg, true, in, s)) return rc;
+  // staging buffers only: the pipelined copies below move the data chunk by chunk
+  if (int rc = stage_blocks(*m, 0, t->n_in, t->nnz_in, 1, n, arg, false, in, s)) return rc;
   if (int rc = stage_blocks(*m, kMaxIo, t->n_out, t->nnz_out, 1, n,
                             reinterpret_cast<const double* const*>(res), false, out, s))
     return rc;
-  if (int rc = stage_blocks(*m, 2 * kMaxIo, t->n_out, t->nnz_out, nadj, n, aseed, true, aseedd, s))
+  if (int rc = stage_blocks(*m, 2 * kMaxIo, t->n_out, t->nnz_out, nadj, n, aseed, false, aseedd,
+                            s))
     return rc;
   if (int rc = stage_blocks(*m, 3 * kMaxIo, t->n_out, t->nnz_out, nz, n,
                             reinterpret_cast<const double* const*>(jac), false, fsens, s))
@@ -1955,19 +2069,31 @@ int casadi_gb300_map_jacobian_reverse(int id, int mem, int64_t n, const double* 
   void* scratch = nullptr;
   size_t bytes = 0;
   if (int rc = map_scratch(*t, *m, n, &scratch, &bytes)) return rc;
-  DerivReq rq[2];
-  rq[0].ndir = nz;
-  rq[0].identity = true;
-  rq[0].seed = fseed;
-  rq[0].sens = fsens;
-  rq[1].ndir = nadj;
-  rq[1].adjoint = true;
-  rq[1].seed = aseedd;
-  rq[1].sens = asensd;
-  if (int rc = run_ad_multi(*t, n, in, out, rq, 2, scratch, bytes, s)) return rc;
-  if (int rc = fetch_blocks(out, t->n_out, t->nnz_out, 1, n, res, s)) return rc;
-  if (int rc = fetch_blocks(fsens, t->n_out, t->nnz_out, nz, n, jac, s)) return rc;
-  if (int rc = fetch_blocks(asensd, t->n_in, t->nnz_in, nadj, n, asens, s)) return rc;
+  std::vector<HostBlock> blocks;
+  collect_blocks(blocks, in, t->n_in, arg, nullptr);
+  collect_blocks(blocks, aseedd, t->n_out, aseed, nullptr);
+  collect_blocks(blocks, out, t->n_out, nullptr, res);
+  collect_blocks(blocks, fsens, t->n_out, nullptr, jac);
+  collect_blocks(blocks, asensd, t->n_in, nullptr, asens);
+  if (int rc = run_pipelined(*m, n, blocks, [&](long long i0, long long cnt) {
+        IoDesc in_c[kMaxIo], out_c[kMaxIo], fsens_c[kMaxIo], aseed_c[kMaxIo], asens_c[kMaxIo];
+        shift_io(in, t->n_in, i0, in_c);
+        shift_io(out, t->n_out, i0, out_c);
+        shift_io(fsens, t->n_out, i0, fsens_c);
+        shift_io(aseedd, t->n_out, i0, aseed_c);
+        shift_io(asensd, t->n_in, i0, asens_c);
+        DerivReq rq[2];
+        rq[0].ndir = nz;
+        rq[0].identity = true;
+        rq[0].seed = fseed;
+        rq[0].sens = fsens_c;
+        rq[1].ndir = nadj;
+        rq[1].adjoint = true;
+        rq[1].seed = aseed_c;
+        rq[1].sens = asens_c;
+        return run_ad_multi(*t, cnt, in_c, out_c, rq, 2, scratch, bytes, s);
+      }))
+    return rc;
   return casadi_gb300_sync(id, s);
 }
 
