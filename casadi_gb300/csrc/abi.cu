@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -122,7 +123,7 @@ struct Tape {
                       // 1 global memory, 2 shared memory whenever it fits
   // per PrimalKind and launch size class (0: at most 16 tiles per SM): 0 shared, 1 global,
   // 2 cooperative level sweep (autotuned)
-  int primal_tuned[5][2] = {{-1, -1}, {-1, -1}, {-1, -1}, {-1, -1}, {-1, -1}};
+  std::atomic<int> primal_tuned[5][2];
   // level schedule of the cooperative value/record sweeps, built on first use
   int lv_state = 0;  // 0 not built, 1 built, -1 unavailable
   u64* d_lcode = nullptr;
@@ -155,7 +156,13 @@ struct Tape {
   std::mutex shape_mtx;
   // derivative-sweep variant per kind (seeded/identity tangent, adjoint) and launch size class
   // (0: at most 16 tiles per SM); tangent kinds may keep the cooperative sweep (TV_COUNT)
-  int tuned[3][2] = {{-1, -1}, {-1, -1}, {-1, -1}};
+  std::atomic<int> tuned[3][2];
+  // one thread tunes a tape at a time; others meanwhile run the untuned defaults
+  std::mutex tune_mtx;
+  Tape() {
+    for (auto& k : primal_tuned) k[0] = k[1] = -1;
+    for (auto& k : tuned) k[0] = k[1] = -1;
+  }
   std::vector<double> h_consts;  // constant pool (host copy, for inlining into callers)
   std::vector<u64> h_code;                            // padded instruction stream
   std::vector<std::unique_ptr<TanPlan>> tan_plans;
@@ -880,14 +887,16 @@ int primal_launch(Tape& t, SweepArgs& a, long long m, PrimalKind kind, cudaStrea
   cand[nc++] = M_GLOBAL;
   if (coop_kind && can_coop && (cls == 0 || t.residence == 3))
     for (int c = M_COOP; c <= M_COOP_LAST; ++c) cand[nc++] = c;
-  int& choice = t.primal_tuned[kind][cls];
+  std::atomic<int>& choice = t.primal_tuned[kind][cls];
   // sp_reverse consumes its seeds and cannot be timed twice: it follows sp_forward's choice
   if (rev && choice < 0 && t.primal_tuned[PK_SP_FORWARD][cls] >= 0)
-    choice = t.primal_tuned[PK_SP_FORWARD][cls];
+    choice = t.primal_tuned[PK_SP_FORWARD][cls].load();
   // residence is tuned like the derivative variants: every candidate timed once on the first
   // call of each kind and size class (every sweep here but sp_reverse, which consumes its
   // seeds, can run twice with the same results)
-  if (choice < 0 && nc > 1 && g_autotune && kind != PK_SP_REVERSE && !capturing(s)) {
+  std::unique_lock<std::mutex> tune_lock(t.tune_mtx, std::defer_lock);
+  if (choice < 0 && nc > 1 && g_autotune && kind != PK_SP_REVERSE && !capturing(s) &&
+      tune_lock.try_lock()) {
     float ms[5] = {0, 0, 0, 0, 0};
     for (int c = 0; c < nc; ++c) {
       int rc = 0;
@@ -901,8 +910,9 @@ int primal_launch(Tape& t, SweepArgs& a, long long m, PrimalKind kind, cudaStrea
     choice = cand[best];
     return 0;  // every run produced the same (complete) results
   }
-  if (choice >= 0 && (choice < M_COOP || can_coop) && (choice != M_SHARED || fits_smem(t.sz_w)))
-    return run(choice, true);
+  const int chosen = choice;
+  if (chosen >= 0 && (chosen < M_COOP || can_coop) && (chosen != M_SHARED || fits_smem(t.sz_w)))
+    return run(chosen, true);
   return run(cand[0], true);
 }
 
@@ -1048,13 +1058,15 @@ int run_deriv(Tape& t, SweepArgs a, long long m, const DerivReq& rq, cudaStream_
   auto run_v = [&](int v) {
     return v == kCoop ? (adjoint ? launch_coop_adj() : launch_coop_tan()) : launch(v);
   };
-  int& kept = t.tuned[kind][cls];
+  std::atomic<int>& kept = t.tuned[kind][cls];
   int variant = kept;
   if (variant >= 0 && !usable(variant)) variant = -1;
   if (variant < 0) {
     // tune outside capture: on waves that fill the GPU at least twice at 8 warps per SM, and
     // on every small launch, where the cooperative sweep is a candidate too
-    if (g_autotune && !capturing(s) && (work >= 2ll * sms * 8 || cls == 0)) {
+    std::unique_lock<std::mutex> tune_lock(t.tune_mtx, std::defer_lock);
+    if (g_autotune && !capturing(s) && (work >= 2ll * sms * 8 || cls == 0) &&
+        tune_lock.try_lock()) {
       float best = 0;
       for (int c = 0; c <= n_variants; ++c) {
         // the variants of the kind, then (tangents) the cooperative sweep
