@@ -136,12 +136,6 @@ struct Tape {
   int* d_rbegin = nullptr;
   int* d_rpidx = nullptr;
   int n_rlevels = 0, rlv_sz_w = 0;
-  // the narrow schedule of one warp's walk with instruction-level parallelism (batch)
-  int ilv_state = 0;
-  u64* d_icode = nullptr;
-  int* d_ibegin = nullptr;
-  int* d_ipidx = nullptr;
-  int n_ilevels = 0, ilv_sz_w = 0;
   // global work vector: per-CTA blocks, grown on demand; uses on different streams are
   // ordered by gw_event
   std::mutex gw_mtx;
@@ -191,9 +185,6 @@ struct Tape {
     cudaFree(d_rcode);
     cudaFree(d_rbegin);
     cudaFree(d_rpidx);
-    cudaFree(d_icode);
-    cudaFree(d_ibegin);
-    cudaFree(d_ipidx);
     if (gw_event) cudaEventSynchronize(gw_event);
     cudaFree(d_gw);
     if (gw_event) cudaEventDestroy(gw_event);
@@ -221,11 +212,6 @@ struct Tape {
     v.rpidx = d_rpidx;
     v.n_rlevels = n_rlevels;
     v.rlv_sz_w = rlv_sz_w;
-    v.icode = ilv_state > 0 ? d_icode : nullptr;
-    v.ibegin = d_ibegin;
-    v.ipidx = d_ipidx;
-    v.n_ilevels = n_ilevels;
-    v.ilv_sz_w = ilv_sz_w;
     return v;
   }
 };
@@ -763,22 +749,15 @@ int coop_threads_for(long long tiles) {
   const long long want = static_cast<long long>(sm_count()) * 32 / std::max(1ll, tiles);
   return want >= 32 ? 1024 : (want >= 16 ? 512 : 256);
 }
-// which: 0 the cooperative forward schedule, 1 the cooperative reverse schedule (ordered
-// users), 2 the narrow schedule of the batch's one-warp walk (width 32, at most sz_w live
-// values, so the work vector does not grow)
-enum { LV_COOP = 0, LV_REVERSE = 1, LV_ILP = 2 };
-bool ensure_levels(Tape& t, int which = LV_COOP) {
+bool ensure_levels(Tape& t, bool reverse = false) {
   std::lock_guard<std::mutex> lk(t.shape_mtx);
-  const bool reverse = which == LV_REVERSE;
-  int& state = which == LV_ILP ? t.ilv_state : (reverse ? t.rlv_state : t.lv_state);
+  int& state = reverse ? t.rlv_state : t.lv_state;
   if (state != 0) return state > 0;
   state = -1;
   Levels lv;
   std::string err;
-  const int cap = which == LV_ILP ? std::max(1, t.sz_w)
-                                  : (t.sz_w <= 400 ? 400 : t.sz_w + kLevelWidth);
-  const int width = which == LV_ILP ? 32 : kLevelWidth;
-  const int nl = level_schedule(t.h_code, width, cap, lv, err, reverse);
+  const int cap = t.sz_w <= 400 ? 400 : t.sz_w + kLevelWidth;
+  const int nl = level_schedule(t.h_code, kLevelWidth, cap, lv, err, reverse);
   if (nl <= 0 || lv.code.empty()) return false;
   u64* code = nullptr;
   int *begin = nullptr, *pidx = nullptr;
@@ -799,13 +778,7 @@ bool ensure_levels(Tape& t, int which = LV_COOP) {
     cudaGetLastError();
     return false;
   }
-  if (which == LV_ILP) {
-    t.d_icode = code;
-    t.d_ibegin = begin;
-    t.d_ipidx = pidx;
-    t.n_ilevels = nl;
-    t.ilv_sz_w = lv.sz_w;
-  } else if (reverse) {
+  if (reverse) {
     t.d_rcode = code;
     t.d_rbegin = begin;
     t.d_rpidx = pidx;
@@ -2299,7 +2272,6 @@ struct BatchHost {
   // work-vector residence: 0 shared memory, 1 global memory (grid_gw CTAs), -1 not tuned yet
   int residence = -1;
   int forced = 0;  // 0 tune, 1 global memory, 2 shared memory
-  bool ilp = true;  // value/record walks over the narrow level schedule when built
   int grid_gw = 1;
   unsigned char* d_gw = nullptr;
   int device = 0;
@@ -2362,12 +2334,7 @@ int batch_prepare(BatchHost& b) {
     if (!t) return fail(CASADI_GB300_ERR_ID, "batch item %zu: tape %d is gone", k, it.tape);
     BatchItem bi;
     std::memset(&bi, 0, sizeof(bi));
-    // the one-warp walk over the narrow level schedule (instruction-level parallelism) when
-    // it is available and the batch does not force the sequential walk
-    if (b.ilp) ensure_levels(*t, LV_ILP);
     bi.t = t->view();
-    if (!b.ilp) bi.t.icode = nullptr;
-    if (bi.t.icode) b.szw = std::max(b.szw, t->ilv_sz_w);
     bi.n_code = t->n_chunks * kChunk;
     bi.ndir = it.ndir;
     bi.n = it.n;
@@ -2420,9 +2387,7 @@ int batch_prepare(BatchHost& b) {
                        smem_coop(t->lv_sz_w) <= static_cast<size_t>(max_smem_optin());
       if (pre) {
         b.pre.push_back({static_cast<int>(k), n_flags, tiles, tp});
-        const u64* icode = bi.t.icode;
         bi.t = t->view();
-        bi.t.icode = icode;
       }
       for (long long tile = 0; tile < tiles; ++tile) {
         if (!pre)
@@ -2605,14 +2570,6 @@ int casadi_gb300_batch_add_jacobian_colored(int batch, int id, int64_t n, int64_
   b->items.push_back(std::move(it));
   b->dirty = true;
   return static_cast<int>(b->items.size()) - 1;
-}
-
-int casadi_gb300_batch_set_ilp(int batch, int enable) {
-  BatchHost* b = get_batch(batch);
-  if (!b) return fail(CASADI_GB300_ERR_ID, "no batch %d", batch);
-  b->ilp = enable != 0;
-  b->dirty = true;
-  return 0;
 }
 
 int casadi_gb300_batch_set_residence(int batch, int mode) {

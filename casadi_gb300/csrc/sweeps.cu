@@ -1350,79 +1350,6 @@ __device__ __forceinline__ void primal_walk(const TapeView& t, int n_code, doubl
   }
 }
 
-// The same walk over the narrow level schedule: the instructions of a level are independent,
-// so the warp loads the operands of Q of them, computes all Q results into registers and only
-// then stores them -- Q FP64 chains in flight instead of one. Partials go to each
-// instruction's index of the sequential order (the adjoint walk reads them there).
-template <bool RECORD, int Q>
-__device__ __forceinline__ void primal_walk_levels(const TapeView& t, double* pt,
-                                                   unsigned char* wb, const IoDesc* in,
-                                                   const IoDesc* out, bool active,
-                                                   long long ig) {
-  const u64 nop = static_cast<u64>(D_NOP);
-  int end = __ldg(t.ibegin);
-#pragma unroll 1
-  for (int l = 0; l < t.n_ilevels; ++l) {
-    const int beg = end;
-    end = __ldg(t.ibegin + l + 1);
-#pragma unroll 1
-    for (int base = beg; base < end; base += Q) {
-      u64 ins[Q];
-      double x[Q], y[Q], f[Q], p0[Q], p1[Q];
-#pragma unroll
-      for (int q = 0; q < Q; ++q) {
-        ins[q] = base + q < end ? __ldg(t.icode + base + q) : nop;
-        const unsigned op = dec_op(ins[q]), A = dec_a(ins[q]), B = dec_b(ins[q]),
-                       C = dec_c(ins[q]);
-        x[q] = 0.0;
-        y[q] = 0.0;
-        if (op == D_CONST) {
-          x[q] = __ldg(t.consts + B);
-        } else if (op == D_INPUT) {
-          const IoDesc& d = in[B];
-          if (active && d.ptr) x[q] = __ldg(static_cast<const double*>(d.ptr) + io_off(d, 0, C, ig));
-        } else if (op == D_OUTPUT) {
-          x[q] = wreg(wb, B * 256u);
-        } else if (op != D_NOP) {
-          x[q] = wreg(wb, B * 256u);
-          y[q] = wreg(wb, C * 256u);
-        }
-        (void)A;
-      }
-#pragma unroll
-      for (int q = 0; q < Q; ++q) {
-        const unsigned op = dec_op(ins[q]);
-        f[q] = x[q];
-        p0[q] = 0.0;
-        p1[q] = 0.0;
-        if (is_arith(op)) {
-          if (RECORD) f[q] = dev_fun_der(op, x[q], y[q], p0[q], p1[q]);
-          else f[q] = dev_fun(op, x[q], y[q]);
-        }
-      }
-#pragma unroll
-      for (int q = 0; q < Q; ++q) {
-        const unsigned op = dec_op(ins[q]), A = dec_a(ins[q]), C = dec_c(ins[q]);
-        if (op == D_NOP) continue;
-        if (op == D_OUTPUT) {
-          const IoDesc& d = out[A];
-          if (active && d.ptr) static_cast<double*>(d.ptr)[io_off(d, 0, C, ig)] = f[q];
-          continue;
-        }
-        if (RECORD && is_arith(op)) {
-          const unsigned m = dec_pmask(ins[q]);
-          if (m) {
-            const size_t pk = static_cast<size_t>(__ldg(t.ipidx + base + q));
-            if (m & 1u) pt[32 * pk] = p0[q];
-            if (m & 2u) pt[32 * (pk + (m & 1u))] = p1[q];
-          }
-        }
-        wreg(wb, A * 256u) = f[q];
-      }
-    }
-  }
-}
-
 // Bounded wait (lane 0, then shared with the warp) for a split item's tile flag. Every record
 // unit precedes every direction unit in the list, so the unit that sets the flag was taken by
 // a CTA that is already running and waits on nothing: the wait ends unless that CTA faults.
@@ -1473,16 +1400,10 @@ __global__ void __launch_bounds__(32, 16) k_batch(const __grid_constant__ BatchA
     if (!kSplit || unit.z < 0) {
       // record (or value) unit
       if (it.ndir == 0) {
-        if (it.t.icode)
-          primal_walk_levels<false, kIlpGroup>(it.t, pt, wb, io, io + kMaxIo, active, il);
-        else
-          primal_walk<false>(it.t, it.n_code, pt, wb, io, io + kMaxIo, active, il);
+        primal_walk<false>(it.t, it.n_code, pt, wb, io, io + kMaxIo, active, il);
         continue;
       }
-      if (it.t.icode)
-        primal_walk_levels<true, kIlpGroup>(it.t, pt, wb, io, io + kMaxIo, active, il);
-      else
-        primal_walk<true>(it.t, it.n_code, pt, wb, io, io + kMaxIo, active, il);
+      primal_walk<true>(it.t, it.n_code, pt, wb, io, io + kMaxIo, active, il);
       if (kSplit && it.tile_partials) {
         // split item: publish the tile's partials; its directions are separate units
         __threadfence();

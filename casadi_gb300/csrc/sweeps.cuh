@@ -11,8 +11,7 @@ constexpr int kChunk = 256;      // instructions per staged chunk (2 KiB), value
 constexpr int kPofsGran = 16;    // granularity of the per-chunk partial offsets
 constexpr int kLeanPB = 63;      // partials per staged chunk block (plan-free adjoint)
 constexpr int kEntGroup = 8;     // entry streams are padded to a multiple of this
-constexpr int kBatchGroup = 4;
-constexpr int kIlpGroup = 4;    // independent instructions a batch warp computes at once   // entries per software-pipelined group in the batch kernel
+constexpr int kBatchGroup = 4;   // entries per software-pipelined group in the batch kernel
 constexpr unsigned kMaxPartials = 1u << 21;  // recorded partials per instance the entries address
 
 // Entry kinds of the lean derivative streams (bits 16-19 of an entry's meta word).
@@ -54,13 +53,6 @@ struct TapeView {
   const int* rpidx;
   int n_rlevels;
   int rlv_sz_w;
-  // narrow level schedule (at most sz_w live values) for one warp's value/record walk with
-  // instruction-level parallelism (persistent batch); null when not built
-  const u64* icode;
-  const int* ibegin;
-  const int* ipidx;
-  int n_ilevels;
-  int ilv_sz_w;
 };
 
 struct SweepArgs {

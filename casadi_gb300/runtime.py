@@ -115,7 +115,6 @@ def load(path=None):
         "casadi_gb300_batch_scratch_size": (cint, [cint, vp]),
         "casadi_gb300_batch_status": (cint, [cint]),
         "casadi_gb300_batch_set_residence": (cint, [cint, cint]),
-        "casadi_gb300_batch_set_ilp": (cint, [cint, cint]),
         "casadi_gb300_batch_add_jacobian_colored": (cint, [cint, cint, i64, i64, cint, vp, vp, vp,
                                                            vp]),
         "casadi_gb300_batch_run": (cint, [cint, vp, sz, cint, vp]),
@@ -726,10 +725,6 @@ class Batch:
     def set_residence(self, mode):
         """Work vectors: 0 tuned (default), 1 global memory, 2 shared memory."""
         check(load().casadi_gb300_batch_set_residence(self.id, mode))
-
-    def set_ilp(self, enable=True):
-        """Value/record walks over the tapes' narrow level schedules (default) or in order."""
-        check(load().casadi_gb300_batch_set_ilp(self.id, 1 if enable else 0))
 
     def status(self):
         """Wait for the last run and raise if a unit of it failed on the device."""

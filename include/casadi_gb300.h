@@ -406,10 +406,6 @@ CASADI_GB300_API int casadi_gb300_batch_scratch_size(int batch, size_t* bytes);
 CASADI_GB300_API int casadi_gb300_batch_set_residence(int batch, int mode);
 /* Waits for the batch's stream and reports a device-side failure of its last run (a
  * direction unit whose tile's record unit did not finish within its bounded wait). */
-/* Value/record walks of the batch's units over each tape's narrow level schedule (enable,
- * the default: a warp computes up to four independent instructions before storing any) or
- * over the tape in order (0). Results are identical either way. */
-CASADI_GB300_API int casadi_gb300_batch_set_ilp(int batch, int enable);
 CASADI_GB300_API int casadi_gb300_batch_status(int batch);
 CASADI_GB300_API int casadi_gb300_batch_run(int batch, void* scratch, size_t scratch_bytes,
                            int use_graph, void* stream);

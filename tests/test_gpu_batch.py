@@ -161,25 +161,3 @@ def test_batch_residence_gives_the_same_bits(gpu_lib, mode):
             want_r, want_s = t.reverse(dargs, dseeds)
             for g, w in zip(res + asens, want_r + want_s):
                 assert same_bits(g.cpu().numpy(), w.cpu().numpy()).all()
-
-
-def test_batch_ilp_walk_gives_the_same_bits(gpu_lib):
-    """Value/record walks over the narrow level schedule (several independent instructions in
-    flight per warp) and in tape order: identical results."""
-    items = _items()
-    tapes = {}
-    outs = []
-    for ilp in (True, False):
-        b = R.Batch()
-        b.set_ilp(ilp)
-        got = []
-        for k, (f, n, nadj, args) in enumerate(items):
-            t = tapes.setdefault(id(f), R.CudaTape(f))
-            dseeds = [_cuda(s) for s in _seeds(f, n, nadj, k)] if nadj else None
-            got.append(b.add(t, [_cuda(a) for a in args], dseeds))
-        b.run(graph=True)
-        b.status()
-        outs.append([[x.cpu().numpy() for x in (res + (asens or []))] for res, asens in got])
-    for a_item, b_item in zip(*outs):
-        for x, y in zip(a_item, b_item):
-            assert same_bits(x, y).all()
