@@ -3283,3 +3283,25 @@ int casadi_gb300_mapaccum_reverse(int id, int N, int n_accum, int64_t n, int64_t
 }
 
 }  // extern "C"
+
+// ---- Self-check of the bounded waits ------------------------------------------------------
+extern "C" {
+
+int casadi_gb300_check_wait_timeout(void* stream) {
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  unsigned* words = nullptr;  // [0] a flag nothing sets, [1] the error word
+  cudaError_t e = cudaMalloc(&words, 2 * sizeof(unsigned));
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(wait probe)");
+  unsigned host[2] = {0, 0};
+  if ((e = cudaMemsetAsync(words, 0, 2 * sizeof(unsigned), s)) == cudaSuccess &&
+      (e = launch_wait_probe(words, words + 1, s)) == cudaSuccess &&
+      (e = cudaMemcpyAsync(host, words, sizeof(host), cudaMemcpyDeviceToHost, s)) == cudaSuccess)
+    e = cudaStreamSynchronize(s);
+  cudaFree(words);
+  if (e != cudaSuccess) return cuda_fail(e, "wait probe");
+  if (host[1] & kErrWaitTimeout)
+    return fail(CASADI_GB300_ERR_DEVICE, "bounded wait ran out (flag never set)");
+  return fail(CASADI_GB300_ERR_CUDA, "bounded wait did not report its timeout");
+}
+
+}  // extern "C"

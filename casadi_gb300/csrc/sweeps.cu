@@ -1372,6 +1372,15 @@ __device__ __forceinline__ bool wait_tile(const unsigned* flag, unsigned* err) {
   return ok;
 }
 
+// One warp waiting, with the batch's bounded wait, on a flag that nothing sets: the wait runs
+// out after kWaitCycles, records kErrWaitTimeout in *err and the kernel returns.
+__global__ void k_wait_probe(const unsigned* flag, unsigned* err) { wait_tile(flag, err); }
+
+cudaError_t launch_wait_probe(const unsigned* flag, unsigned* err, cudaStream_t s) {
+  k_wait_probe<<<1, 32, 0, s>>>(flag, err);
+  return cudaGetLastError();
+}
+
 // kSplit: the batch has split items (per-tile record units and per-direction units); batches
 // without any run the instance that holds only the whole-unit path. GW: the work vector lives
 // in global memory (per-CTA blocks) instead of shared memory, so residency is not capped by

@@ -163,6 +163,9 @@ cudaError_t launch_adjoint_dense(const SweepArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_sp_forward(const SweepArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_sp_reverse(const SweepArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_activity(const SweepArgs& a, int grid, cudaStream_t s);
+// The persistent batch's bounded wait on flag (nonzero: ready); a timeout ORs kErrWaitTimeout
+// into *err (one warp).
+cudaError_t launch_wait_probe(const unsigned* flag, unsigned* err, cudaStream_t s);
 // Cooperative value (record = false) or record sweep: a.block threads (a multiple of 32, at
 // most kCoopMaxThreads) share one 32-instance tile and run its level schedule; the work vector
 // in shared memory (lv_sz_w x 32 doubles), or in a.wglob blocks when set.

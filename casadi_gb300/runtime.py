@@ -115,6 +115,7 @@ def load(path=None):
         "casadi_gb300_batch_scratch_size": (cint, [cint, vp]),
         "casadi_gb300_batch_status": (cint, [cint]),
         "casadi_gb300_batch_set_residence": (cint, [cint, cint]),
+        "casadi_gb300_check_wait_timeout": (cint, [vp]),
         "casadi_gb300_batch_add_jacobian_colored": (cint, [cint, cint, i64, i64, cint, vp, vp, vp,
                                                            vp]),
         "casadi_gb300_batch_run": (cint, [cint, vp, sz, cint, vp]),

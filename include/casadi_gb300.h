@@ -436,6 +436,13 @@ CASADI_GB300_API int casadi_gb300_reverse_noalloc(int id, int64_t n, int64_t ld,
 CASADI_GB300_API int casadi_gb300_profile(int enable);
 CASADI_GB300_API int casadi_gb300_profile_collect(double* ms, int* launches, int count);
 
+/* Self-check of the device-side failure path: one warp runs the persistent batch's bounded
+ * wait on a flag that nothing sets. The wait gives up after about a second, the kernel records
+ * the timeout in its error word and returns, and this call reports it as
+ * CASADI_GB300_ERR_DEVICE ("bounded wait ran out"); the CUDA context stays usable. Any other
+ * result is an error of the failure path itself. */
+CASADI_GB300_API int casadi_gb300_check_wait_timeout(void* stream);
+
 #ifdef __cplusplus
 }
 #endif
