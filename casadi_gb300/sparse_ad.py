@@ -167,3 +167,73 @@ class ColoredHessian(_Compressed):
         color = K.star_coloring(self.pattern)
         self.rows, self.cols, idx = K.hessian_recovery(self.pattern, color)
         self._setup(tape, 0, wrt, color, idx)
+
+
+class KKT:
+    """The KKT Function of an NLP, ``Nlpsol::kkt()`` (casadi/core/nlpsol.cpp:936-954):
+    ``(x, p, lam_f, lam_g) -> (jac:g:x, hess:gamma:x:x)`` with the Lagrangian
+    ``gamma = lam_f*f + lam_g'g``, evaluated over many scenarios by colour-compressed sweeps
+    (:class:`ColoredJacobian` of g, :class:`ColoredHessian` of gamma).
+
+    ``x``, ``p`` are lists of SX symbols, ``f`` an SX scalar, ``g`` a list of SX. Values come
+    back as device tensors: the Jacobian's nonzeros (nnz_J, n) in compressed-column order of
+    :attr:`jac_pattern` (rows: constraints, columns: x), the Hessian's nonzeros (nnz_H, n) in
+    compressed-column order of the full symmetric :attr:`hess_pattern` (both triangles; the
+    upper one mirrored from the lower on the device)."""
+
+    def __init__(self, x, p, f, g, name="nlp"):
+        import torch
+        x, p, g = list(x), list(p), list(g)
+        lam_f = S.sym("lam_f")
+        lam_g = S.sym("lam_g", len(g))
+        gamma = lam_f * f
+        for li, gi in zip(lam_g, g):
+            gamma = gamma + li * gi
+        inputs = [x, p, [lam_f], lam_g]
+        self.g_function = S.Function(name + "_g", inputs, [g])
+        self.gamma_function = S.Function(name + "_gamma", inputs, [[gamma]])
+        self.jac = ColoredJacobian(self.g_function, out=0, wrt=0)
+        self.hess = ColoredHessian(self.gamma_function, out=0, wrt=0)
+        self.jac_pattern = self.jac.pattern
+        h = self.hess
+        nx = len(x)
+        mask = np.zeros((nx, nx), dtype=bool)
+        mask[h.rows, h.cols] = True
+        mask[h.cols, h.rows] = True
+        self.hess_pattern = K.Pattern.from_dense(mask)
+        lower = {(int(i), int(j)): k for k, (i, j) in enumerate(zip(h.rows, h.cols))}
+        rows, cols = self.hess_pattern.row, self.hess_pattern.col()
+        mirror = [lower[(max(int(i), int(j)), min(int(i), int(j)))] for i, j in zip(rows, cols)]
+        self._mirror = torch.tensor(mirror, dtype=torch.int64).cuda()
+
+    def _full(self, lower, n, stream=None):
+        import torch
+        vals = torch.empty((self._mirror.numel(), n), dtype=torch.float64, device="cuda")
+        R.check(R.load().casadi_gb300_gather(
+            n, n, self._mirror.numel(), ct.c_void_p(self._mirror.data_ptr()),
+            ct.c_void_p(lower.data_ptr()), ct.c_void_p(vals.data_ptr()),
+            R._stream_handle(stream)))
+        return vals
+
+    def __call__(self, args, n=None, stream=None):
+        """args: [x, p, lam_f, lam_g] as (nnz, n) device tensors; returns (jac, hess)."""
+        n = R.CudaTape._n(args) if n is None else n
+        jac = self.jac(args, n, stream=stream)
+        hess = self._full(self.hess(args, n, stream=stream), n, stream)
+        return jac, hess
+
+    def batched(self, args, n=None):
+        """Both coloured sweeps as items of one persistent batch replayed from a CUDA graph;
+        returns a function that runs it and returns (jac, hess)."""
+        n = R.CudaTape._n(args) if n is None else n
+        b = R.Batch()
+        cj = self.jac.add_to_batch(b, args, n)
+        ch = self.hess.add_to_batch(b, args, n)
+
+        def run(stream=None):
+            b.run(graph=True, stream=stream)
+            return self.jac.gather(cj, n, stream=stream), self._full(
+                self.hess.gather(ch, n, stream=stream), n, stream)
+
+        run.batch = b
+        return run

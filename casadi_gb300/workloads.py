@@ -178,15 +178,14 @@ def quad_ms_constraints(intervals=100):
     return S.Function("g", L.inputs, [L.outputs[0]])
 
 
-def quad_ms_lagrangian(intervals=100):
-    """Multiple-shooting NLP pieces: decision vector w = (x_0, u_0, ..., x_{K-1}, u_{K-1},
-    x_K) with 12 + 4 variables per interval, constraints g_k = F(x_k, u_k) - x_{k+1}
-    (and x_0 - x0bar), objective sum ||x_k||^2 + 0.1 ||u_k||^2.
-    Returns Function ``L(w, lam, x0bar) -> (g, lagrangian)``."""
+def quad_ms_nlp(intervals=100):
+    """The multiple-shooting NLP as SX expressions: decision vector w = (x_0, u_0, ...,
+    x_{K-1}, u_{K-1}, x_K) with 12 + 4 variables per interval, parameter x0bar (initial
+    state), constraints g_k = F(x_k, u_k) - x_{k+1} (and x_0 - x0bar), objective
+    sum ||x_k||^2 + 0.1 ||u_k||^2. Returns ``(w, x0bar, objective, g)``."""
     nx, nu = 12, 4
     K = intervals
     w = S.sym("w", K * (nx + nu) + nx)
-    lam = S.sym("lam", (K + 1) * nx)
     x0bar = S.sym("x0", nx)
     xs = [w[k * (nx + nu): k * (nx + nu) + nx] for k in range(K + 1)]
     us = [w[k * (nx + nu) + nx: k * (nx + nu) + nx + nu] for k in range(K)]
@@ -197,6 +196,14 @@ def quad_ms_lagrangian(intervals=100):
         g += [xn[i] - xs[k + 1][i] for i in range(nx)]
         obj = obj + sum((xi * xi for xi in xs[k]), S.const(0.0)) + \
             0.1 * sum((ui * ui for ui in us[k]), S.const(0.0))
+    return w, x0bar, obj, g
+
+
+def quad_ms_lagrangian(intervals=100):
+    """The Lagrangian of :func:`quad_ms_nlp` with multipliers lam (one per constraint):
+    Function ``L(w, lam, x0bar) -> (g, objective + lam'g)``."""
+    w, x0bar, obj, g = quad_ms_nlp(intervals)
+    lam = S.sym("lam", len(g))
     lag = obj
     for i, gi in enumerate(g):
         lag = lag + lam[i] * gi

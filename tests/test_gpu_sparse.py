@@ -135,3 +135,39 @@ def test_jacobian_pattern_forward_equals_reverse(gpu_lib):
         pa = jacobian_pattern(ct, out, 0)
         assert np.array_equal(pa.dense(), pf.dense())
         ct.sync()
+
+
+def test_kkt_function_of_the_nlp(gpu_lib):
+    """Nlpsol::kkt(): the constraint Jacobian and the full symmetric Lagrangian Hessian (upper
+    triangle mirrored on the device) of the multiple-shooting NLP, against the oracle's dense
+    derivatives; the batched graph gives the same bits as the separate calls."""
+    from casadi_gb300.sparse_ad import KKT
+    w, x0bar, obj, g = W.quad_ms_nlp(INTERVALS)
+    kkt = KKT(w, x0bar, obj, g)
+    n = 129
+    rng = np.random.default_rng(6)
+    ww, _, xb = _inputs(n, 6)
+    lam_f = rng.uniform(0.5, 2.0, (1, n))
+    lam_g = rng.standard_normal((len(g), n))
+    args_h = [ww, xb, lam_f, lam_g]
+    args = [torch.from_numpy(a).cuda() for a in args_h]
+    jac, hess = [t.cpu().numpy() for t in kkt(args)]
+    nw = len(w)
+    # Jacobian of g against the oracle's dense Jacobian
+    _, gj = O.jacobian(kkt.g_function.tape, args_h, n)
+    rows, cols = kkt.jac_pattern.row, kkt.jac_pattern.col()
+    assert_close(jac, gj[0][cols, rows], "jac:g:x", rtol=RTOL)
+    # Hessian: symmetric bit for bit, and the oracle's Jacobian of the symbolic gradient
+    hp = kkt.hess_pattern
+    hr, hc = hp.row, hp.col()
+    full = {(int(i), int(j)): k for k, (i, j) in enumerate(zip(hr, hc))}
+    for k, (i, j) in enumerate(zip(hr, hc)):
+        assert same_bits(hess[k], hess[full[(int(j), int(i))]]).all()
+    _, hj = O.jacobian(kkt.hess.gradient_function.tape, args_h, n)
+    assert_close(hess, hj[0][:nw][hc, hr], "hess:gamma:x:x", rtol=1e-12)
+    # the batched graph
+    run = kkt.batched(args)
+    for _ in range(2):
+        bj, bh = run()
+        run.batch.status()
+        assert same_bits(bj.cpu().numpy(), jac).all() and same_bits(bh.cpu().numpy(), hess).all()
