@@ -2113,1195 +2113,8 @@ int casadi_gb300_map_jacobian_reverse(int id, int mem, int64_t n, const double* 
 
 }  // extern "C"
 
-// ---------------------------------------------------------------------------------------------
-// Allocation-free adjoint sweep.
-//
-// Some callers cannot allocate device memory at the point where they need derivatives: a
-// solver running inside a CUDA graph capture, a real-time control loop that forbids
-// allocation after start-up, or a plugin hosted by a framework that owns the device
-// allocator. casadi_gb300_reverse_noalloc serves them: its partials scratch is the file-scope
-// device array below, a fixed 64 MiB that every GPU which loads this library holds until the
-// process exits. It runs the record sweep and the plan-free adjoint variant, so it makes no
-// device allocation of any kind, and it needs no host allocation either.
-// ---------------------------------------------------------------------------------------------
-namespace {
-
-constexpr size_t kNoAllocScratchBytes = 64ull << 20;
-constexpr int kNoAllocMaxDevices = 64;
-
-__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
-
-std::mutex g_noalloc_mtx;
-void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
-
-// Device address of g_noalloc_scratch on the current device. In host code the symbol's name
-// is only a handle, so the address is looked up once per device, with that device current.
-int noalloc_scratch(void** ptr) {
-  int dev = -1;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
-  if (dev < 0 || dev >= kNoAllocMaxDevices)
-    return fail(CASADI_GB300_ERR_UNSUPPORTED, "device %d is beyond the %d supported", dev,
-                kNoAllocMaxDevices);
-  std::lock_guard<std::mutex> lk(g_noalloc_mtx);
-  if (!g_noalloc_ptr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(scratch)");
-    g_noalloc_ptr[dev] = p;
-  }
-  *ptr = g_noalloc_ptr[dev];
-  return 0;
-}
-
-// Launch shape of the plan-free adjoint: the most resident warps that fit, as dir_shape
-// chooses, computed without touching the tape's shape cache.
-DirShape noalloc_shape(const Tape& t, int ndir) {
-  const int max_smem = max_smem_optin();
-  DirShape best;
-  double best_score = -1;
-  for (int ch : {64, 32, 16}) {
-    for (int dw : {8, 6, 4, 2, 1}) {
-      if (dw > 1 && dw >= 2 * ndir) continue;
-      const size_t sm = smem_dir(t.sz_w, dw, ch);
-      if (sm > static_cast<size_t>(max_smem)) continue;
-      const int occ = occupancy_dense(dw, sm);
-      if (occ <= 0) continue;
-      const int groups = (ndir + dw - 1) / dw;
-      const double used = static_cast<double>(ndir) / (groups * dw);
-      const double score = std::min(occ * dw, 8) * used * (1.0 + 0.01 * ch);
-      if (score > best_score) {
-        best_score = score;
-        best.dw = dw;
-        best.ch = ch;
-        best.blocks_per_sm = occ;
-      }
-    }
-  }
-  return best;
-}
-
-}  // namespace
-
-extern "C" {
-
-int casadi_gb300_reverse_noalloc(int id, int64_t n, int64_t ld, int nadj,
-                                 const double* const* arg, double* const* res,
-                                 const double* const* aseed, double* const* asens, void* stream) {
-  Tape* t = get_tape(id);
-  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
-  if (int rc = check_device(*t)) return rc;
-  if (int rc = check_n(n, ld)) return rc;
-  if (nadj < 0 || nadj > 65535) return fail(CASADI_GB300_ERR_ARG, "bad direction count %d", nadj);
-  if (n == 0) return 0;
-  const unsigned long long need =
-      8ull * 32ull * static_cast<unsigned long long>(t->n_partials) *
-      static_cast<unsigned long long>((n + 31) / 32);
-  if (need > kNoAllocScratchBytes)
-    return fail(CASADI_GB300_ERR_SCRATCH,
-                "allocation-free adjoint: %lld instances need %llu bytes of scratch, above its "
-                "fixed %zu bytes; split the call or use casadi_gb300_reverse",
-                static_cast<long long>(n), need, kNoAllocScratchBytes);
-  void* scratch = nullptr;
-  if (int rc = noalloc_scratch(&scratch)) return rc;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  SweepArgs a = base_args(*t, n, 0);
-  a.partials = static_cast<double*>(scratch);
-  a.pofs = t->d_pofs;
-  a.n_code = t->n_chunks * kChunk;
-  a.ndir = nadj;
-  fill_io(a.in, t->n_in, vptrs(arg), t->nnz_in, ld, false);
-  fill_io(a.out, t->n_out, vptrs(res), t->nnz_out, ld, false);
-  a.block = t->primal_block;
-  cudaError_t e = launch_record(a, grid_for((n + a.block - 1) / a.block, t->primal_grid_cap), s);
-  if (e != cudaSuccess) return cuda_fail(e, "record sweep launch");
-  if (nadj == 0) return 0;
-  fill_io(a.seed, t->n_out, vptrs(aseed), t->nnz_out, ld, true);
-  fill_io(a.sens, t->n_in, vptrs(asens), t->nnz_in, ld, true);
-  const DirShape ds = noalloc_shape(*t, nadj);
-  const int groups = (nadj + ds.dw - 1) / ds.dw;
-  a.block = 32 * ds.dw;
-  a.chunk = ds.ch;
-  const long long tiles = (n + 31) / 32;
-  const long long per_group = std::max<long long>(
-      1, std::min<long long>(tiles, static_cast<long long>(sm_count()) * ds.blocks_per_sm / groups));
-  e = launch_adjoint_dense(a, static_cast<int>(per_group * groups), s);
-  if (e != cudaSuccess) return cuda_fail(e, "adjoint launch");
-  return 0;
-}
-
-}  // extern "C"
-
-// ---------------------------------------------------------------------------------------------
-// Persistent multi-tape batches.
-// ---------------------------------------------------------------------------------------------
-namespace {
-
-struct BatchHost {
-  struct Item {
-    int tape;
-    long long n;
-    int ndir;
-    bool forward = false;
-    std::vector<int> dirmap;  // forward items: direction of each flat input nonzero (-1: none)
-    std::vector<IoDesc> io;   // 4*kMaxIo
-  };
-  std::vector<Item> items;
-  bool dirty = true;
-  // device side, rebuilt when dirty
-  BatchItem* d_items = nullptr;
-  IoDesc* d_io = nullptr;
-  int4* d_units = nullptr;
-  unsigned* d_counter = nullptr;  // [0] next unit, [1] error bits
-  unsigned* d_flags = nullptr;    // tile flags of split items
-  size_t n_flags = 0;
-  std::vector<double*> d_tile_partials;  // per split item
-  // split items whose record sweep runs as a cooperative level sweep before the persistent
-  // launch (few tiles: the per-tile record units would leave the GPU idle), their flags set
-  // once it is done
-  struct PreRecord {
-    int item;
-    size_t flag0;
-    long long tiles;
-    double* partials;
-  };
-  std::vector<PreRecord> pre;
-  int n_units = 0;
-  int szw = 1, pmax = 0, grid = 1;
-  size_t smem = 0;
-  // work-vector residence: 0 shared memory, 1 global memory (grid_gw CTAs), -1 not tuned yet
-  int residence = -1;
-  int forced = 0;  // 0 tune, 1 global memory, 2 shared memory
-  int grid_gw = 1;
-  unsigned char* d_gw = nullptr;
-  int device = 0;
-  cudaStream_t stream = nullptr;  // owned: graph capture needs a non-legacy stream
-  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  void* exec_scratch = nullptr;
-  ~BatchHost() {
-    if (exec) cudaGraphExecDestroy(exec);
-    cudaFree(d_items);
-    cudaFree(d_io);
-    cudaFree(d_units);
-    cudaFree(d_counter);
-    cudaFree(d_flags);
-    cudaFree(d_gw);
-    for (double* p : d_tile_partials) cudaFree(p);
-    if (ev_in) cudaEventDestroy(ev_in);
-    if (ev_out) cudaEventDestroy(ev_out);
-    if (stream) cudaStreamDestroy(stream);
-  }
-};
-
-std::vector<std::unique_ptr<BatchHost>> g_batches;
-
-BatchHost* get_batch(int id) {
-  std::lock_guard<std::mutex> lk(g_mtx);
-  if (id < 0 || id >= static_cast<int>(g_batches.size()) || !g_batches[id]) return nullptr;
-  return g_batches[id].get();
-}
-
-// Build items, the longest-first unit list and the launch shape.
-int batch_prepare(BatchHost& b) {
-  if (!b.dirty) return 0;
-  if (b.exec) {
-    cudaGraphExecDestroy(b.exec);
-    b.exec = nullptr;
-  }
-  cudaFree(b.d_items);
-  cudaFree(b.d_io);
-  cudaFree(b.d_units);
-  cudaFree(b.d_flags);
-  for (double* p : b.d_tile_partials) cudaFree(p);
-  b.d_tile_partials.clear();
-  b.d_items = nullptr;
-  b.d_io = nullptr;
-  b.d_units = nullptr;
-  b.d_flags = nullptr;
-  std::vector<BatchItem> items;
-  std::vector<IoDesc> io;
-  // (cost, unit): record and whole units first (longest first), then direction units
-  std::vector<std::pair<double, int4>> units, dir_units;
-  std::vector<std::pair<size_t, size_t>> flag_off;  // (item, first flag) of split items
-  size_t n_flags = 0;
-  b.pre.clear();
-  b.szw = 1;
-  b.pmax = 0;
-  for (size_t k = 0; k < b.items.size(); ++k) {
-    const auto& it = b.items[k];
-    Tape* t = get_tape(it.tape);
-    if (!t) return fail(CASADI_GB300_ERR_ID, "batch item %zu: tape %d is gone", k, it.tape);
-    BatchItem bi;
-    std::memset(&bi, 0, sizeof(bi));
-    bi.t = t->view();
-    bi.n_code = t->n_chunks * kChunk;
-    bi.ndir = it.ndir;
-    bi.n = it.n;
-    bi.forward = it.forward ? 1 : 0;
-    if (it.ndir > 0 && it.forward) {
-      if (static_cast<unsigned>(t->n_partials) >= kMaxPartials)
-        return fail(CASADI_GB300_ERR_UNSUPPORTED, "batch item %zu records too many partials", k);
-      int err = 0;
-      const TanPlan* tp = tan_plan(*t, it.ndir, 1, 0, true, std::vector<char>(t->n_in, 0),
-                                   it.dirmap, &err);
-      if (!tp) return err;
-      bi.tan_stream = tp->d_stream;
-      bi.tan_chunks = tp->d_chunks;
-    } else if (it.ndir > 0) {
-      if (static_cast<unsigned>(t->n_partials) >= kMaxPartials)
-        return fail(CASADI_GB300_ERR_UNSUPPORTED, "batch item %zu records too many partials", k);
-      std::vector<char> seeded(t->n_out);
-      for (int j = 0; j < t->n_out; ++j) seeded[j] = it.io[2 * kMaxIo + j].ptr != nullptr;
-      int err = 0;
-      const AdjPlan* ap = adj_plan(*t, 1, 0, seeded, &err);
-      if (!ap) return err;
-      int2 se;
-      cudaError_t e = cudaMemcpy(&se, ap->d_chunks, sizeof(int2), cudaMemcpyDeviceToHost);
-      if (e != cudaSuccess) return cuda_fail(e, "read adjoint plan");
-      bi.adj_stream = ap->d_stream + se.x;
-      bi.adj_ngr = se.y / kBatchGroup;
-      bi.zero_in = ap->d_zero;
-      bi.n_zero = ap->n_zero;
-    }
-    b.szw = std::max(b.szw, t->sz_w);
-    const long long tiles = (it.n + 31) / 32;
-    if (it.ndir >= 2) {
-      // split: one record unit per tile into the item's own partial buffer, then one unit
-      // per (tile, direction), so the directions of a tile run on different SMs
-      double* tp = nullptr;
-      const size_t bytes = static_cast<size_t>(tiles) * t->n_partials * 32 * sizeof(double);
-      cudaError_t e = cudaMalloc(&tp, std::max<size_t>(bytes, 8));
-      if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(batch tile partials)");
-      b.d_tile_partials.push_back(tp);
-      bi.tile_partials = tp;
-      flag_off.push_back({k, n_flags});
-      std::vector<int2> se(it.forward ? it.ndir : 1);
-      if (it.forward &&
-          (e = cudaMemcpy(se.data(), bi.tan_chunks, sizeof(int2) * it.ndir,
-                          cudaMemcpyDeviceToHost)) != cudaSuccess)
-        return cuda_fail(e, "read tangent plan");
-      // few tiles: the record sweep runs cooperatively (several warps per tile) before the
-      // persistent launch instead of as one-warp record units
-      const bool pre = tiles <= 4ll * sm_count() && ensure_levels(*t) &&
-                       smem_coop(t->lv_sz_w) <= static_cast<size_t>(max_smem_optin());
-      if (pre) {
-        b.pre.push_back({static_cast<int>(k), n_flags, tiles, tp});
-        bi.t = t->view();
-      }
-      for (long long tile = 0; tile < tiles; ++tile) {
-        if (!pre)
-          units.push_back({static_cast<double>(t->n_instr),
-                           make_int4(static_cast<int>(k), static_cast<int>(tile), -1, 0)});
-        for (int d = 0; d < it.ndir; ++d) {
-          const double len = it.forward ? se[d].y : bi.adj_ngr * kBatchGroup;
-          dir_units.push_back({len, make_int4(static_cast<int>(k), static_cast<int>(tile), d, 0)});
-        }
-      }
-      n_flags += static_cast<size_t>(tiles);
-    } else {
-      // whole units: value sweep plus the (at most one) direction in one warp
-      const double cost = static_cast<double>(t->n_instr) * (1 + it.ndir);
-      for (long long tile = 0; tile < tiles; ++tile)
-        units.push_back({cost, make_int4(static_cast<int>(k), static_cast<int>(tile), -1, 0)});
-      if (it.ndir > 0) b.pmax = std::max(b.pmax, t->n_partials);
-    }
-    items.push_back(bi);
-    io.insert(io.end(), it.io.begin(), it.io.end());
-  }
-  auto longest_first = [](const std::pair<double, int4>& x, const std::pair<double, int4>& y) {
-    return x.first > y.first;
-  };
-  std::stable_sort(units.begin(), units.end(), longest_first);
-  std::stable_sort(dir_units.begin(), dir_units.end(), longest_first);
-  std::vector<int4> ulist;
-  ulist.reserve(units.size() + dir_units.size());
-  for (const auto& u : units) ulist.push_back(u.second);
-  for (const auto& u : dir_units) ulist.push_back(u.second);
-  cudaError_t e;
-  if (n_flags && (e = cudaMalloc(&b.d_flags, n_flags * sizeof(unsigned))) != cudaSuccess)
-    return cuda_fail(e, "cudaMalloc(batch flags)");
-  b.n_flags = n_flags;
-  for (const auto& fo : flag_off) items[fo.first].ready = b.d_flags + fo.second;
-  if ((e = upload(&b.d_io, io)) != cudaSuccess) return cuda_fail(e, "upload batch I/O");
-  for (size_t k = 0; k < items.size(); ++k) items[k].io = b.d_io + k * 4 * kMaxIo;
-  if ((e = upload(&b.d_items, items)) != cudaSuccess || (e = upload(&b.d_units, ulist)) != cudaSuccess)
-    return cuda_fail(e, "upload batch");
-  if (!b.d_counter && (e = cudaMalloc(&b.d_counter, 2 * sizeof(unsigned))) != cudaSuccess)
-    return cuda_fail(e, "cudaMalloc(counter)");
-  b.n_units = static_cast<int>(ulist.size());
-  b.smem = static_cast<size_t>(b.szw) * 256;
-  const int occ = b.smem <= static_cast<size_t>(max_smem_optin())
-                      ? std::max(1, occupancy_batch(b.smem, b.n_flags > 0, false))
-                      : 1;
-  b.grid = std::max(1, std::min(sm_count() * occ, std::max(1, b.n_units)));
-  // global-memory work vectors: residency capped by registers (and at 8 CTAs per SM, which
-  // bounds the per-CTA partial scratch the caller provides)
-  const int occ_gw = std::max(1, std::min(8, occupancy_batch(0, b.n_flags > 0, true)));
-  b.grid_gw = std::max(1, std::min(sm_count() * occ_gw, std::max(1, b.n_units)));
-  cudaFree(b.d_gw);
-  b.d_gw = nullptr;
-  const size_t gw_bytes = static_cast<size_t>(b.grid_gw) * b.szw * 256;
-  if ((e = cudaMalloc(&b.d_gw, std::max<size_t>(gw_bytes, 256))) != cudaSuccess)
-    return cuda_fail(e, "cudaMalloc(batch work vectors)");
-  b.residence = b.forced == 1 ? 1 : (b.forced == 2 ? 0 : -1);
-  b.dirty = false;
-  return 0;
-}
-
-int batch_enqueue(BatchHost& b, void* scratch, cudaStream_t s, bool gw) {
-  cudaError_t e = cudaMemsetAsync(b.d_counter, 0, 2 * sizeof(unsigned), s);
-  if (e == cudaSuccess && b.n_flags)
-    e = cudaMemsetAsync(b.d_flags, 0, b.n_flags * sizeof(unsigned), s);
-  if (e != cudaSuccess) return cuda_fail(e, "reset batch counter");
-  for (const auto& pr : b.pre) {
-    const auto& it = b.items[pr.item];
-    Tape* t = get_tape(it.tape);
-    if (!t) return fail(CASADI_GB300_ERR_ID, "batch item %d: tape %d is gone", pr.item, it.tape);
-    SweepArgs a = base_args(*t, it.n, 0);
-    for (int j = 0; j < t->n_in; ++j) a.in[j] = it.io[j];
-    for (int j = 0; j < t->n_out; ++j) a.out[j] = it.io[kMaxIo + j];
-    a.partials = pr.partials;
-    a.block = coop_threads_for(pr.tiles);
-    const size_t sm = smem_coop(t->lv_sz_w);
-    const int occ = std::max(1, occupancy_coop(a.block, sm, false));
-    const int grid = static_cast<int>(std::min<long long>(pr.tiles, 1ll * occ * sm_count()));
-    if ((e = launch_coop(a, true, grid, s)) != cudaSuccess) return cuda_fail(e, "batch record");
-    // every tile of the item is recorded: its direction units need not wait
-    if ((e = cudaMemsetAsync(b.d_flags + pr.flag0, 0xff, pr.tiles * sizeof(unsigned), s)) !=
-        cudaSuccess)
-      return cuda_fail(e, "batch flags");
-  }
-  BatchArgs a;
-  a.items = b.d_items;
-  a.units = b.d_units;
-  a.n_units = b.n_units;
-  a.counter = b.d_counter;
-  a.err = b.d_counter + 1;
-  a.scratch = static_cast<double*>(scratch);
-  a.scratch_stride = static_cast<long long>(b.pmax) * 32;
-  a.wglob = gw ? b.d_gw : nullptr;
-  a.wglob_stride = static_cast<long long>(b.szw) * 256;
-  e = launch_batch(a, gw ? b.grid_gw : b.grid, b.smem, b.n_flags > 0, gw, s);
-  if (e != cudaSuccess) return cuda_fail(e, "batch launch");
-  return 0;
-}
-
-}  // namespace
-
-extern "C" {
-
-int casadi_gb300_batch_create(void) {
-  auto b = std::make_unique<BatchHost>();
-  cudaError_t e = cudaGetDevice(&b->device);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
-  if ((e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess ||
-      (e = cudaEventCreateWithFlags(&b->ev_in, cudaEventDisableTiming)) != cudaSuccess ||
-      (e = cudaEventCreateWithFlags(&b->ev_out, cudaEventDisableTiming)) != cudaSuccess)
-    return cuda_fail(e, "batch stream");
-  std::lock_guard<std::mutex> lk(g_mtx);
-  g_batches.push_back(std::move(b));
-  return static_cast<int>(g_batches.size()) - 1;
-}
-
-int casadi_gb300_batch_free(int batch) {
-  std::lock_guard<std::mutex> lk(g_mtx);
-  if (batch < 0 || batch >= static_cast<int>(g_batches.size()) || !g_batches[batch])
-    return fail(CASADI_GB300_ERR_ID, "no batch %d", batch);
-  g_batches[batch].reset();
-  return 0;
-}
-
-int casadi_gb300_batch_add(int batch, int id, int64_t n, int64_t ld, int nadj,
-                           const double* const* arg, double* const* res,
-                           const double* const* aseed, double* const* asens) {
-  BatchHost* b = get_batch(batch);
-  if (!b) return fail(CASADI_GB300_ERR_ID, "no batch %d", batch);
-  Tape* t = get_tape(id);
-  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
-  if (int rc = check_device(*t)) return rc;
-  if (int rc = check_n(n, ld)) return rc;
-  if (nadj < 0 || nadj > 65535) return fail(CASADI_GB300_ERR_ARG, "bad direction count %d", nadj);
-  if (n > (1ll << 36)) return fail(CASADI_GB300_ERR_ARG, "too many instances");
-  BatchHost::Item it;
-  it.tape = id;
-  it.n = n;
-  it.ndir = nadj;
-  it.io.assign(4 * kMaxIo, IoDesc{nullptr, 0, 0, 0});
-  fill_io(it.io.data(), t->n_in, vptrs(arg), t->nnz_in, ld, false);
-  fill_io(it.io.data() + kMaxIo, t->n_out, vptrs(res), t->nnz_out, ld, false);
-  if (nadj > 0) {
-    fill_io(it.io.data() + 2 * kMaxIo, t->n_out, vptrs(aseed), t->nnz_out, ld, true);
-    fill_io(it.io.data() + 3 * kMaxIo, t->n_in, vptrs(asens), t->nnz_in, ld, true);
-  }
-  b->items.push_back(std::move(it));
-  b->dirty = true;
-  return static_cast<int>(b->items.size()) - 1;
-}
-
-int casadi_gb300_batch_add_jacobian_colored(int batch, int id, int64_t n, int64_t ld,
-                                            int n_colors, const int* color,
-                                            const double* const* arg, double* const* res,
-                                            double* const* comp) {
-  BatchHost* b = get_batch(batch);
-  if (!b) return fail(CASADI_GB300_ERR_ID, "no batch %d", batch);
-  Tape* t = get_tape(id);
-  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
-  if (int rc = check_device(*t)) return rc;
-  if (int rc = check_n(n, ld)) return rc;
-  if (n > (1ll << 36)) return fail(CASADI_GB300_ERR_ARG, "too many instances");
-  int nz = 0;
-  for (int v : t->nnz_in) nz += v;
-  if (!color || n_colors < 1 || n_colors > nz)
-    return fail(CASADI_GB300_ERR_ARG, "bad colouring (%d colours for %d input nonzeros)",
-                n_colors, nz);
-  BatchHost::Item it;
-  it.tape = id;
-  it.n = n;
-  it.ndir = n_colors;
-  it.forward = true;
-  it.dirmap.assign(color, color + nz);
-  for (int v : it.dirmap)
-    if (v < -1 || v >= n_colors) return fail(CASADI_GB300_ERR_ARG, "colour %d out of range", v);
-  it.io.assign(4 * kMaxIo, IoDesc{nullptr, 0, 0, 0});
-  fill_io(it.io.data(), t->n_in, vptrs(arg), t->nnz_in, ld, false);
-  fill_io(it.io.data() + kMaxIo, t->n_out, vptrs(res), t->nnz_out, ld, false);
-  fill_io(it.io.data() + 3 * kMaxIo, t->n_out, vptrs(comp), t->nnz_out, ld, true);
-  b->items.push_back(std::move(it));
-  b->dirty = true;
-  return static_cast<int>(b->items.size()) - 1;
-}
-
-int casadi_gb300_batch_set_residence(int batch, int mode) {
-  BatchHost* b = get_batch(batch);
-  if (!b) return fail(CASADI_GB300_ERR_ID, "no batch %d", batch);
-  if (mode < 0 || mode > 2) return fail(CASADI_GB300_ERR_ARG, "residence must be 0, 1 or 2");
-  b->forced = mode;
-  b->residence = mode == 1 ? 1 : (mode == 2 ? 0 : -1);
-  if (b->exec) {
-    cudaGraphExecDestroy(b->exec);
-    b->exec = nullptr;
-  }
-  return 0;
-}
-
-int casadi_gb300_batch_status(int batch) {
-  BatchHost* b = get_batch(batch);
-  if (!b) return fail(CASADI_GB300_ERR_ID, "no batch %d", batch);
-  if (!b->d_counter) return 0;
-  unsigned w[2] = {0, 0};
-  cudaError_t e = cudaStreamSynchronize(b->stream);
-  if (e == cudaSuccess) e = cudaMemcpy(w, b->d_counter, sizeof(w), cudaMemcpyDeviceToHost);
-  if (e != cudaSuccess) return cuda_fail(e, "batch status");
-  if (w[1] & kErrWaitTimeout)
-    return fail(CASADI_GB300_ERR_CUDA, "batch: a direction unit timed out waiting for its tile");
-  return 0;
-}
-
-int casadi_gb300_batch_scratch_size(int batch, size_t* bytes) {
-  BatchHost* b = get_batch(batch);
-  if (!b) return fail(CASADI_GB300_ERR_ID, "no batch %d", batch);
-  if (!bytes) return fail(CASADI_GB300_ERR_ARG, "bad arguments");
-  if (int rc = batch_prepare(*b)) return rc;
-  *bytes = static_cast<size_t>(std::max(b->grid, b->grid_gw)) * b->pmax * 32 * 8;
-  return 0;
-}
-
-int casadi_gb300_batch_run(int batch, void* scratch, size_t scratch_bytes, int use_graph,
-                           void* stream) {
-  BatchHost* b = get_batch(batch);
-  if (!b) return fail(CASADI_GB300_ERR_ID, "no batch %d", batch);
-  int cur = -1;
-  cudaGetDevice(&cur);
-  if (cur != b->device) return fail(CASADI_GB300_ERR_ARG, "batch lives on device %d", b->device);
-  if (int rc = batch_prepare(*b)) return rc;
-  const size_t need = static_cast<size_t>(std::max(b->grid, b->grid_gw)) * b->pmax * 32 * 8;
-  if (need > 0 && (!scratch || scratch_bytes < need))
-    return fail(CASADI_GB300_ERR_SCRATCH, "batch needs %zu bytes of scratch, got %zu", need,
-                scratch_bytes);
-  cudaStream_t caller = static_cast<cudaStream_t>(stream);
-  // order after the caller's stream, run on the owned stream, order the caller after it
-  cudaError_t e = cudaEventRecord(b->ev_in, caller);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->ev_in, 0);
-  if (e != cudaSuccess) return cuda_fail(e, "batch ordering");
-  if (b->residence < 0) {
-    // tune the work-vector residence once per batch layout: both runs produce the results
-    if (g_autotune && !capturing(caller)) {
-      float ms[2] = {0, 0};
-      for (int gw = 0; gw < 2; ++gw) {
-        if (gw == 0 && b->smem > static_cast<size_t>(max_smem_optin())) {
-          ms[0] = 3.0e38f;  // the shared-memory instance cannot hold this batch
-          continue;
-        }
-        int rc = 0;
-        if (int trc = time_once(b->stream, [&] {
-              rc = batch_enqueue(*b, scratch, b->stream, gw == 1);
-              return cudaSuccess;
-            }, &ms[gw]))
-          return trc;
-        if (rc) return rc;
-      }
-      b->residence = ms[1] < ms[0] ? 1 : 0;
-    } else {
-      b->residence = b->smem <= static_cast<size_t>(max_smem_optin()) ? 0 : 1;
-    }
-  }
-  const bool gw = b->residence == 1;
-  if (use_graph) {
-    if (b->exec && b->exec_scratch != scratch) {
-      cudaGraphExecDestroy(b->exec);
-      b->exec = nullptr;
-    }
-    if (!b->exec) {
-      cudaGraph_t g = nullptr;
-      e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
-      if (e != cudaSuccess) return cuda_fail(e, "begin capture");
-      int rc = batch_enqueue(*b, scratch, b->stream, gw);
-      e = cudaStreamEndCapture(b->stream, &g);
-      if (rc) {
-        if (g) cudaGraphDestroy(g);
-        return rc;
-      }
-      if (e != cudaSuccess) return cuda_fail(e, "end capture");
-      e = cudaGraphInstantiate(&b->exec, g, 0);
-      cudaGraphDestroy(g);
-      if (e != cudaSuccess) return cuda_fail(e, "instantiate batch graph");
-      b->exec_scratch = scratch;
-    }
-    e = timed(F_BATCH, b->stream, [&] { return cudaGraphLaunch(b->exec, b->stream); });
-    if (e != cudaSuccess) return cuda_fail(e, "graph launch");
-  } else {
-    int rc = 0;
-    e = timed(F_BATCH, b->stream, [&] {
-      rc = batch_enqueue(*b, scratch, b->stream, gw);
-      return cudaSuccess;
-    });
-    if (rc) return rc;
-  }
-  e = cudaEventRecord(b->ev_out, b->stream);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(caller, b->ev_out, 0);
-  if (e != cudaSuccess) return cuda_fail(e, "batch ordering");
-  return 0;
-}
-
-}  // extern "C"
-
-// ---- MapSum: shared inputs and instance-summed outputs (casadi/core/mapsum.cpp) -------------
-namespace {
-
-// Bump allocator over the caller's scratch (256-byte aligned regions).
-struct Arena {
-  char* p = nullptr;
-  size_t left = 0;
-  Arena(void* base, size_t bytes) {
-    const uintptr_t b = reinterpret_cast<uintptr_t>(base);
-    const uintptr_t a = (b + 255) & ~static_cast<uintptr_t>(255);
-    if (base && bytes >= a - b) {
-      p = reinterpret_cast<char*>(a);
-      left = bytes - (a - b);
-    }
-  }
-  void* take(size_t bytes) {
-    const size_t b = (bytes + 255) & ~static_cast<size_t>(255);
-    if (!p || b > left) return nullptr;
-    void* r = p;
-    p += b;
-    left -= b;
-    return r;
-  }
-};
-
-struct SumFlags {
-  bool shared[kMaxIo] = {};
-  bool summed[kMaxIo] = {};
-  int order = 0;
-};
-
-int sum_flags(const Tape& t, const casadi_gb300_mapsum_spec* spec, SumFlags* f) {
-  if (!spec) return fail(CASADI_GB300_ERR_ARG, "missing MapSum spec");
-  if (spec->order != 0 && spec->order != 1)
-    return fail(CASADI_GB300_ERR_ARG, "MapSum order must be 0 (instance order) or 1 (tree)");
-  for (int j = 0; j < t.n_in; ++j) f->shared[j] = spec->reduce_in && spec->reduce_in[j] != 0;
-  for (int j = 0; j < t.n_out; ++j) f->summed[j] = spec->reduce_out && spec->reduce_out[j] != 0;
-  f->order = spec->order;
-  return 0;
-}
-
-// An input (or seed) shared by every instance: ptr[d*nnz + k].
-IoDesc shared_io(const void* ptr, int nnz) {
-  return IoDesc{const_cast<void*>(ptr), 1, 0, static_cast<long long>(nnz)};
-}
-// Rows of n instances: ptr[(d*nnz + k)*n + i] (the per-instance values of a summed output).
-IoDesc rows_io(void* ptr, int nnz, long long n) {
-  return IoDesc{ptr, n, 1, static_cast<long long>(nnz) * n};
-}
-// The ordinary instance-minor layout with leading dimension ld.
-IoDesc plain_io(const void* ptr, int nnz, long long ld, bool dir_major) {
-  return IoDesc{const_cast<void*>(ptr), ld, 1, dir_major ? static_cast<long long>(nnz) * ld : 0};
-}
-
-template <class T>
-const void* at(T* const* p, int j) {
-  return p ? static_cast<const void*>(p[j]) : nullptr;
-}
-
-// Scratch the reductions of one call need besides the derivative sweeps: the per-instance rows
-// of every summed output (values and ndir directions) and shared input (ndir sensitivity
-// directions, or the sparsity bits), and the tree's level buffers.
-size_t sum_bytes(const Tape& t, long long n, int ndir, const SumFlags& f) {
-  const long long nd = std::max(1, ndir);
-  size_t bytes = 0;
-  long long max_rows = 0;
-  for (int j = 0; j < t.n_out; ++j) {
-    if (!f.summed[j]) continue;
-    const long long k = t.nnz_out[j];
-    bytes += ((8 * k * n + 255) / 256) * 256 + ((8 * k * nd * n + 255) / 256) * 256;
-    max_rows = std::max(max_rows, k * nd);
-  }
-  for (int j = 0; j < t.n_in; ++j) {
-    if (!f.shared[j]) continue;
-    const long long k = t.nnz_in[j];
-    bytes += ((8 * k * nd * n + 255) / 256) * 256;
-    max_rows = std::max(max_rows, k * nd);
-  }
-  return bytes + ((reduce_scratch_bytes(max_rows, n, f.order) + 255) / 256) * 256 + 256;
-}
-
-// Largest row count one reduction of the call handles (its tree buffers are reused).
-long long max_sum_rows(const Tape& t, int ndir, const SumFlags& f) {
-  const long long nd = std::max(1, ndir);
-  long long m = 0;
-  for (int j = 0; j < t.n_out; ++j)
-    if (f.summed[j]) m = std::max(m, static_cast<long long>(t.nnz_out[j]) * nd);
-  for (int j = 0; j < t.n_in; ++j)
-    if (f.shared[j]) m = std::max(m, static_cast<long long>(t.nnz_in[j]) * nd);
-  return m;
-}
-
-int scratch_short(const char* what) {
-  return fail(CASADI_GB300_ERR_SCRATCH,
-              "MapSum scratch too small for the %s (see casadi_gb300_mapsum_scratch_size)", what);
-}
-
-int take_tree(Arena& ar, const Tape& t, long long n, int ndir, const SumFlags& f, double** tree) {
-  const size_t b = reduce_scratch_bytes(max_sum_rows(t, ndir, f), n, f.order);
-  *tree = nullptr;
-  if (b == 0) return 0;
-  *tree = static_cast<double*>(ar.take(b));
-  return *tree ? 0 : scratch_short("summation tree");
-}
-
-int sum_rows(long long rows, long long n, const double* src, double* dst, int order,
-             double* tree, cudaStream_t s) {
-  cudaError_t e = reduce_sum(rows, n, src, n, dst, order, tree, s);
-  return e == cudaSuccess ? 0 : cuda_fail(e, "MapSum reduction");
-}
-
-}  // namespace
-
-extern "C" {
-
-int casadi_gb300_mapsum_scratch_size(int id, int64_t n, int ndir,
-                                     const casadi_gb300_mapsum_spec* spec, size_t* bytes) {
-  Tape* t = get_tape(id);
-  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
-  if (!bytes || n < 0 || ndir < 0) return fail(CASADI_GB300_ERR_ARG, "bad arguments");
-  SumFlags f;
-  if (int rc = sum_flags(*t, spec, &f)) return rc;
-  const size_t sweep =
-      ndir > 0 ? static_cast<size_t>(8) * t->n_partials * static_cast<size_t>(((n + 31) / 32) * 32)
-               : 0;
-  *bytes = sum_bytes(*t, n, ndir, f) + sweep + 256;
-  return 0;
-}
-
-int casadi_gb300_mapsum_eval(int id, int64_t n, int64_t ld, const casadi_gb300_mapsum_spec* spec,
-                             const double* const* arg, double* const* res, void* scratch,
-                             size_t scratch_bytes, void* stream) {
-  Tape* t = get_tape(id);
-  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
-  if (int rc = check_device(*t)) return rc;
-  if (int rc = check_n(n, ld)) return rc;
-  SumFlags f;
-  if (int rc = sum_flags(*t, spec, &f)) return rc;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  Arena ar(scratch, scratch_bytes);
-  SweepArgs a = base_args(*t, n, 0);
-  double* rows[kMaxIo] = {};
-  for (int j = 0; j < t->n_in; ++j)
-    a.in[j] = f.shared[j] ? shared_io(at(arg, j), t->nnz_in[j])
-                          : plain_io(at(arg, j), t->nnz_in[j], ld, false);
-  for (int j = 0; j < t->n_out; ++j) {
-    if (f.summed[j] && at(res, j)) {
-      rows[j] = static_cast<double*>(ar.take(8 * static_cast<size_t>(t->nnz_out[j]) * n));
-      if (!rows[j]) return scratch_short("summed outputs");
-      a.out[j] = rows_io(rows[j], t->nnz_out[j], n);
-    } else {
-      a.out[j] = plain_io(at(res, j), t->nnz_out[j], ld, false);
-    }
-  }
-  double* tree = nullptr;
-  if (int rc = take_tree(ar, *t, n, 0, f, &tree)) return rc;
-  if (n > 0)
-    if (int rc = primal_launch(*t, a, n, PK_EVAL, s)) return rc;
-  for (int j = 0; j < t->n_out; ++j)
-    if (rows[j])
-      if (int rc = sum_rows(t->nnz_out[j], n, rows[j], res[j], f.order, tree, s)) return rc;
-  return 0;
-}
-
-int casadi_gb300_mapsum_forward(int id, int64_t n, int64_t ld,
-                                const casadi_gb300_mapsum_spec* spec, int nfwd,
-                                const double* const* arg, double* const* res,
-                                const double* const* fseed, double* const* fsens, void* scratch,
-                                size_t scratch_bytes, void* stream) {
-  Tape* t = get_tape(id);
-  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
-  if (int rc = check_device(*t)) return rc;
-  if (int rc = check_n(n, ld)) return rc;
-  if (nfwd < 0 || nfwd > 65535) return fail(CASADI_GB300_ERR_ARG, "bad direction count %d", nfwd);
-  SumFlags f;
-  if (int rc = sum_flags(*t, spec, &f)) return rc;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  Arena ar(scratch, scratch_bytes);
-  IoDesc in[kMaxIo], out[kMaxIo], seed[kMaxIo], sens[kMaxIo];
-  double* rows[kMaxIo] = {};
-  double* srows[kMaxIo] = {};
-  for (int j = 0; j < t->n_in; ++j) {
-    const int k = t->nnz_in[j];
-    in[j] = f.shared[j] ? shared_io(at(arg, j), k) : plain_io(at(arg, j), k, ld, false);
-    seed[j] = f.shared[j] ? shared_io(at(fseed, j), k) : plain_io(at(fseed, j), k, ld, true);
-  }
-  for (int j = 0; j < t->n_out; ++j) {
-    const int k = t->nnz_out[j];
-    out[j] = plain_io(at(res, j), k, ld, false);
-    sens[j] = plain_io(at(fsens, j), k, ld, true);
-    if (!f.summed[j]) continue;
-    if (at(res, j)) {
-      rows[j] = static_cast<double*>(ar.take(8 * static_cast<size_t>(k) * n));
-      if (!rows[j]) return scratch_short("summed outputs");
-      out[j] = rows_io(rows[j], k, n);
-    }
-    if (at(fsens, j) && nfwd > 0) {
-      srows[j] = static_cast<double*>(ar.take(8 * static_cast<size_t>(k) * nfwd * n));
-      if (!srows[j]) return scratch_short("summed sensitivities");
-      sens[j] = rows_io(srows[j], k, n);
-    }
-  }
-  double* tree = nullptr;
-  if (int rc = take_tree(ar, *t, n, nfwd, f, &tree)) return rc;
-  if (int rc = run_ad(*t, n, in, out, seed, sens, nfwd, false, false, ar.p, ar.left, s))
-    return rc;
-  for (int j = 0; j < t->n_out; ++j) {
-    if (rows[j])
-      if (int rc = sum_rows(t->nnz_out[j], n, rows[j], res[j], f.order, tree, s)) return rc;
-    if (srows[j])
-      if (int rc = sum_rows(static_cast<long long>(t->nnz_out[j]) * nfwd, n, srows[j], fsens[j],
-                            f.order, tree, s))
-        return rc;
-  }
-  return 0;
-}
-
-int casadi_gb300_mapsum_reverse(int id, int64_t n, int64_t ld,
-                                const casadi_gb300_mapsum_spec* spec, int nadj,
-                                const double* const* arg, double* const* res,
-                                const double* const* aseed, double* const* asens, void* scratch,
-                                size_t scratch_bytes, void* stream) {
-  Tape* t = get_tape(id);
-  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
-  if (int rc = check_device(*t)) return rc;
-  if (int rc = check_n(n, ld)) return rc;
-  if (nadj < 0 || nadj > 65535) return fail(CASADI_GB300_ERR_ARG, "bad direction count %d", nadj);
-  SumFlags f;
-  if (int rc = sum_flags(*t, spec, &f)) return rc;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  Arena ar(scratch, scratch_bytes);
-  IoDesc in[kMaxIo], out[kMaxIo], seed[kMaxIo], sens[kMaxIo];
-  double* rows[kMaxIo] = {};
-  double* srows[kMaxIo] = {};
-  for (int j = 0; j < t->n_out; ++j) {
-    const int k = t->nnz_out[j];
-    out[j] = plain_io(at(res, j), k, ld, false);
-    seed[j] = f.summed[j] ? shared_io(at(aseed, j), k) : plain_io(at(aseed, j), k, ld, true);
-    if (f.summed[j] && at(res, j)) {
-      rows[j] = static_cast<double*>(ar.take(8 * static_cast<size_t>(k) * n));
-      if (!rows[j]) return scratch_short("summed outputs");
-      out[j] = rows_io(rows[j], k, n);
-    }
-  }
-  for (int j = 0; j < t->n_in; ++j) {
-    const int k = t->nnz_in[j];
-    in[j] = f.shared[j] ? shared_io(at(arg, j), k) : plain_io(at(arg, j), k, ld, false);
-    sens[j] = plain_io(at(asens, j), k, ld, true);
-    if (f.shared[j] && at(asens, j) && nadj > 0) {
-      srows[j] = static_cast<double*>(ar.take(8 * static_cast<size_t>(k) * nadj * n));
-      if (!srows[j]) return scratch_short("summed sensitivities");
-      sens[j] = rows_io(srows[j], k, n);
-    }
-  }
-  double* tree = nullptr;
-  if (int rc = take_tree(ar, *t, n, nadj, f, &tree)) return rc;
-  if (int rc = run_ad(*t, n, in, out, seed, sens, nadj, true, false, ar.p, ar.left, s)) return rc;
-  for (int j = 0; j < t->n_out; ++j)
-    if (rows[j])
-      if (int rc = sum_rows(t->nnz_out[j], n, rows[j], res[j], f.order, tree, s)) return rc;
-  for (int j = 0; j < t->n_in; ++j)
-    if (srows[j])
-      if (int rc = sum_rows(static_cast<long long>(t->nnz_in[j]) * nadj, n, srows[j], asens[j],
-                            f.order, tree, s))
-        return rc;
-  return 0;
-}
-
-int casadi_gb300_mapsum_sp_forward(int id, int64_t n, int64_t ld,
-                                   const casadi_gb300_mapsum_spec* spec,
-                                   const uint64_t* const* arg, uint64_t* const* res,
-                                   void* scratch, size_t scratch_bytes, void* stream) {
-  Tape* t = get_tape(id);
-  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
-  if (int rc = check_device(*t)) return rc;
-  if (int rc = check_n(n, ld)) return rc;
-  SumFlags f;
-  if (int rc = sum_flags(*t, spec, &f)) return rc;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  Arena ar(scratch, scratch_bytes);
-  SweepArgs a = base_args(*t, n, 0);
-  u64* rows[kMaxIo] = {};
-  for (int j = 0; j < t->n_in; ++j)
-    a.in[j] = f.shared[j] ? shared_io(at(arg, j), t->nnz_in[j])
-                          : plain_io(at(arg, j), t->nnz_in[j], ld, false);
-  for (int j = 0; j < t->n_out; ++j) {
-    if (f.summed[j] && at(res, j)) {
-      rows[j] = static_cast<u64*>(ar.take(8 * static_cast<size_t>(t->nnz_out[j]) * n));
-      if (!rows[j]) return scratch_short("summed outputs");
-      a.out[j] = rows_io(rows[j], t->nnz_out[j], n);
-    } else {
-      a.out[j] = plain_io(at(res, j), t->nnz_out[j], ld, false);
-    }
-  }
-  if (n > 0)
-    if (int rc = primal_launch(*t, a, n, PK_SP_FORWARD, s)) return rc;
-  for (int j = 0; j < t->n_out; ++j) {
-    if (!rows[j]) continue;
-    cudaError_t e = reduce_or(t->nnz_out[j], n, rows[j], n, reinterpret_cast<u64*>(res[j]), false, s);
-    if (e != cudaSuccess) return cuda_fail(e, "MapSum OR reduction");
-  }
-  return 0;
-}
-
-int casadi_gb300_mapsum_sp_reverse(int id, int64_t n, int64_t ld,
-                                   const casadi_gb300_mapsum_spec* spec, uint64_t* const* arg,
-                                   uint64_t* const* res, void* scratch, size_t scratch_bytes,
-                                   void* stream) {
-  Tape* t = get_tape(id);
-  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
-  if (int rc = check_device(*t)) return rc;
-  if (int rc = check_n(n, ld)) return rc;
-  SumFlags f;
-  if (int rc = sum_flags(*t, spec, &f)) return rc;
-  if (n == 0) return 0;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  Arena ar(scratch, scratch_bytes);
-  SweepArgs a = base_args(*t, n, 0);
-  u64* arows[kMaxIo] = {};
-  u64* srows[kMaxIo] = {};
-  cudaError_t e = cudaSuccess;
-  for (int j = 0; j < t->n_in; ++j) {
-    const int k = t->nnz_in[j];
-    a.in[j] = plain_io(at(arg, j), k, ld, false);
-    if (f.shared[j] && at(arg, j)) {
-      // every instance ORs its bits into its own row; the rows are OR-ed into arg[j] after
-      arows[j] = static_cast<u64*>(ar.take(8 * static_cast<size_t>(k) * n));
-      if (!arows[j]) return scratch_short("shared inputs");
-      if ((e = cudaMemsetAsync(arows[j], 0, 8 * static_cast<size_t>(k) * n, s)) != cudaSuccess)
-        return cuda_fail(e, "MapSum clear");
-      a.in[j] = rows_io(arows[j], k, n);
-    }
-  }
-  for (int j = 0; j < t->n_out; ++j) {
-    const int k = t->nnz_out[j];
-    a.out[j] = plain_io(at(res, j), k, ld, false);
-    if (f.summed[j] && at(res, j)) {
-      // the summed output's seed reaches every instance (MapSum restores it before each one)
-      srows[j] = static_cast<u64*>(ar.take(8 * static_cast<size_t>(k) * n));
-      if (!srows[j]) return scratch_short("summed outputs");
-      if ((e = broadcast_rows(k, n, reinterpret_cast<const u64*>(res[j]), srows[j], n, s)) !=
-          cudaSuccess)
-        return cuda_fail(e, "MapSum seed broadcast");
-      a.out[j] = rows_io(srows[j], k, n);
-    }
-  }
-  if (int rc = primal_launch(*t, a, n, PK_SP_REVERSE, s)) return rc;
-  for (int j = 0; j < t->n_in; ++j)
-    if (arows[j] && (e = reduce_or(t->nnz_in[j], n, arows[j], n,
-                                   reinterpret_cast<u64*>(arg[j]), true, s)) != cudaSuccess)
-      return cuda_fail(e, "MapSum OR reduction");
-  for (int j = 0; j < t->n_out; ++j)
-    if (srows[j] &&
-        (e = cudaMemsetAsync(res[j], 0, 8 * static_cast<size_t>(t->nnz_out[j]), s)) != cudaSuccess)
-      return cuda_fail(e, "MapSum clear");
-  return 0;
-}
-
-}  // extern "C"
-
-// ---- Mapaccum: N chained calls of one tape (Function::mapaccum, casadi/core/function.cpp) ----
-namespace {
-
-int accum_check(const Tape& t, int N, int n_accum) {
-  if (N < 1) return fail(CASADI_GB300_ERR_ARG, "mapaccum: N must be positive");
-  if (n_accum < 0 || n_accum > std::min(t.n_in, t.n_out))
-    return fail(CASADI_GB300_ERR_ARG, "mapaccum: %d accumulators for %d inputs and %d outputs",
-                n_accum, t.n_in, t.n_out);
-  for (int i = 0; i < n_accum; ++i)
-    if (t.nnz_in[i] != t.nnz_out[i])
-      return fail(CASADI_GB300_ERR_ARG,
-                  "mapaccum: accumulator %d has %d input but %d output nonzeros", i,
-                  t.nnz_in[i], t.nnz_out[i]);
-  return 0;
-}
-
-// Block k of a stacked input/output: nonzeros [k*nnz, (k+1)*nnz) of an (nnz*N, ld) array, and
-// of each direction of an (ndir, nnz*N, ld) one.
-IoDesc step_io(const void* base, int nnz, int N, int k, long long ld) {
-  if (!base) return IoDesc{nullptr, ld, 1, 0};
-  return IoDesc{const_cast<char*>(static_cast<const char*>(base)) +
-                    static_cast<size_t>(k) * nnz * ld * sizeof(double),
-                ld, 1, static_cast<long long>(nnz) * N * ld};
-}
-// A contiguous (ndir, nnz, n) block of the scratch.
-IoDesc block_io(void* p, int nnz, long long n) {
-  return IoDesc{p, n, 1, static_cast<long long>(nnz) * n};
-}
-
-size_t bytes_of(long long count) { return ((static_cast<size_t>(count) * 8 + 255) / 256) * 256; }
-
-// Accumulator values of step k-1 (the input of step k > 0): the caller's output block, or the
-// scratch copy (history: every step kept, for the reverse sweep; else two alternating blocks).
-struct AccumValues {
-  const double* const* res;
-  double* keep[kMaxIo] = {};
-  bool history = false;
-  IoDesc value(int i, int nnz, int N, int k, long long n, long long ld) const {
-    if (res && res[i]) return step_io(res[i], nnz, N, k, ld);
-    double* p = keep[i] + static_cast<size_t>(history ? k : (k & 1)) * nnz * n;
-    return IoDesc{p, n, 1, 0};
-  }
-};
-
-int accum_values(const Tape& t, int N, int n_accum, long long n, const double* const* res,
-                 bool history, Arena& ar, AccumValues* v) {
-  v->res = res;
-  v->history = history;
-  for (int i = 0; i < n_accum; ++i) {
-    if (res && res[i]) continue;
-    v->keep[i] = static_cast<double*>(
-        ar.take(bytes_of(static_cast<long long>(t.nnz_out[i]) * n * (history ? N : 2))));
-    if (!v->keep[i])
-      return fail(CASADI_GB300_ERR_SCRATCH,
-                  "mapaccum scratch too small (see casadi_gb300_mapaccum_scratch_size)");
-  }
-  return 0;
-}
-
-// The value sweep of every step: inputs of step k from arg / the previous step's outputs.
-int accum_forward_values(Tape& t, int N, int n_accum, long long n, long long ld,
-                         const double* const* arg, double* const* res, const AccumValues& v,
-                         cudaStream_t s) {
-  for (int k = 0; k < N; ++k) {
-    SweepArgs a = base_args(t, n, 0);
-    for (int j = 0; j < t.n_in; ++j) {
-      const int nz = t.nnz_in[j];
-      if (j < n_accum)
-        a.in[j] = k == 0 ? plain_io(at(arg, j), nz, ld, false) : v.value(j, nz, N, k - 1, n, ld);
-      else
-        a.in[j] = step_io(at(arg, j), nz, N, k, ld);
-    }
-    for (int j = 0; j < t.n_out; ++j)
-      a.out[j] = j < n_accum ? v.value(j, t.nnz_out[j], N, k, n, ld)
-                             : step_io(res ? res[j] : nullptr, t.nnz_out[j], N, k, ld);
-    if (int rc = primal_launch(t, a, n, PK_EVAL, s)) return rc;
-  }
-  return 0;
-}
-
-}  // namespace
-
-extern "C" {
-
-int casadi_gb300_mapaccum_scratch_size(int id, int N, int n_accum, int64_t n, int ndir,
-                                       size_t* bytes) {
-  Tape* t = get_tape(id);
-  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
-  if (!bytes || n < 0 || ndir < 0) return fail(CASADI_GB300_ERR_ARG, "bad arguments");
-  if (int rc = accum_check(*t, N, n_accum)) return rc;
-  size_t b = 512;
-  for (int i = 0; i < n_accum; ++i) {
-    const long long nz = t->nnz_out[i];
-    b += bytes_of(nz * n * std::max(N, 2));                // accumulator values
-    b += 3 * bytes_of(static_cast<long long>(std::max(ndir, 1)) * nz * n);  // tangents/adjoints
-  }
-  b += static_cast<size_t>(8) * t->n_partials * static_cast<size_t>(((n + 31) / 32) * 32);
-  *bytes = b;
-  return 0;
-}
-
-int casadi_gb300_mapaccum_eval(int id, int N, int n_accum, int64_t n, int64_t ld,
-                               const double* const* arg, double* const* res, void* scratch,
-                               size_t scratch_bytes, void* stream) {
-  Tape* t = get_tape(id);
-  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
-  if (int rc = check_device(*t)) return rc;
-  if (int rc = check_n(n, ld)) return rc;
-  if (int rc = accum_check(*t, N, n_accum)) return rc;
-  if (n == 0) return 0;
-  Arena ar(scratch, scratch_bytes);
-  AccumValues v;
-  if (int rc = accum_values(*t, N, n_accum, n, res, false, ar, &v)) return rc;
-  return accum_forward_values(*t, N, n_accum, n, ld, arg, res, v,
-                              static_cast<cudaStream_t>(stream));
-}
-
-int casadi_gb300_mapaccum_forward(int id, int N, int n_accum, int64_t n, int64_t ld, int nfwd,
-                                  const double* const* arg, double* const* res,
-                                  const double* const* fseed, double* const* fsens,
-                                  void* scratch, size_t scratch_bytes, void* stream) {
-  Tape* t = get_tape(id);
-  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
-  if (int rc = check_device(*t)) return rc;
-  if (int rc = check_n(n, ld)) return rc;
-  if (int rc = accum_check(*t, N, n_accum)) return rc;
-  if (nfwd < 1 || nfwd > 65535) return fail(CASADI_GB300_ERR_ARG, "bad direction count %d", nfwd);
-  if (n == 0) return 0;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  Arena ar(scratch, scratch_bytes);
-  AccumValues v;
-  if (int rc = accum_values(*t, N, n_accum, n, res, false, ar, &v)) return rc;
-  // accumulator tangents the caller does not keep: two alternating blocks
-  double* ttmp[kMaxIo] = {};
-  for (int i = 0; i < n_accum; ++i) {
-    if (fsens && fsens[i]) continue;
-    ttmp[i] = static_cast<double*>(ar.take(bytes_of(2ll * nfwd * t->nnz_out[i] * n)));
-    if (!ttmp[i])
-      return fail(CASADI_GB300_ERR_SCRATCH,
-                  "mapaccum scratch too small (see casadi_gb300_mapaccum_scratch_size)");
-  }
-  auto tangent = [&](int i, int k) -> IoDesc {
-    const int nz = t->nnz_out[i];
-    if (fsens && fsens[i]) return step_io(fsens[i], nz, N, k, ld);
-    return block_io(ttmp[i] + static_cast<size_t>(k & 1) * nfwd * nz * n, nz, n);
-  };
-  for (int k = 0; k < N; ++k) {
-    IoDesc in[kMaxIo], out[kMaxIo], seed[kMaxIo], sens[kMaxIo];
-    for (int j = 0; j < t->n_in; ++j) {
-      const int nz = t->nnz_in[j];
-      if (j < n_accum) {
-        in[j] = k == 0 ? plain_io(at(arg, j), nz, ld, false) : v.value(j, nz, N, k - 1, n, ld);
-        seed[j] = k == 0 ? plain_io(at(fseed, j), nz, ld, true) : tangent(j, k - 1);
-      } else {
-        in[j] = step_io(at(arg, j), nz, N, k, ld);
-        seed[j] = step_io(at(fseed, j), nz, N, k, ld);
-      }
-    }
-    for (int j = 0; j < t->n_out; ++j) {
-      const int nz = t->nnz_out[j];
-      out[j] = j < n_accum ? v.value(j, nz, N, k, n, ld)
-                           : step_io(res ? res[j] : nullptr, nz, N, k, ld);
-      sens[j] = j < n_accum ? tangent(j, k) : step_io(fsens ? fsens[j] : nullptr, nz, N, k, ld);
-    }
-    if (int rc = run_ad(*t, n, in, out, seed, sens, nfwd, false, false, ar.p, ar.left, s))
-      return rc;
-  }
-  return 0;
-}
-
-int casadi_gb300_mapaccum_reverse(int id, int N, int n_accum, int64_t n, int64_t ld, int nadj,
-                                  const double* const* arg, double* const* res,
-                                  const double* const* aseed, double* const* asens,
-                                  void* scratch, size_t scratch_bytes, void* stream) {
-  Tape* t = get_tape(id);
-  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
-  if (int rc = check_device(*t)) return rc;
-  if (int rc = check_n(n, ld)) return rc;
-  if (int rc = accum_check(*t, N, n_accum)) return rc;
-  if (nadj < 1 || nadj > 65535) return fail(CASADI_GB300_ERR_ARG, "bad direction count %d", nadj);
-  if (n == 0) return 0;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  Arena ar(scratch, scratch_bytes);
-  // every step's accumulator values are kept (the caller's outputs or a scratch history): the
-  // reverse sweep of step k records it again from its inputs
-  AccumValues v;
-  if (int rc = accum_values(*t, N, n_accum, n, res, true, ar, &v)) return rc;
-  if (int rc = accum_forward_values(*t, N, n_accum, n, ld, arg, res, v, s)) return rc;
-  // adjoints of the accumulator inputs, carried from step k+1 to step k, and the combined
-  // seeds of the accumulator outputs
-  double* carry[kMaxIo] = {};
-  double* cseed[kMaxIo] = {};
-  for (int i = 0; i < n_accum; ++i) {
-    const long long blk = static_cast<long long>(nadj) * t->nnz_out[i] * n;
-    carry[i] = static_cast<double*>(ar.take(bytes_of(2 * blk)));
-    cseed[i] = static_cast<double*>(ar.take(bytes_of(blk)));
-    if (!carry[i] || !cseed[i])
-      return fail(CASADI_GB300_ERR_SCRATCH,
-                  "mapaccum scratch too small (see casadi_gb300_mapaccum_scratch_size)");
-  }
-  for (int k = N - 1; k >= 0; --k) {
-    IoDesc in[kMaxIo], out[kMaxIo], seed[kMaxIo], sens[kMaxIo];
-    for (int j = 0; j < t->n_out; ++j) {
-      const int nz = t->nnz_out[j];
-      out[j] = IoDesc{nullptr, ld, 1, 0};  // the values were written by the value sweeps
-      if (j < n_accum) {
-        // seed of x_{k+1}: its own adjoint seed plus what step k+1 passed back
-        const double* a_blk = aseed && aseed[j] ? aseed[j] + static_cast<size_t>(k) * nz * ld
-                                                : nullptr;
-        const double* prev = k < N - 1 ? carry[j] + static_cast<size_t>((k + 1) & 1) * nadj * nz * n
-                                       : nullptr;
-        cudaError_t e = add_blocks(nadj, nz, n, a_blk, ld, static_cast<long long>(nz) * N * ld,
-                                   prev, cseed[j], s);
-        if (e != cudaSuccess) return cuda_fail(e, "mapaccum seeds");
-        seed[j] = block_io(cseed[j], nz, n);
-      } else {
-        seed[j] = step_io(at(aseed, j), nz, N, k, ld);
-      }
-    }
-    for (int j = 0; j < t->n_in; ++j) {
-      const int nz = t->nnz_in[j];
-      if (j < n_accum) {
-        in[j] = k == 0 ? plain_io(at(arg, j), nz, ld, false) : v.value(j, nz, N, k - 1, n, ld);
-        sens[j] = k == 0 ? plain_io(asens ? asens[j] : nullptr, nz, ld, true)
-                         : block_io(carry[j] + static_cast<size_t>(k & 1) * nadj * nz * n, nz, n);
-      } else {
-        in[j] = step_io(at(arg, j), nz, N, k, ld);
-        sens[j] = step_io(asens ? asens[j] : nullptr, nz, N, k, ld);
-      }
-    }
-    if (int rc = run_ad(*t, n, in, out, seed, sens, nadj, true, false, ar.p, ar.left, s))
-      return rc;
-  }
-  return 0;
-}
-
-}  // extern "C"
-
-// ---- Self-check of the bounded waits ------------------------------------------------------
-extern "C" {
-
-int casadi_gb300_check_wait_timeout(void* stream) {
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  unsigned* words = nullptr;  // [0] a flag nothing sets, [1] the error word
-  cudaError_t e = cudaMalloc(&words, 2 * sizeof(unsigned));
-  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(wait probe)");
-  unsigned host[2] = {0, 0};
-  if ((e = cudaMemsetAsync(words, 0, 2 * sizeof(unsigned), s)) == cudaSuccess &&
-      (e = launch_wait_probe(words, words + 1, s)) == cudaSuccess &&
-      (e = cudaMemcpyAsync(host, words, sizeof(host), cudaMemcpyDeviceToHost, s)) == cudaSuccess)
-    e = cudaStreamSynchronize(s);
-  cudaFree(words);
-  if (e != cudaSuccess) return cuda_fail(e, "wait probe");
-  if (host[1] & kErrWaitTimeout)
-    return fail(CASADI_GB300_ERR_DEVICE, "bounded wait ran out (flag never set)");
-  return fail(CASADI_GB300_ERR_CUDA, "bounded wait did not report its timeout");
-}
-
-}  // extern "C"
+// The remaining entry points live in parts of this translation unit (they share the
+// internal helpers above).
+#include "abi_noalloc.cuh"
+#include "abi_batch.cuh"
+#include "abi_maps.cuh"

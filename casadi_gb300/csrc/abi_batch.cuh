@@ -1,0 +1,459 @@
+// C ABI: persistent multi-tape batches (host side of k_batch).
+//
+// Part of the abi.cu translation unit (included at its end): it uses that file's internal
+// registry, plans and launch helpers and is not compiled on its own.
+#pragma once
+
+// ---------------------------------------------------------------------------------------------
+// Persistent multi-tape batches.
+// ---------------------------------------------------------------------------------------------
+namespace {
+
+struct BatchHost {
+  struct Item {
+    int tape;
+    long long n;
+    int ndir;
+    bool forward = false;
+    std::vector<int> dirmap;  // forward items: direction of each flat input nonzero (-1: none)
+    std::vector<IoDesc> io;   // 4*kMaxIo
+  };
+  std::vector<Item> items;
+  bool dirty = true;
+  // device side, rebuilt when dirty
+  BatchItem* d_items = nullptr;
+  IoDesc* d_io = nullptr;
+  int4* d_units = nullptr;
+  unsigned* d_counter = nullptr;  // [0] next unit, [1] error bits
+  unsigned* d_flags = nullptr;    // tile flags of split items
+  size_t n_flags = 0;
+  std::vector<double*> d_tile_partials;  // per split item
+  // split items whose record sweep runs as a cooperative level sweep before the persistent
+  // launch (few tiles: the per-tile record units would leave the GPU idle), their flags set
+  // once it is done
+  struct PreRecord {
+    int item;
+    size_t flag0;
+    long long tiles;
+    double* partials;
+  };
+  std::vector<PreRecord> pre;
+  int n_units = 0;
+  int szw = 1, pmax = 0, grid = 1;
+  size_t smem = 0;
+  // work-vector residence: 0 shared memory, 1 global memory (grid_gw CTAs), -1 not tuned yet
+  int residence = -1;
+  int forced = 0;  // 0 tune, 1 global memory, 2 shared memory
+  int grid_gw = 1;
+  unsigned char* d_gw = nullptr;
+  int device = 0;
+  cudaStream_t stream = nullptr;  // owned: graph capture needs a non-legacy stream
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  void* exec_scratch = nullptr;
+  ~BatchHost() {
+    if (exec) cudaGraphExecDestroy(exec);
+    cudaFree(d_items);
+    cudaFree(d_io);
+    cudaFree(d_units);
+    cudaFree(d_counter);
+    cudaFree(d_flags);
+    cudaFree(d_gw);
+    for (double* p : d_tile_partials) cudaFree(p);
+    if (ev_in) cudaEventDestroy(ev_in);
+    if (ev_out) cudaEventDestroy(ev_out);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+std::vector<std::unique_ptr<BatchHost>> g_batches;
+
+BatchHost* get_batch(int id) {
+  std::lock_guard<std::mutex> lk(g_mtx);
+  if (id < 0 || id >= static_cast<int>(g_batches.size()) || !g_batches[id]) return nullptr;
+  return g_batches[id].get();
+}
+
+// Build items, the longest-first unit list and the launch shape.
+int batch_prepare(BatchHost& b) {
+  if (!b.dirty) return 0;
+  if (b.exec) {
+    cudaGraphExecDestroy(b.exec);
+    b.exec = nullptr;
+  }
+  cudaFree(b.d_items);
+  cudaFree(b.d_io);
+  cudaFree(b.d_units);
+  cudaFree(b.d_flags);
+  for (double* p : b.d_tile_partials) cudaFree(p);
+  b.d_tile_partials.clear();
+  b.d_items = nullptr;
+  b.d_io = nullptr;
+  b.d_units = nullptr;
+  b.d_flags = nullptr;
+  std::vector<BatchItem> items;
+  std::vector<IoDesc> io;
+  // (cost, unit): record and whole units first (longest first), then direction units
+  std::vector<std::pair<double, int4>> units, dir_units;
+  std::vector<std::pair<size_t, size_t>> flag_off;  // (item, first flag) of split items
+  size_t n_flags = 0;
+  b.pre.clear();
+  b.szw = 1;
+  b.pmax = 0;
+  for (size_t k = 0; k < b.items.size(); ++k) {
+    const auto& it = b.items[k];
+    Tape* t = get_tape(it.tape);
+    if (!t) return fail(CASADI_GB300_ERR_ID, "batch item %zu: tape %d is gone", k, it.tape);
+    BatchItem bi;
+    std::memset(&bi, 0, sizeof(bi));
+    bi.t = t->view();
+    bi.n_code = t->n_chunks * kChunk;
+    bi.ndir = it.ndir;
+    bi.n = it.n;
+    bi.forward = it.forward ? 1 : 0;
+    if (it.ndir > 0 && it.forward) {
+      if (static_cast<unsigned>(t->n_partials) >= kMaxPartials)
+        return fail(CASADI_GB300_ERR_UNSUPPORTED, "batch item %zu records too many partials", k);
+      int err = 0;
+      const TanPlan* tp = tan_plan(*t, it.ndir, 1, 0, true, std::vector<char>(t->n_in, 0),
+                                   it.dirmap, &err);
+      if (!tp) return err;
+      bi.tan_stream = tp->d_stream;
+      bi.tan_chunks = tp->d_chunks;
+    } else if (it.ndir > 0) {
+      if (static_cast<unsigned>(t->n_partials) >= kMaxPartials)
+        return fail(CASADI_GB300_ERR_UNSUPPORTED, "batch item %zu records too many partials", k);
+      std::vector<char> seeded(t->n_out);
+      for (int j = 0; j < t->n_out; ++j) seeded[j] = it.io[2 * kMaxIo + j].ptr != nullptr;
+      int err = 0;
+      const AdjPlan* ap = adj_plan(*t, 1, 0, seeded, &err);
+      if (!ap) return err;
+      int2 se;
+      cudaError_t e = cudaMemcpy(&se, ap->d_chunks, sizeof(int2), cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) return cuda_fail(e, "read adjoint plan");
+      bi.adj_stream = ap->d_stream + se.x;
+      bi.adj_ngr = se.y / kBatchGroup;
+      bi.zero_in = ap->d_zero;
+      bi.n_zero = ap->n_zero;
+    }
+    b.szw = std::max(b.szw, t->sz_w);
+    const long long tiles = (it.n + 31) / 32;
+    if (it.ndir >= 2) {
+      // split: one record unit per tile into the item's own partial buffer, then one unit
+      // per (tile, direction), so the directions of a tile run on different SMs
+      double* tp = nullptr;
+      const size_t bytes = static_cast<size_t>(tiles) * t->n_partials * 32 * sizeof(double);
+      cudaError_t e = cudaMalloc(&tp, std::max<size_t>(bytes, 8));
+      if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(batch tile partials)");
+      b.d_tile_partials.push_back(tp);
+      bi.tile_partials = tp;
+      flag_off.push_back({k, n_flags});
+      std::vector<int2> se(it.forward ? it.ndir : 1);
+      if (it.forward &&
+          (e = cudaMemcpy(se.data(), bi.tan_chunks, sizeof(int2) * it.ndir,
+                          cudaMemcpyDeviceToHost)) != cudaSuccess)
+        return cuda_fail(e, "read tangent plan");
+      // few tiles: the record sweep runs cooperatively (several warps per tile) before the
+      // persistent launch instead of as one-warp record units
+      const bool pre = tiles <= 4ll * sm_count() && ensure_levels(*t) &&
+                       smem_coop(t->lv_sz_w) <= static_cast<size_t>(max_smem_optin());
+      if (pre) {
+        b.pre.push_back({static_cast<int>(k), n_flags, tiles, tp});
+        bi.t = t->view();
+      }
+      for (long long tile = 0; tile < tiles; ++tile) {
+        if (!pre)
+          units.push_back({static_cast<double>(t->n_instr),
+                           make_int4(static_cast<int>(k), static_cast<int>(tile), -1, 0)});
+        for (int d = 0; d < it.ndir; ++d) {
+          const double len = it.forward ? se[d].y : bi.adj_ngr * kBatchGroup;
+          dir_units.push_back({len, make_int4(static_cast<int>(k), static_cast<int>(tile), d, 0)});
+        }
+      }
+      n_flags += static_cast<size_t>(tiles);
+    } else {
+      // whole units: value sweep plus the (at most one) direction in one warp
+      const double cost = static_cast<double>(t->n_instr) * (1 + it.ndir);
+      for (long long tile = 0; tile < tiles; ++tile)
+        units.push_back({cost, make_int4(static_cast<int>(k), static_cast<int>(tile), -1, 0)});
+      if (it.ndir > 0) b.pmax = std::max(b.pmax, t->n_partials);
+    }
+    items.push_back(bi);
+    io.insert(io.end(), it.io.begin(), it.io.end());
+  }
+  auto longest_first = [](const std::pair<double, int4>& x, const std::pair<double, int4>& y) {
+    return x.first > y.first;
+  };
+  std::stable_sort(units.begin(), units.end(), longest_first);
+  std::stable_sort(dir_units.begin(), dir_units.end(), longest_first);
+  std::vector<int4> ulist;
+  ulist.reserve(units.size() + dir_units.size());
+  for (const auto& u : units) ulist.push_back(u.second);
+  for (const auto& u : dir_units) ulist.push_back(u.second);
+  cudaError_t e;
+  if (n_flags && (e = cudaMalloc(&b.d_flags, n_flags * sizeof(unsigned))) != cudaSuccess)
+    return cuda_fail(e, "cudaMalloc(batch flags)");
+  b.n_flags = n_flags;
+  for (const auto& fo : flag_off) items[fo.first].ready = b.d_flags + fo.second;
+  if ((e = upload(&b.d_io, io)) != cudaSuccess) return cuda_fail(e, "upload batch I/O");
+  for (size_t k = 0; k < items.size(); ++k) items[k].io = b.d_io + k * 4 * kMaxIo;
+  if ((e = upload(&b.d_items, items)) != cudaSuccess || (e = upload(&b.d_units, ulist)) != cudaSuccess)
+    return cuda_fail(e, "upload batch");
+  if (!b.d_counter && (e = cudaMalloc(&b.d_counter, 2 * sizeof(unsigned))) != cudaSuccess)
+    return cuda_fail(e, "cudaMalloc(counter)");
+  b.n_units = static_cast<int>(ulist.size());
+  b.smem = static_cast<size_t>(b.szw) * 256;
+  const int occ = b.smem <= static_cast<size_t>(max_smem_optin())
+                      ? std::max(1, occupancy_batch(b.smem, b.n_flags > 0, false))
+                      : 1;
+  b.grid = std::max(1, std::min(sm_count() * occ, std::max(1, b.n_units)));
+  // global-memory work vectors: residency capped by registers (and at 8 CTAs per SM, which
+  // bounds the per-CTA partial scratch the caller provides)
+  const int occ_gw = std::max(1, std::min(8, occupancy_batch(0, b.n_flags > 0, true)));
+  b.grid_gw = std::max(1, std::min(sm_count() * occ_gw, std::max(1, b.n_units)));
+  cudaFree(b.d_gw);
+  b.d_gw = nullptr;
+  const size_t gw_bytes = static_cast<size_t>(b.grid_gw) * b.szw * 256;
+  if ((e = cudaMalloc(&b.d_gw, std::max<size_t>(gw_bytes, 256))) != cudaSuccess)
+    return cuda_fail(e, "cudaMalloc(batch work vectors)");
+  b.residence = b.forced == 1 ? 1 : (b.forced == 2 ? 0 : -1);
+  b.dirty = false;
+  return 0;
+}
+
+int batch_enqueue(BatchHost& b, void* scratch, cudaStream_t s, bool gw) {
+  cudaError_t e = cudaMemsetAsync(b.d_counter, 0, 2 * sizeof(unsigned), s);
+  if (e == cudaSuccess && b.n_flags)
+    e = cudaMemsetAsync(b.d_flags, 0, b.n_flags * sizeof(unsigned), s);
+  if (e != cudaSuccess) return cuda_fail(e, "reset batch counter");
+  for (const auto& pr : b.pre) {
+    const auto& it = b.items[pr.item];
+    Tape* t = get_tape(it.tape);
+    if (!t) return fail(CASADI_GB300_ERR_ID, "batch item %d: tape %d is gone", pr.item, it.tape);
+    SweepArgs a = base_args(*t, it.n, 0);
+    for (int j = 0; j < t->n_in; ++j) a.in[j] = it.io[j];
+    for (int j = 0; j < t->n_out; ++j) a.out[j] = it.io[kMaxIo + j];
+    a.partials = pr.partials;
+    a.block = coop_threads_for(pr.tiles);
+    const size_t sm = smem_coop(t->lv_sz_w);
+    const int occ = std::max(1, occupancy_coop(a.block, sm, false));
+    const int grid = static_cast<int>(std::min<long long>(pr.tiles, 1ll * occ * sm_count()));
+    if ((e = launch_coop(a, true, grid, s)) != cudaSuccess) return cuda_fail(e, "batch record");
+    // every tile of the item is recorded: its direction units need not wait
+    if ((e = cudaMemsetAsync(b.d_flags + pr.flag0, 0xff, pr.tiles * sizeof(unsigned), s)) !=
+        cudaSuccess)
+      return cuda_fail(e, "batch flags");
+  }
+  BatchArgs a;
+  a.items = b.d_items;
+  a.units = b.d_units;
+  a.n_units = b.n_units;
+  a.counter = b.d_counter;
+  a.err = b.d_counter + 1;
+  a.scratch = static_cast<double*>(scratch);
+  a.scratch_stride = static_cast<long long>(b.pmax) * 32;
+  a.wglob = gw ? b.d_gw : nullptr;
+  a.wglob_stride = static_cast<long long>(b.szw) * 256;
+  e = launch_batch(a, gw ? b.grid_gw : b.grid, b.smem, b.n_flags > 0, gw, s);
+  if (e != cudaSuccess) return cuda_fail(e, "batch launch");
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int casadi_gb300_batch_create(void) {
+  auto b = std::make_unique<BatchHost>();
+  cudaError_t e = cudaGetDevice(&b->device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if ((e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&b->ev_in, cudaEventDisableTiming)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&b->ev_out, cudaEventDisableTiming)) != cudaSuccess)
+    return cuda_fail(e, "batch stream");
+  std::lock_guard<std::mutex> lk(g_mtx);
+  g_batches.push_back(std::move(b));
+  return static_cast<int>(g_batches.size()) - 1;
+}
+
+int casadi_gb300_batch_free(int batch) {
+  std::lock_guard<std::mutex> lk(g_mtx);
+  if (batch < 0 || batch >= static_cast<int>(g_batches.size()) || !g_batches[batch])
+    return fail(CASADI_GB300_ERR_ID, "no batch %d", batch);
+  g_batches[batch].reset();
+  return 0;
+}
+
+int casadi_gb300_batch_add(int batch, int id, int64_t n, int64_t ld, int nadj,
+                           const double* const* arg, double* const* res,
+                           const double* const* aseed, double* const* asens) {
+  BatchHost* b = get_batch(batch);
+  if (!b) return fail(CASADI_GB300_ERR_ID, "no batch %d", batch);
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  if (int rc = check_device(*t)) return rc;
+  if (int rc = check_n(n, ld)) return rc;
+  if (nadj < 0 || nadj > 65535) return fail(CASADI_GB300_ERR_ARG, "bad direction count %d", nadj);
+  if (n > (1ll << 36)) return fail(CASADI_GB300_ERR_ARG, "too many instances");
+  BatchHost::Item it;
+  it.tape = id;
+  it.n = n;
+  it.ndir = nadj;
+  it.io.assign(4 * kMaxIo, IoDesc{nullptr, 0, 0, 0});
+  fill_io(it.io.data(), t->n_in, vptrs(arg), t->nnz_in, ld, false);
+  fill_io(it.io.data() + kMaxIo, t->n_out, vptrs(res), t->nnz_out, ld, false);
+  if (nadj > 0) {
+    fill_io(it.io.data() + 2 * kMaxIo, t->n_out, vptrs(aseed), t->nnz_out, ld, true);
+    fill_io(it.io.data() + 3 * kMaxIo, t->n_in, vptrs(asens), t->nnz_in, ld, true);
+  }
+  b->items.push_back(std::move(it));
+  b->dirty = true;
+  return static_cast<int>(b->items.size()) - 1;
+}
+
+int casadi_gb300_batch_add_jacobian_colored(int batch, int id, int64_t n, int64_t ld,
+                                            int n_colors, const int* color,
+                                            const double* const* arg, double* const* res,
+                                            double* const* comp) {
+  BatchHost* b = get_batch(batch);
+  if (!b) return fail(CASADI_GB300_ERR_ID, "no batch %d", batch);
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  if (int rc = check_device(*t)) return rc;
+  if (int rc = check_n(n, ld)) return rc;
+  if (n > (1ll << 36)) return fail(CASADI_GB300_ERR_ARG, "too many instances");
+  int nz = 0;
+  for (int v : t->nnz_in) nz += v;
+  if (!color || n_colors < 1 || n_colors > nz)
+    return fail(CASADI_GB300_ERR_ARG, "bad colouring (%d colours for %d input nonzeros)",
+                n_colors, nz);
+  BatchHost::Item it;
+  it.tape = id;
+  it.n = n;
+  it.ndir = n_colors;
+  it.forward = true;
+  it.dirmap.assign(color, color + nz);
+  for (int v : it.dirmap)
+    if (v < -1 || v >= n_colors) return fail(CASADI_GB300_ERR_ARG, "colour %d out of range", v);
+  it.io.assign(4 * kMaxIo, IoDesc{nullptr, 0, 0, 0});
+  fill_io(it.io.data(), t->n_in, vptrs(arg), t->nnz_in, ld, false);
+  fill_io(it.io.data() + kMaxIo, t->n_out, vptrs(res), t->nnz_out, ld, false);
+  fill_io(it.io.data() + 3 * kMaxIo, t->n_out, vptrs(comp), t->nnz_out, ld, true);
+  b->items.push_back(std::move(it));
+  b->dirty = true;
+  return static_cast<int>(b->items.size()) - 1;
+}
+
+int casadi_gb300_batch_set_residence(int batch, int mode) {
+  BatchHost* b = get_batch(batch);
+  if (!b) return fail(CASADI_GB300_ERR_ID, "no batch %d", batch);
+  if (mode < 0 || mode > 2) return fail(CASADI_GB300_ERR_ARG, "residence must be 0, 1 or 2");
+  b->forced = mode;
+  b->residence = mode == 1 ? 1 : (mode == 2 ? 0 : -1);
+  if (b->exec) {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  return 0;
+}
+
+int casadi_gb300_batch_status(int batch) {
+  BatchHost* b = get_batch(batch);
+  if (!b) return fail(CASADI_GB300_ERR_ID, "no batch %d", batch);
+  if (!b->d_counter) return 0;
+  unsigned w[2] = {0, 0};
+  cudaError_t e = cudaStreamSynchronize(b->stream);
+  if (e == cudaSuccess) e = cudaMemcpy(w, b->d_counter, sizeof(w), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "batch status");
+  if (w[1] & kErrWaitTimeout)
+    return fail(CASADI_GB300_ERR_CUDA, "batch: a direction unit timed out waiting for its tile");
+  return 0;
+}
+
+int casadi_gb300_batch_scratch_size(int batch, size_t* bytes) {
+  BatchHost* b = get_batch(batch);
+  if (!b) return fail(CASADI_GB300_ERR_ID, "no batch %d", batch);
+  if (!bytes) return fail(CASADI_GB300_ERR_ARG, "bad arguments");
+  if (int rc = batch_prepare(*b)) return rc;
+  *bytes = static_cast<size_t>(std::max(b->grid, b->grid_gw)) * b->pmax * 32 * 8;
+  return 0;
+}
+
+int casadi_gb300_batch_run(int batch, void* scratch, size_t scratch_bytes, int use_graph,
+                           void* stream) {
+  BatchHost* b = get_batch(batch);
+  if (!b) return fail(CASADI_GB300_ERR_ID, "no batch %d", batch);
+  int cur = -1;
+  cudaGetDevice(&cur);
+  if (cur != b->device) return fail(CASADI_GB300_ERR_ARG, "batch lives on device %d", b->device);
+  if (int rc = batch_prepare(*b)) return rc;
+  const size_t need = static_cast<size_t>(std::max(b->grid, b->grid_gw)) * b->pmax * 32 * 8;
+  if (need > 0 && (!scratch || scratch_bytes < need))
+    return fail(CASADI_GB300_ERR_SCRATCH, "batch needs %zu bytes of scratch, got %zu", need,
+                scratch_bytes);
+  cudaStream_t caller = static_cast<cudaStream_t>(stream);
+  // order after the caller's stream, run on the owned stream, order the caller after it
+  cudaError_t e = cudaEventRecord(b->ev_in, caller);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->ev_in, 0);
+  if (e != cudaSuccess) return cuda_fail(e, "batch ordering");
+  if (b->residence < 0) {
+    // tune the work-vector residence once per batch layout: both runs produce the results
+    if (g_autotune && !capturing(caller)) {
+      float ms[2] = {0, 0};
+      for (int gw = 0; gw < 2; ++gw) {
+        if (gw == 0 && b->smem > static_cast<size_t>(max_smem_optin())) {
+          ms[0] = 3.0e38f;  // the shared-memory instance cannot hold this batch
+          continue;
+        }
+        int rc = 0;
+        if (int trc = time_once(b->stream, [&] {
+              rc = batch_enqueue(*b, scratch, b->stream, gw == 1);
+              return cudaSuccess;
+            }, &ms[gw]))
+          return trc;
+        if (rc) return rc;
+      }
+      b->residence = ms[1] < ms[0] ? 1 : 0;
+    } else {
+      b->residence = b->smem <= static_cast<size_t>(max_smem_optin()) ? 0 : 1;
+    }
+  }
+  const bool gw = b->residence == 1;
+  if (use_graph) {
+    if (b->exec && b->exec_scratch != scratch) {
+      cudaGraphExecDestroy(b->exec);
+      b->exec = nullptr;
+    }
+    if (!b->exec) {
+      cudaGraph_t g = nullptr;
+      e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+      if (e != cudaSuccess) return cuda_fail(e, "begin capture");
+      int rc = batch_enqueue(*b, scratch, b->stream, gw);
+      e = cudaStreamEndCapture(b->stream, &g);
+      if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+      }
+      if (e != cudaSuccess) return cuda_fail(e, "end capture");
+      e = cudaGraphInstantiate(&b->exec, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return cuda_fail(e, "instantiate batch graph");
+      b->exec_scratch = scratch;
+    }
+    e = timed(F_BATCH, b->stream, [&] { return cudaGraphLaunch(b->exec, b->stream); });
+    if (e != cudaSuccess) return cuda_fail(e, "graph launch");
+  } else {
+    int rc = 0;
+    e = timed(F_BATCH, b->stream, [&] {
+      rc = batch_enqueue(*b, scratch, b->stream, gw);
+      return cudaSuccess;
+    });
+    if (rc) return rc;
+  }
+  e = cudaEventRecord(b->ev_out, b->stream);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(caller, b->ev_out, 0);
+  if (e != cudaSuccess) return cuda_fail(e, "batch ordering");
+  return 0;
+}
+
+}  // extern "C"
