@@ -95,3 +95,13 @@ def test_rejects_bad_ids(lib):
     assert lib.casadi_gb300_tape_free(12345) == -1
     assert lib.casadi_gb300_eval(12345, 1, 1, None, None, None) == -1
     assert "no tape" in lib.casadi_gb300_last_error().decode()
+
+
+def test_package_map_and_mapaccum_pick_the_reference_shapes():
+    """casadi_gb300.map / mapaccum mirror Function::map / mapaccum: n == 1 returns f, reduce
+    flags give a MapSum, other parallelizations are refused (no device needed to check)."""
+    import casadi_gb300 as cg
+    f = W.cartpole_step()
+    assert cg.map(f, 1) is f
+    with pytest.raises(ValueError):
+        cg.map(f, 4, "openmp")
