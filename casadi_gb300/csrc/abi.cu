@@ -2009,6 +2009,48 @@ int casadi_gb300_map_jacobian(int id, int mem, int64_t n, const double* const* a
   return casadi_gb300_sync(id, s);
 }
 
+int casadi_gb300_map_forward(int id, int mem, int64_t n, int nfwd, const double* const* arg,
+                             double* const* res, const double* const* fseed,
+                             double* const* fsens) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  Mem* m = get_mem(mem);
+  if (!m) return fail(CASADI_GB300_ERR_ID, "no memory object %d", mem);
+  if (int rc = check_device(*t)) return rc;
+  if (n < 0 || nfwd < 1 || nfwd > 65535) return fail(CASADI_GB300_ERR_ARG, "bad arguments");
+  if (n == 0) return 0;
+  cudaStream_t s = m->stream;
+  IoDesc in[kMaxIo], out[kMaxIo], seed[kMaxIo], sens[kMaxIo];
+  if (int rc = stage_blocks(*m, 0, t->n_in, t->nnz_in, 1, n, arg, false, in, s)) return rc;
+  if (int rc = stage_blocks(*m, kMaxIo, t->n_out, t->nnz_out, 1, n,
+                            reinterpret_cast<const double* const*>(res), false, out, s))
+    return rc;
+  if (int rc = stage_blocks(*m, 2 * kMaxIo, t->n_in, t->nnz_in, nfwd, n, fseed, false, seed, s))
+    return rc;
+  if (int rc = stage_blocks(*m, 3 * kMaxIo, t->n_out, t->nnz_out, nfwd, n,
+                            reinterpret_cast<const double* const*>(fsens), false, sens, s))
+    return rc;
+  void* scratch = nullptr;
+  size_t bytes = 0;
+  if (int rc = map_scratch(*t, *m, n, &scratch, &bytes)) return rc;
+  std::vector<HostBlock> blocks;
+  collect_blocks(blocks, in, t->n_in, arg, nullptr);
+  collect_blocks(blocks, seed, t->n_in, fseed, nullptr);
+  collect_blocks(blocks, out, t->n_out, nullptr, res);
+  collect_blocks(blocks, sens, t->n_out, nullptr, fsens);
+  if (int rc = run_pipelined(*m, n, blocks, [&](long long i0, long long cnt) {
+        IoDesc in_c[kMaxIo], out_c[kMaxIo], seed_c[kMaxIo], sens_c[kMaxIo];
+        shift_io(in, t->n_in, i0, in_c);
+        shift_io(out, t->n_out, i0, out_c);
+        shift_io(seed, t->n_in, i0, seed_c);
+        shift_io(sens, t->n_out, i0, sens_c);
+        return run_ad(*t, cnt, in_c, out_c, seed_c, sens_c, nfwd, false, false, scratch, bytes,
+                      s);
+      }))
+    return rc;
+  return casadi_gb300_sync(id, s);
+}
+
 int casadi_gb300_map_reverse(int id, int mem, int64_t n, int nadj, const double* const* arg,
                              double* const* res, const double* const* aseed,
                              double* const* asens) {

@@ -92,6 +92,7 @@ def load(path=None):
         "casadi_gb300_release": (cint, [cint]),
         "casadi_gb300_map_eval": (cint, [cint, cint, i64, vp, vp]),
         "casadi_gb300_map_reverse": (cint, [cint, cint, i64, cint, vp, vp, vp, vp]),
+        "casadi_gb300_map_forward": (cint, [cint, cint, i64, cint, vp, vp, vp, vp]),
         "casadi_gb300_jacobian": (cint, [cint, i64, i64, vp, vp, vp, vp, sz, vp]),
         "casadi_gb300_map_jacobian": (cint, [cint, cint, i64, vp, vp, vp]),
         "casadi_gb300_jacobian_reverse": (cint, [cint, i64, i64, vp, vp, vp, cint, vp, vp, vp, sz,
@@ -648,6 +649,19 @@ class CudaMap:
             self.tape.id, self.mem.id, self.n, _host_ptrs(args), _host_ptrs(res),
             _host_ptrs(jac), nadj, _host_ptrs(aseeds), _host_ptrs(asens)))
         return res, jac, asens
+
+    def forward(self, args, fseeds, res=None, fsens=None):
+        """Forward sweep with instance-major host buffers: fseeds[j] has shape
+        (n, nfwd, nnz_in[j]); returns (res, fsens) with fsens[j] of shape (n, nfwd, nnz_out[j])."""
+        args = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in args]
+        fseeds = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in fseeds]
+        nfwd = next(a.shape[1] for a in fseeds if a is not None)
+        res = self._host_out(self.tape.nnz_out) if res is None else res
+        fsens = [np.empty((self.n, nfwd, k)) for k in self.tape.nnz_out] if fsens is None else fsens
+        check(load().casadi_gb300_map_forward(self.tape.id, self.mem.id, self.n, nfwd,
+                                              _host_ptrs(args), _host_ptrs(res),
+                                              _host_ptrs(fseeds), _host_ptrs(fsens)))
+        return res, fsens
 
     def reverse(self, args, aseeds, res=None, asens=None):
         """Adjoint sweep with instance-major host buffers: aseeds[j] has shape

@@ -302,6 +302,13 @@ CASADI_GB300_API int casadi_gb300_map_eval(int id, int mem, int64_t n, const dou
 CASADI_GB300_API int casadi_gb300_map_jacobian(int id, int mem, int64_t n, const double* const* arg,
                               double* const* res, double* const* jac);
 
+/* Map over the forward sweep with host buffers (the Map's forward(nfwd), map.cpp:219-271):
+ * fseed[j] is instance-major (fseed[j] + (i*nfwd + d)*nnz_in[j] holds direction d of
+ * instance i), fsens likewise with nnz_out[j]. */
+CASADI_GB300_API int casadi_gb300_map_forward(int id, int mem, int64_t n, int nfwd,
+                             const double* const* arg, double* const* res,
+                             const double* const* fseed, double* const* fsens);
+
 /* Map over the reverse sweep with host buffers: aseed[j] is instance-major
  * (aseed[j] + (i*nadj + d)*nnz_out[j] holds direction d of instance i), asens likewise. */
 CASADI_GB300_API int casadi_gb300_map_reverse(int id, int mem, int64_t n, int nadj, const double* const* arg,

@@ -341,6 +341,27 @@ def test_map_eval_and_reverse_host_buffers(gpu_lib):
     _, wasens = O.reverse(f.tape, [x, u], [np.transpose(aseed, (1, 2, 0))], n)
     assert_close(np.transpose(asens[0], (1, 2, 0)), wasens[0], "map reverse x")
     assert_close(np.transpose(asens[1], (1, 2, 0)), wasens[1], "map reverse u")
+    # forward mode: seeds (n, nfwd, nnz) instance-major, the Map's forward(nfwd) layout
+    rng = np.random.default_rng(4)
+    fx, fu = rng.standard_normal((n, 3, 4)), rng.standard_normal((n, 3, 1))
+    _, fsens = F.forward([x.T.copy(), u.T.copy()], [fx, fu])
+    _, wfs = O.forward(f.tape, [x, u], [np.transpose(fx, (1, 2, 0)),
+                                       np.transpose(fu, (1, 2, 0))], n)
+    assert_close(np.transpose(fsens[0], (1, 2, 0)), wfs[0], "map forward")
+
+
+def test_host_buffer_calls_in_pipelined_chunks(gpu_lib):
+    """Host-buffer calls large enough to run in pipelined chunks (copies of one chunk
+    overlapping the sweeps of another) give the device entry points' bits."""
+    f = W.cartpole_rollout(3)
+    n = 2 * 131072 + 77
+    x, u = W.cartpole_inputs(n, steps=3, seed=12)
+    F = CudaMap(f, n)
+    res, jac = F.jacobian(x.T.copy(), u.T.copy())
+    ct = CudaTape(f)
+    dres, djac = ct.jacobian(dev([x, u]))
+    assert_bitexact(res[0].T, host(dres)[0], "values")
+    assert_bitexact(np.transpose(jac[0], (1, 2, 0)), host(djac)[0], "jacobian")
 
 
 # ---- derivative-sweep variants and the autotuner ------------------------------------------------
