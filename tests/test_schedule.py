@@ -186,3 +186,69 @@ def test_reverse_levels_keep_the_users_of_each_value_in_order(name, make, inputs
     aseeds = [rng.standard_normal((1, k, n)) for k in t.nnz_out]
     _all_bits_equal(O.reverse(lt, args, aseeds, n)[1], O.reverse(R.schedule(t), args, aseeds,
                                                                   n)[1], "adjoint")
+
+
+# ---- randomized tapes (hypothesis; skipped where it is not installed) ------------------------
+def _random_tape(seed, n_in, n_nodes, n_out, window):
+    """A random SX DAG over +,-,*,/,sqrt,sin and constants (bounded values)."""
+    from casadi_gb300 import sx as S
+    rng = np.random.default_rng(seed)
+    xs = S.sym("x", n_in)
+    nodes = list(xs)
+    for k in range(n_nodes):
+        a = nodes[int(rng.integers(max(0, len(nodes) - window), len(nodes)))]
+        b = nodes[int(rng.integers(max(0, len(nodes) - window), len(nodes)))]
+        r = rng.random()
+        if r < 0.25:
+            e = a + b
+        elif r < 0.4:
+            e = a - b
+        elif r < 0.6:
+            e = a * b * 0.5
+        elif r < 0.7:
+            e = a / (b * b + 1.0)
+        elif r < 0.8:
+            e = S.sqrt(a * a + 1.0)
+        elif r < 0.9:
+            e = S.sin(a) + 0.25
+        else:
+            e = a * float(rng.integers(1, 4))
+        nodes.append(e)
+    return S.Function("r", [xs], [nodes[-n_out:]]).tape
+
+
+def test_levels_hold_on_random_tapes():
+    hyp = pytest.importorskip("hypothesis")
+    st = hyp.strategies
+
+    @hyp.settings(max_examples=25, deadline=None)
+    @hyp.given(seed=st.integers(0, 10**6), n_in=st.integers(1, 6), n_nodes=st.integers(1, 120),
+               n_out=st.integers(1, 5), window=st.integers(1, 40),
+               width=st.integers(1, 40), cap=st.integers(1, 60),
+               ordered=st.booleans())
+    def check(seed, n_in, n_nodes, n_out, window, width, cap, ordered):
+        t = _random_tape(seed, n_in, n_nodes, min(n_out, n_nodes + n_in), window)
+        s = R.schedule(t)
+        lt, src, begin = R.levels(t, width=-width if ordered else width, slot_cap=cap)
+        assert sorted(src.tolist()) == list(range(s.n_instr))
+        assert np.all(np.diff(begin) >= 1) and np.all(np.diff(begin) <= width)
+        for l in range(len(begin) - 1):
+            ws, rs = [], []
+            for k in range(begin[l], begin[l + 1]):
+                r_, w_ = _reads_writes(lt.op[k], lt.i0[k], lt.i1[k], lt.i2[k])
+                rs.append(r_)
+                ws.append(w_)
+            real = [w_ for w_ in ws if w_ is not None]
+            assert len(real) == len(set(real))
+            for a_, w_ in enumerate(ws):
+                if w_ is not None:
+                    assert all(a_ == b_ or w_ not in r_ for b_, r_ in enumerate(rs))
+        n = 5
+        args = [np.random.default_rng(seed).uniform(-1, 1, (t.nnz_in[0], n))]
+        _all_bits_equal(O.eval(lt, args, n), O.eval(t, args, n), "values")
+        if ordered:
+            aseeds = [np.ones((1, t.nnz_out[0], n))]
+            _all_bits_equal(O.reverse(lt, args, aseeds, n)[1], O.reverse(s, args, aseeds, n)[1],
+                            "adjoint")
+
+    check()
