@@ -49,10 +49,6 @@ struct BatchHost {
   int device = 0;
   cudaStream_t stream = nullptr;  // owned: graph capture needs a non-legacy stream
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
-  // a second stream on which every other cooperative pre-record runs concurrently (forked
-  // from and joined back into the batch's stream, inside the captured graph as well)
-  cudaStream_t side = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   cudaGraphExec_t exec = nullptr;
   void* exec_scratch = nullptr;
   ~BatchHost() {
@@ -66,9 +62,6 @@ struct BatchHost {
     for (double* p : d_tile_partials) cudaFree(p);
     if (ev_in) cudaEventDestroy(ev_in);
     if (ev_out) cudaEventDestroy(ev_out);
-    if (ev_fork) cudaEventDestroy(ev_fork);
-    if (ev_join) cudaEventDestroy(ev_join);
-    if (side) cudaStreamDestroy(side);
     if (stream) cudaStreamDestroy(stream);
   }
 };
@@ -233,13 +226,7 @@ int batch_enqueue(BatchHost& b, void* scratch, cudaStream_t s, bool gw) {
   if (e == cudaSuccess && b.n_flags)
     e = cudaMemsetAsync(b.d_flags, 0, b.n_flags * sizeof(unsigned), s);
   if (e != cudaSuccess) return cuda_fail(e, "reset batch counter");
-  const bool fork = b.pre.size() >= 2;
-  if (fork && ((e = cudaEventRecord(b.ev_fork, s)) != cudaSuccess ||
-               (e = cudaStreamWaitEvent(b.side, b.ev_fork, 0)) != cudaSuccess))
-    return cuda_fail(e, "batch fork");
-  for (size_t k = 0; k < b.pre.size(); ++k) {
-    const auto& pr = b.pre[k];
-    const cudaStream_t ps = (fork && (k & 1)) ? b.side : s;
+  for (const auto& pr : b.pre) {
     const auto& it = b.items[pr.item];
     Tape* t = get_tape(it.tape);
     if (!t) return fail(CASADI_GB300_ERR_ID, "batch item %d: tape %d is gone", pr.item, it.tape);
@@ -251,15 +238,12 @@ int batch_enqueue(BatchHost& b, void* scratch, cudaStream_t s, bool gw) {
     const size_t sm = smem_coop(t->lv_sz_w);
     const int occ = std::max(1, occupancy_coop(a.block, sm, false));
     const int grid = static_cast<int>(std::min<long long>(pr.tiles, 1ll * occ * sm_count()));
-    if ((e = launch_coop(a, true, grid, ps)) != cudaSuccess) return cuda_fail(e, "batch record");
+    if ((e = launch_coop(a, true, grid, s)) != cudaSuccess) return cuda_fail(e, "batch record");
     // every tile of the item is recorded: its direction units need not wait
-    if ((e = cudaMemsetAsync(b.d_flags + pr.flag0, 0xff, pr.tiles * sizeof(unsigned), ps)) !=
+    if ((e = cudaMemsetAsync(b.d_flags + pr.flag0, 0xff, pr.tiles * sizeof(unsigned), s)) !=
         cudaSuccess)
       return cuda_fail(e, "batch flags");
   }
-  if (fork && ((e = cudaEventRecord(b.ev_join, b.side)) != cudaSuccess ||
-               (e = cudaStreamWaitEvent(s, b.ev_join, 0)) != cudaSuccess))
-    return cuda_fail(e, "batch join");
   BatchArgs a;
   a.items = b.d_items;
   a.units = b.d_units;
@@ -284,11 +268,8 @@ int casadi_gb300_batch_create(void) {
   cudaError_t e = cudaGetDevice(&b->device);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
   if ((e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess ||
-      (e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking)) != cudaSuccess ||
       (e = cudaEventCreateWithFlags(&b->ev_in, cudaEventDisableTiming)) != cudaSuccess ||
-      (e = cudaEventCreateWithFlags(&b->ev_out, cudaEventDisableTiming)) != cudaSuccess ||
-      (e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming)) != cudaSuccess ||
-      (e = cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming)) != cudaSuccess)
+      (e = cudaEventCreateWithFlags(&b->ev_out, cudaEventDisableTiming)) != cudaSuccess)
     return cuda_fail(e, "batch stream");
   std::lock_guard<std::mutex> lk(g_mtx);
   g_batches.push_back(std::move(b));
