@@ -92,10 +92,12 @@ struct TanPlan {
   uint4* d_stream = nullptr;  // entry streams of all directions
   int2* d_chunks = nullptr;   // per direction: (first entry, entry count)
   int* d_dirmap = nullptr;    // identity mode with a dirmap: its device copy
+  int* d_order = nullptr;     // groups in work order, longest stream first (null: natural)
   ~TanPlan() {
     cudaFree(d_stream);
     cudaFree(d_chunks);
     cudaFree(d_dirmap);
+    cudaFree(d_order);
   }
 };
 
@@ -449,6 +451,10 @@ int grid_for(long long tiles, int cap) {
   return static_cast<int>(std::max<long long>(g, 1));
 }
 
+// Room the reported scratch sizes leave past the partials for the tangent sweep's work
+// counter.
+constexpr size_t kQueueSlack = 256;
+
 // Instances per AD wave that fit in `bytes` of scratch (multiple of 32).
 long long wave_capacity(const Tape& t, long long n, size_t bytes) {
   if (t.n_partials == 0) return n;
@@ -637,9 +643,18 @@ const TanPlan* tan_plan(Tape& t, int ndir, int dw, int ch, bool identity,
     if (dw == 1) forward_operands(ents);
     se[g] = push_stream(all, ents);
   }
+  // the groups of one tile are claimed longest first, so the last items of a sweep are the
+  // short ones
+  std::vector<int> order(p->groups);
+  for (int g = 0; g < p->groups; ++g) order[g] = g;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int x, int y) { return se[x].y > se[y].y; });
+  bool natural = true;
+  for (int g = 0; g < p->groups; ++g) natural = natural && order[g] == g;
   cudaError_t e;
   if ((e = upload(&p->d_stream, all)) != cudaSuccess ||
       (e = upload(&p->d_chunks, se)) != cudaSuccess ||
+      (!natural && (e = upload(&p->d_order, order)) != cudaSuccess) ||
       (identity && !dirmap.empty() && (e = upload(&p->d_dirmap, dirmap)) != cudaSuccess)) {
     *err = cuda_fail(e, "upload tangent plan");
     return nullptr;
@@ -928,6 +943,17 @@ struct DerivReq {
 };
 
 // Runs one derivative sweep of wave `a` (values and partials already recorded).
+// Tangent sweep launch; with more items than CTAs the items past the grid come from the work
+// counter a.queue (zeroed here), otherwise every CTA takes one item by index.
+cudaError_t launch_tangent_queued(const SweepArgs& a, int grid, bool more_items, int variant,
+                                  cudaStream_t s) {
+  SweepArgs b = a;
+  if (!more_items) b.queue = nullptr;
+  if (b.queue)
+    if (cudaError_t e = cudaMemsetAsync(b.queue, 0, sizeof(*b.queue), s)) return e;
+  return launch_tangent(b, grid, variant, s);
+}
+
 int run_deriv(Tape& t, SweepArgs a, long long m, const DerivReq& rq, cudaStream_t s) {
   const int ndir = rq.ndir;
   const bool adjoint = rq.adjoint, identity = rq.identity;
@@ -972,10 +998,15 @@ int run_deriv(Tape& t, SweepArgs a, long long m, const DerivReq& rq, cudaStream_
     if (kd > 1 && static_cast<long long>(t.sz_w) * 256 >= (1ll << 19)) return false;
     return smem_lean(t.sz_w, ipt * kd, 0) <= static_cast<size_t>(max_smem_optin());
   };
+  auto work_of = [&](int v) {
+    int ipt, kd;
+    shape(v, &ipt, &kd);
+    return (tiles + ipt - 1) / ipt * ((ndir + kd - 1) / kd);
+  };
   auto grid_of = [&](int v) {
     int ipt, kd;
     shape(v, &ipt, &kd);
-    const long long vwork = (tiles + ipt - 1) / ipt * ((ndir + kd - 1) / kd);
+    const long long vwork = work_of(v);
     const int occ = std::max(1, occupancy_dir(v, adjoint, smem_lean(t.sz_w, ipt * kd, 0)));
     return static_cast<int>(std::max<long long>(
         1, std::min<long long>(vwork, static_cast<long long>(sms) * occ)));
@@ -991,7 +1022,9 @@ int run_deriv(Tape& t, SweepArgs a, long long m, const DerivReq& rq, cudaStream_
     if (!tp) return cudaErrorInvalidValue;
     a.dstream = tp->d_stream;
     a.dchunks = tp->d_chunks;
-    return launch_tangent(a, grid_of(v), v, s);
+    a.gorder = tp->d_order;
+    const int grid = grid_of(v);
+    return launch_tangent_queued(a, grid, grid < work_of(v), v, s);
   };
   const long long work = tiles * ndir;
   const int cls = tiles <= 16ll * sms ? 0 : 1;
@@ -1045,7 +1078,8 @@ int run_deriv(Tape& t, SweepArgs a, long long m, const DerivReq& rq, cudaStream_
       if (!tp) return cudaErrorInvalidValue;
       a.dstream = tp->d_stream;
       a.dchunks = tp->d_chunks;
-      return launch_tangent(a, grid, 0, s);
+      a.gorder = tp->d_order;
+      return launch_tangent_queued(a, grid, grid < work, 0, s);
     });
     if (plan_err) return plan_err;
     if (e != cudaSuccess) return cuda_fail(e, "derivative sweep launch");
@@ -1114,6 +1148,12 @@ int run_ad_multi(Tape& t, long long n, const IoDesc* in, const IoDesc* out,
     const long long m = std::min(cap, n - i0);
     SweepArgs a = base_args(t, m, i0);
     a.partials = static_cast<double*>(scratch);
+    // the tangent sweep's work counter: 8 bytes past the wave's partials, where the scratch
+    // has them (the scratch sizes this library reports always do); otherwise the sweep
+    // strides statically
+    const size_t used = 8ull * t.n_partials * static_cast<size_t>(cap);
+    if (scratch && scratch_bytes >= used + sizeof(unsigned long long))
+      a.queue = reinterpret_cast<unsigned long long*>(static_cast<char*>(scratch) + used);
     a.pofs = t.d_pofs;
     a.n_code = t.n_chunks * kChunk;
     for (int j = 0, off = 0; j < t.n_in; off += t.nnz_in[j], ++j) a.in_off[j] = off;
@@ -1533,7 +1573,8 @@ int casadi_gb300_scratch_size(int id, int64_t n, size_t* bytes) {
   Tape* t = get_tape(id);
   if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
   if (!bytes || n < 0) return fail(CASADI_GB300_ERR_ARG, "bad arguments");
-  *bytes = static_cast<size_t>(8) * t->n_partials * static_cast<size_t>(((n + 31) / 32) * 32);
+  *bytes = static_cast<size_t>(8) * t->n_partials * static_cast<size_t>(((n + 31) / 32) * 32) +
+           kQueueSlack;
   return 0;
 }
 
@@ -1541,7 +1582,7 @@ int casadi_gb300_scratch_min(int id, size_t* bytes) {
   Tape* t = get_tape(id);
   if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
   if (!bytes) return fail(CASADI_GB300_ERR_ARG, "bad arguments");
-  *bytes = static_cast<size_t>(8) * 32 * t->n_partials;
+  *bytes = static_cast<size_t>(8) * 32 * t->n_partials + kQueueSlack;
   return 0;
 }
 
@@ -1932,7 +1973,7 @@ static int map_scratch(const Tape& t, Mem& m, long long n, void** scratch, size_
   if (t.n_partials == 0) return 0;
   size_t need = 8ull * t.n_partials * static_cast<size_t>(((n + 31) / 32) * 32);
   const size_t kMaxScratch = 8ull << 30;
-  need = std::min(need, std::max<size_t>(kMaxScratch, 8ull * 32 * t.n_partials));
+  need = std::min(need, std::max<size_t>(kMaxScratch, 8ull * 32 * t.n_partials)) + kQueueSlack;
   cudaError_t e = cudaSuccess;
   *scratch = m.buf(4 * kMaxIo, need, &e);
   if (!*scratch) return cuda_fail(e, "cudaMalloc(scratch)");

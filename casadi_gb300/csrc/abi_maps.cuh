@@ -129,7 +129,7 @@ int casadi_gb300_mapsum_scratch_size(int id, int64_t n, int ndir,
   const size_t sweep =
       ndir > 0 ? static_cast<size_t>(8) * t->n_partials * static_cast<size_t>(((n + 31) / 32) * 32)
                : 0;
-  *bytes = sum_bytes(*t, n, ndir, f) + sweep + 256;
+  *bytes = sum_bytes(*t, n, ndir, f) + sweep + 256 + kQueueSlack;
   return 0;
 }
 
@@ -461,7 +461,7 @@ int casadi_gb300_mapaccum_scratch_size(int id, int N, int n_accum, int64_t n, in
     b += 3 * bytes_of(static_cast<long long>(std::max(ndir, 1)) * nz * n);  // tangents/adjoints
   }
   b += static_cast<size_t>(8) * t->n_partials * static_cast<size_t>(((n + 31) / 32) * 32);
-  *bytes = b;
+  *bytes = b + kQueueSlack;
   return 0;
 }
 

@@ -655,9 +655,22 @@ __global__ void __launch_bounds__(32, MB) k_tangent(const __grid_constant__ Swee
   const int ngroups = (a.ndir + K - 1) / K;
   const long long nwork = (ntiles + IPT - 1) / IPT * ngroups;
   const size_t tstride = static_cast<size_t>(a.t.n_partials) * 32;
-  for (long long work = blockIdx.x; work < nwork; work += gridDim.x) {
+  // Direction streams differ in length (a direction seeded late in the tape has little
+  // work), so a fixed stride over the items leaves some CTAs with several times the work of
+  // others. With a queue, a CTA takes its first item by index and every later one from the
+  // counter, claimed before the current walk so the atomic's latency is hidden.
+  long long work = blockIdx.x;
+  while (work < nwork) {
+    long long next = work + gridDim.x;
+    if (a.queue) {
+      unsigned long long q = 0;
+      if (lane == 0) q = atomicAdd(a.queue, 1ull);
+      next = static_cast<long long>(gridDim.x) +
+             static_cast<long long>(__shfl_sync(0xffffffffu, q, 0));
+    }
     const long long tg = work / ngroups;
-    const int grp = static_cast<int>(work % ngroups);
+    const int pos = static_cast<int>(work % ngroups);
+    const int grp = a.gorder ? __ldg(a.gorder + pos) : pos;
     const int dir0 = grp * K;
     bool active[IPT], tok[IPT];
     long long ig[IPT];
@@ -675,6 +688,7 @@ __global__ void __launch_bounds__(32, MB) k_tangent(const __grid_constant__ Swee
     const double* pt = a.partials + static_cast<size_t>(tg * IPT) * tstride + lane;
     tangent_walk<true, G, IPT, K>(st, ngr, pt, tstride, tok, wb, a.seed, a.sens,
                                   a.identity_seed != 0, active, dir0, a.ndir, ig);
+    work = next;
   }
 }
 

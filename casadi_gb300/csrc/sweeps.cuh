@@ -82,6 +82,11 @@ struct SweepArgs {
   unsigned char* wglob;
   long long wglob_stride;
   const int* dirmap;                // cooperative tangent, identity seeds (see launch_tangent_coop)
+  // tangent sweep work queue: items past the grid are claimed from *queue (zeroed before
+  // each launch; null: static stride), direction groups of a tile in the order gorder
+  // (longest entry stream first; null: natural order)
+  unsigned long long* queue;
+  const int* gorder;
 };
 
 // One item of a persistent batch: a tape over its own instance range.

@@ -131,8 +131,10 @@ CASADI_GB300_API int casadi_gb300_tape_levels(const casadi_gb300_atomic* alg, in
 CASADI_GB300_API int casadi_gb300_tape_info(int id, int* n_instr, int* n_in, int* n_out, int* sz_w,
                            int* n_partials);
 
-/* Scratch bytes the AD sweeps need to process n instances in one wave. A smaller scratch
- * buffer is accepted down to casadi_gb300_scratch_min(); the sweep then runs in waves. */
+/* Scratch bytes the AD sweeps need to process n instances in one wave: the recorded partials
+ * and a few bytes past them for the tangent sweep's work counter (a scratch without them runs
+ * that sweep with a static work split, same results). A smaller scratch buffer is accepted
+ * down to casadi_gb300_scratch_min(); the sweep then runs in waves. */
 CASADI_GB300_API int casadi_gb300_scratch_size(int id, int64_t n, size_t* bytes);
 CASADI_GB300_API int casadi_gb300_scratch_min(int id, size_t* bytes);
 

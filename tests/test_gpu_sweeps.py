@@ -311,6 +311,27 @@ def test_edge_sizes_null_io_and_waves(gpu_lib):
     ct2.sync()
 
 
+def test_tangent_work_queue_gives_the_static_split_bits(gpu_lib):
+    """The tangent sweep claims its items from a counter kept past the partials in the
+    scratch; a scratch without those bytes runs the static split. Both, and a queued sweep in
+    several waves, give the same bits (15000 (tile, direction) items: more than the grid)."""
+    F = W.cartpole_rollout(20)
+    n = 20000
+    args = dev(W.cartpole_inputs(n, steps=20, seed=5))
+    ct = CudaTape(F)
+    _, queued = ct.jacobian(args)
+    exact = 8 * ct.n_partials * ((n + 31) // 32 * 32)
+    ct_static = CudaTape(F)
+    _, static = ct_static.jacobian(args, scratch_limit=exact)
+    ct_waves = CudaTape(F)
+    _, waves = ct_waves.jacobian(args, scratch_limit=8 * ct.n_partials * 6720 + 256)
+    for q, s, w in zip(host(queued), host(static), host(waves)):
+        assert_bitexact(q, s, "queued vs static split")
+        assert_bitexact(q, w, "queued in waves")
+    for c in (ct, ct_static, ct_waves):
+        c.sync()
+
+
 def test_scratch_too_small_is_an_error(gpu_lib):
     F = W.cartpole_rollout(2)
     ct = CudaTape(F)
