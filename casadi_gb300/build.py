@@ -15,7 +15,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(ROOT, "_build", "obj")
 LIB = os.path.join(HERE, "libcasadi_gb300.so")
-SOURCES = ["sweeps.cu", "abi.cu", "schedule.cu", "coloring.cu", "reduce.cu"]
+SOURCES = ["sweeps.cu", "abi.cu", "schedule.cu", "coloring.cu", "reduce.cu", "serial.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # --fmad=false: no multiply-add contraction anywhere, so each op rounds like the CPU VM.
 FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",

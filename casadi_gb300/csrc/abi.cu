@@ -21,6 +21,7 @@
 #include "coloring.cuh"
 #include "schedule.cuh"
 #include "reduce.cuh"
+#include "serial.cuh"
 #include "sweeps.cuh"
 
 using namespace cgb;
@@ -1547,6 +1548,232 @@ int casadi_gb300_tape_create_calls(const casadi_gb300_atomic* alg, int n_instr, 
     return fail(CASADI_GB300_ERR_UNSUPPORTED, "inlined tape too long");
   return casadi_gb300_tape_create(out.data(), static_cast<int>(out.size()), n_in, nnz_in, n_out,
                                   nnz_out, static_cast<int>(wlen));
+}
+
+// Tapes from CasADi's serialized text (serial.cu decodes it on the host).
+int casadi_gb300_serialized_describe(const char* text, size_t len, char* buf, size_t cap,
+                                     size_t* need) {
+  SerialModel m;
+  std::string err;
+  if (int rc = decode_serialized(text, len, m, err)) return fail(rc, "%s", err.c_str());
+  const std::string d = describe_serialized(m);
+  if (need) *need = d.size() + 1;
+  if (buf && cap > 0) {
+    const size_t n = std::min(cap - 1, d.size());
+    std::memcpy(buf, d.data(), n);
+    buf[n] = '\0';
+  }
+  return 0;
+}
+
+extern "C++" {
+namespace {
+// The serialized top-level SXFunction, or an error.
+int serialized_sx(const char* text, size_t len, SerialModel& m) {
+  std::string err;
+  if (int rc = decode_serialized(text, len, m, err)) return fail(rc, "%s", err.c_str());
+  if (m.tops.size() != 1)
+    return fail(CASADI_GB300_ERR_ARG, "the text holds %zu Functions (casadi_gb300_push_file "
+                "loads them all)", m.tops.size());
+  if (m.top < 0) return fail(CASADI_GB300_ERR_ARG, "the serialized Function is null");
+  const SerialFunction& f = m.functions[static_cast<size_t>(m.top)];
+  if (!f.complete)
+    return fail(CASADI_GB300_ERR_UNSUPPORTED, "serialized %s '%s': only SXFunction tapes are read",
+                f.cls.c_str(), f.name.c_str());
+  return 0;
+}
+
+std::vector<int> nnz_of(const std::vector<SerialSparsity>& sp) {
+  std::vector<int> n(sp.size());
+  for (size_t j = 0; j < sp.size(); ++j) n[j] = static_cast<int>(sp[j].nnz);
+  return n;
+}
+
+int check_serial_function(const SerialFunction& f) {
+  if (f.n_free > 0)
+    return fail(CASADI_GB300_ERR_UNSUPPORTED,
+                "'%s' has %lld free variables (the reference cannot evaluate it either)",
+                f.name.c_str(), f.n_free);
+  if (f.alg.size() > static_cast<size_t>(1 << 30) || f.sz_w > (1LL << 30))
+    return fail(CASADI_GB300_ERR_UNSUPPORTED, "'%s' is too large", f.name.c_str());
+  for (const auto& sp : f.sp_in)
+    if (sp.nnz > (1LL << 30)) return fail(CASADI_GB300_ERR_UNSUPPORTED, "input too large");
+  for (const auto& sp : f.sp_out)
+    if (sp.nnz > (1LL << 30)) return fail(CASADI_GB300_ERR_UNSUPPORTED, "output too large");
+  return 0;
+}
+
+// Tape of function k of the model (callees first, memoized in ids; -1: not created yet).
+int serial_tape(const SerialModel& m, int k, std::vector<int>& ids) {
+  if (ids[static_cast<size_t>(k)] >= 0) return ids[static_cast<size_t>(k)];
+  const SerialFunction& f = m.functions[static_cast<size_t>(k)];
+  if (!f.complete)
+    return fail(CASADI_GB300_ERR_UNSUPPORTED, "'%s' (%s) is not an SXFunction", f.name.c_str(),
+                f.cls.c_str());
+  if (int rc = check_serial_function(f)) return rc;
+  const std::vector<int> nin = nnz_of(f.sp_in), nout = nnz_of(f.sp_out);
+  std::vector<int> call_ids(f.calls.size());
+  std::vector<const int*> deps(f.calls.size()), ress(f.calls.size());
+  for (size_t c = 0; c < f.calls.size(); ++c) {
+    const SerialCall& call = f.calls[c];
+    if (call.fn < 0 || call.fn >= k)
+      return fail(CASADI_GB300_ERR_ARG, "'%s': call %zu names no earlier function",
+                  f.name.c_str(), c);
+    const SerialFunction& g = m.functions[static_cast<size_t>(call.fn)];
+    long long nzi = 0, nzo = 0;
+    for (const auto& sp : g.sp_in) nzi += sp.nnz;
+    for (const auto& sp : g.sp_out) nzo += sp.nnz;
+    if (static_cast<long long>(call.dep.size()) != nzi ||
+        static_cast<long long>(call.res.size()) != nzo)
+      return fail(CASADI_GB300_ERR_ARG, "'%s': call %zu has %zu/%zu slots for %lld/%lld nonzeros",
+                  f.name.c_str(), c, call.dep.size(), call.res.size(), nzi, nzo);
+    const int id = serial_tape(m, call.fn, ids);
+    if (id < 0) return id;
+    call_ids[c] = id;
+    deps[c] = call.dep.data();
+    ress[c] = call.res.data();
+  }
+  const int id = f.calls.empty()
+      ? casadi_gb300_tape_create(f.alg.data(), static_cast<int>(f.alg.size()),
+                                 static_cast<int>(nin.size()), nin.data(),
+                                 static_cast<int>(nout.size()), nout.data(),
+                                 static_cast<int>(f.sz_w))
+      : casadi_gb300_tape_create_calls(
+            f.alg.data(), static_cast<int>(f.alg.size()), static_cast<int>(nin.size()),
+            nin.data(), static_cast<int>(nout.size()), nout.data(), static_cast<int>(f.sz_w),
+            static_cast<int>(f.calls.size()), call_ids.data(), deps.data(), ress.data());
+  if (id >= 0) ids[static_cast<size_t>(k)] = id;
+  return id;
+}
+}  // namespace
+}  // extern "C++"
+
+int casadi_gb300_serialized_decode(const char* text, size_t len, casadi_gb300_atomic* alg,
+                                   int cap, int* n_instr, int* n_in, int* nnz_in, int* n_out,
+                                   int* nnz_out, int* sz_w) {
+  SerialModel m;
+  if (int rc = serialized_sx(text, len, m)) return rc;
+  const SerialFunction& f = m.functions[static_cast<size_t>(m.top)];
+  if (int rc = check_serial_function(f)) return rc;
+  if (!f.calls.empty())
+    return fail(CASADI_GB300_ERR_UNSUPPORTED,
+                "'%s' calls %zu functions: use casadi_gb300_tape_deserialize", f.name.c_str(),
+                f.calls.size());
+  if (n_instr) *n_instr = static_cast<int>(f.alg.size());
+  if (n_in) *n_in = static_cast<int>(f.sp_in.size());
+  if (n_out) *n_out = static_cast<int>(f.sp_out.size());
+  if (sz_w) *sz_w = static_cast<int>(f.sz_w);
+  if (nnz_in)
+    for (size_t j = 0; j < f.sp_in.size(); ++j) nnz_in[j] = static_cast<int>(f.sp_in[j].nnz);
+  if (nnz_out)
+    for (size_t j = 0; j < f.sp_out.size(); ++j) nnz_out[j] = static_cast<int>(f.sp_out[j].nnz);
+  if (alg) {
+    if (cap < static_cast<int>(f.alg.size()))
+      return fail(CASADI_GB300_ERR_ARG, "instruction buffer of %d for %zu instructions", cap,
+                  f.alg.size());
+    std::memcpy(alg, f.alg.data(), f.alg.size() * sizeof(casadi_gb300_atomic));
+  }
+  return 0;
+}
+
+// Functions loaded from files, as casadi_c keeps them (casadi/core/casadi_c.cpp:31-130):
+// names and tape ids, and how many each push added
+extern "C++" {
+namespace {
+std::mutex g_loaded_mtx;
+std::vector<std::pair<std::string, int>> g_loaded;
+std::vector<int> g_load_stack;
+}  // namespace
+}  // extern "C++"
+
+int casadi_gb300_push_file(const char* filename) {
+  if (!filename) return fail(CASADI_GB300_ERR_ARG, "null file name");
+  std::string text;
+  {
+    FILE* fh = std::fopen(filename, "rb");
+    if (!fh) return fail(CASADI_GB300_ERR_ARG, "could not open '%s'", filename);
+    char buf[1 << 16];
+    size_t got;
+    while ((got = std::fread(buf, 1, sizeof(buf), fh)) > 0) text.append(buf, got);
+    std::fclose(fh);
+  }
+  SerialModel m;
+  std::string err;
+  if (int rc = decode_serialized(text.data(), text.size(), m, err))
+    return fail(rc, "%s: %s", filename, err.c_str());
+  if (!m.saved_form)
+    return fail(CASADI_GB300_ERR_ARG, "%s holds no 'function' or 'function_vector'", filename);
+  std::vector<int> ids(m.functions.size(), -1);
+  std::vector<std::pair<std::string, int>> added;
+  int rc = 0;
+  for (int k : m.tops) {
+    if (k < 0) {
+      rc = fail(CASADI_GB300_ERR_ARG, "%s holds a null Function", filename);
+      break;
+    }
+    const int id = serial_tape(m, k, ids);
+    if (id < 0) {
+      rc = id;
+      break;
+    }
+    added.emplace_back(m.functions[static_cast<size_t>(k)].name, id);
+  }
+  // keep the tapes of the file's Functions, free the called ones (they were inlined)
+  for (size_t k = 0; k < ids.size(); ++k) {
+    if (ids[k] < 0) continue;
+    bool keep = false;
+    for (const auto& a : added) keep = keep || (rc == 0 && a.second == ids[k]);
+    if (!keep) casadi_gb300_tape_free(ids[k]);
+  }
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(g_loaded_mtx);
+  g_loaded.insert(g_loaded.end(), added.begin(), added.end());
+  g_load_stack.push_back(static_cast<int>(added.size()));
+  return 0;
+}
+
+int casadi_gb300_n_loaded(void) {
+  std::lock_guard<std::mutex> lk(g_loaded_mtx);
+  return static_cast<int>(g_loaded.size());
+}
+
+int casadi_gb300_loaded_tape(const char* name) {
+  std::lock_guard<std::mutex> lk(g_loaded_mtx);
+  if (!name) return fail(CASADI_GB300_ERR_ARG, "null name");
+  for (const auto& a : g_loaded)
+    if (a.first == name) return a.second;
+  std::string avail;
+  for (const auto& a : g_loaded) avail += " " + a.first;
+  return fail(CASADI_GB300_ERR_ID, "no loaded function named '%s' (loaded:%s)", name,
+              avail.c_str());
+}
+
+const char* casadi_gb300_loaded_name(int k) {
+  std::lock_guard<std::mutex> lk(g_loaded_mtx);
+  if (k < 0 || k >= static_cast<int>(g_loaded.size())) return nullptr;
+  return g_loaded[static_cast<size_t>(k)].first.c_str();
+}
+
+int casadi_gb300_pop_file(void) {
+  std::lock_guard<std::mutex> lk(g_loaded_mtx);
+  if (g_load_stack.empty()) return fail(CASADI_GB300_ERR_ARG, "nothing was pushed");
+  for (int c = g_load_stack.back(); c > 0; --c) {
+    casadi_gb300_tape_free(g_loaded.back().second);
+    g_loaded.pop_back();
+  }
+  g_load_stack.pop_back();
+  return 0;
+}
+
+int casadi_gb300_tape_deserialize(const char* text, size_t len) {
+  SerialModel m;
+  if (int rc = serialized_sx(text, len, m)) return rc;
+  std::vector<int> ids(m.functions.size(), -1);
+  const int id = serial_tape(m, m.top, ids);
+  // the called functions' tapes were inlined into the caller's
+  for (size_t k = 0; k < ids.size(); ++k)
+    if (ids[k] >= 0 && static_cast<int>(k) != m.top) casadi_gb300_tape_free(ids[k]);
+  return id;
 }
 
 int casadi_gb300_tape_free(int id) {

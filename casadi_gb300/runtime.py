@@ -61,6 +61,15 @@ def load(path=None):
         "casadi_gb300_tape_free": (cint, [cint]),
         "casadi_gb300_tape_create_calls": (cint, [vp, cint, cint, vp, cint, vp, cint, cint, vp, vp,
                                                   vp]),
+        "casadi_gb300_tape_deserialize": (cint, [ct.c_char_p, sz]),
+        "casadi_gb300_serialized_decode": (cint, [ct.c_char_p, sz, vp, cint, vp, vp, vp, vp, vp,
+                                                  vp]),
+        "casadi_gb300_serialized_describe": (cint, [ct.c_char_p, sz, vp, sz, vp]),
+        "casadi_gb300_push_file": (cint, [ct.c_char_p]),
+        "casadi_gb300_pop_file": (cint, []),
+        "casadi_gb300_n_loaded": (cint, []),
+        "casadi_gb300_loaded_tape": (cint, [ct.c_char_p]),
+        "casadi_gb300_loaded_name": (ct.c_char_p, [cint]),
         "casadi_gb300_tape_schedule": (cint, [vp, cint, cint, vp, cint, vp, cint, vp, vp]),
         "casadi_gb300_tape_info": (cint, [cint, vp, vp, vp, vp, vp]),
         "casadi_gb300_tape_levels": (cint, [vp, cint, cint, vp, cint, vp, cint, cint, cint, vp,
@@ -192,8 +201,110 @@ def levels(tape, width=32, slot_cap=None):
     return lt, src[:tape.n_instr], begin[:nl.value + 1]
 
 
+def _serial_text(text):
+    """Serialized text as bytes: a str/bytes of CasADi's serialization, or a path to a file
+    that Function::save wrote."""
+    if isinstance(text, os.PathLike) or (isinstance(text, str) and os.path.exists(text)):
+        with open(text, "rb") as fh:
+            return fh.read()
+    return text.encode() if isinstance(text, str) else bytes(text)
+
+
+def describe_serialized(text):
+    """Summary of a serialized CasADi Function (any class) as a dict: ``functions`` (class,
+    name, inputs/outputs with their names and sparsity sizes, and for SXFunctions the
+    instruction count, work-vector size and called functions), ``top`` (index of the
+    serialized one), ``debug``, ``saved_form``. Host only."""
+    import json
+    b = _serial_text(text)
+    lib = load()
+    need = ct.c_size_t()
+    check(lib.casadi_gb300_serialized_describe(b, len(b), None, 0, ct.byref(need)))
+    buf = ct.create_string_buffer(need.value)
+    check(lib.casadi_gb300_serialized_describe(b, len(b), buf, need.value, None))
+    return json.loads(buf.value.decode())
+
+
+def decode_serialized(text):
+    """The :class:`sx.Tape` of a serialized SXFunction without calls, decoded on the host (the
+    algorithm, nonzero counts and work-vector size CasADi wrote)."""
+    b = _serial_text(text)
+    lib = load()
+    n, nin, nout, szw = ct.c_int(), ct.c_int(), ct.c_int(), ct.c_int()
+    check(lib.casadi_gb300_serialized_decode(b, len(b), None, 0, ct.byref(n), ct.byref(nin),
+                                             None, ct.byref(nout), None, ct.byref(szw)))
+    atoms = np.zeros(n.value, dtype=np.dtype([("op", "<i4"), ("i0", "<i4"), ("u", "<u8")]))
+    nnz_in = np.zeros(max(1, nin.value), dtype=np.int32)
+    nnz_out = np.zeros(max(1, nout.value), dtype=np.int32)
+    check(lib.casadi_gb300_serialized_decode(b, len(b), atoms.ctypes.data, n.value, None, None,
+                                             nnz_in.ctypes.data, None, nnz_out.ctypes.data,
+                                             None))
+    return _sx.Tape.from_atomic_array(atoms, nnz_in[:nin.value].tolist(),
+                                      nnz_out[:nout.value].tolist(), szw.value)
+
+
+def push_file(path):
+    """Load every SXFunction of a file Function::save or a FileSerializer wrote (one Function
+    or a vector of them) into the library's list of loaded functions, as casadi_c_push_file
+    does; returns {name: CudaTape} for the functions of this file. The tapes belong to the
+    list (pop_file frees them)."""
+    lib = load()
+    check(lib.casadi_gb300_push_file(os.fsencode(path)))
+    d = describe_serialized(path)
+    out = {}
+    for k in d["tops"]:
+        f = d["functions"][k]
+        out[f["name"]] = CudaTape._wrap(check(lib.casadi_gb300_loaded_tape(f["name"].encode())),
+                                        f, None, owned=False)
+    return out
+
+
+def pop_file():
+    """Free the tapes the last push_file loaded."""
+    check(load().casadi_gb300_pop_file())
+
+
+def loaded_names():
+    lib = load()
+    return [lib.casadi_gb300_loaded_name(k).decode() for k in range(lib.casadi_gb300_n_loaded())]
+
+
 class CudaTape:
     """A tape registered with the GPU library (one CUDA device)."""
+
+    @classmethod
+    def deserialize(cls, text):
+        """The tape of a serialized SXFunction (the text Function::serialize() returns, or a
+        file Function::save wrote); SXFunctions it calls are decoded and inlined."""
+        b = _serial_text(text)
+        lib = load()
+        tid = check(lib.casadi_gb300_tape_deserialize(b, len(b)))
+        top = describe_serialized(b)
+        return cls._wrap(tid, top["functions"][top["top"]], b)
+
+    @classmethod
+    def _wrap(cls, tid, f, text, owned=True):
+        """A CudaTape object for tape `tid` of the serialized function described by `f`."""
+        lib = load()
+        self = cls.__new__(cls)
+        self.id = tid
+        self._owned = owned
+        nnz_in = [io["nnz"] for io in f["inputs"]]
+        nnz_out = [io["nnz"] for io in f["outputs"]]
+        self.name = f["name"]
+        self.name_in = [io["name"] for io in f["inputs"]]
+        self.name_out = [io["name"] for io in f["outputs"]]
+        self.tape = decode_serialized(text) if text is not None and not f["calls"] else \
+            _sx.Tape.from_atomic_array(np.zeros(0, dtype=np.dtype([("op", "<i4"), ("i0", "<i4"),
+                                                                    ("u", "<u8")])),
+                                       nnz_in, nnz_out, f["sz_w"])
+        self._nnz_in = np.ascontiguousarray(nnz_in, dtype=np.int32)
+        self._nnz_out = np.ascontiguousarray(nnz_out, dtype=np.int32)
+        vals = [ct.c_int() for _ in range(5)]
+        check(lib.casadi_gb300_tape_info(self.id, *[ct.byref(v) for v in vals]))
+        self.n_instr, self.n_in, self.n_out, self.sz_w, self.n_partials = [v.value for v in vals]
+        self._scratch = None
+        return self
 
     def __init__(self, tape, calls=None):
         """``tape``: an :class:`sx.Function` or :class:`sx.Tape`. ``calls``: for tapes with
@@ -228,7 +339,8 @@ class CudaTape:
 
     def __del__(self):
         try:
-            if getattr(self, "id", None) is not None and _lib is not None:
+            if (getattr(self, "id", None) is not None and _lib is not None
+                    and getattr(self, "_owned", True)):
                 _lib.casadi_gb300_tape_free(self.id)
         except Exception:
             pass

@@ -98,6 +98,48 @@ CASADI_GB300_API int casadi_gb300_tape_create_calls(const casadi_gb300_atomic* a
                            const int* nnz_out, int sz_w, int n_calls, const int* call_tape,
                            const int* const* call_dep, const int* const* call_res);
 
+/* Tapes from CasADi's serialized text: what Function::serialize() returns
+ * (casadi/core/function.cpp:1477-1489) or what Function::save writes to a .casadi file
+ * (serializer.cpp, FileSerializer; Function::load, function.cpp:1541-1549), both in either
+ * debug mode, read without libcasadi. `text`/`len`: the characters (trailing whitespace is
+ * ignored).
+ *
+ * Create the tape of a serialized SXFunction (SXFunction(DeserializingStream&),
+ * casadi/core/sx_function.cpp:1926-1997): its algorithm as casadi_gb300_tape_create takes it,
+ * with the SXFunctions it calls (OP_CALL) decoded and inlined as casadi_gb300_tape_create_calls
+ * does. Returns the tape id, or a negative status: ERR_ARG for malformed text,
+ * ERR_UNSUPPORTED for a Function of another class, free variables, or nested Functions that
+ * are not SXFunctions. */
+CASADI_GB300_API int casadi_gb300_tape_deserialize(const char* text, size_t len);
+
+/* Loading serialized files as casadi_c does (casadi/casadi_c.h:52-86, casadi/core/
+ * casadi_c.cpp:73-130), for SXFunctions: push_file reads a file Function::save or a
+ * FileSerializer wrote (one Function or a vector of them) and creates a tape for each
+ * Function in it; pop_file frees the tapes the last push created. Returns 0 or a negative
+ * status (a file with a Function that is not an SXFunction loads nothing). */
+CASADI_GB300_API int casadi_gb300_push_file(const char* filename);
+CASADI_GB300_API int casadi_gb300_pop_file(void);
+/* Number of loaded Functions; the tape id of the one named `name` (ERR_ID if none, like
+ * casadi_c_id); the name of loaded Function k (NULL if out of range; valid until the next
+ * push or pop). */
+CASADI_GB300_API int casadi_gb300_n_loaded(void);
+CASADI_GB300_API int casadi_gb300_loaded_tape(const char* name);
+CASADI_GB300_API const char* casadi_gb300_loaded_name(int k);
+
+/* The algorithm of a serialized SXFunction without OP_CALL instructions, on the host (no GPU
+ * needed): call with alg == NULL for the sizes (n_instr, n_in, n_out, sz_w), then with alg
+ * holding cap >= n_instr entries; nnz_in/nnz_out (if not NULL) receive n_in/n_out counts. */
+CASADI_GB300_API int casadi_gb300_serialized_decode(const char* text, size_t len,
+                           casadi_gb300_atomic* alg, int cap, int* n_instr, int* n_in,
+                           int* nnz_in, int* n_out, int* nnz_out, int* sz_w);
+
+/* A JSON summary of serialized text (any Function class: the class, name, input and output
+ * names and sparsity sizes, the versions of the bodies read; for SXFunctions the instruction
+ * count, work-vector size, free variables and called functions). Writes at most cap bytes
+ * (NUL-terminated) to buf; *need receives the full length + 1. */
+CASADI_GB300_API int casadi_gb300_serialized_describe(const char* text, size_t len, char* buf,
+                           size_t cap, size_t* need);
+
 /* The tape as the GPU sweeps run it: casadi_gb300_tape_create reorders the instructions so
  * fewer values are live at once (the work vector of every 32-instance tile sits in shared
  * memory, and its length decides how many tiles an SM runs at a time) and reassigns the slots.

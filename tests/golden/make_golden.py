@@ -3,7 +3,7 @@
 Run where the reference source tree is available (it builds oracle/_ref from the reference's
 casadi/core/calculus.hpp):
 
-    python tests/golden/make_golden.py [ops] [enum] [tapes] [activity]   # default: all
+    python tests/golden/make_golden.py [ops] [enum] [tapes] [activity] [serial]  # default: all
 
 Fixtures:
   ops.npz        value and partials of every scalar op over a grid of special and ordinary
@@ -22,6 +22,12 @@ Fixtures:
                  forward sensitivities, adjoint sensitivities and the unit-seed Jacobian
                  (numeric sweeps with partials from CASADI_MATH_DER_BUILTIN and the
                  structural-zero rules of the reference's derivative expressions).
+  serialized_issue3074.txt
+                 the one serialized Function the reference's tests hold (test/python/
+                 function.py, test_issue_3074: the text passed to StringDeserializer), copied
+                 verbatim: an MXFunction written by an earlier CasADi in the saved form (type
+                 byte, shared Function), with ProtoFunction body version 1 and FunctionInternal
+                 body version 2.
 """
 import math
 import os
@@ -178,12 +184,32 @@ def activity_case():
     return out
 
 
+REFERENCE = os.environ.get("CASADI_REFERENCE", "/root/reference")
+
+
+def serialized_fixture():
+    """The serialized text of test_issue_3074 in the reference's test/python/function.py."""
+    path = os.path.join(REFERENCE, "test", "python", "function.py")
+    lines = open(path).read().splitlines()
+    start = next(i for i, l in enumerate(lines) if "def test_issue_3074" in l)
+    for line in lines[start:]:
+        stripped = line.strip()
+        if stripped.startswith("data = \""):
+            return stripped.split("\"")[1]
+    raise SystemExit("no serialized text in test_issue_3074")
+
+
 def main(which=None):
-    which = set(which or ("ops", "enum", "tapes", "activity"))
-    O.build(ref=True)
-    if not O.ref_available():
-        raise SystemExit("the reference harness could not be built")
+    which = set(which or ("ops", "enum", "tapes", "activity", "serial"))
     written = []
+    if "serial" in which:
+        with open(os.path.join(HERE, "serialized_issue3074.txt"), "w") as fh:
+            fh.write(serialized_fixture() + "\n")
+        written.append("serialized_issue3074.txt")
+    if which - {"serial"}:
+        O.build(ref=True)
+        if not O.ref_available():
+            raise SystemExit("the reference harness could not be built")
     if "ops" in which:
         np.savez_compressed(os.path.join(HERE, "ops.npz"), **op_grid())
         written.append("ops.npz")

@@ -81,3 +81,49 @@ def assert_close(a, b, what="", rtol=RTOL, floor=None):
     e = rel_err(a, b, floor)
     assert e <= rtol, "%s: relative error %.3e > %.1e (floor %.3e)" % (what, e, rtol, floor)
     return e
+
+
+def call_rollout(steps):
+    """Caller tape of a `steps`-step cart-pole rollout written as OP_CALL instructions of the
+    one-step function (call index in i1): x0 (4 slots), U (steps slots), one call per step,
+    xN out. Returns the tape and each call's (dep slots, res slots)."""
+    op, i0, i1, i2 = [], [], [], []
+
+    def emit(o, a, b, c):
+        op.append(o), i0.append(a), i1.append(b), i2.append(c)
+
+    for k in range(4):
+        emit(C.OP_INPUT, k, 0, k)
+    for k in range(steps):
+        emit(C.OP_INPUT, 4 + k, 1, k)
+    x = [0, 1, 2, 3]
+    nxt = 4 + steps
+    calls = []
+    for k in range(steps):
+        res = list(range(nxt, nxt + 4))
+        calls.append((x + [4 + k], res))
+        emit(C.OP_CALL, 0, k, 0)
+        x, nxt = res, nxt + 4
+    for k in range(4):
+        emit(C.OP_OUTPUT, 0, x[k], k)
+    tape = S.Tape(op, i0, i1, i2, np.zeros(len(op)), [4, steps], [4], nxt)
+    return tape, calls
+
+
+def call_rollout_serializable(steps):
+    """The caller of :func:`call_rollout` with its expression graph (CallSX/OutputSX nodes of
+    the step function) as the writer of oracle.serialize takes it, and the step function."""
+    from oracle import serialize as SZ
+    from casadi_gb300 import workloads as W
+    step = W.cartpole_step()
+    step_s = SZ.from_function(step)
+    tape, calls = call_rollout(steps)
+    x0, U = S.sym("x0", 4), S.sym("U", steps)
+    x = list(x0)
+    for k in range(steps):
+        c = SZ.CallNode(step_s, x + [U[k]])
+        x = [SZ.OutputNode(c, j) for j in range(4)]
+    caller = SZ.Serializable("rollout_calls", tape, [x0, U], [x],
+                             calls=[(step_s, d, r) for d, r in calls],
+                             name_in=["x0", "U"], name_out=["xN"])
+    return caller, step, calls

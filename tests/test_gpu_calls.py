@@ -11,41 +11,16 @@ from casadi_gb300 import runtime as R
 from casadi_gb300 import sx as S
 from casadi_gb300 import workloads as W
 
-from helpers import RTOL, assert_bitexact, assert_close
+from helpers import RTOL, assert_bitexact, assert_close, call_rollout
 
 pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
 
-def _call_rollout(steps):
-    """Caller tape: x0 (4 slots), U (steps slots), one OP_CALL per step, xN out."""
-    op, i0, i1, i2 = [], [], [], []
-
-    def emit(o, a, b, c):
-        op.append(o), i0.append(a), i1.append(b), i2.append(c)
-
-    for k in range(4):
-        emit(C.OP_INPUT, k, 0, k)
-    for k in range(steps):
-        emit(C.OP_INPUT, 4 + k, 1, k)
-    x = [0, 1, 2, 3]
-    nxt = 4 + steps
-    calls = []
-    for k in range(steps):
-        res = list(range(nxt, nxt + 4))
-        calls.append((x + [4 + k], res))
-        emit(C.OP_CALL, 0, k, 0)
-        x, nxt = res, nxt + 4
-    for k in range(4):
-        emit(C.OP_OUTPUT, 0, x[k], k)
-    tape = S.Tape(op, i0, i1, i2, np.zeros(len(op)), [4, steps], [4], nxt)
-    return tape, calls
-
-
 def test_call_rollout_matches_chained_steps_and_oracle(gpu_lib):
     steps, n = 3, 2049
     step = R.CudaTape(W.cartpole_step())
-    tape, calls = _call_rollout(steps)
+    tape, calls = call_rollout(steps)
     ct = R.CudaTape(tape, calls=[(step, d, r) for d, r in calls])
     x0, U = W.cartpole_inputs(n, steps=steps, seed=13)
     args = [torch.from_numpy(x0).cuda(), torch.from_numpy(U).cuda()]
@@ -69,6 +44,6 @@ def test_call_rollout_matches_chained_steps_and_oracle(gpu_lib):
 
 def test_bad_call_tables_are_refused(gpu_lib):
     step = R.CudaTape(W.cartpole_step())
-    tape, calls = _call_rollout(1)
+    tape, calls = call_rollout(1)
     with pytest.raises(R.CasadiGpuError):
         R.CudaTape(tape, calls=[(step, [0, 1, 2, 3, 99], calls[0][1])])  # dep slot out of range
