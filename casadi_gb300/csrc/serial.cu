@@ -373,6 +373,18 @@ class Reader {
     for (long long k = 0; k < n; ++k) sx_matrix();
   }
 
+  // Functions and GenericType values nest by recursion; a depth limit keeps corrupted or
+  // hostile text from exhausting the stack
+  static constexpr int kMaxDepth = 200;
+  int depth_ = 0;
+  struct Nest {
+    Reader& r;
+    explicit Nest(Reader& rr) : r(rr) {
+      if (++r.depth_ > kMaxDepth) r.fail("objects nested deeper than " + std::to_string(kMaxDepth));
+    }
+    ~Nest() { --r.depth_; }
+  };
+
   void generic(const char* d) {
     descr(d);
     deco('G');
@@ -380,6 +392,7 @@ class Reader {
       reference('G');
       return;
     }
+    Nest nest(*this);
     const int type = i32("GenericType::type");
     const char* v = "GenericType::d";
     switch (type) {
@@ -452,6 +465,7 @@ class Reader {
     const bool partial_ok = partial_ok_;
     partial_ok_ = false;  // nested Functions are always read completely
     if (boolean("Function::null")) return -1;
+    Nest nest(*this);
     SerialFunction f;
     f.cls = str("FunctionInternal::base_function");
     const bool sx = f.cls == "SXFunction";

@@ -169,3 +169,18 @@ def test_push_file_refuses_other_classes(lib, tmp_path):
     with pytest.raises(R.CasadiGpuError, match="no 'function'"):
         R.push_file(str(p))
     assert len(R.loaded_names()) == n0
+
+
+def test_deep_nesting_is_an_error_not_a_crash(lib):
+    """Option dictionaries nest by recursion in the reader: 300 levels are refused, 50 read."""
+    def nested(depth):
+        d = {"leaf": 1.5}
+        for k in range(depth):
+            d = {"level%d" % k: d}
+        return d
+    F = W.cartpole_step()
+    ok = SZ.serialize(SZ.from_function(F, jit_options=nested(50)))
+    assert R.decode_serialized(ok).n_instr == F.tape.n_instr
+    deep = SZ.serialize(SZ.from_function(F, jit_options=nested(300)))
+    with pytest.raises(R.CasadiGpuError, match="nested deeper"):
+        R.describe_serialized(deep)
