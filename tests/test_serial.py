@@ -178,9 +178,15 @@ def test_deep_nesting_is_an_error_not_a_crash(lib):
         for k in range(depth):
             d = {"level%d" % k: d}
         return d
+    import sys
     F = W.cartpole_step()
-    ok = SZ.serialize(SZ.from_function(F, jit_options=nested(50)))
+    limit = sys.getrecursionlimit()
+    sys.setrecursionlimit(max(limit, 10000))  # the writer recurses into nested values too
+    try:
+        ok = SZ.serialize(SZ.from_function(F, jit_options=nested(50)))
+        deep = SZ.serialize(SZ.from_function(F, jit_options=nested(300)))
+    finally:
+        sys.setrecursionlimit(limit)
     assert R.decode_serialized(ok).n_instr == F.tape.n_instr
-    deep = SZ.serialize(SZ.from_function(F, jit_options=nested(300)))
     with pytest.raises(R.CasadiGpuError, match="nested deeper"):
         R.describe_serialized(deep)
