@@ -190,3 +190,24 @@ def test_deep_nesting_is_an_error_not_a_crash(lib):
     assert R.decode_serialized(ok).n_instr == F.tape.n_instr
     with pytest.raises(R.CasadiGpuError, match="nested deeper"):
         R.describe_serialized(deep)
+
+
+@pytest.mark.parametrize("debug", [False, True])
+def test_empty_io_and_constant_kinds(lib, debug):
+    """An empty input and an empty output (0x1 patterns, as in the reference's blob) and
+    constants of every ConstantSX kind the writer emits (0, 1, -1, integers, reals, inf, nan):
+    the tape's constants come back bit for bit from the algorithm's i1/i2 words."""
+    from casadi_gb300 import sx as S
+    x = S.sym("x", 2)
+    outs = [[x[0] * 2.5 + 1.0, x[1] - 1.0, x[0] * 0.0 + 3.0, x[1] * float("inf"),
+             x[0] + (-7.0), x[1] * float("nan"), x[0] * -1.0 + 0.1], []]
+    F = S.Function("edge", [[], x], outs)
+    text = SZ.serialize(F, debug=debug)
+    t = R.decode_serialized(text)
+    want, got = SZ.tape_arrays(F.tape), SZ.tape_arrays(t)
+    for a, b in zip(want[:3], got[:3]):
+        assert np.array_equal(a, b)
+    assert got[3] == [0, 2] and got[4] == [7, 0]
+    f = R.describe_serialized(text)["functions"][0]
+    assert [i["size"] for i in f["inputs"]] == [[0, 1], [2, 1]]
+    assert [o["nnz"] for o in f["outputs"]] == [7, 0]
