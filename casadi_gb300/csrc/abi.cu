@@ -1603,10 +1603,9 @@ int check_serial_function(const SerialFunction& f) {
   return 0;
 }
 
-// Tape of function k of the model (callees first, memoized in ids; -1: not created yet).
-int serial_tape(const SerialModel& m, int k, std::vector<int>& ids) {
-  if (ids[static_cast<size_t>(k)] >= 0) return ids[static_cast<size_t>(k)];
-  const SerialFunction& f = m.functions[static_cast<size_t>(k)];
+// Tape of function j of the model, its callees' tapes already in ids (they precede it).
+int serial_tape_one(const SerialModel& m, int j, std::vector<int>& ids) {
+  const SerialFunction& f = m.functions[static_cast<size_t>(j)];
   if (!f.complete)
     return fail(CASADI_GB300_ERR_UNSUPPORTED, "'%s' (%s) is not an SXFunction", f.name.c_str(),
                 f.cls.c_str());
@@ -1616,9 +1615,6 @@ int serial_tape(const SerialModel& m, int k, std::vector<int>& ids) {
   std::vector<const int*> deps(f.calls.size()), ress(f.calls.size());
   for (size_t c = 0; c < f.calls.size(); ++c) {
     const SerialCall& call = f.calls[c];
-    if (call.fn < 0 || call.fn >= k)
-      return fail(CASADI_GB300_ERR_ARG, "'%s': call %zu names no earlier function",
-                  f.name.c_str(), c);
     const SerialFunction& g = m.functions[static_cast<size_t>(call.fn)];
     long long nzi = 0, nzo = 0;
     for (const auto& sp : g.sp_in) nzi += sp.nnz;
@@ -1627,9 +1623,7 @@ int serial_tape(const SerialModel& m, int k, std::vector<int>& ids) {
         static_cast<long long>(call.res.size()) != nzo)
       return fail(CASADI_GB300_ERR_ARG, "'%s': call %zu has %zu/%zu slots for %lld/%lld nonzeros",
                   f.name.c_str(), c, call.dep.size(), call.res.size(), nzi, nzo);
-    const int id = serial_tape(m, call.fn, ids);
-    if (id < 0) return id;
-    call_ids[c] = id;
+    call_ids[c] = ids[static_cast<size_t>(call.fn)];
     deps[c] = call.dep.data();
     ress[c] = call.res.data();
   }
@@ -1642,8 +1636,32 @@ int serial_tape(const SerialModel& m, int k, std::vector<int>& ids) {
             f.alg.data(), static_cast<int>(f.alg.size()), static_cast<int>(nin.size()),
             nin.data(), static_cast<int>(nout.size()), nout.data(), static_cast<int>(f.sz_w),
             static_cast<int>(f.calls.size()), call_ids.data(), deps.data(), ress.data());
-  if (id >= 0) ids[static_cast<size_t>(k)] = id;
-  return id;
+  if (id < 0) return id;
+  ids[static_cast<size_t>(j)] = id;
+  return 0;
+}
+
+// Tape of function k of the model, memoized in ids (-1: not created yet). A callee always
+// precedes its caller in the model, so the functions k reaches are marked in one descending
+// pass and created in index order: no recursion along call chains of any length.
+int serial_tape(const SerialModel& m, int k, std::vector<int>& ids) {
+  std::vector<char> need(m.functions.size(), 0);
+  need[static_cast<size_t>(k)] = 1;
+  for (int j = k; j >= 0; --j) {
+    if (!need[static_cast<size_t>(j)] || ids[static_cast<size_t>(j)] >= 0) continue;
+    const SerialFunction& f = m.functions[static_cast<size_t>(j)];
+    for (size_t c = 0; c < f.calls.size(); ++c) {
+      const int fn = f.calls[c].fn;
+      if (fn < 0 || fn >= j)
+        return fail(CASADI_GB300_ERR_ARG, "'%s': call %zu names no earlier function",
+                    f.name.c_str(), c);
+      need[static_cast<size_t>(fn)] = 1;
+    }
+  }
+  for (int j = 0; j <= k; ++j)
+    if (need[static_cast<size_t>(j)] && ids[static_cast<size_t>(j)] < 0)
+      if (int rc = serial_tape_one(m, j, ids)) return rc;
+  return ids[static_cast<size_t>(k)];
 }
 }  // namespace
 }  // extern "C++"
