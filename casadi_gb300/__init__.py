@@ -10,7 +10,9 @@
 * :mod:`casadi_gb300.workloads`  synthetic tapes and seeded inputs
 
 :func:`map` and :func:`mapaccum` follow ``Function::map`` / ``Function::mapaccum``
-(casadi/core/function.cpp:668-895) for the ``"cuda"`` parallelization.
+(casadi/core/function.cpp:668-895) for the ``"cuda"`` parallelization; :func:`load` and
+:func:`deserialize` follow ``Function::load`` / ``Function::deserialize`` (function.cpp:
+1541-1560) for SXFunctions, giving their tapes on the GPU.
 """
 __version__ = "0.1.0"
 
@@ -35,3 +37,19 @@ def mapaccum(f, N, n_accum=1):
     first ``n_accum`` outputs feeding the first ``n_accum`` inputs (:class:`runtime.CudaMapaccum`)."""
     from . import runtime as R
     return R.CudaMapaccum(f, N, n_accum)
+
+
+def load(path):
+    """``Function.load(path)`` (casadi/core/function.cpp:1541-1549) for a file that
+    ``Function::save`` wrote holding one SXFunction: its tape as a :class:`runtime.CudaTape`
+    (called SXFunctions inlined). Files holding several Functions: :func:`runtime.push_file`."""
+    from . import runtime as R
+    with open(path, "rb") as fh:
+        return R.CudaTape.deserialize(fh.read())
+
+
+def deserialize(text):
+    """``Function.deserialize(text)`` (function.cpp:1556-1560): the tape of the SXFunction
+    that ``Function::serialize()`` returned the text of, as a :class:`runtime.CudaTape`."""
+    from . import runtime as R
+    return R.CudaTape.deserialize(text.encode() if isinstance(text, str) else bytes(text))

@@ -90,3 +90,14 @@ def test_push_file_loads_every_function(gpu_lib, tmp_path):
     torch.cuda.synchronize()
     R.pop_file()
     assert len(R.loaded_names()) == n0
+
+
+def test_package_load_and_deserialize(gpu_lib, tmp_path):
+    import casadi_gb300 as cg
+    F = W.cartpole_step()
+    path = tmp_path / "step.casadi"
+    path.write_text(SZ.serialize(F, saved_form=True))
+    a, b = cg.load(str(path)), cg.deserialize(SZ.serialize(F))
+    args = dev(W.cartpole_inputs(300, steps=1, seed=2))
+    assert_bitexact(host(a.eval(args))[0], host(b.eval(args))[0], "load vs deserialize")
+    a.sync()
