@@ -383,6 +383,67 @@ def mixed_component(torch, R, stream, reps=3, total=1 << 20, cpu=False):
             "bitwise_equal": same}
 
 
+def maps_component(torch, stream, n=1 << 18, steps=20, reps=3):
+    """Function::mapaccum and MapSum on the headline's shapes. mapaccum: the 20-step cart-pole
+    rollout written as mapaccum(20) of the one-step function with its stage cost, values of
+    every step and the reverse sweep of x_20 and all stage costs back to x0 and U (the
+    accumulator checkpointed at every call), against the unrolled rollout tape's value and
+    adjoint sweeps on the same inputs. MapSum: the unrolled rollout with the control sequence
+    U shared by all instances (reduce_in) and the cost summed over instances (reduce_out), in
+    instance order (the reference's bits) and in the blocked-tree order: values, and the
+    adjoint of the summed cost, which gives the gradient with respect to the shared U summed
+    over the instances."""
+    from casadi_gb300 import runtime as R
+    from casadi_gb300 import sx as S
+    from casadi_gb300 import workloads as W
+    x, u = S.sym("x", 4), S.sym("u")
+    cost = (x[0] * x[0] + x[1] * x[1] + x[2] * x[2] + x[3] * x[3]) + 0.01 * u * u
+    f = S.Function("fc", [x, [u]], [W.rk4_step(x, u), [cost]])
+    x0, U = W.cartpole_inputs(n, steps=steps, seed=5)
+    dx0 = torch.from_numpy(x0).cuda()
+    dU = torch.from_numpy(np.ascontiguousarray(U * 0.3)).cuda()
+
+    def ms(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    acc = R.CudaMapaccum(f, steps)
+    sx = torch.zeros((1, 4 * steps, n), dtype=torch.float64, device="cuda")
+    sx[:, -4:] = 1.0
+    sc = torch.ones((1, steps, n), dtype=torch.float64, device="cuda")
+    out = {"instances": n, "steps": steps}
+    out["mapaccum_eval_ms"] = ms(lambda: acc.eval([dx0, dU], stream=stream))
+    out["mapaccum_reverse_ms"] = ms(lambda: acc.reverse([dx0, dU], [sx, sc], stream=stream))
+    F = W.cartpole_rollout(steps)
+    ct = R.CudaTape(F)
+    seeds = [torch.ones((1, 4, n), dtype=torch.float64, device="cuda"),
+             torch.ones((1, 1, n), dtype=torch.float64, device="cuda")]
+    out["unrolled_eval_ms"] = ms(lambda: ct.eval([dx0, dU], stream=stream))
+    out["unrolled_reverse_ms"] = ms(lambda: ct.reverse([dx0, dU], seeds, stream=stream))
+    dUs = dU[:, 0].contiguous()
+    aseeds = [None, torch.ones((1, 1), dtype=torch.float64, device="cuda")]
+    # order 0: instance order, one dependent add per instance (the reference's bits);
+    # order 1: the blocked tree (deterministic, other bits)
+    for order, tag in ((0, "mapsum"), (1, "mapsum_tree")):
+        msum = R.CudaMapSum(F, n, reduce_in=[False, True], reduce_out=[False, True],
+                            order=order)
+        out[tag + "_eval_ms"] = ms(lambda: msum.eval([dx0, dUs], stream=stream))
+        out[tag + "_reverse_ms"] = ms(lambda: msum.reverse([dx0, dUs], aseeds, stream=stream))
+    for k in ("mapaccum_eval", "mapaccum_reverse", "unrolled_eval", "unrolled_reverse",
+              "mapsum_eval", "mapsum_reverse", "mapsum_tree_eval", "mapsum_tree_reverse"):
+        out[k + "_evals_per_s"] = n / (out[k + "_ms"] * 1e-3)
+    acc.tape.sync()
+    ct.sync()
+    return out
+
+
 def rollout_autograd_component(torch, stream, n=1 << 20, reps=2):
     """The cart-pole 100-step rollout over 2^20 instances differentiated through
     torch.autograd: ten checkpointed 10-step segment tapes; forward stores only the segment
@@ -634,6 +695,7 @@ def run_native(a):
         comps["mixed_batch"] = mixed_component(torch, R, stream, cpu=cpu)
         comps["rollout100_autograd"] = rollout_autograd_component(torch, stream)
         comps["mpc_sparse_hessian"] = mpc_sparse_component(torch, stream, cpu=cpu)
+        comps["mapaccum_mapsum"] = maps_component(torch, stream)
 
     # roofline of the dominant kernel family (device time from the per-launch events)
     weights = load_weights()

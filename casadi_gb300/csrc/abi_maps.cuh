@@ -115,6 +115,24 @@ int sum_rows(long long rows, long long n, const double* src, double* dst, int or
   return e == cudaSuccess ? 0 : cuda_fail(e, "MapSum reduction");
 }
 
+// The row sums of one call: instance-order sums are collected and run by one launch, since
+// their chains are independent; tree sums run as they come.
+struct RowSums {
+  int order;
+  double* tree;
+  std::vector<SumRows> g;
+  int add(long long rows, long long n, const double* src, double* dst, cudaStream_t s) {
+    if (order != kOrderInstance) return sum_rows(rows, n, src, dst, order, tree, s);
+    g.push_back({src, n, dst, rows});
+    return 0;
+  }
+  int flush(long long n, cudaStream_t s) {
+    cudaError_t e = reduce_sum_instance_multi(g.data(), static_cast<int>(g.size()), n, s);
+    g.clear();
+    return e == cudaSuccess ? 0 : cuda_fail(e, "MapSum reduction");
+  }
+};
+
 }  // namespace
 
 extern "C" {
@@ -162,10 +180,11 @@ int casadi_gb300_mapsum_eval(int id, int64_t n, int64_t ld, const casadi_gb300_m
   if (int rc = take_tree(ar, *t, n, 0, f, &tree)) return rc;
   if (n > 0)
     if (int rc = primal_launch(*t, a, n, PK_EVAL, s)) return rc;
+  RowSums sums{f.order, tree, {}};
   for (int j = 0; j < t->n_out; ++j)
     if (rows[j])
-      if (int rc = sum_rows(t->nnz_out[j], n, rows[j], res[j], f.order, tree, s)) return rc;
-  return 0;
+      if (int rc = sums.add(t->nnz_out[j], n, rows[j], res[j], s)) return rc;
+  return sums.flush(n, s);
 }
 
 int casadi_gb300_mapsum_forward(int id, int64_t n, int64_t ld,
@@ -210,15 +229,16 @@ int casadi_gb300_mapsum_forward(int id, int64_t n, int64_t ld,
   if (int rc = take_tree(ar, *t, n, nfwd, f, &tree)) return rc;
   if (int rc = run_ad(*t, n, in, out, seed, sens, nfwd, false, false, ar.p, ar.left, s))
     return rc;
+  RowSums sums{f.order, tree, {}};
   for (int j = 0; j < t->n_out; ++j) {
     if (rows[j])
-      if (int rc = sum_rows(t->nnz_out[j], n, rows[j], res[j], f.order, tree, s)) return rc;
+      if (int rc = sums.add(t->nnz_out[j], n, rows[j], res[j], s)) return rc;
     if (srows[j])
-      if (int rc = sum_rows(static_cast<long long>(t->nnz_out[j]) * nfwd, n, srows[j], fsens[j],
-                            f.order, tree, s))
+      if (int rc = sums.add(static_cast<long long>(t->nnz_out[j]) * nfwd, n, srows[j],
+                            fsens[j], s))
         return rc;
   }
-  return 0;
+  return sums.flush(n, s);
 }
 
 int casadi_gb300_mapsum_reverse(int id, int64_t n, int64_t ld,
@@ -261,15 +281,16 @@ int casadi_gb300_mapsum_reverse(int id, int64_t n, int64_t ld,
   double* tree = nullptr;
   if (int rc = take_tree(ar, *t, n, nadj, f, &tree)) return rc;
   if (int rc = run_ad(*t, n, in, out, seed, sens, nadj, true, false, ar.p, ar.left, s)) return rc;
+  RowSums sums{f.order, tree, {}};
   for (int j = 0; j < t->n_out; ++j)
     if (rows[j])
-      if (int rc = sum_rows(t->nnz_out[j], n, rows[j], res[j], f.order, tree, s)) return rc;
+      if (int rc = sums.add(t->nnz_out[j], n, rows[j], res[j], s)) return rc;
   for (int j = 0; j < t->n_in; ++j)
     if (srows[j])
-      if (int rc = sum_rows(static_cast<long long>(t->nnz_in[j]) * nadj, n, srows[j], asens[j],
-                            f.order, tree, s))
+      if (int rc = sums.add(static_cast<long long>(t->nnz_in[j]) * nadj, n, srows[j],
+                            asens[j], s))
         return rc;
-  return 0;
+  return sums.flush(n, s);
 }
 
 int casadi_gb300_mapsum_sp_forward(int id, int64_t n, int64_t ld,

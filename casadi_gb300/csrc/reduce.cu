@@ -21,13 +21,46 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32)
   const long long r = static_cast<long long>(blockIdx.x) * kWarpsPerCta + (threadIdx.x >> 5);
   if (r >= rows) return;
   const double* row = src + r * ld;
+  // one lane runs the chain: no shuffle between two dependent adds, and the FP64 pipe takes
+  // one active lane per add instead of a full warp; the loads are independent of the chain
+  // and run ahead of it (unrolled)
+  if (lane != 0) return;
   double acc = 0.0;
-  for (long long base = 0; base < n; base += 32) {
-    const double v = base + lane < n ? __ldg(row + base + lane) : 0.0;
-    const int cnt = static_cast<int>(n - base < 32 ? n - base : 32);
-    for (int k = 0; k < cnt; ++k) acc = __dadd_rn(acc, __shfl_sync(kFull, v, k));
+  long long i = 0;
+  for (; i + 8 <= n; i += 8) {
+    double v[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = __ldg(row + i + k);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) acc = __dadd_rn(acc, v[k]);
   }
-  if (lane == 0) dst[r] = acc;
+  for (; i < n; ++i) acc = __dadd_rn(acc, __ldg(row + i));
+  dst[r] = acc;
+}
+
+struct SumRowsArgs {
+  SumRows g[kMaxSumGroups];
+  int count;
+};
+
+__global__ void __launch_bounds__(128)
+    k_sum_instance_multi(const __grid_constant__ SumRowsArgs a, long long n) {
+  long long r = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  int k = 0;
+  while (k < a.count && r >= a.g[k].rows) r -= a.g[k++].rows;
+  if (k >= a.count) return;
+  const double* row = a.g[k].src + r * a.g[k].ld;
+  double acc = 0.0;
+  long long i = 0;
+  for (; i + 8 <= n; i += 8) {
+    double v[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[j] = __ldg(row + i + j);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc = __dadd_rn(acc, v[j]);
+  }
+  for (; i < n; ++i) acc = __dadd_rn(acc, __ldg(row + i));
+  a.g[k].dst[r] = acc;
 }
 
 // One level of the blocked tree: item (r, b) sums x[r][b*256 .. b*256+255] into y[r][b].
@@ -139,6 +172,23 @@ cudaError_t reduce_sum(long long rows, long long n, const double* src, long long
     m = nb;
     which ^= 1;
   }
+}
+
+cudaError_t reduce_sum_instance_multi(const SumRows* groups, int count, long long n,
+                                      cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  if (count > kMaxSumGroups) return cudaErrorInvalidValue;
+  SumRowsArgs a;
+  long long total = 0;
+  for (int k = 0; k < count; ++k) {
+    a.g[k] = groups[k];
+    total += groups[k].rows;
+  }
+  a.count = count;
+  if (total == 0) return cudaSuccess;
+  const long long blocks = (total + 127) / 128;
+  k_sum_instance_multi<<<static_cast<unsigned>(blocks), 128, 0, s>>>(a, n);
+  return cudaGetLastError();
 }
 
 cudaError_t reduce_or(long long rows, long long n, const unsigned long long* src, long long ld,

@@ -29,6 +29,20 @@ size_t reduce_scratch_bytes(long long rows, long long n, int order);
 // dst[r] (= or +=, see `accumulate`) the sum of row r. `scratch` as reduce_scratch_bytes.
 cudaError_t reduce_sum(long long rows, long long n, const double* src, long long ld, double* dst,
                        int order, double* scratch, cudaStream_t s);
+// Several blocks of rows summed in instance order (kOrderInstance) by one launch, one thread
+// per row: the rows' chains of n dependent adds run concurrently instead of one block after
+// the other (each add waits for the previous one, ~85 cycles on GB300's FP64 pipe, so a chain
+// costs ~40 ns per instance whatever else runs beside it). Same bits as reduce_sum.
+struct SumRows {
+  const double* src;  // rows of n values, row r at src + r*ld
+  long long ld;
+  double* dst;        // dst[r] = the sum of row r
+  long long rows;
+};
+constexpr int kMaxSumGroups = 128;
+cudaError_t reduce_sum_instance_multi(const SumRows* groups, int count, long long n,
+                                      cudaStream_t s);
+
 // dst[r] |= OR of row r (accumulate) or dst[r] = OR of row r.
 cudaError_t reduce_or(long long rows, long long n, const unsigned long long* src, long long ld,
                       unsigned long long* dst, bool accumulate, cudaStream_t s);
