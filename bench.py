@@ -421,6 +421,9 @@ def maps_component(torch, stream, n=1 << 18, steps=20, reps=3):
     out = {"instances": n, "steps": steps}
     out["mapaccum_eval_ms"] = ms(lambda: acc.eval([dx0, dU], stream=stream))
     out["mapaccum_reverse_ms"] = ms(lambda: acc.reverse([dx0, dU], [sx, sc], stream=stream))
+    acc2 = R.CudaMapaccum(f, steps)
+    out["mapaccum_reverse_recorded_ms"] = ms(
+        lambda: acc2.reverse([dx0, dU], [sx, sc], stream=stream, record_all=True))
     F = W.cartpole_rollout(steps)
     ct = R.CudaTape(F)
     seeds = [torch.ones((1, 4, n), dtype=torch.float64, device="cuda"),
@@ -436,10 +439,12 @@ def maps_component(torch, stream, n=1 << 18, steps=20, reps=3):
                             order=order)
         out[tag + "_eval_ms"] = ms(lambda: msum.eval([dx0, dUs], stream=stream))
         out[tag + "_reverse_ms"] = ms(lambda: msum.reverse([dx0, dUs], aseeds, stream=stream))
-    for k in ("mapaccum_eval", "mapaccum_reverse", "unrolled_eval", "unrolled_reverse",
+    for k in ("mapaccum_eval", "mapaccum_reverse", "mapaccum_reverse_recorded",
+              "unrolled_eval", "unrolled_reverse",
               "mapsum_eval", "mapsum_reverse", "mapsum_tree_eval", "mapsum_tree_reverse"):
         out[k + "_evals_per_s"] = n / (out[k + "_ms"] * 1e-3)
     acc.tape.sync()
+    acc2.tape.sync()
     ct.sync()
     return out
 

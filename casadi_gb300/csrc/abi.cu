@@ -1133,9 +1133,13 @@ int run_deriv(Tape& t, SweepArgs a, long long m, const DerivReq& rq, cudaStream_
 // `in/out` and the requests' descriptors address the whole instance range.
 int run_ad_multi(Tape& t, long long n, const IoDesc* in, const IoDesc* out,
                  const DerivReq* reqs, int nreq, void* scratch, size_t scratch_bytes,
-                 cudaStream_t s) {
+                 cudaStream_t s, bool recorded = false) {
   if (n == 0) return 0;
   const long long cap = wave_capacity(t, n, scratch_bytes);
+  // recorded: the scratch already holds the partials of all n instances (one wave), and the
+  // values were written by that record sweep
+  if (recorded && cap < n)
+    return fail(CASADI_GB300_ERR_SCRATCH, "recorded partials cover fewer than %lld instances", n);
   if (t.n_partials > 0 && (scratch == nullptr || cap < 32))
     return fail(CASADI_GB300_ERR_SCRATCH,
                 "scratch of %zu bytes is below the minimum of %lld bytes for this tape",
@@ -1160,7 +1164,8 @@ int run_ad_multi(Tape& t, long long n, const IoDesc* in, const IoDesc* out,
     for (int j = 0, off = 0; j < t.n_in; off += t.nnz_in[j], ++j) a.in_off[j] = off;
     std::memcpy(a.in, in, sizeof(IoDesc) * t.n_in);
     std::memcpy(a.out, out, sizeof(IoDesc) * t.n_out);
-    if (int rc = primal_launch(t, a, m, PK_RECORD, s)) return rc;
+    if (!recorded)
+      if (int rc = primal_launch(t, a, m, PK_RECORD, s)) return rc;
     for (int r = 0; r < nreq; ++r)
       if (reqs[r].ndir > 0)
         if (int rc = run_deriv(t, a, m, reqs[r], s)) return rc;
@@ -1170,14 +1175,14 @@ int run_ad_multi(Tape& t, long long n, const IoDesc* in, const IoDesc* out,
 
 int run_ad(Tape& t, long long n, const IoDesc* in, const IoDesc* out, const IoDesc* seed,
            const IoDesc* sens, int ndir, bool adjoint, bool identity, void* scratch,
-           size_t scratch_bytes, cudaStream_t s) {
+           size_t scratch_bytes, cudaStream_t s, bool recorded = false) {
   DerivReq rq;
   rq.ndir = ndir;
   rq.adjoint = adjoint;
   rq.identity = identity;
   rq.seed = seed;
   rq.sens = sens;
-  return run_ad_multi(t, n, in, out, &rq, 1, scratch, scratch_bytes, s);
+  return run_ad_multi(t, n, in, out, &rq, 1, scratch, scratch_bytes, s, recorded);
 }
 
 // Pointer arrays of any element type, seen as untyped pointers (the kernels know the type).

@@ -445,11 +445,25 @@ int accum_values(const Tape& t, int N, int n_accum, long long n, const double* c
 }
 
 // The value sweep of every step: inputs of step k from arg / the previous step's outputs.
+// Partials scratch of one call over n instances (tile-major, as run_ad_multi lays it out).
+size_t accum_call_partials(const Tape& t, long long n) {
+  return static_cast<size_t>(8) * t.n_partials * static_cast<size_t>(((n + 31) / 32) * 32);
+}
+
+// The N calls forward. With `partials`, each call is a record sweep that leaves its partials at
+// partials + k * accum_call_partials (the reverse sweep then needs no record of its own);
+// otherwise a value sweep.
 int accum_forward_values(Tape& t, int N, int n_accum, long long n, long long ld,
                          const double* const* arg, double* const* res, const AccumValues& v,
-                         cudaStream_t s) {
+                         cudaStream_t s, char* partials = nullptr) {
   for (int k = 0; k < N; ++k) {
     SweepArgs a = base_args(t, n, 0);
+    if (partials) {
+      a.partials = reinterpret_cast<double*>(partials + k * accum_call_partials(t, n));
+      a.pofs = t.d_pofs;
+      a.n_code = t.n_chunks * kChunk;
+      for (int j = 0, off = 0; j < t.n_in; off += t.nnz_in[j], ++j) a.in_off[j] = off;
+    }
     for (int j = 0; j < t.n_in; ++j) {
       const int nz = t.nnz_in[j];
       if (j < n_accum)
@@ -460,7 +474,7 @@ int accum_forward_values(Tape& t, int N, int n_accum, long long n, long long ld,
     for (int j = 0; j < t.n_out; ++j)
       a.out[j] = j < n_accum ? v.value(j, t.nnz_out[j], N, k, n, ld)
                              : step_io(res ? res[j] : nullptr, t.nnz_out[j], N, k, ld);
-    if (int rc = primal_launch(t, a, n, PK_EVAL, s)) return rc;
+    if (int rc = primal_launch(t, a, n, partials ? PK_RECORD : PK_EVAL, s)) return rc;
   }
   return 0;
 }
@@ -572,7 +586,6 @@ int casadi_gb300_mapaccum_reverse(int id, int N, int n_accum, int64_t n, int64_t
   // reverse sweep of step k records it again from its inputs
   AccumValues v;
   if (int rc = accum_values(*t, N, n_accum, n, res, true, ar, &v)) return rc;
-  if (int rc = accum_forward_values(*t, N, n_accum, n, ld, arg, res, v, s)) return rc;
   // adjoints of the accumulator inputs, carried from step k+1 to step k, and the combined
   // seeds of the accumulator outputs
   double* carry[kMaxIo] = {};
@@ -585,6 +598,14 @@ int casadi_gb300_mapaccum_reverse(int id, int N, int n_accum, int64_t n, int64_t
       return fail(CASADI_GB300_ERR_SCRATCH,
                   "mapaccum scratch too small (see casadi_gb300_mapaccum_scratch_size)");
   }
+  // with room for every call's partials (casadi_gb300_mapaccum_reverse_scratch_size), the
+  // forward pass records them and the reverse pass runs adjoint sweeps only; otherwise each
+  // call is recorded again from its checkpointed inputs on the way back
+  const size_t per_call = accum_call_partials(*t, n);
+  char* recorded = nullptr;
+  if (t->n_partials > 0 && ar.left >= per_call * static_cast<size_t>(N) + kQueueSlack)
+    recorded = static_cast<char*>(ar.take(per_call * static_cast<size_t>(N)));
+  if (int rc = accum_forward_values(*t, N, n_accum, n, ld, arg, res, v, s, recorded)) return rc;
   for (int k = N - 1; k >= 0; --k) {
     IoDesc in[kMaxIo], out[kMaxIo], seed[kMaxIo], sens[kMaxIo];
     for (int j = 0; j < t->n_out; ++j) {
@@ -615,9 +636,24 @@ int casadi_gb300_mapaccum_reverse(int id, int N, int n_accum, int64_t n, int64_t
         sens[j] = step_io(asens ? asens[j] : nullptr, nz, N, k, ld);
       }
     }
-    if (int rc = run_ad(*t, n, in, out, seed, sens, nadj, true, false, ar.p, ar.left, s))
+    if (recorded) {
+      if (int rc = run_ad(*t, n, in, out, seed, sens, nadj, true, false,
+                          recorded + static_cast<size_t>(k) * per_call, per_call, s, true))
+        return rc;
+    } else if (int rc = run_ad(*t, n, in, out, seed, sens, nadj, true, false, ar.p, ar.left, s)) {
       return rc;
+    }
   }
+  return 0;
+}
+
+// Scratch for the mapaccum reverse sweep that records every call's partials on the way
+// forward: casadi_gb300_mapaccum_scratch_size plus N calls' partials.
+int casadi_gb300_mapaccum_reverse_scratch_size(int id, int N, int n_accum, int64_t n, int nadj,
+                                               size_t* bytes) {
+  if (int rc = casadi_gb300_mapaccum_scratch_size(id, N, n_accum, n, nadj, bytes)) return rc;
+  const Tape* t = get_tape(id);
+  *bytes += accum_call_partials(*t, n) * static_cast<size_t>(std::max(N, 0)) + 256;
   return 0;
 }
 

@@ -84,6 +84,7 @@ def load(path=None):
         "casadi_gb300_eval_activity": (cint, [cint, i64, i64, vp, vp, vp]),
         "casadi_gb300_mapsum_scratch_size": (cint, [cint, i64, cint, vp, vp]),
         "casadi_gb300_mapaccum_scratch_size": (cint, [cint, cint, cint, i64, cint, vp]),
+        "casadi_gb300_mapaccum_reverse_scratch_size": (cint, [cint, cint, cint, i64, cint, vp]),
         "casadi_gb300_mapaccum_eval": (cint, [cint, cint, cint, i64, i64, vp, vp, vp, sz, vp]),
         "casadi_gb300_mapaccum_forward": (cint, [cint, cint, cint, i64, i64, cint, vp, vp, vp,
                                                  vp, vp, sz, vp]),
@@ -633,10 +634,12 @@ class CudaMapaccum:
         k = self.tape.nnz_in[j]
         return k if j < self.n_accum else k * self.N
 
-    def scratch(self, n, ndir=0):
+    def scratch(self, n, ndir=0, record_all=False):
         import torch
         b = ct.c_size_t()
-        check(load().casadi_gb300_mapaccum_scratch_size(self.tape.id, self.N, self.n_accum, n,
+        size = (load().casadi_gb300_mapaccum_reverse_scratch_size if record_all
+                else load().casadi_gb300_mapaccum_scratch_size)
+        check(size(self.tape.id, self.N, self.n_accum, n,
                                                         ndir, ct.byref(b)))
         if self._scratch is None or self._scratch.numel() < b.value:
             self._scratch = torch.empty(max(b.value, 8), dtype=torch.uint8, device="cuda")
@@ -674,14 +677,14 @@ class CudaMapaccum:
             _stream_handle(stream)))
         return res, fsens
 
-    def reverse(self, args, aseeds, n=None, keep=None, stream=None):
+    def reverse(self, args, aseeds, n=None, keep=None, stream=None, record_all=False):
         import torch
         n = CudaTape._n(args) if n is None else n
         nadj = next(s.shape[0] for s in aseeds if s is not None)
         res = self._outs(n, keep=keep)
         asens = [torch.empty((nadj, self._in_rows(j), n), dtype=torch.float64, device="cuda")
                  for j in range(len(self.tape.nnz_in))]
-        sc = self.scratch(n, nadj)
+        sc = self.scratch(n, nadj, record_all)
         check(load().casadi_gb300_mapaccum_reverse(
             self.tape.id, self.N, self.n_accum, n, n, nadj, _ptr_array(args), _ptr_array(res),
             _ptr_array(aseeds), _ptr_array(asens), ct.c_void_p(sc.data_ptr()), sc.numel(),

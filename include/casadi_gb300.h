@@ -305,6 +305,12 @@ CASADI_GB300_API int casadi_gb300_mapsum_sp_reverse(int id, int64_t n, int64_t l
  * ndir directions). Nothing is unrolled: one tape, N launches, outputs fed back in place. */
 CASADI_GB300_API int casadi_gb300_mapaccum_scratch_size(int id, int N, int n_accum, int64_t n,
                             int ndir, size_t* bytes);
+/* Scratch with which casadi_gb300_mapaccum_reverse records the partials of every call on the
+ * way forward and runs adjoint sweeps only on the way back (same bits; no record per call in
+ * the reverse pass): the size above plus N calls' partials. A smaller scratch (down to the
+ * size above) runs the checkpointed form. */
+CASADI_GB300_API int casadi_gb300_mapaccum_reverse_scratch_size(int id, int N, int n_accum,
+                           int64_t n, int nadj, size_t* bytes);
 CASADI_GB300_API int casadi_gb300_mapaccum_eval(int id, int N, int n_accum, int64_t n,
                             int64_t ld, const double* const* arg, double* const* res,
                             void* scratch, size_t scratch_bytes, void* stream);
