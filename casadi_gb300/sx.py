@@ -944,9 +944,39 @@ def reverse(f, aseed):
     return [[sens_of.get(e, zero) for e in vec] for vec in f.inputs]
 
 
+class _Helper:
+    """Inputs and outputs of a temporary Function whose other symbols stay free (the
+    reference's ``allow_free`` helper Functions)."""
+
+    def __init__(self, inputs, outputs):
+        self.inputs = [list(v) for v in inputs]
+        self.outputs = [[_sx(e) for e in v] for v in outputs]
+
+
+def gradient_expr(ex, arg):
+    """Gradient expressions of the scalar ``ex`` with respect to the symbols ``arg``, built as
+    the reference builds ``gradient(ex, arg)``: ``jtimes(ex, arg, 1, true)``
+    (casadi/core/generic_matrix.hpp:1695-1704), i.e. one symbolic adjoint sweep of a
+    temporary Function ``arg -> ex`` with free variables allowed (``SX::reverse``,
+    casadi/core/sx_instantiator.cpp:1208-1230). The sweep's order, and with it the order of
+    every adjoint sum, follows that temporary Function's tape."""
+    return reverse(_Helper([list(arg)], [[ex]]), [[1.0]])[0]
+
+
 def gradient(f, out, wrt):
     """Gradient expressions of the scalar output ``out`` of ``f`` with respect to input
-    ``wrt``: one adjoint sweep seeded with 1 on that output."""
-    seeds = [None] * f.n_out()
-    seeds[out] = [1.0] * len(f.outputs[out])
-    return reverse(f, seeds)[wrt]
+    ``wrt``, as the reference's ``gradient(f_out, f_wrt)`` (:func:`gradient_expr`)."""
+    if len(f.outputs[out]) != 1:
+        raise ValueError("the gradient needs a scalar output")
+    return gradient_expr(f.outputs[out][0], f.inputs[wrt])
+
+
+def reverse_function(f):
+    """The Function ``f.reverse(1)`` as the reference builds it (XFunction::get_reverse with
+    SXFunction::ad_reverse, casadi/core/sx_function.cpp:1368-1569): inputs are f's inputs,
+    one placeholder per output with no nonzeros (``out_*``), then one adjoint seed per output
+    (``adj_*``); outputs are the adjoint sensitivities of f's inputs. Evaluating its tape
+    with the value sweep gives the reference's adjoint results operation for operation."""
+    adj = [sym("adj_o%d" % j, len(v)) for j, v in enumerate(f.outputs)]
+    sens = reverse(f, adj)
+    return Function("adj1_" + f.name, f.inputs + [[] for _ in f.outputs] + adj, sens)

@@ -76,47 +76,68 @@ DAG_OPS = ["add", "sub", "mul", "div", "sin", "cos", "exp", "log", "sqrt", "tanh
 DAG_P = [0.25, 0.15, 0.25, 0.05, 0.06, 0.06, 0.06, 0.04, 0.04, 0.04]
 
 
-def random_dag(n_in=64, n_nodes=10000, n_out=16, seed=0, window=256, bounded=False):
-    """A seeded random expression DAG. Node k (k >= n_in) applies an op drawn from the
-    mix above to operands drawn uniformly from the previous ``window`` nodes; the
-    outputs are the last ``n_out`` nodes. Unary ops are guarded: exp(clip(x,-5,5)),
-    log(|x|+1), sqrt(x^2+1). With ``bounded`` the sums are averaged (0.5*(a+b)), products
-    take one tanh-squashed factor (a*tanh(b)) and exp is clipped to [-1, 1], which keeps
-    every node of a deep, narrow DAG finite and of order one."""
+def dag_nodes(n_in=64, n_nodes=10000, seed=0, window=256):
+    """The node list of the seeded random DAG: for every node k >= n_in, the index of its op
+    in ``DAG_OPS`` and two operand indices drawn uniformly from the previous ``window`` nodes
+    (unary ops ignore the second). Returns int32 arrays ``(op, a, b)`` of n_nodes - n_in."""
     rng = np.random.default_rng(seed)
-    xs = S.sym("x", n_in)
-    nodes = list(xs)
     cum = np.cumsum(DAG_P)
+    m = n_nodes - n_in
+    op = np.empty(m, np.int32)
+    a = np.empty(m, np.int32)
+    b = np.empty(m, np.int32)
     for k in range(n_in, n_nodes):
         r = rng.random()
-        op = DAG_OPS[int(np.searchsorted(cum, r * cum[-1], side="right"))]
+        op[k - n_in] = int(np.searchsorted(cum, r * cum[-1], side="right"))
         lo = max(0, k - window)
-        a = nodes[int(rng.integers(lo, k))]
-        b = nodes[int(rng.integers(lo, k))]
-        if op == "add":
-            e = 0.5 * (a + b) if bounded else a + b
-        elif op == "sub":
-            e = 0.5 * (a - b) if bounded else a - b
-        elif op == "mul":
-            e = a * S.tanh(b) if bounded else a * b
-        elif op == "div":
-            e = a / (S.sq(b) + 1.0)
-        elif op == "sin":
-            e = S.sin(a)
-        elif op == "cos":
-            e = S.cos(a)
-        elif op == "exp":
+        a[k - n_in] = int(rng.integers(lo, k))
+        b[k - n_in] = int(rng.integers(lo, k))
+    return op, a, b
+
+
+def dag_from_nodes(n_in, n_out, op, a, b, bounded=False):
+    """Build the DAG of a node list (see :func:`dag_nodes`); the outputs are the last
+    ``n_out`` nodes. Unary ops are guarded: exp(clip(x,-5,5)), log(|x|+1), sqrt(x^2+1). With
+    ``bounded`` the sums are averaged (0.5*(a+b)), products take one tanh-squashed factor
+    (a*tanh(b)) and exp is clipped to [-1, 1], which keeps every node of a deep, narrow DAG
+    finite and of order one."""
+    xs = S.sym("x", n_in)
+    nodes = list(xs)
+    for code, ia, ib in zip(op.tolist(), a.tolist(), b.tolist()):
+        name = DAG_OPS[code]
+        x, y = nodes[ia], nodes[ib]
+        if name == "add":
+            e = 0.5 * (x + y) if bounded else x + y
+        elif name == "sub":
+            e = 0.5 * (x - y) if bounded else x - y
+        elif name == "mul":
+            e = x * S.tanh(y) if bounded else x * y
+        elif name == "div":
+            e = x / (S.sq(y) + 1.0)
+        elif name == "sin":
+            e = S.sin(x)
+        elif name == "cos":
+            e = S.cos(x)
+        elif name == "exp":
             c = 1.0 if bounded else 5.0
-            e = S.exp(S.fmin(S.fmax(a, -c), c))
-        elif op == "log":
-            e = S.log(S.fabs(a) + 1.0)
-        elif op == "sqrt":
-            e = S.sqrt(S.sq(a) + 1.0)
+            e = S.exp(S.fmin(S.fmax(x, -c), c))
+        elif name == "log":
+            e = S.log(S.fabs(x) + 1.0)
+        elif name == "sqrt":
+            e = S.sqrt(S.sq(x) + 1.0)
         else:
-            e = S.tanh(a)
+            e = S.tanh(x)
         nodes.append(e)
     outs = nodes[-n_out:]
     return S.Function("G", [xs], [outs])
+
+
+def random_dag(n_in=64, n_nodes=10000, n_out=16, seed=0, window=256, bounded=False):
+    """A seeded random expression DAG: node k (k >= n_in) applies an op drawn from the mix
+    above to operands drawn uniformly from the previous ``window`` nodes; the outputs are the
+    last ``n_out`` nodes (:func:`dag_nodes`, :func:`dag_from_nodes`)."""
+    op, a, b = dag_nodes(n_in, n_nodes, seed, window)
+    return dag_from_nodes(n_in, n_out, op, a, b, bounded)
 
 
 def dag_inputs(n, n_in=64, seed=0):

@@ -17,19 +17,33 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libref_calculus.so")
-REFERENCE_TREE = "/root/reference"
 
 _lib = None
 _ref = None
 
 
-def build(ref=None):
-    """Compile the oracle; also the reference harness when the reference tree exists."""
+def reference_tree():
+    """The reference source tree named by the CASADI_REFERENCE environment variable, or None
+    (no default: the tree exists only where the fixtures are generated)."""
+    tree = os.environ.get("CASADI_REFERENCE")
+    if tree and os.path.isdir(os.path.join(tree, "casadi", "core")):
+        return tree
+    return None
+
+
+def build(ref=None, tree=None):
+    """Compile the oracle; with a reference tree (``tree`` or CASADI_REFERENCE) also the
+    reference op-semantics harness and the reference's own libcasadi with its bridge."""
     subprocess.check_call(["make", "-s", "-C", HERE, "all"])
+    tree = tree or reference_tree()
     if ref is None:
-        ref = os.path.isdir(os.path.join(REFERENCE_TREE, "casadi", "core"))
+        ref = tree is not None
     if ref:
-        subprocess.check_call(["make", "-s", "-C", HERE, "ref", "REF=" + REFERENCE_TREE])
+        if tree is None:
+            raise RuntimeError("the reference harness needs CASADI_REFERENCE")
+        jobs = str(max(1, min(16, os.cpu_count() or 1)))
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref", "casadi", "REF=" + tree,
+                               "JOBS=" + jobs])
 
 
 class _Tape(ct.Structure):
@@ -170,6 +184,22 @@ def reverse(tape, args, aseeds, n, nthreads=1):
                            _ptrs(res), _ptrs(aseeds), _ptrs(asens), ct.c_int(nthreads))
     assert rc == 0
     return res, asens
+
+
+class magnitude:
+    """Context in which forward / jacobian / reverse return magnitudes: the same sweeps over
+    |partials| and |seeds|, i.e. per derivative entry the sum over its chain-rule paths of
+    |product of partials| x |seed|. Two evaluations of one derivative that round differently
+    (this sweep, the reference's symbolic derivative Function) differ by at most a modest
+    multiple of eps times that magnitude, which is how the tests compare them."""
+
+    def __enter__(self):
+        lib().sxo_set_magnitude(1)
+        return self
+
+    def __exit__(self, *exc):
+        lib().sxo_set_magnitude(0)
+        return False
 
 
 def sp_forward(tape, args, n, nthreads=1):

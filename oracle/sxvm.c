@@ -219,6 +219,16 @@ static void eval_one(const sxo_tape* t, long n, long i, const double* const* arg
   }
 }
 
+/* Magnitude mode (set by sxo_set_magnitude): the AD sweeps run on |partials| and |seeds|,
+ * so each derivative result is the sum over its chain-rule paths of |product of partials| x
+ * |seed| -- the scale that the rounding error of any evaluation order of that derivative is
+ * bounded by (each path's product and the sum over paths round with relative error of order
+ * path length x eps). The tests use it to compare two AD results that round differently
+ * (this numeric sweep, the reference's symbolic one) element by element. */
+static int g_magnitude = 0;
+
+void sxo_set_magnitude(int on) { g_magnitude = on != 0; }
+
 /* values plus the partials of every arithmetic instruction, in tape order */
 static void eval_partials(const sxo_tape* t, long n, long i, const double* const* arg,
                           double* const* res, double* w, double* dp) {
@@ -232,6 +242,10 @@ static void eval_partials(const sxo_tape* t, long n, long i, const double* const
         double x = w[i1], y = w[i2];
         double f = sxo_fun(op, x, y);
         sxo_der(op, x, y, f, dp + 2 * (long)k);
+        if (g_magnitude) {
+          dp[2 * (long)k] = fabs(dp[2 * (long)k]);
+          dp[2 * (long)k + 1] = fabs(dp[2 * (long)k + 1]);
+        }
         w[i0] = f;
       }
     }
@@ -296,6 +310,7 @@ static void tangent_one(const sxo_tape* t, const double* dp, double* wd, char* a
           const double* s = fseed[i1];
           act[i0] = s != 0;
           if (s) wd[i0] = s[((long)dir * t->nnz_in[i1] + i2) * n + i];
+          if (s && g_magnitude) wd[i0] = fabs(wd[i0]);
         }
         break;
       case SXO_OUTPUT: {
@@ -405,6 +420,7 @@ int sxo_reverse(const sxo_tape* t, long n, int nadj, const double* const* arg,
                 const double* s = aseed[i0];
                 if (s) {
                   double v = s[((long)dir * t->nnz_out[i0] + i2) * n + i];
+                  if (g_magnitude) v = fabs(v);
                   wb[i1] = act[i1] ? wb[i1] + v : v;
                   act[i1] = 1;
                 }

@@ -49,6 +49,7 @@ int sxo_sp_forward(const sxo_tape* t, long n, const uint64_t* const* arg, uint64
 int sxo_sp_reverse(const sxo_tape* t, long n, uint64_t* const* arg, uint64_t* const* res,
                    int nthreads);
 int sxo_zero_checker(int which, int op);
+void sxo_set_magnitude(int on);
 int sxo_activity(const sxo_tape* t, long n, const uint64_t* const* arg, uint64_t* const* res,
                  int nthreads);
 #endif

@@ -1,9 +1,10 @@
 """Generate the golden fixtures of this directory from the reference's own op semantics.
 
 Run where the reference source tree is available (it builds oracle/_ref from the reference's
-casadi/core/calculus.hpp):
+casadi/core sources):
 
-    python tests/golden/make_golden.py [ops] [enum] [tapes] [activity] [serial]  # default: all
+    CASADI_REFERENCE=<reference tree> python tests/golden/make_golden.py \
+        [ops] [enum] [tapes] [activity] [serial]  # default: all
 
 Fixtures:
   ops.npz        value and partials of every scalar op over a grid of special and ordinary
@@ -184,11 +185,13 @@ def activity_case():
     return out
 
 
-REFERENCE = os.environ.get("CASADI_REFERENCE", "/root/reference")
+REFERENCE = os.environ.get("CASADI_REFERENCE")
 
 
 def serialized_fixture():
     """The serialized text of test_issue_3074 in the reference's test/python/function.py."""
+    if not REFERENCE:
+        raise SystemExit("set CASADI_REFERENCE to the reference source tree")
     path = os.path.join(REFERENCE, "test", "python", "function.py")
     lines = open(path).read().splitlines()
     start = next(i for i, l in enumerate(lines) if "def test_issue_3074" in l)
@@ -207,7 +210,7 @@ def main(which=None):
             fh.write(serialized_fixture() + "\n")
         written.append("serialized_issue3074.txt")
     if which - {"serial"}:
-        O.build(ref=True)
+        O.build(ref=True, tree=REFERENCE)
         if not O.ref_available():
             raise SystemExit("the reference harness could not be built")
     if "ops" in which:

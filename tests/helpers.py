@@ -35,6 +35,37 @@ def golden_tape(z, name):
     return t
 
 
+def canonical_tape_bytes(op, i0, i1, i2, d):
+    """The bytes two tapes are compared by. The reference's ScalarAtomic overlays the constant
+    ``d`` on ``{i1, i2}`` (casadi/core/sx_function.hpp:37-44), so an OP_CONST is compared by its
+    ``d`` and every other instruction by ``i1, i2``: int32 op, i0, i1, i2 (zero for constants)
+    followed by the float64 bits of d (zero for non-constants)."""
+    op = np.asarray(op, np.int32)
+    c = op == C.OP_CONST
+    i1 = np.where(c, 0, np.asarray(i1)).astype(np.int32)
+    i2 = np.where(c, 0, np.asarray(i2)).astype(np.int32)
+    d = np.where(c, np.asarray(d, np.float64), 0.0)
+    return b"".join(np.ascontiguousarray(a).tobytes()
+                    for a in (op, np.asarray(i0, np.int32), i1, i2, d))
+
+
+def tape_sha256(t):
+    """SHA-256 of a Tape's canonical bytes."""
+    import hashlib
+    return hashlib.sha256(canonical_tape_bytes(t.op, t.i0, t.i1, t.i2, t.d)).hexdigest()
+
+
+def casadi_tape(z, name):
+    """A tape the reference's libcasadi built, from casadi.npz (stored in full), with the
+    union of d and {i1, i2} resolved: constants carry d, other instructions i1, i2."""
+    op = z[name + "/op"]
+    c = op == C.OP_CONST
+    return S.Tape(op, z[name + "/i0"], np.where(c, 0, z[name + "/i1"]),
+                  np.where(c, 0, z[name + "/i2"]), np.where(c, z[name + "/d"], 0.0),
+                  z[name + "/nnz_in"].tolist(), z[name + "/nnz_out"].tolist(),
+                  int(z[name + "/sz_w"]))
+
+
 def golden_list(z, name, key, count):
     return [z["%s/%s%d" % (name, key, j)] for j in range(count)]
 

@@ -1,6 +1,6 @@
 """Tape builder: CasADi's SX simplification rules and SXFunction::init, checked against the
-tape facts of the reference (instruction counts, work-vector sizes and op histograms that
-libcasadi produces for the same functions) and against the committed golden tapes."""
+tapes the reference's own libcasadi builds for the same functions (tests/golden/casadi.npz,
+written by tests/golden/make_casadi_golden.py; more cases in test_casadi_parity.py)."""
 import numpy as np
 import pytest
 
@@ -8,37 +8,31 @@ from casadi_gb300 import calculus as C
 from casadi_gb300 import sx as S
 from casadi_gb300 import workloads as W
 
-from helpers import golden_tape, load_npz
-
-# libcasadi 3.7.2 on the same functions (cart-pole RK4 step and 20-step rollout)
-REF_CARTPOLE = dict(n_instr=158, sz_w=27, hist={
-    "ADD": 40, "SUB": 5, "MUL": 69, "DIV": 8, "NEG": 2, "TWICE": 8, "SIN": 4, "COS": 4,
-    "CONST": 9, "INPUT": 5, "OUTPUT": 4})
-REF_ROLLOUT = dict(n_instr=3057, sz_w=122, hist={
-    "ADD": 899, "SUB": 100, "MUL": 1420, "DIV": 160, "NEG": 40, "SQ": 80, "TWICE": 160,
-    "SIN": 80, "COS": 80, "CONST": 9, "INPUT": 24, "OUTPUT": 5})
+from helpers import golden_tape, load_npz, tape_sha256
 
 
-def test_cartpole_tape_matches_reference():
-    t = W.cartpole_step().tape
-    assert t.n_instr == REF_CARTPOLE["n_instr"]
-    assert t.sz_w == REF_CARTPOLE["sz_w"]
-    assert t.histogram() == REF_CARTPOLE["hist"]
-
-
-def test_rollout_tape_matches_reference():
-    t = W.cartpole_rollout(20).tape
-    assert t.n_instr == REF_ROLLOUT["n_instr"]
-    assert t.sz_w == REF_ROLLOUT["sz_w"]
-    assert t.histogram() == REF_ROLLOUT["hist"]
 
 
 @pytest.mark.parametrize("name,make", [
     ("cartpole", W.cartpole_step),
     ("rollout", lambda: W.cartpole_rollout(20)),
-    ("dag", lambda: W.random_dag(n_in=16, n_nodes=800, n_out=6, seed=3)),
 ])
-def test_builder_reproduces_golden_tapes(name, make):
+def test_tape_matches_casadi(name, make):
+    z = load_npz("casadi.npz")
+    t = make().tape
+    assert t.n_instr == int(z[name + "/n_instr"]) and t.sz_w == int(z[name + "/sz_w"])
+    ops = z[name + "/op"]
+    assert t.histogram() == {C.OP_NAMES[int(o)]: int((ops == o).sum()) for o in np.unique(ops)}
+    assert tape_sha256(t) == str(z[name + "/tape_sha256"])
+
+
+@pytest.mark.parametrize("name,casadi_name,make", [
+    ("cartpole", "cartpole", W.cartpole_step),
+    ("rollout", "rollout", lambda: W.cartpole_rollout(20)),
+    ("dag", "dag_small", lambda: W.random_dag(n_in=16, n_nodes=800, n_out=6, seed=3)),
+])
+def test_builder_reproduces_golden_tapes(name, casadi_name, make):
+    """tapes.npz holds the builder's tapes of these functions; they are CasADi's."""
     z = load_npz("tapes.npz")
     g = golden_tape(z, name)
     t = make().tape
@@ -46,6 +40,7 @@ def test_builder_reproduces_golden_tapes(name, make):
         np.testing.assert_array_equal(getattr(t, f), getattr(g, f), err_msg=f)
     np.testing.assert_array_equal(t.d.view(np.uint64), g.d.view(np.uint64))
     assert t.sz_w == g.sz_w and t.nnz_in == g.nnz_in and t.nnz_out == g.nnz_out
+    assert tape_sha256(g) == str(load_npz("casadi.npz")[casadi_name + "/tape_sha256"])
 
 
 def _check_tape_wellformed(t):
