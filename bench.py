@@ -104,7 +104,7 @@ def structural_tangent_ops(tape, unit_dirs=True, ndir=None):
             elif op in (C.OP_NEG, C.OP_ASSIGN, C.OP_IF_ELSE_ZERO):
                 pass
             else:
-                total += 3 if (cb and cc) else 1
+                total += 2 if (cb and cc) else 1  # d1*xc, then one FMA with d0*xb
     return total * (1 if unit_dirs else (ndir or 1))
 
 
@@ -137,7 +137,7 @@ def structural_adjoint_ops(tape, seeded_out):
             elif op == C.OP_TWICE:
                 total += 1 if first else 2
             else:
-                total += 1 if first else 2
+                total += 1  # d*seed, or one FMA into the running adjoint
             act[slot] = True
     return total
 
@@ -223,6 +223,13 @@ class ClockSampler:
 
 
 # ---- FP64 peak, measured live ------------------------------------------------------------------
+def fp64_pipe_rates(R):
+    """The FP64 pipe's measured instruction rates (T thread-instructions/s) from the library's
+    chain probe: DFMA (the roofline denominator: every sweep instruction counts one), DADD,
+    DMUL."""
+    return {k: R.fp64_rate(k, reps=5) / 1e12 for k in ("dfma", "dadd", "dmul")}
+
+
 def fp64_peak_tflops(torch):
     """cuBLAS FP64 GEMM throughput (4096^3, best of 5) — the measured FP64 ceiling, in the
     spirit of the driver's cuBLAS bf16 figure."""
@@ -246,16 +253,11 @@ def fp64_peak_tflops(torch):
 # ---- CPU baseline (oracle port, all host threads, bounded sample) -------------------------------
 def cpu_step(tape, args, aseeds, n, threads, workload):
     import oracle as O
-    nz = sum(tape.nnz_in)
     if workload == "rollout20":
-        eye = np.eye(nz)
-        offs = np.cumsum([0] + tape.nnz_in)
-        fseeds = [np.ascontiguousarray(np.broadcast_to(eye[:, offs[j]:offs[j + 1], None],
-                                                       (nz, tape.nnz_in[j], n)))
-                  for j in range(len(tape.nnz_in))]
+        # the same step as the device's: one record of the partials per instance feeding the
+        # unit-seed Jacobian (structurally zero work skipped) and the cost adjoint
         t0 = time.perf_counter()
-        O.forward(tape, args, fseeds, n, threads)
-        O.reverse(tape, args, aseeds, n, threads)
+        O.jacobian_reverse(tape, args, aseeds, n, threads)
         return time.perf_counter() - t0
     t0 = time.perf_counter()
     if workload == "dag":
@@ -280,6 +282,31 @@ def cpu_baseline(F, args, aseeds, workload, budget_s=12.0):
     return {"value": m2 / t2, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": "%d of the instances, same step (oracle C restatement, OpenMP, %d threads)"
                       % (m2, threads)}
+
+
+def headline_parity(F, args_h, aseeds_h, res, jac, asens, m=1024, threads=None):
+    """Check of the timed step's own results, part of the CPU-baseline leg: the device's
+    values, Jacobian and cost adjoint of the last timed step on the first m instances against
+    the oracle's same step; values element-wise (relative), derivatives element-wise against
+    the magnitude of their chain-rule terms (oracle.magnitude)."""
+    import oracle as O
+    threads = threads or os.cpu_count() or 1
+    sub = [np.ascontiguousarray(x[..., :m]) for x in args_h]
+    seeds = [np.ascontiguousarray(x[..., :m]) for x in aseeds_h]
+    r, j, a = O.jacobian_reverse(F.tape, sub, seeds, m, threads)
+    with O.magnitude():
+        _, jm, am = O.jacobian_reverse(F.tape, sub, seeds, m, threads)
+    worst, same, total = 0.0, 0, 0
+    for got, want, mag in ([(x[..., :m].cpu().numpy(), y, np.abs(y)) for x, y in zip(res, r)] +
+                           [(x[..., :m].cpu().numpy(), y, z) for x, y, z in zip(jac, j, jm)] +
+                           [(x[..., :m].cpu().numpy(), y, z) for x, y, z in zip(asens, a, am)]):
+        d = np.abs(got - want)
+        worst = max(worst, float(np.max(np.where(d == 0, 0.0, d / np.maximum(mag, 1e-300)),
+                                        initial=0.0)))
+        same += int(np.sum(got.view(np.uint64) == want.view(np.uint64)))
+        total += got.size
+    return {"instances": m, "outputs_checked": total, "bitwise_equal_fraction": same / total,
+            "max_error_over_magnitude": worst, "bar": 1e-13, "ok": worst <= 1e-13}
 
 
 # ---- native arm ----------------------------------------------------------------------------------
@@ -556,6 +583,89 @@ def mpc_sparse_component(torch, stream, n=4096, intervals=100, reps=3, cpu=False
             "bitwise_equal": same, "host_setup_s": setup_s}
 
 
+def side_workload_component(torch, R, stream, name, dfma_tips, weights, cpu=False, reps=10):
+    """The other single-tape workloads of the benchmark set, each timed like the headline step
+    (L2 flushed between timed steps, CUDA events on the launching stream) with the per-launch
+    device time of every kernel family and a roofline entry per family:
+      cartpole: the RK4 step f(x[4],u) -> x_next[4] over 65536 instances, values only;
+      dag: the random DAG (64 inputs, 10000 nodes, 16 outputs) over 16384 instances: values +
+           adjoint of the sum of the outputs, then the bvec_t sp_forward (64 directions, input
+           k on bit k) and sp_reverse (output k on bit k) sweeps."""
+    F, n, args_h, aseeds_h, desc = make_workload(name)
+    ct = R.CudaTape(F)
+    dargs = [torch.from_numpy(x).cuda() for x in args_h]
+    daseeds = [torch.from_numpy(x).cuda() for x in aseeds_h]
+    res = [torch.empty((k, n), dtype=torch.float64, device="cuda") for k in F.tape.nnz_out]
+    asens = [torch.empty((1, k, n), dtype=torch.float64, device="cuda") for k in F.tape.nnz_in]
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    if name == "dag":
+        sp_in = torch.tensor([1 << k if k < 63 else -(1 << 63) for k in range(64)],
+                             dtype=torch.int64, device="cuda")[:, None].expand(64, n).contiguous()
+        sp_seed0 = torch.tensor([1 << k for k in range(16)], dtype=torch.int64,
+                                device="cuda")[:, None].expand(16, n).contiguous()
+        sp_seed = torch.empty_like(sp_seed0)
+        sp_sens = torch.empty((64, n), dtype=torch.int64, device="cuda")
+
+    def step():
+        if name == "dag":
+            ct.reverse(dargs, daseeds, res=res, asens=asens, stream=stream)
+            ct.sp_forward([sp_in], stream=stream)
+            sp_seed.copy_(sp_seed0)
+            sp_sens.zero_()
+            ct.sp_reverse([sp_sens], [sp_seed], stream=stream)
+        else:
+            ct.eval(dargs, res=res, stream=stream)
+
+    for _ in range(3):
+        step()
+    ct.sync()
+    R.profile(True)
+    R.profile_collect()
+    times = []
+    torch.cuda.synchronize()
+    for _ in range(reps):
+        flush.fill_(1.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step()
+        e1.record(stream)
+        times.append((e0, e1))
+    torch.cuda.synchronize()
+    prof = R.profile_collect()
+    R.profile(False)
+    ct.sync()
+    ms = sum(e0.elapsed_time(e1) for e0, e1 in times) / reps
+    work = algorithmic_flops(F.tape, weights)
+    per_inst = {"eval": work["eval"], "record": work["record"],
+                "adjoint": work["adjoint_per_dir"]}
+    sp_bytes = 8 * (sum(F.tape.nnz_in) + sum(F.tape.nnz_out))
+    roof = {}
+    for fam, (fms, nl) in prof.items():
+        if nl == 0:
+            continue
+        per_launch_ms = fms / nl
+        inst_per_launch = n * reps / nl
+        if fam in per_inst:
+            ach = per_inst[fam] * inst_per_launch / (per_launch_ms * 1e-3) / 1e12
+            roof[fam] = {"bound": "fp64", "achieved": ach, "peak": dfma_tips,
+                         "unit": "T FP64 instr/s", "frac": ach / dfma_tips,
+                         "ms_per_launch": per_launch_ms,
+                         "instr_per_instance": per_inst[fam]}
+        else:
+            ach = sp_bytes * inst_per_launch / (per_launch_ms * 1e-3) / 1e9
+            roof[fam] = {"bound": "smem/latency (bvec OR sweep; HBM bytes shown)",
+                         "achieved": ach, "unit": "GB/s", "ms_per_launch": per_launch_ms,
+                         "algorithmic_bytes_per_instance": sp_bytes}
+    out = {"workload": desc, "instances": n, "tape_instructions": F.tape.n_instr,
+           "ms_per_step": ms, "evals_per_s": n / (ms * 1e-3),
+           "kernel_ms_per_step": {k: v[0] / reps for k, v in prof.items() if v[1]},
+           "launches_per_step": {k: v[1] / reps for k, v in prof.items() if v[1]},
+           "roofline": roof}
+    if cpu:
+        out["cpu_baseline"] = cpu_baseline(F, args_h, aseeds_h, name, budget_s=6.0)
+    return out
+
+
 def run_mixed(a):
     """The mixed-size persistent batch alone (profiling captures of k_batch): one line with
     the persistent batch's rate and the one-launch-pair-per-item comparison."""
@@ -695,15 +805,20 @@ def run_native(a):
             lambda: ct.jacobian(dargs, res=res, jac=jac, stream=stream))
     ct.sync()
 
+    weights = load_weights()
+    rates = fp64_pipe_rates(R)
     if not a.no_mixed:
         cpu = not a.no_cpu and rank == 0
+        if a.workload == "rollout20":
+            for side in ("cartpole", "dag"):
+                comps[side] = side_workload_component(torch, R, stream, side, rates["dfma"],
+                                                      weights, cpu=cpu)
         comps["mixed_batch"] = mixed_component(torch, R, stream, cpu=cpu)
         comps["rollout100_autograd"] = rollout_autograd_component(torch, stream)
         comps["mpc_sparse_hessian"] = mpc_sparse_component(torch, stream, cpu=cpu)
         comps["mapaccum_mapsum"] = maps_component(torch, stream)
 
     # roofline of the dominant kernel family (device time from the per-launch events)
-    weights = load_weights()
     work = algorithmic_flops(F.tape, weights)
     fam_ms = {k: v for k, v in prof.items() if v[1] > 0}
     dom = max(fam_ms, key=lambda k: fam_ms[k][0])
@@ -713,7 +828,8 @@ def run_native(a):
     launches_per_step = dom_launches / a.steps
     flops_per_launch = per_inst * n / launches_per_step
     achieved = flops_per_launch / (dom_ms / dom_launches * 1e-3) / 1e12
-    peak = fp64_peak_tflops(torch) / 2.0  # DFMA instructions/s: the FP64-pipe instruction rate
+    peak = rates["dfma"]  # measured DFMA instructions/s: the FP64 pipe's instruction rate
+    dgemm = fp64_peak_tflops(torch)
     gpu_launches = sum(v[1] for v in prof.values())
     # DRAM bytes per launch of the dominant kernel from the committed ncu capture, scaled by
     # the instances one launch processes (traffic grows in proportion: the partial reads do)
@@ -789,19 +905,26 @@ def run_native(a):
         "gpu_launches": gpu_launches,
         "kernel_ms": {k: round(v[0], 4) for k, v in prof.items() if v[1]},
         "roofline": {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": peak,
-                     "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
+                     "unit": "T FP64 instr/s", "frac": achieved / peak if peak else None,
                      "traffic": traffic,
                      "traffic_unit": "bytes per launch (ncu, scaled from the committed capture)",
                      "flop": "one FP64-pipe instruction (DADD, DMUL, DFMA); libm calls weighted by "
-                             "casadi_gb300/op_weights.json; derivative sweeps count structural work",
-                     "peak_source": "cuBLAS FP64 GEMM FLOP/s measured in this run / 2 "
-                                    "(DFMA instructions per second)",
+                             "casadi_gb300/op_weights.json; derivative sweeps count structural work "
+                             "(a two-operand tangent: DMUL + DFMA; a later adjoint contribution: "
+                             "one DFMA)",
+                     "peak_source": "DFMA chain probe of this run (casadi_gb300_fp64_rate: "
+                                    "every thread of a full grid runs 8 independent DFMA "
+                                    "chains; thread-level instructions per second)",
+                     "fp64_pipe_rates_tips": rates,
+                     "cublas_dgemm_tflops": dgemm,
                      "io_bytes_per_step": io_bytes,
                      "hbm_gbs_io": io_bytes / (ms_step * 1e-3) / 1e9},
         "clocks": clk.summary(),
     }
     if not a.no_cpu:
         line["cpu_baseline"] = cpu_baseline(F, args_h, aseeds_h, a.workload)
+        if a.workload == "rollout20":
+            line["parity_check"] = headline_parity(F, args_h, aseeds_h, res, jac, asens)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -818,8 +941,10 @@ def run_reference(a):
     m = 256
     sub = lambda arrs, k: [np.ascontiguousarray(x[..., :k]) for x in arrs]  # noqa: E731
     t = cpu_step(F.tape, sub(args_h, m), sub(aseeds_h, m), m, threads, a.workload)
-    per_step = 150.0 / max(1, a.steps + a.warmup)
-    m = int(min(n, max(m, m * per_step / max(t, 1e-6) / 2)))
+    # every instance of the workload when warmup + steps fit in about three minutes, else the
+    # largest prefix that does
+    per_step = 180.0 / max(1, a.steps + a.warmup)
+    m = int(min(n, max(m, m * per_step / max(t, 1e-6) * 0.8)))
     sa, ss = sub(args_h, m), sub(aseeds_h, m)
     for _ in range(a.warmup):
         cpu_step(F.tape, sa, ss, m, threads, a.workload)
@@ -829,9 +954,12 @@ def run_reference(a):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 1,
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": sec * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": desc, "instances_per_step": m},
+            "data": "synthetic",
+            "config": {"workload": desc, "instances_per_step": m, "same_instances": m == n},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": "%d instances per step of the same workload" % m},
+                             "sample": "%d of the %d instances per step, the same step "
+                                       "(oracle C restatement, OpenMP, %d threads; CasADi's own "
+                                       "library cannot be built on this host)" % (m, n, threads)},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 

@@ -2451,3 +2451,4 @@ int casadi_gb300_map_jacobian_reverse(int id, int mem, int64_t n, const double* 
 #include "abi_noalloc.cuh"
 #include "abi_batch.cuh"
 #include "abi_maps.cuh"
+#include "abi_probe.cuh"

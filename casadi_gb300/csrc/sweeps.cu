@@ -359,27 +359,24 @@ __global__ void __launch_bounds__(32 * DW) k_adjoint_tape(const __grid_constant_
         }
         const double seed = wb[A * BS + tid];
         wb[A * BS + tid] = 0.0;
+        // a contribution d*seed is added with one fused multiply-add (one rounding)
         if (f & 2u) {
-          double c0;
-          switch (op) {
-            case D_ADD: case D_SUB: case D_ASSIGN: c0 = seed; break;
-            case D_NEG: c0 = d_neg(seed); break;
-            case D_TWICE: c0 = d_twice(seed); break;
-            default: c0 = __dmul_rn(d0, seed);
-          }
           double* w1 = wb + B * BS + tid;
-          *w1 = (f & 8u) ? c0 : __dadd_rn(*w1, c0);
+          switch (op) {
+            case D_ADD: case D_SUB: case D_ASSIGN: *w1 = __dadd_rn(*w1, seed); break;
+            case D_NEG: *w1 = __dsub_rn(*w1, seed); break;
+            case D_TWICE: *w1 = __dadd_rn(*w1, d_twice(seed)); break;
+            default: *w1 = __fma_rn(d0, seed, *w1);
+          }
         }
         if (f & 4u) {
-          double c1;
-          switch (op) {
-            case D_ADD: c1 = seed; break;
-            case D_SUB: c1 = d_neg(seed); break;
-            case D_IF_ELSE_ZERO: c1 = d1 == 0.0 ? 0.0 : seed; break;
-            default: c1 = __dmul_rn(d1, seed);
-          }
           double* w2 = wb + C * BS + tid;
-          *w2 = (f & 16u) ? c1 : __dadd_rn(*w2, c1);
+          switch (op) {
+            case D_ADD: *w2 = __dadd_rn(*w2, seed); break;
+            case D_SUB: *w2 = __dsub_rn(*w2, seed); break;
+            case D_IF_ELSE_ZERO: *w2 = __dadd_rn(*w2, d1 == 0.0 ? 0.0 : seed); break;
+            default: *w2 = __fma_rn(d1, seed, *w2);
+          }
         }
       }
       __syncthreads();
@@ -510,7 +507,7 @@ __device__ __forceinline__ void tangent_walk(const uint4* st, int ngr, const dou
 case (LK_GEN << 2) | 1u: R = __dmul_rn(P0[i][j], CGB_OP(cur.y, j, k)); break;              \
 case (LK_GEN << 2) | 2u: R = __dmul_rn(Q0[i][j], CGB_OP(cur.z, j, k)); break;              \
 case (LK_GEN << 2) | 3u:                                                                   \
-  R = __dadd_rn(__dmul_rn(P0[i][j], CGB_OP(cur.y, j, k)), __dmul_rn(Q0[i][j], CGB_OP(cur.z, j, k))); \
+  R = __fma_rn(P0[i][j], CGB_OP(cur.y, j, k), __dmul_rn(Q0[i][j], CGB_OP(cur.z, j, k)));         \
   break;                                                                                   \
 case (LK_ADD << 2) | 1u: R = CGB_OP(cur.y, j, k); break;                                   \
 case (LK_ADD << 2) | 2u: R = CGB_OP(cur.z, j, k); break;                                   \
@@ -756,7 +753,7 @@ __device__ __forceinline__ void adjoint_walk(const uint4* st, int ngr, const dou
             case (LK_GEN << 2) | 1u:
               CGB_J {
                 double& w1 = wj<IPT>(wb, cur.y, j);
-                w1 = __dadd_rn(w1, __dmul_rn(P0[i][j], sd[j]));
+                w1 = __fma_rn(P0[i][j], sd[j], w1);
               }
               break;
             case (LK_GEN << 2) | 3u: CGB_J wj<IPT>(wb, cur.y, j) = __dmul_rn(P0[i][j], sd[j]); break;
@@ -790,7 +787,7 @@ __device__ __forceinline__ void adjoint_walk(const uint4* st, int ngr, const dou
             case (LK_GEN << 2) | 1u:
               CGB_J {
                 double& w2 = wj<IPT>(wb, cur.z, j);
-                w2 = __dadd_rn(w2, __dmul_rn(Q0[i][j], sd[j]));
+                w2 = __fma_rn(Q0[i][j], sd[j], w2);
               }
               break;
             case (LK_GEN << 2) | 3u: CGB_J wj<IPT>(wb, cur.z, j) = __dmul_rn(Q0[i][j], sd[j]); break;

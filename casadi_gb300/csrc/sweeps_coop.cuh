@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(kCoopTanThreads)
               r = d_iszero(p1[q]) ? 0.0 : xc[q];
               break;
             default:
-              r = f == 3u ? __dadd_rn(__dmul_rn(p0[q], xb[q]), __dmul_rn(p1[q], xc[q]))
+              r = f == 3u ? __fma_rn(p0[q], xb[q], __dmul_rn(p1[q], xc[q]))
                           : (f == 1u ? __dmul_rn(p0[q], xb[q]) : __dmul_rn(p1[q], xc[q]));
           }
           wd[A * 32 + lane] = r;
@@ -403,7 +403,7 @@ __global__ void __launch_bounds__(kCoopTanThreads)
                 nb = first ? d_twice(s) : __dadd_rn(ob[q], d_twice(s));
                 break;
               default:
-                nb = first ? __dmul_rn(p0[q], s) : __dadd_rn(ob[q], __dmul_rn(p0[q], s));
+                nb = first ? __dmul_rn(p0[q], s) : __fma_rn(p0[q], s, ob[q]);
             }
             wd[B * 32 + lane] = nb;
             if (lane == 0) act[B] = 1;
@@ -424,7 +424,7 @@ __global__ void __launch_bounds__(kCoopTanThreads)
                            : (d_iszero(p1[q]) ? __dadd_rn(old, 0.0) : __dadd_rn(old, s));
                 break;
               default:
-                nc = first ? __dmul_rn(p1[q], s) : __dadd_rn(old, __dmul_rn(p1[q], s));
+                nc = first ? __dmul_rn(p1[q], s) : __fma_rn(p1[q], s, old);
             }
             wd[C * 32 + lane] = nc;
             if (lane == 0) act[C] = 1;

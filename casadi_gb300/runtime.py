@@ -879,6 +879,15 @@ FAMILIES = ("eval", "record", "tangent", "adjoint", "sp_forward", "sp_reverse", 
             "activity")
 
 
+def fp64_rate(kind="dfma", reps=5):
+    """Measured FP64 pipe rate of the current device (thread-level instructions per second)
+    for independent chains of DFMA, DADD or DMUL (casadi_gb300_fp64_rate)."""
+    k = {"dfma": 0, "dadd": 1, "dmul": 2}[kind]
+    out = ct.c_double()
+    check(load().casadi_gb300_fp64_rate(k, reps, ct.byref(out)))
+    return out.value
+
+
 def profile(enable=True):
     """Turn per-launch CUDA-event timing of the sweep kernels on or off."""
     check(load().casadi_gb300_profile(1 if enable else 0))

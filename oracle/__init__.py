@@ -186,6 +186,41 @@ def reverse(tape, args, aseeds, n, nthreads=1):
     return res, asens
 
 
+def jacobian_reverse(tape, args, aseeds, n, nthreads=1):
+    """Values, the unit-seed Jacobian (as :func:`jacobian`) and nadj adjoint directions (as
+    :func:`reverse`) from one record of the partials per instance."""
+    t = TapeArrays(tape)
+    args = _prep(args)
+    aseeds = _prep(aseeds)
+    nadj = next(s.shape[0] for s in aseeds if s is not None)
+    _check(args, tape.nnz_in, n, "arguments")
+    _check(aseeds, tape.nnz_out, n, "adjoint seeds", nadj)
+    nz = sum(tape.nnz_in)
+    res = _outs(tape.nnz_out, n)
+    jac = _outs(tape.nnz_out, n, nz)
+    asens = _outs(tape.nnz_in, n, nadj)
+    rc = lib().sxo_jacobian_reverse(ct.byref(t.struct), ct.c_long(n), _ptrs(args), _ptrs(res),
+                                    _ptrs(jac), ct.c_int(nadj), _ptrs(aseeds), _ptrs(asens),
+                                    ct.c_int(nthreads))
+    assert rc == 0
+    return res, jac, asens
+
+
+def libm_bound(tape, args, n, nthreads=1):
+    """Per output element, the first-order sensitivity to relative perturbations of the
+    tape's libm results: sum over libm instructions k of |d out / d w_k| * |w_k| (through
+    |partials|). Two evaluations whose libm results differ by at most c ulps give outputs
+    within about c * 2**-52 times this bound; shape (nnz_out[j], n) per output."""
+    t = TapeArrays(tape)
+    args = _prep(args)
+    _check(args, tape.nnz_in, n, "arguments")
+    out = _outs(tape.nnz_out, n)
+    rc = lib().sxo_libm_bound(ct.byref(t.struct), ct.c_long(n), _ptrs(args), _ptrs(out),
+                              ct.c_int(nthreads))
+    assert rc == 0
+    return out
+
+
 class magnitude:
     """Context in which forward / jacobian / reverse return magnitudes: the same sweeps over
     |partials| and |seeds|, i.e. per derivative entry the sum over its chain-rule paths of

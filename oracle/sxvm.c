@@ -293,6 +293,12 @@ static int nonzero_d1(int op) {
   }
 }
 
+/* Ops whose partials are exactly +-1 or 2 (their products with a seed are exact). */
+static int exact_partials(int op) {
+  return op == SXO_ADD || op == SXO_SUB || op == SXO_NEG || op == SXO_TWICE ||
+         op == SXO_ASSIGN;
+}
+
 /* one forward direction over one instance; seed(j, k) gives the seed (NAN-free) of input
  * nonzero k of input j, active(j, k) whether it is seeded */
 static void tangent_one(const sxo_tape* t, const double* dp, double* wd, char* act,
@@ -325,7 +331,8 @@ static void tangent_one(const sxo_tape* t, const double* dp, double* wd, char* a
         if (cb || cc) {
           double xb = cb ? wd[i1] : 0, xc = cc ? wd[i2] : 0, r;
           if (op == SXO_IF_ELSE_ZERO) r = d[1] == 0 ? 0 : xc;
-          else if (cb && cc) r = d[0] * xb + d[1] * xc;
+          /* both operands: one fused multiply-add, d0*xb + (d1*xc) rounded once */
+          else if (cb && cc) r = fma(d[0], xb, d[1] * xc);
           else if (cb) r = d[0] * xb;
           else r = d[1] * xc;
           wd[i0] = r;
@@ -381,10 +388,77 @@ int sxo_jacobian(const sxo_tape* t, long n, const double* const* arg, double* co
   return forward_impl(t, n, nz, 1, arg, res, 0, jac, nthreads);
 }
 
-int sxo_reverse(const sxo_tape* t, long n, int nadj, const double* const* arg,
-                double* const* res, const double* const* aseed, double* const* asens,
-                int nthreads) {
+/* nadj adjoint directions over one instance from its recorded partials dp */
+static void adjoint_one(const sxo_tape* t, const double* dp, double* wb, char* act, long n,
+                        long i, int nadj, const double* const* aseed, double* const* asens) {
+  for (int dir = 0; dir < nadj; ++dir) {
+    for (int s = 0; s < t->sz_w; ++s) { wb[s] = 0; act[s] = 0; }
+    /* asens starts at zero for every input nonzero (sx_function.cpp:1413-1422) */
+    for (int j = 0; j < t->n_in; ++j) {
+      if (!asens[j]) continue;
+      for (int k = 0; k < t->nnz_in[j]; ++k)
+        asens[j][((long)dir * t->nnz_in[j] + k) * n + i] = 0;
+    }
+    for (int k = t->n_instr - 1; k >= 0; --k) {
+      int op = t->op[k], i0 = t->i0[k], i1 = t->i1[k], i2 = t->i2[k];
+      const double* d = dp + 2 * (long)k;
+      switch (op) {
+        case SXO_INPUT: {
+          double* s = asens[i1];
+          if (s) s[((long)dir * t->nnz_in[i1] + i2) * n + i] = act[i0] ? wb[i0] : 0;
+          wb[i0] = 0; act[i0] = 0;
+        } break;
+        case SXO_OUTPUT: {
+          const double* s = aseed[i0];
+          if (s) {
+            double v = s[((long)dir * t->nnz_out[i0] + i2) * n + i];
+            if (g_magnitude) v = fabs(v);
+            wb[i1] = act[i1] ? wb[i1] + v : v;
+            act[i1] = 1;
+          }
+        } break;
+        case SXO_CONST: case SXO_PARAMETER: wb[i0] = 0; act[i0] = 0; break;
+        default: {
+          if (!act[i0]) break;
+          double seed = wb[i0], c;
+          wb[i0] = 0; act[i0] = 0;
+          /* a later contribution d*seed of a general op is added with one fused
+           * multiply-add; the partials of ADD, SUB, NEG, TWICE and ASSIGN are exact
+           * (+-1, 2), so their products are exact and added with one rounding */
+          if (nonzero_d0(op)) {
+            c = d[0] * seed;
+            wb[i1] = !act[i1] ? c : exact_partials(op) ? wb[i1] + c
+                                                       : fma(d[0], seed, wb[i1]);
+            act[i1] = 1;
+          }
+          if (sxo_ndeps(op) == 2 && nonzero_d1(op)) {
+            if (op == SXO_IF_ELSE_ZERO) {
+              c = d[1] == 0 ? 0 : seed;
+              wb[i2] = act[i2] ? wb[i2] + c : c;
+            } else {
+              c = d[1] * seed;
+              wb[i2] = !act[i2] ? c : exact_partials(op) ? wb[i2] + c
+                                                         : fma(d[1], seed, wb[i2]);
+            }
+            act[i2] = 1;
+          }
+        }
+      }
+    }
+  }
+}
+
+/* Values, tangents of the unit directions (jac, as sxo_jacobian) when jac is given, and
+ * nadj adjoint directions (asens, as sxo_reverse) when nadj > 0, all from one record of the
+ * partials per instance. */
+static int derivs_impl(const sxo_tape* t, long n, const double* const* arg, double* const* res,
+                       double* const* jac, int nadj, const double* const* aseed,
+                       double* const* asens, int nthreads) {
   int err = 0;
+  int in_off[256];
+  if (t->n_in > 256) return 1;
+  int nz = 0;
+  for (int j = 0; j < t->n_in; nz += t->nnz_in[j], ++j) in_off[j] = nz;
 #pragma omp parallel num_threads(nthreads > 0 ? nthreads : 1)
   {
     int sz = t->sz_w > 0 ? t->sz_w : 1;
@@ -399,54 +473,102 @@ int sxo_reverse(const sxo_tape* t, long n, int nadj, const double* const* arg,
 #pragma omp for schedule(static)
       for (long i = 0; i < n; ++i) {
         eval_partials(t, n, i, arg, res, w, dp);
-        for (int dir = 0; dir < nadj; ++dir) {
-          for (int s = 0; s < t->sz_w; ++s) { wb[s] = 0; act[s] = 0; }
-          /* asens starts at zero for every input nonzero (sx_function.cpp:1413-1422) */
-          for (int j = 0; j < t->n_in; ++j) {
-            if (!asens[j]) continue;
-            for (int k = 0; k < t->nnz_in[j]; ++k)
-              asens[j][((long)dir * t->nnz_in[j] + k) * n + i] = 0;
-          }
-          for (int k = t->n_instr - 1; k >= 0; --k) {
-            int op = t->op[k], i0 = t->i0[k], i1 = t->i1[k], i2 = t->i2[k];
-            const double* d = dp + 2 * (long)k;
-            switch (op) {
-              case SXO_INPUT: {
-                double* s = asens[i1];
-                if (s) s[((long)dir * t->nnz_in[i1] + i2) * n + i] = act[i0] ? wb[i0] : 0;
-                wb[i0] = 0; act[i0] = 0;
-              } break;
-              case SXO_OUTPUT: {
-                const double* s = aseed[i0];
-                if (s) {
-                  double v = s[((long)dir * t->nnz_out[i0] + i2) * n + i];
-                  if (g_magnitude) v = fabs(v);
-                  wb[i1] = act[i1] ? wb[i1] + v : v;
-                  act[i1] = 1;
-                }
-              } break;
-              case SXO_CONST: case SXO_PARAMETER: wb[i0] = 0; act[i0] = 0; break;
-              default: {
-                if (!act[i0]) break;
-                double seed = wb[i0], c;
-                wb[i0] = 0; act[i0] = 0;
-                if (nonzero_d0(op)) {
-                  c = d[0] * seed;
-                  wb[i1] = act[i1] ? wb[i1] + c : c;
-                  act[i1] = 1;
-                }
-                if (sxo_ndeps(op) == 2 && nonzero_d1(op)) {
-                  c = op == SXO_IF_ELSE_ZERO ? (d[1] == 0 ? 0 : seed) : d[1] * seed;
-                  wb[i2] = act[i2] ? wb[i2] + c : c;
-                  act[i2] = 1;
-                }
-              }
-            }
-          }
-        }
+        if (jac)
+          for (int dir = 0; dir < nz; ++dir)
+            tangent_one(t, dp, wb, act, in_off, dir, n, i, dir, 0, jac);
+        if (nadj > 0) adjoint_one(t, dp, wb, act, n, i, nadj, aseed, asens);
       }
     }
     free(w); free(wb); free(act); free(dp);
+  }
+  return err;
+}
+
+int sxo_reverse(const sxo_tape* t, long n, int nadj, const double* const* arg,
+                double* const* res, const double* const* aseed, double* const* asens,
+                int nthreads) {
+  return derivs_impl(t, n, arg, res, 0, nadj, aseed, asens, nthreads);
+}
+
+int sxo_jacobian_reverse(const sxo_tape* t, long n, const double* const* arg,
+                         double* const* res, double* const* jac, int nadj,
+                         const double* const* aseed, double* const* asens, int nthreads) {
+  return derivs_impl(t, n, arg, res, jac, nadj, aseed, asens, nthreads);
+}
+
+/* Ops whose results are libm calls (not correctly rounded in general, so two libms may
+ * return different last bits): everything but the IEEE-exact arithmetic, comparisons and
+ * selections. */
+static int is_libm(int op) {
+  switch (op) {
+    case SXO_EXP: case SXO_LOG: case SXO_POW: case SXO_CONSTPOW: case SXO_SIN: case SXO_COS:
+    case SXO_TAN: case SXO_ASIN: case SXO_ACOS: case SXO_ATAN: case SXO_ERF: case SXO_SINH:
+    case SXO_COSH: case SXO_TANH: case SXO_ASINH: case SXO_ACOSH: case SXO_ATANH:
+    case SXO_ATAN2: case SXO_ERFINV: case SXO_LOG1P: case SXO_EXPM1: case SXO_HYPOT:
+      return 1;
+    default: return 0;
+  }
+}
+
+/* First-order sensitivity of every output to relative perturbations of the libm results:
+ * bound[j][nz] = sum over libm instructions k of |d out(j,nz) / d w_k| * |w_k|, the
+ * derivative taken through |partials| (one magnitude adjoint sweep per output nonzero).
+ * If two evaluations differ only in that each libm result may be off by up to c ulps, their
+ * outputs differ by at most about c * 2^-52 * bound (to first order). */
+int sxo_libm_bound(const sxo_tape* t, long n, const double* const* arg, double* const* bound,
+                   int nthreads) {
+  int err = 0;
+#pragma omp parallel num_threads(nthreads > 0 ? nthreads : 1)
+  {
+    int sz = t->sz_w > 0 ? t->sz_w : 1;
+    long ni = t->n_instr > 0 ? t->n_instr : 1;
+    double* w = (double*)malloc(sizeof(double) * sz);
+    double* wb = (double*)malloc(sizeof(double) * sz);
+    double* dp = (double*)malloc(sizeof(double) * 2 * ni);
+    double* fv = (double*)malloc(sizeof(double) * ni);
+    if (!w || !wb || !dp || !fv) {
+#pragma omp atomic write
+      err = 1;
+    } else {
+#pragma omp for schedule(static)
+      for (long i = 0; i < n; ++i) {
+        /* values, partials and every instruction's own result */
+        for (int k = 0; k < t->n_instr; ++k) {
+          int op = t->op[k], i0 = t->i0[k], i1 = t->i1[k], i2 = t->i2[k];
+          fv[k] = 0;
+          switch (op) {
+            case SXO_CONST: w[i0] = t->d[k]; break;
+            case SXO_INPUT: w[i0] = arg[i1] ? arg[i1][(long)i2 * n + i] : 0; break;
+            case SXO_OUTPUT: break;
+            default: {
+              double x = w[i1], y = w[i2];
+              double f = sxo_fun(op, x, y);
+              sxo_der(op, x, y, f, dp + 2 * (long)k);
+              w[i0] = fv[k] = f;
+            }
+          }
+        }
+        for (int ko = 0; ko < t->n_instr; ++ko) {
+          if (t->op[ko] != SXO_OUTPUT || !bound[t->i0[ko]]) continue;
+          for (int s = 0; s < t->sz_w; ++s) wb[s] = 0;
+          double acc = 0;
+          wb[t->i1[ko]] = 1;
+          for (int k = ko - 1; k >= 0; --k) {
+            int op = t->op[k], i0 = t->i0[k], i1 = t->i1[k], i2 = t->i2[k];
+            if (op == SXO_OUTPUT) continue;
+            double seed = wb[i0];
+            wb[i0] = 0;
+            if (op == SXO_CONST || op == SXO_INPUT || op == SXO_PARAMETER || seed == 0) continue;
+            if (is_libm(op)) acc += seed * fabs(fv[k]);
+            const double* d = dp + 2 * (long)k;
+            wb[i1] += fabs(d[0]) * seed;
+            if (sxo_ndeps(op) == 2) wb[i2] += fabs(d[1]) * seed;
+          }
+          bound[t->i0[ko]][(long)t->i2[ko] * n + i] = acc;
+        }
+      }
+    }
+    free(w); free(wb); free(dp); free(fv);
   }
   return err;
 }

@@ -44,12 +44,17 @@ int sxo_jacobian(const sxo_tape* t, long n, const double* const* arg, double* co
 int sxo_reverse(const sxo_tape* t, long n, int nadj, const double* const* arg,
                 double* const* res, const double* const* aseed, double* const* asens,
                 int nthreads);
+int sxo_jacobian_reverse(const sxo_tape* t, long n, const double* const* arg,
+                         double* const* res, double* const* jac, int nadj,
+                         const double* const* aseed, double* const* asens, int nthreads);
 int sxo_sp_forward(const sxo_tape* t, long n, const uint64_t* const* arg, uint64_t* const* res,
                    int nthreads);
 int sxo_sp_reverse(const sxo_tape* t, long n, uint64_t* const* arg, uint64_t* const* res,
                    int nthreads);
 int sxo_zero_checker(int which, int op);
 void sxo_set_magnitude(int on);
+int sxo_libm_bound(const sxo_tape* t, long n, const double* const* arg, double* const* bound,
+                   int nthreads);
 int sxo_activity(const sxo_tape* t, long n, const uint64_t* const* arg, uint64_t* const* res,
                  int nthreads);
 #endif

@@ -6,13 +6,16 @@ Bars (the fixtures were computed with the generating host's glibc; the GPU uses 
   * sparsity sweeps and Jacobian patterns: identical;
   * values of tapes of IEEE-exact ops (+,-,*,/,sqrt and exact sign/compare/select ops, no FMA
     contraction): bit-exact;
-  * values where libm transcendentals are involved: relative error <= 1e-13 per element;
+  * values where libm transcendentals are involved: relative error <= 1e-13 per element, or,
+    where an output cancels (or a long trajectory amplifies), within 4 ulp-sized relative
+    perturbations of every libm result propagated to that output (oracle.libm_bound: the sum
+    over libm instructions of |d out / d w_k| * |w_k|);
   * the numeric AD sweeps against CasADi's symbolic derivative Functions: |a - b| <= 1e-13 x
     the magnitude of the derivative's chain-rule terms per element (oracle.magnitude on the
     same inputs); the two round differently by construction (CasADi simplifies inv(y)*seed to
     seed/y, and so on), so no bit parity is possible there;
   * CasADi's derivative Function f.reverse(1) evaluated by the value sweep (what a mapped
-    derivative runs): bit-exact on exact tapes, <= 1e-13 relative elsewhere.
+    derivative runs): bit-exact on exact tapes, the value bars above elsewhere.
 """
 import os
 
@@ -20,18 +23,20 @@ import numpy as np
 import pytest
 
 import oracle as O
+from casadi_gb300 import calculus as C
 from casadi_gb300 import sx as S
 from casadi_gb300 import workloads as W
 from casadi_gb300.runtime import CudaTape
 
 from helpers import (EXACT_OPS, GOLDEN, assert_bitexact, casadi_tape, golden_list, load_npz,
-                     rel_err, same_bits, tape_sha256)
+                     same_bits, tape_sha256)
 
 pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
 AD_RTOL = 1e-13
 VALUE_RTOL = 1e-13
+LIBM_ULPS = 4
 EXACT_MAP = np.array([0, 1, 3, 3, 8, 3, 8, 1, 8, 0], np.int32)
 
 
@@ -51,7 +56,8 @@ def host(ts):
 
 
 def is_exact(t):
-    return all(int(o) in EXACT_OPS or o in (44, 45, 46) for o in np.unique(t.op))
+    return all(int(o) in EXACT_OPS or int(o) in (C.OP_CONST, C.OP_INPUT, C.OP_OUTPUT)
+               for o in np.unique(t.op))
 
 
 def assert_within_magnitude(got, ref, mag, what, rtol=AD_RTOL):
@@ -64,12 +70,22 @@ def assert_within_magnitude(got, ref, mag, what, rtol=AD_RTOL):
                              % (what, int(bad.sum()), bad.size, rtol, i, got[i], ref[i], mag[i]))
 
 
-def assert_values(got, ref, exact, what):
+def assert_values(got, ref, exact, what, bound=None):
+    """Bit-exact on exact tapes; else relative error <= 1e-13 or, given the libm bound of the
+    output, a difference within LIBM_ULPS ulps of every libm result propagated to it."""
     if exact:
         assert_bitexact(got, ref, what)
-    else:
-        e = rel_err(got, ref)
-        assert e <= VALUE_RTOL, "%s: relative error %.3e > %.0e" % (what, e, VALUE_RTOL)
+        return
+    got, ref = np.asarray(got, np.float64), np.asarray(ref, np.float64)
+    d = np.abs(got - ref)
+    ok = same_bits(got, ref) | (d <= VALUE_RTOL * np.abs(ref))
+    if bound is not None:
+        ok |= d <= LIBM_ULPS * 2.0**-52 * np.asarray(bound)
+    if not ok.all():
+        i = tuple(np.argwhere(~ok)[0])
+        raise AssertionError("%s: %d of %d beyond the bar, e.g. %s: %r vs %r%s" % (
+            what, int((~ok).sum()), ok.size, i, got[i], ref[i],
+            "" if bound is None else " (libm bound %r)" % np.asarray(bound)[i]))
 
 
 def tape_of(z, name):
@@ -86,13 +102,10 @@ def test_eval_matches_casadi(gpu_lib, z, name):
     ct = CudaTape(t)
     args = golden_list(z, name, "arg", len(t.nnz_in))
     res = host(ct.eval(dev(args)))
+    bound = None if is_exact(t) else O.libm_bound(t, args, args[0].shape[1])
     for j, r in enumerate(golden_list(z, name, "res", len(t.nnz_out))):
-        if name == "rollout100":
-            # a hundred RK4 steps of the cart-pole amplify the <= 1-ulp differences between
-            # CUDA's and glibc's sin/cos; the element-wise bar there is the measured one
-            assert rel_err(res[j], r) <= 1e-11, name
-        else:
-            assert_values(res[j], r, is_exact(t), "%s res%d" % (name, j))
+        assert_values(res[j], r, is_exact(t), "%s res%d" % (name, j),
+                      None if bound is None else bound[j])
     ct.sync()
 
 
@@ -184,9 +197,12 @@ def test_casadi_reverse_function_on_the_value_sweep(gpu_lib, z, name):
     args = golden_list(z, name, "arg", nin)
     seeds = [s[0] for s in golden_list(z, name, "aseed", nout)]
     ct = CudaTape(B.tape)
-    res = host(ct.eval(dev(args + [None] * nout + seeds)))
+    bargs = args + [None] * nout + seeds
+    res = host(ct.eval(dev(bargs)))
+    bound = None if is_exact(f.tape) else O.libm_bound(B.tape, bargs, args[0].shape[1])
     for j, r in enumerate(golden_list(z, name, "asens", nin)):
-        assert_values(res[j], r[0], is_exact(f.tape), "%s reverse(1) %d" % (name, j))
+        assert_values(res[j], r[0], is_exact(f.tape), "%s reverse(1) %d" % (name, j),
+                      None if bound is None else bound[j])
     ct.sync()
 
 
@@ -248,7 +264,8 @@ def test_casadi_call_records_on_the_gpu(gpu_lib, z):
     ct = CudaTape(t, calls=[(step, c[:5].tolist(), c[5:].tolist()) for c in calls])
     args = golden_list(z, "rollout_calls", "arg", 2)
     res = host(ct.eval(dev(args)))
-    assert_values(res[0], z["rollout_calls/res0"], False, "rollout calls")
+    bound = O.libm_bound(W.cartpole_rollout(20).tape, args, args[0].shape[1])
+    assert_values(res[0], z["rollout_calls/res0"], False, "rollout calls", bound[0])
     ct.sync()
 
 
@@ -259,5 +276,6 @@ def test_casadi_serialized_text_on_the_gpu(gpu_lib, z):
     res = host(ct.eval(dev(args)))
     ref = host(CudaTape(casadi_tape(z, "cartpole")).eval(dev(args)))
     assert_bitexact(res[0], ref[0], "deserialized vs in-memory")
-    assert_values(res[0], z["cartpole/res0"], False, "deserialized cartpole")
+    bound = O.libm_bound(casadi_tape(z, "cartpole"), args, args[0].shape[1])
+    assert_values(res[0], z["cartpole/res0"], False, "deserialized cartpole", bound[0])
     ct.sync()

@@ -8,6 +8,7 @@ import pytest
 
 import oracle as O
 from casadi_gb300 import calculus as C
+from casadi_gb300 import sx as S
 
 from helpers import (EXACT_OPS, RTOL, assert_bitexact, assert_close, golden_list, golden_tape,
                      load_npz, same_bits)
@@ -217,3 +218,32 @@ def test_oracle_mapsum_matches_unrolled_instances():
     one = [np.zeros((8, 1), np.uint64)]
     O.sp_reverse(t, one, [np.array([[1], [2], [4]], np.uint64)], 1)
     assert np.array_equal(arg[0], one[0][:, 0]) and not seed[0].any()
+
+
+def test_libm_bound_on_hand_checked_tapes():
+    """sum over libm results of |d out / d w_k| * |w_k|: 3 sin(x) - x gives 3|sin x|;
+    exp(sin x) gives exp(sin x) (the exp) + exp(sin x)|sin x| (the sin through exp)."""
+    x = S.sym("x", 1)
+    f = S.Function("f", [x], [[S.sin(x[0]) * 3.0 - x[0], S.exp(S.sin(x[0]))]])
+    xs = np.array([0.5, -1e-3, 2.0, 0.0])
+    b = O.libm_bound(f.tape, [xs[None, :]], xs.size)[0]
+    np.testing.assert_allclose(b[0], 3 * np.abs(np.sin(xs)), rtol=1e-15)
+    e = np.exp(np.sin(xs))
+    np.testing.assert_allclose(b[1], e + e * np.abs(np.sin(xs)), rtol=1e-15)
+    # exact tapes have no libm term
+    g = S.Function("g", [x], [[x[0] * x[0] / (x[0] + 3.0)]])
+    assert (O.libm_bound(g.tape, [xs[None, :]], xs.size)[0] == 0).all()
+
+
+def test_magnitude_mode_is_the_sweep_over_absolute_values():
+    """In magnitude mode the adjoint of a * b - c * d at (2, -3, 5, 7) with seed -1 is
+    (|b|, |a|, |d|, |c|) = (3, 2, 7, 5); outside it the signed adjoint returns."""
+    v = S.sym("v", 4)
+    f = S.Function("f", [v], [[v[0] * v[1] - v[2] * v[3]]])
+    args = [np.array([[2.0], [-3.0], [5.0], [7.0]])]
+    seed = [-np.ones((1, 1, 1))]
+    with O.magnitude():
+        _, m = O.reverse(f.tape, args, seed, 1)
+    np.testing.assert_array_equal(m[0][0][:, 0], [3, 2, 7, 5])
+    _, a = O.reverse(f.tape, args, seed, 1)
+    np.testing.assert_array_equal(a[0][0][:, 0], [3, -2, 7, 5])
