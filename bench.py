@@ -59,9 +59,9 @@ def make_workload(name, instances=None):
 
 # ---- algorithmic work per instance --------------------------------------------------------------
 # Counted in FP64-pipe instructions (DADD, DMUL and DFMA each count one; a libm call counts its
-# measured DFMA-instruction equivalents from op_weights.json): that is what bounds these sweeps
-# on GB300. The ceiling in the same unit is the DFMA instruction rate, i.e. the cuBLAS DGEMM
-# FLOP/s measured in the run divided by two.
+# measured DFMA-instruction equivalents from op_weights.json), split by kind: on GB300 the pipe
+# issues a DFMA chain at a higher rate than DADD or DMUL (casadi_gb300_fp64_rate, measured in the
+# same run), so each kernel's ceiling is the rate of its own instruction mix.
 def _carries(op):
     from casadi_gb300 import calculus as C
     zero_d0 = {C.OP_LT, C.OP_LE, C.OP_EQ, C.OP_NE, C.OP_NOT, C.OP_AND, C.OP_OR, C.OP_FLOOR,
@@ -71,15 +71,22 @@ def _carries(op):
     return op not in zero_d0, op in d1
 
 
+def _mix():
+    return {"dadd": 0, "dmul": 0, "dfma": 0}
+
+
 def structural_tangent_ops(tape, unit_dirs=True, ndir=None):
-    """FP64 instructions of the forward sweep with unit seeds, summed over all directions,
-    following the structural rules the sweeps apply (same cases as the tangent kernel)."""
+    """FP64 instructions of the forward sweep with unit seeds, summed over all directions and
+    split by kind, following the structural rules the sweeps apply (the tangent kernel's
+    cases): ADD/SUB of two carried operands one DADD; a general op one DMUL per carried
+    operand, two carried: DMUL + DFMA; TWICE, NEG, ASSIGN, IF_ELSE_ZERO none (integer
+    exponent/sign operations, selections)."""
     from casadi_gb300 import calculus as C
     nz = sum(tape.nnz_in)
     offs = np.cumsum([0] + list(tape.nnz_in))
     ops, i0, i1, i2 = (tape.op.tolist(), tape.i0.tolist(), tape.i1.tolist(), tape.i2.tolist())
     carry = {op: _carries(op) for op in set(ops)}
-    total = 0
+    mix = _mix()
     for d in range(nz if unit_dirs else 1):
         act = [False] * max(1, tape.sz_w)
         for k, op in enumerate(ops):
@@ -98,27 +105,30 @@ def structural_tangent_ops(tape, unit_dirs=True, ndir=None):
             if not (cb or cc):
                 continue
             if op in (C.OP_ADD, C.OP_SUB):
-                total += 1 if (cb and cc) else 0
-            elif op == C.OP_TWICE:
-                total += 1
-            elif op in (C.OP_NEG, C.OP_ASSIGN, C.OP_IF_ELSE_ZERO):
+                mix["dadd"] += 1 if (cb and cc) else 0
+            elif op in (C.OP_TWICE, C.OP_NEG, C.OP_ASSIGN, C.OP_IF_ELSE_ZERO):
                 pass
             else:
-                total += 2 if (cb and cc) else 1  # d1*xc, then one FMA with d0*xb
-    return total * (1 if unit_dirs else (ndir or 1))
+                mix["dmul"] += 1
+                mix["dfma"] += 1 if (cb and cc) else 0
+    scale = 1 if unit_dirs else (ndir or 1)
+    return {k: v * scale for k, v in mix.items()}
 
 
 def structural_adjoint_ops(tape, seeded_out):
-    """FP64 instructions of one adjoint direction (same cases as the adjoint kernel)."""
+    """FP64 instructions of one adjoint direction by kind (the adjoint kernel's cases): a
+    seeded output or an ADD/SUB/ASSIGN/NEG/TWICE/IF_ELSE_ZERO contribution that is not the
+    slot's first one DADD; a general op's contribution DMUL when first, else one DFMA into the
+    running adjoint."""
     from casadi_gb300 import calculus as C
     ops, i0, i1, i2 = (tape.op.tolist(), tape.i0.tolist(), tape.i1.tolist(), tape.i2.tolist())
     act = [False] * max(1, tape.sz_w)
-    total = 0
+    mix = _mix()
     for k in range(len(ops) - 1, -1, -1):
         op = ops[k]
         if op == C.OP_OUTPUT:
             if seeded_out[i0[k]]:
-                total += 1 if act[i1[k]] else 0
+                mix["dadd"] += 1 if act[i1[k]] else 0
                 act[i1[k]] = True
             continue
         if op in (C.OP_INPUT, C.OP_CONST):
@@ -128,36 +138,50 @@ def structural_adjoint_ops(tape, seeded_out):
             continue
         act[i0[k]] = False
         c0, c1 = _carries(op)
-        for slot, carries, which in ((i1[k], c0, 0), (i2[k], c1 and op in C.BINARY_OPS, 1)):
+        for slot, carries in ((i1[k], c0), (i2[k], c1 and op in C.BINARY_OPS)):
             if not carries:
                 continue
             first = not act[slot]
-            if op in (C.OP_ADD, C.OP_SUB, C.OP_ASSIGN, C.OP_NEG, C.OP_IF_ELSE_ZERO):
-                total += 0 if first else 1
-            elif op == C.OP_TWICE:
-                total += 1 if first else 2
+            if op in (C.OP_ADD, C.OP_SUB, C.OP_ASSIGN, C.OP_NEG, C.OP_IF_ELSE_ZERO, C.OP_TWICE):
+                mix["dadd"] += 0 if first else 1
             else:
-                total += 1  # d*seed, or one FMA into the running adjoint
+                mix["dmul" if first else "dfma"] += 1
             act[slot] = True
-    return total
+    return mix
 
 
-def algorithmic_flops(tape, weights, seeded_out=None, unit_dirs=True):
-    """FP64-pipe instructions per instance for each kernel family (see above)."""
+SIMPLE_OPS = ("ADD", "SUB", "MUL", "SQ", "IF_ELSE_ZERO", "LT", "LE", "EQ", "NE", "FMIN", "FMAX")
+
+
+def algorithmic_flops(tape, weights, rates, seeded_out=None, unit_dirs=True):
+    """Per instance and kernel family: FP64-pipe instructions ("instr") and their time at the
+    measured rates expressed in DFMA-chain instructions ("dfma_time"); the family's ceiling
+    is rate_dfma * instr / dfma_time. Value and record sweeps: simple ops (one DADD or DMUL
+    each, weight 1) at the DADD/DMUL rate, libm calls at their measured DFMA equivalents
+    (op_weights.json); TWICE, the sign-bit ops and selections cost no FP64 instruction."""
     from casadi_gb300 import calculus as C
-    val = rec = 0.0
+    slow = rates["dfma"] / min(rates["dadd"], rates["dmul"])
+    out = {"eval": {"instr": 0.0, "dfma_time": 0.0}, "record": {"instr": 0.0, "dfma_time": 0.0}}
     for op, cnt in zip(*np.unique(tape.op, return_counts=True)):
         op = int(op)
         if op in (C.OP_CONST, C.OP_INPUT, C.OP_OUTPUT):
             continue
         name = C.OP_NAMES[op]
-        w = float(weights.get(name, 1.0))
-        val += cnt * w
-        rec += cnt * (w + float(weights.get(name + "_partial", 0.0)))
+        w = 0.0 if name == "TWICE" else float(weights.get(name, 1.0))
+        t = w * (slow if name in SIMPLE_OPS else 1.0)
+        wp = float(weights.get(name + "_partial", 0.0))
+        out["eval"]["instr"] += cnt * w
+        out["eval"]["dfma_time"] += cnt * t
+        out["record"]["instr"] += cnt * (w + wp)
+        out["record"]["dfma_time"] += cnt * (t + wp)
     seeded_out = seeded_out or [True] * len(tape.nnz_out)
-    return dict(eval=val, record=rec,
-                tangent_all_dirs=float(structural_tangent_ops(tape, unit_dirs)),
-                adjoint_per_dir=float(structural_adjoint_ops(tape, seeded_out)))
+    for fam, mix in (("tangent", structural_tangent_ops(tape, unit_dirs)),
+                     ("adjoint", structural_adjoint_ops(tape, seeded_out))):
+        out[fam] = {"instr": float(sum(mix.values())), "mix": mix,
+                    "dfma_time": mix["dfma"] + (mix["dadd"] + mix["dmul"]) * slow}
+    for v in out.values():
+        v["peak"] = rates["dfma"] * v["instr"] / v["dfma_time"] if v["dfma_time"] else None
+    return out
 
 
 def load_weights():
@@ -227,7 +251,8 @@ def fp64_pipe_rates(R):
     """The FP64 pipe's measured instruction rates (T thread-instructions/s) from the library's
     chain probe: DFMA (the roofline denominator: every sweep instruction counts one), DADD,
     DMUL."""
-    return {k: R.fp64_rate(k, reps=5) / 1e12 for k in ("dfma", "dadd", "dmul")}
+    return {k: R.fp64_rate(k, reps=5) / 1e12
+            for k in ("dfma", "dadd", "dmul", "dmul_as_dfma", "dadd_as_dfma")}
 
 
 def fp64_peak_tflops(torch):
@@ -583,7 +608,7 @@ def mpc_sparse_component(torch, stream, n=4096, intervals=100, reps=3, cpu=False
             "bitwise_equal": same, "host_setup_s": setup_s}
 
 
-def side_workload_component(torch, R, stream, name, dfma_tips, weights, cpu=False, reps=10):
+def side_workload_component(torch, R, stream, name, rates, weights, cpu=False, reps=10):
     """The other single-tape workloads of the benchmark set, each timed like the headline step
     (L2 flushed between timed steps, CUDA events on the launching stream) with the per-launch
     device time of every kernel family and a roofline entry per family:
@@ -635,9 +660,7 @@ def side_workload_component(torch, R, stream, name, dfma_tips, weights, cpu=Fals
     R.profile(False)
     ct.sync()
     ms = sum(e0.elapsed_time(e1) for e0, e1 in times) / reps
-    work = algorithmic_flops(F.tape, weights)
-    per_inst = {"eval": work["eval"], "record": work["record"],
-                "adjoint": work["adjoint_per_dir"]}
+    work = algorithmic_flops(F.tape, weights, rates)
     sp_bytes = 8 * (sum(F.tape.nnz_in) + sum(F.tape.nnz_out))
     roof = {}
     for fam, (fms, nl) in prof.items():
@@ -645,12 +668,13 @@ def side_workload_component(torch, R, stream, name, dfma_tips, weights, cpu=Fals
             continue
         per_launch_ms = fms / nl
         inst_per_launch = n * reps / nl
-        if fam in per_inst:
-            ach = per_inst[fam] * inst_per_launch / (per_launch_ms * 1e-3) / 1e12
-            roof[fam] = {"bound": "fp64", "achieved": ach, "peak": dfma_tips,
-                         "unit": "T FP64 instr/s", "frac": ach / dfma_tips,
+        if fam in ("eval", "record", "adjoint"):
+            w = work[fam]
+            ach = w["instr"] * inst_per_launch / (per_launch_ms * 1e-3) / 1e12
+            roof[fam] = {"bound": "fp64", "achieved": ach, "peak": w["peak"],
+                         "unit": "T FP64 instr/s", "frac": ach / w["peak"],
                          "ms_per_launch": per_launch_ms,
-                         "instr_per_instance": per_inst[fam]}
+                         "instr_per_instance": w["instr"], "mix": w.get("mix")}
         else:
             ach = sp_bytes * inst_per_launch / (per_launch_ms * 1e-3) / 1e9
             roof[fam] = {"bound": "smem/latency (bvec OR sweep; HBM bytes shown)",
@@ -811,7 +835,7 @@ def run_native(a):
         cpu = not a.no_cpu and rank == 0
         if a.workload == "rollout20":
             for side in ("cartpole", "dag"):
-                comps[side] = side_workload_component(torch, R, stream, side, rates["dfma"],
+                comps[side] = side_workload_component(torch, R, stream, side, rates,
                                                       weights, cpu=cpu)
         comps["mixed_batch"] = mixed_component(torch, R, stream, cpu=cpu)
         comps["rollout100_autograd"] = rollout_autograd_component(torch, stream)
@@ -819,17 +843,27 @@ def run_native(a):
         comps["mapaccum_mapsum"] = maps_component(torch, stream)
 
     # roofline of the dominant kernel family (device time from the per-launch events)
-    work = algorithmic_flops(F.tape, weights)
+    work = algorithmic_flops(F.tape, weights, rates,
+                             seeded_out=[bool(np.any(x)) for x in aseeds_h])
     fam_ms = {k: v for k, v in prof.items() if v[1] > 0}
     dom = max(fam_ms, key=lambda k: fam_ms[k][0])
     dom_ms, dom_launches = fam_ms[dom]
-    per_inst = {"eval": work["eval"], "record": work["record"],
-                "tangent": work["tangent_all_dirs"], "adjoint": work["adjoint_per_dir"]}.get(dom, 0.0)
+    per_inst = work[dom]["instr"] if dom in work else 0.0
     launches_per_step = dom_launches / a.steps
     flops_per_launch = per_inst * n / launches_per_step
     achieved = flops_per_launch / (dom_ms / dom_launches * 1e-3) / 1e12
-    peak = rates["dfma"]  # measured DFMA instructions/s: the FP64 pipe's instruction rate
+    # the FP64 pipe's measured rate for this kernel's instruction mix (DFMA chains issue
+    # faster than DADD/DMUL on this part)
+    peak = work[dom]["peak"] if dom in work else rates["dfma"]
     dgemm = fp64_peak_tflops(torch)
+    fam_roof = {}
+    for fam, (fms, nl) in fam_ms.items():
+        if fam in work:
+            ach_f = work[fam]["instr"] * n / (nl / a.steps) / (fms / nl * 1e-3) / 1e12
+            fam_roof[fam] = {"achieved": ach_f, "peak": work[fam]["peak"],
+                             "frac": ach_f / work[fam]["peak"], "ms_per_step": fms / a.steps,
+                             "instr_per_instance": work[fam]["instr"],
+                             "mix": work[fam].get("mix")}
     gpu_launches = sum(v[1] for v in prof.values())
     # DRAM bytes per launch of the dominant kernel from the committed ncu capture, scaled by
     # the instances one launch processes (traffic grows in proportion: the partial reads do)
@@ -912,9 +946,11 @@ def run_native(a):
                              "casadi_gb300/op_weights.json; derivative sweeps count structural work "
                              "(a two-operand tangent: DMUL + DFMA; a later adjoint contribution: "
                              "one DFMA)",
-                     "peak_source": "DFMA chain probe of this run (casadi_gb300_fp64_rate: "
-                                    "every thread of a full grid runs 8 independent DFMA "
-                                    "chains; thread-level instructions per second)",
+                     "peak_source": "FP64 chain probes of this run (casadi_gb300_fp64_rate: "
+                                    "every thread of a full grid runs 8 independent chains; "
+                                    "thread-level instructions per second), weighted by the "
+                                    "kernel's DFMA/DADD/DMUL mix",
+                     "families": fam_roof,
                      "fp64_pipe_rates_tips": rates,
                      "cublas_dgemm_tflops": dgemm,
                      "io_bytes_per_step": io_bytes,

@@ -23,8 +23,17 @@ constexpr int kProbeCtasPerSm = 8;
 
 __device__ double g_probe_sink;
 
+__device__ __forceinline__ double probe_fma(double a, double b, double c) {
+  double r;
+  asm volatile("fma.rn.f64 %0, %1, %2, %3;" : "=d"(r) : "d"(a), "d"(b), "d"(c));
+  return r;
+}
+
+// KIND 0 DFMA, 1 DADD, 2 DMUL, 3 a product issued as DFMA (x*a + m, m = -0 from a kernel
+// argument), 4 a sum issued as DFMA (x*u + b, u = 1 from a kernel argument)
 template <int KIND>
-__global__ void __launch_bounds__(kProbeThreads) k_fp64_rate(double a, double b) {
+__global__ void __launch_bounds__(kProbeThreads) k_fp64_rate(double a, double b, double u,
+                                                             double m) {
   double x[kProbeChains];
 #pragma unroll
   for (int c = 0; c < kProbeChains; ++c) x[c] = 1.0 + 1e-3 * (threadIdx.x + c);
@@ -34,7 +43,9 @@ __global__ void __launch_bounds__(kProbeThreads) k_fp64_rate(double a, double b)
     for (int c = 0; c < kProbeChains; ++c) {
       if (KIND == 0) x[c] = __fma_rn(x[c], a, b);
       else if (KIND == 1) x[c] = __dadd_rn(x[c], b);
-      else x[c] = __dmul_rn(x[c], a);
+      else if (KIND == 2) x[c] = __dmul_rn(x[c], a);
+      else if (KIND == 3) x[c] = probe_fma(x[c], a, m);
+      else x[c] = probe_fma(x[c], u, b);
     }
   }
   double s = 0.0;
@@ -50,8 +61,8 @@ __global__ void __launch_bounds__(kProbeThreads) k_fp64_rate(double a, double b)
 extern "C" {
 
 CASADI_GB300_API int casadi_gb300_fp64_rate(int kind, int reps, double* instr_per_s) {
-  if (!instr_per_s || kind < 0 || kind > 2 || reps < 1 || reps > 100)
-    return fail(CASADI_GB300_ERR_ARG, "fp64_rate: kind 0..2, reps 1..100, result pointer");
+  if (!instr_per_s || kind < 0 || kind > 4 || reps < 1 || reps > 100)
+    return fail(CASADI_GB300_ERR_ARG, "fp64_rate: kind 0..4, reps 1..100, result pointer");
   int dev = 0, sms = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
@@ -70,9 +81,14 @@ CASADI_GB300_API int casadi_gb300_fp64_rate(int kind, int reps, double* instr_pe
     return cuda_fail(e, "fp64_rate set-up");
   }
   auto launch = [&]() {
-    if (kind == 0) k_fp64_rate<0><<<grid, kProbeThreads, 0, s>>>(a, b);
-    else if (kind == 1) k_fp64_rate<1><<<grid, kProbeThreads, 0, s>>>(a, b);
-    else k_fp64_rate<2><<<grid, kProbeThreads, 0, s>>>(a, b);
+    const double u = 1.0, m = -0.0;
+    switch (kind) {
+      case 0: k_fp64_rate<0><<<grid, kProbeThreads, 0, s>>>(a, b, u, m); break;
+      case 1: k_fp64_rate<1><<<grid, kProbeThreads, 0, s>>>(a, b, u, m); break;
+      case 2: k_fp64_rate<2><<<grid, kProbeThreads, 0, s>>>(a, b, u, m); break;
+      case 3: k_fp64_rate<3><<<grid, kProbeThreads, 0, s>>>(a, b, u, m); break;
+      default: k_fp64_rate<4><<<grid, kProbeThreads, 0, s>>>(a, b, u, m); break;
+    }
     return cudaGetLastError();
   };
   float best_ms = 0.0f;

@@ -881,8 +881,9 @@ FAMILIES = ("eval", "record", "tangent", "adjoint", "sp_forward", "sp_reverse", 
 
 def fp64_rate(kind="dfma", reps=5):
     """Measured FP64 pipe rate of the current device (thread-level instructions per second)
-    for independent chains of DFMA, DADD or DMUL (casadi_gb300_fp64_rate)."""
-    k = {"dfma": 0, "dadd": 1, "dmul": 2}[kind]
+    for independent chains of DFMA, DADD, DMUL, or a product / sum issued as a DFMA
+    (casadi_gb300_fp64_rate)."""
+    k = {"dfma": 0, "dadd": 1, "dmul": 2, "dmul_as_dfma": 3, "dadd_as_dfma": 4}[kind]
     out = ct.c_double()
     check(load().casadi_gb300_fp64_rate(k, reps, ct.byref(out)))
     return out.value

@@ -502,7 +502,8 @@ CASADI_GB300_API int casadi_gb300_check_wait_timeout(void* stream);
 
 /* FP64 pipe rate of the current device, the ceiling of the sweeps: a full grid of threads
  * each running independent dependent chains of one FP64 instruction kind (0 DFMA, 1 DADD,
- * 2 DMUL); writes the best of reps timed launches as thread-level instructions per second.
+ * 2 DMUL, 3 a product issued as DFMA with a -0 addend, 4 a sum issued as DFMA with a unit
+ * factor); writes the best of reps timed launches as thread-level instructions per second.
  * Synchronous; creates and destroys its own stream and events. No counterpart in the
  * reference (a measurement of the hardware the sweeps run on). */
 CASADI_GB300_API int casadi_gb300_fp64_rate(int kind, int reps, double* instr_per_s);

@@ -220,9 +220,7 @@ def test_rollout100_gradient_through_autograd_matches_casadi(gpu_lib, z):
     for j, g in enumerate((tx.grad, tu.grad)):
         ref = z["rollout100/asens%d" % j][0]
         got = g.cpu().numpy()
-        # the 100-step trajectories amplify libm ulp differences in the values themselves
-        # (see test_eval_matches_casadi); the gradient bar is the measured one
-        assert_within_magnitude(got, ref, m[j][0], "rollout100 gradient %d" % j, rtol=1e-11)
+        assert_within_magnitude(got, ref, m[j][0], "rollout100 gradient %d" % j)
 
 
 def test_mpc_sparse_jacobian_and_hessian_match_casadi(gpu_lib, z):
