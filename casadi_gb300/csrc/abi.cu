@@ -102,6 +102,23 @@ struct TanPlan {
   }
 };
 
+// Window plan of the windowed tangent sweep (k_tangent_win) for one seed pattern: the tape cut
+// into windows, each window's entry block per direction group, and the launch shape.
+struct WinPlan {
+  int ndir = 0;
+  bool identity = false;
+  std::vector<int> dirmap;
+  std::vector<char> seeded;
+  bool usable = false;  // false: the sweep does not fit (or has too few directions to pay)
+  int dirs = 0, groups = 0, stages = 0, rows = 0, ents = 0, nwin = 0;
+  uint4* d_blocks = nullptr;
+  int4* d_meta = nullptr;
+  ~WinPlan() {
+    cudaFree(d_blocks);
+    cudaFree(d_meta);
+  }
+};
+
 // Activity plan of the adjoint sweep for one pattern of seeded outputs and chunk size.
 struct AdjPlan {
   int ch = 0;
@@ -169,6 +186,7 @@ struct Tape {
   std::vector<double> h_consts;  // constant pool (host copy, for inlining into callers)
   std::vector<u64> h_code;                            // padded instruction stream
   std::vector<std::unique_ptr<TanPlan>> tan_plans;
+  std::vector<std::unique_ptr<WinPlan>> win_plans;
   std::vector<std::unique_ptr<AdjPlan>> adj_plans;
 
   ~Tape() {
@@ -176,6 +194,7 @@ struct Tape {
     cudaGetDevice(&cur);
     if (cur != device) cudaSetDevice(device);
     tan_plans.clear();
+    win_plans.clear();
     adj_plans.clear();
     cudaFree(d_code);
     cudaFree(d_pofs);
@@ -557,27 +576,16 @@ std::vector<int> partial_starts(const Tape& t) {
 // Structural activity of the tangent sweep, per direction: an input slot is active when it is
 // seeded (unit seeds: when it is the direction's own input nonzero), an arithmetic result
 // when an operand that carries a derivative is active (the reference's 0*x -> 0, x+0 -> x).
-// Each direction group gets a compacted entry stream of the instructions with work for it.
-const TanPlan* tan_plan(Tape& t, int ndir, int dw, int ch, bool identity,
-                        const std::vector<char>& seeded, const std::vector<int>& dirmap,
-                        int* err) {
-  std::lock_guard<std::mutex> lk(t.shape_mtx);
-  for (auto& p : t.tan_plans)
-    if (p->ndir == ndir && p->dw == dw && p->ch == ch && p->identity == identity &&
-        (identity ? p->dirmap == dirmap : p->seeded == seeded))
-      return p.get();
-  auto p = std::make_unique<TanPlan>();
-  p->ndir = ndir;
-  p->dw = dw;
-  p->ch = ch;
-  p->identity = identity;
-  p->dirmap = dirmap;
-  p->seeded = seeded;
-  p->groups = (ndir + dw - 1) / dw;
+// Returns, per group of dw directions and instruction, 2 bits per direction (operand b / c
+// carries a derivative; an input or output: bit 0 when active).
+std::vector<unsigned short> tan_activity(const Tape& t, int ndir, int dw, bool identity,
+                                         const std::vector<char>& seeded,
+                                         const std::vector<int>& dirmap) {
+  const int groups = (ndir + dw - 1) / dw;
   const size_t nc = t.h_code.size();
   std::vector<int> off(t.n_in + 1, 0);
   for (int j = 0; j < t.n_in; ++j) off[j + 1] = off[j] + t.nnz_in[j];
-  std::vector<unsigned short> bits(static_cast<size_t>(p->groups) * nc, 0);
+  std::vector<unsigned short> bits(static_cast<size_t>(groups) * nc, 0);
   std::vector<char> act(std::max(1, t.sz_w));
   const int ncomp = identity ? ndir : 1;  // general seeds: every direction has the same pattern
   for (int d = 0; d < ncomp; ++d) {
@@ -611,6 +619,28 @@ const TanPlan* tan_plan(Tape& t, int ndir, int dw, int ch, bool identity,
             static_cast<unsigned short>(b << (2 * (dd % dw)));
     }
   }
+  return bits;
+}
+
+// Each direction group gets a compacted entry stream of the instructions with work for it.
+const TanPlan* tan_plan(Tape& t, int ndir, int dw, int ch, bool identity,
+                        const std::vector<char>& seeded, const std::vector<int>& dirmap,
+                        int* err) {
+  std::lock_guard<std::mutex> lk(t.shape_mtx);
+  for (auto& p : t.tan_plans)
+    if (p->ndir == ndir && p->dw == dw && p->ch == ch && p->identity == identity &&
+        (identity ? p->dirmap == dirmap : p->seeded == seeded))
+      return p.get();
+  auto p = std::make_unique<TanPlan>();
+  p->ndir = ndir;
+  p->dw = dw;
+  p->ch = ch;
+  p->identity = identity;
+  p->dirmap = dirmap;
+  p->seeded = seeded;
+  p->groups = (ndir + dw - 1) / dw;
+  const size_t nc = t.h_code.size();
+  const std::vector<unsigned short> bits = tan_activity(t, ndir, dw, identity, seeded, dirmap);
   // one stream per group of dw directions (the union of their work); an entry whose flags
   // differ between the group's directions becomes LK_MIXED with the real kind in x bits
   // 19-22 and the flags of direction k in bits 24+2k (see the tangent kernel)
@@ -662,6 +692,151 @@ const TanPlan* tan_plan(Tape& t, int ndir, int dw, int ch, bool identity,
   }
   t.tan_plans.push_back(std::move(p));
   return t.tan_plans.back().get();
+}
+
+// The windowed tangent sweep's plan. Directions per CTA and ring stages come from the
+// shared-memory budget (each direction's work vector, sz_w x 256 bytes, plus the stages);
+// the stage bytes are split between partial rows and entry-block room in the proportion the
+// tape needs them; windows are cut greedily, instruction by instruction, so that a window's
+// partial rows and its largest group's entry block (header included) fit one stage. Fewer
+// than 4 directions, or a work vector too long for 4 of them, give an unusable plan.
+constexpr int kWinMinDirs = 4;
+const WinPlan* win_plan(Tape& t, int ndir, bool identity, const std::vector<char>& seeded,
+                        const std::vector<int>& dirmap, int* err) {
+  std::lock_guard<std::mutex> lk(t.shape_mtx);
+  for (auto& p : t.win_plans)
+    if (p->ndir == ndir && p->identity == identity &&
+        (identity ? p->dirmap == dirmap : p->seeded == seeded))
+      return p.get();
+  auto p = std::make_unique<WinPlan>();
+  p->ndir = ndir;
+  p->identity = identity;
+  p->dirmap = dirmap;
+  p->seeded = seeded;
+  const long long wv = static_cast<long long>(std::max(1, t.sz_w)) * 256;
+  const long long budget = static_cast<long long>(max_smem_optin()) - 1024 - kWinBarBytes;
+  constexpr long long kMinStage = 16 * 256 + 256 * 16;
+  int dirs = std::min(ndir, kWinMaxDirs);
+  while (dirs >= kWinMinDirs && budget - dirs * wv < 2 * kMinStage) --dirs;
+  if (ndir < kWinMinDirs || dirs < kWinMinDirs) {
+    t.win_plans.push_back(std::move(p));
+    return t.win_plans.back().get();
+  }
+  p->groups = (ndir + dirs - 1) / dirs;
+  p->dirs = dirs = (ndir + p->groups - 1) / p->groups;  // balanced groups
+  const long long left = budget - dirs * wv;
+  p->stages = left >= 3 * kMinStage ? 3 : 2;
+  const long long per_stage = left / p->stages / 16 * 16;
+
+  const size_t nc = t.h_code.size();
+  const std::vector<int> pk = partial_starts(t);
+  const std::vector<unsigned short> bits = tan_activity(t, ndir, 1, identity, seeded, dirmap);
+  // entries of every stream (identity: one per direction; general seeds: one for all), with
+  // the instruction each belongs to, operand forwarding marked over the whole stream
+  const int nstreams = identity ? ndir : 1;
+  std::vector<std::vector<uint4>> ents(nstreams);
+  std::vector<std::vector<int>> at(nstreams);
+  for (int d = 0; d < nstreams; ++d) {
+    for (size_t k = 0; k < nc; ++k) {
+      const u64 w = t.h_code[k];
+      const unsigned op = dec_op(w);
+      const unsigned b = bits[static_cast<size_t>(d) * nc + k] & 3u;
+      if (!b && op != D_OUTPUT) continue;
+      ents[d].push_back(dir_entry(w, b, pk[k]));
+      at[d].push_back(static_cast<int>(k));
+    }
+    forward_operands(ents[d]);
+  }
+  // per instruction: partial rows, and the largest group's entry count
+  std::vector<int> rows_k(nc), ents_k(nc, 0);
+  long long rows_total = 0, ents_total = 0;
+  for (size_t k = 0; k < nc; ++k) {
+    rows_k[k] = (k + 1 < nc ? pk[k + 1] : t.n_partials) - pk[k];
+    rows_total += rows_k[k];
+  }
+  {
+    std::vector<int> cnt(static_cast<size_t>(p->groups) * nc, 0);
+    for (int d = 0; d < nstreams; ++d)
+      for (int k : at[d]) ++cnt[static_cast<size_t>(d / dirs) * nc + k];
+    for (int g = 0; g < (identity ? p->groups : 1); ++g)
+      for (size_t k = 0; k < nc; ++k)
+        ents_k[k] = std::max(ents_k[k], cnt[static_cast<size_t>(g) * nc + k]);
+    for (size_t k = 0; k < nc; ++k) ents_total += ents_k[k];
+  }
+  const int hdr_u4 = win_header_words(dirs) / 4;
+  // split a stage between partial rows and entry room as the tape needs them
+  const double share = static_cast<double>(rows_total * 256) /
+                       std::max<double>(1.0, rows_total * 256.0 + ents_total * 16.0);
+  p->rows = std::max(4, static_cast<int>(per_stage * share / 256));
+  p->ents = static_cast<int>((per_stage - static_cast<long long>(p->rows) * 256) / 16);
+  if (p->ents < hdr_u4 + dirs + 1) {
+    p->ents = hdr_u4 + dirs + 1;
+    p->rows = static_cast<int>((per_stage - p->ents * 16ll) / 256);
+  }
+  // windows: [win_k[w], win_k[w+1])
+  std::vector<int> win_k{0};
+  {
+    int r = 0, e = 0;
+    for (size_t k = 0; k < nc; ++k) {
+      if (r + rows_k[k] > p->rows || hdr_u4 + e + ents_k[k] > p->ents) {
+        win_k.push_back(static_cast<int>(k));
+        r = e = 0;
+      }
+      r += rows_k[k];
+      e += ents_k[k];
+    }
+    win_k.push_back(static_cast<int>(nc));
+    if (win_k.size() >= 2 && win_k[win_k.size() - 2] == static_cast<int>(nc)) win_k.pop_back();
+  }
+  p->nwin = static_cast<int>(win_k.size()) - 1;
+  // blocks: header words [p0, rows, off_0 .. off_dirs] padded to 16 bytes, then the entries of
+  // the group's directions in order
+  std::vector<unsigned> words;
+  std::vector<int4> meta(static_cast<size_t>(p->groups) * p->nwin);
+  std::vector<size_t> pos(nstreams, 0);  // next entry of each stream
+  for (int g = 0; g < (identity ? p->groups : 1); ++g) {
+    for (int w = 0; w < p->nwin; ++w) {
+      const int k0 = win_k[w], k1 = win_k[w + 1];
+      const int p0 = k0 < static_cast<int>(nc) ? pk[k0] : t.n_partials;
+      const int p1 = k1 < static_cast<int>(nc) ? pk[k1] : t.n_partials;
+      const size_t start = words.size();
+      words.resize(start + win_header_words(dirs), 0u);
+      words[start] = static_cast<unsigned>(p0);
+      words[start + 1] = static_cast<unsigned>(p1 - p0);
+      unsigned off = 0;
+      for (int j = 0; j < dirs; ++j) {
+        words[start + 2 + j] = off;
+        const int d = identity ? g * dirs + j : 0;
+        if ((identity || j == 0) && d < nstreams) {
+          size_t& q = pos[d];
+          while (q < at[d].size() && at[d][q] < k1) {
+            const uint4 e = ents[d][q++];
+            words.insert(words.end(), {e.x, e.y, e.z, e.w});
+            ++off;
+          }
+        }
+      }
+      words[start + 2 + dirs] = off;
+      meta[static_cast<size_t>(g) * p->nwin + w] =
+          make_int4(p0, p1 - p0, static_cast<int>(start / 4),
+                    static_cast<int>((words.size() - start) / 4));
+    }
+  }
+  if (!identity)  // general seeds: every group walks the same blocks
+    for (int g = 1; g < p->groups; ++g)
+      for (int w = 0; w < p->nwin; ++w)
+        meta[static_cast<size_t>(g) * p->nwin + w] = meta[w];
+  std::vector<uint4> blocks(words.size() / 4);
+  std::memcpy(blocks.data(), words.data(), blocks.size() * sizeof(uint4));
+  cudaError_t e;
+  if ((e = upload(&p->d_blocks, blocks)) != cudaSuccess ||
+      (e = upload(&p->d_meta, meta)) != cudaSuccess) {
+    *err = cuda_fail(e, "upload window plan");
+    return nullptr;
+  }
+  p->usable = true;
+  t.win_plans.push_back(std::move(p));
+  return t.win_plans.back().get();
 }
 
 // Structural activity of the adjoint sweep (direction-independent), last instruction first.
@@ -1086,11 +1261,39 @@ int run_deriv(Tape& t, SweepArgs a, long long m, const DerivReq& rq, cudaStream_
     if (e != cudaSuccess) return cuda_fail(e, "derivative sweep launch");
     return gw_done(t, s);
   }
+  // the windowed tangent sweep (directions of a tile co-scheduled on one SM, partials and
+  // entries staged window by window): a candidate for tangent sweeps with enough directions
+  const int kWin = TV_COUNT + 1;
+  const WinPlan* wp = nullptr;
+  auto win = [&]() -> const WinPlan* {
+    static const std::vector<int> kNoMap;
+    if (!wp && !plan_err)
+      wp = win_plan(t, ndir, identity, seeded_in, rq.dirmap ? *rq.dirmap : kNoMap, &plan_err);
+    return wp;
+  };
+  auto launch_win = [&]() -> cudaError_t {
+    const WinPlan* p = win();
+    if (!p || !p->usable) return cudaErrorInvalidValue;
+    SweepArgs c = a;
+    c.win_blocks = p->d_blocks;
+    c.win_meta = p->d_meta;
+    c.win_n = p->nwin;
+    c.win_dirs = p->dirs;
+    c.win_stages = p->stages;
+    c.win_rows = p->rows;
+    c.win_ents = p->ents;
+    c.block = (p->dirs + 1) * 32;
+    const long long items = tiles * p->groups;
+    const int grid = static_cast<int>(std::max<long long>(1, std::min<long long>(items, sms)));
+    return launch_tangent_win(c, grid, s);
+  };
   const int n_variants = adjoint ? AV_COUNT : TV_COUNT;
   auto usable = [&](int v) {
+    if (v == kWin) return !adjoint && win() && win()->usable;
     return v == kCoop ? coop_ok : (v >= 0 && v < n_variants && fits(v));
   };
   auto run_v = [&](int v) {
+    if (v == kWin) return launch_win();
     return v == kCoop ? (adjoint ? launch_coop_adj() : launch_coop_tan()) : launch(v);
   };
   std::atomic<int>& kept = t.tuned[kind][cls];
@@ -1103,9 +1306,9 @@ int run_deriv(Tape& t, SweepArgs a, long long m, const DerivReq& rq, cudaStream_
     if (g_autotune && !capturing(s) && (work >= 2ll * sms * 8 || cls == 0) &&
         tune_lock.try_lock()) {
       float best = 0;
-      for (int c = 0; c <= n_variants; ++c) {
-        // the variants of the kind, then (tangents) the cooperative sweep
-        const int v = c < n_variants ? c : kCoop;
+      for (int c = 0; c <= n_variants + (adjoint ? 0 : 1); ++c) {
+        // the variants of the kind, then the cooperative sweep, then (tangents) the windowed
+        const int v = c < n_variants ? c : (c == n_variants ? kCoop : kWin);
         if (!usable(v)) continue;
         float ms = 0;
         if (int rc = time_once(s, [&] { return run_v(v); }, &ms)) return plan_err ? plan_err : rc;
@@ -2008,7 +2211,7 @@ int casadi_gb300_set_residence(int id, int mode) {
 int casadi_gb300_set_variant(int id, int kind, int variant) {
   Tape* t = get_tape(id);
   if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
-  if (kind < 0 || kind > 2 || variant < -1 || variant > (kind == 2 ? AV_COUNT : TV_COUNT))
+  if (kind < 0 || kind > 2 || variant < -1 || variant > (kind == 2 ? AV_COUNT : TV_COUNT + 1))
     return fail(CASADI_GB300_ERR_ARG, "bad arguments");
   t->tuned[kind][0] = t->tuned[kind][1] = variant;
   return 0;

@@ -689,6 +689,8 @@ __global__ void __launch_bounds__(32, MB) k_tangent(const __grid_constant__ Swee
   }
 }
 
+#include "sweeps_win.cuh"
+
 #define CGB_J _Pragma("unroll") for (int j = 0; j < IPT; ++j)
 
 // One adjoint sweep of IPT 32-instance tiles by one warp: entry stream st (ngr groups),
@@ -1173,6 +1175,21 @@ cudaError_t launch_tangent(const SweepArgs& a, int grid, int variant, cudaStream
 #undef CGB_LAUNCH
     default: return cudaErrorInvalidValue;
   }
+}
+
+size_t smem_tangent_win(int sz_w, int dirs, int stages, int rows, int ents) {
+  return kWinBarBytes + static_cast<size_t>(stages) * (static_cast<size_t>(rows) * 256 +
+                                                       static_cast<size_t>(ents) * 16) +
+         static_cast<size_t>(dirs) * (sz_w > 0 ? sz_w : 1) * 256;
+}
+
+cudaError_t launch_tangent_win(const SweepArgs& a, int grid, cudaStream_t s) {
+  if (a.win_dirs < 1 || a.win_dirs > kWinMaxDirs || a.win_stages < 2 ||
+      a.win_stages > kWinBarBytes / 16 || a.win_n < 1)
+    return cudaErrorInvalidValue;
+  const size_t smem =
+      smem_tangent_win(a.t.sz_w, a.win_dirs, a.win_stages, a.win_rows, a.win_ents);
+  return launch_k(k_tangent_win, dim3(grid), (a.win_dirs + 1) * 32, smem, a, s);
 }
 
 cudaError_t launch_adjoint(const SweepArgs& a, int grid, int variant, cudaStream_t s) {

@@ -87,6 +87,17 @@ struct SweepArgs {
   // (longest entry stream first; null: natural order)
   unsigned long long* queue;
   const int* gorder;
+  // windowed tangent sweep (launch_tangent_win): per (direction group, window) the window's
+  // first partial row, partial rows, entry block start and length (uint4 units) in win_blocks;
+  // win_dirs directions per CTA (one consumer warp each), win_stages ring stages of win_rows
+  // partial rows + win_ents block uint4s each
+  const uint4* win_blocks;
+  const int4* win_meta;
+  int win_n;
+  int win_dirs;
+  int win_stages;
+  int win_rows;
+  int win_ents;
 };
 
 // One item of a persistent batch: a tape over its own instance range.
@@ -162,6 +173,16 @@ enum AdjVariant : int {
 void tan_variant_shape(int variant, int* ipt, int* k);
 int adj_variant_ipt(int variant);
 cudaError_t launch_tangent(const SweepArgs& a, int grid, int variant, cudaStream_t s);
+// Windowed tangent sweep: one CTA per SM of a warp that stages, window by window, a tile's
+// recorded partials and the window's entry block into a shared-memory ring with bulk copies,
+// and win_dirs warps that each walk one direction's entries of the window from shared memory
+// (the same arithmetic as k_tangent, so the same bits). Work items (tile, direction group)
+// in a static stride over a persistent grid.
+constexpr int kWinMaxDirs = 31;
+constexpr int kWinBarBytes = 128;  // full/empty mbarriers of up to 8 stages
+__host__ __device__ inline int win_header_words(int dirs) { return (dirs + 3 + 3) & ~3; }
+size_t smem_tangent_win(int sz_w, int dirs, int stages, int rows, int ents);
+cudaError_t launch_tangent_win(const SweepArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_adjoint(const SweepArgs& a, int grid, int variant, cudaStream_t s);
 // The adjoint sweep without an activity plan (see k_adjoint<DW, true>).
 cudaError_t launch_adjoint_dense(const SweepArgs& a, int grid, cudaStream_t s);

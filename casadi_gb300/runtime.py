@@ -874,6 +874,8 @@ N_TAN_VARIANTS = 8  # tangent-sweep kernel variants (forward, Jacobian); the las
 #                     cooperative level sweep, used only by launches of few tiles
 N_ADJ_VARIANTS = 7  # adjoint-sweep kernel variants; the last one is the cooperative level
 #                     sweep, used only by launches of few tiles
+TAN_WINDOWED = 8    # the windowed tangent sweep (a tile's directions on one SM, partials and
+#                     entries staged in shared memory window by window; >= 4 directions)
 
 FAMILIES = ("eval", "record", "tangent", "adjoint", "sp_forward", "sp_reverse", "batch",
             "activity")

@@ -394,9 +394,11 @@ CASADI_GB300_API int casadi_gb300_tuned_variant(int id, int kind, int* variant);
  * first used inside a CUDA graph capture. No counterpart in the reference, whose work vector
  * is the caller's w array (casadi/core/function_internal.hpp:414). */
 CASADI_GB300_API int casadi_gb300_set_residence(int id, int mode);
-/* Fixes the variant of one kind on a tape (kinds 0 and 1: 0..7; kind 2: 0..6; the last one
- * of each kind is the cooperative level sweep, which only launches of at most 16 tiles per SM
- * use), or clears it for retuning (-1). */
+/* Fixes the variant of one kind on a tape (kinds 0 and 1: 0..8; kind 2: 0..6), or clears it
+ * for retuning (-1). Tangent variant 7 and adjoint variant 6 are the cooperative level sweeps,
+ * which only launches of at most 16 tiles per SM use; tangent variant 8 is the windowed sweep
+ * (the directions of a tile on one SM, recorded partials and entries staged into shared memory
+ * window by window), used when at least 4 directions are swept and their work vectors fit. */
 CASADI_GB300_API int casadi_gb300_set_variant(int id, int kind, int variant);
 
 /* Colour-compressed Jacobian: n_colors forward directions, direction d seeded with 1 on

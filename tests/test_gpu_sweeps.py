@@ -484,3 +484,38 @@ def test_sweeps_replay_from_a_cuda_graph(gpu_lib):
                         host(want_r) + host(want_j) + host(want_a)):
             assert_bitexact(x, y, "graph replay")
     ct.sync()
+
+
+@pytest.mark.parametrize("case", ["rollout_general", "rollout_jacobian", "dag_jacobian"])
+def test_windowed_tangent_gives_the_warp_sweep_bits(gpu_lib, case):
+    """The windowed tangent sweep (a tile's directions co-scheduled on one SM, partials and
+    entries staged into shared memory) does k_tangent's arithmetic entry for entry: forward
+    sensitivities and Jacobians are identical bit for bit, with ragged instance counts,
+    general seeds, and more directions than one CTA holds (several direction groups)."""
+    from casadi_gb300 import runtime as R
+    if case == "dag_jacobian":
+        F = W.random_dag(n_in=40, n_nodes=1500, n_out=6, seed=8, bounded=True)
+        n = 1000
+        args = dev(W.dag_inputs(n, n_in=40, seed=8))
+    else:
+        F = W.cartpole_rollout(8)
+        n = 2003
+        args = dev(W.cartpole_inputs(n, steps=8, seed=23))
+    ct = CudaTape(F)
+    kind = 0 if case == "rollout_general" else 1
+
+    def run():
+        if kind == 0:
+            rng = np.random.default_rng(23)
+            fseeds = dev([rng.standard_normal((6, k, n)) for k in F.tape.nnz_in])
+            return host(ct.forward(args, fseeds)[1])
+        return host(ct.jacobian(args)[1])
+
+    ct.set_variant(kind, 0)
+    want = run()
+    ct.set_variant(kind, R.TAN_WINDOWED)
+    got = run()
+    assert ct.tuned_variant(kind) == R.TAN_WINDOWED
+    for x, y in zip(got, want):
+        assert_bitexact(x, y, "windowed tangent, " + case)
+    ct.sync()
