@@ -827,6 +827,8 @@ def run_native(a):
     if a.workload == "rollout20":
         comps["jacobian24_evals_per_s"] = rate(
             lambda: ct.jacobian(dargs, res=res, jac=jac, stream=stream))
+    # derivative-sweep variants the autotuner kept (tangent 8: the windowed sweep)
+    comps["tuned_variants"] = {"jacobian": ct.tuned_variant(1), "adjoint": ct.tuned_variant(2)}
     ct.sync()
 
     weights = load_weights()
