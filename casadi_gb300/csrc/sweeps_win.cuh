@@ -58,33 +58,63 @@ __device__ __forceinline__ bool mbar_wait(u64* bar, unsigned parity, volatile in
   }
 }
 
-// One direction's entries of one window (k_tangent's K = 1 cases). pw: the window's partial
-// rows in shared memory, lane-offset (row r at pw + r*32), p0 the window's first partial row;
-// wb the warp's work vector w[slot][lane], lane-offset; last the value the previous entry of
-// the direction wrote (operand forwarding carries across windows).
+// Everything an entry reads besides the value the previous entry wrote: its partials (1.0 /
+// 0.0 where none is recorded, as k_tangent) and both operand slots. The operand loads are
+// issued one entry ahead, before the current entry stores its result: an operand that is the
+// previous entry's result is marked for forwarding (bit 31) and taken from `last` instead, so
+// a value loaded early is never one the current entry is about to write. Fields that hold I/O
+// indices rather than slots (an INPUT's y and z, an OUTPUT's z) are not loaded.
+struct WinOps {
+  double p0, p1, y, z;
+};
+
+__device__ __forceinline__ WinOps win_ops(const uint4& c, const double* pw, unsigned p0,
+                                          unsigned char* wb) {
+  const unsigned m = ent_pmask(c.w);
+  const unsigned r0 = ent_pk(c.w) - p0;
+  WinOps o;
+  o.p0 = (m & 1u) ? pw[r0 * 32] : 1.0;
+  o.p1 = (m & 2u) ? pw[(r0 + (m & 1u)) * 32] : 0.0;
+  const unsigned kind = ent_kind(c.w);
+  o.y = kind == LK_INPUT ? 0.0 : wreg(wb, c.y & 0x7fffffffu);
+  o.z = (kind == LK_INPUT || kind == LK_OUTPUT) ? 0.0 : wreg(wb, c.z & 0x7fffffffu);
+  return o;
+}
+
+// One direction's entries of one window (k_tangent's K = 1 cases), software-pipelined by one
+// entry. pw: the window's partial rows in shared memory, lane-offset (row r at pw + r*32), p0
+// the window's first partial row; wb the warp's work vector w[slot][lane], lane-offset; last
+// the value the previous entry of the direction wrote (operand forwarding carries across
+// windows).
 __device__ __forceinline__ void win_walk(const uint4* ents, int cnt, const double* pw,
                                          unsigned p0, unsigned char* wb, double& last,
                                          const SweepArgs& a, int dir, bool active,
                                          long long ig) {
-#define CGB_WOP(off) (((off) & 0x80000000u) ? last : wreg(wb, (off) & 0x7fffffffu))
+  if (cnt <= 0) return;
+  uint4 cur = ents[0];
+  WinOps o = win_ops(cur, pw, p0, wb);
 #pragma unroll 1
   for (int e = 0; e < cnt; ++e) {
-    const uint4 cur = ents[e];
+    uint4 nxt = cur;
+    WinOps no = o;
+    if (e + 1 < cnt) {
+      nxt = ents[e + 1];
+      no = win_ops(nxt, pw, p0, wb);
+    }
     const unsigned meta = cur.w;
     const unsigned key = (ent_kind(meta) << 2) | (ent_flags(meta) & 3u);
-    const unsigned m = ent_pmask(meta);
-    const unsigned r0 = ent_pk(meta) - p0;
-    const unsigned r1 = r0 + (m & 1u);
-    double r;
+    const double oy = (cur.y & 0x80000000u) ? last : o.y;
+    const double oz = (cur.z & 0x80000000u) ? last : o.z;
+    double r = 0.0;
+    bool store = true;
     switch (key) {
       case (LK_OUTPUT << 2) | 0u:
       case (LK_OUTPUT << 2) | 1u: {
         const IoDesc& d = a.sens[cur.x];
         if (active && d.ptr)
-          static_cast<double*>(d.ptr)[io_off(d, dir, cur.z, ig)] =
-              (meta & 1u) ? CGB_WOP(cur.y) : 0.0;
-        continue;
-      }
+          static_cast<double*>(d.ptr)[io_off(d, dir, cur.z, ig)] = (meta & 1u) ? oy : 0.0;
+        store = false;
+      } break;
       case (LK_INPUT << 2) | 1u:
         if (a.identity_seed) {
           r = 1.0;
@@ -94,35 +124,28 @@ __device__ __forceinline__ void win_walk(const uint4* ents, int cnt, const doubl
                      : 0.0;
         }
         break;
-      case (LK_GEN << 2) | 1u:
-        r = __dmul_rn((m & 1u) ? pw[r0 * 32] : 1.0, CGB_WOP(cur.y));
-        break;
-      case (LK_GEN << 2) | 2u:
-        r = __dmul_rn((m & 2u) ? pw[r1 * 32] : 0.0, CGB_WOP(cur.z));
-        break;
-      case (LK_GEN << 2) | 3u:
-        r = __fma_rn((m & 1u) ? pw[r0 * 32] : 1.0, CGB_WOP(cur.y),
-                     __dmul_rn((m & 2u) ? pw[r1 * 32] : 0.0, CGB_WOP(cur.z)));
-        break;
-      case (LK_ADD << 2) | 1u: r = CGB_WOP(cur.y); break;
-      case (LK_ADD << 2) | 2u: r = CGB_WOP(cur.z); break;
-      case (LK_ADD << 2) | 3u: r = __dadd_rn(CGB_WOP(cur.y), CGB_WOP(cur.z)); break;
-      case (LK_SUB << 2) | 1u: r = CGB_WOP(cur.y); break;
-      case (LK_SUB << 2) | 2u: r = d_neg(CGB_WOP(cur.z)); break;
-      case (LK_SUB << 2) | 3u: r = __dsub_rn(CGB_WOP(cur.y), CGB_WOP(cur.z)); break;
-      case (LK_NEG << 2) | 1u: r = d_neg(CGB_WOP(cur.y)); break;
-      case (LK_TWICE << 2) | 1u: r = d_twice(CGB_WOP(cur.y)); break;
-      case (LK_ASSIGN << 2) | 1u: r = CGB_WOP(cur.y); break;
-      case (LK_IFZ << 2) | 2u:
-        r = d_iszero((m & 2u) ? pw[r1 * 32] : 0.0) ? 0.0 : CGB_WOP(cur.z);
-        break;
-      default:
-        continue;  // NOP padding
+      case (LK_GEN << 2) | 1u: r = __dmul_rn(o.p0, oy); break;
+      case (LK_GEN << 2) | 2u: r = __dmul_rn(o.p1, oz); break;
+      case (LK_GEN << 2) | 3u: r = __fma_rn(o.p0, oy, __dmul_rn(o.p1, oz)); break;
+      case (LK_ADD << 2) | 1u: r = oy; break;
+      case (LK_ADD << 2) | 2u: r = oz; break;
+      case (LK_ADD << 2) | 3u: r = __dadd_rn(oy, oz); break;
+      case (LK_SUB << 2) | 1u: r = oy; break;
+      case (LK_SUB << 2) | 2u: r = d_neg(oz); break;
+      case (LK_SUB << 2) | 3u: r = __dsub_rn(oy, oz); break;
+      case (LK_NEG << 2) | 1u: r = d_neg(oy); break;
+      case (LK_TWICE << 2) | 1u: r = d_twice(oy); break;
+      case (LK_ASSIGN << 2) | 1u: r = oy; break;
+      case (LK_IFZ << 2) | 2u: r = d_iszero(o.p1) ? 0.0 : oz; break;
+      default: store = false; break;  // NOP padding
     }
-    wreg(wb, cur.x) = r;
-    last = r;
+    if (store) {
+      wreg(wb, cur.x) = r;
+      last = r;
+    }
+    cur = nxt;
+    o = no;
   }
-#undef CGB_WOP
 }
 
 __global__ void __launch_bounds__(kWinMaxThreads, 1)
