@@ -15,7 +15,11 @@
 // partial row and per-direction entry offsets, then every direction's entries). Warps 1..D each
 // walk one direction's entries of the window with partials and entries read from shared
 // memory, then release the stage. The arithmetic of every entry is k_tangent's, so results are
-// the same bits. Waits are bounded (~1 s): a wait that runs out sets kErrWaitTimeout, the other
+// the same bits. Measured on the 20-step rollout (262144 instances, 24 directions): 29.9 ms
+// against 24.1 ms for k_tangent. With one tile in flight per SM the densest direction's chain
+// of dependent entries (2976 of the tape's 3057 instructions) gates every window of the tile,
+// where k_tangent overlaps such chains of many tiles; the autotuner keeps it for tapes where it
+// wins. Waits are bounded (~1 s): a wait that runs out sets kErrWaitTimeout, the other
 // warps see the abort flag and leave, and warp 0 waits (bounded) for its copies in flight.
 #pragma once
 
@@ -37,7 +41,9 @@ __device__ __forceinline__ void mbar_expect_tx(u64* bar, unsigned bytes) {
 }
 
 // Bounded wait for the completion of the phase of `bar` with the given parity. False when
-// about 1 s passes, or when another warp has set *abort (if given).
+// about 1 s passes, or when another warp has set *abort (if given). A waiting warp backs off
+// with a short sleep between tests, so it leaves the issue slots of its SM sub-partition to
+// the warps that are still walking the window.
 __device__ __forceinline__ bool mbar_wait(u64* bar, unsigned parity, volatile int* abort) {
   const unsigned addr = smem_u32(bar);
   const long long t0 = clock64();
@@ -51,6 +57,7 @@ __device__ __forceinline__ bool mbar_wait(u64* bar, unsigned parity, volatile in
         : "r"(addr), "r"(parity)
         : "memory");
     if (done) return true;
+    __nanosleep(it < 4 ? 32 : 256);
     if ((it & 31u) == 31u) {
       if (abort && *abort) return false;
       if (clock64() - t0 > kWaitCycles) return false;
@@ -58,63 +65,35 @@ __device__ __forceinline__ bool mbar_wait(u64* bar, unsigned parity, volatile in
   }
 }
 
-// Everything an entry reads besides the value the previous entry wrote: its partials (1.0 /
-// 0.0 where none is recorded, as k_tangent) and both operand slots. The operand loads are
-// issued one entry ahead, before the current entry stores its result: an operand that is the
-// previous entry's result is marked for forwarding (bit 31) and taken from `last` instead, so
-// a value loaded early is never one the current entry is about to write. Fields that hold I/O
-// indices rather than slots (an INPUT's y and z, an OUTPUT's z) are not loaded.
-struct WinOps {
-  double p0, p1, y, z;
-};
-
-__device__ __forceinline__ WinOps win_ops(const uint4& c, const double* pw, unsigned p0,
-                                          unsigned char* wb) {
-  const unsigned m = ent_pmask(c.w);
-  const unsigned r0 = ent_pk(c.w) - p0;
-  WinOps o;
-  o.p0 = (m & 1u) ? pw[r0 * 32] : 1.0;
-  o.p1 = (m & 2u) ? pw[(r0 + (m & 1u)) * 32] : 0.0;
-  const unsigned kind = ent_kind(c.w);
-  o.y = kind == LK_INPUT ? 0.0 : wreg(wb, c.y & 0x7fffffffu);
-  o.z = (kind == LK_INPUT || kind == LK_OUTPUT) ? 0.0 : wreg(wb, c.z & 0x7fffffffu);
-  return o;
-}
-
-// One direction's entries of one window (k_tangent's K = 1 cases), software-pipelined by one
-// entry. pw: the window's partial rows in shared memory, lane-offset (row r at pw + r*32), p0
-// the window's first partial row; wb the warp's work vector w[slot][lane], lane-offset; last
-// the value the previous entry of the direction wrote (operand forwarding carries across
-// windows).
+// One direction's entries of one window (k_tangent's K = 1 cases). pw: the window's partial
+// rows in shared memory, lane-offset (row r at pw + r*32), p0 the window's first partial row;
+// wb the warp's work vector w[slot][lane], lane-offset; last the value the previous entry of
+// the direction wrote (operand forwarding carries across windows). Only the partials and
+// operands an entry uses are read. (Loading the next entry's partials and operands before the
+// current one computes made the sweep slower on the rollout, 29.9 -> 41.0 ms.)
 __device__ __forceinline__ void win_walk(const uint4* ents, int cnt, const double* pw,
                                          unsigned p0, unsigned char* wb, double& last,
                                          const SweepArgs& a, int dir, bool active,
                                          long long ig) {
-  if (cnt <= 0) return;
-  uint4 cur = ents[0];
-  WinOps o = win_ops(cur, pw, p0, wb);
+#define CGB_WOP(off) (((off) & 0x80000000u) ? last : wreg(wb, (off) & 0x7fffffffu))
 #pragma unroll 1
   for (int e = 0; e < cnt; ++e) {
-    uint4 nxt = cur;
-    WinOps no = o;
-    if (e + 1 < cnt) {
-      nxt = ents[e + 1];
-      no = win_ops(nxt, pw, p0, wb);
-    }
+    const uint4 cur = ents[e];
     const unsigned meta = cur.w;
     const unsigned key = (ent_kind(meta) << 2) | (ent_flags(meta) & 3u);
-    const double oy = (cur.y & 0x80000000u) ? last : o.y;
-    const double oz = (cur.z & 0x80000000u) ? last : o.z;
-    double r = 0.0;
-    bool store = true;
+    const unsigned m = ent_pmask(meta);
+    const unsigned r0 = ent_pk(meta) - p0;
+    const unsigned r1 = r0 + (m & 1u);
+    double r;
     switch (key) {
       case (LK_OUTPUT << 2) | 0u:
       case (LK_OUTPUT << 2) | 1u: {
         const IoDesc& d = a.sens[cur.x];
         if (active && d.ptr)
-          static_cast<double*>(d.ptr)[io_off(d, dir, cur.z, ig)] = (meta & 1u) ? oy : 0.0;
-        store = false;
-      } break;
+          static_cast<double*>(d.ptr)[io_off(d, dir, cur.z, ig)] =
+              (meta & 1u) ? CGB_WOP(cur.y) : 0.0;
+        continue;
+      }
       case (LK_INPUT << 2) | 1u:
         if (a.identity_seed) {
           r = 1.0;
@@ -124,28 +103,35 @@ __device__ __forceinline__ void win_walk(const uint4* ents, int cnt, const doubl
                      : 0.0;
         }
         break;
-      case (LK_GEN << 2) | 1u: r = __dmul_rn(o.p0, oy); break;
-      case (LK_GEN << 2) | 2u: r = __dmul_rn(o.p1, oz); break;
-      case (LK_GEN << 2) | 3u: r = __fma_rn(o.p0, oy, __dmul_rn(o.p1, oz)); break;
-      case (LK_ADD << 2) | 1u: r = oy; break;
-      case (LK_ADD << 2) | 2u: r = oz; break;
-      case (LK_ADD << 2) | 3u: r = __dadd_rn(oy, oz); break;
-      case (LK_SUB << 2) | 1u: r = oy; break;
-      case (LK_SUB << 2) | 2u: r = d_neg(oz); break;
-      case (LK_SUB << 2) | 3u: r = __dsub_rn(oy, oz); break;
-      case (LK_NEG << 2) | 1u: r = d_neg(oy); break;
-      case (LK_TWICE << 2) | 1u: r = d_twice(oy); break;
-      case (LK_ASSIGN << 2) | 1u: r = oy; break;
-      case (LK_IFZ << 2) | 2u: r = d_iszero(o.p1) ? 0.0 : oz; break;
-      default: store = false; break;  // NOP padding
+      case (LK_GEN << 2) | 1u:
+        r = __dmul_rn((m & 1u) ? pw[r0 * 32] : 1.0, CGB_WOP(cur.y));
+        break;
+      case (LK_GEN << 2) | 2u:
+        r = __dmul_rn((m & 2u) ? pw[r1 * 32] : 0.0, CGB_WOP(cur.z));
+        break;
+      case (LK_GEN << 2) | 3u:
+        r = __fma_rn((m & 1u) ? pw[r0 * 32] : 1.0, CGB_WOP(cur.y),
+                     __dmul_rn((m & 2u) ? pw[r1 * 32] : 0.0, CGB_WOP(cur.z)));
+        break;
+      case (LK_ADD << 2) | 1u: r = CGB_WOP(cur.y); break;
+      case (LK_ADD << 2) | 2u: r = CGB_WOP(cur.z); break;
+      case (LK_ADD << 2) | 3u: r = __dadd_rn(CGB_WOP(cur.y), CGB_WOP(cur.z)); break;
+      case (LK_SUB << 2) | 1u: r = CGB_WOP(cur.y); break;
+      case (LK_SUB << 2) | 2u: r = d_neg(CGB_WOP(cur.z)); break;
+      case (LK_SUB << 2) | 3u: r = __dsub_rn(CGB_WOP(cur.y), CGB_WOP(cur.z)); break;
+      case (LK_NEG << 2) | 1u: r = d_neg(CGB_WOP(cur.y)); break;
+      case (LK_TWICE << 2) | 1u: r = d_twice(CGB_WOP(cur.y)); break;
+      case (LK_ASSIGN << 2) | 1u: r = CGB_WOP(cur.y); break;
+      case (LK_IFZ << 2) | 2u:
+        r = d_iszero((m & 2u) ? pw[r1 * 32] : 0.0) ? 0.0 : CGB_WOP(cur.z);
+        break;
+      default:
+        continue;  // NOP padding
     }
-    if (store) {
-      wreg(wb, cur.x) = r;
-      last = r;
-    }
-    cur = nxt;
-    o = no;
+    wreg(wb, cur.x) = r;
+    last = r;
   }
+#undef CGB_WOP
 }
 
 __global__ void __launch_bounds__(kWinMaxThreads, 1)
