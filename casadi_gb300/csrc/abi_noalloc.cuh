@@ -8,9 +8,8 @@
 // Allocation-free adjoint sweep.
 //
 // Some callers cannot allocate device memory at the point where they need derivatives: a
-// solver running inside a CUDA graph capture, a real-time control loop that forbids
-// allocation after start-up, or a plugin hosted by a framework that owns the device
-// allocator. casadi_gb300_reverse_noalloc serves them: its partials scratch is the file-scope
+// real-time control loop that forbids allocation after start-up, or a plugin hosted by a
+// framework that owns the device allocator. casadi_gb300_reverse_noalloc serves them: its partials scratch is the file-scope
 // device array below, a fixed 64 MiB that every GPU which loads this library holds until the
 // process exits. It runs the record sweep and the plan-free adjoint variant, so it makes no
 // device allocation of any kind, and it needs no host allocation either.
@@ -46,10 +45,12 @@ int noalloc_scratch(void** ptr) {
 }
 
 // Launch shape of the plan-free adjoint: the most resident warps that fit, as dir_shape
-// chooses, computed without touching the tape's shape cache.
+// chooses, computed without touching the tape's shape cache. dw = 0: no shape fits (the
+// work vector is too long for shared memory).
 DirShape noalloc_shape(const Tape& t, int ndir) {
   const int max_smem = max_smem_optin();
   DirShape best;
+  best.dw = 0;
   double best_score = -1;
   for (int ch : {64, 32, 16}) {
     for (int dw : {8, 6, 4, 2, 1}) {
@@ -85,6 +86,21 @@ int casadi_gb300_reverse_noalloc(int id, int64_t n, int64_t ld, int nadj,
   if (int rc = check_n(n, ld)) return rc;
   if (nadj < 0 || nadj > 65535) return fail(CASADI_GB300_ERR_ARG, "bad direction count %d", nadj);
   if (n == 0) return 0;
+  // both sweeps keep the work vector in shared memory (the global-memory form would need
+  // device buffers of its own): find the record sweep's block size and the adjoint's shape
+  int block = 0;
+  for (int bs : {t->primal_block, 128, 64, 32})
+    if (bs >= 32 && smem_primal(t->sz_w, bs) <= static_cast<size_t>(max_smem_optin())) {
+      block = bs;
+      break;
+    }
+  const DirShape ds = noalloc_shape(*t, std::max(nadj, 1));
+  if (block == 0 || (nadj > 0 && ds.dw == 0))
+    return fail(CASADI_GB300_ERR_UNSUPPORTED,
+                "allocation-free adjoint: the tape's work vector (%d slots, %zu bytes per "
+                "32-instance tile) does not fit in shared memory, where this entry point keeps "
+                "it; use casadi_gb300_reverse",
+                t->sz_w, static_cast<size_t>(t->sz_w) * 256);
   const unsigned long long need =
       8ull * 32ull * static_cast<unsigned long long>(t->n_partials) *
       static_cast<unsigned long long>((n + 31) / 32);
@@ -103,20 +119,23 @@ int casadi_gb300_reverse_noalloc(int id, int64_t n, int64_t ld, int nadj,
   a.ndir = nadj;
   fill_io(a.in, t->n_in, vptrs(arg), t->nnz_in, ld, false);
   fill_io(a.out, t->n_out, vptrs(res), t->nnz_out, ld, false);
-  a.block = t->primal_block;
-  cudaError_t e = launch_record(a, grid_for((n + a.block - 1) / a.block, t->primal_grid_cap), s);
+  a.block = block;
+  const int rgrid = grid_for((n + a.block - 1) / a.block,
+                             sm_count() * std::max(1, occupancy_primal(
+                                                          block, smem_primal(t->sz_w, block))));
+  cudaError_t e = timed(F_RECORD, s, [&] { return launch_record(a, rgrid, s); });
   if (e != cudaSuccess) return cuda_fail(e, "record sweep launch");
   if (nadj == 0) return 0;
   fill_io(a.seed, t->n_out, vptrs(aseed), t->nnz_out, ld, true);
   fill_io(a.sens, t->n_in, vptrs(asens), t->nnz_in, ld, true);
-  const DirShape ds = noalloc_shape(*t, nadj);
   const int groups = (nadj + ds.dw - 1) / ds.dw;
   a.block = 32 * ds.dw;
   a.chunk = ds.ch;
   const long long tiles = (n + 31) / 32;
   const long long per_group = std::max<long long>(
       1, std::min<long long>(tiles, static_cast<long long>(sm_count()) * ds.blocks_per_sm / groups));
-  e = launch_adjoint_dense(a, static_cast<int>(per_group * groups), s);
+  e = timed(F_ADJOINT, s,
+            [&] { return launch_adjoint_dense(a, static_cast<int>(per_group * groups), s); });
   if (e != cudaSuccess) return cuda_fail(e, "adjoint launch");
   return 0;
 }

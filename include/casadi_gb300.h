@@ -471,9 +471,9 @@ CASADI_GB300_API int casadi_gb300_batch_run(int batch, void* scratch, size_t scr
 
 /* Allocation-free adjoint sweep: the same values and adjoint sensitivities as
  * casadi_gb300_reverse (arguments and layouts alike, no scratch argument), for callers that
- * cannot allocate device memory when they need derivatives -- solvers inside a CUDA graph
- * capture, real-time loops that forbid allocation after start-up, plugins whose host
- * framework owns the allocator. It has no counterpart in the reference.
+ * cannot allocate device memory when they need derivatives -- real-time loops that forbid
+ * allocation after start-up, plugins whose host framework owns the device allocator. It has
+ * no counterpart in the reference.
  * Scratch is a fixed 64 MiB file-scope device array that each GPU loading the library holds
  * until exit; a call needing more (8 bytes x recorded partials x instances rounded up to 32)
  * is rejected with CASADI_GB300_ERR_SCRATCH. The first call on a device looks up the array's
@@ -481,7 +481,11 @@ CASADI_GB300_API int casadi_gb300_batch_run(int batch, void* scratch, size_t scr
  * All calls share the array and it keeps the last call's contents (nothing in it needs to
  * start at zero): calls that overlap on the GPU race, so serialize them, e.g. on one stream.
  * It uses no activity plan: contributions are always added to a zeroed adjoint, which can
- * differ from casadi_gb300_reverse only in the sign of zero results and in inf/NaN cases. */
+ * differ from casadi_gb300_reverse only in the sign of zero results and in inf/NaN cases.
+ * Both of its sweeps keep the work vector in shared memory: a tape whose work vector does not
+ * fit there (sz_w x 256 bytes per 32-instance tile beyond the device's per-CTA limit, about
+ * 880 slots on GB300) is refused with CASADI_GB300_ERR_UNSUPPORTED; casadi_gb300_reverse
+ * handles it with global-memory work vectors. */
 CASADI_GB300_API int casadi_gb300_reverse_noalloc(int id, int64_t n, int64_t ld, int nadj,
                                  const double* const* arg, double* const* res,
                                  const double* const* aseed, double* const* asens, void* stream);
