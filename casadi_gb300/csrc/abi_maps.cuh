@@ -4,6 +4,10 @@
 // registry, plans and launch helpers and is not compiled on its own.
 #pragma once
 
+// A MapSum call sums at most two row groups per output (values and their directions) in
+// forward mode and one per output and per shared input in reverse mode, all in one launch.
+static_assert(kMaxSumGroups >= 2 * kMaxIo, "MapSum row groups of one call must fit a launch");
+
 // ---- MapSum: shared inputs and instance-summed outputs (casadi/core/mapsum.cpp) -------------
 namespace {
 
