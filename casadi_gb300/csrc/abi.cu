@@ -2327,9 +2327,13 @@ static Mem* get_mem(int mem) {
 
 // Instance-major device blocks for the host-buffer Map path: block j holds
 // n * per_inst[j] doubles; descriptor strides address (dir, nz, inst).
+// dir_major: the host blocks hold direction d of instance i at (d*n + i)*nnz (the order of
+// CasADi's Map::get_forward/get_reverse seeds and sensitivities, casadi/core/map.cpp:233-264);
+// otherwise at (i*ndir + d)*nnz (the inner f.forward(ndir).map(n) order). The staging buffer
+// takes the host block's order, so copies stay contiguous.
 static int stage_blocks(Mem& m, size_t first_buf, int count, const std::vector<int>& nnz,
                         int ndir, long long n, const double* const* host, bool upload,
-                        IoDesc* desc, cudaStream_t s) {
+                        IoDesc* desc, cudaStream_t s, bool dir_major = false) {
   for (int j = 0; j < count; ++j) {
     desc[j].ptr = nullptr;
     if (!host || !host[j] || nnz[j] == 0) continue;
@@ -2341,27 +2345,35 @@ static int stage_blocks(Mem& m, size_t first_buf, int count, const std::vector<i
       return cuda_fail(e, "cudaMemcpyAsync(H2D)");
     desc[j].ptr = d;
     desc[j].nz_stride = 1;
-    desc[j].dir_stride = nnz[j];
-    desc[j].inst_stride = static_cast<long long>(nnz[j]) * std::max(1, ndir);
+    if (dir_major) {
+      desc[j].dir_stride = static_cast<long long>(nnz[j]) * n;
+      desc[j].inst_stride = nnz[j];
+    } else {
+      desc[j].dir_stride = nnz[j];
+      desc[j].inst_stride = static_cast<long long>(nnz[j]) * std::max(1, ndir);
+    }
   }
   return 0;
 }
 
 extern "C++" {
 namespace {
-// Host blocks of a host-buffer call: each device descriptor (instance-major staging buffer,
-// desc->inst_stride doubles per instance) with the host array it is uploaded from or
-// downloaded to.
+// Host blocks of a host-buffer call: each device descriptor (staging buffer in the host
+// block's order, desc->inst_stride doubles per instance and direction block) with the host
+// array it is uploaded from or downloaded to. dir_blocks > 1: direction-major blocks, one
+// contiguous piece of an instance range per direction (desc->dir_stride apart).
 struct HostBlock {
   const IoDesc* desc;
   const double* up;  // upload source (inputs, seeds) or null
   double* down;      // download target (outputs, sensitivities) or null
+  int dir_blocks;
 };
 
 void collect_blocks(std::vector<HostBlock>& v, const IoDesc* desc, int count, const double* const* up,
-                double* const* down) {
+                double* const* down, int dir_blocks = 1) {
   for (int j = 0; j < count; ++j)
-    if (desc[j].ptr) v.push_back({&desc[j], up ? up[j] : nullptr, down ? down[j] : nullptr});
+    if (desc[j].ptr)
+      v.push_back({&desc[j], up ? up[j] : nullptr, down ? down[j] : nullptr, dir_blocks});
 }
 
 // Descriptors of instances [i0, ...) of instance-major staging descriptors.
@@ -2390,10 +2402,13 @@ int run_pipelined(Mem& m, long long n, const std::vector<HostBlock>& blocks, F c
     for (const auto& b : blocks) {
       if (!b.up) continue;
       const size_t bytes = sizeof(double) * static_cast<size_t>(b.desc->inst_stride);
-      if ((e = cudaMemcpyAsync(static_cast<double*>(b.desc->ptr) + i0 * b.desc->inst_stride,
-                               b.up + i0 * b.desc->inst_stride, bytes * cnt,
-                               cudaMemcpyHostToDevice, m.s_in)) != cudaSuccess)
-        return cuda_fail(e, "cudaMemcpyAsync(H2D)");
+      for (int d = 0; d < b.dir_blocks; ++d) {
+        const long long off = d * (b.dir_blocks > 1 ? b.desc->dir_stride : 0) +
+                              i0 * b.desc->inst_stride;
+        if ((e = cudaMemcpyAsync(static_cast<double*>(b.desc->ptr) + off, b.up + off,
+                                 bytes * cnt, cudaMemcpyHostToDevice, m.s_in)) != cudaSuccess)
+          return cuda_fail(e, "cudaMemcpyAsync(H2D)");
+      }
     }
     if ((e = cudaEventRecord(m.ev_in[c], m.s_in)) != cudaSuccess ||
         (e = cudaStreamWaitEvent(m.stream, m.ev_in[c], 0)) != cudaSuccess)
@@ -2405,10 +2420,13 @@ int run_pipelined(Mem& m, long long n, const std::vector<HostBlock>& blocks, F c
     for (const auto& b : blocks) {
       if (!b.down) continue;
       const size_t bytes = sizeof(double) * static_cast<size_t>(b.desc->inst_stride);
-      if ((e = cudaMemcpyAsync(b.down + i0 * b.desc->inst_stride,
-                               static_cast<double*>(b.desc->ptr) + i0 * b.desc->inst_stride,
-                               bytes * cnt, cudaMemcpyDeviceToHost, m.s_out)) != cudaSuccess)
-        return cuda_fail(e, "cudaMemcpyAsync(D2H)");
+      for (int d = 0; d < b.dir_blocks; ++d) {
+        const long long off = d * (b.dir_blocks > 1 ? b.desc->dir_stride : 0) +
+                              i0 * b.desc->inst_stride;
+        if ((e = cudaMemcpyAsync(b.down + off, static_cast<double*>(b.desc->ptr) + off,
+                                 bytes * cnt, cudaMemcpyDeviceToHost, m.s_out)) != cudaSuccess)
+          return cuda_fail(e, "cudaMemcpyAsync(D2H)");
+      }
     }
   }
   if ((e = cudaEventRecord(m.ev_out, m.s_out)) != cudaSuccess ||
@@ -2503,9 +2521,9 @@ int casadi_gb300_map_jacobian(int id, int mem, int64_t n, const double* const* a
   return casadi_gb300_sync(id, s);
 }
 
-int casadi_gb300_map_forward(int id, int mem, int64_t n, int nfwd, const double* const* arg,
-                             double* const* res, const double* const* fseed,
-                             double* const* fsens) {
+static int map_forward_impl(int id, int mem, int64_t n, int nfwd, const double* const* arg,
+                            double* const* res, const double* const* fseed,
+                            double* const* fsens, bool outer) {
   Tape* t = get_tape(id);
   if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
   Mem* m = get_mem(mem);
@@ -2519,19 +2537,21 @@ int casadi_gb300_map_forward(int id, int mem, int64_t n, int nfwd, const double*
   if (int rc = stage_blocks(*m, kMaxIo, t->n_out, t->nnz_out, 1, n,
                             reinterpret_cast<const double* const*>(res), false, out, s))
     return rc;
-  if (int rc = stage_blocks(*m, 2 * kMaxIo, t->n_in, t->nnz_in, nfwd, n, fseed, false, seed, s))
+  if (int rc = stage_blocks(*m, 2 * kMaxIo, t->n_in, t->nnz_in, nfwd, n, fseed, false, seed, s,
+                            outer))
     return rc;
   if (int rc = stage_blocks(*m, 3 * kMaxIo, t->n_out, t->nnz_out, nfwd, n,
-                            reinterpret_cast<const double* const*>(fsens), false, sens, s))
+                            reinterpret_cast<const double* const*>(fsens), false, sens, s,
+                            outer))
     return rc;
   void* scratch = nullptr;
   size_t bytes = 0;
   if (int rc = map_scratch(*t, *m, n, &scratch, &bytes)) return rc;
   std::vector<HostBlock> blocks;
   collect_blocks(blocks, in, t->n_in, arg, nullptr);
-  collect_blocks(blocks, seed, t->n_in, fseed, nullptr);
+  collect_blocks(blocks, seed, t->n_in, fseed, nullptr, outer ? nfwd : 1);
   collect_blocks(blocks, out, t->n_out, nullptr, res);
-  collect_blocks(blocks, sens, t->n_out, nullptr, fsens);
+  collect_blocks(blocks, sens, t->n_out, nullptr, fsens, outer ? nfwd : 1);
   if (int rc = run_pipelined(*m, n, blocks, [&](long long i0, long long cnt) {
         IoDesc in_c[kMaxIo], out_c[kMaxIo], seed_c[kMaxIo], sens_c[kMaxIo];
         shift_io(in, t->n_in, i0, in_c);
@@ -2545,9 +2565,9 @@ int casadi_gb300_map_forward(int id, int mem, int64_t n, int nfwd, const double*
   return casadi_gb300_sync(id, s);
 }
 
-int casadi_gb300_map_reverse(int id, int mem, int64_t n, int nadj, const double* const* arg,
-                             double* const* res, const double* const* aseed,
-                             double* const* asens) {
+static int map_reverse_impl(int id, int mem, int64_t n, int nadj, const double* const* arg,
+                            double* const* res, const double* const* aseed,
+                            double* const* asens, bool outer) {
   Tape* t = get_tape(id);
   if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
   Mem* m = get_mem(mem);
@@ -2561,19 +2581,21 @@ int casadi_gb300_map_reverse(int id, int mem, int64_t n, int nadj, const double*
   if (int rc = stage_blocks(*m, kMaxIo, t->n_out, t->nnz_out, 1, n,
                             reinterpret_cast<const double* const*>(res), false, out, s))
     return rc;
-  if (int rc = stage_blocks(*m, 2 * kMaxIo, t->n_out, t->nnz_out, nadj, n, aseed, false, seed, s))
+  if (int rc = stage_blocks(*m, 2 * kMaxIo, t->n_out, t->nnz_out, nadj, n, aseed, false, seed, s,
+                            outer))
     return rc;
   if (int rc = stage_blocks(*m, 3 * kMaxIo, t->n_in, t->nnz_in, nadj, n,
-                            reinterpret_cast<const double* const*>(asens), false, sens, s))
+                            reinterpret_cast<const double* const*>(asens), false, sens, s,
+                            outer))
     return rc;
   void* scratch = nullptr;
   size_t bytes = 0;
   if (int rc = map_scratch(*t, *m, n, &scratch, &bytes)) return rc;
   std::vector<HostBlock> blocks;
   collect_blocks(blocks, in, t->n_in, arg, nullptr);
-  collect_blocks(blocks, seed, t->n_out, aseed, nullptr);
+  collect_blocks(blocks, seed, t->n_out, aseed, nullptr, outer ? nadj : 1);
   collect_blocks(blocks, out, t->n_out, nullptr, res);
-  collect_blocks(blocks, sens, t->n_in, nullptr, asens);
+  collect_blocks(blocks, sens, t->n_in, nullptr, asens, outer ? nadj : 1);
   if (int rc = run_pipelined(*m, n, blocks, [&](long long i0, long long cnt) {
         IoDesc in_c[kMaxIo], out_c[kMaxIo], seed_c[kMaxIo], sens_c[kMaxIo];
         shift_io(in, t->n_in, i0, in_c);
@@ -2584,6 +2606,30 @@ int casadi_gb300_map_reverse(int id, int mem, int64_t n, int nadj, const double*
       }))
     return rc;
   return casadi_gb300_sync(id, s);
+}
+
+int casadi_gb300_map_forward(int id, int mem, int64_t n, int nfwd, const double* const* arg,
+                             double* const* res, const double* const* fseed,
+                             double* const* fsens) {
+  return map_forward_impl(id, mem, n, nfwd, arg, res, fseed, fsens, false);
+}
+
+int casadi_gb300_map_forward_outer(int id, int mem, int64_t n, int nfwd,
+                                   const double* const* arg, double* const* res,
+                                   const double* const* fseed, double* const* fsens) {
+  return map_forward_impl(id, mem, n, nfwd, arg, res, fseed, fsens, true);
+}
+
+int casadi_gb300_map_reverse(int id, int mem, int64_t n, int nadj, const double* const* arg,
+                             double* const* res, const double* const* aseed,
+                             double* const* asens) {
+  return map_reverse_impl(id, mem, n, nadj, arg, res, aseed, asens, false);
+}
+
+int casadi_gb300_map_reverse_outer(int id, int mem, int64_t n, int nadj,
+                                   const double* const* arg, double* const* res,
+                                   const double* const* aseed, double* const* asens) {
+  return map_reverse_impl(id, mem, n, nadj, arg, res, aseed, asens, true);
 }
 
 int casadi_gb300_map_jacobian_reverse(int id, int mem, int64_t n, const double* const* arg,

@@ -103,6 +103,8 @@ def load(path=None):
         "casadi_gb300_map_eval": (cint, [cint, cint, i64, vp, vp]),
         "casadi_gb300_map_reverse": (cint, [cint, cint, i64, cint, vp, vp, vp, vp]),
         "casadi_gb300_map_forward": (cint, [cint, cint, i64, cint, vp, vp, vp, vp]),
+        "casadi_gb300_map_forward_outer": (cint, [cint, cint, i64, cint, vp, vp, vp, vp]),
+        "casadi_gb300_map_reverse_outer": (cint, [cint, cint, i64, cint, vp, vp, vp, vp]),
         "casadi_gb300_jacobian": (cint, [cint, i64, i64, vp, vp, vp, vp, sz, vp]),
         "casadi_gb300_map_jacobian": (cint, [cint, cint, i64, vp, vp, vp]),
         "casadi_gb300_jacobian_reverse": (cint, [cint, i64, i64, vp, vp, vp, cint, vp, vp, vp, sz,
@@ -765,30 +767,38 @@ class CudaMap:
             _host_ptrs(jac), nadj, _host_ptrs(aseeds), _host_ptrs(asens)))
         return res, jac, asens
 
-    def forward(self, args, fseeds, res=None, fsens=None):
-        """Forward sweep with instance-major host buffers: fseeds[j] has shape
-        (n, nfwd, nnz_in[j]); returns (res, fsens) with fsens[j] of shape (n, nfwd, nnz_out[j])."""
+    def forward(self, args, fseeds, res=None, fsens=None, outer=False):
+        """Forward sweep with host buffers. Inner order (the mapped f.forward(nfwd)'s):
+        fseeds[j] of shape (n, nfwd, nnz_in[j]), fsens[j] (n, nfwd, nnz_out[j]). outer=True:
+        the Map's own derivative order (Map::get_forward), fseeds[j] of shape
+        (nfwd, n, nnz_in[j]), fsens[j] (nfwd, n, nnz_out[j]). Returns (res, fsens)."""
         args = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in args]
         fseeds = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in fseeds]
-        nfwd = next(a.shape[1] for a in fseeds if a is not None)
+        nfwd = next(a.shape[0 if outer else 1] for a in fseeds if a is not None)
         res = self._host_out(self.tape.nnz_out) if res is None else res
-        fsens = [np.empty((self.n, nfwd, k)) for k in self.tape.nnz_out] if fsens is None else fsens
-        check(load().casadi_gb300_map_forward(self.tape.id, self.mem.id, self.n, nfwd,
-                                              _host_ptrs(args), _host_ptrs(res),
-                                              _host_ptrs(fseeds), _host_ptrs(fsens)))
+        if fsens is None:
+            fsens = [np.empty((nfwd, self.n, k) if outer else (self.n, nfwd, k))
+                     for k in self.tape.nnz_out]
+        fn = load().casadi_gb300_map_forward_outer if outer else load().casadi_gb300_map_forward
+        check(fn(self.tape.id, self.mem.id, self.n, nfwd, _host_ptrs(args), _host_ptrs(res),
+                 _host_ptrs(fseeds), _host_ptrs(fsens)))
         return res, fsens
 
-    def reverse(self, args, aseeds, res=None, asens=None):
-        """Adjoint sweep with instance-major host buffers: aseeds[j] has shape
-        (n, nadj, nnz_out[j]); returns (res, asens) with asens[j] of shape (n, nadj, nnz_in[j])."""
+    def reverse(self, args, aseeds, res=None, asens=None, outer=False):
+        """Adjoint sweep with host buffers. Inner order: aseeds[j] of shape
+        (n, nadj, nnz_out[j]), asens[j] (n, nadj, nnz_in[j]); outer=True: the Map's own
+        derivative order (Map::get_reverse), aseeds[j] (nadj, n, nnz_out[j]), asens[j]
+        (nadj, n, nnz_in[j]). Returns (res, asens)."""
         args = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in args]
         aseeds = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in aseeds]
-        nadj = next(a.shape[1] for a in aseeds if a is not None)
+        nadj = next(a.shape[0 if outer else 1] for a in aseeds if a is not None)
         res = self._host_out(self.tape.nnz_out) if res is None else res
-        asens = [np.empty((self.n, nadj, k)) for k in self.tape.nnz_in] if asens is None else asens
-        check(load().casadi_gb300_map_reverse(self.tape.id, self.mem.id, self.n, nadj,
-                                              _host_ptrs(args), _host_ptrs(res),
-                                              _host_ptrs(aseeds), _host_ptrs(asens)))
+        if asens is None:
+            asens = [np.empty((nadj, self.n, k) if outer else (self.n, nadj, k))
+                     for k in self.tape.nnz_in]
+        fn = load().casadi_gb300_map_reverse_outer if outer else load().casadi_gb300_map_reverse
+        check(fn(self.tape.id, self.mem.id, self.n, nadj, _host_ptrs(args), _host_ptrs(res),
+                 _host_ptrs(aseeds), _host_ptrs(asens)))
         return res, asens
 
 

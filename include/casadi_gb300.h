@@ -364,6 +364,18 @@ CASADI_GB300_API int casadi_gb300_map_forward(int id, int mem, int64_t n, int nf
 CASADI_GB300_API int casadi_gb300_map_reverse(int id, int mem, int64_t n, int nadj, const double* const* arg,
                              double* const* res, const double* const* aseed,
                              double* const* asens);
+/* The same two calls with seeds and sensitivities in the order of the Map's own derivative
+ * Functions: direction d of instance i of block j at fseed[j] + (d*n + i)*nnz_in[j] (and
+ * likewise fsens, aseed, asens), values as above. Replaces: the MX index-slice reorders that
+ * Map::get_forward / Map::get_reverse wrap around f.forward(nfwd).map(n) and
+ * f.reverse(nadj).map(n) (casadi/core/map.cpp:219-325), so a cuda Map's derivative needs no
+ * reorder pass: the sweeps address this order through their block strides. */
+CASADI_GB300_API int casadi_gb300_map_forward_outer(int id, int mem, int64_t n, int nfwd,
+                             const double* const* arg, double* const* res,
+                             const double* const* fseed, double* const* fsens);
+CASADI_GB300_API int casadi_gb300_map_reverse_outer(int id, int mem, int64_t n, int nadj,
+                             const double* const* arg, double* const* res,
+                             const double* const* aseed, double* const* asens);
 /* Host-buffer form of casadi_gb300_jacobian_reverse: arg/res/aseed as in the two calls
  * above, jac[j] as in casadi_gb300_map_jacobian, asens[j] as in casadi_gb300_map_reverse. */
 CASADI_GB300_API int casadi_gb300_map_jacobian_reverse(int id, int mem, int64_t n,

@@ -385,6 +385,30 @@ def test_host_buffer_calls_in_pipelined_chunks(gpu_lib):
     assert_bitexact(np.transpose(jac[0], (1, 2, 0)), host(djac)[0], "jacobian")
 
 
+@pytest.mark.parametrize("n", [1000, 2 * 131072 + 77])
+def test_map_derivatives_in_the_maps_own_order(gpu_lib, n):
+    """Seeds and sensitivities in the order of Map::get_forward/get_reverse (direction-major,
+    (d*n + i)*nnz; casadi/core/map.cpp:233-264) give the bits of the inner order
+    ((i*ndir + d)*nnz), at a size run in one chunk and at one run in pipelined chunks."""
+    f = W.cartpole_rollout(2)
+    x, u = W.cartpole_inputs(n, steps=2, seed=31)
+    args = [x.T.copy(), u.T.copy()]
+    F = CudaMap(f, n)
+    rng = np.random.default_rng(31)
+    fo = [rng.standard_normal((3, n, 4)), rng.standard_normal((3, n, 2))]
+    r_o, s_o = F.forward(args, fo, outer=True)
+    r_i, s_i = F.forward(args, [np.ascontiguousarray(np.transpose(a, (1, 0, 2))) for a in fo])
+    for a, b in zip(r_o, r_i):
+        assert_bitexact(a, b, "forward values")
+    for a, b in zip(s_o, s_i):
+        assert_bitexact(a, np.transpose(b, (1, 0, 2)), "forward, Map order")
+    ao = [rng.standard_normal((2, n, 4)), rng.standard_normal((2, n, 1))]
+    r_o, a_o = F.reverse(args, ao, outer=True)
+    r_i, a_i = F.reverse(args, [np.ascontiguousarray(np.transpose(a, (1, 0, 2))) for a in ao])
+    for a, b in zip(a_o, a_i):
+        assert_bitexact(a, np.transpose(b, (1, 0, 2)), "reverse, Map order")
+
+
 # ---- derivative-sweep variants and the autotuner ------------------------------------------------
 def test_every_variant_gives_the_same_bits(gpu_lib):
     """The variants differ in prefetch depth and register cap only: forward, Jacobian and
