@@ -2480,6 +2480,49 @@ int casadi_gb300_map_eval(int id, int mem, int64_t n, const double* const* arg,
   return casadi_gb300_sync(id, s);
 }
 
+// bvec_t blocks travel through the same 8-byte staging as doubles (bit copies).
+static int map_sp(int id, int mem, int64_t n, uint64_t* const* arg, uint64_t* const* res,
+                  bool reverse) {
+  Tape* t = get_tape(id);
+  if (!t) return fail(CASADI_GB300_ERR_ID, "no tape with id %d", id);
+  Mem* m = get_mem(mem);
+  if (!m) return fail(CASADI_GB300_ERR_ID, "no memory object %d", mem);
+  if (int rc = check_device(*t)) return rc;
+  if (n < 0) return fail(CASADI_GB300_ERR_ARG, "negative instance count");
+  if (n == 0) return 0;
+  cudaStream_t s = m->stream;
+  const double* const* harg = reinterpret_cast<const double* const*>(arg);
+  const double* const* hres = reinterpret_cast<const double* const*>(res);
+  IoDesc in[kMaxIo], out[kMaxIo];
+  if (int rc = stage_blocks(*m, 0, t->n_in, t->nnz_in, 1, n, harg, false, in, s)) return rc;
+  if (int rc = stage_blocks(*m, kMaxIo, t->n_out, t->nnz_out, 1, n, hres, false, out, s))
+    return rc;
+  std::vector<HostBlock> blocks;
+  // forward: arg in, res out; reverse (in place): res seeds in and cleared, arg |= out
+  collect_blocks(blocks, in, t->n_in, harg, reverse ? reinterpret_cast<double* const*>(arg)
+                                                    : nullptr);
+  collect_blocks(blocks, out, t->n_out, reverse ? hres : nullptr,
+                 reinterpret_cast<double* const*>(res));
+  if (int rc = run_pipelined(*m, n, blocks, [&](long long i0, long long cnt) {
+        SweepArgs a = base_args(*t, cnt, 0);
+        shift_io(in, t->n_in, i0, a.in);
+        shift_io(out, t->n_out, i0, a.out);
+        return primal_launch(*t, a, cnt, reverse ? PK_SP_REVERSE : PK_SP_FORWARD, s);
+      }))
+    return rc;
+  return casadi_gb300_sync(id, s);
+}
+
+int casadi_gb300_map_sp_forward(int id, int mem, int64_t n, const uint64_t* const* arg,
+                                uint64_t* const* res) {
+  return map_sp(id, mem, n, const_cast<uint64_t* const*>(arg), res, false);
+}
+
+int casadi_gb300_map_sp_reverse(int id, int mem, int64_t n, uint64_t* const* arg,
+                                uint64_t* const* res) {
+  return map_sp(id, mem, n, arg, res, true);
+}
+
 int casadi_gb300_map_jacobian(int id, int mem, int64_t n, const double* const* arg,
                               double* const* res, double* const* jac) {
   Tape* t = get_tape(id);

@@ -104,6 +104,8 @@ def load(path=None):
         "casadi_gb300_map_reverse": (cint, [cint, cint, i64, cint, vp, vp, vp, vp]),
         "casadi_gb300_map_forward": (cint, [cint, cint, i64, cint, vp, vp, vp, vp]),
         "casadi_gb300_map_forward_outer": (cint, [cint, cint, i64, cint, vp, vp, vp, vp]),
+        "casadi_gb300_map_sp_forward": (cint, [cint, cint, i64, vp, vp]),
+        "casadi_gb300_map_sp_reverse": (cint, [cint, cint, i64, vp, vp]),
         "casadi_gb300_map_reverse_outer": (cint, [cint, cint, i64, cint, vp, vp, vp, vp]),
         "casadi_gb300_jacobian": (cint, [cint, i64, i64, vp, vp, vp, vp, sz, vp]),
         "casadi_gb300_map_jacobian": (cint, [cint, cint, i64, vp, vp, vp]),
@@ -740,6 +742,22 @@ class CudaMap:
         check(load().casadi_gb300_map_eval(self.tape.id, self.mem.id, self.n, _host_ptrs(args),
                                            _host_ptrs(res)))
         return res
+
+    def sp_forward(self, args, res=None):
+        """bvec_t forward sweep with instance-major uint64 host buffers ((n, nnz_in[j]) per
+        input); returns the output words (n, nnz_out[j]) (Map::sp_forward)."""
+        args = [None if a is None else np.ascontiguousarray(a, dtype=np.uint64) for a in args]
+        res = [np.zeros((self.n, k), np.uint64) for k in self.tape.nnz_out] if res is None else res
+        check(load().casadi_gb300_map_sp_forward(self.tape.id, self.mem.id, self.n,
+                                                 _host_ptrs(args), _host_ptrs(res)))
+        return res
+
+    def sp_reverse(self, args, res):
+        """bvec_t reverse sweep in place (Map::sp_reverse): args[j] |= propagated bits,
+        res[j] (the seeds) cleared; uint64 arrays of shape (n, nnz)."""
+        check(load().casadi_gb300_map_sp_reverse(self.tape.id, self.mem.id, self.n,
+                                                 _host_ptrs(args), _host_ptrs(res)))
+        return args, res
 
     def jacobian(self, *args, res=None, jac=None):
         """Jacobian with instance-major host buffers: jac[j] has shape

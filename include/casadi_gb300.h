@@ -349,6 +349,14 @@ CASADI_GB300_API int casadi_gb300_map_eval(int id, int mem, int64_t n, const dou
 
 /* Map over the Jacobian with host buffers: jac[j] is instance-major
  * (jac[j] + (i*nnz_in_total + d)*nnz_out[j] holds column d of instance i). */
+/* Map over the bvec_t sparsity sweeps with host buffers in the Map layout (arg[j] +
+ * i*nnz_in[j], res[j] + i*nnz_out[j]). Replaces: Map::sp_forward / Map::sp_reverse, which call
+ * the function's sweep instance by instance (casadi/core/map.cpp:164-184); sp_reverse is in
+ * place as there: arg[j] |= propagated bits, res[j] cleared. A null block is skipped. */
+CASADI_GB300_API int casadi_gb300_map_sp_forward(int id, int mem, int64_t n,
+                             const uint64_t* const* arg, uint64_t* const* res);
+CASADI_GB300_API int casadi_gb300_map_sp_reverse(int id, int mem, int64_t n,
+                             uint64_t* const* arg, uint64_t* const* res);
 CASADI_GB300_API int casadi_gb300_map_jacobian(int id, int mem, int64_t n, const double* const* arg,
                               double* const* res, double* const* jac);
 

@@ -277,3 +277,20 @@ def test_casadi_serialized_text_on_the_gpu(gpu_lib, z):
     bound = O.libm_bound(casadi_tape(z, "cartpole"), args, args[0].shape[1])
     assert_values(res[0], z["cartpole/res0"], False, "deserialized cartpole", bound[0])
     ct.sync()
+
+
+def test_map_sparsity_sweeps_with_host_buffers_match_casadi(gpu_lib, z):
+    """Map::sp_forward / sp_reverse through the host-buffer entry points (instance-major bvec
+    words, casadi_gb300_map_sp_forward/_reverse) against CasADi's own sweeps, bit for bit."""
+    from casadi_gb300.runtime import CudaMap
+    t = tape_of(z, "dag")
+    seeds = golden_list(z, "dag", "spf_seed", 1)
+    n = seeds[0].shape[1]
+    M = CudaMap(CudaTape(t), n)
+    res = M.sp_forward([np.ascontiguousarray(seeds[0].T)])
+    assert (res[0].T == z["dag/spf_res0"]).all()
+    out = [np.ascontiguousarray(np.array(s).T) for s in golden_list(z, "dag", "spr_seed", 1)]
+    arg = [np.zeros((n, 64), np.uint64)]
+    M.sp_reverse(arg, out)
+    assert (arg[0].T == z["dag/spr_res0"]).all()
+    assert (out[0] == 0).all()
