@@ -275,14 +275,51 @@ def fp64_peak_tflops(torch):
     return best
 
 
-# ---- CPU baseline (oracle port, all host threads, bounded sample) -------------------------------
+# ---- CPU baseline (the reference's algorithm restated, all host threads) -----------------------
+_CASADI_TAPES = {}
+
+
+def casadi_rollout_tapes():
+    """CasADi's own derivative Functions of the 20-step rollout: the jacobian() tape as the
+    reference built it (tests/golden/casadi_rollout20_jacobian.npz, pinned by its SHA-256) and
+    reverse(1), which sx.reverse_function rebuilds instruction for instruction."""
+    if not _CASADI_TAPES:
+        from casadi_gb300 import calculus as C
+        from casadi_gb300 import sx as S
+        from casadi_gb300 import workloads as W
+        z = np.load(os.path.join(ROOT, "tests", "golden", "casadi_rollout20_jacobian.npz"))
+        op = z["jacobian/op"]
+        c = op == C.OP_CONST
+        _CASADI_TAPES["jacobian"] = S.Tape(
+            op, z["jacobian/i0"], np.where(c, 0, z["jacobian/i1"]),
+            np.where(c, 0, z["jacobian/i2"]), np.where(c, z["jacobian/d"], 0.0),
+            z["jacobian/nnz_in"].tolist(), z["jacobian/nnz_out"].tolist(),
+            int(z["jacobian/sz_w"]))
+        _CASADI_TAPES["reverse"] = S.reverse_function(W.cartpole_rollout(20)).tape
+    return _CASADI_TAPES["jacobian"], _CASADI_TAPES["reverse"]
+
+
+def casadi_calibration():
+    """CasADi's compiled library against the oracle's restatement of its algorithm, both on
+    the dev host's cores (profiles/cpu_casadi_openmp_devhost.json; the reference library cannot
+    be built where its sources are absent)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "cpu_casadi_openmp_devhost.json")) as f:
+            return json.load(f)["workloads"]
+    except (OSError, ValueError, KeyError):
+        return {}
+
+
 def cpu_step(tape, args, aseeds, n, threads, workload):
     import oracle as O
     if workload == "rollout20":
-        # the same step as the device's: one record of the partials per instance feeding the
-        # unit-seed Jacobian (structurally zero work skipped) and the cost adjoint
+        # the reference's algorithm: CasADi's F.jacobian() and F.reverse(1) are SXFunctions
+        # of their own (symbolic derivative tapes) that its VM evaluates; here those very
+        # tapes run on the oracle's restatement of SXFunction::eval
+        jt, bt = casadi_rollout_tapes()
         t0 = time.perf_counter()
-        O.jacobian_reverse(tape, args, aseeds, n, threads)
+        O.eval(jt, list(args) + [None, None], n, threads)
+        O.eval(bt, list(args) + [None, None] + [s[0] for s in aseeds], n, threads)
         return time.perf_counter() - t0
     t0 = time.perf_counter()
     if workload == "dag":
@@ -304,9 +341,18 @@ def cpu_baseline(F, args, aseeds, workload, budget_s=12.0):
     t = cpu_step(tape, sub(args, m), sub(aseeds, m), m, threads, workload)
     m2 = int(min(args[0].shape[-1], max(m, m * budget_s / max(t, 1e-6) / 2)))
     t2 = cpu_step(tape, sub(args, m2), sub(aseeds, m2), m2, threads, workload)
-    return {"value": m2 / t2, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "%d of the instances, same step (oracle C restatement, OpenMP, %d threads)"
-                      % (m2, threads)}
+    out = {"value": m2 / t2, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": "%d of the instances, same step (oracle C restatement, OpenMP, %d threads)"
+                     % (m2, threads)}
+    if workload == "rollout20":
+        out["sample"] = ("%d of the instances per step: CasADi's own jacobian() and reverse(1) "
+                         "tapes on the oracle's restatement of SXFunction::eval (OpenMP, %d "
+                         "threads)" % (m2, threads))
+        cal = casadi_calibration().get("rollout", {})
+        if cal.get("casadi_over_restated"):
+            out["casadi_compiled_over_restatement_devhost"] = cal["casadi_over_restated"]
+            out["casadi_openmp_estimate"] = out["value"] * cal["casadi_over_restated"]
+    return out
 
 
 def headline_parity(F, args_h, aseeds_h, res, jac, asens, m=1024, threads=None):
@@ -829,6 +875,24 @@ def run_native(a):
             lambda: ct.jacobian(dargs, res=res, jac=jac, stream=stream))
     # derivative-sweep variants the autotuner kept (tangent 8: the windowed sweep)
     comps["tuned_variants"] = {"jacobian": ct.tuned_variant(1), "adjoint": ct.tuned_variant(2)}
+    if a.workload == "rollout20":
+        # the drop-in's own route for the same results: CasADi's derivative Functions
+        # (jacobian(), reverse(1)) mapped with "cuda", i.e. their tapes on the value sweep
+        jt, bt = casadi_rollout_tapes()
+        cj, cb = R.CudaTape(jt), R.CudaTape(bt)
+        jres = [torch.empty((k, n), dtype=torch.float64, device="cuda") for k in jt.nnz_out]
+        bres = [torch.empty((k, n), dtype=torch.float64, device="cuda") for k in bt.nnz_out]
+        bargs = dargs + [None, None] + [x[0] for x in daseeds]
+
+        def derivative_functions():
+            cj.eval(dargs + [None, None], res=jres, stream=stream)
+            cb.eval(bargs, res=bres, stream=stream)
+
+        comps["casadi_derivative_functions_evals_per_s"] = rate(derivative_functions)
+        comps["casadi_derivative_function_instructions"] = {"jacobian": jt.n_instr,
+                                                            "reverse": bt.n_instr}
+        cj.sync()
+        cb.sync()
     ct.sync()
 
     weights = load_weights()
@@ -968,7 +1032,14 @@ def run_native(a):
         dist.destroy_process_group()
 
 
-# ---- reference arm (the oracle port of CasADi's VM on the host cores) ----------------------------
+# ---- reference arm (the reference's algorithm restated, on the host cores) ------------------------
+def ref_algo(workload):
+    return {"rollout20": "CasADi's own jacobian() and reverse(1) tapes on the oracle's "
+                         "restatement of SXFunction::eval",
+            "cartpole": "the tape on the oracle's restatement of SXFunction::eval",
+            "dag": "the oracle's numeric adjoint and bvec sweeps"}.get(workload, "oracle")
+
+
 def run_reference(a):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -995,10 +1066,16 @@ def run_reference(a):
             "data": "synthetic",
             "config": {"workload": desc, "instances_per_step": m, "same_instances": m == n},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": "%d of the %d instances per step, the same step "
-                                       "(oracle C restatement, OpenMP, %d threads; CasADi's own "
-                                       "library cannot be built on this host)" % (m, n, threads)},
+                             "sample": "%d of the %d instances per step, the same step by the "
+                                       "reference's algorithm (%s; OpenMP, %d threads; the "
+                                       "reference library itself needs its sources, absent on "
+                                       "this host)" % (m, n, ref_algo(a.workload), threads)},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    cal = casadi_calibration().get("rollout", {}) if a.workload == "rollout20" else {}
+    if cal.get("casadi_over_restated"):
+        line["cpu_baseline"]["casadi_compiled_over_restatement_devhost"] = \
+            cal["casadi_over_restated"]
+        line["cpu_baseline"]["casadi_openmp_estimate"] = v * cal["casadi_over_restated"]
     print(json.dumps(line), flush=True)
 
 

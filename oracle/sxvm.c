@@ -77,7 +77,7 @@ static double sxo_erfinv(double x) {
   }
 }
 
-double sxo_fun(int op, double x, double y) {
+static inline double fun_op(int op, double x, double y) {
   switch (op) {
     case SXO_ASSIGN: return x;
     case SXO_ADD: return x + y;
@@ -135,7 +135,7 @@ double sxo_fun(int op, double x, double y) {
 }
 
 /* BinaryOperation<OP>::der (calculus.hpp:598-1018); unary ops set d[1] = 0 (:384-387) */
-void sxo_der(int op, double x, double y, double f, double* d) {
+static inline void der_op(int op, double x, double y, double f, double* d) {
   d[1] = 0;
   switch (op) {
     case SXO_ASSIGN: d[0] = 1; break;
@@ -190,6 +190,10 @@ void sxo_der(int op, double x, double y, double f, double* d) {
   }
 }
 
+/* the exported forms of the two (the sweeps below use the inlined ones) */
+double sxo_fun(int op, double x, double y) { return fun_op(op, x, y); }
+void sxo_der(int op, double x, double y, double f, double* d) { der_op(op, x, y, f, d); }
+
 int sxo_ndeps(int op) {
   switch (op) {
     case SXO_CONST: case SXO_PARAMETER: case SXO_INPUT: return 0;
@@ -206,15 +210,20 @@ int sxo_ndeps(int op) {
 /* one instance                                                                              */
 /* ---------------------------------------------------------------------------------------- */
 
-static void eval_one(const sxo_tape* t, long n, long i, const double* const* arg,
+/* One instruction as SXFunction::eval walks it: an AlgEl-like record (op, i0, i1, i2, d). */
+typedef struct {
+  int op, i0, i1, i2;
+  double d;
+} sxo_ins;
+
+static void eval_one(const sxo_ins* alg, int n_instr, long n, long i, const double* const* arg,
                      double* const* res, double* w) {
-  for (int k = 0; k < t->n_instr; ++k) {
-    int op = t->op[k], i0 = t->i0[k], i1 = t->i1[k], i2 = t->i2[k];
-    switch (op) {
-      case SXO_CONST: w[i0] = t->d[k]; break;
-      case SXO_INPUT: w[i0] = arg[i1] ? arg[i1][(long)i2 * n + i] : 0; break;
-      case SXO_OUTPUT: if (res[i0]) res[i0][(long)i2 * n + i] = w[i1]; break;
-      default: w[i0] = sxo_fun(op, w[i1], w[i2]);
+  for (const sxo_ins* e = alg; e != alg + n_instr; ++e) {
+    switch (e->op) {
+      case SXO_CONST: w[e->i0] = e->d; break;
+      case SXO_INPUT: w[e->i0] = arg[e->i1] ? arg[e->i1][(long)e->i2 * n + i] : 0; break;
+      case SXO_OUTPUT: if (res[e->i0]) res[e->i0][(long)e->i2 * n + i] = w[e->i1]; break;
+      default: w[e->i0] = fun_op(e->op, w[e->i1], w[e->i2]);
     }
   }
 }
@@ -240,8 +249,8 @@ static void eval_partials(const sxo_tape* t, long n, long i, const double* const
       case SXO_OUTPUT: if (res && res[i0]) res[i0][(long)i2 * n + i] = w[i1]; break;
       default: {
         double x = w[i1], y = w[i2];
-        double f = sxo_fun(op, x, y);
-        sxo_der(op, x, y, f, dp + 2 * (long)k);
+        double f = fun_op(op, x, y);
+        der_op(op, x, y, f, dp + 2 * (long)k);
         if (g_magnitude) {
           dp[2 * (long)k] = fabs(dp[2 * (long)k]);
           dp[2 * (long)k + 1] = fabs(dp[2 * (long)k + 1]);
@@ -255,6 +264,16 @@ static void eval_partials(const sxo_tape* t, long n, long i, const double* const
 int sxo_eval(const sxo_tape* t, long n, const double* const* arg, double* const* res,
              int nthreads) {
   int err = 0;
+  /* the tape as one array of records, walked once per instance */
+  sxo_ins* alg = (sxo_ins*)malloc(sizeof(sxo_ins) * (t->n_instr > 0 ? t->n_instr : 1));
+  if (!alg) return 1;
+  for (int k = 0; k < t->n_instr; ++k) {
+    alg[k].op = t->op[k];
+    alg[k].i0 = t->i0[k];
+    alg[k].i1 = t->i1[k];
+    alg[k].i2 = t->i2[k];
+    alg[k].d = t->d[k];
+  }
 #pragma omp parallel num_threads(nthreads > 0 ? nthreads : 1)
   {
     double* w = (double*)malloc(sizeof(double) * (t->sz_w > 0 ? t->sz_w : 1));
@@ -263,10 +282,11 @@ int sxo_eval(const sxo_tape* t, long n, const double* const* arg, double* const*
       err = 1;
     } else {
 #pragma omp for schedule(static)
-      for (long i = 0; i < n; ++i) eval_one(t, n, i, arg, res, w);
+      for (long i = 0; i < n; ++i) eval_one(alg, t->n_instr, n, i, arg, res, w);
     }
     free(w);
   }
+  free(alg);
   return err;
 }
 
@@ -542,8 +562,8 @@ int sxo_libm_bound(const sxo_tape* t, long n, const double* const* arg, double* 
             case SXO_OUTPUT: break;
             default: {
               double x = w[i1], y = w[i2];
-              double f = sxo_fun(op, x, y);
-              sxo_der(op, x, y, f, dp + 2 * (long)k);
+              double f = fun_op(op, x, y);
+              der_op(op, x, y, f, dp + 2 * (long)k);
               w[i0] = fv[k] = f;
             }
           }

@@ -236,6 +236,21 @@ def main():
     out["quad/uni_coloring_jac"] = R.coloring("uni", jp)[0]
     out["quad/star_coloring_hess"] = R.coloring("star", hp, 1)[0]
 
+    # the 20-step rollout's jacobian() tape in full: the CPU reference legs of the benchmark
+    # evaluate CasADi's own derivative tapes (this one and reverse(1), which
+    # sx.reverse_function rebuilds) on the oracle's restatement of SXFunction::eval
+    J = R.build("rollout", 20).jacobian()
+    jt = {}
+    put_tape(jt, "jacobian", J)
+    op, i0, i1, i2, d = J.tape()
+    jt.update({"jacobian/op": op, "jacobian/i0": i0, "jacobian/i1": i1, "jacobian/i2": i2,
+               "jacobian/d": d})
+    for k in range(J.n_out):
+        put_pattern(jt, "jacobian/out%d" % k, J.sparsity_out(k))
+    jpath = os.path.join(HERE, "casadi_rollout20_jacobian.npz")
+    np.savez_compressed(jpath, **jt)
+    print("casadi_rollout20_jacobian.npz", os.path.getsize(jpath), "bytes")
+
     path = os.path.join(HERE, "casadi.npz")
     np.savez_compressed(path, **out)
     print("casadi.npz", os.path.getsize(path), "bytes")

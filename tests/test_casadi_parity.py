@@ -356,3 +356,21 @@ def test_live_random_dags(seed, n_in, n_nodes, n_out, bounded):
     args = W.dag_inputs(n, n_in=n_in, seed=seed)
     for got, want in zip(O.eval(mine.tape, args, n), ref.eval(args, n)):
         assert_bitexact(got, want, "live DAG %d" % seed)
+
+
+def _jacobian_tape():
+    j = load_npz("casadi_rollout20_jacobian.npz")
+    return casadi_tape(j, "jacobian"), j
+
+
+def test_casadi_jacobian_tape_fixture_gives_casadis_jacobian(z):
+    """The rollout's jacobian() tape, as CasADi built it, on the oracle's restatement of
+    SXFunction::eval gives CasADi's Jacobian bit for bit (the CPU reference legs of the
+    benchmark run exactly this)."""
+    t, j = _jacobian_tape()
+    assert tape_sha256(t) == str(j["jacobian/tape_sha256"]) and t.n_instr == 19964
+    args = golden_list(z, "rollout", "arg", 2)
+    n = args[0].shape[1]
+    res = O.eval(t, list(args) + [None, None], n)
+    for k, key in enumerate(("jac_0_0", "jac_0_1", "jac_1_0", "jac_1_1")):
+        assert_bitexact(res[k], z["rollout/" + key], key)

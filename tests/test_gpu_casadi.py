@@ -294,3 +294,20 @@ def test_map_sparsity_sweeps_with_host_buffers_match_casadi(gpu_lib, z):
     M.sp_reverse(arg, out)
     assert (arg[0].T == z["dag/spr_res0"]).all()
     assert (out[0] == 0).all()
+
+
+def test_casadi_jacobian_function_on_the_value_sweep(gpu_lib, z):
+    """CasADi's F.jacobian() tape of the rollout (the drop-in's F.jacobian().map(N, "cuda"))
+    evaluated by the GPU value sweep against CasADi's Jacobian: element-wise within 1e-13
+    relative or the libm-propagation bound of each entry."""
+    j = load_npz("casadi_rollout20_jacobian.npz")
+    t = casadi_tape(j, "jacobian")
+    assert tape_sha256(t) == str(j["jacobian/tape_sha256"])
+    args = golden_list(z, "rollout", "arg", 2)
+    n = args[0].shape[1]
+    ct = CudaTape(t)
+    res = host(ct.eval(dev(list(args) + [None, None])))
+    bound = O.libm_bound(t, list(args) + [None, None], n)
+    for k, key in enumerate(("jac_0_0", "jac_0_1", "jac_1_0", "jac_1_1")):
+        assert_values(res[k], z["rollout/" + key], False, key, bound[k])
+    ct.sync()
