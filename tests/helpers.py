@@ -3,8 +3,9 @@
 Tolerances:
   * EXACT_OPS and tapes built only from them (+,-,*,/,sqrt and the sign/compare/select ops):
     bit-exact (NaN == NaN, -0 and +0 distinguished only where the op defines the sign).
-  * anything that calls a libm transcendental: |a-b| <= RTOL * max(|b|, floor) with
-    RTOL = 1e-13, the tolerance the evaluator is held to against the CPU reference.
+  * anything that calls a libm transcendental: element-wise |a-b| <= RTOL * |b| with
+    RTOL = 1e-13, or within a stated per-element bound (assert_close: the libm-propagation
+    bound of a value, or 1e-13 of the magnitude of a derivative's chain-rule terms).
 """
 import math
 import os
@@ -102,16 +103,41 @@ def rel_err(a, b, floor=1e-300):
     return float(d.max())
 
 
-def assert_close(a, b, what="", rtol=RTOL, floor=None):
-    """Relative check; `floor` (default: 1e-3 of the largest magnitude in b, at least 1e-300)
-    keeps values that cancel to near zero from dominating."""
+def assert_close(a, b, what="", rtol=RTOL, floor=None, bound=None):
+    """Element-wise: |a - b| <= rtol * max(|b|, floor) for every element (floor defaults to
+    1e-300, i.e. none: each element is held to the relative bar), or, where a per-element
+    ``bound`` is given, |a - b| <= bound -- the scale a difference of rounding is limited to
+    for that element: 4 ulps of every libm result propagated to a value
+    (``libm_ulps(oracle.libm_bound(...))``), or rtol times the magnitude of a derivative's
+    chain-rule terms (``rtol * mag`` with mag from ``oracle.magnitude``). NaN and inf must
+    match exactly. Returns the largest relative error."""
+    a = np.asarray(a, np.float64)
     b_arr = np.asarray(b, np.float64)
-    if floor is None:
-        fin = b_arr[np.isfinite(b_arr)]
-        floor = max(1e-300, 1e-3 * float(np.abs(fin).max())) if fin.size else 1e-300
-    e = rel_err(a, b, floor)
-    assert e <= rtol, "%s: relative error %.3e > %.1e (floor %.3e)" % (what, e, rtol, floor)
+    floor = 1e-300 if floor is None else floor
+    if not np.array_equal(np.isnan(a), np.isnan(b_arr)):
+        raise AssertionError("%s: NaN positions differ" % what)
+    inf = np.isinf(b_arr)
+    if not np.array_equal(a[inf], b_arr[inf]):
+        raise AssertionError("%s: inf entries differ" % what)
+    fin = np.isfinite(b_arr)
+    d = np.abs(a - b_arr)
+    ok = ~fin | (d <= rtol * np.maximum(np.abs(b_arr), floor))
+    if bound is not None:
+        ok |= d <= np.asarray(bound, np.float64)
+    if not ok.all():
+        i = tuple(np.argwhere(~ok)[0])
+        raise AssertionError("%s: %d of %d elements beyond the bar (rtol %.1e, floor %.1e%s), "
+                             "e.g. %s: %r vs %r" % (what, int((~ok).sum()), ok.size, rtol,
+                                                   floor, ", bounded" if bound is not None
+                                                   else "", i, a[i], b_arr[i]))
+    e = rel_err(a, b_arr, floor)
     return e
+
+
+def libm_ulps(bound, ulps=4):
+    """Per-element allowance for values: ``ulps`` relative perturbations of every libm result
+    propagated to each value (bound from oracle.libm_bound)."""
+    return ulps * 2.0**-52 * np.asarray(bound, np.float64)
 
 
 def call_rollout(steps):
