@@ -221,6 +221,21 @@ def libm_bound(tape, args, n, nthreads=1):
     return out
 
 
+def rounding_bound(tape, args, n, nthreads=1):
+    """As libm_bound over every computing instruction (sum over all of them of
+    |d out / d w_k| * |w_k|): two evaluations of the same function whose instructions round
+    differently, or that differ in the order of their sums, give outputs within a few times
+    2**-52 times this bound."""
+    t = TapeArrays(tape)
+    args = _prep(args)
+    _check(args, tape.nnz_in, n, "arguments")
+    out = _outs(tape.nnz_out, n)
+    rc = lib().sxo_rounding_bound(ct.byref(t.struct), ct.c_long(n), _ptrs(args), _ptrs(out),
+                                  ct.c_int(nthreads))
+    assert rc == 0
+    return out
+
+
 class magnitude:
     """Context in which forward / jacobian / reverse return magnitudes: the same sweeps over
     |partials| and |seeds|, i.e. per derivative entry the sum over its chain-rule paths of

@@ -535,8 +535,8 @@ static int is_libm(int op) {
  * derivative taken through |partials| (one magnitude adjoint sweep per output nonzero).
  * If two evaluations differ only in that each libm result may be off by up to c ulps, their
  * outputs differ by at most about c * 2^-52 * bound (to first order). */
-int sxo_libm_bound(const sxo_tape* t, long n, const double* const* arg, double* const* bound,
-                   int nthreads) {
+static int bound_impl(const sxo_tape* t, long n, const double* const* arg, double* const* bound,
+                      int nthreads, int every_op) {
   int err = 0;
 #pragma omp parallel num_threads(nthreads > 0 ? nthreads : 1)
   {
@@ -579,7 +579,7 @@ int sxo_libm_bound(const sxo_tape* t, long n, const double* const* arg, double* 
             double seed = wb[i0];
             wb[i0] = 0;
             if (op == SXO_CONST || op == SXO_INPUT || op == SXO_PARAMETER || seed == 0) continue;
-            if (is_libm(op)) acc += seed * fabs(fv[k]);
+            if (every_op || is_libm(op)) acc += seed * fabs(fv[k]);
             const double* d = dp + 2 * (long)k;
             wb[i1] += fabs(d[0]) * seed;
             if (sxo_ndeps(op) == 2) wb[i2] += fabs(d[1]) * seed;
@@ -591,6 +591,16 @@ int sxo_libm_bound(const sxo_tape* t, long n, const double* const* arg, double* 
     free(w); free(wb); free(dp); free(fv);
   }
   return err;
+}
+
+int sxo_libm_bound(const sxo_tape* t, long n, const double* const* arg, double* const* bound,
+                   int nthreads) {
+  return bound_impl(t, n, arg, bound, nthreads, 0);
+}
+
+int sxo_rounding_bound(const sxo_tape* t, long n, const double* const* arg,
+                       double* const* bound, int nthreads) {
+  return bound_impl(t, n, arg, bound, nthreads, 1);
 }
 
 int sxo_sp_forward(const sxo_tape* t, long n, const uint64_t* const* arg,

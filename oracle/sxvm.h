@@ -55,6 +55,11 @@ int sxo_zero_checker(int which, int op);
 void sxo_set_magnitude(int on);
 int sxo_libm_bound(const sxo_tape* t, long n, const double* const* arg, double* const* bound,
                    int nthreads);
+/* As sxo_libm_bound over every computing instruction: the first-order sensitivity of each
+ * output to a relative perturbation of every rounded result, which bounds (times a few ulps)
+ * the difference between two evaluations that round any instruction differently. */
+int sxo_rounding_bound(const sxo_tape* t, long n, const double* const* arg,
+                       double* const* bound, int nthreads);
 int sxo_activity(const sxo_tape* t, long n, const uint64_t* const* arg, uint64_t* const* res,
                  int nthreads);
 #endif

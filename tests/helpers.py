@@ -4,8 +4,10 @@ Tolerances:
   * EXACT_OPS and tapes built only from them (+,-,*,/,sqrt and the sign/compare/select ops):
     bit-exact (NaN == NaN, -0 and +0 distinguished only where the op defines the sign).
   * anything that calls a libm transcendental: element-wise |a-b| <= RTOL * |b| with
-    RTOL = 1e-13, or within a stated per-element bound (assert_close: the libm-propagation
-    bound of a value, or 1e-13 of the magnitude of a derivative's chain-rule terms).
+    RTOL = 1e-13, or within a stated per-element bound (assert_close): for a value, the
+    libm and rounding perturbations propagated to it (value_bounds); for a derivative, 1e-13
+    of the magnitude of its chain-rule terms (magnitudes), plus, on long chains, the libm
+    propagation through the derivative Function (adjoint_bounds).
 """
 import math
 import os
@@ -120,7 +122,8 @@ def assert_close(a, b, what="", rtol=RTOL, floor=None, bound=None):
     if not np.array_equal(a[inf], b_arr[inf]):
         raise AssertionError("%s: inf entries differ" % what)
     fin = np.isfinite(b_arr)
-    d = np.abs(a - b_arr)
+    with np.errstate(invalid="ignore"):  # inf - inf at matching infinities
+        d = np.abs(a - b_arr)
     ok = ~fin | (d <= rtol * np.maximum(np.abs(b_arr), floor))
     if bound is not None:
         ok |= d <= np.asarray(bound, np.float64)
@@ -138,6 +141,73 @@ def libm_ulps(bound, ulps=4):
     """Per-element allowance for values: ``ulps`` relative perturbations of every libm result
     propagated to each value (bound from oracle.libm_bound)."""
     return ulps * 2.0**-52 * np.asarray(bound, np.float64)
+
+
+def value_bounds(tape, args, n, nthreads=None):
+    """Per output, the element-wise allowance of a value against the oracle's evaluation of the
+    same tape: 4 ulps of every libm result (CUDA's and the host's libm each err by up to about
+    2 ulps) and 1 ulp of every rounded result (an input that moved by a few ulps can flip the
+    rounding of any instruction downstream), each propagated to the value to first order:
+    2**-52 * (4 * libm_bound + rounding_bound)."""
+    import oracle as O
+    nt = nthreads or os.cpu_count() or 1
+    lb = O.libm_bound(tape, args, n, nt)
+    rb = O.rounding_bound(tape, args, n, nt)
+    return [2.0**-52 * (4.0 * a + b) for a, b in zip(lb, rb)]
+
+
+def rounding_bounds(tape, args, n):
+    """Per output, the element-wise allowance of a value against the same function evaluated
+    by a tape that rounds any instruction differently (another association of its sums, a
+    chain of calls instead of one unrolled tape): 4 ulps of every rounded result propagated
+    to it."""
+    import oracle as O
+    return [libm_ulps(b) for b in O.rounding_bound(tape, args, n)]
+
+
+def adjoint_bounds(f, args, aseed, n):
+    """Per input, the allowance of one adjoint direction (seeds ``aseed``, one (nnz_out, n)
+    array per output) against the oracle's: 4 ulps of every libm result of the reference's
+    adjoint Function f.reverse(1) (sx.reverse_function) at the same point, propagated to each
+    sensitivity -- the sin/cos differences of the primal values carried through the partials.
+    On long chains (a 100-step rollout) this exceeds 1e-13 of the magnitude of the chain-rule
+    terms; the rounding of the adjoint sums themselves is what that magnitude term covers."""
+    import oracle as O
+    B = S.reverse_function(f)
+    bargs = list(args) + [None] * len(f.tape.nnz_out) + list(aseed)
+    return [libm_ulps(b) for b in O.libm_bound(B.tape, bargs, n, os.cpu_count() or 1)]
+
+
+def magnitudes(fn, *args, **kw):
+    """``fn`` (oracle.forward / reverse / jacobian) run in the oracle's magnitude mode: its
+    derivative outputs are then the sums over chain-rule paths of |partials| x |seeds|."""
+    import oracle as O
+    with O.magnitude():
+        return fn(*args, **kw)
+
+
+def assert_adjoint_close(got, want, mag, f, args, aseed, what=""):
+    """One adjoint direction of ``f`` (sensitivities ``got`` against the oracle's ``want``, one
+    (nnz_in, n) array per input; ``mag`` their magnitudes; ``aseed`` one (nnz_out, n) seed per
+    output) element-wise within 1e-13 of the magnitude, or, on the instances where that is
+    exceeded, within that plus :func:`adjoint_bounds` (computed on those instances only)."""
+    got = [np.asarray(g, np.float64) for g in got]
+    want = [np.asarray(w, np.float64) for w in want]
+    over = set()
+    for g, w, m in zip(got, want, mag):
+        bad = ~(same_bits(g, w) | (np.abs(g - w) <= RTOL * m))
+        over.update(np.nonzero(bad.any(axis=0))[0].tolist())
+    cols = np.array(sorted(over), dtype=np.int64)
+    ab = None
+    if cols.size:
+        sub = [None if a is None else np.ascontiguousarray(a[:, cols]) for a in args]
+        ab = adjoint_bounds(f, sub, [np.ascontiguousarray(s[:, cols]) for s in aseed], cols.size)
+    for j, (g, w, m) in enumerate(zip(got, want, mag)):
+        bound = RTOL * np.asarray(m, np.float64)
+        if ab is not None:
+            bound = bound.copy()
+            bound[:, cols] += ab[j]
+        assert_close(g, w, "%s (input %d)" % (what, j), bound=bound)
 
 
 def call_rollout(steps):

@@ -11,7 +11,7 @@ import oracle as O
 from casadi_gb300 import runtime as R
 from casadi_gb300 import workloads as W
 
-from helpers import RTOL, assert_bitexact, assert_close
+from helpers import assert_adjoint_close, assert_bitexact, assert_close, magnitudes, value_bounds
 
 pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
@@ -73,14 +73,17 @@ def test_tape_larger_than_shared_memory(gpu_lib):
     args = W.quad_ms_inputs(n, intervals=100, seed=7)
     res = _host(ct.eval(_dev(args)))
     want = O.eval(F.tape, args, n)
-    for g, w in zip(res, want):
-        assert_close(g, w, "values", rtol=RTOL)
+    for g, w, b in zip(res, want, value_bounds(F.tape, args, n)):
+        assert_close(g, w, "values", bound=b)
     seeds = [np.zeros((1, k, n)) for k in F.tape.nnz_out]
     seeds[1][:] = 1.0
     _, asens = ct.reverse(_dev(args), _dev(seeds))
     _, was = O.reverse(F.tape, args, seeds, n)
-    for g, w in zip(_host(asens), was):
-        assert_close(g, w, "adjoint of the Lagrangian", rtol=RTOL)
+    _, mag = magnitudes(O.reverse, F.tape, args, seeds, n)
+    # a handful of sensitivities cancel so far that the sin/cos ulps of the primal values,
+    # carried through the partials, exceed 1e-13 of their magnitude: the adjoint-Function bound
+    assert_adjoint_close([a[0] for a in _host(asens)], [w[0] for w in was], [m[0] for m in mag],
+                         F, args, [s[0] for s in seeds], "adjoint of the Lagrangian")
     ct.sync()
 
 
@@ -119,6 +122,7 @@ def test_cooperative_sweeps_on_wide_tapes(gpu_lib, n):
                     assert_bitexact(x, y, "residence %d" % mode)
         if n <= 4096:
             m = min(n, 64)
-            want = O.eval(F.tape, [a[:, :m].copy() for a in args_h], m)
-            for g, w in zip(out[3][0], want):
-                assert_close(g[:, :m], w, "values", rtol=RTOL)
+            sub = [a[:, :m].copy() for a in args_h]
+            want = O.eval(F.tape, sub, m)
+            for g, w, b in zip(out[3][0], want, value_bounds(F.tape, sub, m)):
+                assert_close(g[:, :m], w, "values", bound=b)

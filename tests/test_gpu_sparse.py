@@ -9,7 +9,7 @@ import pytest
 import oracle as O
 from casadi_gb300 import workloads as W
 
-from helpers import RTOL, assert_close, same_bits
+from helpers import RTOL, assert_close, magnitudes, same_bits
 
 pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
@@ -40,7 +40,9 @@ def test_colored_constraint_jacobian(gpu_lib):
     mask[cols, rows] = False
     assert not np.any(dense[mask])
     _, wjac = O.jacobian(F.tape, args, n)
-    assert_close(vals, wjac[0][cols, rows], "colored constraint Jacobian", rtol=RTOL)
+    _, jmag = magnitudes(O.jacobian, F.tape, args, n)
+    assert_close(vals, wjac[0][cols, rows], "colored constraint Jacobian",
+                 bound=RTOL * jmag[0][cols, rows])
 
 
 def test_colored_lagrangian_hessian(gpu_lib):
@@ -55,10 +57,15 @@ def test_colored_lagrangian_hessian(gpu_lib):
     # oracle: dense Jacobian of the same gradient tape
     G = H.gradient_function
     _, gj = O.jacobian(G.tape, args, n)
+    _, gm = magnitudes(O.jacobian, G.tape, args, n)
     dense = gj[0][:nw]  # [w nonzero j][gradient entry i][instance] = H[i, j]
-    assert_close(vals, dense[H.cols, H.rows], "colored Hessian vs oracle", rtol=1e-12)
-    # symmetric: H[i, j] == H[j, i] in the oracle's dense Hessian
-    assert_close(dense[H.rows, H.cols], dense[H.cols, H.rows], "symmetry", rtol=1e-12)
+    mag = gm[0][:nw]
+    assert_close(vals, dense[H.cols, H.rows], "colored Hessian vs oracle",
+                 bound=RTOL * mag[H.cols, H.rows])
+    # symmetric: H[i, j] == H[j, i] in the oracle's dense Hessian, up to the rounding of the
+    # two different chain-rule sums that give them
+    assert_close(dense[H.rows, H.cols], dense[H.cols, H.rows], "symmetry",
+                 bound=RTOL * (mag[H.rows, H.cols] + mag[H.cols, H.rows]))
     # central differences of the oracle's adjoint (gradient of the Lagrangian) on 3 instances
     m, h = 3, 1e-6
     Hd = np.zeros((nw, nw, m))
@@ -155,8 +162,9 @@ def test_kkt_function_of_the_nlp(gpu_lib):
     nw = len(w)
     # Jacobian of g against the oracle's dense Jacobian
     _, gj = O.jacobian(kkt.g_function.tape, args_h, n)
+    _, gm = magnitudes(O.jacobian, kkt.g_function.tape, args_h, n)
     rows, cols = kkt.jac_pattern.row, kkt.jac_pattern.col()
-    assert_close(jac, gj[0][cols, rows], "jac:g:x", rtol=RTOL)
+    assert_close(jac, gj[0][cols, rows], "jac:g:x", bound=RTOL * gm[0][cols, rows])
     # Hessian: symmetric bit for bit, and the oracle's Jacobian of the symbolic gradient
     hp = kkt.hess_pattern
     hr, hc = hp.row, hp.col()
@@ -164,7 +172,8 @@ def test_kkt_function_of_the_nlp(gpu_lib):
     for k, (i, j) in enumerate(zip(hr, hc)):
         assert same_bits(hess[k], hess[full[(int(j), int(i))]]).all()
     _, hj = O.jacobian(kkt.hess.gradient_function.tape, args_h, n)
-    assert_close(hess, hj[0][:nw][hc, hr], "hess:gamma:x:x", rtol=1e-12)
+    _, hm = magnitudes(O.jacobian, kkt.hess.gradient_function.tape, args_h, n)
+    assert_close(hess, hj[0][:nw][hc, hr], "hess:gamma:x:x", bound=RTOL * hm[0][:nw][hc, hr])
     # the batched graph
     run = kkt.batched(args)
     for _ in range(2):

@@ -243,6 +243,21 @@ def test_libm_bound_on_hand_checked_tapes():
     assert (O.libm_bound(g.tape, [xs[None, :]], xs.size)[0] == 0).all()
 
 
+def test_rounding_bound_counts_every_rounded_result():
+    """x*x / (x+3): each of the three rounded results w_k contributes |d out/d w_k| |w_k| =
+    |out|, so the bound is 3|out|; 3 sin(x) - x: 3|sin x| (the sin and the product, each) plus
+    |3 sin x - x| (the difference)."""
+    x = S.sym("x", 1)
+    xs = np.array([0.5, -1e-3, 2.0, 0.0, -2.5])
+    g = S.Function("g", [x], [[x[0] * x[0] / (x[0] + 3.0)]])
+    b = O.rounding_bound(g.tape, [xs[None, :]], xs.size)[0][0]
+    np.testing.assert_allclose(b, 3 * np.abs(xs * xs / (xs + 3.0)), rtol=1e-15)
+    f = S.Function("f", [x], [[S.sin(x[0]) * 3.0 - x[0]]])
+    b = O.rounding_bound(f.tape, [xs[None, :]], xs.size)[0][0]
+    s = np.abs(np.sin(xs))
+    np.testing.assert_allclose(b, 6 * s + np.abs(3 * np.sin(xs) - xs), rtol=1e-15)
+
+
 def test_magnitude_mode_is_the_sweep_over_absolute_values():
     """In magnitude mode the adjoint of a * b - c * d at (2, -3, 5, 7) with seed -1 is
     (|b|, |a|, |d|, |c|) = (3, 2, 7, 5); outside it the signed adjoint returns."""
@@ -255,3 +270,29 @@ def test_magnitude_mode_is_the_sweep_over_absolute_values():
     np.testing.assert_array_equal(m[0][0][:, 0], [3, 2, 7, 5])
     _, a = O.reverse(f.tape, args, seed, 1)
     np.testing.assert_array_equal(a[0][0][:, 0], [3, -2, 7, 5])
+
+
+def test_adjoint_bound_helper_takes_rounding_and_rejects_a_planted_error():
+    """assert_adjoint_close passes the oracle's own adjoint moved within 1e-13 of the
+    magnitude, and on one element by a little over that but within the adjoint-Function bound;
+    an error planted at 1e-9 relative on one element fails it."""
+    from casadi_gb300 import workloads as W
+    from helpers import adjoint_bounds, assert_adjoint_close
+    F = W.cartpole_rollout(10)
+    n = 48
+    args = list(W.cartpole_inputs(n, steps=10, seed=2))
+    seeds = [np.zeros((1, 4, n)), np.ones((1, 1, n))]
+    _, was = O.reverse(F.tape, args, seeds, n)
+    with O.magnitude():
+        _, mag = O.reverse(F.tape, args, seeds, n)
+    want = [w[0] for w in was]
+    mags = [m[0] for m in mag]
+    aseed = [s[0] for s in seeds]
+    got = [w + 0.5 * RTOL * m for w, m in zip(want, mags)]
+    assert_adjoint_close(got, want, mags, F, args, aseed, "rounding")
+    ab = adjoint_bounds(F, args, aseed, n)
+    got[1][3, 7] = want[1][3, 7] + RTOL * mags[1][3, 7] + 0.5 * ab[1][3, 7]
+    assert_adjoint_close(got, want, mags, F, args, aseed, "within the adjoint bound")
+    got[1][3, 7] = want[1][3, 7] * (1 + 1e-9) + 1e-9
+    with pytest.raises(AssertionError):
+        assert_adjoint_close(got, want, mags, F, args, aseed, "planted")
