@@ -188,6 +188,12 @@ struct Tape {
   std::vector<std::unique_ptr<TanPlan>> tan_plans;
   std::vector<std::unique_ptr<WinPlan>> win_plans;
   std::vector<std::unique_ptr<AdjPlan>> adj_plans;
+  // the checkpointed adjoint's segment tapes, for one segment count at a time (seg_count 0:
+  // none yet); calls on this tape's checkpointed entry point are serialised by seg_mtx
+  std::mutex seg_mtx;
+  int seg_count = 0, seg_req = 0;                 // segments made, segments asked for
+  std::vector<std::vector<int>> seg_live;         // live slots at each cut (seg_count + 1)
+  std::vector<std::unique_ptr<Tape>> seg;         // segment tapes, in tape order
 
   ~Tape() {
     int cur = 0;
@@ -196,6 +202,7 @@ struct Tape {
     tan_plans.clear();
     win_plans.clear();
     adj_plans.clear();
+    seg.clear();
     cudaFree(d_code);
     cudaFree(d_pofs);
     cudaFree(d_consts);
@@ -1409,8 +1416,11 @@ struct Encoded {
   long long n_partials = 0;
 };
 
+// all_outputs: every output nonzero must be written (a user's tape); a segment tape of the
+// checkpointed adjoint writes only the outputs of its own instructions.
 int encode_tape(const casadi_gb300_atomic* alg, int n_instr, int n_in, const int* nnz_in,
-                int n_out, const int* nnz_out, int sz_w, Encoded& enc_out) {
+                int n_out, const int* nnz_out, int sz_w, Encoded& enc_out,
+                bool all_outputs = true) {
   if (n_instr < 0 || (n_instr > 0 && !alg)) return fail(CASADI_GB300_ERR_ARG, "no instructions");
   if (n_in < 0 || n_out < 0 || sz_w < 0) return fail(CASADI_GB300_ERR_ARG, "negative size");
   if ((n_in > 0 && !nnz_in) || (n_out > 0 && !nnz_out))
@@ -1473,7 +1483,7 @@ int encode_tape(const casadi_gb300_atomic* alg, int n_instr, int n_in, const int
       n_partials += __builtin_popcount(partial_mask(dop));
     }
   }
-  for (int j = 0; j < n_out; ++j)
+  for (int j = 0; j < n_out && all_outputs; ++j)
     for (int nz = 0; nz < nnz_out[j]; ++nz)
       if (!seen_out[j][nz])
         return fail(CASADI_GB300_ERR_ARG, "output %d nonzero %d is never written", j, nz);
@@ -1489,8 +1499,9 @@ int encode_tape(const casadi_gb300_atomic* alg, int n_instr, int n_in, const int
 // Encoded tape in the scheduled order; returns the scheduled work-vector length or a status.
 int encode_and_schedule(const casadi_gb300_atomic* alg, int n_instr, int n_in,
                         const int* nnz_in, int n_out, const int* nnz_out, int sz_w,
-                        Encoded& e) {
-  if (int rc = encode_tape(alg, n_instr, n_in, nnz_in, n_out, nnz_out, sz_w, e)) return rc;
+                        Encoded& e, bool all_outputs = true) {
+  if (int rc = encode_tape(alg, n_instr, n_in, nnz_in, n_out, nnz_out, sz_w, e, all_outputs))
+    return rc;
   std::vector<u64> sched;
   std::string err;
   const int w = schedule_code(e.code, sched, err);
@@ -1498,6 +1509,28 @@ int encode_and_schedule(const casadi_gb300_atomic* alg, int n_instr, int n_in,
   e.code.swap(sched);
   return w;
 }
+
+// One encoded instruction back in the reference's format.
+casadi_gb300_atomic decode_atomic(u64 w, const std::vector<double>& consts) {
+  casadi_gb300_atomic e;
+  std::memset(&e, 0, sizeof(e));
+  const unsigned op = dec_op(w);
+  e.op = reference_opcode(op);
+  e.i0 = static_cast<int>(dec_a(w));
+  if (op == D_CONST) {
+    e.a.d = consts[dec_b(w)];
+  } else {
+    e.a.i[0] = static_cast<int>(dec_b(w));
+    e.a.i[1] = static_cast<int>(dec_c(w));
+  }
+  return e;
+}
+
+// Validates, encodes, schedules and uploads a tape without registering it. A non-null
+// `absent` replaces the list of input nonzeros whose sensitivities the adjoint zeroes.
+int make_tape(const casadi_gb300_atomic* alg, int n_instr, int n_in, const int* nnz_in,
+              int n_out, const int* nnz_out, int sz_w, bool all_outputs,
+              const std::vector<int2>* absent, std::unique_ptr<Tape>& out);
 
 }  // namespace
 
@@ -1509,8 +1542,24 @@ const char* casadi_gb300_version(void) { return "0.1.0"; }
 
 int casadi_gb300_tape_create(const casadi_gb300_atomic* alg, int n_instr, int n_in,
                              const int* nnz_in, int n_out, const int* nnz_out, int sz_w) {
+  std::unique_ptr<Tape> t;
+  if (int rc = make_tape(alg, n_instr, n_in, nnz_in, n_out, nnz_out, sz_w, true, nullptr, t))
+    return rc;
+  std::lock_guard<std::mutex> lk(g_mtx);
+  g_tapes.push_back(std::move(t));
+  return static_cast<int>(g_tapes.size()) - 1;
+}
+
+}  // extern "C"
+
+namespace {
+
+int make_tape(const casadi_gb300_atomic* alg, int n_instr, int n_in, const int* nnz_in,
+              int n_out, const int* nnz_out, int sz_w, bool all_outputs,
+              const std::vector<int2>* absent, std::unique_ptr<Tape>& out) {
   Encoded en;
-  const int wlen = encode_and_schedule(alg, n_instr, n_in, nnz_in, n_out, nnz_out, sz_w, en);
+  const int wlen =
+      encode_and_schedule(alg, n_instr, n_in, nnz_in, n_out, nnz_out, sz_w, en, all_outputs);
   if (wlen < 0) return wlen;
   auto t = std::make_unique<Tape>();
   t->n_instr = n_instr;
@@ -1520,7 +1569,7 @@ int casadi_gb300_tape_create(const casadi_gb300_atomic* alg, int n_instr, int n_
   t->ref_sz_w = sz_w;
   t->nnz_in.assign(nnz_in, nnz_in + n_in);
   t->nnz_out.assign(nnz_out, nnz_out + n_out);
-  t->absent_in = en.absent_in;
+  t->absent_in = absent ? *absent : en.absent_in;
   std::vector<u64>& code = en.code;
   std::vector<double>& consts = en.consts;
   t->h_consts = consts;
@@ -1566,11 +1615,13 @@ int casadi_gb300_tape_create(const casadi_gb300_atomic* alg, int n_instr, int n_
     return cuda_fail(e, "upload absent inputs");
   if ((e = cudaMemset(t->d_err, 0, sizeof(int))) != cudaSuccess) return cuda_fail(e, "clear err");
   choose_shapes(*t);
-
-  std::lock_guard<std::mutex> lk(g_mtx);
-  g_tapes.push_back(std::move(t));
-  return static_cast<int>(g_tapes.size()) - 1;
+  out = std::move(t);
+  return 0;
 }
+
+}  // namespace
+
+extern "C" {
 
 int casadi_gb300_tape_schedule(const casadi_gb300_atomic* alg, int n_instr, int n_in,
                                const int* nnz_in, int n_out, const int* nnz_out, int sz_w,
@@ -1579,25 +1630,7 @@ int casadi_gb300_tape_schedule(const casadi_gb300_atomic* alg, int n_instr, int 
   Encoded en;
   const int wlen = encode_and_schedule(alg, n_instr, n_in, nnz_in, n_out, nnz_out, sz_w, en);
   if (wlen < 0) return wlen;
-  for (int k = 0; k < n_instr; ++k) {
-    const u64 w = en.code[k];
-    const unsigned op = dec_op(w);
-    casadi_gb300_atomic& e = out[k];
-    std::memset(&e, 0, sizeof(e));
-    e.op = reference_opcode(op);
-    if (op == D_CONST) {
-      e.i0 = static_cast<int>(dec_a(w));
-      e.a.d = en.consts[dec_b(w)];
-    } else if (op == D_OUTPUT) {
-      e.i0 = static_cast<int>(dec_a(w));
-      e.a.i[0] = static_cast<int>(dec_b(w));
-      e.a.i[1] = static_cast<int>(dec_c(w));
-    } else {
-      e.i0 = static_cast<int>(dec_a(w));
-      e.a.i[0] = static_cast<int>(dec_b(w));
-      e.a.i[1] = static_cast<int>(dec_c(w));
-    }
-  }
+  for (int k = 0; k < n_instr; ++k) out[k] = decode_atomic(en.code[k], en.consts);
   *sz_w_out = wlen;
   return 0;
 }
@@ -2744,3 +2777,4 @@ int casadi_gb300_map_jacobian_reverse(int id, int mem, int64_t n, const double* 
 #include "abi_batch.cuh"
 #include "abi_maps.cuh"
 #include "abi_probe.cuh"
+#include "abi_segments.cuh"

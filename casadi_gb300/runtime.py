@@ -113,6 +113,11 @@ def load(path=None):
                                                  vp]),
         "casadi_gb300_map_jacobian_reverse": (cint, [cint, cint, i64, vp, vp, vp, cint, vp, vp]),
         "casadi_gb300_reverse_noalloc": (cint, [cint, i64, i64, cint, vp, vp, vp, vp, vp]),
+        "casadi_gb300_checkpoint_scratch_size": (cint, [cint, cint, cint, i64, vp, vp]),
+        "casadi_gb300_reverse_checkpointed": (cint, [cint, i64, i64, cint, cint, vp, vp, vp, vp,
+                                                     vp, sz, vp]),
+        "casadi_gb300_tape_segments": (cint, [vp, cint, cint, vp, cint, vp, cint, cint, vp, vp,
+                                              vp, vp, cint, vp]),
         "casadi_gb300_profile": (cint, [cint]),
         "casadi_gb300_profile_collect": (cint, [vp, vp, cint]),
         "casadi_gb300_autotune": (cint, [cint]),
@@ -181,6 +186,40 @@ def schedule(tape):
                                          nnz_out.ctypes.data, tape.sz_w, out.ctypes.data,
                                          ct.byref(szw)))
     return _sx.Tape.from_atomic_array(out, tape.nnz_in, tape.nnz_out, szw.value)
+
+
+def segments(tape, count):
+    """The segment plan of :meth:`CudaTape.reverse_checkpointed` (host only, no device
+    needed): returns (cut positions in :func:`schedule`'s instruction list, live slot count at
+    each cut, the segment tapes as :class:`sx.Tape`). Segment s has the tape's inputs plus one
+    more (the slots live at cut s) and its outputs plus one more (the slots live at cut s+1);
+    it writes only the outputs of its own instructions."""
+    if isinstance(tape, _sx.Function):
+        tape = tape.tape
+    lib = load()
+    atoms = tape.atomic_array()
+    nnz_in = np.ascontiguousarray(tape.nnz_in, dtype=np.int32)
+    nnz_out = np.ascontiguousarray(tape.nnz_out, dtype=np.int32)
+    cut = np.zeros(count + 1, dtype=np.int32)
+    live = np.zeros(count + 1, dtype=np.int32)
+    seg_len = np.zeros(max(1, count), dtype=np.int32)
+    cap = tape.n_instr + 2 * tape.sz_w * count
+    out = np.zeros(max(1, cap), dtype=atoms.dtype)
+    szw = ct.c_int()
+    k = check(lib.casadi_gb300_tape_segments(atoms.ctypes.data, tape.n_instr, len(tape.nnz_in),
+                                             nnz_in.ctypes.data, len(tape.nnz_out),
+                                             nnz_out.ctypes.data, tape.sz_w, count,
+                                             cut.ctypes.data, live.ctypes.data,
+                                             seg_len.ctypes.data, out.ctypes.data, cap,
+                                             ct.byref(szw)))
+    tapes, off = [], 0
+    for s in range(k):
+        a = out[off:off + seg_len[s]]
+        off += seg_len[s]
+        tapes.append(_sx.Tape.from_atomic_array(a.copy(), list(tape.nnz_in) + [int(live[s])],
+                                                list(tape.nnz_out) + [int(live[s + 1])],
+                                                szw.value))
+    return cut[:k + 1].tolist(), live[:k + 1].tolist(), tapes
 
 
 def levels(tape, width=32, slot_cap=None):
@@ -449,6 +488,32 @@ class CudaTape:
             _ptr_array(aseeds), _ptr_array(asens), ct.c_void_p(sc.data_ptr()), sc.numel(),
             _stream_handle(stream)))
         return res, jac, asens
+
+    def checkpoint_scratch(self, segments, nadj, n, max_bytes=None):
+        """Scratch of :meth:`reverse_checkpointed` (one wave of all n instances, or at most
+        max_bytes but not below the minimum); returns (buffer, segments made)."""
+        import torch
+        full, least = ct.c_size_t(), ct.c_size_t()
+        k = check(load().casadi_gb300_checkpoint_scratch_size(self.id, segments, nadj, n,
+                                                              ct.byref(full), ct.byref(least)))
+        need = full.value if max_bytes is None else max(least.value, min(full.value, max_bytes))
+        return torch.empty(max(need, 8), dtype=torch.uint8, device="cuda"), k
+
+    def reverse_checkpointed(self, args, aseeds, segments, n=None, res=None, asens=None,
+                             stream=None, scratch_limit=None):
+        """As :meth:`reverse`, with segment checkpointing: the tape cut into ``segments``
+        runs, the live slots at each cut kept, each run re-recorded in the backward pass."""
+        n = self._n(args) if n is None else n
+        nadj = next((s.shape[0] for s in aseeds if s is not None), 0) if aseeds else 0
+        res = self._outs(self.nnz_out, n) if res is None else res
+        asens = self._outs(self.nnz_in, n, nadj) if asens is None else asens
+        sc, _ = self.checkpoint_scratch(segments, nadj, n, scratch_limit)
+        check(load().casadi_gb300_reverse_checkpointed(
+            self.id, n, n, nadj, segments, _ptr_array(args), _ptr_array(res),
+            _ptr_array(aseeds) if aseeds else None, _ptr_array(asens) if nadj else None,
+            ct.c_void_p(sc.data_ptr()), sc.numel(), _stream_handle(stream)))
+        self._keep = sc  # the sweep may still be running on the stream
+        return res, asens
 
     def sp_forward(self, args, n=None, stream=None):
         """args: int64 tensors holding bvec_t bit patterns, shape (nnz, n)."""

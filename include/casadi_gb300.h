@@ -489,6 +489,45 @@ CASADI_GB300_API int casadi_gb300_batch_status(int batch);
 CASADI_GB300_API int casadi_gb300_batch_run(int batch, void* scratch, size_t scratch_bytes,
                            int use_graph, void* stream);
 
+/* Reverse-mode AD with segment checkpointing, for tapes whose recorded partials (8 bytes x
+ * partials x instances) would not fit: the tape is cut into `segments` runs of consecutive
+ * instructions (at most one per instruction), near equal shares of the partials and where the
+ * fewest work-vector slots are live. The forward pass keeps only the live slots at each cut;
+ * the backward pass re-records one segment at a time from its checkpoint and sweeps it in
+ * reverse, so partials are held for one segment. Arguments as casadi_gb300_reverse; values
+ * equal casadi_gb300_eval's, sensitivities casadi_gb300_reverse's up to the rounding of adjoint
+ * sums that a cut associates differently. The scratch holds the checkpoints, two adjoint
+ * buffers and one segment's partials: casadi_gb300_checkpoint_scratch_size gives its size for
+ * one wave of all n instances and its minimum (below that: CASADI_GB300_ERR_SCRATCH; between
+ * the two the segments' sweeps run in instance waves). Both return the number of segments
+ * made, or a negative status. The segment tapes are built on the first call for a segment
+ * count and kept with the tape; calls on one tape are serialised. Replaces the reverse sweep
+ * over a stored work vector (SXFunction::ad_reverse, sx_function.cpp:1454-1560) when the
+ * storage does not fit. */
+CASADI_GB300_API int casadi_gb300_checkpoint_scratch_size(int id, int segments, int nadj,
+                                                          int64_t n, size_t* bytes,
+                                                          size_t* min_bytes);
+CASADI_GB300_API int casadi_gb300_reverse_checkpointed(int id, int64_t n, int64_t ld, int nadj,
+                                                       int segments, const double* const* arg,
+                                                       double* const* res,
+                                                       const double* const* aseed,
+                                                       double* const* asens, void* scratch,
+                                                       size_t scratch_bytes, void* stream);
+
+/* Host only (no GPU needed): the segment plan of casadi_gb300_reverse_checkpointed for a
+ * tape in the reference's format, after this library's scheduling (sz_w_out: its work-vector
+ * length). cut[0..k]: positions in the scheduled instruction list; live_count[0..k]: live
+ * slots at each cut; seg_len[0..k-1]: instructions of each segment tape, written one after
+ * another to seg_alg (capacity entries; each segment tape has the tape's inputs plus input
+ * n_in, the live slots at its first cut, and its outputs plus output n_out, the live slots at
+ * its last cut). Returns k, the number of segments made. */
+CASADI_GB300_API int casadi_gb300_tape_segments(const casadi_gb300_atomic* alg, int n_instr,
+                                                int n_in, const int* nnz_in, int n_out,
+                                                const int* nnz_out, int sz_w, int segments,
+                                                int* cut, int* live_count, int* seg_len,
+                                                casadi_gb300_atomic* seg_alg, int capacity,
+                                                int* sz_w_out);
+
 /* Allocation-free adjoint sweep: the same values and adjoint sensitivities as
  * casadi_gb300_reverse (arguments and layouts alike, no scratch argument), for callers that
  * cannot allocate device memory when they need derivatives -- real-time loops that forbid
