@@ -581,6 +581,51 @@ def rollout_autograd_component(torch, stream, n=1 << 20, reps=2):
             "peak_device_gb": torch.cuda.max_memory_allocated() / 1e9}
 
 
+def checkpoint_component(torch, stream, n=1 << 18, steps=100, reps=3):
+    """The adjoint of one long tape with segment checkpointing (casadi_gb300_reverse_checkpointed):
+    the cart-pole 100-step rollout as a single tape, adjoint of the cost, N = 2^18. The plain
+    adjoint records all partials (one wave); the checkpointed one keeps the live slots at each
+    cut and re-records one segment at a time. Time and scratch bytes of each."""
+    from casadi_gb300 import runtime as R
+    from casadi_gb300 import workloads as W
+    F = W.cartpole_rollout(steps)
+    x0, U = W.cartpole_inputs(n, steps=steps, seed=0)
+    args = [torch.from_numpy(x0).cuda(), torch.from_numpy(np.ascontiguousarray(U * 0.1)).cuda()]
+    seeds = [torch.zeros((1, 4, n), dtype=torch.float64, device="cuda"),
+             torch.ones((1, 1, n), dtype=torch.float64, device="cuda")]
+    ct = R.CudaTape(F)
+    res, asens = ct.reverse(args, seeds, stream=stream)
+
+    def ms(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    out = {"instances": n, "steps": steps, "tape_instructions": F.tape.n_instr,
+           "plain_ms": ms(lambda: ct.reverse(args, seeds, res=res, asens=asens, stream=stream)),
+           "plain_scratch_gb": ct.scratch_bytes(n) / 1e9}
+    lib = R.load()
+    for k in (5, 10, 20):
+        sc, made = ct.checkpoint_scratch(k, 1, n)
+
+        def run():
+            R.check(lib.casadi_gb300_reverse_checkpointed(
+                ct.id, n, n, 1, k, R._ptr_array(args), R._ptr_array(res), R._ptr_array(seeds),
+                R._ptr_array(asens), R.ct.c_void_p(sc.data_ptr()), sc.numel(),
+                R._stream_handle(stream)))
+
+        out["segments_%d" % made] = {"ms": ms(run), "scratch_gb": sc.numel() / 1e9}
+        del sc
+    ct.sync(stream)
+    return out
+
+
 def mpc_sparse_component(torch, stream, n=4096, intervals=100, reps=3, cpu=False):
     """Scenario MPC: the quadcopter multiple-shooting NLP (100 intervals, 1612 decision
     variables, 1212 constraints) over 4096 scenarios: the constraint Jacobian by uni-coloured
@@ -905,6 +950,7 @@ def run_native(a):
                                                       weights, cpu=cpu)
         comps["mixed_batch"] = mixed_component(torch, R, stream, cpu=cpu)
         comps["rollout100_autograd"] = rollout_autograd_component(torch, stream)
+        comps["checkpointed_adjoint"] = checkpoint_component(torch, stream)
         comps["mpc_sparse_hessian"] = mpc_sparse_component(torch, stream, cpu=cpu)
         comps["mapaccum_mapsum"] = maps_component(torch, stream)
 
