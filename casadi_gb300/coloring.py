@@ -37,6 +37,17 @@ class Pattern:
         row = np.concatenate(rows) if rows else np.zeros(0, np.int64)
         return Pattern(nrow, ncol, colind, row)
 
+    @staticmethod
+    def from_triplets(nrow, ncol, rows, cols):
+        """Pattern of the (row, col) pairs given (duplicates merged), rows sorted per column."""
+        rows = np.asarray(rows, dtype=np.int64)
+        cols = np.asarray(cols, dtype=np.int64)
+        key = np.unique(cols * max(1, int(nrow)) + rows)
+        c, r = np.divmod(key, max(1, int(nrow)))
+        colind = np.zeros(int(ncol) + 1, np.int64)
+        np.add.at(colind, c + 1, 1)
+        return Pattern(nrow, ncol, np.cumsum(colind), r)
+
     @property
     def nnz(self):
         return int(self.colind[-1])

@@ -141,7 +141,31 @@ def test_jacobian_pattern_forward_equals_reverse(gpu_lib):
         assert np.array_equal(pf.dense(), pr.dense())
         pa = jacobian_pattern(ct, out, 0)
         assert np.array_equal(pa.dense(), pf.dense())
+        ph = jacobian_pattern(ct, out, 0, mode="hierarchical")
+        assert np.array_equal(ph.dense(), pf.dense())
         ct.sync()
+
+
+def test_hierarchical_pattern_on_the_device_is_casadis(gpu_lib):
+    """The MPC constraint Jacobian (1212 x 1612, hierarchical in the reference as here) from
+    the device's refinement sweeps equals CasADi's get_jac_sparsity_hierarchical pattern, in
+    two levels of one word each."""
+    from casadi_gb300 import runtime as R
+    from casadi_gb300 import sx as S
+    from casadi_gb300.sparse_ad import jacobian_pattern_hierarchical
+    from helpers import load_npz
+    L = W.quad_ms_lagrangian(100)
+    g = S.Function("g", L.inputs, [L.outputs[0]])
+    ct = R.CudaTape(g)
+    stats = {}
+    p = jacobian_pattern_hierarchical(ct, 0, 0, stats=stats)
+    z = load_npz("casadi.npz")
+    nr, nc = z["quad/jac_jacsp_shape"]
+    assert (p.nrow, p.ncol) == (nr, nc)
+    assert np.array_equal(p.colind, z["quad/jac_jacsp_colind"])
+    assert np.array_equal(p.row, z["quad/jac_jacsp_row"])
+    assert stats == {"levels": 2, "words": 2}
+    ct.sync()
 
 
 def test_kkt_function_of_the_nlp(gpu_lib):
