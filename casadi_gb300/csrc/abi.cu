@@ -252,6 +252,9 @@ struct Mem {
   // copy streams and events of the pipelined host-buffer calls (created on first use)
   cudaStream_t s_in = nullptr, s_out = nullptr;
   cudaEvent_t ev_in[kMaxChunks] = {}, ev_done[kMaxChunks] = {}, ev_out = nullptr;
+  // per chunk: the outputs a call finishes before its last sweep (the Jacobian of a Jacobian +
+  // adjoint call) can be downloaded from here on
+  cudaEvent_t ev_early[kMaxChunks] = {};
   std::vector<void*> bufs;   // device staging buffers, grown on demand
   std::vector<size_t> caps;
   ~Mem() {
@@ -259,6 +262,7 @@ struct Mem {
     for (int k = 0; k < kMaxChunks; ++k) {
       if (ev_in[k]) cudaEventDestroy(ev_in[k]);
       if (ev_done[k]) cudaEventDestroy(ev_done[k]);
+      if (ev_early[k]) cudaEventDestroy(ev_early[k]);
     }
     if (ev_out) cudaEventDestroy(ev_out);
     if (s_in) cudaStreamDestroy(s_in);
@@ -274,7 +278,8 @@ struct Mem {
       return e;
     for (int k = 0; k < kMaxChunks; ++k)
       if ((e = cudaEventCreateWithFlags(&ev_in[k], cudaEventDisableTiming)) != cudaSuccess ||
-          (e = cudaEventCreateWithFlags(&ev_done[k], cudaEventDisableTiming)) != cudaSuccess)
+          (e = cudaEventCreateWithFlags(&ev_done[k], cudaEventDisableTiming)) != cudaSuccess ||
+          (e = cudaEventCreateWithFlags(&ev_early[k], cudaEventDisableTiming)) != cudaSuccess)
         return e;
     return cudaSuccess;
   }
@@ -2400,13 +2405,14 @@ struct HostBlock {
   const double* up;  // upload source (inputs, seeds) or null
   double* down;      // download target (outputs, sensitivities) or null
   int dir_blocks;
+  bool early;        // downloaded once the chunk's early event has passed
 };
 
 void collect_blocks(std::vector<HostBlock>& v, const IoDesc* desc, int count, const double* const* up,
-                double* const* down, int dir_blocks = 1) {
+                double* const* down, int dir_blocks = 1, bool early = false) {
   for (int j = 0; j < count; ++j)
     if (desc[j].ptr)
-      v.push_back({&desc[j], up ? up[j] : nullptr, down ? down[j] : nullptr, dir_blocks});
+      v.push_back({&desc[j], up ? up[j] : nullptr, down ? down[j] : nullptr, dir_blocks, early});
 }
 
 // Descriptors of instances [i0, ...) of instance-major staging descriptors.
@@ -2422,14 +2428,32 @@ void shift_io(const IoDesc* src, int count, long long i0, IoDesc* dst) {
 // stream s_in) and the download of chunk c-1 (s_out) overlap the sweeps of chunk c (the
 // memory object's stream). `compute(i0, count)` enqueues one chunk's sweeps on m.stream.
 template <class F>
-int run_pipelined(Mem& m, long long n, const std::vector<HostBlock>& blocks, F compute) {
+int run_pipelined(Mem& m, long long n, const std::vector<HostBlock>& blocks, F compute,
+                  int max_chunks = kMaxChunks) {
   cudaError_t e = m.pipe();
   if (e != cudaSuccess) return cuda_fail(e, "copy streams");
   // chunks of at least 131072 instances: smaller launches lose more sweep efficiency than the
-  // overlap gains (rollout, 262144 instances: 1 chunk 44.8 ms, 2 chunks 43.7, 4 chunks 45.8)
-  int chunks = static_cast<int>(std::max(1ll, std::min<long long>(kMaxChunks, n / 131072)));
+  // overlap gains (rollout Jacobian + adjoint, 262144 instances, without early downloads:
+  // 1 chunk 34.9 ms, 2 chunks 34.8, 3 chunks 37.0, 4 chunks 39.0)
+  int chunks = static_cast<int>(std::max(1ll, std::min<long long>(max_chunks, n / 131072)));
   const long long per = ((n + chunks - 1) / chunks + 31) / 32 * 32;
   chunks = static_cast<int>((n + per - 1) / per);
+  bool any_early = false;
+  for (const auto& b : blocks) any_early = any_early || (b.down && b.early);
+  auto download = [&](long long i0, long long cnt, bool early) -> cudaError_t {
+    for (const auto& b : blocks) {
+      if (!b.down || b.early != early) continue;
+      const size_t bytes = sizeof(double) * static_cast<size_t>(b.desc->inst_stride);
+      for (int d = 0; d < b.dir_blocks; ++d) {
+        const long long off = d * (b.dir_blocks > 1 ? b.desc->dir_stride : 0) +
+                              i0 * b.desc->inst_stride;
+        cudaError_t r = cudaMemcpyAsync(b.down + off, static_cast<double*>(b.desc->ptr) + off,
+                                        bytes * cnt, cudaMemcpyDeviceToHost, m.s_out);
+        if (r != cudaSuccess) return r;
+      }
+    }
+    return cudaSuccess;
+  };
   for (int c = 0; c < chunks; ++c) {
     const long long i0 = c * per, cnt = std::min(per, n - i0);
     for (const auto& b : blocks) {
@@ -2446,21 +2470,17 @@ int run_pipelined(Mem& m, long long n, const std::vector<HostBlock>& blocks, F c
     if ((e = cudaEventRecord(m.ev_in[c], m.s_in)) != cudaSuccess ||
         (e = cudaStreamWaitEvent(m.stream, m.ev_in[c], 0)) != cudaSuccess)
       return cuda_fail(e, "chunk ordering");
-    if (int rc = compute(i0, cnt)) return rc;
+    // compute records m.ev_early[c] on m.stream when the early outputs are final
+    if (int rc = compute(i0, cnt, m.ev_early[c])) return rc;
+    if (any_early) {
+      if ((e = cudaStreamWaitEvent(m.s_out, m.ev_early[c], 0)) != cudaSuccess)
+        return cuda_fail(e, "chunk ordering");
+      if ((e = download(i0, cnt, true)) != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(D2H)");
+    }
     if ((e = cudaEventRecord(m.ev_done[c], m.stream)) != cudaSuccess ||
         (e = cudaStreamWaitEvent(m.s_out, m.ev_done[c], 0)) != cudaSuccess)
       return cuda_fail(e, "chunk ordering");
-    for (const auto& b : blocks) {
-      if (!b.down) continue;
-      const size_t bytes = sizeof(double) * static_cast<size_t>(b.desc->inst_stride);
-      for (int d = 0; d < b.dir_blocks; ++d) {
-        const long long off = d * (b.dir_blocks > 1 ? b.desc->dir_stride : 0) +
-                              i0 * b.desc->inst_stride;
-        if ((e = cudaMemcpyAsync(b.down + off, static_cast<double*>(b.desc->ptr) + off,
-                                 bytes * cnt, cudaMemcpyDeviceToHost, m.s_out)) != cudaSuccess)
-          return cuda_fail(e, "cudaMemcpyAsync(D2H)");
-      }
-    }
+    if ((e = download(i0, cnt, false)) != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(D2H)");
   }
   if ((e = cudaEventRecord(m.ev_out, m.s_out)) != cudaSuccess ||
       (e = cudaStreamWaitEvent(m.stream, m.ev_out, 0)) != cudaSuccess)
@@ -2503,7 +2523,7 @@ int casadi_gb300_map_eval(int id, int mem, int64_t n, const double* const* arg,
   std::vector<HostBlock> blocks;
   collect_blocks(blocks, in, t->n_in, arg, nullptr);
   collect_blocks(blocks, out, t->n_out, nullptr, res);
-  if (int rc = run_pipelined(*m, n, blocks, [&](long long i0, long long cnt) {
+  if (int rc = run_pipelined(*m, n, blocks, [&](long long i0, long long cnt, cudaEvent_t) {
         SweepArgs a = base_args(*t, cnt, 0);
         shift_io(in, t->n_in, i0, a.in);
         shift_io(out, t->n_out, i0, a.out);
@@ -2536,7 +2556,7 @@ static int map_sp(int id, int mem, int64_t n, uint64_t* const* arg, uint64_t* co
                                                     : nullptr);
   collect_blocks(blocks, out, t->n_out, reverse ? hres : nullptr,
                  reinterpret_cast<double* const*>(res));
-  if (int rc = run_pipelined(*m, n, blocks, [&](long long i0, long long cnt) {
+  if (int rc = run_pipelined(*m, n, blocks, [&](long long i0, long long cnt, cudaEvent_t) {
         SweepArgs a = base_args(*t, cnt, 0);
         shift_io(in, t->n_in, i0, a.in);
         shift_io(out, t->n_out, i0, a.out);
@@ -2586,7 +2606,7 @@ int casadi_gb300_map_jacobian(int id, int mem, int64_t n, const double* const* a
   collect_blocks(blocks, in, t->n_in, arg, nullptr);
   collect_blocks(blocks, out, t->n_out, nullptr, res);
   collect_blocks(blocks, sens, t->n_out, nullptr, jac);
-  if (int rc = run_pipelined(*m, n, blocks, [&](long long i0, long long cnt) {
+  if (int rc = run_pipelined(*m, n, blocks, [&](long long i0, long long cnt, cudaEvent_t) {
         IoDesc in_c[kMaxIo], out_c[kMaxIo], sens_c[kMaxIo];
         shift_io(in, t->n_in, i0, in_c);
         shift_io(out, t->n_out, i0, out_c);
@@ -2628,7 +2648,7 @@ static int map_forward_impl(int id, int mem, int64_t n, int nfwd, const double* 
   collect_blocks(blocks, seed, t->n_in, fseed, nullptr, outer ? nfwd : 1);
   collect_blocks(blocks, out, t->n_out, nullptr, res);
   collect_blocks(blocks, sens, t->n_out, nullptr, fsens, outer ? nfwd : 1);
-  if (int rc = run_pipelined(*m, n, blocks, [&](long long i0, long long cnt) {
+  if (int rc = run_pipelined(*m, n, blocks, [&](long long i0, long long cnt, cudaEvent_t) {
         IoDesc in_c[kMaxIo], out_c[kMaxIo], seed_c[kMaxIo], sens_c[kMaxIo];
         shift_io(in, t->n_in, i0, in_c);
         shift_io(out, t->n_out, i0, out_c);
@@ -2672,7 +2692,7 @@ static int map_reverse_impl(int id, int mem, int64_t n, int nadj, const double* 
   collect_blocks(blocks, seed, t->n_out, aseed, nullptr, outer ? nadj : 1);
   collect_blocks(blocks, out, t->n_out, nullptr, res);
   collect_blocks(blocks, sens, t->n_in, nullptr, asens, outer ? nadj : 1);
-  if (int rc = run_pipelined(*m, n, blocks, [&](long long i0, long long cnt) {
+  if (int rc = run_pipelined(*m, n, blocks, [&](long long i0, long long cnt, cudaEvent_t) {
         IoDesc in_c[kMaxIo], out_c[kMaxIo], seed_c[kMaxIo], sens_c[kMaxIo];
         shift_io(in, t->n_in, i0, in_c);
         shift_io(out, t->n_out, i0, out_c);
@@ -2745,9 +2765,13 @@ int casadi_gb300_map_jacobian_reverse(int id, int mem, int64_t n, const double* 
   collect_blocks(blocks, in, t->n_in, arg, nullptr);
   collect_blocks(blocks, aseedd, t->n_out, aseed, nullptr);
   collect_blocks(blocks, out, t->n_out, nullptr, res);
-  collect_blocks(blocks, fsens, t->n_out, nullptr, jac);
+  // the Jacobian is final after the tangent sweep: its download overlaps the adjoint sweep
+  collect_blocks(blocks, fsens, t->n_out, nullptr, jac, 1, true);
   collect_blocks(blocks, asensd, t->n_in, nullptr, asens);
-  if (int rc = run_pipelined(*m, n, blocks, [&](long long i0, long long cnt) {
+  // one chunk when the partials of all instances fit one wave: the Jacobian's download then
+  // hides behind the adjoint sweep, and full-size sweeps run faster than two half-size ones
+  const int max_chunks = wave_capacity(*t, n, bytes) >= n ? 1 : kMaxChunks;
+  if (int rc = run_pipelined(*m, n, blocks, [&](long long i0, long long cnt, cudaEvent_t early) {
         IoDesc in_c[kMaxIo], out_c[kMaxIo], fsens_c[kMaxIo], aseed_c[kMaxIo], asens_c[kMaxIo];
         shift_io(in, t->n_in, i0, in_c);
         shift_io(out, t->n_out, i0, out_c);
@@ -2763,8 +2787,18 @@ int casadi_gb300_map_jacobian_reverse(int id, int mem, int64_t n, const double* 
         rq[1].adjoint = true;
         rq[1].seed = aseed_c;
         rq[1].sens = asens_c;
-        return run_ad_multi(*t, cnt, in_c, out_c, rq, 2, scratch, bytes, s);
-      }))
+        // record + tangent, the early event, then the adjoint on the recorded partials (one
+        // wave); with waves both requests run wave by wave and the event follows them
+        if (wave_capacity(*t, cnt, bytes) < cnt) {
+          if (int rc = run_ad_multi(*t, cnt, in_c, out_c, rq, 2, scratch, bytes, s)) return rc;
+          cudaError_t e = cudaEventRecord(early, s);
+          return e == cudaSuccess ? 0 : cuda_fail(e, "early event");
+        }
+        if (int rc = run_ad_multi(*t, cnt, in_c, out_c, rq, 1, scratch, bytes, s)) return rc;
+        cudaError_t e = cudaEventRecord(early, s);
+        if (e != cudaSuccess) return cuda_fail(e, "early event");
+        return run_ad_multi(*t, cnt, in_c, out_c, rq + 1, 1, scratch, bytes, s, true);
+      }, max_chunks))
     return rc;
   return casadi_gb300_sync(id, s);
 }

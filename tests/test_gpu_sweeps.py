@@ -473,11 +473,12 @@ def test_autotuner_keeps_a_variant_and_results(gpu_lib):
     ct.sync()
 
 
-def test_jacobian_reverse_equals_the_two_calls(gpu_lib):
+@pytest.mark.parametrize("n", [3001, 2 * 131072 + 77])
+def test_jacobian_reverse_equals_the_two_calls(gpu_lib, n):
     """One record sweep feeding both derivative sweeps gives the same bits as calling
-    jacobian and reverse one after the other, on device buffers and on host buffers."""
+    jacobian and reverse one after the other, on device buffers and on host buffers (where
+    the Jacobian's download overlaps the adjoint sweep)."""
     F = W.cartpole_rollout(5)
-    n = 3001
     args_h = W.cartpole_inputs(n, steps=5, seed=31)
     rng = np.random.default_rng(31)
     aseeds_h = [rng.standard_normal((2, k, n)) for k in F.tape.nnz_out]
