@@ -40,7 +40,7 @@ def make_workload(name, instances=None):
         n = instances or 262144
         args = W.cartpole_inputs(n, steps=20, seed=0)
         desc = "cart-pole 20-step RK4 rollout F(x0[4],U[20])->(xN[4],cost), N=%d: " \
-               "forward Jacobian (24 unit directions) + adjoint of cost" % n
+               "forward Jacobian of xN (24 unit directions) + adjoint of cost" % n
         return F, n, args, [np.zeros((1, 4, n)), np.ones((1, 1, n))], desc
     if name == "cartpole":
         F = W.cartpole_step()
@@ -75,17 +75,47 @@ def _mix():
     return {"dadd": 0, "dmul": 0, "dfma": 0}
 
 
-def structural_tangent_ops(tape, unit_dirs=True, ndir=None):
+def _needed(tape, wanted_out):
+    """Per instruction: does its result reach an output in ``wanted_out`` (None: all)? The
+    tangent plans prune the others (one backward pass over the slots read later)."""
+    from casadi_gb300 import calculus as C
+    ops, i0, i1, i2 = (tape.op.tolist(), tape.i0.tolist(), tape.i1.tolist(), tape.i2.tolist())
+    if wanted_out is None or all(wanted_out):
+        return [True] * len(ops)
+    need = [False] * len(ops)
+    live = [False] * max(1, tape.sz_w)
+    for k in range(len(ops) - 1, -1, -1):
+        op = ops[k]
+        if op == C.OP_OUTPUT:
+            need[k] = bool(wanted_out[i0[k]])
+            if need[k]:
+                live[i1[k]] = True
+            continue
+        if not live[i0[k]]:
+            continue
+        need[k] = True
+        live[i0[k]] = False
+        if op in (C.OP_CONST, C.OP_INPUT):
+            continue
+        live[i1[k]] = True
+        if op in C.BINARY_OPS:
+            live[i2[k]] = True
+    return need
+
+
+def structural_tangent_ops(tape, unit_dirs=True, ndir=None, wanted_out=None):
     """FP64 instructions of the forward sweep with unit seeds, summed over all directions and
     split by kind, following the structural rules the sweeps apply (the tangent kernel's
     cases): ADD/SUB of two carried operands one DADD; a general op one DMUL per carried
     operand, two carried: DMUL + DFMA; TWICE, NEG, ASSIGN, IF_ELSE_ZERO none (integer
-    exponent/sign operations, selections)."""
+    exponent/sign operations, selections). Instructions that reach no output of
+    ``wanted_out`` (the outputs whose sensitivities are requested) count nothing."""
     from casadi_gb300 import calculus as C
     nz = sum(tape.nnz_in)
     offs = np.cumsum([0] + list(tape.nnz_in))
     ops, i0, i1, i2 = (tape.op.tolist(), tape.i0.tolist(), tape.i1.tolist(), tape.i2.tolist())
     carry = {op: _carries(op) for op in set(ops)}
+    need = _needed(tape, wanted_out)
     mix = _mix()
     for d in range(nz if unit_dirs else 1):
         act = [False] * max(1, tape.sz_w)
@@ -102,7 +132,7 @@ def structural_tangent_ops(tape, unit_dirs=True, ndir=None):
             cb = act[i1[k]] and c0
             cc = op in C.BINARY_OPS and act[i2[k]] and c1
             act[i0[k]] = cb or cc
-            if not (cb or cc):
+            if not (cb or cc) or not need[k]:
                 continue
             if op in (C.OP_ADD, C.OP_SUB):
                 mix["dadd"] += 1 if (cb and cc) else 0
@@ -153,7 +183,7 @@ def structural_adjoint_ops(tape, seeded_out):
 SIMPLE_OPS = ("ADD", "SUB", "MUL", "SQ", "IF_ELSE_ZERO", "LT", "LE", "EQ", "NE", "FMIN", "FMAX")
 
 
-def algorithmic_flops(tape, weights, rates, seeded_out=None, unit_dirs=True):
+def algorithmic_flops(tape, weights, rates, seeded_out=None, unit_dirs=True, wanted_out=None):
     """Per instance and kernel family: FP64-pipe instructions ("instr") and their time at the
     measured rates expressed in DFMA-chain instructions ("dfma_time"); the family's ceiling
     is rate_dfma * instr / dfma_time. Value and record sweeps: simple ops (one DADD or DMUL
@@ -175,7 +205,7 @@ def algorithmic_flops(tape, weights, rates, seeded_out=None, unit_dirs=True):
         out["record"]["instr"] += cnt * (w + wp)
         out["record"]["dfma_time"] += cnt * (t + wp)
     seeded_out = seeded_out or [True] * len(tape.nnz_out)
-    for fam, mix in (("tangent", structural_tangent_ops(tape, unit_dirs)),
+    for fam, mix in (("tangent", structural_tangent_ops(tape, unit_dirs, wanted_out=wanted_out)),
                      ("adjoint", structural_adjoint_ops(tape, seeded_out))):
         out[fam] = {"instr": float(sum(mix.values())), "mix": mix,
                     "dfma_time": mix["dfma"] + (mix["dadd"] + mix["dmul"]) * slow}
@@ -280,21 +310,22 @@ _CASADI_TAPES = {}
 
 
 def casadi_rollout_tapes():
-    """CasADi's own derivative Functions of the 20-step rollout: the jacobian() tape as the
-    reference built it (tests/golden/casadi_rollout20_jacobian.npz, pinned by its SHA-256) and
-    reverse(1), which sx.reverse_function rebuilds instruction for instruction."""
+    """CasADi's own derivative Functions for the 20-step rollout's step: the jacobian() tape
+    of xN (the rollout with xN as its only output, as the reference built it:
+    tests/golden/casadi_rollout20_jacobian.npz, pinned by its SHA-256) and F.reverse(1),
+    which sx.reverse_function rebuilds instruction for instruction."""
     if not _CASADI_TAPES:
         from casadi_gb300 import calculus as C
         from casadi_gb300 import sx as S
         from casadi_gb300 import workloads as W
         z = np.load(os.path.join(ROOT, "tests", "golden", "casadi_rollout20_jacobian.npz"))
-        op = z["jacobian/op"]
+        key = "jacobian_xn"
+        op = z[key + "/op"]
         c = op == C.OP_CONST
         _CASADI_TAPES["jacobian"] = S.Tape(
-            op, z["jacobian/i0"], np.where(c, 0, z["jacobian/i1"]),
-            np.where(c, 0, z["jacobian/i2"]), np.where(c, z["jacobian/d"], 0.0),
-            z["jacobian/nnz_in"].tolist(), z["jacobian/nnz_out"].tolist(),
-            int(z["jacobian/sz_w"]))
+            op, z[key + "/i0"], np.where(c, 0, z[key + "/i1"]),
+            np.where(c, 0, z[key + "/i2"]), np.where(c, z[key + "/d"], 0.0),
+            z[key + "/nnz_in"].tolist(), z[key + "/nnz_out"].tolist(), int(z[key + "/sz_w"]))
         _CASADI_TAPES["reverse"] = S.reverse_function(W.cartpole_rollout(20)).tape
     return _CASADI_TAPES["jacobian"], _CASADI_TAPES["reverse"]
 
@@ -313,12 +344,12 @@ def casadi_calibration():
 def cpu_step(tape, args, aseeds, n, threads, workload):
     import oracle as O
     if workload == "rollout20":
-        # the reference's algorithm: CasADi's F.jacobian() and F.reverse(1) are SXFunctions
+        # the reference's algorithm: CasADi's Jacobian of xN and F.reverse(1) are SXFunctions
         # of their own (symbolic derivative tapes) that its VM evaluates; here those very
         # tapes run on the oracle's restatement of SXFunction::eval
         jt, bt = casadi_rollout_tapes()
         t0 = time.perf_counter()
-        O.eval(jt, list(args) + [None, None], n, threads)
+        O.eval(jt, list(args) + [None] * (len(jt.nnz_in) - 2), n, threads)
         O.eval(bt, list(args) + [None, None] + [s[0] for s in aseeds], n, threads)
         return time.perf_counter() - t0
     t0 = time.perf_counter()
@@ -345,9 +376,9 @@ def cpu_baseline(F, args, aseeds, workload, budget_s=12.0):
            "sample": "%d of the instances, same step (oracle C restatement, OpenMP, %d threads)"
                      % (m2, threads)}
     if workload == "rollout20":
-        out["sample"] = ("%d of the instances per step: CasADi's own jacobian() and reverse(1) "
-                         "tapes on the oracle's restatement of SXFunction::eval (OpenMP, %d "
-                         "threads)" % (m2, threads))
+        out["sample"] = ("%d of the instances per step: CasADi's own jacobian() of xN and "
+                         "reverse(1) tapes on the oracle's restatement of SXFunction::eval "
+                         "(OpenMP, %d threads)" % (m2, threads))
         cal = casadi_calibration().get("rollout", {})
         if cal.get("casadi_over_restated"):
             out["casadi_compiled_over_restatement_devhost"] = cal["casadi_over_restated"]
@@ -369,7 +400,8 @@ def headline_parity(F, args_h, aseeds_h, res, jac, asens, m=1024, threads=None):
         _, jm, am = O.jacobian_reverse(F.tape, sub, seeds, m, threads)
     worst, same, total = 0.0, 0, 0
     for got, want, mag in ([(x[..., :m].cpu().numpy(), y, np.abs(y)) for x, y in zip(res, r)] +
-                           [(x[..., :m].cpu().numpy(), y, z) for x, y, z in zip(jac, j, jm)] +
+                           [(x[..., :m].cpu().numpy(), y, z) for x, y, z in zip(jac, j, jm)
+                            if x is not None] +
                            [(x[..., :m].cpu().numpy(), y, z) for x, y, z in zip(asens, a, am)]):
         d = np.abs(got - want)
         worst = max(worst, float(np.max(np.where(d == 0, 0.0, d / np.maximum(mag, 1e-300)),
@@ -838,7 +870,9 @@ def run_native(a):
     stream = torch.cuda.current_stream()
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     res = [torch.empty((k, n), dtype=torch.float64, device="cuda") for k in F.tape.nnz_out]
-    jac = [torch.empty((nz, k, n), dtype=torch.float64, device="cuda") for k in F.tape.nnz_out] \
+    # the step's Jacobian is of xN (output 0); the cost's row comes from its adjoint, and the
+    # tangent plan prunes the instructions that only the cost needs
+    jac = [torch.empty((nz, F.tape.nnz_out[0], n), dtype=torch.float64, device="cuda"), None] \
         if a.workload == "rollout20" else None
     asens = [torch.empty((1, k, n), dtype=torch.float64, device="cuda") for k in F.tape.nnz_in]
     ct.scratch(n)
@@ -855,7 +889,7 @@ def run_native(a):
 
     def step():
         if a.workload == "rollout20":
-            # one record sweep feeds the Jacobian (24 unit directions) and the cost adjoint
+            # one record sweep feeds the Jacobian of xN (24 unit directions) and the cost adjoint
             ct.jacobian_reverse(dargs, daseeds, res=res, jac=jac, asens=asens, stream=stream)
         elif a.workload == "dag":
             # eval + adjoint of the sum of outputs, then both sparsity sweeps
@@ -916,8 +950,12 @@ def run_native(a):
     comps["adjoint_evals_per_s"] = rate(
         lambda: ct.reverse(dargs, daseeds, res=res, asens=asens, stream=stream))
     if a.workload == "rollout20":
+        # the Jacobian of every output (xN and the cost) alone
+        jac_all = [torch.empty((nz, k, n), dtype=torch.float64, device="cuda")
+                   for k in F.tape.nnz_out]
         comps["jacobian24_evals_per_s"] = rate(
-            lambda: ct.jacobian(dargs, res=res, jac=jac, stream=stream))
+            lambda: ct.jacobian(dargs, res=res, jac=jac_all, stream=stream))
+        del jac_all
     # derivative-sweep variants the autotuner kept (tangent 8: the windowed sweep)
     comps["tuned_variants"] = {"jacobian": ct.tuned_variant(1), "adjoint": ct.tuned_variant(2)}
     if a.workload == "rollout20":
@@ -930,7 +968,7 @@ def run_native(a):
         bargs = dargs + [None, None] + [x[0] for x in daseeds]
 
         def derivative_functions():
-            cj.eval(dargs + [None, None], res=jres, stream=stream)
+            cj.eval(dargs + [None] * (len(jt.nnz_in) - 2), res=jres, stream=stream)
             cb.eval(bargs, res=bres, stream=stream)
 
         comps["casadi_derivative_functions_evals_per_s"] = rate(derivative_functions)
@@ -956,7 +994,8 @@ def run_native(a):
 
     # roofline of the dominant kernel family (device time from the per-launch events)
     work = algorithmic_flops(F.tape, weights, rates,
-                             seeded_out=[bool(np.any(x)) for x in aseeds_h])
+                             seeded_out=[bool(np.any(x)) for x in aseeds_h],
+                             wanted_out=[True, False] if a.workload == "rollout20" else None)
     fam_ms = {k: v for k, v in prof.items() if v[1] > 0}
     dom = max(fam_ms, key=lambda k: fam_ms[k][0])
     dom_ms, dom_launches = fam_ms[dom]
@@ -1006,7 +1045,7 @@ def run_native(a):
         for h, x in zip(hseed, aseeds_h):
             h[:] = np.transpose(x, (2, 0, 1))
         hasens = [pinned((n, 1, k)) for k in F.tape.nnz_in]
-        hjac = [pinned((n, nz, k)) for k in F.tape.nnz_out] if a.workload == "rollout20" else None
+        hjac = [pinned((n, nz, F.tape.nnz_out[0])), None] if a.workload == "rollout20" else None
 
         def e2e_step():
             if a.workload == "rollout20":
@@ -1026,7 +1065,7 @@ def run_native(a):
         out_b = 8 * n * sum(F.tape.nnz_out)
         if a.workload == "rollout20":
             h2d = in_b + 8 * n * sum(F.tape.nnz_out)
-            d2h = out_b + 8 * n * nz * sum(F.tape.nnz_out) + in_b
+            d2h = out_b + 8 * n * nz * F.tape.nnz_out[0] + in_b
         elif a.workload == "dag":
             h2d = in_b + 8 * n * sum(F.tape.nnz_out)
             d2h = out_b + in_b
@@ -1080,7 +1119,7 @@ def run_native(a):
 
 # ---- reference arm (the reference's algorithm restated, on the host cores) ------------------------
 def ref_algo(workload):
-    return {"rollout20": "CasADi's own jacobian() and reverse(1) tapes on the oracle's "
+    return {"rollout20": "CasADi's own jacobian() of xN and reverse(1) tapes on the oracle's "
                          "restatement of SXFunction::eval",
             "cartpole": "the tape on the oracle's restatement of SXFunction::eval",
             "dag": "the oracle's numeric adjoint and bvec sweeps"}.get(workload, "oracle")

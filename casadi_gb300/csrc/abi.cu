@@ -89,6 +89,7 @@ struct TanPlan {
   std::vector<int> dirmap;   // identity mode: direction seeded by each flat input nonzero
                              // (empty: nonzero k seeds direction k; -1: not seeded)
   std::vector<char> seeded;  // per input: seed pointer given (general seeds)
+  std::vector<char> wanted;  // per output: sensitivities requested (others are pruned)
   int groups = 0;
   uint4* d_stream = nullptr;  // entry streams of all directions
   int2* d_chunks = nullptr;   // per direction: (first entry, entry count)
@@ -109,6 +110,7 @@ struct WinPlan {
   bool identity = false;
   std::vector<int> dirmap;
   std::vector<char> seeded;
+  std::vector<char> wanted;
   bool usable = false;  // false: the sweep does not fit (or has too few directions to pay)
   int dirs = 0, groups = 0, stages = 0, rows = 0, ents = 0, nwin = 0;
   uint4* d_blocks = nullptr;
@@ -589,12 +591,40 @@ std::vector<int> partial_starts(const Tape& t) {
 // seeded (unit seeds: when it is the direction's own input nonzero), an arithmetic result
 // when an operand that carries a derivative is active (the reference's 0*x -> 0, x+0 -> x).
 // Returns, per group of dw directions and instruction, 2 bits per direction (operand b / c
-// carries a derivative; an input or output: bit 0 when active).
+// carries a derivative; an input or output: bit 0 when active). Instructions whose result
+// reaches no output in `wanted` (outputs whose sensitivities were requested; empty: all) get
+// no bits: their tangents would feed nothing that is written. Activity itself is propagated
+// over every instruction, so the entries kept are the same as without pruning.
 std::vector<unsigned short> tan_activity(const Tape& t, int ndir, int dw, bool identity,
                                          const std::vector<char>& seeded,
-                                         const std::vector<int>& dirmap) {
+                                         const std::vector<int>& dirmap,
+                                         const std::vector<char>& wanted) {
   const int groups = (ndir + dw - 1) / dw;
   const size_t nc = t.h_code.size();
+  // instructions a wanted output depends on: a backward pass over the slots read later
+  std::vector<char> need(nc, 1);
+  bool all = true;
+  for (char c : wanted) all = all && c;
+  if (!all) {
+    std::vector<char> live(std::max(1, t.sz_w), 0);
+    for (size_t kk = nc; kk-- > 0;) {
+      const u64 w = t.h_code[kk];
+      const unsigned op = dec_op(w), A = dec_a(w), B = dec_b(w), C = dec_c(w);
+      need[kk] = 0;
+      if (op == D_NOP) continue;
+      if (op == D_OUTPUT) {
+        need[kk] = wanted[A];
+        if (wanted[A]) live[B] = 1;
+        continue;
+      }
+      if (!live[A]) continue;
+      need[kk] = 1;
+      live[A] = 0;
+      if (op == D_CONST || op == D_INPUT) continue;
+      live[B] = 1;
+      if (is_binary(op)) live[C] = 1;
+    }
+  }
   std::vector<int> off(t.n_in + 1, 0);
   for (int j = 0; j < t.n_in; ++j) off[j + 1] = off[j] + t.nnz_in[j];
   std::vector<unsigned short> bits(static_cast<size_t>(groups) * nc, 0);
@@ -625,7 +655,7 @@ std::vector<unsigned short> tan_activity(const Tape& t, int ndir, int dw, bool i
         act[A] = cb || cc;
         b = (cb ? 1u : 0u) | (cc ? 2u : 0u);
       }
-      if (!b) continue;
+      if (!b || !need[k]) continue;
       for (int dd = identity ? d : 0; dd < (identity ? d + 1 : ndir); ++dd)
         bits[static_cast<size_t>(dd / dw) * nc + k] |=
             static_cast<unsigned short>(b << (2 * (dd % dw)));
@@ -637,11 +667,11 @@ std::vector<unsigned short> tan_activity(const Tape& t, int ndir, int dw, bool i
 // Each direction group gets a compacted entry stream of the instructions with work for it.
 const TanPlan* tan_plan(Tape& t, int ndir, int dw, int ch, bool identity,
                         const std::vector<char>& seeded, const std::vector<int>& dirmap,
-                        int* err) {
+                        const std::vector<char>& wanted, int* err) {
   std::lock_guard<std::mutex> lk(t.shape_mtx);
   for (auto& p : t.tan_plans)
     if (p->ndir == ndir && p->dw == dw && p->ch == ch && p->identity == identity &&
-        (identity ? p->dirmap == dirmap : p->seeded == seeded))
+        (identity ? p->dirmap == dirmap : p->seeded == seeded) && p->wanted == wanted)
       return p.get();
   auto p = std::make_unique<TanPlan>();
   p->ndir = ndir;
@@ -650,9 +680,11 @@ const TanPlan* tan_plan(Tape& t, int ndir, int dw, int ch, bool identity,
   p->identity = identity;
   p->dirmap = dirmap;
   p->seeded = seeded;
+  p->wanted = wanted;
   p->groups = (ndir + dw - 1) / dw;
   const size_t nc = t.h_code.size();
-  const std::vector<unsigned short> bits = tan_activity(t, ndir, dw, identity, seeded, dirmap);
+  const std::vector<unsigned short> bits =
+      tan_activity(t, ndir, dw, identity, seeded, dirmap, wanted);
   // one stream per group of dw directions (the union of their work); an entry whose flags
   // differ between the group's directions becomes LK_MIXED with the real kind in x bits
   // 19-22 and the flags of direction k in bits 24+2k (see the tangent kernel)
@@ -714,17 +746,19 @@ const TanPlan* tan_plan(Tape& t, int ndir, int dw, int ch, bool identity,
 // than 4 directions, or a work vector too long for 4 of them, give an unusable plan.
 constexpr int kWinMinDirs = 4;
 const WinPlan* win_plan(Tape& t, int ndir, bool identity, const std::vector<char>& seeded,
-                        const std::vector<int>& dirmap, int* err) {
+                        const std::vector<int>& dirmap, const std::vector<char>& wanted,
+                        int* err) {
   std::lock_guard<std::mutex> lk(t.shape_mtx);
   for (auto& p : t.win_plans)
     if (p->ndir == ndir && p->identity == identity &&
-        (identity ? p->dirmap == dirmap : p->seeded == seeded))
+        (identity ? p->dirmap == dirmap : p->seeded == seeded) && p->wanted == wanted)
       return p.get();
   auto p = std::make_unique<WinPlan>();
   p->ndir = ndir;
   p->identity = identity;
   p->dirmap = dirmap;
   p->seeded = seeded;
+  p->wanted = wanted;
   const long long wv = static_cast<long long>(std::max(1, t.sz_w)) * 256;
   const long long budget = static_cast<long long>(max_smem_optin()) - 1024 - kWinBarBytes;
   constexpr long long kMinStage = 16 * 256 + 256 * 16;
@@ -742,7 +776,8 @@ const WinPlan* win_plan(Tape& t, int ndir, bool identity, const std::vector<char
 
   const size_t nc = t.h_code.size();
   const std::vector<int> pk = partial_starts(t);
-  const std::vector<unsigned short> bits = tan_activity(t, ndir, 1, identity, seeded, dirmap);
+  const std::vector<unsigned short> bits =
+      tan_activity(t, ndir, 1, identity, seeded, dirmap, wanted);
   // entries of every stream (identity: one per direction; general seeds: one for all), with
   // the instruction each belongs to, operand forwarding marked over the whole stream
   const int nstreams = identity ? ndir : 1;
@@ -1151,6 +1186,10 @@ int run_deriv(Tape& t, SweepArgs a, long long m, const DerivReq& rq, cudaStream_
   const AdjPlan* ap = nullptr;
   std::vector<char> seeded_in(t.n_in);
   for (int j = 0; j < t.n_in; ++j) seeded_in[j] = rq.seed && rq.seed[j].ptr != nullptr;
+  // tangents: outputs whose sensitivities are requested (the others' instructions are pruned)
+  std::vector<char> wanted_out(adjoint ? 0 : t.n_out);
+  for (int j = 0; j < static_cast<int>(wanted_out.size()); ++j)
+    wanted_out[j] = rq.sens && rq.sens[j].ptr != nullptr;
   if (adjoint) {
     std::vector<char> seeded(t.n_out);
     for (int j = 0; j < t.n_out; ++j) seeded[j] = rq.seed[j].ptr != nullptr;
@@ -1206,7 +1245,8 @@ int run_deriv(Tape& t, SweepArgs a, long long m, const DerivReq& rq, cudaStream_
     tan_variant_shape(v, &ipt, &kd);
     static const std::vector<int> kNoMap;
     const TanPlan* tp =
-        tan_plan(t, ndir, kd, 0, identity, seeded_in, rq.dirmap ? *rq.dirmap : kNoMap, &plan_err);
+        tan_plan(t, ndir, kd, 0, identity, seeded_in, rq.dirmap ? *rq.dirmap : kNoMap,
+                 wanted_out, &plan_err);
     if (!tp) return cudaErrorInvalidValue;
     a.dstream = tp->d_stream;
     a.dchunks = tp->d_chunks;
@@ -1238,7 +1278,8 @@ int run_deriv(Tape& t, SweepArgs a, long long m, const DerivReq& rq, cudaStream_
   auto launch_coop_tan = [&]() -> cudaError_t {
     static const std::vector<int> kNoMap;
     const TanPlan* tp =
-        tan_plan(t, ndir, 1, 0, identity, seeded_in, rq.dirmap ? *rq.dirmap : kNoMap, &plan_err);
+        tan_plan(t, ndir, 1, 0, identity, seeded_in, rq.dirmap ? *rq.dirmap : kNoMap,
+                 wanted_out, &plan_err);
     if (!tp) return cudaErrorInvalidValue;
     SweepArgs c = a;
     c.t = t.view();
@@ -1262,7 +1303,7 @@ int run_deriv(Tape& t, SweepArgs a, long long m, const DerivReq& rq, cudaStream_
       if (adjoint) return launch_adjoint(a, grid, 0, s);
       static const std::vector<int> kNoMap;
       const TanPlan* tp = tan_plan(t, ndir, 1, 0, identity, seeded_in,
-                                   rq.dirmap ? *rq.dirmap : kNoMap, &plan_err);
+                                   rq.dirmap ? *rq.dirmap : kNoMap, wanted_out, &plan_err);
       if (!tp) return cudaErrorInvalidValue;
       a.dstream = tp->d_stream;
       a.dchunks = tp->d_chunks;
@@ -1280,7 +1321,8 @@ int run_deriv(Tape& t, SweepArgs a, long long m, const DerivReq& rq, cudaStream_
   auto win = [&]() -> const WinPlan* {
     static const std::vector<int> kNoMap;
     if (!wp && !plan_err)
-      wp = win_plan(t, ndir, identity, seeded_in, rq.dirmap ? *rq.dirmap : kNoMap, &plan_err);
+      wp = win_plan(t, ndir, identity, seeded_in, rq.dirmap ? *rq.dirmap : kNoMap, wanted_out,
+                    &plan_err);
     return wp;
   };
   auto launch_win = [&]() -> cudaError_t {

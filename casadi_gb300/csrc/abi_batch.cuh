@@ -116,7 +116,7 @@ int batch_prepare(BatchHost& b) {
         return fail(CASADI_GB300_ERR_UNSUPPORTED, "batch item %zu records too many partials", k);
       int err = 0;
       const TanPlan* tp = tan_plan(*t, it.ndir, 1, 0, true, std::vector<char>(t->n_in, 0),
-                                   it.dirmap, &err);
+                                   it.dirmap, std::vector<char>(t->n_out, 1), &err);
       if (!tp) return err;
       bi.tan_stream = tp->d_stream;
       bi.tan_chunks = tp->d_chunks;

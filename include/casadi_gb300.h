@@ -189,6 +189,9 @@ CASADI_GB300_API int casadi_gb300_eval(int id, int64_t n, int64_t ld, const doub
 /* Forward-mode AD: values plus nfwd directional derivatives.
  * fseed[j]: nfwd x nnz_in[j] x ld, fsens[j]: nfwd x nnz_out[j] x ld (direction-major).
  * res may be all-null. scratch: device buffer of scratch_bytes (casadi_gb300_scratch_size).
+ * A null fsens[j] leaves output j's sensitivities out, and the tangent sweep skips every
+ * instruction that reaches no requested output (the same holds for the Jacobian entry
+ * points' jac[j]); the requested ones are unchanged bit for bit.
  * Replaces evaluating Function::forward(nfwd) (function_internal.cpp:2220-2283, built by
  * SXFunction::ad_forward, sx_function.cpp:1194-1366) under a Map. */
 CASADI_GB300_API int casadi_gb300_forward(int id, int64_t n, int64_t ld, int nfwd, const double* const* arg,

@@ -144,6 +144,19 @@ Function build_rollout(int steps) {
   return Function("F", {x0, U}, {SX(x), SX(cost)});
 }
 
+// The rollout's final state alone, F(x0, U) -> xN (the same operations as build_rollout
+// without the cost): its jacobian() is CasADi's own Jacobian of xN.
+Function build_rollout_xn(int steps) {
+  SX x0 = SX::sym("x0", 4), U = SX::sym("U", steps);
+  std::vector<SXElem> x = elems(x0), u = elems(U);
+  for (int k = 0; k < steps; ++k) {
+    SXElem uk = u[k];
+    x = rk4_step(x, [&](const std::vector<SXElem>& s) { return cartpole_ode(s, uk); },
+                 Cartpole().dt);
+  }
+  return Function("FxN", {x0, U}, {SX(x)});
+}
+
 // The rollout as never-inlined calls of the step Function: one OP_CALL per step
 // (Function::call(..., never_inline=true), sx_function.cpp:630-661 for the tape records).
 Function build_rollout_calls(int steps) {
@@ -282,6 +295,7 @@ int cb_build(const char* name, int param) {
   if (n == "quad_grad_helper")
     return put(Function("jac_helper", {q.w}, {gradient(q.lag, q.w)}, free));
   if (n == "rollout_calls") return put(build_rollout_calls(param));
+  if (n == "rollout_xn") return put(build_rollout_xn(param));
   g_err = "unknown workload " + n;
   return -2;
   CB_CATCH

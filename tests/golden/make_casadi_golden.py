@@ -247,6 +247,19 @@ def main():
                "jacobian/d": d})
     for k in range(J.n_out):
         put_pattern(jt, "jacobian/out%d" % k, J.sparsity_out(k))
+    # CasADi's own Jacobian of xN alone (the rollout with xN as its only output): the CPU legs
+    # of the benchmark's step (forward Jacobian of xN + adjoint of the cost) run this tape;
+    # its values on the rollout's golden inputs pin it
+    Jx = R.build("rollout_xn", 20).jacobian()
+    put_tape(jt, "jacobian_xn", Jx)
+    op, i0, i1, i2, d = Jx.tape()
+    jt.update({"jacobian_xn/op": op, "jacobian_xn/i0": i0, "jacobian_xn/i1": i1,
+               "jacobian_xn/i2": i2, "jacobian_xn/d": d})
+    for k in range(Jx.n_out):
+        put_pattern(jt, "jacobian_xn/out%d" % k, Jx.sparsity_out(k))
+    ra = W.cartpole_inputs(32, steps=20, seed=22)  # the "rollout" case's inputs
+    for k, r in enumerate(Jx.eval(list(ra) + [None], ra[0].shape[1])):
+        jt["jacobian_xn/res%d" % k] = r
     jpath = os.path.join(HERE, "casadi_rollout20_jacobian.npz")
     np.savez_compressed(jpath, **jt)
     print("casadi_rollout20_jacobian.npz", os.path.getsize(jpath), "bytes")

@@ -27,8 +27,8 @@ from casadi_gb300 import sx as S
 from casadi_gb300 import workloads as W
 from oracle import casadi_ref as CR
 
-from helpers import (EXACT_OPS, assert_bitexact, casadi_tape, golden_list, load_npz, rel_err,
-                     same_bits, tape_sha256)
+from helpers import (EXACT_OPS, assert_bitexact, casadi_tape, golden_list, load_npz,
+                     rel_err, same_bits, tape_sha256)
 
 AD_RTOL = 1e-13
 EXACT_MAP = np.array([0, 1, 3, 3, 8, 3, 8, 1, 8, 0], np.int32)
@@ -361,6 +361,26 @@ def test_live_random_dags(seed, n_in, n_nodes, n_out, bounded):
 def _jacobian_tape():
     j = load_npz("casadi_rollout20_jacobian.npz")
     return casadi_tape(j, "jacobian"), j
+
+
+def test_casadi_jacobian_of_xn_fixture_gives_casadis_values(z):
+    """CasADi's Jacobian of the rollout's xN alone (the benchmark's CPU legs run it for the
+    step's forward Jacobian of xN): the stored tape is pinned by its SHA-256, and the oracle's
+    restatement of SXFunction::eval gives CasADi's values of it bit for bit, and they are the
+    full jacobian()'s xN blocks at their structural positions, bit for bit."""
+    j = load_npz("casadi_rollout20_jacobian.npz")
+    t = casadi_tape(j, "jacobian_xn")
+    assert tape_sha256(t) == str(j["jacobian_xn/tape_sha256"]) and t.n_instr == 15467
+    args = golden_list(z, "rollout", "arg", 2)
+    n = args[0].shape[1]
+    res = O.eval(t, list(args) + [None], n)
+    for k in range(2):
+        assert_bitexact(res[k], j["jacobian_xn/res%d" % k], "jac xN block %d" % k)
+        p = _pattern(j, "jacobian_xn/out%d" % k)
+        full = _pattern(z, "rollout/jac_0_%d" % k)
+        dense = np.zeros((full.nrow, full.ncol, n))
+        dense[full.row, full.col()] = z["rollout/jac_0_%d" % k]
+        assert_bitexact(res[k], dense[p.row, p.col()], "against jacobian()'s xN block")
 
 
 def test_casadi_jacobian_tape_fixture_gives_casadis_jacobian(z):

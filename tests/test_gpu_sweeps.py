@@ -502,6 +502,33 @@ def test_jacobian_reverse_equals_the_two_calls(gpu_lib, n):
     ct.sync()
 
 
+def test_jacobian_of_some_outputs_prunes_and_keeps_their_bits(gpu_lib):
+    """A Jacobian requested for xN only (the cost's sensitivities null): the tangent plan
+    drops the instructions only the cost needs, and xN's rows are the full Jacobian's bit for
+    bit, with the device entry points and with host buffers; the cost adjoint is unchanged."""
+    F = W.cartpole_rollout(20)
+    n = 4099
+    args_h = W.cartpole_inputs(n, steps=20, seed=41)
+    aseeds_h = [np.zeros((1, 4, n)), np.ones((1, 1, n))]
+    ct = CudaTape(F)
+    args, aseeds = dev(args_h), dev(aseeds_h)
+    _, full = ct.jacobian(args)
+    part = [torch.empty((24, 4, n), dtype=torch.float64, device="cuda"), None]
+    ct.jacobian(args, jac=part)
+    assert_bitexact(host([part[0]])[0], host(full)[0], "jacobian of xN")
+    r1, j1, a1 = ct.jacobian_reverse(args, aseeds)
+    j2 = [torch.empty((24, 4, n), dtype=torch.float64, device="cuda"), None]
+    r2, _, a2 = ct.jacobian_reverse(args, aseeds, jac=j2)
+    for x, y in zip(host(r1) + [host(j1)[0]] + host(a1), host(r2) + host([j2[0]]) + host(a2)):
+        assert_bitexact(x, y, "jacobian_reverse with the cost's Jacobian left out")
+    m = CudaMap(F, n)
+    hargs = [a.T.copy() for a in args_h]
+    hseeds = [np.transpose(s, (2, 0, 1)).copy() for s in aseeds_h]
+    _, hj, ha = m.jacobian_reverse(hargs, hseeds, jac=[np.empty((n, 24, 4)), None])
+    assert_bitexact(np.transpose(hj[0], (1, 2, 0)), host(j1)[0], "host buffers")
+    ct.sync()
+
+
 def test_sweeps_replay_from_a_cuda_graph(gpu_lib):
     """After one warm-up call (plans built, variants tuned), the derivative entry points can
     be captured into a CUDA graph and replayed: the replays read the inputs' current contents
