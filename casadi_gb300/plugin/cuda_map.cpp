@@ -37,6 +37,12 @@ Function CudaMap::create(const Function& f, casadi_int n) {
 
 void CudaMap::init(const Dict& opts) {
   Map::init(opts);
+  take_tape();
+}
+
+CudaMap::CudaMap(DeserializingStream& s) : Map(s) { take_tape(); }
+
+void CudaMap::take_tape() {
   casadi_assert(f_.is_a("SXFunction"), "CudaMap needs an SX Function, got " + f_.class_name());
   // the algorithm through the public accessors, in the ScalarAtomic layout the library takes
   const casadi_int n_instr = f_.n_instructions();

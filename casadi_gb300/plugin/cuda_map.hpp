@@ -13,7 +13,9 @@
 // Building: compile this file against the CasADi headers and link libcasadi and
 // libcasadi_gb300. Map::create's string switch (map.cpp:39-51) gets one branch returning
 // CudaMap::create(f, n) for "cuda"; until a CasADi build carries it, CudaMap::create builds
-// the Function directly.
+// the Function directly. Map::deserialize's class-name switch (map.cpp:110-122) gets one
+// branch returning CudaMap::deserialize(s) for "CudaMap" (Map::serialize_type writes the
+// class name), so a serialized cuda map reads back as one.
 #pragma once
 
 #include <mutex>
@@ -29,6 +31,12 @@ class CudaMap : public Map {
  public:
   CudaMap(const std::string& name, const Function& f, casadi_int n) : Map(name, f, n) {}
   ~CudaMap() override;
+
+  // the "CudaMap" branch of Map::deserialize: the Map's fields from the stream, then the tape
+  // records from the deserialized Function (a deserialized Function is finalized, not
+  // initialised again)
+  explicit CudaMap(DeserializingStream& s);
+  static ProtoFunction* deserialize(DeserializingStream& s) { return new CudaMap(s); }
 
   // Function::map(n, "cuda") of f
   static Function create(const Function& f, casadi_int n);
@@ -56,6 +64,7 @@ class CudaMap : public Map {
 
  private:
   int ensure(void* mem) const;
+  void take_tape();
   std::vector<casadi_gb300_atomic> alg_;
   std::vector<int> nnz_in_, nnz_out_;
   int sz_w_ = 0;

@@ -1,7 +1,9 @@
 // Check of the CudaMap plugin built against the reference's own libcasadi: the cart-pole RK4
 // step mapped over 8 instances with CudaMap::create and with Function::map(8, "serial"), its
 // class, I/O and sparsity as CasADi reports them, then one numeric call of each. Without a GPU
-// the CudaMap call must fail cleanly with the library's message. Prints key=value lines.
+// the CudaMap call must fail cleanly with the library's message. Then a Function::serialize()
+// round trip, with the "Map" entry of CasADi's deserializer table dispatching "CudaMap" as
+// the one-line patch of Map::deserialize would. Prints key=value lines.
 #include <cmath>
 #include <iostream>
 
@@ -25,6 +27,27 @@ static Function cartpole_step() {
   return Function("f", {x, u}, {x + dt / 6 * (k1 + 2 * k2 + 2 * k3 + k4)});
 }
 
+// Map::deserialize with the "CudaMap" branch (the classes CasADi itself knows are not needed
+// here: this check serializes a CudaMap only)
+static ProtoFunction* map_deserialize_with_cuda(DeserializingStream& s) {
+  std::string class_name;
+  s.unpack("Map::class_name", class_name);
+  casadi_assert(class_name == "CudaMap", "this check reads CudaMap only, got " + class_name);
+  return CudaMap::deserialize(s);
+}
+
+static void call(const char* key, const Function& fn, const std::vector<DM>& in, const DM& want) {
+  try {
+    DM got = fn(in).at(0);
+    std::cout << key << "_ok=1\n";
+    std::cout << key << "_max_abs_diff=" << static_cast<double>(norm_inf(got - want)) << "\n";
+  } catch (std::exception& e) {
+    std::string msg = e.what();
+    for (char& c : msg) if (c == '\n') c = ' ';
+    std::cout << key << "_ok=0\n" << key << "_error=" << msg << "\n";
+  }
+}
+
 int main() {
   Function f = cartpole_step();
   const casadi_int n = 8;
@@ -40,14 +63,14 @@ int main() {
                                     cm.sparsity_out(0) == sm.sparsity_out(0)) << "\n";
   DM x = DM::rand(4, n), u = DM::rand(1, n);
   DM want = sm(std::vector<DM>{x, u}).at(0);
-  try {
-    DM got = cm(std::vector<DM>{x, u}).at(0);
-    std::cout << "eval_ok=1\n";
-    std::cout << "max_abs_diff=" << static_cast<double>(norm_inf(got - want)) << "\n";
-  } catch (std::exception& e) {
-    std::string msg = e.what();
-    for (char& c : msg) if (c == '\n') c = ' ';
-    std::cout << "eval_ok=0\n" << "eval_error=" << msg << "\n";
-  }
+  call("eval", cm, {x, u}, want);
+  // serialize, then read back through CasADi's own Function::deserialize
+  const std::string text = cm.serialize();
+  FunctionInternal::deserialize_map["Map"] = &map_deserialize_with_cuda;
+  Function back = Function::deserialize(text);
+  std::cout << "back_class=" << back.class_name() << "\n";
+  std::cout << "back_same_sparsity=" << (back.sparsity_in(0) == cm.sparsity_in(0) &&
+                                         back.sparsity_out(0) == cm.sparsity_out(0)) << "\n";
+  call("back_eval", back, {x, u}, want);
   return 0;
 }

@@ -3,7 +3,8 @@ and driven through CasADi's C++ API (tests/plugin/cuda_map_check.cpp): CudaMap::
 of the cart-pole step is a Map of class CudaMap with the same I/O and sparsity as
 f.map(8, "serial"); its numeric call matches the serial Map where a GPU is present and fails
 cleanly -- the library's message as a CasADi warning, an evaluation-failed error, nothing
-crossing the C ABI -- where none is. Runs where libcasadi was built (oracle/Makefile casadi);
+crossing the C ABI -- where none is. A Function::serialize() / Function::deserialize() round
+trip gives a CudaMap back that behaves the same. Runs where libcasadi was built (oracle/Makefile casadi);
 skipped elsewhere."""
 import os
 import subprocess
@@ -28,8 +29,12 @@ def test_cuda_map_plugin_through_casadis_api():
     assert kv["class"] == "CudaMap" and kv["is_map"] == "1" and kv["is_cuda_map"] == "1"
     assert (kv["n_in"], kv["n_out"]) == ("2", "1")
     assert kv["size_in0"] == "4x8" and kv["size_out0"] == "4x8" and kv["same_sparsity"] == "1"
-    if kv["eval_ok"] == "1":
-        assert float(kv["max_abs_diff"]) <= 1e-12
-    else:
-        assert "Evaluation failed" in kv["eval_error"]
-        assert "CudaMap:" in r.stdout + r.stderr  # the library's message, as a warning
+    for key in ("eval", "back_eval"):
+        if kv[key + "_ok"] == "1":
+            assert float(kv[key + "_max_abs_diff"]) <= 1e-12
+        else:
+            assert "Evaluation failed" in kv[key + "_error"]
+            assert "CudaMap:" in r.stdout + r.stderr  # the library's message, as a warning
+    # Function::deserialize of the serialized text (with Map::deserialize's "CudaMap" branch)
+    # gives a CudaMap with the same I/O back
+    assert kv["back_class"] == "CudaMap" and kv["back_same_sparsity"] == "1"
