@@ -703,8 +703,10 @@ def mpc_sparse_component(torch, stream, n=4096, intervals=100, reps=3, cpu=False
 
     ms = timeit(step)
     ms_batch = timeit(step_batch)
-    same = bool(torch.equal(vj.view(torch.int64), J(args, stream=stream).view(torch.int64)) and
-                torch.equal(vh.view(torch.int64), H(args, stream=stream).view(torch.int64)))
+    rj, rh = J(args, stream=stream), H(args, stream=stream)
+    stream.synchronize()  # the separate calls ran on `stream`; compare after they finish
+    same = bool(torch.equal(vj.view(torch.int64), rj.view(torch.int64)) and
+                torch.equal(vh.view(torch.int64), rh.view(torch.int64)))
     cpu_rate = None
     if cpu:
         # the oracle port on the host cores: the same coloured forward sweeps on 64 scenarios

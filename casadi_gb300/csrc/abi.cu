@@ -91,13 +91,17 @@ struct TanPlan {
   std::vector<char> seeded;  // per input: seed pointer given (general seeds)
   std::vector<char> wanted;  // per output: sensitivities requested (others are pruned)
   int groups = 0;
-  uint4* d_stream = nullptr;  // entry streams of all directions
-  int2* d_chunks = nullptr;   // per direction: (first entry, entry count)
+  // keyed entry streams of all direction groups, one layout per group size (group_slot)
+  uint4* d_stream[kNumGroupSizes] = {};
+  int2* d_chunks[kNumGroupSizes] = {};  // per direction group: (first entry, body entries)
+  std::vector<int2> h_chunks[kNumGroupSizes];
   int* d_dirmap = nullptr;    // identity mode with a dirmap: its device copy
   int* d_order = nullptr;     // groups in work order, longest stream first (null: natural)
   ~TanPlan() {
-    cudaFree(d_stream);
-    cudaFree(d_chunks);
+    for (int g = 0; g < kNumGroupSizes; ++g) {
+      cudaFree(d_stream[g]);
+      cudaFree(d_chunks[g]);
+    }
     cudaFree(d_dirmap);
     cudaFree(d_order);
   }
@@ -126,13 +130,17 @@ struct AdjPlan {
   int ch = 0;
   std::vector<char> seeded;  // per output: seed pointer given
   int dw = 0;
-  uint4* d_stream = nullptr;  // entry stream
-  int2* d_chunks = nullptr;   // (first entry, entry count)
+  // keyed entry stream, one layout per group size (group_slot)
+  uint4* d_stream[kNumGroupSizes] = {};
+  int2* d_chunks[kNumGroupSizes] = {};  // (first entry, body entries)
+  int2 h_chunks[kNumGroupSizes] = {};
   int2* d_zero = nullptr;
   int n_zero = 0;
   ~AdjPlan() {
-    cudaFree(d_stream);
-    cudaFree(d_chunks);
+    for (int g = 0; g < kNumGroupSizes; ++g) {
+      cudaFree(d_stream[g]);
+      cudaFree(d_chunks[g]);
+    }
     cudaFree(d_zero);
   }
 };
@@ -522,8 +530,9 @@ unsigned lean_kind(unsigned op) {
   }
 }
 
-// Entry of instruction word w (flags: see the derivative sweeps); slot fields become byte
-// offsets into the warp's work vector w[slot][lane] (slot * 256).
+// Entry of the windowed tangent sweep (k_tangent_win) for instruction word w (flags: 1/2
+// operand b/c carries a derivative); slot fields become byte offsets into the warp's work
+// vector w[slot][lane] (slot * 256).
 uint4 dir_entry(u64 w, unsigned flags, int pk) {
   const unsigned op = dec_op(w), A = dec_a(w), B = dec_b(w), C = dec_c(w);
   uint4 e;
@@ -539,7 +548,7 @@ uint4 dir_entry(u64 w, unsigned flags, int pk) {
   return e;
 }
 
-// Operand forwarding in a one-direction tangent stream: an operand that is the value the
+// Operand forwarding in the windowed sweep's entries: an operand that is the value the
 // previous value-writing entry just computed is marked (bit 31 of its slot offset) and the
 // sweep takes it from a register instead of reading it back from shared memory.
 constexpr unsigned kFwdBit = 1u << 31;
@@ -567,12 +576,187 @@ void forward_operands(std::vector<uint4>& ents) {
   }
 }
 
-// Appends one stream, padded with NOP entries to whole groups; returns (first, count).
-int2 push_stream(std::vector<uint4>& all, const std::vector<uint4>& ents) {
+// One entry of a keyed stream before layout (see the keyed streams in sweeps.cuh).
+struct KEnt {
+  unsigned x = 0, y = 0, z = 0;
+  unsigned key = 0;    // TK_* or AK_*
+  unsigned pinfo = 0;  // what the walk loads for this entry: kPiP, kPiQ, kPiQNext, index << 3
+};
+
+// The partial loads of an entry: P (its d0) and/or Q (its d1) of an instruction with
+// recorded-partial mask pm whose first recorded partial is pk.
+unsigned pinfo_of(bool lp, bool lq, unsigned pm, int pk) {
+  if (!lp && !lq) return 0;
+  return (lp ? kPiP : 0u) | (lq ? kPiQ : 0u) | ((pm & 1u) ? kPiQNext : 0u) |
+         (static_cast<unsigned>(pk) << (kPiIndexShift - kPiShift));
+}
+
+// Lays out one keyed stream for group size gsz at the end of `all`: a header group, the body
+// padded to an even number of groups, one trailing group; entry p carries the partial loads of
+// entry p + gsz. Returns (first entry, body entries).
+int2 lay_out(std::vector<uint4>& all, const std::vector<KEnt>& ents, int gsz) {
+  const long long n = static_cast<long long>(ents.size());
+  long long ngr = (n + gsz - 1) / gsz;
+  if (ngr & 1) ++ngr;
+  const long long body = ngr * gsz;
   const int first = static_cast<int>(all.size());
-  all.insert(all.end(), ents.begin(), ents.end());
-  while ((all.size() - first) % kEntGroup) all.push_back(make_uint4(0, 0, 0, 0));
-  return make_int2(first, static_cast<int>(all.size()) - first);
+  for (long long p = -gsz; p < body + gsz; ++p) {
+    uint4 u = make_uint4(0, 0, 0, 0);
+    if (p >= 0 && p < n) u = make_uint4(ents[p].x, ents[p].y, ents[p].z, ents[p].key);
+    const long long q = p + gsz;
+    if (q >= 0 && q < n) u.w |= ents[q].pinfo << kPiShift;
+    all.push_back(u);
+  }
+  return make_int2(first, static_cast<int>(body));
+}
+
+constexpr int kGroupSizeOf[kNumGroupSizes] = {1, 2, 4, 8};
+
+// Tangent entry before keying: fields as the walks read them, the instruction's kind, flags
+// (1/2: operand b/c carries a derivative; inputs/outputs: 1 active), recorded-partial mask and
+// first partial, and whether an operand is the previous result (one-direction streams).
+struct TanRaw {
+  unsigned x = 0, y = 0, z = 0;
+  unsigned op = 0, kind = 0, f = 0, pm = 0;
+  int pk = 0;
+  bool mixed = false, yf = false, zf = false;
+};
+
+TanRaw tan_raw(u64 w, unsigned flags, int pk) {
+  const unsigned op = dec_op(w), A = dec_a(w), B = dec_b(w), C = dec_c(w);
+  TanRaw e;
+  if (op == D_INPUT) {
+    e.x = A * 256u, e.y = B, e.z = C;
+  } else if (op == D_OUTPUT) {
+    e.x = A, e.y = B * 256u, e.z = C;
+  } else {
+    e.x = A * 256u, e.y = B * 256u, e.z = C * 256u;
+  }
+  e.op = op;
+  e.kind = lean_kind(op);
+  e.f = flags & 3u;
+  e.pm = dec_pmask(w);
+  e.pk = pk;
+  return e;
+}
+
+// Operand forwarding in a one-direction tangent stream: an operand that is the value the
+// previous value-writing entry (an input or an arithmetic entry) just computed is read from
+// the register holding it instead of from shared memory.
+void forward_raw(std::vector<TanRaw>& ents) {
+  bool have = false;
+  unsigned last = 0;  // slot byte offset the previous value-writing entry wrote
+  for (TanRaw& e : ents) {
+    if (e.kind == LK_OUTPUT) {
+      e.yf = have && (e.f & 1u) && e.y == last;
+      continue;
+    }
+    if (e.kind == LK_INPUT) {
+      if (e.f & 1u) {
+        have = true;
+        last = e.x;
+      }
+      continue;
+    }
+    if (e.kind == LK_NOP || e.kind == LK_CONST || !e.f) continue;
+    e.yf = have && (e.f & 1u) && e.y == last;
+    e.zf = have && (e.f & 2u) && e.z == last;
+    have = true;
+    last = e.x;
+  }
+}
+
+// Tangent form of an arithmetic entry (-1: none). GEN ops whose d0 is a constant 1 and not
+// recorded (FMOD, REMAINDER, PRINTME, LIFT) take the unit forms: 1*a + q*b and 1*a are a + q*b
+// and a, bit for bit.
+int tan_form(const TanRaw& e) {
+  const unsigned f = e.f;
+  switch (e.kind) {
+    case LK_GEN: {
+      const bool p = e.pm & 1u, q = e.pm & 2u, unit = !p && const_d0(e.op) == 1.0;
+      if (f == 1u) return p ? TF_PY : unit ? TF_Y : -1;
+      if (f == 2u) return q ? TF_QZ : -1;
+      if (f == 3u) return !q ? -1 : p ? TF_PYQZ : unit ? TF_YQZ : -1;
+      return -1;
+    }
+    case LK_ADD: return f == 1u ? TF_Y : f == 2u ? TF_Z : f == 3u ? TF_YZ : -1;
+    case LK_SUB: return f == 1u ? TF_Y : f == 2u ? TF_NZ : f == 3u ? TF_YMZ : -1;
+    case LK_NEG: return f == 1u ? TF_NY : -1;
+    case LK_TWICE: return f == 1u ? TF_2Y : -1;
+    case LK_ASSIGN: return f == 1u ? TF_Y : -1;
+    case LK_IFZ: return f == 2u ? TF_IFZ : -1;
+    default: return -1;
+  }
+}
+
+unsigned tan_key_of(int form, bool yf, bool zf) {
+  yf = yf && tf_uses_y(form);
+  zf = zf && tf_uses_z(form);
+#define CGB_FIND(KEY, F, YF, ZF) \
+  if (form == (F) && yf == ((YF) != 0) && zf == ((ZF) != 0)) return KEY;
+  CGB_TK_ARITH(CGB_FIND)
+#undef CGB_FIND
+  return ~0u;
+}
+
+// Keyed tangent entry; false when the instruction has no tangent form (not expected).
+bool tan_keyed(const TanRaw& e, KEnt* k) {
+  k->x = e.x, k->y = e.y, k->z = e.z;
+  k->pinfo = 0;
+  if (e.mixed) {
+    k->key = TK_MIXED + e.pm;
+    k->pinfo = pinfo_of(e.pm & 1u, e.pm & 2u, e.pm, e.pk);
+    return true;
+  }
+  if (e.kind == LK_OUTPUT) {
+    k->key = !(e.f & 1u) ? TK_OUT0 : e.yf ? TK_OUT_F : TK_OUT;
+    return true;
+  }
+  if (e.kind == LK_INPUT) {
+    k->key = TK_IN;
+    return true;
+  }
+  const int form = tan_form(e);
+  if (form < 0) return false;
+  k->key = tan_key_of(form, e.yf, e.zf);
+  k->pinfo = pinfo_of(tf_uses_p(form), tf_uses_q(form), e.pm, e.pk);
+  return k->key != ~0u;
+}
+
+// Adjoint contribution forms of an arithmetic instruction (op, kind, recorded-partial mask pm)
+// with adjoint-plan flags f (2/4: operand b/c receives, 8/16: its first contribution); -1:
+// none. GEN ops with an unrecorded unit d0 take the unit forms (1*s and fma(1, s, w) are s
+// and w + s, bit for bit).
+int adj_bform(unsigned op, unsigned kind, unsigned pm, unsigned f) {
+  if (!(f & 2u)) return CF_N;
+  const bool first = f & 8u;
+  switch (kind) {
+    case LK_GEN:
+      if (pm & 1u) return first ? CF_RF : CF_RA;
+      return const_d0(op) == 1.0 ? (first ? CF_UF : CF_UA) : -1;
+    case LK_ADD: case LK_SUB: case LK_ASSIGN: return first ? CF_UF : CF_UA;
+    case LK_NEG: return first ? CF_MF : CF_MA;
+    case LK_TWICE: return first ? CF_TF : CF_TA;
+    default: return -1;
+  }
+}
+int adj_cform(unsigned kind, unsigned pm, unsigned f) {
+  if (!(f & 4u)) return CF_N;
+  const bool first = f & 16u;
+  switch (kind) {
+    case LK_GEN: return (pm & 2u) ? (first ? CF_RF : CF_RA) : -1;
+    case LK_ADD: return first ? CF_UF : CF_UA;
+    case LK_SUB: return first ? CF_MF : CF_MA;
+    case LK_IFZ: return first ? CF_IF : CF_IA;
+    default: return -1;
+  }
+}
+unsigned adj_key_of(int bf, int cf) {
+#define CGB_FIND(KEY, BF, CF) \
+  if (bf == (BF) && cf == (CF)) return KEY;
+  CGB_AK_ARITH(CGB_FIND)
+#undef CGB_FIND
+  return ~0u;
 }
 
 std::vector<int> partial_starts(const Tape& t) {
@@ -686,18 +870,21 @@ const TanPlan* tan_plan(Tape& t, int ndir, int dw, int ch, bool identity,
   const std::vector<unsigned short> bits =
       tan_activity(t, ndir, dw, identity, seeded, dirmap, wanted);
   // one stream per group of dw directions (the union of their work); an entry whose flags
-  // differ between the group's directions becomes LK_MIXED with the real kind in x bits
-  // 19-22 and the flags of direction k in bits 24+2k (see the tangent kernel)
+  // differ between the group's directions is mixed: the real kind in x bits 19-22 and the
+  // flags of direction k in bits 24+2k (see the tangent kernel)
   const std::vector<int> pk = partial_starts(t);
-  std::vector<uint4> all;
-  std::vector<int2> se(p->groups);
+  std::vector<uint4> all[kNumGroupSizes];
+  for (int gs = 0; gs < kNumGroupSizes; ++gs) p->h_chunks[gs].resize(p->groups);
+  std::vector<size_t> len(p->groups, 0);
   for (int g = 0; g < p->groups; ++g) {
     if (!identity && g > 0) {
-      se[g] = se[0];  // general seeds: one stream serves every group
+      // general seeds: one stream serves every group
+      for (int gs = 0; gs < kNumGroupSizes; ++gs) p->h_chunks[gs][g] = p->h_chunks[gs][0];
+      len[g] = len[0];
       continue;
     }
     const int kv = std::min(dw, ndir - g * dw);  // directions in this group
-    std::vector<uint4> ents;
+    std::vector<TanRaw> raw;
     for (size_t k = 0; k < nc; ++k) {
       const u64 w = t.h_code[k];
       const unsigned op = dec_op(w);
@@ -707,28 +894,38 @@ const TanPlan* tan_plan(Tape& t, int ndir, int dw, int ch, bool identity,
       bool uniform = true;
       for (int d = 1; d < kv; ++d) uniform = uniform && ((gb >> (2 * d)) & 3u) == f0;
       if (uniform) {
-        ents.push_back(dir_entry(w, f0, pk[k]));
+        raw.push_back(tan_raw(w, f0, pk[k]));
       } else {
-        uint4 e = dir_entry(w, 0, pk[k]);
+        TanRaw e = tan_raw(w, 0, pk[k]);
         e.x |= (lean_kind(op) << 19) | ((gb & 0xffu) << 24);
-        e.w = (e.w & ~(15u << 5)) | (static_cast<unsigned>(LK_MIXED) << 5);
-        ents.push_back(e);
+        e.mixed = true;
+        raw.push_back(e);
       }
     }
-    if (dw == 1) forward_operands(ents);
-    se[g] = push_stream(all, ents);
+    if (dw == 1) forward_raw(raw);
+    std::vector<KEnt> ents(raw.size());
+    for (size_t q = 0; q < raw.size(); ++q)
+      if (!tan_keyed(raw[q], &ents[q])) {
+        *err = fail(CASADI_GB300_ERR_UNSUPPORTED, "tangent entry of op %u has no form",
+                    raw[q].op);
+        return nullptr;
+      }
+    for (int gs = 0; gs < kNumGroupSizes; ++gs)
+      p->h_chunks[gs][g] = lay_out(all[gs], ents, kGroupSizeOf[gs]);
+    len[g] = ents.size();
   }
   // the groups of one tile are claimed longest first, so the last items of a sweep are the
   // short ones
   std::vector<int> order(p->groups);
   for (int g = 0; g < p->groups; ++g) order[g] = g;
-  std::stable_sort(order.begin(), order.end(),
-                   [&](int x, int y) { return se[x].y > se[y].y; });
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return len[x] > len[y]; });
   bool natural = true;
   for (int g = 0; g < p->groups; ++g) natural = natural && order[g] == g;
-  cudaError_t e;
-  if ((e = upload(&p->d_stream, all)) != cudaSuccess ||
-      (e = upload(&p->d_chunks, se)) != cudaSuccess ||
+  cudaError_t e = cudaSuccess;
+  for (int gs = 0; gs < kNumGroupSizes && e == cudaSuccess; ++gs)
+    if ((e = upload(&p->d_stream[gs], all[gs])) == cudaSuccess)
+      e = upload(&p->d_chunks[gs], p->h_chunks[gs]);
+  if (e != cudaSuccess ||
       (!natural && (e = upload(&p->d_order, order)) != cudaSuccess) ||
       (identity && !dirmap.empty() && (e = upload(&p->d_dirmap, dirmap)) != cudaSuccess)) {
     *err = cuda_fail(e, "upload tangent plan");
@@ -938,17 +1135,49 @@ const AdjPlan* adj_plan(Tape& t, int dw, int ch, const std::vector<char>& seeded
     }
     bits[kk] = static_cast<unsigned char>(f);
   }
+  // keyed entries in sweep order (last instruction first). Constants and arithmetic entries
+  // that pass nothing on are left out: every slot's first contribution is assigned, so no
+  // adjoint needs resetting after it is read.
   const std::vector<int> pk = partial_starts(t);
-  std::vector<uint4> ents, all;
-  for (size_t k = 0; k < nc; ++k) {
-    if (!bits[k]) continue;
-    ents.push_back(dir_entry(t.h_code[k], bits[k] & 31u, pk[k]));
+  std::vector<KEnt> ents;
+  for (size_t kk = nc; kk-- > 0;) {
+    const unsigned f = bits[kk];
+    if (!f) continue;
+    const u64 w = t.h_code[kk];
+    const unsigned op = dec_op(w), A = dec_a(w), B = dec_b(w), C = dec_c(w);
+    KEnt e;
+    if (op == D_OUTPUT) {
+      e.x = A, e.y = B * 256u, e.z = C;
+      e.key = (f & 8u) ? AK_OUT_SET : AK_OUT_ADD;
+    } else if (op == D_INPUT) {
+      e.x = A * 256u, e.y = B, e.z = C;
+      e.key = AK_IN;
+    } else if (op == D_CONST) {
+      continue;
+    } else {
+      const unsigned kind = lean_kind(op), pm = dec_pmask(w);
+      const int bf = adj_bform(op, kind, pm, f), cf = adj_cform(kind, pm, f);
+      if (bf == CF_N && cf == CF_N) continue;
+      e.x = A * 256u, e.y = B * 256u, e.z = C * 256u;
+      e.key = (bf < 0 || cf < 0) ? ~0u : adj_key_of(bf, cf);
+      if (e.key == ~0u) {
+        *err = fail(CASADI_GB300_ERR_UNSUPPORTED, "adjoint entry of op %u has no form", op);
+        return nullptr;
+      }
+      e.pinfo = pinfo_of(bf == CF_RF || bf == CF_RA,
+                         cf == CF_RF || cf == CF_RA || cf == CF_IF || cf == CF_IA, pm, pk[kk]);
+    }
+    ents.push_back(e);
   }
-  std::vector<int2> se = {push_stream(all, ents)};
   p->n_zero = static_cast<int>(zero.size());
-  cudaError_t e;
-  if ((e = upload(&p->d_stream, all)) != cudaSuccess ||
-      (e = upload(&p->d_chunks, se)) != cudaSuccess || (e = upload(&p->d_zero, zero)) != cudaSuccess) {
+  cudaError_t e = cudaSuccess;
+  for (int gs = 0; gs < kNumGroupSizes && e == cudaSuccess; ++gs) {
+    std::vector<uint4> all;
+    p->h_chunks[gs] = lay_out(all, ents, kGroupSizeOf[gs]);
+    if ((e = upload(&p->d_stream[gs], all)) == cudaSuccess)
+      e = upload(&p->d_chunks[gs], std::vector<int2>{p->h_chunks[gs]});
+  }
+  if (e != cudaSuccess || (e = upload(&p->d_zero, zero)) != cudaSuccess) {
     *err = cuda_fail(e, "upload adjoint plan");
     return nullptr;
   }
@@ -1177,6 +1406,15 @@ cudaError_t launch_tangent_queued(const SweepArgs& a, int grid, bool more_items,
   return launch_tangent(b, grid, variant, s);
 }
 
+// The keyed streams (every group-size layout) and work order of a tangent plan.
+void set_streams(SweepArgs& a, const TanPlan* tp) {
+  for (int gs = 0; gs < kNumGroupSizes; ++gs) {
+    a.dstreams[gs] = tp->d_stream[gs];
+    a.dchunkss[gs] = tp->d_chunks[gs];
+  }
+  a.gorder = tp->d_order;
+}
+
 int run_deriv(Tape& t, SweepArgs a, long long m, const DerivReq& rq, cudaStream_t s) {
   const int ndir = rq.ndir;
   const bool adjoint = rq.adjoint, identity = rq.identity;
@@ -1203,8 +1441,10 @@ int run_deriv(Tape& t, SweepArgs a, long long m, const DerivReq& rq, cudaStream_
   a.block = 32;
   a.chunk = 0;
   if (ap) {
-    a.dstream = ap->d_stream;
-    a.dchunks = ap->d_chunks;
+    for (int gs = 0; gs < kNumGroupSizes; ++gs) {
+      a.dstreams[gs] = ap->d_stream[gs];
+      a.dchunkss[gs] = ap->d_chunks[gs];
+    }
     a.zero_in = ap->d_zero;
     a.n_zero = ap->n_zero;
   }
@@ -1248,9 +1488,7 @@ int run_deriv(Tape& t, SweepArgs a, long long m, const DerivReq& rq, cudaStream_
         tan_plan(t, ndir, kd, 0, identity, seeded_in, rq.dirmap ? *rq.dirmap : kNoMap,
                  wanted_out, &plan_err);
     if (!tp) return cudaErrorInvalidValue;
-    a.dstream = tp->d_stream;
-    a.dchunks = tp->d_chunks;
-    a.gorder = tp->d_order;
+    set_streams(a, tp);
     const int grid = grid_of(v);
     return launch_tangent_queued(a, grid, grid < work_of(v), v, s);
   };
@@ -1305,9 +1543,7 @@ int run_deriv(Tape& t, SweepArgs a, long long m, const DerivReq& rq, cudaStream_
       const TanPlan* tp = tan_plan(t, ndir, 1, 0, identity, seeded_in,
                                    rq.dirmap ? *rq.dirmap : kNoMap, wanted_out, &plan_err);
       if (!tp) return cudaErrorInvalidValue;
-      a.dstream = tp->d_stream;
-      a.dchunks = tp->d_chunks;
-      a.gorder = tp->d_order;
+      set_streams(a, tp);
       return launch_tangent_queued(a, grid, grid < work, 0, s);
     });
     if (plan_err) return plan_err;

@@ -118,8 +118,8 @@ int batch_prepare(BatchHost& b) {
       const TanPlan* tp = tan_plan(*t, it.ndir, 1, 0, true, std::vector<char>(t->n_in, 0),
                                    it.dirmap, std::vector<char>(t->n_out, 1), &err);
       if (!tp) return err;
-      bi.tan_stream = tp->d_stream;
-      bi.tan_chunks = tp->d_chunks;
+      bi.tan_stream = tp->d_stream[group_slot(kBatchTanGroup)];
+      bi.tan_chunks = tp->d_chunks[group_slot(kBatchTanGroup)];
     } else if (it.ndir > 0) {
       if (static_cast<unsigned>(t->n_partials) >= kMaxPartials)
         return fail(CASADI_GB300_ERR_UNSUPPORTED, "batch item %zu records too many partials", k);
@@ -128,11 +128,9 @@ int batch_prepare(BatchHost& b) {
       int err = 0;
       const AdjPlan* ap = adj_plan(*t, 1, 0, seeded, &err);
       if (!ap) return err;
-      int2 se;
-      cudaError_t e = cudaMemcpy(&se, ap->d_chunks, sizeof(int2), cudaMemcpyDeviceToHost);
-      if (e != cudaSuccess) return cuda_fail(e, "read adjoint plan");
-      bi.adj_stream = ap->d_stream + se.x;
-      bi.adj_ngr = se.y / kBatchGroup;
+      const int2 se = ap->h_chunks[group_slot(kBatchAdjGroup)];
+      bi.adj_stream = ap->d_stream[group_slot(kBatchAdjGroup)] + se.x;
+      bi.adj_ngr = se.y / kBatchAdjGroup;
       bi.zero_in = ap->d_zero;
       bi.n_zero = ap->n_zero;
     }
@@ -166,7 +164,7 @@ int batch_prepare(BatchHost& b) {
           units.push_back({static_cast<double>(t->n_instr),
                            make_int4(static_cast<int>(k), static_cast<int>(tile), -1, 0)});
         for (int d = 0; d < it.ndir; ++d) {
-          const double len = it.forward ? se[d].y : bi.adj_ngr * kBatchGroup;
+          const double len = it.forward ? se[d].y : bi.adj_ngr * kBatchAdjGroup;
           dir_units.push_back({len, make_int4(static_cast<int>(k), static_cast<int>(tile), d, 0)});
         }
       }

@@ -391,42 +391,35 @@ __global__ void __launch_bounds__(32 * DW) k_adjoint_tape(const __grid_constant_
 // Each warp owns one (32-instance tile, direction) work item at a time and walks its own
 // host-compiled entry stream: for the tangent sweep the stream of its direction (only the
 // instructions whose derivative is structurally nonzero for that direction, plus outputs),
-// for the adjoint sweep the one stream of instructions with a nonzero adjoint. Warps never
-// wait for each other, so a sparse direction finishes early instead of waiting for a dense
-// one. Entries and recorded partials are loaded straight from global memory (L2-resident,
-// one coalesced 256-byte request per partial) and software-pipelined through registers:
-// entries two groups of G ahead, partials one group ahead. Shared memory holds only
-// the work vector, w[slot][lane], so as many warps fit as the work vector allows.
-//
-// Entry: {a, b, c, meta}; a/b/c are slot byte offsets (slot*256) or I/O indices; meta bits
-// 0-4 flags (tangent: 1/2 operand b/c carries a derivative; adjoint: 2/4 operand b/c
-// receives a contribution, 8/16 it is the first one), 5-8 kind, 9-10 recorded-partial mask,
-// 11-31 index of the instruction's first recorded partial.
+// for the adjoint sweep the one stream of instructions with a nonzero adjoint, last
+// instruction first. Warps never wait for each other, so a sparse direction finishes early
+// instead of waiting for a dense one. Entries and recorded partials are loaded straight from
+// global memory (L2-resident, one coalesced 256-byte request per partial) and
+// software-pipelined through registers: while group g computes, the entries of group g+1 and
+// the partials they use (described by group g's entries, see the keyed streams in sweeps.cuh)
+// are in flight. Two groups are unrolled per iteration, so the pipeline needs no register
+// moves. Each entry is one jump-table dispatch on its key, whose case holds only the FP64
+// operations and work-vector accesses that entry needs. Shared memory holds only the work
+// vector, w[slot][lane], so as many warps fit as the work vector allows.
 // ---------------------------------------------------------------------------------------------
 
 __device__ __forceinline__ double& wreg(unsigned char* base, unsigned off) {
   return *reinterpret_cast<double*>(base + off);
 }
 
-// meta layout shared by both streams
+// Meta word of the windowed tangent sweep's entries (k_tangent_win): bits 0-4 flags (1/2
+// operand b/c carries a derivative), 5-8 kind, 9-10 recorded-partial mask, 11-31 index of the
+// instruction's first recorded partial.
 __host__ __device__ __forceinline__ unsigned ent_flags(unsigned m) { return m & 31u; }
 __host__ __device__ __forceinline__ unsigned ent_kind(unsigned m) { return (m >> 5) & 15u; }
 __host__ __device__ __forceinline__ unsigned ent_pmask(unsigned m) { return (m >> 9) & 3u; }
 __host__ __device__ __forceinline__ unsigned ent_pk(unsigned m) { return m >> 11; }
 
-// Load the partials of one group of entries (d0 at pk, d1 at pk+1 or pk). kNC: read-only
-// path (partials written by an earlier launch); otherwise L2 loads that see the same
-// kernel's stores.
+// kNC: read-only path (partials written by an earlier launch); otherwise L2 loads that see the
+// same kernel's stores.
 template <bool kNC>
 __device__ __forceinline__ double ld_partial(const double* p) {
   return kNC ? __ldg(p) : __ldcg(p);
-}
-
-template <int G>
-__device__ __forceinline__ void load_group(const uint4* st, int g, int ngr, uint4 (&E)[G]) {
-#pragma unroll
-  for (int i = 0; i < G; ++i)
-    E[i] = g < ngr ? __ldg(st + g * G + i) : make_uint4(0, 0, 0, 0);
 }
 
 // G: entries per software-pipeline group; MB: minimum resident CTAs per SM the register
@@ -438,36 +431,185 @@ __device__ __forceinline__ double& wj(unsigned char* wb, unsigned off, int j) {
   return wreg(wb, off * IPT + j * 256);
 }
 
-// Partials of one group of entries for IPT tiles (tile j's block at pt + j*tstride; tiles
-// past the wave's end are not read). Only the partials an entry uses are loaded: a tangent
-// entry uses d0 when operand b carries a derivative (flag 1) and d1 when c does (flag 2); an
-// adjoint entry uses d0 when b receives a contribution (flag 2) and d1 when c does (flag 4);
-// a mixed tangent entry (flags per direction) loads both.
-template <bool kNC, bool kAdj, int G, int IPT>
-__device__ __forceinline__ void load_partials_n(const uint4 (&E)[G], const double* pt,
-                                                size_t tstride, const bool (&tok)[IPT],
-                                                double (&P0)[G][IPT], double (&P1)[G][IPT]) {
+// Group gi of a keyed stream (0: the header, g+1: body group g).
+template <int G>
+__device__ __forceinline__ void load_grp(const uint4* st, int gi, uint4 (&E)[G]) {
+  const uint4* p = st + gi * G;
+#pragma unroll
+  for (int i = 0; i < G; ++i) E[i] = __ldg(p + i);
+}
+
+// The partials group E describes (those of the next group) for IPT tiles, tile j's block at
+// pt + j*tstride; tiles past the wave's end are not read. Registers of partials not loaded
+// keep stale values that the entries' cases do not read.
+template <bool kNC, int G, int IPT>
+__device__ __forceinline__ void issue_partials(const uint4 (&E)[G], const double* pt,
+                                               size_t tstride, const bool (&tok)[IPT],
+                                               double (&P)[G][IPT], double (&Q)[G][IPT]) {
 #pragma unroll
   for (int i = 0; i < G; ++i) {
-    const unsigned meta = E[i].w;
-    const unsigned f = ent_flags(meta);
-    const unsigned use = kAdj ? (f >> 1) & 3u : (ent_kind(meta) == LK_MIXED ? 3u : f & 3u);
-    const unsigned m = ent_pmask(meta);
-    const size_t pk = ent_pk(meta);
-    const size_t k1 = pk + ((m & 1u) ? 1 : 0);
+    const unsigned w = E[i].w;
+    const double* pp = pt + static_cast<size_t>(w >> kPiIndexShift) * 32;
+    const double* pq = pp + ((w >> (kPiShift + 2 - 5)) & 32u);  // next partial row if kPiQNext
 #pragma unroll
     for (int j = 0; j < IPT; ++j) {
-      P0[i][j] = ((m & use & 1u) && tok[j]) ? ld_partial<kNC>(pt + j * tstride + pk * 32) : 1.0;
-      P1[i][j] = ((m & use & 2u) && tok[j]) ? ld_partial<kNC>(pt + j * tstride + k1 * 32) : 0.0;
+      if ((w & (kPiP << kPiShift)) && tok[j]) P[i][j] = ld_partial<kNC>(pp + j * tstride);
+      if ((w & (kPiQ << kPiShift)) && tok[j]) Q[i][j] = ld_partial<kNC>(pq + j * tstride);
     }
+  }
+}
+
+// Tangent of form F from the operand tangents a, b and the partials p, q.
+template <int F>
+__device__ __forceinline__ double tf_eval(double p, double q, double a, double b) {
+  if constexpr (F == TF_PY) return __dmul_rn(p, a);
+  else if constexpr (F == TF_QZ) return __dmul_rn(q, b);
+  else if constexpr (F == TF_PYQZ) return __fma_rn(p, a, __dmul_rn(q, b));
+  else if constexpr (F == TF_Y) return a;
+  else if constexpr (F == TF_Z) return b;
+  else if constexpr (F == TF_YQZ) return __dadd_rn(a, __dmul_rn(q, b));
+  else if constexpr (F == TF_YZ) return __dadd_rn(a, b);
+  else if constexpr (F == TF_NZ) return d_neg(b);
+  else if constexpr (F == TF_YMZ) return __dsub_rn(a, b);
+  else if constexpr (F == TF_NY) return d_neg(a);
+  else if constexpr (F == TF_2Y) return d_twice(a);
+  else return d_iszero(q) ? 0.0 : b;  // TF_IFZ
+}
+
+// Tangent of one direction of a mixed union-stream entry: instruction kind rk, flags fk
+// (1/2: operand b/c carries a derivative), partials p (1 when d0 is not recorded) and q.
+__device__ __forceinline__ double tan_mixed(unsigned rk, unsigned fk, double p, double q,
+                                            double a, double b) {
+  switch ((rk << 2) | fk) {
+    case (LK_GEN << 2) | 1u: return __dmul_rn(p, a);
+    case (LK_GEN << 2) | 2u: return __dmul_rn(q, b);
+    case (LK_GEN << 2) | 3u: return __fma_rn(p, a, __dmul_rn(q, b));
+    case (LK_ADD << 2) | 1u: case (LK_SUB << 2) | 1u: case (LK_ASSIGN << 2) | 1u: return a;
+    case (LK_ADD << 2) | 2u: return b;
+    case (LK_ADD << 2) | 3u: return __dadd_rn(a, b);
+    case (LK_SUB << 2) | 2u: return d_neg(b);
+    case (LK_SUB << 2) | 3u: return __dsub_rn(a, b);
+    case (LK_NEG << 2) | 1u: return d_neg(a);
+    case (LK_TWICE << 2) | 1u: return d_twice(a);
+    case (LK_IFZ << 2) | 2u: return d_iszero(q) ? 0.0 : b;
+    default: return 0.0;
   }
 }
 
 // Tangent entries of K > 1 directions: x bits 0-18 hold the destination (see k_tangent).
 constexpr unsigned kTanXMask = (1u << 19) - 1;
 
-// One tangent sweep by one warp over its entry stream st (ngr groups of G): IPT tiles (tile j's
-// partials at pt + j*tstride), K directions dir0.. (the union stream of the K directions).
+// One group of tangent entries (IPT tiles, K directions dir0..): their keys in E, their
+// partials in P/Q. `last` holds the previous arithmetic or input entry's result (one-direction
+// streams only).
+template <int G, int IPT, int K>
+__device__ __forceinline__ void tan_group(const uint4 (&E)[G], const double (&P)[G][IPT],
+                                          const double (&Q)[G][IPT], double (&last)[IPT],
+                                          unsigned char* wb, const IoDesc* seed,
+                                          const IoDesc* sens, bool identity,
+                                          const bool (&active)[IPT], int dir0, int ndir,
+                                          const long long (&ig)[IPT]) {
+#define CGB_W(off, j, k) wj<IPT * K>(wb, (off), (j) * K + (k))
+#define CGB_JK _Pragma("unroll") for (int j = 0; j < IPT; ++j) _Pragma("unroll") for (int k = 0; k < K; ++k)
+#pragma unroll
+  for (int i = 0; i < G; ++i) {
+    const uint4 cur = E[i];
+    const unsigned key = ent_key(cur.w);
+    const unsigned xo = K > 1 ? (cur.x & kTanXMask) : cur.x;
+    double r[IPT][K];
+    switch (key) {
+      case TK_OUT0:
+      case TK_OUT:
+      case TK_OUT_F: {
+        const IoDesc& d = sens[xo];
+        CGB_JK {
+          if (dir0 + k < ndir && active[j] && d.ptr)
+            static_cast<double*>(d.ptr)[io_off(d, dir0 + k, cur.z, ig[j])] =
+                key == TK_OUT ? CGB_W(cur.y, j, k) : key == TK_OUT_F ? last[j] : 0.0;
+        }
+        continue;
+      }
+      case TK_IN:
+        if (identity) {
+          CGB_JK r[j][k] = 1.0;
+        } else {
+          const IoDesc& d = seed[cur.y];
+          CGB_JK r[j][k] = (active[j] && dir0 + k < ndir)
+              ? __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir0 + k, cur.z, ig[j]))
+              : 0.0;
+        }
+        break;
+#define CGB_TK_CASE(KEY, F, YF, ZF)                                                  \
+  case KEY:                                                                          \
+    CGB_JK {                                                                         \
+      const double av = tf_uses_y(F) ? ((YF) ? last[j] : CGB_W(cur.y, j, k)) : 0.0;  \
+      const double bv = tf_uses_z(F) ? ((ZF) ? last[j] : CGB_W(cur.z, j, k)) : 0.0;  \
+      r[j][k] = tf_eval<F>(P[i][j], Q[i][j], av, bv);                                \
+    }                                                                                \
+    break;
+      CGB_TK_ARITH(CGB_TK_CASE)
+#undef CGB_TK_CASE
+      case TK_MIXED:
+      case TK_MIXED + 1:
+      case TK_MIXED + 2:
+      case TK_MIXED + 3: {
+        if (K == 1) continue;
+        // directions of the group differ: one dispatch per direction
+        const unsigned pm = key - TK_MIXED;
+        const unsigned rk = (cur.x >> 19) & 15u;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          const unsigned fk = (cur.x >> (24 + 2 * k)) & 3u;
+          if (rk == LK_OUTPUT) {
+            const IoDesc& d = sens[xo];
+#pragma unroll
+            for (int j = 0; j < IPT; ++j)
+              if (dir0 + k < ndir && active[j] && d.ptr)
+                static_cast<double*>(d.ptr)[io_off(d, dir0 + k, cur.z, ig[j])] =
+                    (fk & 1u) ? CGB_W(cur.y, j, k) : 0.0;
+            continue;
+          }
+          if (!fk) continue;
+          if (rk == LK_INPUT) {
+#pragma unroll
+            for (int j = 0; j < IPT; ++j) {
+              double v = 1.0;
+              if (!identity) {
+                const IoDesc& d = seed[cur.y];
+                v = (active[j] && dir0 + k < ndir)
+                    ? __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir0 + k, cur.z, ig[j]))
+                    : 0.0;
+              }
+              CGB_W(xo, j, k) = v;
+            }
+            continue;
+          }
+#pragma unroll
+          for (int j = 0; j < IPT; ++j) {
+            const double a = (fk & 1u) ? CGB_W(cur.y, j, k) : 0.0;
+            const double b = (fk & 2u) ? CGB_W(cur.z, j, k) : 0.0;
+            CGB_W(xo, j, k) = tan_mixed(rk, fk, (pm & 1u) ? P[i][j] : 1.0,
+                                        (pm & 2u) ? Q[i][j] : 0.0, a, b);
+          }
+        }
+        continue;
+      }
+      default:
+        continue;  // NOP padding
+    }
+    CGB_JK CGB_W(xo, j, k) = r[j][k];
+    if (K == 1) {
+#pragma unroll
+      for (int j = 0; j < IPT; ++j) last[j] = r[j][0];
+    }
+  }
+#undef CGB_JK
+#undef CGB_W
+}
+
+// One tangent sweep by one warp over its keyed stream st (body of ngr groups of G, ngr even):
+// IPT tiles (tile j's partials at pt + j*tstride), K directions dir0.. (the union stream of
+// the K directions).
 template <bool kNC, int G, int IPT, int K>
 __device__ __forceinline__ void tangent_walk(const uint4* st, int ngr, const double* pt,
                                              size_t tstride, const bool (&tok)[IPT],
@@ -475,163 +617,26 @@ __device__ __forceinline__ void tangent_walk(const uint4* st, int ngr, const dou
                                              const IoDesc* sens, bool identity,
                                              const bool (&active)[IPT], int dir0, int ndir,
                                              const long long (&ig)[IPT]) {
-  uint4 E0[G], E1[G];
-  double P0[G][IPT], Q0[G][IPT];
-  // one-direction streams mark operands that are the previous written value (bit 31 of the
-  // slot offset): they come from `last` instead of shared memory
+  uint4 Ea[G], Eb[G];
+  double Pa[G][IPT], Qa[G][IPT], Pb[G][IPT], Qb[G][IPT];
   double last[IPT];
 #pragma unroll
+  for (int i = 0; i < G; ++i)
+#pragma unroll
+    for (int j = 0; j < IPT; ++j) Pa[i][j] = Qa[i][j] = Pb[i][j] = Qb[i][j] = 0.0;
+#pragma unroll
   for (int j = 0; j < IPT; ++j) last[j] = 0.0;
-  load_group<G>(st, 0, ngr, E0);
-  load_group<G>(st, 1, ngr, E1);
-  load_partials_n<kNC, false, G, IPT>(E0, pt, tstride, tok, P0, Q0);
+  load_grp<G>(st, 0, Eb);  // the header: the first group's partials
+  issue_partials<kNC, G, IPT>(Eb, pt, tstride, tok, Pa, Qa);
+  load_grp<G>(st, 1, Ea);
 #pragma unroll 1
-  for (int g = 0; g < ngr; ++g) {
-    uint4 E2[G];
-    double P1[G][IPT], Q1[G][IPT];
-    load_group<G>(st, g + 2, ngr, E2);
-    load_partials_n<kNC, false, G, IPT>(E1, pt, tstride, tok, P1, Q1);
-#pragma unroll
-    for (int i = 0; i < G; ++i) {
-      const uint4 cur = E0[i];
-      const unsigned meta = cur.w;
-      const unsigned xo = K > 1 ? (cur.x & kTanXMask) : cur.x;
-#define CGB_W(off, j, k) wj<IPT * K>(wb, (off), (j) * K + (k))
-// operand at slot offset `off` of tile j, direction k (forwarded from `last` when marked;
-// only one-direction streams carry marks)
-#define CGB_OP(off, j, k) \
-  ((K == 1 && ((off) & 0x80000000u)) ? last[j] : CGB_W((off) & 0x7fffffffu, j, k))
-#define CGB_JK _Pragma("unroll") for (int j = 0; j < IPT; ++j) _Pragma("unroll") for (int k = 0; k < K; ++k)
-// tangent of one arithmetic entry (kind and flags in `key`) for tile j, direction k
-#define CGB_TAN_CASES(R, j, k)                                                               \
-case (LK_GEN << 2) | 1u: R = __dmul_rn(P0[i][j], CGB_OP(cur.y, j, k)); break;              \
-case (LK_GEN << 2) | 2u: R = __dmul_rn(Q0[i][j], CGB_OP(cur.z, j, k)); break;              \
-case (LK_GEN << 2) | 3u:                                                                   \
-  R = __fma_rn(P0[i][j], CGB_OP(cur.y, j, k), __dmul_rn(Q0[i][j], CGB_OP(cur.z, j, k)));         \
-  break;                                                                                   \
-case (LK_ADD << 2) | 1u: R = CGB_OP(cur.y, j, k); break;                                   \
-case (LK_ADD << 2) | 2u: R = CGB_OP(cur.z, j, k); break;                                   \
-case (LK_ADD << 2) | 3u: R = __dadd_rn(CGB_OP(cur.y, j, k), CGB_OP(cur.z, j, k)); break;   \
-case (LK_SUB << 2) | 1u: R = CGB_OP(cur.y, j, k); break;                                   \
-case (LK_SUB << 2) | 2u: R = d_neg(CGB_OP(cur.z, j, k)); break;                            \
-case (LK_SUB << 2) | 3u: R = __dsub_rn(CGB_OP(cur.y, j, k), CGB_OP(cur.z, j, k)); break;   \
-case (LK_NEG << 2) | 1u: R = d_neg(CGB_OP(cur.y, j, k)); break;                            \
-case (LK_TWICE << 2) | 1u: {                                                               \
-  const double xb = CGB_OP(cur.y, j, k);                                                   \
-  R = d_twice(xb);                                                                         \
-} break;                                                                                   \
-case (LK_ASSIGN << 2) | 1u: R = CGB_OP(cur.y, j, k); break;                                \
-case (LK_IFZ << 2) | 2u: R = d_iszero(Q0[i][j]) ? 0.0 : CGB_OP(cur.z, j, k); break;
-      // one jump-table dispatch on (kind, active operands): every case holds only the FP64
-      // operations it needs, so nothing is computed speculatively (an FP64 instruction holds
-      // a sub-partition's FP64 unit for ~64 cycles on GB300)
-      const unsigned key = (ent_kind(meta) << 2) | (ent_flags(meta) & 3u);
-      double r[IPT][K];
-      switch (key) {
-        case (LK_OUTPUT << 2) | 0u:
-        case (LK_OUTPUT << 2) | 1u: {
-          const IoDesc& d = sens[xo];
-          CGB_JK {
-            if (dir0 + k < ndir && active[j] && d.ptr)
-              static_cast<double*>(d.ptr)[io_off(d, dir0 + k, cur.z, ig[j])] =
-                  (meta & 1u) ? CGB_OP(cur.y, j, k) : 0.0;
-          }
-          continue;
-        }
-        case (LK_INPUT << 2) | 1u:
-          if (identity) {
-            CGB_JK r[j][k] = 1.0;
-          } else {
-            const IoDesc& d = seed[cur.y];
-            CGB_JK r[j][k] = (active[j] && dir0 + k < ndir)
-                ? __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir0 + k, cur.z, ig[j]))
-                : 0.0;
-          }
-          break;
-#define CGB_UNIFORM(KEY) \
-case KEY: {            \
-  CGB_JK switch (KEY) { CGB_TAN_CASES(r[j][k], j, k) default: break; } \
-} break;
-        CGB_UNIFORM((LK_GEN << 2) | 1u)
-        CGB_UNIFORM((LK_GEN << 2) | 2u)
-        CGB_UNIFORM((LK_GEN << 2) | 3u)
-        CGB_UNIFORM((LK_ADD << 2) | 1u)
-        CGB_UNIFORM((LK_ADD << 2) | 2u)
-        CGB_UNIFORM((LK_ADD << 2) | 3u)
-        CGB_UNIFORM((LK_SUB << 2) | 1u)
-        CGB_UNIFORM((LK_SUB << 2) | 2u)
-        CGB_UNIFORM((LK_SUB << 2) | 3u)
-        CGB_UNIFORM((LK_NEG << 2) | 1u)
-        CGB_UNIFORM((LK_TWICE << 2) | 1u)
-        CGB_UNIFORM((LK_ASSIGN << 2) | 1u)
-        CGB_UNIFORM((LK_IFZ << 2) | 2u)
-#undef CGB_UNIFORM
-        case (LK_MIXED << 2): {
-          if (K == 1) continue;
-          // directions of the group differ: one dispatch per direction
-          const unsigned rk = (cur.x >> 19) & 15u;
-#pragma unroll
-          for (int k = 0; k < K; ++k) {
-            const unsigned fk = (cur.x >> (24 + 2 * k)) & 3u;
-            if (rk == LK_OUTPUT) {
-              const IoDesc& d = sens[xo];
-#pragma unroll
-              for (int j = 0; j < IPT; ++j)
-                if (dir0 + k < ndir && active[j] && d.ptr)
-                  static_cast<double*>(d.ptr)[io_off(d, dir0 + k, cur.z, ig[j])] =
-                      (fk & 1u) ? CGB_W(cur.y, j, k) : 0.0;
-              continue;
-            }
-            if (!fk) continue;
-            if (rk == LK_INPUT) {
-#pragma unroll
-              for (int j = 0; j < IPT; ++j) {
-                double v = 1.0;
-                if (!identity) {
-                  const IoDesc& d = seed[cur.y];
-                  v = (active[j] && dir0 + k < ndir)
-                      ? __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir0 + k, cur.z, ig[j]))
-                      : 0.0;
-                }
-                CGB_W(xo, j, k) = v;
-              }
-              continue;
-            }
-#pragma unroll
-            for (int j = 0; j < IPT; ++j) {
-              double rr = 0.0;
-              switch ((rk << 2) | fk) {
-                CGB_TAN_CASES(rr, j, k)
-                default: break;
-              }
-              CGB_W(xo, j, k) = rr;
-            }
-          }
-          continue;
-        }
-        default:
-          continue;  // NOP padding
-      }
-      CGB_JK CGB_W(xo, j, k) = r[j][k];
-      if (K == 1) {
-#pragma unroll
-        for (int j = 0; j < IPT; ++j) last[j] = r[j][0];
-      }
-#undef CGB_TAN_CASES
-#undef CGB_JK
-#undef CGB_OP
-#undef CGB_W
-    }
-#pragma unroll
-    for (int i = 0; i < G; ++i) {
-      E0[i] = E1[i];
-      E1[i] = E2[i];
-#pragma unroll
-      for (int j = 0; j < IPT; ++j) {
-        P0[i][j] = P1[i][j];
-        Q0[i][j] = Q1[i][j];
-      }
-    }
+  for (int g = 0; g < ngr; g += 2) {
+    load_grp<G>(st, g + 2, Eb);
+    issue_partials<kNC, G, IPT>(Ea, pt, tstride, tok, Pb, Qb);
+    tan_group<G, IPT, K>(Ea, Pa, Qa, last, wb, seed, sens, identity, active, dir0, ndir, ig);
+    load_grp<G>(st, g + 3, Ea);
+    issue_partials<kNC, G, IPT>(Eb, pt, tstride, tok, Pa, Qa);
+    tan_group<G, IPT, K>(Eb, Pb, Qb, last, wb, seed, sens, identity, active, dir0, ndir, ig);
   }
 }
 
@@ -693,150 +698,105 @@ __global__ void __launch_bounds__(32, MB) k_tangent(const __grid_constant__ Swee
 
 #define CGB_J _Pragma("unroll") for (int j = 0; j < IPT; ++j)
 
-// One adjoint sweep of IPT 32-instance tiles by one warp: entry stream st (ngr groups),
-// recorded partials at pt (lane-offset, first tile; tile j at pt + j*tstride), work vector at
-// wb (lane-offset, w[slot][j][lane]).
+// Adjoint contribution of form F into a slot holding w, from the entry's adjoint s and the
+// operand's partial m.
+template <int F>
+__device__ __forceinline__ double cf_eval(double w, double m, double s) {
+  if constexpr (F == CF_RF) return __dmul_rn(m, s);
+  else if constexpr (F == CF_RA) return __fma_rn(m, s, w);
+  else if constexpr (F == CF_UF) return s;
+  else if constexpr (F == CF_UA) return __dadd_rn(w, s);
+  else if constexpr (F == CF_MF) return d_neg(s);
+  else if constexpr (F == CF_MA) return __dsub_rn(w, s);
+  else if constexpr (F == CF_TF) return d_twice(s);
+  else if constexpr (F == CF_TA) return __dadd_rn(w, d_twice(s));
+  else if constexpr (F == CF_IF) return d_iszero(m) ? 0.0 : s;
+  else return __dadd_rn(w, d_iszero(m) ? 0.0 : s);  // CF_IA
+}
+
+// One group of adjoint entries (IPT tiles, direction dir): keys in E, partials in P/Q. Every
+// slot's first contribution (in sweep order) is assigned, so a slot is never read before it
+// is written and the adjoint read by an entry needs no reset afterwards.
+template <int G, int IPT>
+__device__ __forceinline__ void adj_group(const uint4 (&E)[G], const double (&P)[G][IPT],
+                                          const double (&Q)[G][IPT], unsigned char* wb,
+                                          const IoDesc* seed, const IoDesc* sens,
+                                          const bool (&active)[IPT], long long dir,
+                                          const long long (&ig)[IPT]) {
+#pragma unroll
+  for (int i = 0; i < G; ++i) {
+    const uint4 cur = E[i];
+    switch (ent_key(cur.w)) {
+      case AK_OUT_SET:
+      case AK_OUT_ADD: {
+        const IoDesc& d = seed[cur.x];
+        CGB_J {
+          const double sd = active[j]
+              ? __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir, cur.z, ig[j])) : 0.0;
+          double& w = wj<IPT>(wb, cur.y, j);
+          w = ent_key(cur.w) == AK_OUT_SET ? sd : __dadd_rn(w, sd);
+        }
+      } break;
+      case AK_IN: {
+        const IoDesc& d = sens[cur.y];
+        CGB_J {
+          if (active[j] && d.ptr)
+            static_cast<double*>(d.ptr)[io_off(d, dir, cur.z, ig[j])] = wj<IPT>(wb, cur.x, j);
+        }
+      } break;
+#define CGB_AK_CASE(KEY, BF, CF)                                     \
+  case KEY:                                                          \
+    CGB_J {                                                          \
+      const double sd = wj<IPT>(wb, cur.x, j);                       \
+      if constexpr (BF != CF_N) {                                    \
+        double& w1 = wj<IPT>(wb, cur.y, j);                          \
+        w1 = cf_eval<BF>(cf_reads(BF) ? w1 : 0.0, P[i][j], sd);      \
+      }                                                              \
+      if constexpr (CF != CF_N) {                                    \
+        double& w2 = wj<IPT>(wb, cur.z, j);                          \
+        w2 = cf_eval<CF>(cf_reads(CF) ? w2 : 0.0, Q[i][j], sd);      \
+      }                                                              \
+    }                                                                \
+    break;
+      CGB_AK_ARITH(CGB_AK_CASE)
+#undef CGB_AK_CASE
+      default:
+        break;  // NOP padding
+    }
+  }
+}
+
+// One adjoint sweep of IPT 32-instance tiles by one warp: keyed stream st (body of ngr groups,
+// ngr even, last instruction first), recorded partials at pt (lane-offset, first tile; tile j
+// at pt + j*tstride), work vector at wb (lane-offset, w[slot][j][lane]).
 template <bool kNC, int G, int IPT>
 __device__ __forceinline__ void adjoint_walk(const uint4* st, int ngr, const double* pt,
                                              size_t tstride, const bool (&tok)[IPT],
                                              unsigned char* wb, const IoDesc* seed,
                                              const IoDesc* sens, const bool (&active)[IPT],
                                              long long dir, const long long (&ig)[IPT]) {
-  uint4 E0[G], E1[G];
-  double P0[G][IPT], Q0[G][IPT];
-  load_group<G>(st, ngr - 1, ngr, E0);
-  load_group<G>(st, ngr - 2 >= 0 ? ngr - 2 : ngr, ngr, E1);
-  load_partials_n<kNC, true, G, IPT>(E0, pt, tstride, tok, P0, Q0);
+  uint4 Ea[G], Eb[G];
+  double Pa[G][IPT], Qa[G][IPT], Pb[G][IPT], Qb[G][IPT];
+#pragma unroll
+  for (int i = 0; i < G; ++i)
+#pragma unroll
+    for (int j = 0; j < IPT; ++j) Pa[i][j] = Qa[i][j] = Pb[i][j] = Qb[i][j] = 0.0;
+  load_grp<G>(st, 0, Eb);  // the header: the first group's partials
+  issue_partials<kNC, G, IPT>(Eb, pt, tstride, tok, Pa, Qa);
+  load_grp<G>(st, 1, Ea);
 #pragma unroll 1
-  for (int g = ngr - 1; g >= 0; --g) {
-    uint4 E2[G];
-    double P1[G][IPT], Q1[G][IPT];
-    load_group<G>(st, g - 2 >= 0 ? g - 2 : ngr, ngr, E2);
-    load_partials_n<kNC, true, G, IPT>(E1, pt, tstride, tok, P1, Q1);
-#pragma unroll
-    for (int i = G - 1; i >= 0; --i) {
-      const uint4 cur = E0[i];
-      const unsigned meta = cur.w;
-      const unsigned f = ent_flags(meta);
-      const unsigned kind = ent_kind(meta);
-      // first contributions are assigned (0 + x -> x); dispatch on (kind, flags) so only the
-      // FP64 operations a case needs are issued
-      switch (kind) {
-        case LK_OUTPUT: {
-          const IoDesc& d = seed[cur.x];
-          CGB_J {
-            const double sd = active[j]
-                ? __ldg(static_cast<const double*>(d.ptr) + io_off(d, dir, cur.z, ig[j])) : 0.0;
-            double& w = wj<IPT>(wb, cur.y, j);
-            if (f & 8u) w = sd; else w = __dadd_rn(w, sd);
-          }
-        } break;
-        case LK_INPUT: {
-          const IoDesc& d = sens[cur.y];
-          CGB_J {
-            if (active[j] && d.ptr)
-              static_cast<double*>(d.ptr)[io_off(d, dir, cur.z, ig[j])] = wj<IPT>(wb, cur.x, j);
-            wj<IPT>(wb, cur.x, j) = 0.0;
-          }
-        } break;
-        case LK_CONST:
-          CGB_J wj<IPT>(wb, cur.x, j) = 0.0;
-          break;
-        case LK_NOP:
-          break;
-        default: {
-          double sd[IPT];
-          CGB_J {
-            sd[j] = wj<IPT>(wb, cur.x, j);
-            wj<IPT>(wb, cur.x, j) = 0.0;
-          }
-          // contribution to operand b
-          switch ((kind << 2) | ((f >> 1) & 1u) | ((f >> 2) & 2u)) {  // (kind, b?, first?)
-            case (LK_GEN << 2) | 1u:
-              CGB_J {
-                double& w1 = wj<IPT>(wb, cur.y, j);
-                w1 = __fma_rn(P0[i][j], sd[j], w1);
-              }
-              break;
-            case (LK_GEN << 2) | 3u: CGB_J wj<IPT>(wb, cur.y, j) = __dmul_rn(P0[i][j], sd[j]); break;
-            case (LK_ADD << 2) | 1u: case (LK_SUB << 2) | 1u: case (LK_ASSIGN << 2) | 1u:
-              CGB_J {
-                double& w1 = wj<IPT>(wb, cur.y, j);
-                w1 = __dadd_rn(w1, sd[j]);
-              }
-              break;
-            case (LK_ADD << 2) | 3u: case (LK_SUB << 2) | 3u: case (LK_ASSIGN << 2) | 3u:
-              CGB_J wj<IPT>(wb, cur.y, j) = sd[j];
-              break;
-            case (LK_NEG << 2) | 1u:
-              CGB_J {
-                double& w1 = wj<IPT>(wb, cur.y, j);
-                w1 = __dsub_rn(w1, sd[j]);
-              }
-              break;
-            case (LK_NEG << 2) | 3u: CGB_J wj<IPT>(wb, cur.y, j) = d_neg(sd[j]); break;
-            case (LK_TWICE << 2) | 1u:
-              CGB_J {
-                double& w1 = wj<IPT>(wb, cur.y, j);
-                w1 = __dadd_rn(w1, d_twice(sd[j]));
-              }
-              break;
-            case (LK_TWICE << 2) | 3u: CGB_J wj<IPT>(wb, cur.y, j) = d_twice(sd[j]); break;
-            default: break;  // operand b receives nothing
-          }
-          // contribution to operand c
-          switch ((kind << 2) | ((f >> 2) & 1u) | ((f >> 3) & 2u)) {  // (kind, c?, first?)
-            case (LK_GEN << 2) | 1u:
-              CGB_J {
-                double& w2 = wj<IPT>(wb, cur.z, j);
-                w2 = __fma_rn(Q0[i][j], sd[j], w2);
-              }
-              break;
-            case (LK_GEN << 2) | 3u: CGB_J wj<IPT>(wb, cur.z, j) = __dmul_rn(Q0[i][j], sd[j]); break;
-            case (LK_ADD << 2) | 1u:
-              CGB_J {
-                double& w2 = wj<IPT>(wb, cur.z, j);
-                w2 = __dadd_rn(w2, sd[j]);
-              }
-              break;
-            case (LK_ADD << 2) | 3u: CGB_J wj<IPT>(wb, cur.z, j) = sd[j]; break;
-            case (LK_SUB << 2) | 1u:
-              CGB_J {
-                double& w2 = wj<IPT>(wb, cur.z, j);
-                w2 = __dsub_rn(w2, sd[j]);
-              }
-              break;
-            case (LK_SUB << 2) | 3u: CGB_J wj<IPT>(wb, cur.z, j) = d_neg(sd[j]); break;
-            case (LK_IFZ << 2) | 1u:
-              CGB_J {
-                double& w2 = wj<IPT>(wb, cur.z, j);
-                if (!d_iszero(Q0[i][j])) w2 = __dadd_rn(w2, sd[j]);
-                else w2 = __dadd_rn(w2, 0.0);
-              }
-              break;
-            case (LK_IFZ << 2) | 3u:
-              CGB_J wj<IPT>(wb, cur.z, j) = d_iszero(Q0[i][j]) ? 0.0 : sd[j];
-              break;
-            default: break;  // operand c receives nothing
-          }
-        }
-      }
-    }
-#pragma unroll
-    for (int i = 0; i < G; ++i) {
-      E0[i] = E1[i];
-      E1[i] = E2[i];
-#pragma unroll
-      for (int j = 0; j < IPT; ++j) {
-        P0[i][j] = P1[i][j];
-        Q0[i][j] = Q1[i][j];
-      }
-    }
+  for (int g = 0; g < ngr; g += 2) {
+    load_grp<G>(st, g + 2, Eb);
+    issue_partials<kNC, G, IPT>(Ea, pt, tstride, tok, Pb, Qb);
+    adj_group<G, IPT>(Ea, Pa, Qa, wb, seed, sens, active, dir, ig);
+    load_grp<G>(st, g + 3, Ea);
+    issue_partials<kNC, G, IPT>(Eb, pt, tstride, tok, Pa, Qa);
+    adj_group<G, IPT>(Eb, Pb, Qb, wb, seed, sens, active, dir, ig);
   }
 }
 
-// Flags (bits 0-4): 2/4 operand b/c receives a contribution, 8/16 it is the first one
-// (1 marks an entry with work; outputs carry 8 when their seed is the slot's first).
+// Adjoint sweep: a warp takes one work item (IPT tiles, one direction) at a time and walks the
+// keyed adjoint stream over the tiles' recorded partials.
 template <int G, int MB, int IPT, bool GW = false>
 __global__ void __launch_bounds__(32, MB) k_adjoint(const __grid_constant__ SweepArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
@@ -1164,13 +1124,40 @@ int adj_variant_ipt(int variant) {
   }
 }
 
+// The launch's arguments with the keyed streams laid out for group size G.
+SweepArgs with_group(const SweepArgs& a, int g) {
+  SweepArgs b = a;
+  b.dstream = a.dstreams[group_slot(g)];
+  b.dchunks = a.dchunkss[group_slot(g)];
+  return b;
+}
+
+int tan_variant_group(int variant) {
+  switch (variant) {
+#define CGB_G(V, G, MB, IPT, K) case V: return G;
+    CGB_TAN_VARIANTS(CGB_G)
+#undef CGB_G
+    default: return 2;
+  }
+}
+
+int adj_variant_group(int variant) {
+  switch (variant) {
+#define CGB_G(V, G, MB, IPT) case V: return G;
+    CGB_ADJ_VARIANTS(CGB_G)
+#undef CGB_G
+    default: return 2;
+  }
+}
+
 cudaError_t launch_tangent(const SweepArgs& a, int grid, int variant, cudaStream_t s) {
-  if (a.wglob) return launch_k(k_tangent<2, 32, 1, 1, true>, dim3(grid), 32, 0, a, s);
+  if (a.wglob)
+    return launch_k(k_tangent<2, 32, 1, 1, true>, dim3(grid), 32, 0, with_group(a, 2), s);
   switch (variant) {
 #define CGB_LAUNCH(V, G, MB, IPT, K)                                                          \
   case V:                                                                                     \
     return launch_k(k_tangent<G, MB, IPT, K>, dim3(grid), 32, smem_lean(a.t.sz_w, IPT * K, 0), \
-                    a, s);
+                    with_group(a, G), s);
     CGB_TAN_VARIANTS(CGB_LAUNCH)
 #undef CGB_LAUNCH
     default: return cudaErrorInvalidValue;
@@ -1193,11 +1180,13 @@ cudaError_t launch_tangent_win(const SweepArgs& a, int grid, cudaStream_t s) {
 }
 
 cudaError_t launch_adjoint(const SweepArgs& a, int grid, int variant, cudaStream_t s) {
-  if (a.wglob) return launch_k(k_adjoint<2, 32, 1, true>, dim3(grid), 32, 0, a, s);
+  if (a.wglob)
+    return launch_k(k_adjoint<2, 32, 1, true>, dim3(grid), 32, 0, with_group(a, 2), s);
   switch (variant) {
-#define CGB_LAUNCH(V, G, MB, IPT)                                                              \
-  case V:                                                                                      \
-    return launch_k(k_adjoint<G, MB, IPT>, dim3(grid), 32, smem_lean(a.t.sz_w, IPT, 0), a, s);
+#define CGB_LAUNCH(V, G, MB, IPT)                                                       \
+  case V:                                                                               \
+    return launch_k(k_adjoint<G, MB, IPT>, dim3(grid), 32, smem_lean(a.t.sz_w, IPT, 0), \
+                    with_group(a, G), s);
     CGB_ADJ_VARIANTS(CGB_LAUNCH)
 #undef CGB_LAUNCH
     default: return cudaErrorInvalidValue;

@@ -10,16 +10,129 @@ namespace cgb {
 constexpr int kChunk = 256;      // instructions per staged chunk (2 KiB), value sweeps
 constexpr int kPofsGran = 16;    // granularity of the per-chunk partial offsets
 constexpr int kLeanPB = 63;      // partials per staged chunk block (plan-free adjoint)
-constexpr int kEntGroup = 8;     // entry streams are padded to a multiple of this
-constexpr int kBatchGroup = 4;   // entries per software-pipelined group in the batch kernel
+// entries per software-pipelined group of the batch kernel's tangent and adjoint walks: small
+// groups keep the kernel's code (value walk and both keyed walks) small; the tangent walk
+// of the coloured MPC items wants two entries of partial loads in flight
+constexpr int kBatchTanGroup = 2;
+constexpr int kBatchAdjGroup = 1;
 constexpr unsigned kMaxPartials = 1u << 21;  // recorded partials per instance the entries address
 
-// Entry kinds of the lean derivative streams (bits 16-19 of an entry's meta word).
+// Instruction kinds of the derivative sweeps (the windowed tangent sweep's entries carry them
+// in bits 5-8 of their meta word; mixed tangent entries in bits 19-22 of x).
 enum LeanKind : unsigned {
   LK_NOP = 0, LK_GEN, LK_ADD, LK_SUB, LK_NEG, LK_TWICE, LK_ASSIGN, LK_IFZ, LK_INPUT, LK_OUTPUT,
   LK_CONST, LK_MIXED
 };
 constexpr int kMaxIo = 64;       // inputs/outputs per tape handled by one launch
+
+// ---------------------------------------------------------------------------------------------
+// Keyed entry streams of the tangent and adjoint walks. An entry is {x, y, z, w}: x the slot
+// the entry writes (tangent) or whose adjoint it reads (adjoint), y and z its operand slots,
+// all as byte offsets into the warp's work vector (slot * 256); inputs and outputs put their
+// I/O index and nonzero in the fields the walks name. w bits 0-5 are the entry's key, the
+// walk's jump-table case: the arithmetic form, and for the tangent which operand is the
+// previous entry's result (held in a register), for the adjoint which operand receives its
+// first contribution. w bits 6-31 describe the recorded partials of the entry G positions
+// later (G: entries per pipeline group of the walk that reads the stream), so a walk issues
+// the loads of group g+1 while group g computes, with no decoding of g+1's entries first:
+// bit 6 load P, bit 7 load Q, bit 8 Q is the partial after P's (otherwise at P's index),
+// bits 9-31 P's partial index. A stream for group size G is a header group (no work; it carries
+// the first group's partials), the body (an even number of groups, NOP-padded) and one
+// trailing NOP group: the walks unroll two groups per iteration and read one group past the
+// body. Key 0 is NOP in both walks.
+// ---------------------------------------------------------------------------------------------
+constexpr int kNumGroupSizes = 4;  // streams are laid out for G = 1, 2, 4, 8
+__host__ __device__ constexpr int group_slot(int g) { return g >= 8 ? 3 : g >= 4 ? 2 : g >= 2 ? 1 : 0; }
+__host__ __device__ constexpr unsigned ent_key(unsigned w) { return w & 63u; }
+constexpr unsigned kPiP = 1u, kPiQ = 2u, kPiQNext = 4u;  // partial-info bits (w >> 6)
+constexpr unsigned kPiShift = 6, kPiIndexShift = 9;
+
+// Tangent forms: the tangent of one arithmetic entry from operand tangents a (y) and b (z) and
+// the recorded partials p (d0) and q (d1).
+enum TanForm : int {
+  TF_PY,    // p*a                     (recorded d0)
+  TF_QZ,    // q*b                     (recorded d1)
+  TF_PYQZ,  // fma(p, a, q*b)
+  TF_Y,     // a                       (d0 = 1: ADD, SUB, ASSIGN and GEN ops with a unit d0)
+  TF_Z,     // b                       (ADD)
+  TF_YQZ,   // a + q*b                 (d0 = 1, d1 recorded: FMOD, REMAINDER)
+  TF_YZ,    // a + b                   (ADD)
+  TF_NZ,    // -b                      (SUB)
+  TF_YMZ,   // a - b                   (SUB)
+  TF_NY,    // -a                      (NEG)
+  TF_2Y,    // 2a                      (TWICE)
+  TF_IFZ    // q == 0 ? 0 : b          (IF_ELSE_ZERO)
+};
+__host__ __device__ constexpr bool tf_uses_y(int f) {
+  return f == TF_PY || f == TF_PYQZ || f == TF_Y || f == TF_YQZ || f == TF_YZ || f == TF_YMZ ||
+         f == TF_NY || f == TF_2Y;
+}
+__host__ __device__ constexpr bool tf_uses_z(int f) {
+  return f == TF_QZ || f == TF_PYQZ || f == TF_Z || f == TF_YQZ || f == TF_YZ || f == TF_NZ ||
+         f == TF_YMZ || f == TF_IFZ;
+}
+__host__ __device__ constexpr bool tf_uses_p(int f) { return f == TF_PY || f == TF_PYQZ; }
+__host__ __device__ constexpr bool tf_uses_q(int f) {
+  return f == TF_QZ || f == TF_PYQZ || f == TF_YQZ || f == TF_IFZ;
+}
+// Arithmetic tangent keys: (key, form, y forwarded, z forwarded).
+#define CGB_TK_ARITH(X)                                                                      \
+  X(TK_PY, TF_PY, 0, 0) X(TK_PY_F, TF_PY, 1, 0)                                              \
+  X(TK_QZ, TF_QZ, 0, 0) X(TK_QZ_F, TF_QZ, 0, 1)                                              \
+  X(TK_Y, TF_Y, 0, 0) X(TK_Y_F, TF_Y, 1, 0)                                                  \
+  X(TK_Z, TF_Z, 0, 0) X(TK_Z_F, TF_Z, 0, 1)                                                  \
+  X(TK_NZ, TF_NZ, 0, 0) X(TK_NZ_F, TF_NZ, 0, 1)                                              \
+  X(TK_NY, TF_NY, 0, 0) X(TK_NY_F, TF_NY, 1, 0)                                              \
+  X(TK_2Y, TF_2Y, 0, 0) X(TK_2Y_F, TF_2Y, 1, 0)                                              \
+  X(TK_IFZ, TF_IFZ, 0, 0) X(TK_IFZ_F, TF_IFZ, 0, 1)                                          \
+  X(TK_PYQZ, TF_PYQZ, 0, 0) X(TK_PYQZ_FS, TF_PYQZ, 1, 0) X(TK_PYQZ_SF, TF_PYQZ, 0, 1)        \
+  X(TK_PYQZ_FF, TF_PYQZ, 1, 1)                                                               \
+  X(TK_YQZ, TF_YQZ, 0, 0) X(TK_YQZ_FS, TF_YQZ, 1, 0) X(TK_YQZ_SF, TF_YQZ, 0, 1)              \
+  X(TK_YQZ_FF, TF_YQZ, 1, 1)                                                                 \
+  X(TK_YZ, TF_YZ, 0, 0) X(TK_YZ_FS, TF_YZ, 1, 0) X(TK_YZ_SF, TF_YZ, 0, 1)                    \
+  X(TK_YZ_FF, TF_YZ, 1, 1)                                                                   \
+  X(TK_YMZ, TF_YMZ, 0, 0) X(TK_YMZ_FS, TF_YMZ, 1, 0) X(TK_YMZ_SF, TF_YMZ, 0, 1)              \
+  X(TK_YMZ_FF, TF_YMZ, 1, 1)
+#define CGB_KEY_ENUM(K, ...) K,
+// TK_OUT0/TK_OUT/TK_OUT_F: an output's sensitivity (x output, y slot, z nonzero) is 0, the
+// slot's tangent, or the previous result; TK_IN: an input's seed (x slot, y input, z
+// nonzero); TK_MIXED + pm: a union-stream entry whose flags differ between the directions
+// (x bits 19-22 kind, 24+2k flags of direction k), pm its recorded-partial mask.
+enum TanKey : unsigned {
+  TK_NOP = 0, TK_OUT0, TK_OUT, TK_OUT_F, TK_IN, TK_MIXED, TK_MIXED_LAST = TK_MIXED + 3,
+  CGB_TK_ARITH(CGB_KEY_ENUM) TK_COUNT
+};
+static_assert(TK_COUNT <= 64, "tangent keys fit 6 bits");
+
+// Adjoint contributions of one entry to an operand slot w, from the entry's adjoint s and the
+// operand's partial m: R recorded partial, U unit (ADD, SUB's first operand, ASSIGN and GEN ops
+// with a unit d0), M minus one (NEG, SUB's second operand), T two (TWICE), I IF_ELSE_ZERO
+// (s unless m is zero); F the slot's first contribution (assigned), A a later one (added).
+enum AdjForm : int { CF_N, CF_RF, CF_RA, CF_UF, CF_UA, CF_MF, CF_MA, CF_TF, CF_TA, CF_IF, CF_IA };
+__host__ __device__ constexpr bool cf_reads(int f) {
+  return f == CF_RA || f == CF_UA || f == CF_MA || f == CF_TA || f == CF_IA;
+}
+// Arithmetic adjoint keys: (key, contribution to y, contribution to z).
+#define CGB_AK_ARITH(X)                                                                      \
+  X(AK_RF_N, CF_RF, CF_N) X(AK_RF_RF, CF_RF, CF_RF) X(AK_RF_RA, CF_RF, CF_RA)                \
+  X(AK_RA_N, CF_RA, CF_N) X(AK_RA_RF, CF_RA, CF_RF) X(AK_RA_RA, CF_RA, CF_RA)                \
+  X(AK_UF_N, CF_UF, CF_N) X(AK_UF_RF, CF_UF, CF_RF) X(AK_UF_RA, CF_UF, CF_RA)                \
+  X(AK_UF_UF, CF_UF, CF_UF) X(AK_UF_UA, CF_UF, CF_UA) X(AK_UF_MF, CF_UF, CF_MF)              \
+  X(AK_UF_MA, CF_UF, CF_MA)                                                                  \
+  X(AK_UA_N, CF_UA, CF_N) X(AK_UA_RF, CF_UA, CF_RF) X(AK_UA_RA, CF_UA, CF_RA)                \
+  X(AK_UA_UF, CF_UA, CF_UF) X(AK_UA_UA, CF_UA, CF_UA) X(AK_UA_MF, CF_UA, CF_MF)              \
+  X(AK_UA_MA, CF_UA, CF_MA)                                                                  \
+  X(AK_MF_N, CF_MF, CF_N) X(AK_MA_N, CF_MA, CF_N) X(AK_TF_N, CF_TF, CF_N)                    \
+  X(AK_TA_N, CF_TA, CF_N)                                                                    \
+  X(AK_N_RF, CF_N, CF_RF) X(AK_N_RA, CF_N, CF_RA) X(AK_N_IF, CF_N, CF_IF)                    \
+  X(AK_N_IA, CF_N, CF_IA)
+// AK_OUT_SET/AK_OUT_ADD: an output's seed (x output, y slot, z nonzero) assigned to or added
+// into the slot's adjoint; AK_IN: an input's sensitivity (x slot, y input, z nonzero).
+enum AdjKey : unsigned {
+  AK_NOP = 0, AK_OUT_SET, AK_OUT_ADD, AK_IN, CGB_AK_ARITH(CGB_KEY_ENUM) AK_COUNT
+};
+static_assert(AK_COUNT <= 64, "adjoint keys fit 6 bits");
+#undef CGB_KEY_ENUM
 
 // One input/output block: element (direction d, nonzero k, instance i) lives at
 // ptr[d*dir_stride + k*nz_stride + i*inst_stride].
@@ -75,9 +188,13 @@ struct SweepArgs {
   int in_off[kMaxIo];       // flat offset of each input's first nonzero (identity seeds)
   const int2* zero_in;              // adjoint: (input, nonzero) pairs with a zero sensitivity
   int n_zero;
-  // derivative entry streams (host-compiled; see the derivative sweeps)
+  // keyed entry streams (host-compiled, one layout per group size; the launchers pick the
+  // variant's into dstream/dchunks)
   const uint4* dstream;             // entries of all streams
-  const int2* dchunks;              // per direction (tangent) or one (adjoint): first entry, count
+  const int2* dchunks;              // per direction (tangent) or one (adjoint): first entry,
+                                    // body entries
+  const uint4* dstreams[kNumGroupSizes];
+  const int2* dchunkss[kNumGroupSizes];
   // global work vector (null: shared memory): CTA b uses wglob + b*wglob_stride
   unsigned char* wglob;
   long long wglob_stride;
@@ -109,7 +226,7 @@ struct BatchItem {
   long long n;              // instances
   const IoDesc* io;         // 4*kMaxIo descriptors: inputs, outputs, seeds, sensitivities
   const uint4* adj_stream;  // adjoint entry stream (ndir > 0, !forward)
-  int adj_ngr;              // its groups of kBatchGroup entries
+  int adj_ngr;              // its groups of kBatchAdjGroup entries
   const int2* zero_in;      // inputs with a structurally zero adjoint
   int n_zero;
   const uint4* tan_stream;  // tangent entry streams (forward)
@@ -172,6 +289,9 @@ enum AdjVariant : int {
 };
 void tan_variant_shape(int variant, int* ipt, int* k);
 int adj_variant_ipt(int variant);
+// entries per pipeline group (G) of a variant: the keyed-stream layout it reads
+int tan_variant_group(int variant);
+int adj_variant_group(int variant);
 cudaError_t launch_tangent(const SweepArgs& a, int grid, int variant, cudaStream_t s);
 // Windowed tangent sweep: one CTA per SM of a warp that stages, window by window, a tile's
 // recorded partials and the window's entry block into a shared-memory ring with bulk copies,

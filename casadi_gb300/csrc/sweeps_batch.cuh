@@ -144,12 +144,12 @@ __global__ void __launch_bounds__(32, 16) k_batch(const __grid_constant__ BatchA
     for (int dir = d0; dir < d1; ++dir) {
       if (it.forward) {
         const int2 se = __ldg(it.tan_chunks + dir);
-        tangent_walk<false, kBatchGroup, 1, 1>(it.tan_stream + se.x, se.y / kBatchGroup, pt, 0,
-                                               tok1, wb, io + 2 * kMaxIo, io + 3 * kMaxIo, true,
-                                               act1, dir, it.ndir, ig1);
+        tangent_walk<false, kBatchTanGroup, 1, 1>(it.tan_stream + se.x, se.y / kBatchTanGroup,
+                                                  pt, 0, tok1, wb, io + 2 * kMaxIo,
+                                                  io + 3 * kMaxIo, true, act1, dir, it.ndir, ig1);
         continue;
       }
-      for (int q = 0; q < it.t.sz_w; ++q) wreg(wb, q * 256u) = 0.0;
+      // (the work vector needs no clearing: the adjoint walk assigns every slot before reading)
       if (active) {
         for (int k = 0; k < it.n_zero; ++k) {
           const int2 jk = __ldg(it.zero_in + k);
@@ -157,8 +157,8 @@ __global__ void __launch_bounds__(32, 16) k_batch(const __grid_constant__ BatchA
           if (d.ptr) static_cast<double*>(d.ptr)[io_off(d, dir, jk.y, il)] = 0.0;
         }
       }
-      adjoint_walk<false, kBatchGroup, 1>(it.adj_stream, it.adj_ngr, pt, 0, tok1, wb,
-                                          io + 2 * kMaxIo, io + 3 * kMaxIo, act1, dir, ig1);
+      adjoint_walk<false, kBatchAdjGroup, 1>(it.adj_stream, it.adj_ngr, pt, 0, tok1, wb,
+                                             io + 2 * kMaxIo, io + 3 * kMaxIo, act1, dir, ig1);
     }
   }
 }
