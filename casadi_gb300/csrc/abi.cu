@@ -614,12 +614,12 @@ constexpr int kGroupSizeOf[kNumGroupSizes] = {1, 2, 4, 8};
 
 // Tangent entry before keying: fields as the walks read them, the instruction's kind, flags
 // (1/2: operand b/c carries a derivative; inputs/outputs: 1 active), recorded-partial mask and
-// first partial, and whether an operand is the previous result (one-direction streams).
+// first partial.
 struct TanRaw {
   unsigned x = 0, y = 0, z = 0;
   unsigned op = 0, kind = 0, f = 0, pm = 0;
   int pk = 0;
-  bool mixed = false, yf = false, zf = false;
+  bool mixed = false;
 };
 
 TanRaw tan_raw(u64 w, unsigned flags, int pk) {
@@ -638,32 +638,6 @@ TanRaw tan_raw(u64 w, unsigned flags, int pk) {
   e.pm = dec_pmask(w);
   e.pk = pk;
   return e;
-}
-
-// Operand forwarding in a one-direction tangent stream: an operand that is the value the
-// previous value-writing entry (an input or an arithmetic entry) just computed is read from
-// the register holding it instead of from shared memory.
-void forward_raw(std::vector<TanRaw>& ents) {
-  bool have = false;
-  unsigned last = 0;  // slot byte offset the previous value-writing entry wrote
-  for (TanRaw& e : ents) {
-    if (e.kind == LK_OUTPUT) {
-      e.yf = have && (e.f & 1u) && e.y == last;
-      continue;
-    }
-    if (e.kind == LK_INPUT) {
-      if (e.f & 1u) {
-        have = true;
-        last = e.x;
-      }
-      continue;
-    }
-    if (e.kind == LK_NOP || e.kind == LK_CONST || !e.f) continue;
-    e.yf = have && (e.f & 1u) && e.y == last;
-    e.zf = have && (e.f & 2u) && e.z == last;
-    have = true;
-    last = e.x;
-  }
 }
 
 // Tangent form of an arithmetic entry (-1: none). GEN ops whose d0 is a constant 1 and not
@@ -689,11 +663,9 @@ int tan_form(const TanRaw& e) {
   }
 }
 
-unsigned tan_key_of(int form, bool yf, bool zf) {
-  yf = yf && tf_uses_y(form);
-  zf = zf && tf_uses_z(form);
-#define CGB_FIND(KEY, F, YF, ZF) \
-  if (form == (F) && yf == ((YF) != 0) && zf == ((ZF) != 0)) return KEY;
+unsigned tan_key_of(int form) {
+#define CGB_FIND(KEY, F) \
+  if (form == (F)) return KEY;
   CGB_TK_ARITH(CGB_FIND)
 #undef CGB_FIND
   return ~0u;
@@ -709,7 +681,7 @@ bool tan_keyed(const TanRaw& e, KEnt* k) {
     return true;
   }
   if (e.kind == LK_OUTPUT) {
-    k->key = !(e.f & 1u) ? TK_OUT0 : e.yf ? TK_OUT_F : TK_OUT;
+    k->key = (e.f & 1u) ? TK_OUT : TK_OUT0;
     return true;
   }
   if (e.kind == LK_INPUT) {
@@ -718,7 +690,7 @@ bool tan_keyed(const TanRaw& e, KEnt* k) {
   }
   const int form = tan_form(e);
   if (form < 0) return false;
-  k->key = tan_key_of(form, e.yf, e.zf);
+  k->key = tan_key_of(form);
   k->pinfo = pinfo_of(tf_uses_p(form), tf_uses_q(form), e.pm, e.pk);
   return k->key != ~0u;
 }
@@ -902,7 +874,6 @@ const TanPlan* tan_plan(Tape& t, int ndir, int dw, int ch, bool identity,
         raw.push_back(e);
       }
     }
-    if (dw == 1) forward_raw(raw);
     std::vector<KEnt> ents(raw.size());
     for (size_t q = 0; q < raw.size(); ++q)
       if (!tan_keyed(raw[q], &ents[q])) {

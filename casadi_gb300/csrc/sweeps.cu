@@ -500,12 +500,10 @@ __device__ __forceinline__ double tan_mixed(unsigned rk, unsigned fk, double p, 
 constexpr unsigned kTanXMask = (1u << 19) - 1;
 
 // One group of tangent entries (IPT tiles, K directions dir0..): their keys in E, their
-// partials in P/Q. `last` holds the previous arithmetic or input entry's result (one-direction
-// streams only).
+// partials in P/Q.
 template <int G, int IPT, int K>
 __device__ __forceinline__ void tan_group(const uint4 (&E)[G], const double (&P)[G][IPT],
-                                          const double (&Q)[G][IPT], double (&last)[IPT],
-                                          unsigned char* wb, const IoDesc* seed,
+                                          const double (&Q)[G][IPT], unsigned char* wb, const IoDesc* seed,
                                           const IoDesc* sens, bool identity,
                                           const bool (&active)[IPT], int dir0, int ndir,
                                           const long long (&ig)[IPT]) {
@@ -519,13 +517,12 @@ __device__ __forceinline__ void tan_group(const uint4 (&E)[G], const double (&P)
     double r[IPT][K];
     switch (key) {
       case TK_OUT0:
-      case TK_OUT:
-      case TK_OUT_F: {
+      case TK_OUT: {
         const IoDesc& d = sens[xo];
         CGB_JK {
           if (dir0 + k < ndir && active[j] && d.ptr)
             static_cast<double*>(d.ptr)[io_off(d, dir0 + k, cur.z, ig[j])] =
-                key == TK_OUT ? CGB_W(cur.y, j, k) : key == TK_OUT_F ? last[j] : 0.0;
+                key == TK_OUT ? CGB_W(cur.y, j, k) : 0.0;
         }
         continue;
       }
@@ -539,13 +536,13 @@ __device__ __forceinline__ void tan_group(const uint4 (&E)[G], const double (&P)
               : 0.0;
         }
         break;
-#define CGB_TK_CASE(KEY, F, YF, ZF)                                                  \
-  case KEY:                                                                          \
-    CGB_JK {                                                                         \
-      const double av = tf_uses_y(F) ? ((YF) ? last[j] : CGB_W(cur.y, j, k)) : 0.0;  \
-      const double bv = tf_uses_z(F) ? ((ZF) ? last[j] : CGB_W(cur.z, j, k)) : 0.0;  \
-      r[j][k] = tf_eval<F>(P[i][j], Q[i][j], av, bv);                                \
-    }                                                                                \
+#define CGB_TK_CASE(KEY, F)                                              \
+  case KEY:                                                              \
+    CGB_JK {                                                             \
+      const double av = tf_uses_y(F) ? CGB_W(cur.y, j, k) : 0.0;         \
+      const double bv = tf_uses_z(F) ? CGB_W(cur.z, j, k) : 0.0;         \
+      r[j][k] = tf_eval<F>(P[i][j], Q[i][j], av, bv);                    \
+    }                                                                    \
     break;
       CGB_TK_ARITH(CGB_TK_CASE)
 #undef CGB_TK_CASE
@@ -598,10 +595,6 @@ __device__ __forceinline__ void tan_group(const uint4 (&E)[G], const double (&P)
         continue;  // NOP padding
     }
     CGB_JK CGB_W(xo, j, k) = r[j][k];
-    if (K == 1) {
-#pragma unroll
-      for (int j = 0; j < IPT; ++j) last[j] = r[j][0];
-    }
   }
 #undef CGB_JK
 #undef CGB_W
@@ -619,13 +612,10 @@ __device__ __forceinline__ void tangent_walk(const uint4* st, int ngr, const dou
                                              const long long (&ig)[IPT]) {
   uint4 Ea[G], Eb[G];
   double Pa[G][IPT], Qa[G][IPT], Pb[G][IPT], Qb[G][IPT];
-  double last[IPT];
 #pragma unroll
   for (int i = 0; i < G; ++i)
 #pragma unroll
     for (int j = 0; j < IPT; ++j) Pa[i][j] = Qa[i][j] = Pb[i][j] = Qb[i][j] = 0.0;
-#pragma unroll
-  for (int j = 0; j < IPT; ++j) last[j] = 0.0;
   load_grp<G>(st, 0, Eb);  // the header: the first group's partials
   issue_partials<kNC, G, IPT>(Eb, pt, tstride, tok, Pa, Qa);
   load_grp<G>(st, 1, Ea);
@@ -633,10 +623,10 @@ __device__ __forceinline__ void tangent_walk(const uint4* st, int ngr, const dou
   for (int g = 0; g < ngr; g += 2) {
     load_grp<G>(st, g + 2, Eb);
     issue_partials<kNC, G, IPT>(Ea, pt, tstride, tok, Pb, Qb);
-    tan_group<G, IPT, K>(Ea, Pa, Qa, last, wb, seed, sens, identity, active, dir0, ndir, ig);
+    tan_group<G, IPT, K>(Ea, Pa, Qa, wb, seed, sens, identity, active, dir0, ndir, ig);
     load_grp<G>(st, g + 3, Ea);
     issue_partials<kNC, G, IPT>(Eb, pt, tstride, tok, Pa, Qa);
-    tan_group<G, IPT, K>(Eb, Pb, Qb, last, wb, seed, sens, identity, active, dir0, ndir, ig);
+    tan_group<G, IPT, K>(Eb, Pb, Qb, wb, seed, sens, identity, active, dir0, ndir, ig);
   }
 }
 

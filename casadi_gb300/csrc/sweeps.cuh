@@ -30,8 +30,7 @@ constexpr int kMaxIo = 64;       // inputs/outputs per tape handled by one launc
 // the entry writes (tangent) or whose adjoint it reads (adjoint), y and z its operand slots,
 // all as byte offsets into the warp's work vector (slot * 256); inputs and outputs put their
 // I/O index and nonzero in the fields the walks name. w bits 0-5 are the entry's key, the
-// walk's jump-table case: the arithmetic form, and for the tangent which operand is the
-// previous entry's result (held in a register), for the adjoint which operand receives its
+// walk's jump-table case: the arithmetic form, and for the adjoint which operand receives its
 // first contribution. w bits 6-31 describe the recorded partials of the entry G positions
 // later (G: entries per pipeline group of the walk that reads the stream), so a walk issues
 // the loads of group g+1 while group g computes, with no decoding of g+1's entries first:
@@ -75,31 +74,20 @@ __host__ __device__ constexpr bool tf_uses_p(int f) { return f == TF_PY || f == 
 __host__ __device__ constexpr bool tf_uses_q(int f) {
   return f == TF_QZ || f == TF_PYQZ || f == TF_YQZ || f == TF_IFZ;
 }
-// Arithmetic tangent keys: (key, form, y forwarded, z forwarded).
+// Arithmetic tangent keys: (key, form). Operands are read from the work vector: taking the
+// previous result from a register instead (operand forwarding) doubles the cases, and the
+// larger jump tables cost more in instruction fetch than the shared-memory loads they save.
 #define CGB_TK_ARITH(X)                                                                      \
-  X(TK_PY, TF_PY, 0, 0) X(TK_PY_F, TF_PY, 1, 0)                                              \
-  X(TK_QZ, TF_QZ, 0, 0) X(TK_QZ_F, TF_QZ, 0, 1)                                              \
-  X(TK_Y, TF_Y, 0, 0) X(TK_Y_F, TF_Y, 1, 0)                                                  \
-  X(TK_Z, TF_Z, 0, 0) X(TK_Z_F, TF_Z, 0, 1)                                                  \
-  X(TK_NZ, TF_NZ, 0, 0) X(TK_NZ_F, TF_NZ, 0, 1)                                              \
-  X(TK_NY, TF_NY, 0, 0) X(TK_NY_F, TF_NY, 1, 0)                                              \
-  X(TK_2Y, TF_2Y, 0, 0) X(TK_2Y_F, TF_2Y, 1, 0)                                              \
-  X(TK_IFZ, TF_IFZ, 0, 0) X(TK_IFZ_F, TF_IFZ, 0, 1)                                          \
-  X(TK_PYQZ, TF_PYQZ, 0, 0) X(TK_PYQZ_FS, TF_PYQZ, 1, 0) X(TK_PYQZ_SF, TF_PYQZ, 0, 1)        \
-  X(TK_PYQZ_FF, TF_PYQZ, 1, 1)                                                               \
-  X(TK_YQZ, TF_YQZ, 0, 0) X(TK_YQZ_FS, TF_YQZ, 1, 0) X(TK_YQZ_SF, TF_YQZ, 0, 1)              \
-  X(TK_YQZ_FF, TF_YQZ, 1, 1)                                                                 \
-  X(TK_YZ, TF_YZ, 0, 0) X(TK_YZ_FS, TF_YZ, 1, 0) X(TK_YZ_SF, TF_YZ, 0, 1)                    \
-  X(TK_YZ_FF, TF_YZ, 1, 1)                                                                   \
-  X(TK_YMZ, TF_YMZ, 0, 0) X(TK_YMZ_FS, TF_YMZ, 1, 0) X(TK_YMZ_SF, TF_YMZ, 0, 1)              \
-  X(TK_YMZ_FF, TF_YMZ, 1, 1)
+  X(TK_PY, TF_PY) X(TK_QZ, TF_QZ) X(TK_Y, TF_Y) X(TK_Z, TF_Z) X(TK_NZ, TF_NZ)                 \
+  X(TK_NY, TF_NY) X(TK_2Y, TF_2Y) X(TK_IFZ, TF_IFZ) X(TK_PYQZ, TF_PYQZ) X(TK_YQZ, TF_YQZ)    \
+  X(TK_YZ, TF_YZ) X(TK_YMZ, TF_YMZ)
 #define CGB_KEY_ENUM(K, ...) K,
-// TK_OUT0/TK_OUT/TK_OUT_F: an output's sensitivity (x output, y slot, z nonzero) is 0, the
-// slot's tangent, or the previous result; TK_IN: an input's seed (x slot, y input, z
-// nonzero); TK_MIXED + pm: a union-stream entry whose flags differ between the directions
-// (x bits 19-22 kind, 24+2k flags of direction k), pm its recorded-partial mask.
+// TK_OUT0/TK_OUT: an output's sensitivity (x output, y slot, z nonzero) is 0 or the slot's
+// tangent; TK_IN: an input's seed (x slot, y input, z nonzero); TK_MIXED + pm: a union-stream
+// entry whose flags differ between the directions (x bits 19-22 kind, 24+2k flags of
+// direction k), pm its recorded-partial mask.
 enum TanKey : unsigned {
-  TK_NOP = 0, TK_OUT0, TK_OUT, TK_OUT_F, TK_IN, TK_MIXED, TK_MIXED_LAST = TK_MIXED + 3,
+  TK_NOP = 0, TK_OUT0, TK_OUT, TK_IN, TK_MIXED, TK_MIXED_LAST = TK_MIXED + 3,
   CGB_TK_ARITH(CGB_KEY_ENUM) TK_COUNT
 };
 static_assert(TK_COUNT <= 64, "tangent keys fit 6 bits");
