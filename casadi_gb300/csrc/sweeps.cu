@@ -1,10 +1,12 @@
 // Tape-sweep kernels for sm_103a.
 //
-// Every kernel interprets the same instruction stream. It is staged chunk by chunk
+// The value and sparsity sweeps interpret the instruction stream, staged chunk by chunk
 // (kChunk 8-byte words) from global memory into a two-slot shared-memory ring with TMA bulk
-// copies (cp.async.bulk ... mbarrier::complete_tx), while the previous chunk is being
-// interpreted. Every thread of a CTA runs the same instruction on a different instance
-// (or instance/direction pair), so the opcode dispatch is warp-uniform and never diverges.
+// copies (cp.async.bulk ... mbarrier::complete_tx) while the previous chunk is being
+// interpreted; the warp-level derivative sweeps walk host-compiled keyed entry streams over the
+// recorded partials (see "Derivative sweeps, warp-independent" below). Every thread of a CTA
+// runs the same instruction on a different instance (or instance/direction pair), so the
+// dispatch is warp-uniform and never diverges.
 // The work vector lives in shared memory in slot-major order, w[slot*BS + thread]:
 // consecutive lanes hit consecutive 8-byte words, so every work-vector access is
 // bank-conflict free. Instance data in global memory is read and written through IoDesc
@@ -14,8 +16,10 @@
 // Kernels:
 //   k_primal<BS,false>  forward value sweep           SXFunction::eval (sx_function.cpp:110-124)
 //   k_primal<BS,true>   values + recorded partials    (first half of the AD sweeps)
-//   k_tangent<DW>       forward-mode directions       ad_forward, numeric (sx_function.cpp:1318-1364)
-//   k_adjoint<DW>       adjoint directions            ad_reverse, numeric (sx_function.cpp:1454-1560)
+//   k_tangent<G,MB,IPT,K>  forward-mode directions    ad_forward, numeric
+//                                                     (sx_function.cpp:1318-1364)
+//   k_adjoint<G,MB,IPT>    adjoint directions         ad_reverse, numeric
+//                                                     (sx_function.cpp:1454-1560)
 //   k_sp_forward<BS>    bvec_t OR-propagation         sp_forward (sx_function.cpp:1657-1682)
 //   k_sp_forward<BS,GW,true>  activity propagation    eval_activity (sx_function.cpp:1684-1718)
 //   k_sp_reverse<BS>    bvec_t reverse propagation    sp_reverse (sx_function.cpp:1742-1782)
@@ -503,8 +507,8 @@ constexpr unsigned kTanXMask = (1u << 19) - 1;
 // partials in P/Q.
 template <int G, int IPT, int K>
 __device__ __forceinline__ void tan_group(const uint4 (&E)[G], const double (&P)[G][IPT],
-                                          const double (&Q)[G][IPT], unsigned char* wb, const IoDesc* seed,
-                                          const IoDesc* sens, bool identity,
+                                          const double (&Q)[G][IPT], unsigned char* wb,
+                                          const IoDesc* seed, const IoDesc* sens, bool identity,
                                           const bool (&active)[IPT], int dir0, int ndir,
                                           const long long (&ig)[IPT]) {
 #define CGB_W(off, j, k) wj<IPT * K>(wb, (off), (j) * K + (k))

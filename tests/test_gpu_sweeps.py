@@ -128,6 +128,59 @@ def test_ops_grid_values_and_partials(gpu_lib):
         ct.sync()
 
 
+def _twice_op_tape(op):
+    """op(x, y) and op(y, x) (op(x) and op(y) when unary) as two outputs: each operand slot
+    receives two adjoint contributions (assigned, then accumulated), and seeds on x and y
+    activate one or both operands of each instruction."""
+    binary = op in C.BINARY_OPS
+    ops = [C.OP_INPUT, C.OP_INPUT, op, op, C.OP_OUTPUT, C.OP_OUTPUT]
+    i0 = [0, 1, 2, 3, 0, 1]
+    i1 = [0, 1, 0, 1, 2, 3]
+    i2 = [0, 0, 1 if binary else 0, 0 if binary else 1, 0, 0]
+    return S.Tape(ops, i0, i1, i2, [0.0] * 6, [1, 1], [1, 1], 4)
+
+
+def test_ops_grid_tangents_and_accumulated_adjoints(gpu_lib):
+    """Every op's tangent forms (one operand or both carrying a derivative) and adjoint
+    contributions (first and later ones) against the oracle, over the golden grid."""
+    z = load_npz("ops.npz")
+    rng = np.random.default_rng(3)
+    for op in sorted(set(z["op"].tolist())):
+        m = z["op"] == op
+        x, y = z["x"][m][None, :], z["y"][m][None, :]
+        n = x.shape[1]
+        t = _twice_op_tape(op)
+        ct = CudaTape(t)
+        name = C.OP_NAMES[op]
+        tol = {C.OP_ERFINV: 1e-9}.get(op, None)
+
+        def check(got, want, mag, what):
+            # exact ops: bit for bit; libm ops: within 1e-13 (erfinv: 1e-9, see above) of the
+            # magnitude of the chain-rule terms, since the partials of the two libms differ by
+            # an ulp and two contributions can cancel
+            if op in EXACT_OPS:
+                assert_bitexact(got, want, "%s %s" % (name, what))
+            else:
+                assert_close(got, want, "%s %s" % (name, what),
+                             bound=(RTOL if tol is None else tol) * np.asarray(mag))
+
+        # directions: x only, y only, both (general seeds)
+        fseeds = [np.array([1.0, 0.0, 0.7])[:, None, None] * np.ones((3, 1, n)),
+                  np.array([0.0, 1.0, -1.3])[:, None, None] * np.ones((3, 1, n))]
+        _, fs = ct.forward(dev([x, y]), dev(fseeds))
+        _, wfs = O.forward(t, [x, y], fseeds, n, NTHREADS)
+        _, mfs = magnitudes(O.forward, t, [x, y], fseeds, n, NTHREADS)
+        for k, (g, w, mg) in enumerate(zip(host(fs), wfs, mfs)):
+            check(g, w, mg, "tangent of output %d" % k)
+        aseeds = [rng.standard_normal((2, 1, n)), rng.standard_normal((2, 1, n))]
+        _, asn = ct.reverse(dev([x, y]), dev(aseeds))
+        _, was = O.reverse(t, [x, y], aseeds, n, NTHREADS)
+        _, mas = magnitudes(O.reverse, t, [x, y], aseeds, n, NTHREADS)
+        for k, (g, w, mg) in enumerate(zip(host(asn), was, mas)):
+            check(g, w, mg, "adjoint of input %d" % k)
+        ct.sync()
+
+
 # ---- bit-exact on +,-,*,/,sqrt tapes -----------------------------------------------------------
 def _arith_dag(n_in=24, n_nodes=3000, n_out=8, seed=11):
     rng = np.random.default_rng(seed)
