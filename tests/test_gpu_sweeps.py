@@ -508,6 +508,39 @@ def test_every_variant_gives_the_same_bits(gpu_lib):
     ct.sync()
 
 
+def test_linear_tape_with_a_constant_output_every_variant(gpu_lib):
+    """A tape with no recorded partials (ADD, SUB, NEG, TWICE), a constant output (no tangent
+    entries; its adjoint seed lands on a constant's slot) and an unused input: forward,
+    Jacobian and adjoint of every variant against the oracle, bit for bit."""
+    from casadi_gb300 import runtime as R
+    x, u = S.sym("x", 3), S.sym("u", 2)
+    f = S.Function("L", [x, u], [[x[0] + x[1], x[0] - (x[2] + x[2]), -x[1]],
+                                 [S.const(3.0), x[1] - x[0] - x[0]]])
+    t = f.tape
+    assert C.OP_CONST in t.op.tolist() and C.OP_TWICE in t.op.tolist()
+    n = 777
+    rng = np.random.default_rng(5)
+    args = [rng.standard_normal((3, n)), rng.standard_normal((2, n))]
+    fseeds = [rng.standard_normal((3, 3, n)), rng.standard_normal((3, 2, n))]
+    aseeds = [rng.standard_normal((2, 3, n)), rng.standard_normal((2, 2, n))]
+    _, wfs = O.forward(t, args, fseeds, n, NTHREADS)
+    _, was = O.reverse(t, args, aseeds, n, NTHREADS)
+    _, wj = O.jacobian(t, args, n, NTHREADS)
+    ct = CudaTape(t)
+    assert ct.n_partials == 0
+    for v in range(max(R.N_TAN_VARIANTS, R.N_ADJ_VARIANTS)):
+        ct.set_variant(0, min(v, R.N_TAN_VARIANTS - 1))
+        ct.set_variant(1, min(v, R.N_TAN_VARIANTS - 1))
+        ct.set_variant(2, min(v, R.N_ADJ_VARIANTS - 1))
+        for g, w in zip(host(ct.forward(dev(args), dev(fseeds))[1]), wfs):
+            assert_bitexact(g, w, "forward, variant %d" % v)
+        for g, w in zip(host(ct.jacobian(dev(args))[1]), wj):
+            assert_bitexact(g, w, "jacobian, variant %d" % v)
+        for g, w in zip(host(ct.reverse(dev(args), dev(aseeds))[1]), was):
+            assert_bitexact(g, w, "reverse, variant %d" % v)
+    ct.sync()
+
+
 def test_autotuner_keeps_a_variant_and_results(gpu_lib):
     from casadi_gb300 import runtime as R
     F = W.cartpole_rollout(4)
