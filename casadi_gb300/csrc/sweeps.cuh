@@ -45,6 +45,7 @@ __host__ __device__ constexpr int group_slot(int g) { return g >= 8 ? 3 : g >= 4
 __host__ __device__ constexpr unsigned ent_key(unsigned w) { return w & 63u; }
 constexpr unsigned kPiP = 1u, kPiQ = 2u, kPiQNext = 4u;  // partial-info bits (w >> 6)
 constexpr unsigned kPiShift = 6, kPiIndexShift = 9;
+static_assert(kMaxPartials <= (1u << (32 - kPiIndexShift)), "partial indices fit the key word");
 
 // Tangent forms: the tangent of one arithmetic entry from operand tangents a (y) and b (z) and
 // the recorded partials p (d0) and q (d1).
