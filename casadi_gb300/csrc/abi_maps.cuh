@@ -5,8 +5,8 @@
 #pragma once
 
 // A MapSum call sums at most two row groups per output (values and their directions) in
-// forward mode and one per output and per shared input in reverse mode, all in one launch.
-static_assert(kMaxSumGroups >= 2 * kMaxIo, "MapSum row groups of one call must fit a launch");
+// forward mode and one per output and per shared input in reverse mode; the instance-order
+// reduction takes them in launches of up to kMaxSumGroups groups.
 
 // ---- MapSum: shared inputs and instance-summed outputs (casadi/core/mapsum.cpp) -------------
 namespace {

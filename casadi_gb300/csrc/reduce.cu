@@ -176,19 +176,23 @@ cudaError_t reduce_sum(long long rows, long long n, const double* src, long long
 
 cudaError_t reduce_sum_instance_multi(const SumRows* groups, int count, long long n,
                                       cudaStream_t s) {
-  if (count <= 0) return cudaSuccess;
-  if (count > kMaxSumGroups) return cudaErrorInvalidValue;
-  SumRowsArgs a;
-  long long total = 0;
-  for (int k = 0; k < count; ++k) {
-    a.g[k] = groups[k];
-    total += groups[k].rows;
+  // at most kMaxSumGroups groups per launch (the launch's parameter block holds them); more
+  // groups take more launches, each row's chain being the same
+  for (int k0 = 0; k0 < count; k0 += kMaxSumGroups) {
+    const int c = std::min(kMaxSumGroups, count - k0);
+    SumRowsArgs a;
+    long long total = 0;
+    for (int k = 0; k < c; ++k) {
+      a.g[k] = groups[k0 + k];
+      total += groups[k0 + k].rows;
+    }
+    a.count = c;
+    if (total == 0) continue;
+    const long long blocks = (total + 127) / 128;
+    k_sum_instance_multi<<<static_cast<unsigned>(blocks), 128, 0, s>>>(a, n);
+    if (cudaError_t e = cudaGetLastError()) return e;
   }
-  a.count = count;
-  if (total == 0) return cudaSuccess;
-  const long long blocks = (total + 127) / 128;
-  k_sum_instance_multi<<<static_cast<unsigned>(blocks), 128, 0, s>>>(a, n);
-  return cudaGetLastError();
+  return cudaSuccess;
 }
 
 cudaError_t reduce_or(long long rows, long long n, const unsigned long long* src, long long ld,

@@ -39,7 +39,7 @@ struct SumRows {
   double* dst;        // dst[r] = the sum of row r
   long long rows;
 };
-constexpr int kMaxSumGroups = 128;
+constexpr int kMaxSumGroups = 120;  // groups per launch: the parameter block stays under 4 KB
 cudaError_t reduce_sum_instance_multi(const SumRows* groups, int count, long long n,
                                       cudaStream_t s);
 
