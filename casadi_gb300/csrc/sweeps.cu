@@ -454,7 +454,10 @@ __device__ __forceinline__ void issue_partials(const uint4 (&E)[G], const double
   for (int i = 0; i < G; ++i) {
     const unsigned w = E[i].w;
     const double* pp = pt + static_cast<size_t>(w >> kPiIndexShift) * 32;
-    const double* pq = pp + ((w >> (kPiShift + 2 - 5)) & 32u);  // next partial row if kPiQNext
+    // Q's row: P's, or the next one (32 doubles on) when kPiQNext is set; the shift moves that
+    // bit (bit 8 of w) onto the value 32 (bit 5)
+    static_assert(kPiQNext << kPiShift == (32u << 3), "kPiQNext sits at bit 8 of the key word");
+    const double* pq = pp + ((w >> 3) & 32u);
 #pragma unroll
     for (int j = 0; j < IPT; ++j) {
       if ((w & (kPiP << kPiShift)) && tok[j]) P[i][j] = ld_partial<kNC>(pp + j * tstride);
