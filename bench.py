@@ -183,15 +183,38 @@ def structural_adjoint_ops(tape, seeded_out):
 SIMPLE_OPS = ("ADD", "SUB", "MUL", "SQ", "IF_ELSE_ZERO", "LT", "LE", "EQ", "NE", "FMIN", "FMAX")
 
 
+def sincos_reuse(tape):
+    """SIN/COS instructions whose sin/cos pair the record sweeps take again from the previous
+    SIN/COS of the same operand value (the library's rule, on the scheduled tape): op -> count."""
+    from casadi_gb300 import calculus as C
+    from casadi_gb300 import runtime as R
+    t = R.schedule(tape)
+    ver, cache, out = {}, None, {C.OP_SIN: 0, C.OP_COS: 0}
+    for k in range(t.n_instr):
+        o = int(t.op[k])
+        if o in (C.OP_SIN, C.OP_COS):
+            key = (int(t.i1[k]), ver.get(int(t.i1[k])))
+            if key == cache:
+                out[o] += 1
+            else:
+                cache = key
+        if o != C.OP_OUTPUT:
+            ver[int(t.i0[k])] = k
+    return out
+
+
 def algorithmic_flops(tape, weights, rates, seeded_out=None, unit_dirs=True, wanted_out=None):
     """Per instance and kernel family: FP64-pipe instructions ("instr") and their time at the
     measured rates expressed in DFMA-chain instructions ("dfma_time"); the family's ceiling
     is rate_dfma * instr / dfma_time. Value and record sweeps: simple ops (one DADD or DMUL
     each, weight 1) at the DADD/DMUL rate, libm calls at their measured DFMA equivalents
-    (op_weights.json); TWICE, the sign-bit ops and selections cost no FP64 instruction."""
+    (op_weights.json); TWICE, the sign-bit ops and selections cost no FP64 instruction. A record
+    of SIN or COS is one sincos (the value and the partial), none for the second of a pair
+    whose sincos the previous one computed (sincos_reuse)."""
     from casadi_gb300 import calculus as C
     slow = rates["dfma"] / min(rates["dadd"], rates["dmul"])
     out = {"eval": {"instr": 0.0, "dfma_time": 0.0}, "record": {"instr": 0.0, "dfma_time": 0.0}}
+    reuse = sincos_reuse(tape)
     for op, cnt in zip(*np.unique(tape.op, return_counts=True)):
         op = int(op)
         if op in (C.OP_CONST, C.OP_INPUT, C.OP_OUTPUT):
@@ -202,8 +225,9 @@ def algorithmic_flops(tape, weights, rates, seeded_out=None, unit_dirs=True, wan
         wp = float(weights.get(name + "_partial", 0.0))
         out["eval"]["instr"] += cnt * w
         out["eval"]["dfma_time"] += cnt * t
-        out["record"]["instr"] += cnt * (w + wp)
-        out["record"]["dfma_time"] += cnt * (t + wp)
+        rc = cnt - reuse.get(op, 0)
+        out["record"]["instr"] += rc * (w + wp)
+        out["record"]["dfma_time"] += rc * (t + wp)
     seeded_out = seeded_out or [True] * len(tape.nnz_out)
     for fam, mix in (("tangent", structural_tangent_ops(tape, unit_dirs, wanted_out=wanted_out)),
                      ("adjoint", structural_adjoint_ops(tape, seeded_out))):

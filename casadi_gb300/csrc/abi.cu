@@ -1750,6 +1750,33 @@ int encode_tape(const casadi_gb300_atomic* alg, int n_instr, int n_in, const int
   return 0;
 }
 
+// Sine/cosine pairs. The record sweeps compute sin and cos of the operand together for either
+// op (one is the value, the other its partial), so a SIN or COS whose operand is the value the
+// previous SIN/COS read -- no instruction rewrote that slot in between -- takes that result
+// again: bit 63 of its word, which every decoder ignores; orders that differ (level schedules,
+// segment tapes) are re-encoded without it. The 20-step rollout's 80 SIN/COS pairs each save
+// one sincos.
+void mark_sincos_pairs(std::vector<u64>& code) {
+  unsigned slots = 1;
+  for (u64 w : code) slots = std::max(slots, std::max(dec_a(w), std::max(dec_b(w), dec_c(w))) + 1);
+  std::vector<long long> ver(slots, -1);  // slot -> instruction that last wrote it
+  long long cache_slot = -1, cache_ver = -1;
+  for (size_t k = 0; k < code.size(); ++k) {
+    const u64 w = code[k];
+    const unsigned op = dec_op(w);
+    if (op == D_SIN || op == D_COS) {
+      const unsigned b = dec_b(w);
+      if (static_cast<long long>(b) == cache_slot && ver[b] == cache_ver) {
+        code[k] = w | kSincosReuse;
+      } else {
+        cache_slot = b;
+        cache_ver = ver[b];
+      }
+    }
+    if (op != D_OUTPUT && op != D_NOP) ver[dec_a(w)] = static_cast<long long>(k);
+  }
+}
+
 // Encoded tape in the scheduled order; returns the scheduled work-vector length or a status.
 int encode_and_schedule(const casadi_gb300_atomic* alg, int n_instr, int n_in,
                         const int* nnz_in, int n_out, const int* nnz_out, int sz_w,
@@ -1761,6 +1788,7 @@ int encode_and_schedule(const casadi_gb300_atomic* alg, int n_instr, int n_in,
   const int w = schedule_code(e.code, sched, err);
   if (w < 0) return fail(CASADI_GB300_ERR_ARG, "%s", err.c_str());
   e.code.swap(sched);
+  mark_sincos_pairs(e.code);
   return w;
 }
 

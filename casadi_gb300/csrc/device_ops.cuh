@@ -45,6 +45,9 @@ __host__ __device__ __forceinline__ unsigned dec_b(u64 w) { return (unsigned)(w 
 __host__ __device__ __forceinline__ unsigned dec_c(u64 w) { return (unsigned)(w >> 42) & kFieldMax; }
 __host__ __device__ __forceinline__ unsigned dec_pmask(u64 w) { return (unsigned)(w >> 60) & 3u; }
 __host__ __device__ __forceinline__ bool dec_binary(u64 w) { return (w >> 62) & 1u; }
+// Bit 63: a SIN or COS whose sin/cos pair the previous SIN/COS of the same operand value
+// computed (the record sweeps take it again; see mark_sincos_pairs).
+constexpr u64 kSincosReuse = 1ull << 63;
 
 // Partials an instruction records for the AD sweeps: bit 0 = d0, bit 1 = d1.
 // Ops whose partials are constants (ADD, SUB, NEG, TWICE, ASSIGN, comparisons, ...) record
@@ -357,6 +360,19 @@ __device__ __forceinline__ double dev_fun_der(unsigned op, double x, double y, d
     default:
       return dev_fun(op, x, y);
   }
+}
+
+// dev_fun_der with the record sweeps' sin/cos pair (s, c): a SIN or COS computes the pair and
+// keeps it, or, marked kSincosReuse, takes the kept pair of the same operand value; the bits
+// are dev_fun_der's either way.
+__device__ __forceinline__ double dev_fun_der_pair(unsigned op, double x, double y, double& d0,
+                                                   double& d1, u64 ins, double& s, double& c) {
+  if (op == D_SIN || op == D_COS) {
+    if (!(ins & kSincosReuse)) sincos(x, &s, &c);
+    d0 = op == D_SIN ? c : d_neg(s);
+    return op == D_SIN ? s : c;
+  }
+  return dev_fun_der(op, x, y, d0, d1);
 }
 #endif  // __CUDACC__
 

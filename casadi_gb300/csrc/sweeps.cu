@@ -171,6 +171,7 @@ __global__ void __launch_bounds__(BS) k_primal(const __grid_constant__ SweepArgs
     const bool active = il < a.n;
     const long long ig = a.i_begin + il;
     long long pidx = 0;
+    double sc_s = 0.0, sc_c = 0.0;  // the last sin/cos pair (record sweeps)
     const bool ok = sweep_forward(a.t, ring, bars, seq, [&](u64 ins) {
       const unsigned op = dec_op(ins), A = dec_a(ins), B = dec_b(ins), C = dec_c(ins);
       switch (op) {
@@ -194,7 +195,7 @@ __global__ void __launch_bounds__(BS) k_primal(const __grid_constant__ SweepArgs
           if (RECORD) {
             const unsigned m = partial_mask(op);
             double d0 = 0.0, d1 = 0.0;
-            const double f = dev_fun_der(op, x, y, d0, d1);
+            const double f = dev_fun_der_pair(op, x, y, d0, d1, ins, sc_s, sc_c);
             if (m & 1u) {
               if (active) a.partials[((il >> 5) * a.t.n_partials + pidx) * 32 + (il & 31)] = d0;
               ++pidx;

@@ -22,6 +22,7 @@ __device__ __forceinline__ void primal_walk(const TapeView& t, int n_code, doubl
                                             const IoDesc* out, bool active, long long ig) {
   const u64* code = t.code;
   int pidx = 0;
+  double sc_s = 0.0, sc_c = 0.0;  // the last sin/cos pair (RECORD)
   u64 nxt = __ldg(code);
 #pragma unroll 1
   for (int k = 0; k < n_code; ++k) {
@@ -49,7 +50,7 @@ __device__ __forceinline__ void primal_walk(const TapeView& t, int n_code, doubl
         if (RECORD) {
           const unsigned m = dec_pmask(ins);
           double d0 = 0.0, d1 = 0.0;
-          const double f = dev_fun_der(op, x, y, d0, d1);
+          const double f = dev_fun_der_pair(op, x, y, d0, d1, ins, sc_s, sc_c);
           if (m & 1u) pt[32 * pidx++] = d0;
           if (m & 2u) pt[32 * pidx++] = d1;
           wreg(wb, A * 256u) = f;

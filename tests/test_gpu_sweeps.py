@@ -601,6 +601,40 @@ def test_every_op_tape_every_variant(gpu_lib):
     ct.sync()
 
 
+def test_sin_cos_pairs_share_one_sincos(gpu_lib):
+    """The record sweeps compute a SIN/COS pair of one operand value once (the second takes the
+    first's sincos): adjacent pairs, pairs broken by another SIN/COS in between, repeats and
+    large arguments give the value sweep's bits, and derivatives agree with the oracle."""
+    import bench
+    x, y = S.sym("x"), S.sym("y")
+    u = x * y
+    outs = [S.sin(x), S.cos(x), S.sin(y), S.cos(x) + S.sin(x), S.sin(u), S.cos(y), S.cos(u),
+            S.sin(u) * S.cos(u), S.sin(x + 1.0), S.cos(y * 2.0), S.sin(y * 2.0)]
+    f = S.Function("P", [[x, y]], [outs])
+    t = f.tape
+    assert sum(bench.sincos_reuse(t).values()) > 0
+    n = 997
+    rng = np.random.default_rng(12)
+    args = [np.vstack([rng.uniform(-4, 4, n), 10.0 ** rng.uniform(-3, 6, n)])]
+    aseeds = [rng.standard_normal((2, len(outs), n))]
+    ct = CudaTape(t)
+    vals = host(ct.eval(dev(args)))
+    res_r, asens = ct.reverse(dev(args), dev(aseeds))
+    res_j, jac = ct.jacobian(dev(args))
+    for a, b, c in zip(vals, host(res_r), host(res_j)):
+        assert_bitexact(a, b, "eval vs record values")
+        assert_bitexact(a, c, "eval vs jacobian record values")
+    _, wa = O.reverse(t, args, aseeds, n, NTHREADS)
+    _, ma = magnitudes(O.reverse, t, args, aseeds, n, NTHREADS)
+    for g, w, m in zip(host(asens), wa, ma):
+        assert_close(g, w, "adjoint", bound=RTOL * m)
+    _, wj = O.jacobian(t, args, n, NTHREADS)
+    _, mj = magnitudes(O.jacobian, t, args, n, NTHREADS)
+    for g, w, m in zip(host(jac), wj, mj):
+        assert_close(g, w, "jacobian", bound=RTOL * m)
+    ct.sync()
+
+
 def test_autotuner_keeps_a_variant_and_results(gpu_lib):
     from casadi_gb300 import runtime as R
     F = W.cartpole_rollout(4)
