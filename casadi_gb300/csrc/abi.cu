@@ -1277,7 +1277,8 @@ int primal_launch(Tape& t, SweepArgs& a, long long m, PrimalKind kind, cudaStrea
     } else if (global) {
       a.block = kGwBlock;
       const int occ =
-          std::max(1, kind >= PK_SP_FORWARD ? occupancy_gw_sp() : occupancy_gw_primal());
+          std::max(1, kind >= PK_SP_FORWARD ? occupancy_gw_sp()
+                                            : occupancy_gw_primal(kind == PK_RECORD));
       grid = grid_for((m + kGwBlock - 1) / kGwBlock, occ * sm_count());
       const size_t elem = 8;  // a double or a bvec_t per slot and instance
       if (int rc = gw_prepare(t, a, &grid,

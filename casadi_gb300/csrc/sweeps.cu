@@ -154,6 +154,15 @@ __device__ __forceinline__ long long io_off(const IoDesc& d, long long dir, long
 // GW: the work vector lives in global memory (a per-CTA block of a.wglob, L1/L2-cached)
 // instead of shared memory, for tapes whose work vector does not fit or is worth trading for
 // residency.
+// The record sweeps' last sin/cos pair (dev_fun_der_pair); the value sweep keeps none, so its
+// code is that of a sweep without the pair.
+template <bool RECORD>
+struct PairState {
+  double s = 0.0, c = 0.0;
+};
+template <>
+struct PairState<false> {};
+
 template <int BS, bool RECORD, bool GW = false>
 __global__ void __launch_bounds__(BS) k_primal(const __grid_constant__ SweepArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
@@ -171,7 +180,7 @@ __global__ void __launch_bounds__(BS) k_primal(const __grid_constant__ SweepArgs
     const bool active = il < a.n;
     const long long ig = a.i_begin + il;
     long long pidx = 0;
-    double sc_s = 0.0, sc_c = 0.0;  // the last sin/cos pair (record sweeps)
+    PairState<RECORD> pair;
     const bool ok = sweep_forward(a.t, ring, bars, seq, [&](u64 ins) {
       const unsigned op = dec_op(ins), A = dec_a(ins), B = dec_b(ins), C = dec_c(ins);
       switch (op) {
@@ -192,10 +201,10 @@ __global__ void __launch_bounds__(BS) k_primal(const __grid_constant__ SweepArgs
         } break;
         default: {
           const double x = w[B * BS + tid], y = w[C * BS + tid];
-          if (RECORD) {
+          if constexpr (RECORD) {
             const unsigned m = partial_mask(op);
             double d0 = 0.0, d1 = 0.0;
-            const double f = dev_fun_der_pair(op, x, y, d0, d1, ins, sc_s, sc_c);
+            const double f = dev_fun_der_pair(op, x, y, d0, d1, ins, pair.s, pair.c);
             if (m & 1u) {
               if (active) a.partials[((il >> 5) * a.t.n_partials + pidx) * 32 + (il & 31)] = d0;
               ++pidx;
@@ -1079,7 +1088,10 @@ cudaError_t launch_sp_reverse(const SweepArgs& a, int grid, cudaStream_t s) {
   CGB_DISPATCH_BS(k_sp_reverse)
 }
 
-int occupancy_gw_primal() { return occ_of_k(k_primal<kGwBlock, true, true>, kGwBlock, kHeaderBytes); }
+int occupancy_gw_primal(bool record) {
+  return record ? occ_of_k(k_primal<kGwBlock, true, true>, kGwBlock, kHeaderBytes)
+                : occ_of_k(k_primal<kGwBlock, false, true>, kGwBlock, kHeaderBytes);
+}
 int occupancy_gw_sp() { return occ_of_k(k_sp_reverse<kGwBlock, true>, kGwBlock, kHeaderBytes); }
 
 // Derivative-sweep variants: G entries per software-pipeline group, MB minimum CTAs per SM

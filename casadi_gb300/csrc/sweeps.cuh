@@ -241,7 +241,7 @@ struct BatchArgs {
 };
 
 constexpr int kGwBlock = 128;   // threads per CTA of the global-work-vector value sweeps
-int occupancy_gw_primal();       // CTAs per SM of the global-work-vector value/record sweep
+int occupancy_gw_primal(bool record);  // CTAs per SM of the global-work-vector value/record sweep
 int occupancy_gw_sp();           // ... of the sparsity sweeps
 int occupancy_gw_dir(bool adjoint);  // ... of the derivative sweeps (one warp per CTA)
 cudaError_t launch_gather(long long n, long long ld, int count, const long long* src_row,

@@ -22,7 +22,7 @@ __device__ __forceinline__ void primal_walk(const TapeView& t, int n_code, doubl
                                             const IoDesc* out, bool active, long long ig) {
   const u64* code = t.code;
   int pidx = 0;
-  double sc_s = 0.0, sc_c = 0.0;  // the last sin/cos pair (RECORD)
+  PairState<RECORD> pair;  // the last sin/cos pair (record walks)
   u64 nxt = __ldg(code);
 #pragma unroll 1
   for (int k = 0; k < n_code; ++k) {
@@ -47,10 +47,10 @@ __device__ __forceinline__ void primal_walk(const TapeView& t, int n_code, doubl
       } break;
       default: {
         const double x = wreg(wb, B * 256u), y = wreg(wb, C * 256u);
-        if (RECORD) {
+        if constexpr (RECORD) {
           const unsigned m = dec_pmask(ins);
           double d0 = 0.0, d1 = 0.0;
-          const double f = dev_fun_der_pair(op, x, y, d0, d1, ins, sc_s, sc_c);
+          const double f = dev_fun_der_pair(op, x, y, d0, d1, ins, pair.s, pair.c);
           if (m & 1u) pt[32 * pidx++] = d0;
           if (m & 2u) pt[32 * pidx++] = d1;
           wreg(wb, A * 256u) = f;
