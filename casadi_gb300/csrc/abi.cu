@@ -1754,14 +1754,15 @@ int encode_tape(const casadi_gb300_atomic* alg, int n_instr, int n_in, const int
 // Sine/cosine pairs. The record sweeps compute sin and cos of the operand together for either
 // op (one is the value, the other its partial), so a SIN or COS whose operand is the value the
 // previous SIN/COS read -- no instruction rewrote that slot in between -- takes that result
-// again: bit 63 of its word, which every decoder ignores; orders that differ (level schedules,
-// segment tapes) are re-encoded without it. The 20-step rollout's 80 SIN/COS pairs each save
-// one sincos.
+// again: bit 63 of its word, which every decoder ignores; the first of such a pair gets bit 62
+// (clear on unary ops otherwise), so the value sweeps compute it as one sincos where they would
+// call sin and cos. Orders that differ (level schedules, segment tapes) are re-encoded without
+// either bit. The 20-step rollout's 80 SIN/COS pairs each save one sincos.
 void mark_sincos_pairs(std::vector<u64>& code) {
   unsigned slots = 1;
   for (u64 w : code) slots = std::max(slots, std::max(dec_a(w), std::max(dec_b(w), dec_c(w))) + 1);
   std::vector<long long> ver(slots, -1);  // slot -> instruction that last wrote it
-  long long cache_slot = -1, cache_ver = -1;
+  long long cache_slot = -1, cache_ver = -1, cache_at = -1;
   for (size_t k = 0; k < code.size(); ++k) {
     const u64 w = code[k];
     const unsigned op = dec_op(w);
@@ -1769,9 +1770,11 @@ void mark_sincos_pairs(std::vector<u64>& code) {
       const unsigned b = dec_b(w);
       if (static_cast<long long>(b) == cache_slot && ver[b] == cache_ver) {
         code[k] = w | kSincosReuse;
+        code[cache_at] |= kSincosFirst;  // the value sweeps compute the pair there
       } else {
         cache_slot = b;
         cache_ver = ver[b];
+        cache_at = static_cast<long long>(k);
       }
     }
     if (op != D_OUTPUT && op != D_NOP) ver[dec_a(w)] = static_cast<long long>(k);

@@ -46,8 +46,11 @@ __host__ __device__ __forceinline__ unsigned dec_c(u64 w) { return (unsigned)(w 
 __host__ __device__ __forceinline__ unsigned dec_pmask(u64 w) { return (unsigned)(w >> 60) & 3u; }
 __host__ __device__ __forceinline__ bool dec_binary(u64 w) { return (w >> 62) & 1u; }
 // Bit 63: a SIN or COS whose sin/cos pair the previous SIN/COS of the same operand value
-// computed (the record sweeps take it again; see mark_sincos_pairs).
+// computed (the sweeps take it again); bit 62 on a SIN or COS (unary ops leave it clear): the
+// first of such a pair, which the value sweeps then compute as one sincos (see
+// mark_sincos_pairs).
 constexpr u64 kSincosReuse = 1ull << 63;
+constexpr u64 kSincosFirst = 1ull << 62;
 
 // Partials an instruction records for the AD sweeps: bit 0 = d0, bit 1 = d1.
 // Ops whose partials are constants (ADD, SUB, NEG, TWICE, ASSIGN, comparisons, ...) record
@@ -373,6 +376,18 @@ __device__ __forceinline__ double dev_fun_der_pair(unsigned op, double x, double
     return op == D_SIN ? s : c;
   }
   return dev_fun_der(op, x, y, d0, d1);
+}
+
+// dev_fun with the value sweeps' sin/cos pair: the first of a marked pair computes both as one
+// sincos and keeps them, the second takes the kept one; unpaired SIN/COS call sin or cos. Same
+// bits as dev_fun (sincos gives sin's and cos's results).
+__device__ __forceinline__ double dev_fun_pair(unsigned op, double x, double y, u64 ins,
+                                               double& s, double& c) {
+  if ((op == D_SIN || op == D_COS) && (ins & (kSincosReuse | kSincosFirst))) {
+    if (!(ins & kSincosReuse)) sincos(x, &s, &c);
+    return op == D_SIN ? s : c;
+  }
+  return dev_fun(op, x, y);
 }
 #endif  // __CUDACC__
 

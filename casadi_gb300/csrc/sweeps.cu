@@ -154,14 +154,10 @@ __device__ __forceinline__ long long io_off(const IoDesc& d, long long dir, long
 // GW: the work vector lives in global memory (a per-CTA block of a.wglob, L1/L2-cached)
 // instead of shared memory, for tapes whose work vector does not fit or is worth trading for
 // residency.
-// The record sweeps' last sin/cos pair (dev_fun_der_pair); the value sweep keeps none, so its
-// code is that of a sweep without the pair.
-template <bool RECORD>
+// The last sin/cos pair of a value or record sweep (dev_fun_pair, dev_fun_der_pair).
 struct PairState {
   double s = 0.0, c = 0.0;
 };
-template <>
-struct PairState<false> {};
 
 template <int BS, bool RECORD, bool GW = false>
 __global__ void __launch_bounds__(BS) k_primal(const __grid_constant__ SweepArgs a) {
@@ -180,7 +176,7 @@ __global__ void __launch_bounds__(BS) k_primal(const __grid_constant__ SweepArgs
     const bool active = il < a.n;
     const long long ig = a.i_begin + il;
     long long pidx = 0;
-    PairState<RECORD> pair;
+    PairState pair;
     const bool ok = sweep_forward(a.t, ring, bars, seq, [&](u64 ins) {
       const unsigned op = dec_op(ins), A = dec_a(ins), B = dec_b(ins), C = dec_c(ins);
       switch (op) {
@@ -215,7 +211,7 @@ __global__ void __launch_bounds__(BS) k_primal(const __grid_constant__ SweepArgs
             }
             w[A * BS + tid] = f;
           } else {
-            w[A * BS + tid] = dev_fun(op, x, y);
+            w[A * BS + tid] = dev_fun_pair(op, x, y, ins, pair.s, pair.c);
           }
         }
       }
@@ -886,7 +882,7 @@ __global__ void __launch_bounds__(BS) k_sp_forward(const __grid_constant__ Sweep
         } break;
         default:
           if (ACT)
-            w[A * BS + tid] = activity_of(op, dec_binary(ins), w[B * BS + tid], w[C * BS + tid]);
+            w[A * BS + tid] = activity_of(op, is_binary(op), w[B * BS + tid], w[C * BS + tid]);
           else
             w[A * BS + tid] = w[B * BS + tid] | w[C * BS + tid];
       }

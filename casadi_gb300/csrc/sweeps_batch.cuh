@@ -22,7 +22,7 @@ __device__ __forceinline__ void primal_walk(const TapeView& t, int n_code, doubl
                                             const IoDesc* out, bool active, long long ig) {
   const u64* code = t.code;
   int pidx = 0;
-  PairState<RECORD> pair;  // the last sin/cos pair (record walks)
+  PairState pair;  // the last sin/cos pair
   u64 nxt = __ldg(code);
 #pragma unroll 1
   for (int k = 0; k < n_code; ++k) {
@@ -55,7 +55,7 @@ __device__ __forceinline__ void primal_walk(const TapeView& t, int n_code, doubl
           if (m & 2u) pt[32 * pidx++] = d1;
           wreg(wb, A * 256u) = f;
         } else {
-          wreg(wb, A * 256u) = dev_fun(op, x, y);
+          wreg(wb, A * 256u) = dev_fun_pair(op, x, y, ins, pair.s, pair.c);
         }
       }
     }
