@@ -183,24 +183,35 @@ def structural_adjoint_ops(tape, seeded_out):
 SIMPLE_OPS = ("ADD", "SUB", "MUL", "SQ", "IF_ELSE_ZERO", "LT", "LE", "EQ", "NE", "FMIN", "FMAX")
 
 
-def sincos_reuse(tape):
-    """SIN/COS instructions whose sin/cos pair the record sweeps take again from the previous
-    SIN/COS of the same operand value (the library's rule, on the scheduled tape): op -> count."""
+def sincos_pairs(tape):
+    """SIN/COS pairs of one operand value (the library's rule, on the scheduled tape): per op,
+    the instructions that take the previous SIN/COS's sin/cos again ("reuse") and those whose
+    sincos a later one takes ("first")."""
     from casadi_gb300 import calculus as C
     from casadi_gb300 import runtime as R
     t = R.schedule(tape)
-    ver, cache, out = {}, None, {C.OP_SIN: 0, C.OP_COS: 0}
+    ver, cache, owner = {}, None, None
+    reuse, first = {C.OP_SIN: 0, C.OP_COS: 0}, set()
     for k in range(t.n_instr):
         o = int(t.op[k])
         if o in (C.OP_SIN, C.OP_COS):
             key = (int(t.i1[k]), ver.get(int(t.i1[k])))
             if key == cache:
-                out[o] += 1
+                reuse[o] += 1
+                first.add(owner)
             else:
-                cache = key
+                cache, owner = key, k
         if o != C.OP_OUTPUT:
             ver[int(t.i0[k])] = k
-    return out
+    firsts = {C.OP_SIN: 0, C.OP_COS: 0}
+    for k in first:
+        firsts[int(t.op[k])] += 1
+    return {"reuse": reuse, "first": firsts}
+
+
+def sincos_reuse(tape):
+    """SIN/COS instructions that take the previous SIN/COS's sin/cos pair: op -> count."""
+    return sincos_pairs(tape)["reuse"]
 
 
 def algorithmic_flops(tape, weights, rates, seeded_out=None, unit_dirs=True, wanted_out=None):
@@ -208,13 +219,15 @@ def algorithmic_flops(tape, weights, rates, seeded_out=None, unit_dirs=True, wan
     measured rates expressed in DFMA-chain instructions ("dfma_time"); the family's ceiling
     is rate_dfma * instr / dfma_time. Value and record sweeps: simple ops (one DADD or DMUL
     each, weight 1) at the DADD/DMUL rate, libm calls at their measured DFMA equivalents
-    (op_weights.json); TWICE, the sign-bit ops and selections cost no FP64 instruction. A record
-    of SIN or COS is one sincos (the value and the partial), none for the second of a pair
-    whose sincos the previous one computed (sincos_reuse)."""
+    (op_weights.json); TWICE, the sign-bit ops and selections cost no FP64 instruction. A SIN or
+    COS that takes the previous one's sin/cos pair costs none; a record of SIN or COS is one
+    sincos (the value and the partial), and so is the value of the first of a pair
+    (sincos_pairs)."""
     from casadi_gb300 import calculus as C
     slow = rates["dfma"] / min(rates["dadd"], rates["dmul"])
     out = {"eval": {"instr": 0.0, "dfma_time": 0.0}, "record": {"instr": 0.0, "dfma_time": 0.0}}
-    reuse = sincos_reuse(tape)
+    pairs = sincos_pairs(tape)
+    reuse, first = pairs["reuse"], pairs["first"]
     for op, cnt in zip(*np.unique(tape.op, return_counts=True)):
         op = int(op)
         if op in (C.OP_CONST, C.OP_INPUT, C.OP_OUTPUT):
@@ -223,8 +236,9 @@ def algorithmic_flops(tape, weights, rates, seeded_out=None, unit_dirs=True, wan
         w = 0.0 if name == "TWICE" else float(weights.get(name, 1.0))
         t = w * (slow if name in SIMPLE_OPS else 1.0)
         wp = float(weights.get(name + "_partial", 0.0))
-        out["eval"]["instr"] += cnt * w
-        out["eval"]["dfma_time"] += cnt * t
+        ec, fc = cnt - reuse.get(op, 0) - first.get(op, 0), first.get(op, 0)
+        out["eval"]["instr"] += ec * w + fc * (w + wp)
+        out["eval"]["dfma_time"] += ec * t + fc * (t + wp)
         rc = cnt - reuse.get(op, 0)
         out["record"]["instr"] += rc * (w + wp)
         out["record"]["dfma_time"] += rc * (t + wp)
